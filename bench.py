@@ -1,0 +1,339 @@
+"""Benchmark of the GB300 PDDSparse hot path (one JSON line on rank 0).
+
+A step is one pass of the hot path over one batch of synthetic input: the
+Feynman-Kac estimation of every knot's G row and B entry followed by the
+interface solve (I + G) u = B, on the 12x12-subdomain / 43-knot Poisson
+workload (10,989 knots, 2e4 paths per knot, h = 5e-4) in the MIXED form
+(FP32 paths, FP64 accumulation, FP64 RBF factorisation, FP32 GMRES under
+FP64 refinement).
+
+  value  path-steps/s of the device-timed step (inputs resident in HBM),
+         CUDA events on the library's stream, L2 flushed between steps
+  e2e    the same metric through the public API call a user makes: layout
+         upload from host, estimation, solve, and G/B/u copied back to host
+  roofline  FP32 issue-slot roof of the path kernel (the path is issue-bound:
+         it reads a few MB of stencil tables and no large arrays)
+  cpu_baseline  the CPU restatement of the reference (OpenMP paths, serial
+         O(n_s^2) reduction), on a bounded sample of knots of the same workload
+
+--impl reference runs the reference's CPU algorithm (the restatement, all host
+threads) on the same workload and prints the same metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "path-steps/s & interface solves/s at RMSE<=2e-3, mixed+batched vs plain FP64"
+
+# Algorithmic thread-instruction counts (fixed before tuning, counted from the
+# algorithm, not from the compiler): one Euler-Maruyama step = half a
+# Philox-4x32-10 call (10 rounds of 2 wide multiplies and 2 three-way XORs,
+# 40 INT) + Box-Muller (2 converts, log, sqrt, sin, cos, 4 FP32: 10) +
+# Poisson coefficients (sin/cos of pi x and pi y, source, gradient: 14) +
+# control-variate update and state update (14) + rectangle distance and
+# projection (12) + Gobet-shifted exit test (4) = 94.  One exit = side
+# classification and projection (10) + cubic weights and 4 shared-memory
+# deposits (16) + B accumulation in FP64 (6) + refill (10) = 42.  The G
+# contraction adds one FMA per (bin, side knot) pair per knot.
+W_STEP = 94
+W_EXIT = 42
+
+
+def _env_rank():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), \
+        int(os.environ.get("LOCAL_RANK", "0"))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS, "--format=csv,noheader",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [q.strip() for q in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1].split()[0]))
+                smax.append(float(p[2].split()[0]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(smax)) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def cpu_baseline(workload: dict, fac, n_knots: int, seed: int = 1234, npaths=None):
+    """The reference's CPU path restated (oracle): OpenMP over paths with every
+    host core, serial O(n_s^2) reduction, libm, per-knot factorisation; on a
+    fixed random sample of knots of the workload (seed 1234)."""
+    import oracle as O
+    L = O.Layout(workload["sw"], workload["ne"], workload["nsub"], workload["nnode"])
+    rng = np.random.default_rng(seed)
+    # sample among knots that run paths
+    cx = 0.5 * (workload["sw"][0] + workload["ne"][0])
+    cy = 0.5 * (workload["sw"][1] + workload["ne"][1])
+    hx, hy = workload["ne"][0] - cx, workload["ne"][1] - cy
+    inner = [i for i in range(len(L.work_idx))
+             if abs(max(abs(L.work_x[i] - cx) - hx, abs(L.work_y[i] - cy) - hy)) > 1e-8]
+    sel = sorted(rng.choice(inner, size=min(n_knots, len(inner)), replace=False).tolist())
+    N = npaths or workload["npaths"]
+    threads = os.cpu_count() or 1
+    prm = O.make_params(N, workload["h"], seed=seed, fac=fac, sublinear=True, threads=threads)
+    prob = O.make_problem(O.POISSON_SINCOS)
+    t0 = time.perf_counter()
+    res = L.run(prob, prm, knots=sel)
+    dt = time.perf_counter() - t0
+    steps = int(res["stats"][0])
+    return {"value": steps / dt, "unit": "path-steps/s", "cores": threads, "kind": "port",
+            "sample": f"{len(sel)} random knots (seed {seed}) of {workload['name']}, {N} paths each, "
+                      f"{steps} path steps in {dt:.2f} s",
+            "seconds": dt, "knots": len(sel), "path_steps": steps}
+
+
+def run_reference(args, workload, fac):
+    rank, world, _ = _env_rank()
+    if rank != 0:
+        return
+    per_step = []
+    steps_total = 0
+    base = None
+    for s in range(args.warmup + args.steps):
+        r = cpu_baseline(workload, fac, args.ref_knots, seed=1234 + s)
+        if s >= args.warmup:
+            per_step.append(r["seconds"])
+            steps_total += r["path_steps"]
+            base = r
+    value = steps_total / sum(per_step)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "path-steps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * float(np.mean(per_step)),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": workload["name"], "knots_per_step": base["knots"],
+                                            "paths_per_knot": workload["npaths"], "h": workload["h"]},
+            "cpu_baseline": {"value": value, "unit": "path-steps/s", "cores": base["cores"], "kind": "port",
+                             "sample": base["sample"]},
+            "e2e": {"value": value, "unit": "path-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def contraction_fma(pd) -> int:
+    """FMAs of the G contraction per knot summed over knots (sum over sides of n * nbins)."""
+    return int(pd.layout_info.get("_contraction_fma", 0))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="poisson_12x12_n43")
+    ap.add_argument("--npaths", type=int, default=0)
+    ap.add_argument("--ref-knots", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+
+    from pdds_gb300.config import WORKLOADS, fac_rule
+    workload = dict(WORKLOADS[args.workload])
+    workload["name"] = args.workload
+    if args.npaths:
+        workload["npaths"] = args.npaths
+    side = workload["ne"][0] - workload["sw"][0]
+    fac = fac_rule(side, workload["nsub"], workload["nnode"])
+
+    if args.impl == "reference":
+        run_reference(args, workload, fac)
+        return
+
+    rank, world, local = _env_rank()
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as td
+        td.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        dist = td
+    import torch
+    torch.cuda.set_device(local)
+    import pdds_gb300 as P
+
+    bvp = P.BVP.poisson_sincos()
+    N, h = workload["npaths"], workload["h"]
+    pd = P.PDDSparseGM(workload["sw"], workload["ne"], workload["nsub"], workload["nnode"], fac, device=local)
+    exact = bvp.u(pd.x, pd.y)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def step(instance):
+        est = pd.estimate(bvp, N, h, mode=P.MODE_MIXED, seed=1234, instance=instance)
+        u, sinfo = pd.solve_interface(P.SOLVE_GMRES_FP32_IR, tol=1e-10)
+        return est, u, sinfo
+
+    for w in range(args.warmup):
+        step(1000 + w)
+        flush.fill_(float(w))
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms_dev, steps_done, exits, launches, ms_paths, rmses, solve_ms = [], 0, 0, 0, [], [], []
+    t_wall0 = time.perf_counter()
+    for s in range(args.steps):
+        est, u, sinfo = step(rank * 100000 + s)
+        ms_dev.append(est.info["ms_setup"] + est.info["ms_paths"] + sinfo["ms"])
+        ms_paths.append(est.info["ms_paths"])
+        solve_ms.append(sinfo["ms"])
+        steps_done += est.info["path_steps"]
+        exits += est.info["exits_global"] + est.info["exits_stencil"]
+        launches += est.info["kernel_launches"] + sinfo["kernel_launches"]
+        rmses.append(float(np.sqrt(np.mean((u - exact) ** 2))))
+        flush.fill_(float(s))
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t_wall0
+    clk = clocks.stop()
+    t_dev = sum(ms_dev) / 1000.0
+    if dist:
+        tt = torch.tensor([t_dev], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_dev = float(tt.item())
+        st = torch.tensor([float(steps_done)], device="cuda")
+        dist.all_reduce(st)
+        steps_all = float(st.item())
+    else:
+        steps_all = float(steps_done)
+    value = steps_all / t_dev
+
+    extra = {}
+    # plain FP64 GPU form on the same workload (the >= 3x comparison)
+    if not args.no_fp64 and rank == 0:
+        est64 = pd.estimate(bvp, N, h, mode=P.MODE_FP64, seed=1234, instance=7)
+        u64, s64 = pd.solve_interface(P.SOLVE_BICGSTAB_FP64, tol=1e-10)
+        t64 = (est64.info["ms_setup"] + est64.info["ms_paths"] + s64["ms"]) / 1000.0
+        estm = pd.estimate(bvp, N, h, mode=P.MODE_MIXED, seed=1234, instance=7)
+        um, sm = pd.solve_interface(P.SOLVE_GMRES_FP32_IR, tol=1e-10)
+        extra["fp64"] = {
+            "path_steps_per_s": est64.info["path_steps"] / t64,
+            "ms_per_step": 1000 * t64,
+            "rmse_vs_analytic": float(np.sqrt(np.mean((u64 - exact) ** 2))),
+            "mixed_over_fp64": value / (est64.info["path_steps"] / t64),
+            "mixed_err_vs_fp64": {
+                "G_max_abs": float(np.max(np.abs(estm.val - est64.val))),
+                "B_max_abs": float(np.max(np.abs(estm.B - est64.B))),
+                "u_max_abs": float(np.max(np.abs(um - u64))),
+            },
+        }
+
+    # end to end through the public API: layout upload, estimation, solve,
+    # and G, B, u back on the host, every step
+    e2e = None
+    if not args.no_e2e:
+        h2d = d2h = 0
+        t0 = time.perf_counter()
+        e2e_steps = 0
+        for s in range(max(1, min(args.steps, 3))):
+            with P.PDDSparseGM(workload["sw"], workload["ne"], workload["nsub"], workload["nnode"], fac,
+                               device=local) as q:
+                u2, est2, si2 = q.Solve(bvp, N, h, mode=P.MODE_MIXED, seed=1234, instance=50 + s)
+                e2e_steps += est2.info["path_steps"]
+                K, nnz = q.K, q.nnz
+        dt = time.perf_counter() - t0
+        ns = max(1, min(args.steps, 3))
+        # layout arrays uploaded (knots, stencils, sides, shapes, CSR) and results read back
+        h2d = K * (8 + 8 + 4 + 8) + nnz * 4 + 4096
+        d2h = nnz * 16 + K * 24
+        e2e = {"value": e2e_steps / dt, "unit": "path-steps/s", "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "ms_per_step": 1000 * dt / ns}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        try:
+            cpu = cpu_baseline(workload, fac, args.ref_knots)
+        except Exception as exc:  # report, do not fail the bench
+            cpu = {"value": None, "unit": "path-steps/s", "cores": os.cpu_count(), "kind": "port",
+                   "sample": f"failed: {exc}"}
+
+    # issue-slot roofline of the path kernel
+    sm_count = torch.cuda.get_device_properties(local).multi_processor_count
+    f_mhz = clk.get("sm_mhz") or 1920.0
+    peak = sm_count * 4 * 32 * f_mhz * 1e6  # thread-instructions per second
+    t_paths = sum(ms_paths) / 1000.0
+    contr = pd.layout_info.get("nnz", 0)  # placeholder replaced below
+    work = steps_done * W_STEP + exits * W_EXIT
+    achieved = work / t_paths if t_paths > 0 else 0.0
+    roof = {"bound": "issue", "achieved": achieved / 1e9, "peak": peak / 1e9, "unit": "Ginst/s",
+            "frac": achieved / peak, "traffic": None,
+            "peak_source": f"{sm_count} SMs x 128 issue lanes x median SM clock {f_mhz:.0f} MHz under load",
+            "kernel": "k_paths_mixed", "kernel_ms_per_launch": 1000 * t_paths / args.steps}
+    del contr
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "path-steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000 * t_dev / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
+        "config": {"workload": workload["name"], "knots": pd.K, "paths_per_knot": N, "h": h,
+                   "mode": "MIXED", "solver": "GMRES(30) FP32 + FP64 refinement", "l2": "flushed (256 MB write)"},
+        "interface_solves_per_s": args.steps / t_dev,
+        "rmse_vs_analytic": float(np.mean(rmses)),
+        "solve_ms": float(np.mean(solve_ms)),
+        "wall_s": wall,
+        "gpu_launches": int(launches),
+        "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+    }
+    line.update(extra)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    pd.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,175 @@
+/* pdds_gb300 -- C ABI of the GB300-native PDDSparse hot path.
+ *
+ * The library estimates, on one GPU, the sparse interface system of the
+ * probabilistic domain decomposition method PDDSparse: for every collocation
+ * knot it runs Euler-Maruyama paths of the Feynman-Kac diffusion until they
+ * leave the knot's stencil rectangle (Gobet-Menozzi shifted exit), turns the
+ * exits into one row of G (Gaussian-RBF interpolation weights of the stencil
+ * knots) and one entry of B, and solves (I + G) u = B.
+ *
+ * Reference interfaces replaced (paths inside the PDDS repository):
+ *   struct bvp                          BVPs/BVP.hpp:89-137
+ *   Fullfill_interfaces/Compute_Stencil PDDAlgorithms/PDDSparseGM.cpp:346-689, 1845-2041
+ *   Stencil::Compute_ipsi               Meshes/stencil.cpp:115-243
+ *   EMFKACSolver::Solve_OMP_Analytic    Solvers/EMFKACSolver.hpp:711-729
+ *     (Simulate_OMP :108-216, Reduce_Analytic :514-575, G_update stencil.cpp:244-307,
+ *      G_return_withrep stencil.cpp:343-406)
+ *   PDDSparseGM::Solve worker loop      PDDAlgorithms/PDDSparseGM.cpp:795-848
+ *   PDDSparseGM::Compute_Solution       PDDAlgorithms/PDDSparseGM.cpp:3168-3246
+ *   MCinCUDA (the reference's unused GPU entry) Solvers/MCinCUDA.cu:441-480
+ *
+ * Conventions: every call returns a pdds_status; nothing aborts.  All work is
+ * ordered on the context's CUDA stream; one context per host thread.  Output
+ * buffers are caller-owned host memory; device scratch is context-owned.
+ */
+#ifndef PDDS_H
+#define PDDS_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  PDDS_OK = 0,
+  PDDS_ERR_INVALID = 1,         /* bad argument or call order            */
+  PDDS_ERR_CUDA = 2,            /* CUDA runtime error (see last_error)   */
+  PDDS_ERR_STEP_LIMIT = 3,      /* a path exceeded max_steps             */
+  PDDS_ERR_TIMEOUT = 4,         /* a bounded device wait gave up         */
+  PDDS_ERR_ILL_CONDITIONED = 5, /* an RBF matrix is numerically singular */
+  PDDS_ERR_NOT_CONVERGED = 6,   /* interface solve missed its tolerance  */
+  PDDS_ERR_NO_MEMORY = 7,
+  PDDS_ERR_EXIT_SIDE = 8        /* an exit matched no stencil side       */
+} pdds_status;
+
+typedef struct pdds_ctx pdds_ctx;
+
+/* ---------------------------------------------------------------- context */
+pdds_status pdds_create(pdds_ctx** ctx, int device, uint32_t flags);
+pdds_status pdds_destroy(pdds_ctx* ctx);
+const char* pdds_last_error(const pdds_ctx* ctx);
+const char* pdds_version(void);
+
+/* ---------------------------------------------------------------- problem
+ * Replaces the function-pointer struct bvp (BVPs/BVP.hpp:89-137) on the GPU:
+ * problems are compiled device functors selected by kind. */
+typedef enum {
+  PDDS_POISSON_SINCOS = 0, /* u = sin(pi x)cos(pi y) + x y, sigma = sqrt2 I, f = -Lap u  */
+  PDDS_MONEGROS = 1,       /* the reference's Monegros Poisson test problem            */
+  PDDS_HELMHOLTZ = 2,      /* u = sin(a x)cos(b y); p = {a, b, c}, c <= 0               */
+  PDDS_VARCOEF = 3         /* sigma = diag(1+x^2/2, 1+y^2/2), b = (y,-x),
+                              c = -(1+x^2+y^2), u = e^x cos 2y + 1                      */
+} pdds_problem_kind;
+
+typedef struct {
+  int32_t kind;       /* pdds_problem_kind                                   */
+  int32_t use_cv;     /* 1: control variate xi with the exact gradient       */
+  double p[8];        /* kind parameters                                     */
+} pdds_problem_desc;
+
+pdds_status pdds_problem_set(pdds_ctx* ctx, const pdds_problem_desc* desc);
+
+/* ---------------------------------------------------------------- layout
+ * Rectangular domain [SW, NE] split into nsub x nsub subdomains with nnode
+ * knots per interface segment (INTERSECTIONS_YES numbering) and the
+ * reference's stencils (STEN_ELONG = 0.5).  fac[kind] is the RBF shape c of a
+ * stencil side of that kind (c2[kind] in Stencil::Compute_ipsi). */
+typedef struct {
+  double sw[2], ne[2];
+  int32_t nsub;
+  int32_t nnode;
+  double fac[4];
+} pdds_layout_desc;
+
+typedef struct {
+  int32_t nknots;        /* K                                              */
+  int32_t nboundary;     /* knots on the domain boundary (B = g, no paths) */
+  int32_t nstencils;     /* distinct stencils                              */
+  int32_t nsides;        /* distinct stencil sides                         */
+  int32_t nshapes;       /* distinct side shapes (translates share one)    */
+  int32_t max_side;      /* largest side                                   */
+  int64_t nnz;           /* entries of G (rows of all knots)               */
+} pdds_layout_info;
+
+pdds_status pdds_layout_build(pdds_ctx* ctx, const pdds_layout_desc* desc, pdds_layout_info* info);
+/* Knot i's position (the one the reference hands to its worker) and the
+ * hand-out order of the reference's server loop. */
+pdds_status pdds_layout_knots(pdds_ctx* ctx, double* x, double* y, int32_t* order);
+/* CSR structure of G: row_ptr[K+1], col[nnz] (columns sorted per row). */
+pdds_status pdds_layout_csr(pdds_ctx* ctx, int64_t* row_ptr, int32_t* col);
+/* Stencil of knot k as the reference builds it: rect {x0,y0,x1,y1}, side kinds
+ * and sizes (N,S,E,W), side knot indices packed [4][maxn]. */
+pdds_status pdds_layout_stencil(pdds_ctx* ctx, int32_t knot, double* rect, int32_t* kinds,
+                                int32_t* sizes, int32_t* idx, int32_t maxn);
+
+/* ---------------------------------------------------------------- estimate */
+typedef enum {
+  PDDS_MODE_REPLAY_FP64 = 0, /* bit-exact replay of the CPU restatement          */
+  PDDS_MODE_FP64 = 1,        /* plain FP64 GPU form                               */
+  PDDS_MODE_MIXED = 2        /* FP32 paths, FP64 accumulation and factorisation   */
+} pdds_mode;
+
+typedef struct {
+  int32_t mode;          /* pdds_mode                                           */
+  int32_t npaths;        /* paths per knot (N)                                  */
+  double h;              /* Euler-Maruyama step                                 */
+  uint64_t seed;         /* Philox key                                          */
+  uint32_t instance;     /* Philox counter word 3 (independent replicas)        */
+  int32_t dup_sum;       /* 0: G_return_withrep overwrite (reference), 1: sum   */
+  int32_t want_var;      /* 1: compute G_var                                    */
+  int32_t bins_per_gap;  /* MIXED: exit bins per knot spacing (0 = default 16)  */
+  int64_t max_steps;     /* per path (0 = 1e6); exceeded -> PDDS_ERR_STEP_LIMIT */
+  /* REPLAY only, optional: RBF inverse matrices per knot, packed knot by knot
+   * in hand-out order, sides N,S,E,W, each n x n row-major with element
+   * (j,i) = ipsi(j,i) of the reference; NULL = factorise on the device. */
+  const double* ipsi_override;
+  int64_t ipsi_override_len;
+} pdds_estimate_desc;
+
+typedef struct {
+  int64_t path_steps;    /* Euler-Maruyama steps to the shifted exit     */
+  int64_t paths;         /* simulated paths                              */
+  int64_t exits_global;  /* exits on the domain boundary                 */
+  int64_t exits_stencil; /* exits on interior stencil sides              */
+  double ms_setup;       /* factorisation and tables                     */
+  double ms_paths;       /* path kernels and reduction                   */
+  int32_t kernel_launches;
+} pdds_estimate_info;
+
+/* Runs the estimation for all knots and keeps G and B on the device.  Any of
+ * the host output pointers may be NULL: val[nnz], var[nnz] (needs want_var),
+ * B[K], BB[K] (mean of the squared score, as Reduce_Analytic's BB). */
+pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double* val, double* var,
+                          double* B, double* BB, pdds_estimate_info* info);
+
+/* ---------------------------------------------------------------- solve */
+typedef enum {
+  PDDS_SOLVE_BICGSTAB_FP64 = 0, /* Jacobi-preconditioned BiCGSTAB, FP64 (reference) */
+  PDDS_SOLVE_GMRES_FP32_IR = 1  /* FP32 GMRES(m) inside FP64 iterative refinement   */
+} pdds_solve_method;
+
+typedef struct {
+  int32_t method;
+  int32_t restart;       /* GMRES(m), 2 <= m <= 40 (0 = 30) */
+  int32_t max_iter;      /* inner iterations per call / refinement step */
+  int32_t max_refine;    /* FP64 refinement steps */
+  double tol;            /* relative residual in FP64 */
+} pdds_solve_desc;
+
+typedef struct {
+  int32_t iterations;
+  int32_t refinements;
+  double rel_residual;
+  double ms;
+  int32_t kernel_launches;
+} pdds_solve_info;
+
+/* Solves (I + G) u = B with the G and B of the last pdds_estimate. */
+pdds_status pdds_solve_interface(pdds_ctx* ctx, const pdds_solve_desc* desc, double* u,
+                                 pdds_solve_info* info);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PDDS_H */

@@ -71,6 +71,7 @@ def lib():
         L.orc_layout_interface.argtypes = [vp, C.c_int, ip, ip, dp, dp]
         L.orc_stencil.argtypes = [vp, C.c_int, dp, ip, ip, ip, dp, dp, C.c_int]
         L.orc_ipsi.argtypes = [C.c_int, dp, dp, C.c_double, dp, dp]
+        L.orc_ipsi_ex.argtypes = [C.c_int, dp, dp, C.c_double, C.c_int, dp, dp]
         L.orc_knot.argtypes = [vp, C.POINTER(Problem), C.POINTER(Params), C.c_int, C.c_double,
                                C.c_double, dp, ip, dp, dp, C.c_int, ip, dp, dp, i64p]
         L.orc_knot_paths.argtypes = [vp, C.POINTER(Problem), C.POINTER(Params), C.c_int, C.c_double,
@@ -223,15 +224,40 @@ class Layout:
                     gvar=gv[:nnz], B=B, BB=BB, stats=st)
 
 
-def ipsi(x, y, c):
+def ipsi(x, y, c, portable=False):
     n = len(x)
     out = np.zeros((n, n))
     cond = C.c_double(0)
     x = np.ascontiguousarray(x, np.float64)
     y = np.ascontiguousarray(y, np.float64)
-    rank = lib().orc_ipsi(n, _p(x, C.c_double), _p(y, C.c_double), float(c), _p(out, C.c_double),
-                          C.byref(cond))
+    rank = lib().orc_ipsi_ex(n, _p(x, C.c_double), _p(y, C.c_double), float(c), int(bool(portable)),
+                             _p(out, C.c_double), C.byref(cond))
     return out, cond.value, rank
+
+
+def replay_ipsi(layout: "Layout", fac, portable=True):
+    """RBF inverses of every knot that runs paths, packed for the library's
+    replay mode: knots in hand-out order, sides N,S,E,W, each n x n row-major
+    ipsi(j,i) -- exactly the matrices this oracle uses in portable mode."""
+    blocks, mc = [], []
+    cache = {}
+    for kn, x0, y0 in zip(layout.work_idx, layout.work_x, layout.work_y):
+        params, kinds, sides = layout.stencil(int(kn))
+        # boundary knots (B = g) run no paths
+        cx, cy = 0.5 * (layout.sw[0] + layout.ne[0]), 0.5 * (layout.sw[1] + layout.ne[1])
+        hx, hy = layout.ne[0] - cx, layout.ne[1] - cy
+        if abs(max(abs(x0 - cx) - hx, abs(y0 - cy) - hy)) <= 1e-8:
+            continue
+        mc.append(int(kn))
+        for d in range(4):
+            idx, xs, ys = sides[d]
+            if len(idx) == 0:
+                continue
+            key = (tuple(idx.tolist()), int(kinds[d]))
+            if key not in cache:
+                cache[key] = ipsi(xs, ys, fac[kinds[d]], portable=portable)[0]
+            blocks.append(cache[key].ravel())
+    return np.concatenate(blocks) if blocks else np.zeros(0), mc
 
 
 def bicgstab(K, rows, cols, vals, b, maxit=None, tol=2.220446049250313e-16):

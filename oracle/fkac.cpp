@@ -525,8 +525,13 @@ int orc_stencil(const void* Lv, int knot, double* params, int* kinds, int* sizes
   return 0;
 }
 int orc_ipsi(int n, const double* x, const double* y, double c, double* ipsi, double* cond) {
+  return orc_ipsi_ex(n, x, y, c, 0, ipsi, cond);
+}
+int orc_ipsi_ex(int n, const double* x, const double* y, double c, int portable, double* ipsi,
+                double* cond) {
   std::vector<double> psi, inv;
-  build_psi<LibmMath>(n, x, y, c, psi);
+  if (portable) build_psi<PortMath>(n, x, y, c, psi);
+  else build_psi<LibmMath>(n, x, y, c, psi);
   const int rank = fullpiv_inverse(n, psi, inv);
   double a = 0.0, b = 0.0;
   for (size_t i = 0; i < psi.size(); i++) { a += psi[i] * psi[i]; b += inv[i] * inv[i]; }

@@ -53,6 +53,10 @@ int orc_stencil(const void* L, int knot, double* params, int* kinds, int* sizes,
 /* Psi_ij = exp(-|p_i - p_j|^2 / c^2); ipsi = full-pivot LU inverse, row-major.
  * cond = ||Psi||_F ||ipsi||_F (Meshes/stencil.cpp:171).  Returns rank. */
 int orc_ipsi(int n, const double* x, const double* y, double c, double* ipsi, double* cond);
+/* Same with the exponentials of the portable math (portable = 1), i.e. the
+ * inverse the portable-mode estimation computes internally. */
+int orc_ipsi_ex(int n, const double* x, const double* y, double c, int portable, double* ipsi,
+                double* cond);
 
 /* ---- estimation -----------------------------------------------------------*/
 /* stats[0] linear steps, [1] sublinear steps, [2] global exits, [3] stencil exits */

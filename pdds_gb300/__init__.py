@@ -1,0 +1,12 @@
+"""pdds_gb300: GB300-native Feynman-Kac estimation of the PDDSparse interface system.
+
+The compute path is libpdds_gb300.so (hand-written sm_103a CUDA behind the C
+ABI of include/pdds.h); this package is its host-side mirror of the
+reference's BVP / PDDSparseGM call surface.
+"""
+from ._capi import (MODE_FP64, MODE_MIXED, MODE_REPLAY_FP64, SOLVE_BICGSTAB_FP64, SOLVE_GMRES_FP32_IR,
+                    PDDSError)
+from .api import BVP, Estimate, PDDSparseGM, read_configuration
+
+__all__ = ["BVP", "Estimate", "PDDSparseGM", "PDDSError", "read_configuration", "MODE_FP64", "MODE_MIXED",
+           "MODE_REPLAY_FP64", "SOLVE_BICGSTAB_FP64", "SOLVE_GMRES_FP32_IR"]

@@ -1,0 +1,108 @@
+"""ctypes mirror of include/pdds.h.
+
+Loading fails loudly when the CUDA library has not been built: there is no
+CPU fallback for any entry point.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libpdds_gb300.so")
+
+# status codes
+OK, ERR_INVALID, ERR_CUDA, ERR_STEP_LIMIT, ERR_TIMEOUT, ERR_ILL_CONDITIONED, ERR_NOT_CONVERGED, \
+    ERR_NO_MEMORY, ERR_EXIT_SIDE = range(9)
+STATUS_NAMES = {0: "PDDS_OK", 1: "PDDS_ERR_INVALID", 2: "PDDS_ERR_CUDA", 3: "PDDS_ERR_STEP_LIMIT",
+                4: "PDDS_ERR_TIMEOUT", 5: "PDDS_ERR_ILL_CONDITIONED", 6: "PDDS_ERR_NOT_CONVERGED",
+                7: "PDDS_ERR_NO_MEMORY", 8: "PDDS_ERR_EXIT_SIDE"}
+
+POISSON_SINCOS, MONEGROS, HELMHOLTZ, VARCOEF = 0, 1, 2, 3
+MODE_REPLAY_FP64, MODE_FP64, MODE_MIXED = 0, 1, 2
+SOLVE_BICGSTAB_FP64, SOLVE_GMRES_FP32_IR = 0, 1
+
+EXPORTS = [
+    "pdds_create", "pdds_destroy", "pdds_last_error", "pdds_version", "pdds_problem_set",
+    "pdds_layout_build", "pdds_layout_knots", "pdds_layout_csr", "pdds_layout_stencil",
+    "pdds_estimate", "pdds_solve_interface",
+]
+
+
+class ProblemDesc(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("use_cv", C.c_int32), ("p", C.c_double * 8)]
+
+
+class LayoutDesc(C.Structure):
+    _fields_ = [("sw", C.c_double * 2), ("ne", C.c_double * 2), ("nsub", C.c_int32),
+                ("nnode", C.c_int32), ("fac", C.c_double * 4)]
+
+
+class LayoutInfo(C.Structure):
+    _fields_ = [("nknots", C.c_int32), ("nboundary", C.c_int32), ("nstencils", C.c_int32),
+                ("nsides", C.c_int32), ("nshapes", C.c_int32), ("max_side", C.c_int32),
+                ("nnz", C.c_int64)]
+
+
+class EstimateDesc(C.Structure):
+    _fields_ = [("mode", C.c_int32), ("npaths", C.c_int32), ("h", C.c_double), ("seed", C.c_uint64),
+                ("instance", C.c_uint32), ("dup_sum", C.c_int32), ("want_var", C.c_int32),
+                ("bins_per_gap", C.c_int32), ("max_steps", C.c_int64),
+                ("ipsi_override", C.POINTER(C.c_double)), ("ipsi_override_len", C.c_int64)]
+
+
+class EstimateInfo(C.Structure):
+    _fields_ = [("path_steps", C.c_int64), ("paths", C.c_int64), ("exits_global", C.c_int64),
+                ("exits_stencil", C.c_int64), ("ms_setup", C.c_double), ("ms_paths", C.c_double),
+                ("kernel_launches", C.c_int32)]
+
+
+class SolveDesc(C.Structure):
+    _fields_ = [("method", C.c_int32), ("restart", C.c_int32), ("max_iter", C.c_int32),
+                ("max_refine", C.c_int32), ("tol", C.c_double)]
+
+
+class SolveInfo(C.Structure):
+    _fields_ = [("iterations", C.c_int32), ("refinements", C.c_int32), ("rel_residual", C.c_double),
+                ("ms", C.c_double), ("kernel_launches", C.c_int32)]
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Loads the CUDA library; raises if it is missing (no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(
+            f"pdds_gb300 CUDA library not found at {path}; build it with "
+            "`python -c 'import __graft_entry__ as g; g.build()'`")
+    L = C.CDLL(path)
+    vp = C.c_void_p
+    dp = C.POINTER(C.c_double)
+    L.pdds_create.argtypes = [C.POINTER(vp), C.c_int, C.c_uint32]
+    L.pdds_destroy.argtypes = [vp]
+    L.pdds_last_error.restype = C.c_char_p
+    L.pdds_last_error.argtypes = [vp]
+    L.pdds_version.restype = C.c_char_p
+    L.pdds_problem_set.argtypes = [vp, C.POINTER(ProblemDesc)]
+    L.pdds_layout_build.argtypes = [vp, C.POINTER(LayoutDesc), C.POINTER(LayoutInfo)]
+    L.pdds_layout_knots.argtypes = [vp, dp, dp, C.POINTER(C.c_int32)]
+    L.pdds_layout_csr.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int32)]
+    L.pdds_layout_stencil.argtypes = [vp, C.c_int32, dp, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                      C.POINTER(C.c_int32), C.c_int32]
+    L.pdds_estimate.argtypes = [vp, C.POINTER(EstimateDesc), dp, dp, dp, dp, C.POINTER(EstimateInfo)]
+    L.pdds_solve_interface.argtypes = [vp, C.POINTER(SolveDesc), dp, C.POINTER(SolveInfo)]
+    for name in EXPORTS:
+        if not hasattr(L, name):
+            raise RuntimeError("missing export " + name)
+    _lib = L
+    return L
+
+
+class PDDSError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status

@@ -1,0 +1,270 @@
+"""Host-side mirror of the reference's PDDSparse call surface over the C ABI.
+
+  BVP            <- struct bvp (BVPs/BVP.hpp:89-137): problem selected by kind
+  read_configuration <- PDDSparseGM::ReadFromFile (PDDAlgorithms/PDDSparseGM.cpp:99-345)
+  PDDSparseGM    <- PDDSparseGM (PDDAlgorithms/PDDSparseGM.hpp:103-280):
+                    constructor = Fullfill_interfaces, estimate = the worker
+                    loop of Solve (:795-848) for every knot at once,
+                    solve_interface = Compute_Solution (:3168-3246),
+                    Solve = both.
+Everything runs through libpdds_gb300.so on one GPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _capi as capi
+from ._capi import PDDSError
+
+
+def _p(a, t):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+class BVP:
+    """A boundary value problem  1/2 tr(sigma sigma^T D^2 u) + b.grad u + c u + f = 0,
+    u = g on the boundary, compiled into the library and selected by kind."""
+
+    POISSON_SINCOS = capi.POISSON_SINCOS
+    MONEGROS = capi.MONEGROS
+    HELMHOLTZ = capi.HELMHOLTZ
+    VARCOEF = capi.VARCOEF
+
+    def __init__(self, kind: int, params=(), use_cv: bool = True):
+        self.kind = int(kind)
+        self.params = tuple(float(v) for v in params)
+        self.use_cv = bool(use_cv)
+
+    @classmethod
+    def poisson_sincos(cls):
+        """Lap u = f on the domain with u = sin(pi x)cos(pi y) + x y (sigma = sqrt2 I)."""
+        return cls(cls.POISSON_SINCOS)
+
+    @classmethod
+    def monegros(cls):
+        return cls(cls.MONEGROS)
+
+    @classmethod
+    def helmholtz(cls, a: float, b: float, c: float):
+        """Lap u + c u + f = 0 with u = sin(a x) cos(b y), c <= 0."""
+        return cls(cls.HELMHOLTZ, (a, b, c))
+
+    @classmethod
+    def varcoef(cls):
+        return cls(cls.VARCOEF)
+
+    def desc(self) -> capi.ProblemDesc:
+        d = capi.ProblemDesc()
+        d.kind = self.kind
+        d.use_cv = int(self.use_cv)
+        for i, v in enumerate(self.params):
+            d.p[i] = v
+        return d
+
+    def u(self, x, y):
+        """Exact solution (numpy, FP64)."""
+        x = np.asarray(x, np.float64)
+        y = np.asarray(y, np.float64)
+        if self.kind == self.POISSON_SINCOS:
+            return np.sin(np.pi * x) * np.cos(np.pi * y) + x * y
+        if self.kind == self.HELMHOLTZ:
+            return np.sin(self.params[0] * x) * np.cos(self.params[1] * y)
+        if self.kind == self.VARCOEF:
+            return np.exp(x) * np.cos(2 * y) + 1.0
+        q = 1.0 + 0.01 * x * x + 0.02 * y * y
+        return 3.0 + 0.333 * (np.sin(np.sqrt(q)) +
+                              np.tanh(np.sin(0.12 * x + 0.05 * y) + np.sin(0.05 * x - 0.12 * y)))
+
+
+def read_configuration(path: str) -> dict:
+    """Key = value configuration file of the reference (ReadFromFile).
+
+    Keys: h0, eps, fac (four values), T, SW (two), NE (two), N, N_job,
+    N_subdo, N_node; lines starting with '%' are comments.  As in the
+    reference a key is recognised with or without spaces around '=' and only
+    the first value of N_subdo / N_node is used for both directions.  A
+    single fac value is used for every side kind.
+    """
+    out = {"T": math.inf}
+    with open(path) as f:
+        for line in f:
+            if not line.strip() or line.lstrip().startswith("%"):
+                continue
+            if "=" not in line:
+                continue
+            key, _, rest = line.partition("=")
+            key = key.strip()
+            vals = rest.split()
+            if not vals:
+                continue
+            if key in ("h0", "eps", "T"):
+                out[key] = float(vals[0])
+            elif key in ("N", "N_job"):
+                out[key] = int(float(vals[0]))
+            elif key in ("N_subdo", "N_node"):
+                out[key] = int(float(vals[0]))
+            elif key in ("SW", "NE"):
+                out[key] = (float(vals[0]), float(vals[1]))
+            elif key == "fac":
+                f4 = [float(v) for v in vals[:4]]
+                while len(f4) < 4:
+                    f4.append(f4[-1])
+                out[key] = tuple(f4)
+    return out
+
+
+@dataclass
+class Estimate:
+    """G in CSR (row_ptr, col, val, var), B, BB and counters of one estimation."""
+
+    row_ptr: np.ndarray
+    col: np.ndarray
+    val: np.ndarray
+    var: np.ndarray
+    B: np.ndarray
+    BB: np.ndarray
+    info: dict = field(default_factory=dict)
+
+    @property
+    def B_var(self):
+        """The reference's signed B_var = B^2 - BB (PDDSparseGM.cpp:833)."""
+        return self.B * self.B - self.BB
+
+    def triplets(self):
+        rows = np.repeat(np.arange(len(self.row_ptr) - 1), np.diff(self.row_ptr))
+        return rows, self.col, self.val
+
+
+class PDDSparseGM:
+    """GPU PDDSparse interface system on a rectangular layout.
+
+    fac[kind] is the Gaussian RBF shape c of a stencil side of that kind
+    (the reference's c2[kind], Meshes/stencil.cpp:211-243)."""
+
+    def __init__(self, sw=(-1.0, -1.0), ne=(1.0, 1.0), nsub: int = 4, nnode: int = 11,
+                 fac=(1.0, 1.0, 1.0, 1.0), device: int = 0):
+        self._lib = capi.load()
+        self._ctx = C.c_void_p()
+        st = self._lib.pdds_create(C.byref(self._ctx), int(device), 0)
+        if st != capi.OK:
+            raise PDDSError(st, "pdds_create failed (device %d)" % device)
+        self.device = device
+        d = capi.LayoutDesc()
+        d.sw[0], d.sw[1] = float(sw[0]), float(sw[1])
+        d.ne[0], d.ne[1] = float(ne[0]), float(ne[1])
+        d.nsub = int(nsub)
+        d.nnode = int(nnode)
+        for i in range(4):
+            d.fac[i] = float(fac[i])
+        info = capi.LayoutInfo()
+        self._check(self._lib.pdds_layout_build(self._ctx, C.byref(d), C.byref(info)))
+        self.sw, self.ne, self.nsub, self.nnode, self.fac = tuple(sw), tuple(ne), nsub, nnode, tuple(fac)
+        self.layout_info = {f: getattr(info, f) for f, _ in capi.LayoutInfo._fields_}
+        K = info.nknots
+        self.K = K
+        self.x = np.zeros(K)
+        self.y = np.zeros(K)
+        self.order = np.zeros(K, np.int32)
+        self._check(self._lib.pdds_layout_knots(self._ctx, _p(self.x, C.c_double), _p(self.y, C.c_double),
+                                                _p(self.order, C.c_int32)))
+        self.row_ptr = np.zeros(K + 1, np.int64)
+        self.col = np.zeros(max(info.nnz, 1), np.int32)
+        self._check(self._lib.pdds_layout_csr(self._ctx, _p(self.row_ptr, C.c_int64),
+                                              _p(self.col, C.c_int32)))
+        self.col = self.col[:info.nnz]
+        self.nnz = int(info.nnz)
+
+    @classmethod
+    def from_configuration(cls, path: str, device: int = 0):
+        cfg = read_configuration(path)
+        return cls(cfg["SW"], cfg["NE"], cfg["N_subdo"], cfg["N_node"], cfg["fac"], device=device)
+
+    # ------------------------------------------------------------------
+    def _check(self, st):
+        if st != capi.OK:
+            msg = self._lib.pdds_last_error(self._ctx).decode() if self._ctx else ""
+            raise PDDSError(st, msg)
+
+    def close(self):
+        if getattr(self, "_ctx", None) and self._ctx.value:
+            self._lib.pdds_destroy(self._ctx)
+            self._ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ------------------------------------------------------------------
+    def stencil(self, knot: int, maxn: int = 512):
+        rect = np.zeros(4)
+        kinds = np.zeros(4, np.int32)
+        sizes = np.zeros(4, np.int32)
+        idx = np.zeros(4 * maxn, np.int32)
+        self._check(self._lib.pdds_layout_stencil(self._ctx, int(knot), _p(rect, C.c_double),
+                                                  _p(kinds, C.c_int32), _p(sizes, C.c_int32),
+                                                  _p(idx, C.c_int32), maxn))
+        return rect, kinds, [idx[d * maxn:d * maxn + sizes[d]].copy() for d in range(4)]
+
+    def estimate(self, bvp: BVP, npaths: int, h: float, mode: int = capi.MODE_MIXED, seed: int = 1234,
+                 instance: int = 0, dup_sum: bool = False, want_var: bool = False,
+                 bins_per_gap: int = 0, max_steps: int = 0, ipsi_override=None) -> Estimate:
+        """Runs the Feynman-Kac estimation of every knot's G row and B entry."""
+        self._check(self._lib.pdds_problem_set(self._ctx, C.byref(bvp.desc())))
+        d = capi.EstimateDesc()
+        d.mode = int(mode)
+        d.npaths = int(npaths)
+        d.h = float(h)
+        d.seed = int(seed)
+        d.instance = int(instance)
+        d.dup_sum = int(bool(dup_sum))
+        d.want_var = int(bool(want_var))
+        d.bins_per_gap = int(bins_per_gap)
+        d.max_steps = int(max_steps)
+        keep = None
+        if ipsi_override is not None:
+            keep = np.ascontiguousarray(ipsi_override, np.float64)
+            d.ipsi_override = _p(keep, C.c_double)
+            d.ipsi_override_len = keep.size
+        val = np.zeros(max(self.nnz, 1))
+        var = np.zeros(max(self.nnz, 1))
+        B = np.zeros(self.K)
+        BB = np.zeros(self.K)
+        info = capi.EstimateInfo()
+        self._check(self._lib.pdds_estimate(self._ctx, C.byref(d), _p(val, C.c_double), _p(var, C.c_double),
+                                            _p(B, C.c_double), _p(BB, C.c_double), C.byref(info)))
+        del keep
+        return Estimate(self.row_ptr, self.col, val[:self.nnz], var[:self.nnz], B, BB,
+                        {f: getattr(info, f) for f, _ in capi.EstimateInfo._fields_})
+
+    def solve_interface(self, method: int = capi.SOLVE_GMRES_FP32_IR, tol: float = 1e-10,
+                        restart: int = 30, max_iter: int = 0, max_refine: int = 0):
+        """Solves (I + G) u = B for the last estimate; returns (u, info)."""
+        d = capi.SolveDesc()
+        d.method = int(method)
+        d.restart = int(restart)
+        d.max_iter = int(max_iter)
+        d.max_refine = int(max_refine)
+        d.tol = float(tol)
+        u = np.zeros(self.K)
+        info = capi.SolveInfo()
+        self._check(self._lib.pdds_solve_interface(self._ctx, C.byref(d), _p(u, C.c_double), C.byref(info)))
+        return u, {f: getattr(info, f) for f, _ in capi.SolveInfo._fields_}
+
+    def Solve(self, bvp: BVP, npaths: int, h: float, mode: int = capi.MODE_MIXED, seed: int = 1234,
+              method: int = capi.SOLVE_GMRES_FP32_IR, tol: float = 1e-10, **kw):
+        """Estimate G and B for all knots, then solve the interface system."""
+        est = self.estimate(bvp, npaths, h, mode=mode, seed=seed, **kw)
+        u, sinfo = self.solve_interface(method=method, tol=tol)
+        return u, est, sinfo

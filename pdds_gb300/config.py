@@ -1,0 +1,38 @@
+"""Workload definitions and the RBF shape rule.
+
+The reference sets the Gaussian RBF shape c of a stencil side from fac[kind]
+(Meshes/stencil.cpp:211-243); its configuration.txt uses
+fac = 1.5 1.27 1.2 1.13 at a knot spacing of 10/28, i.e. c = kappa * spacing
+with kappa = (4.2, 3.556, 3.36, 3.164) for side kinds 0..3 (one interface with
+one elongation ... two interfaces with two elongations).  fac_rule keeps those
+ratios for any layout, which keeps cond(Psi) near the reference's 1e9..1e11.
+"""
+from __future__ import annotations
+
+REF_FAC = (1.5, 1.27, 1.2, 1.13)
+REF_SPACING = 10.0 / 28.0
+KAPPA = tuple(f / REF_SPACING for f in REF_FAC)
+
+
+def fac_rule(side_length: float, nsub: int, nnode: int):
+    """fac[kind] = kappa[kind] * knot spacing for a square layout of side length L.
+
+    With more than 16 knots per segment the sides hold 45..130 knots and the
+    kind 0..2 ratios push cond(Psi) past 1e12 (4e13 for the 84-knot sides of
+    43-knot segments, where two inverse algorithms then disagree by 1e-4 in
+    the cardinal weights); there every kind uses the kind-3 ratio 3.164,
+    which keeps cond(Psi) near 4e10."""
+    gap = side_length / ((nnode - 1) * nsub)
+    kappa = KAPPA if nnode <= 16 else (KAPPA[3],) * 4
+    return tuple(k * gap for k in kappa)
+
+
+# The synthetic workloads of the benchmark configurations.
+WORKLOADS = {
+    # 2-D Poisson on [-1,1]^2, u = sin(pi x)cos(pi y) + xy, 4x4 subdomains, 11 knots per segment
+    "poisson_4x4_n11": dict(sw=(-1.0, -1.0), ne=(1.0, 1.0), nsub=4, nnode=11, npaths=10_000, h=1e-3),
+    # the same problem scaled up: 12x12 subdomains, 43 knots per segment
+    "poisson_12x12_n43": dict(sw=(-1.0, -1.0), ne=(1.0, 1.0), nsub=12, nnode=43, npaths=20_000, h=5e-4),
+    # variable coefficients on [0,1]^2, 8x8 subdomains, 31 knots per segment
+    "varcoef_8x8_n31": dict(sw=(0.0, 0.0), ne=(1.0, 1.0), nsub=8, nnode=31, npaths=50_000, h=5e-4),
+}

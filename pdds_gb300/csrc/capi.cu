@@ -1,0 +1,689 @@
+// C ABI of pdds_gb300 (declared in include/pdds.h): context, problem, layout,
+// estimation and interface solve.  Host orchestration in C++; the work runs in
+// the kernels of k_*.cu on the context's stream.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/pdds.h"
+#include "kernels.h"
+#include "pdds_internal.h"
+#include "solve.h"
+
+using namespace pdds;
+
+namespace {
+
+template <typename T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  cudaError_t resize(size_t count) {
+    if (count <= n && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    if (count == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    if (e == cudaSuccess) n = count;
+    return e;
+  }
+  cudaError_t upload(const std::vector<T>& v, cudaStream_t s) {
+    cudaError_t e = resize(std::max<size_t>(v.size(), 1));
+    if (e != cudaSuccess || v.empty()) return e;
+    return cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s);
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+}  // namespace
+
+struct pdds_ctx {
+  int device = -1;
+  cudaStream_t stream = nullptr;
+  int num_sms = 0;
+  std::string err;
+  bool has_problem = false;
+  pdds_problem_desc prob{};
+  bool has_layout = false;
+  HostLayout L;
+  int bins = 16;
+  bool tables_ready = false;
+  // device layout
+  DBuf<double> kx, ky, st_rect, sd_c, sd_origin, side_px, side_py, sh_c, sh_lo, sh_delta, sh_t, ipsi;
+  DBuf<int> knot_stencil, st_side, st_glob, map_pos, sd_n, sd_orient, sd_shape, side_knot, sh_n,
+      sh_nbins, col, mc_knots, bnd_knots;
+  DBuf<int64_t> row_ptr, st_map_off, sd_knot_off, sh_tab_off, sh_ipsi_off, sh_t_off;
+  DBuf<unsigned char> map_owner;
+  DBuf<float> tab;
+  DevLayout dl{};
+  int n_mc = 0, n_bnd = 0;
+  size_t mixed_smem = 0, fp64_smem = 0;
+  int max_nbins = 0;
+  // results and scratch
+  DBuf<double> G, GG, B, BB, Bsum, BBsum;
+  DBuf<unsigned long long> stats;
+  DBuf<unsigned> errf;
+  DBuf<int> counter;
+  bool has_estimate = false;
+  // replay scratch
+  DBuf<double> rx, ry, rY, rZ, rxi, Gside, GGside, ipsi_knot;
+  DBuf<int> rside, rsl, rss, task_m, task_d, task_i;
+  DBuf<int64_t> task_out, knot_task_off, knot_ipsi_off;
+  // solve scratch
+  DBuf<double> sv64, sscal, spart, shess, su;
+  DBuf<float> sV32, sw32, sval32;
+  double* host_rr = nullptr;
+  int solve_m = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
+};
+
+namespace {
+
+pdds_status fail(pdds_ctx* c, pdds_status s, const std::string& msg) {
+  if (c) c->err = msg;
+  return s;
+}
+
+#define CK(call)                                                                         \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess)                                                               \
+      return fail(ctx, PDDS_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+pdds_status upload_layout(pdds_ctx* ctx) {
+  HostLayout& L = ctx->L;
+  cudaStream_t s = ctx->stream;
+  std::vector<double> st_rect;
+  std::vector<int> st_side, st_glob;
+  std::vector<int64_t> st_map_off;
+  for (auto& st : L.stencils) {
+    for (int q = 0; q < 4; q++) {
+      st_rect.push_back(st.rect[q]);
+      st_side.push_back(st.side[q]);
+      st_glob.push_back(st.glob[q]);
+    }
+    st_map_off.push_back(st.map_off);
+  }
+  std::vector<int> sd_n, sd_orient, sd_shape;
+  std::vector<double> sd_c, sd_origin;
+  std::vector<int64_t> sd_knot_off;
+  for (auto& sd : L.sides) {
+    sd_n.push_back(sd.n);
+    sd_orient.push_back(sd.orient);
+    sd_shape.push_back(sd.shape);
+    sd_c.push_back(sd.c);
+    sd_origin.push_back(sd.origin);
+    sd_knot_off.push_back(sd.knot_off);
+  }
+  std::vector<int> sh_n, sh_nbins;
+  std::vector<double> sh_c, sh_lo, sh_delta, sh_t;
+  std::vector<int64_t> sh_tab_off, sh_ipsi_off, sh_t_off;
+  int64_t ipsi_len = 0, tab_len = 0;
+  int max_n = 0;
+  ctx->max_nbins = 0;
+  for (auto& sh : L.shapes) {
+    sh_n.push_back(sh.n);
+    sh_nbins.push_back(sh.nbins);
+    sh_c.push_back(sh.c);
+    sh_lo.push_back(sh.lo);
+    sh_delta.push_back(sh.delta);
+    sh_tab_off.push_back(sh.tab_off);
+    sh_ipsi_off.push_back(sh.ipsi_off);
+    sh_t_off.push_back((int64_t)sh_t.size());
+    for (double v : sh.t) sh_t.push_back(v);
+    ipsi_len = std::max<int64_t>(ipsi_len, sh.ipsi_off + (int64_t)sh.n * sh.n);
+    tab_len = std::max<int64_t>(tab_len, sh.tab_off + (int64_t)sh.nbins * sh.n);
+    max_n = std::max(max_n, sh.n);
+    ctx->max_nbins = std::max(ctx->max_nbins, sh.nbins);
+  }
+  if (max_n > 160) return fail(ctx, PDDS_ERR_INVALID, "stencil side larger than 160 knots");
+  std::vector<int> mc, bnd;
+  for (int v : L.order) (L.knot_boundary[v] ? bnd : mc).push_back(v);
+  ctx->n_mc = (int)mc.size();
+  ctx->n_bnd = (int)bnd.size();
+  // shared-memory needs of the path kernels
+  size_t msm = 0, fsm = 0;
+  for (auto& st : L.stencils) {
+    size_t nb = 0, nn = 0;
+    for (int q = 0; q < 4; q++)
+      if (st.side[q] >= 0) {
+        nb += L.shapes[L.sides[st.side[q]].shape].nbins;
+        nn += L.sides[st.side[q]].n;
+      }
+    msm = std::max(msm, nb);
+    fsm = std::max(fsm, nn);
+  }
+  ctx->mixed_smem = msm * sizeof(float);
+  ctx->fp64_smem = 2 * fsm * sizeof(double);
+  std::vector<unsigned char> owner(L.map_owner.begin(), L.map_owner.end());
+  std::vector<int> knot_stencil(L.knot_stencil.begin(), L.knot_stencil.end());
+  CK(ctx->kx.upload(L.kx, s));
+  CK(ctx->ky.upload(L.ky, s));
+  CK(ctx->knot_stencil.upload(knot_stencil, s));
+  CK(ctx->row_ptr.upload(L.row_ptr, s));
+  CK(ctx->col.upload(L.col, s));
+  CK(ctx->st_rect.upload(st_rect, s));
+  CK(ctx->st_side.upload(st_side, s));
+  CK(ctx->st_glob.upload(st_glob, s));
+  CK(ctx->st_map_off.upload(st_map_off, s));
+  CK(ctx->map_pos.upload(L.map_pos, s));
+  CK(ctx->map_owner.upload(owner, s));
+  CK(ctx->sd_n.upload(sd_n, s));
+  CK(ctx->sd_orient.upload(sd_orient, s));
+  CK(ctx->sd_shape.upload(sd_shape, s));
+  CK(ctx->sd_c.upload(sd_c, s));
+  CK(ctx->sd_origin.upload(sd_origin, s));
+  CK(ctx->sd_knot_off.upload(sd_knot_off, s));
+  CK(ctx->side_knot.upload(L.side_knot, s));
+  CK(ctx->side_px.upload(L.side_px, s));
+  CK(ctx->side_py.upload(L.side_py, s));
+  CK(ctx->sh_n.upload(sh_n, s));
+  CK(ctx->sh_nbins.upload(sh_nbins, s));
+  CK(ctx->sh_c.upload(sh_c, s));
+  CK(ctx->sh_lo.upload(sh_lo, s));
+  CK(ctx->sh_delta.upload(sh_delta, s));
+  CK(ctx->sh_tab_off.upload(sh_tab_off, s));
+  CK(ctx->sh_ipsi_off.upload(sh_ipsi_off, s));
+  CK(ctx->sh_t_off.upload(sh_t_off, s));
+  CK(ctx->sh_t.upload(sh_t, s));
+  CK(ctx->mc_knots.upload(mc, s));
+  CK(ctx->bnd_knots.upload(bnd, s));
+  CK(ctx->ipsi.resize(std::max<int64_t>(ipsi_len, 1)));
+  CK(ctx->tab.resize(std::max<int64_t>(tab_len, 1)));
+  const int64_t nnz = L.row_ptr[L.K];
+  CK(ctx->G.resize(std::max<int64_t>(nnz, 1)));
+  CK(ctx->GG.resize(std::max<int64_t>(nnz, 1)));
+  CK(ctx->B.resize(std::max(L.K, 1)));
+  CK(ctx->BB.resize(std::max(L.K, 1)));
+  CK(ctx->Bsum.resize(std::max(L.K, 1)));
+  CK(ctx->BBsum.resize(std::max(L.K, 1)));
+  DevLayout& d = ctx->dl;
+  d.K = L.K;
+  d.S = (int)L.stencils.size();
+  d.D = (int)L.sides.size();
+  d.P = (int)L.shapes.size();
+  d.dom[0] = L.sw[0]; d.dom[1] = L.sw[1]; d.dom[2] = L.ne[0]; d.dom[3] = L.ne[1];
+  d.kx = ctx->kx.p; d.ky = ctx->ky.p; d.knot_stencil = ctx->knot_stencil.p; d.row_ptr = ctx->row_ptr.p;
+  d.st_rect = ctx->st_rect.p; d.st_side = ctx->st_side.p; d.st_glob = ctx->st_glob.p;
+  d.st_map_off = ctx->st_map_off.p; d.map_pos = ctx->map_pos.p; d.map_owner = ctx->map_owner.p;
+  d.sd_n = ctx->sd_n.p; d.sd_orient = ctx->sd_orient.p; d.sd_shape = ctx->sd_shape.p;
+  d.sd_c = ctx->sd_c.p; d.sd_origin = ctx->sd_origin.p; d.sd_knot_off = ctx->sd_knot_off.p;
+  d.side_knot = ctx->side_knot.p; d.side_px = ctx->side_px.p; d.side_py = ctx->side_py.p;
+  d.sh_n = ctx->sh_n.p; d.sh_c = ctx->sh_c.p; d.sh_lo = ctx->sh_lo.p; d.sh_delta = ctx->sh_delta.p;
+  d.sh_nbins = ctx->sh_nbins.p; d.sh_tab_off = ctx->sh_tab_off.p; d.sh_ipsi_off = ctx->sh_ipsi_off.p;
+  d.sh_t_off = ctx->sh_t_off.p; d.sh_t = ctx->sh_t.p;
+  d.tab = ctx->tab.p;
+  d.ipsi = ctx->ipsi.p;
+  ctx->tables_ready = false;
+  return PDDS_OK;
+}
+
+ProblemDev problem_dev(const pdds_problem_desc& p) {
+  ProblemDev d;
+  d.kind = p.kind;
+  d.use_cv = p.use_cv;
+  for (int i = 0; i < 8; i++) d.p[i] = p.p[i];
+  return d;
+}
+
+pdds_status check_err_flags(pdds_ctx* ctx) {
+  unsigned f = 0;
+  CK(cudaMemcpyAsync(&f, ctx->errf.p, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (f & ERR_FLAG_SINGULAR) return fail(ctx, PDDS_ERR_ILL_CONDITIONED, "RBF matrix numerically singular");
+  if (f & ERR_FLAG_STEP_LIMIT) return fail(ctx, PDDS_ERR_STEP_LIMIT, "a path exceeded max_steps");
+  if (f & ERR_FLAG_EXIT_SIDE) return fail(ctx, PDDS_ERR_EXIT_SIDE, "an exit matched no stencil side");
+  return PDDS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* pdds_version(void) { return "pdds_gb300 0.1 (sm_103a)"; }
+
+pdds_status pdds_create(pdds_ctx** out, int device, uint32_t flags) {
+  (void)flags;
+  if (!out) return PDDS_ERR_INVALID;
+  pdds_ctx* ctx = new pdds_ctx();
+  ctx->device = device;
+  if (device >= 0) {
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev2);
+    if (e == cudaSuccess) e = cudaMallocHost(&ctx->host_rr, sizeof(double));
+    if (e == cudaSuccess) e = ctx->stats.resize(8);
+    if (e == cudaSuccess) e = ctx->errf.resize(1);
+    if (e == cudaSuccess) e = ctx->counter.resize(1);
+    if (e != cudaSuccess) {
+      delete ctx;
+      return PDDS_ERR_CUDA;
+    }
+  }
+  *out = ctx;
+  return PDDS_OK;
+}
+
+pdds_status pdds_destroy(pdds_ctx* ctx) {
+  if (!ctx) return PDDS_ERR_INVALID;
+  if (ctx->device >= 0) {
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    DBuf<double>* d64[] = {&ctx->kx, &ctx->ky, &ctx->st_rect, &ctx->sd_c, &ctx->sd_origin, &ctx->side_px,
+                           &ctx->side_py, &ctx->sh_c, &ctx->sh_lo, &ctx->sh_delta, &ctx->sh_t, &ctx->ipsi,
+                           &ctx->G, &ctx->GG, &ctx->B, &ctx->BB, &ctx->Bsum, &ctx->BBsum, &ctx->rx,
+                           &ctx->ry, &ctx->rY, &ctx->rZ, &ctx->rxi, &ctx->Gside, &ctx->GGside,
+                           &ctx->ipsi_knot, &ctx->sv64, &ctx->sscal, &ctx->spart, &ctx->shess, &ctx->su};
+    for (auto* b : d64) b->release();
+    DBuf<int>* di[] = {&ctx->knot_stencil, &ctx->st_side, &ctx->st_glob, &ctx->map_pos, &ctx->sd_n,
+                       &ctx->sd_orient, &ctx->sd_shape, &ctx->side_knot, &ctx->sh_n, &ctx->sh_nbins,
+                       &ctx->col, &ctx->mc_knots, &ctx->bnd_knots, &ctx->counter, &ctx->rside,
+                       &ctx->rsl, &ctx->rss, &ctx->task_m, &ctx->task_d, &ctx->task_i};
+    for (auto* b : di) b->release();
+    DBuf<int64_t>* dl[] = {&ctx->row_ptr, &ctx->st_map_off, &ctx->sd_knot_off, &ctx->sh_tab_off,
+                           &ctx->sh_ipsi_off, &ctx->sh_t_off, &ctx->task_out, &ctx->knot_task_off,
+                           &ctx->knot_ipsi_off};
+    for (auto* b : dl) b->release();
+    ctx->map_owner.release();
+    ctx->tab.release();
+    ctx->stats.release();
+    ctx->errf.release();
+    ctx->sV32.release();
+    ctx->sw32.release();
+    ctx->sval32.release();
+    if (ctx->host_rr) cudaFreeHost(ctx->host_rr);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->ev2) cudaEventDestroy(ctx->ev2);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  }
+  delete ctx;
+  return PDDS_OK;
+}
+
+const char* pdds_last_error(const pdds_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+pdds_status pdds_problem_set(pdds_ctx* ctx, const pdds_problem_desc* desc) {
+  if (!ctx || !desc) return PDDS_ERR_INVALID;
+  if (desc->kind < 0 || desc->kind > 3) return fail(ctx, PDDS_ERR_INVALID, "unknown problem kind");
+  if (desc->kind == PDDS_HELMHOLTZ && desc->p[2] > 0.0)
+    return fail(ctx, PDDS_ERR_INVALID, "Helmholtz reaction c must be <= 0");
+  ctx->prob = *desc;
+  ctx->has_problem = true;
+  return PDDS_OK;
+}
+
+pdds_status pdds_layout_build(pdds_ctx* ctx, const pdds_layout_desc* desc, pdds_layout_info* info) {
+  if (!ctx || !desc) return PDDS_ERR_INVALID;
+  for (int q = 0; q < 4; q++)
+    if (!(desc->fac[q] > 0.0)) return fail(ctx, PDDS_ERR_INVALID, "fac must be positive");
+  const std::string e = build_rect_layout(ctx->L, desc->sw, desc->ne, desc->nsub, desc->nnode, desc->fac,
+                                          ctx->bins);
+  if (!e.empty()) return fail(ctx, PDDS_ERR_INVALID, e);
+  ctx->has_layout = true;
+  ctx->has_estimate = false;
+  if (ctx->device >= 0) {
+    pdds_status st = upload_layout(ctx);
+    if (st != PDDS_OK) return st;
+  }
+  if (info) {
+    info->nknots = ctx->L.K;
+    info->nboundary = ctx->L.nboundary;
+    info->nstencils = (int)ctx->L.stencils.size();
+    info->nsides = (int)ctx->L.sides.size();
+    info->nshapes = (int)ctx->L.shapes.size();
+    info->max_side = ctx->L.max_side;
+    info->nnz = ctx->L.row_ptr[ctx->L.K];
+  }
+  return PDDS_OK;
+}
+
+pdds_status pdds_layout_knots(pdds_ctx* ctx, double* x, double* y, int32_t* order) {
+  if (!ctx || !ctx->has_layout) return fail(ctx, PDDS_ERR_INVALID, "no layout");
+  const HostLayout& L = ctx->L;
+  if (x) std::copy(L.kx.begin(), L.kx.end(), x);
+  if (y) std::copy(L.ky.begin(), L.ky.end(), y);
+  if (order) std::copy(L.order.begin(), L.order.end(), order);
+  return PDDS_OK;
+}
+
+pdds_status pdds_layout_csr(pdds_ctx* ctx, int64_t* row_ptr, int32_t* col) {
+  if (!ctx || !ctx->has_layout) return fail(ctx, PDDS_ERR_INVALID, "no layout");
+  if (row_ptr) std::copy(ctx->L.row_ptr.begin(), ctx->L.row_ptr.end(), row_ptr);
+  if (col) std::copy(ctx->L.col.begin(), ctx->L.col.end(), col);
+  return PDDS_OK;
+}
+
+pdds_status pdds_layout_stencil(pdds_ctx* ctx, int32_t knot, double* rect, int32_t* kinds,
+                                int32_t* sizes, int32_t* idx, int32_t maxn) {
+  if (!ctx || !ctx->has_layout) return fail(ctx, PDDS_ERR_INVALID, "no layout");
+  const HostLayout& L = ctx->L;
+  if (knot < 0 || knot >= L.K) return fail(ctx, PDDS_ERR_INVALID, "knot out of range");
+  const StencilRec& st = L.stencils[L.knot_stencil[knot]];
+  for (int q = 0; q < 4; q++) {
+    if (rect) rect[q] = st.rect[q];
+    if (kinds) kinds[q] = st.kind[q];
+    const int sd = st.side[q];
+    const int n = sd >= 0 ? L.sides[sd].n : 0;
+    if (sizes) sizes[q] = n;
+    if (n > maxn) return fail(ctx, PDDS_ERR_INVALID, "maxn too small");
+    if (idx)
+      for (int i = 0; i < n; i++) idx[q * maxn + i] = L.side_knot[L.sides[sd].knot_off + i];
+  }
+  return PDDS_OK;
+}
+
+pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double* val, double* var,
+                          double* Bout, double* BBout, pdds_estimate_info* info) {
+  if (!ctx || !desc) return PDDS_ERR_INVALID;
+  if (ctx->device < 0) return fail(ctx, PDDS_ERR_INVALID, "context has no device");
+  if (!ctx->has_problem) return fail(ctx, PDDS_ERR_INVALID, "no problem set");
+  if (!ctx->has_layout) return fail(ctx, PDDS_ERR_INVALID, "no layout built");
+  if (desc->npaths < 1 || !(desc->h > 0.0)) return fail(ctx, PDDS_ERR_INVALID, "npaths >= 1 and h > 0 required");
+  const int mode = desc->mode;
+  if (mode < 0 || mode > 2) return fail(ctx, PDDS_ERR_INVALID, "unknown mode");
+  if (mode == PDDS_MODE_REPLAY_FP64 && ctx->prob.kind == PDDS_MONEGROS)
+    return fail(ctx, PDDS_ERR_INVALID, "the Monegros problem has no replay form");
+  CK(cudaSetDevice(ctx->device));
+  cudaStream_t s = ctx->stream;
+  HostLayout& L = ctx->L;
+  const int bins = desc->bins_per_gap > 0 ? desc->bins_per_gap : 16;
+  if (bins != ctx->bins) {
+    ctx->bins = bins;
+    set_shape_bins(L, bins);
+    pdds_status st = upload_layout(ctx);
+    if (st != PDDS_OK) return st;
+  }
+  const int64_t nnz = L.row_ptr[L.K];
+  const long long max_steps = desc->max_steps > 0 ? desc->max_steps : 1000000LL;
+  const ProblemDev P = problem_dev(ctx->prob);
+  const int N = desc->npaths;
+  int launches = 0;
+  CK(cudaEventRecord(ctx->ev0, s));
+  CK(cudaMemsetAsync(ctx->errf.p, 0, sizeof(unsigned), s));
+  CK(cudaMemsetAsync(ctx->stats.p, 0, 8 * sizeof(unsigned long long), s));
+  const bool need_ipsi = !(mode == PDDS_MODE_REPLAY_FP64 && desc->ipsi_override);
+  if (need_ipsi && !ctx->tables_ready) {
+    int max_n = 0;
+    for (auto& sh : L.shapes) max_n = std::max(max_n, sh.n);
+    CK(launch_rbf_setup(ctx->dl, max_n, ctx->max_nbins, ctx->ipsi.p, ctx->tab.p, ctx->errf.p, s));
+    launches += 2;
+    ctx->tables_ready = true;
+  }
+  CK(cudaEventRecord(ctx->ev1, s));
+  CK(cudaMemsetAsync(ctx->G.p, 0, std::max<int64_t>(nnz, 1) * sizeof(double), s));
+  CK(cudaMemsetAsync(ctx->GG.p, 0, std::max<int64_t>(nnz, 1) * sizeof(double), s));
+  CK(cudaMemsetAsync(ctx->Bsum.p, 0, L.K * sizeof(double), s));
+  CK(cudaMemsetAsync(ctx->BBsum.p, 0, L.K * sizeof(double), s));
+  CK(launch_boundary_b(ctx->dl, P, mode, ctx->bnd_knots.p, ctx->n_bnd, ctx->B.p, ctx->BB.p, s));
+  launches += ctx->n_bnd > 0;
+  const int n_mc = ctx->n_mc;
+  if (mode == PDDS_MODE_REPLAY_FP64) {
+    const int64_t total = (int64_t)n_mc * N;
+    CK(ctx->rx.resize(std::max<int64_t>(total, 1)));
+    CK(ctx->ry.resize(std::max<int64_t>(total, 1)));
+    CK(ctx->rY.resize(std::max<int64_t>(total, 1)));
+    CK(ctx->rZ.resize(std::max<int64_t>(total, 1)));
+    CK(ctx->rxi.resize(std::max<int64_t>(total, 1)));
+    CK(ctx->rside.resize(std::max<int64_t>(total, 1)));
+    CK(ctx->rsl.resize(std::max<int64_t>(total, 1)));
+    CK(ctx->rss.resize(std::max<int64_t>(total, 1)));
+    // (knot, side, side knot) tasks in hand-out order
+    std::vector<int> tm, td, ti;
+    std::vector<int64_t> tout, ktoff(std::max(n_mc, 1), 0), kipoff(4 * std::max(n_mc, 1), -1);
+    std::vector<int> mc;
+    for (int v : L.order) if (!L.knot_boundary[v]) mc.push_back(v);
+    int64_t ipo = 0;
+    for (int m = 0; m < n_mc; m++) {
+      const StencilRec& st = L.stencils[L.knot_stencil[mc[m]]];
+      ktoff[m] = (int64_t)tm.size();
+      for (int d = 0; d < 4; d++) {
+        if (st.side[d] < 0) continue;
+        const int n = L.sides[st.side[d]].n;
+        kipoff[4 * m + d] = ipo;
+        ipo += (int64_t)n * n;
+        for (int i = 0; i < n; i++) {
+          tm.push_back(m); td.push_back(d); ti.push_back(i);
+          tout.push_back((int64_t)tout.size());
+        }
+      }
+    }
+    if (desc->ipsi_override && desc->ipsi_override_len != ipo)
+      return fail(ctx, PDDS_ERR_INVALID, "ipsi_override_len does not match the layout (expected " +
+                                             std::to_string(ipo) + ")");
+    CK(ctx->task_m.upload(tm, s));
+    CK(ctx->task_d.upload(td, s));
+    CK(ctx->task_i.upload(ti, s));
+    CK(ctx->task_out.upload(tout, s));
+    CK(ctx->knot_task_off.upload(ktoff, s));
+    CK(ctx->Gside.resize(std::max<size_t>(tm.size(), 1)));
+    CK(ctx->GGside.resize(std::max<size_t>(tm.size(), 1)));
+    if (desc->ipsi_override) {
+      CK(ctx->knot_ipsi_off.upload(kipoff, s));
+      CK(ctx->ipsi_knot.resize(std::max<int64_t>(ipo, 1)));
+      CK(cudaMemcpyAsync(ctx->ipsi_knot.p, desc->ipsi_override, ipo * sizeof(double),
+                         cudaMemcpyHostToDevice, s));
+    }
+    ReplayArgs a;
+    a.L = ctx->dl;
+    a.P = P;
+    a.N = N;
+    a.h = desc->h;
+    a.sqrth = std::sqrt(desc->h);
+    a.seed = desc->seed;
+    a.instance = desc->instance;
+    a.sublinear = 1;
+    a.max_steps = max_steps;
+    a.mc_knots = ctx->mc_knots.p;
+    a.n_mc = n_mc;
+    a.knot_ipsi_off = desc->ipsi_override ? ctx->knot_ipsi_off.p : nullptr;
+    a.ipsi_knot = desc->ipsi_override ? ctx->ipsi_knot.p : nullptr;
+    a.ex = ctx->rx.p; a.ey = ctx->ry.p; a.eY = ctx->rY.p; a.eZ = ctx->rZ.p; a.exi = ctx->rxi.p;
+    a.eside = ctx->rside.p; a.esteps_l = ctx->rsl.p; a.esteps_s = ctx->rss.p;
+    a.G = ctx->G.p;
+    a.GG = ctx->GG.p;
+    a.B = ctx->B.p;
+    a.BB = ctx->BB.p;
+    a.dup_sum = desc->dup_sum;
+    a.err_flags = ctx->errf.p;
+    CK(launch_replay_paths(a, P.kind, s));
+    CK(launch_replay_reduce(a, P.kind, ctx->task_m.p, ctx->task_d.p, ctx->task_i.p, (int)tm.size(),
+                            ctx->task_out.p, ctx->knot_task_off.p, ctx->Gside.p, ctx->GGside.p, s));
+    launches += 4;
+    if (info) {
+      // step counts from the exit records
+      std::vector<int> sl(total), ss(total), sd(total);
+      CK(cudaMemcpyAsync(sl.data(), ctx->rsl.p, total * sizeof(int), cudaMemcpyDeviceToHost, s));
+      CK(cudaMemcpyAsync(sd.data(), ctx->rside.p, total * sizeof(int), cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      int64_t steps = 0, ng = 0, nsn = 0;
+      for (int64_t q = 0; q < total; q++) {
+        steps += sl[q];
+        if (sd[q] == -1) ng++;
+        else if (sd[q] >= 0) nsn++;
+      }
+      info->path_steps = steps;
+      info->exits_global = ng;
+      info->exits_stencil = nsn;
+    }
+  } else {
+    const int target = 4 * std::max(ctx->num_sms, 1) * 4;
+    int chunks = std::max(1, (target + std::max(n_mc, 1) - 1) / std::max(n_mc, 1));
+    chunks = std::min(chunks, std::max(1, N / 256));
+    const int ppc = (N + chunks - 1) / chunks;
+    chunks = (N + ppc - 1) / ppc;
+    const int n_items = n_mc * chunks;
+    CK(cudaMemsetAsync(ctx->counter.p, 0, sizeof(int), s));
+    if (mode == PDDS_MODE_MIXED) {
+      MixedArgs a;
+      a.L = ctx->dl;
+      a.P = P;
+      a.N = N;
+      a.h = (float)desc->h;
+      a.sqrth = (float)std::sqrt(desc->h);
+      a.inv_N = 1.0 / N;
+      a.seed = desc->seed;
+      a.instance = desc->instance;
+      a.chunks = chunks;
+      a.paths_per_chunk = ppc;
+      a.n_items = n_items;
+      a.want_var = desc->want_var ? 1 : 0;
+      a.dup_sum = desc->dup_sum;
+      a.max_steps = max_steps;
+      a.mc_knots = ctx->mc_knots.p;
+      a.item_counter = ctx->counter.p;
+      a.G = ctx->G.p;
+      a.GG = ctx->GG.p;
+      a.Bsum = ctx->Bsum.p;
+      a.BBsum = ctx->BBsum.p;
+      a.stats = ctx->stats.p;
+      a.err_flags = ctx->errf.p;
+      const size_t smem = ctx->mixed_smem * (a.want_var ? 2 : 1);
+      if (smem > 200 * 1024) return fail(ctx, PDDS_ERR_INVALID, "exit histograms exceed shared memory; lower bins_per_gap");
+      int bps = mixed_blocks_per_sm(P.kind, smem);
+      if (bps < 1) bps = 1;
+      const int grid = std::max(1, std::min(n_items, bps * ctx->num_sms));
+      if (n_items > 0) {
+        CK(launch_paths_mixed(a, P.kind, grid, smem, s));
+        launches++;
+      }
+    } else {
+      Fp64Args a;
+      a.L = ctx->dl;
+      a.P = P;
+      a.N = N;
+      a.h = desc->h;
+      a.sqrth = std::sqrt(desc->h);
+      a.inv_N = 1.0 / N;
+      a.seed = desc->seed;
+      a.instance = desc->instance;
+      a.chunks = chunks;
+      a.paths_per_chunk = ppc;
+      a.n_items = n_items;
+      a.dup_sum = desc->dup_sum;
+      a.max_steps = max_steps;
+      a.mc_knots = ctx->mc_knots.p;
+      a.item_counter = ctx->counter.p;
+      a.G = ctx->G.p;
+      a.Bsum = ctx->Bsum.p;
+      a.BBsum = ctx->BBsum.p;
+      a.stats = ctx->stats.p;
+      a.err_flags = ctx->errf.p;
+      const size_t smem = ctx->fp64_smem;
+      cudaFuncAttributes fa;
+      (void)fa;
+      int bps = fp64_blocks_per_sm(P.kind, smem);
+      if (bps < 1) bps = 1;
+      const int grid = std::max(1, std::min(n_items, bps * ctx->num_sms));
+      if (n_items > 0) {
+        CK(launch_paths_fp64(a, P.kind, grid, smem, s));
+        launches++;
+      }
+    }
+    CK(launch_finalize(ctx->mc_knots.p, n_mc, N, ctx->Bsum.p, ctx->BBsum.p, ctx->B.p, ctx->BB.p,
+                       ctx->row_ptr.p, nnz, ctx->G.p, ctx->GG.p,
+                       (mode == PDDS_MODE_MIXED && desc->want_var) ? 1 : 0, s));
+    launches += 1 + ((mode == PDDS_MODE_MIXED && desc->want_var) ? 1 : 0);
+  }
+  CK(cudaEventRecord(ctx->ev2, s));
+  if (val && nnz) CK(cudaMemcpyAsync(val, ctx->G.p, nnz * sizeof(double), cudaMemcpyDeviceToHost, s));
+  if (var && nnz) {
+    if (mode == PDDS_MODE_FP64) std::fill(var, var + nnz, 0.0);
+    else CK(cudaMemcpyAsync(var, ctx->GG.p, nnz * sizeof(double), cudaMemcpyDeviceToHost, s));
+  }
+  if (Bout) CK(cudaMemcpyAsync(Bout, ctx->B.p, L.K * sizeof(double), cudaMemcpyDeviceToHost, s));
+  if (BBout) CK(cudaMemcpyAsync(BBout, ctx->BB.p, L.K * sizeof(double), cudaMemcpyDeviceToHost, s));
+  unsigned long long st[8] = {0};
+  CK(cudaMemcpyAsync(st, ctx->stats.p, sizeof(st), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  ctx->has_estimate = true;
+  if (info) {
+    float ms_setup = 0.f, ms_paths = 0.f;
+    cudaEventElapsedTime(&ms_setup, ctx->ev0, ctx->ev1);
+    cudaEventElapsedTime(&ms_paths, ctx->ev1, ctx->ev2);
+    info->ms_setup = ms_setup;
+    info->ms_paths = ms_paths;
+    info->kernel_launches = launches;
+    info->paths = (int64_t)n_mc * N;
+    if (mode != PDDS_MODE_REPLAY_FP64) {
+      info->path_steps = (int64_t)st[0];
+      info->exits_global = (int64_t)st[2];
+      info->exits_stencil = (int64_t)st[3];
+    }
+  }
+  return check_err_flags(ctx);
+}
+
+pdds_status pdds_solve_interface(pdds_ctx* ctx, const pdds_solve_desc* desc, double* u,
+                                 pdds_solve_info* info) {
+  if (!ctx || !desc) return PDDS_ERR_INVALID;
+  if (!ctx->has_estimate) return fail(ctx, PDDS_ERR_INVALID, "no estimate to solve");
+  CK(cudaSetDevice(ctx->device));
+  cudaStream_t s = ctx->stream;
+  const HostLayout& L = ctx->L;
+  const int K = L.K;
+  const int64_t nnz = L.row_ptr[K];
+  const int m = std::max(2, std::min(desc->restart > 0 ? desc->restart : 30, 40));
+  CK(ctx->sv64.resize((size_t)6 * K));
+  CK(ctx->sscal.resize(64));
+  CK(ctx->spart.resize(64 * 256 + 1024));
+  CK(ctx->shess.resize((size_t)(m + 1) * m + 2 * m + 3 * (m + 1) + 16));
+  CK(ctx->su.resize(std::max(K, 1)));
+  SolveCsr A{K, nnz, ctx->row_ptr.p, ctx->col.p, ctx->G.p};
+  SolveWork w;
+  for (int q = 0; q < 6; q++) w.v64[q] = ctx->sv64.p + (size_t)q * K;
+  w.scal = ctx->sscal.p;
+  w.part = ctx->spart.p;
+  w.hess = ctx->shess.p;
+  w.host_rr = ctx->host_rr;
+  int iters = 0, refines = 0;
+  double relres = 0.0;
+  const double tol = desc->tol > 0 ? desc->tol : 1e-10;
+  CK(cudaEventRecord(ctx->ev0, s));
+  if (desc->method == PDDS_SOLVE_BICGSTAB_FP64) {
+    const int maxit = desc->max_iter > 0 ? desc->max_iter : 2 * K;
+    CK(solve_bicgstab(A, ctx->B.p, ctx->su.p, w, maxit, tol, &iters, &relres, s));
+  } else if (desc->method == PDDS_SOLVE_GMRES_FP32_IR) {
+    CK(ctx->sV32.resize((size_t)(m + 1) * K));
+    CK(ctx->sw32.resize(std::max(K, 1)));
+    CK(ctx->sval32.resize(std::max<int64_t>(nnz, 1)));
+    w.V32 = ctx->sV32.p;
+    w.w32 = ctx->sw32.p;
+    w.val32 = ctx->sval32.p;
+    const int maxit = desc->max_iter > 0 ? desc->max_iter : 1000;
+    const int maxref = desc->max_refine > 0 ? desc->max_refine : 30;
+    CK(solve_gmres_ir(A, ctx->B.p, ctx->su.p, w, m, maxit, maxref, tol, &iters, &refines, &relres, s));
+  } else {
+    return fail(ctx, PDDS_ERR_INVALID, "unknown solve method");
+  }
+  CK(cudaEventRecord(ctx->ev1, s));
+  if (u) CK(cudaMemcpyAsync(u, ctx->su.p, K * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (info) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    info->iterations = iters;
+    info->refinements = refines;
+    info->rel_residual = relres;
+    info->ms = ms;
+    info->kernel_launches = w.launches;
+  }
+  if (!(relres <= tol * 1.0000001) && !(relres == 0.0))
+    return fail(ctx, PDDS_ERR_NOT_CONVERGED, "interface solve reached " + std::to_string(relres));
+  return PDDS_OK;
+}
+
+}  // extern "C"

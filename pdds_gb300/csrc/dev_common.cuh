@@ -1,0 +1,278 @@
+// Device-side view of the layout, problem functors and the rectangle exit
+// geometry shared by the path kernels.
+//
+// Problems replace the reference's host function pointers (struct bvp,
+// BVPs/BVP.hpp:89-137) and its __device__ function-pointer table (bvpdev,
+// BVPs/BVP.cuh:44-77) by compiled functors selected with a template argument.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pdds_portable.h"
+
+namespace pdds {
+
+struct DevLayout {
+  int K, S, D, P;
+  double dom[4];  // domain rectangle {SW.x, SW.y, NE.x, NE.y}
+  // knots
+  const double* kx;
+  const double* ky;
+  const int* knot_stencil;
+  const int64_t* row_ptr;
+  // stencils
+  const double* st_rect;     // [S][4]
+  const int* st_side;        // [S][4] side id per N,S,E,W or -1
+  const int* st_glob;        // [S][4]
+  const int64_t* st_map_off; // [S]
+  const int* map_pos;
+  const unsigned char* map_owner;
+  // sides
+  const int* sd_n;
+  const int* sd_orient;
+  const int* sd_shape;
+  const double* sd_c;
+  const double* sd_origin;
+  const int64_t* sd_knot_off;
+  const int* side_knot;
+  const double* side_px;
+  const double* side_py;
+  // shapes
+  const int* sh_n;
+  const double* sh_c;
+  const double* sh_lo;
+  const double* sh_delta;
+  const int* sh_nbins;
+  const int64_t* sh_tab_off;
+  const int64_t* sh_ipsi_off;
+  const int64_t* sh_t_off;
+  const double* sh_t;
+  const float* tab;
+  const double* ipsi;
+};
+
+struct ProblemDev {
+  int kind;
+  int use_cv;
+  double p[8];
+};
+
+enum { PK_POISSON_SINCOS = 0, PK_MONEGROS = 1, PK_HELMHOLTZ = 2, PK_VARCOEF = 3 };
+
+template <typename T>
+struct Coef {
+  T s00, s01, s10, s11;  // sigma, row-major
+  T b0, b1;              // drift
+  T c;                   // reaction
+  T f;                   // source
+  T g0, g1;              // gradient of u (control variate)
+};
+
+// ------------------------------------------------------------------ FP32
+// Fast-intrinsic single precision (MIXED mode paths).
+template <int KIND>
+__device__ __forceinline__ void coef_f32(const ProblemDev& P, float x, float y, Coef<float>& k) {
+  const float PI = 3.14159265358979f;
+  if (KIND == PK_POISSON_SINCOS) {
+    float sx, cx, sy, cy;
+    __sincosf(PI * x, &sx, &cx);
+    __sincosf(PI * y, &sy, &cy);
+    k.s00 = 1.41421356f; k.s01 = 0.f; k.s10 = 0.f; k.s11 = 1.41421356f;
+    k.b0 = 0.f; k.b1 = 0.f; k.c = 0.f;
+    k.f = 19.7392088f * (sx * cy);
+    k.g0 = PI * (cx * cy) + y;
+    k.g1 = x - PI * (sx * sy);
+  } else if (KIND == PK_HELMHOLTZ) {
+    const float a = (float)P.p[0], b = (float)P.p[1], c = (float)P.p[2];
+    float sa, ca, sb, cb;
+    __sincosf(a * x, &sa, &ca);
+    __sincosf(b * y, &sb, &cb);
+    k.s00 = 1.41421356f; k.s01 = 0.f; k.s10 = 0.f; k.s11 = 1.41421356f;
+    k.b0 = 0.f; k.b1 = 0.f; k.c = c;
+    k.f = ((a * a + b * b) - c) * (sa * cb);
+    k.g0 = a * (ca * cb);
+    k.g1 = -(b * (sa * sb));
+  } else if (KIND == PK_VARCOEF) {
+    const float s1 = 1.f + 0.5f * (x * x), s2 = 1.f + 0.5f * (y * y);
+    float sn, cs;
+    __sincosf(2.f * y, &sn, &cs);
+    const float ex = __expf(x);
+    const float ux = ex * cs, uy = -2.f * (ex * sn), uxx = ux, uyy = -4.f * ux;
+    const float c = -(1.f + x * x + y * y);
+    k.s00 = s1; k.s01 = 0.f; k.s10 = 0.f; k.s11 = s2;
+    k.b0 = y; k.b1 = -x; k.c = c;
+    k.f = -(0.5f * (s1 * s1 * uxx + s2 * s2 * uyy) + (y * ux - x * uy) + c * (ux + 1.f));
+    k.g0 = ux;
+    k.g1 = uy;
+  } else {  // PK_MONEGROS (BVPs/EDPs/Monegros_Poisson_CPP.hpp)
+    const float k2 = 0.01f, k3 = 0.02f, k4 = 0.12f, k5 = 0.05f, k6 = 0.05f, k7 = -0.12f, sf = 0.333f;
+    const float q = 1.f + k2 * x * x + k3 * y * y;
+    const float a1 = sqrtf(q);
+    float s1, c1, sA, cA, sB, cB;
+    __sincosf(a1, &s1, &c1);
+    __sincosf(k4 * x + k5 * y, &sA, &cA);
+    __sincosf(k6 * x + k7 * y, &sB, &cB);
+    const float a2 = tanhf(sA + sB);
+    const float m = a2 * a2 - 1.f;
+    const float p4 = k4 * cA + k6 * cB, p5 = k5 * cA + k7 * cB;
+    const float dxx = ((k2 / a1) - (k2 * k2 * x * x / (a1 * a1 * a1))) * c1 - (x * x * k2 * k2 / (a1 * a1)) * s1 +
+                      2.f * p4 * p4 * m * a2 + (k4 * k4 * sA + k6 * k6 * sB) * m;
+    const float dyy = ((k3 / a1) - (k3 * k3 * y * y / (a1 * a1 * a1))) * c1 - (y * y * k3 * k3 / (a1 * a1)) * s1 +
+                      2.f * p5 * p5 * m * a2 + (k5 * k5 * sA + k7 * k7 * sB) * m;
+    k.s00 = 1.41421356237f; k.s01 = 0.f; k.s10 = 0.f; k.s11 = 1.41421356237f;
+    k.b0 = 0.f; k.b1 = 0.f; k.c = 0.f;
+    k.f = -sf * dxx - sf * dyy;
+    k.g0 = sf * (c1 * k2 * x / a1 - p4 * m);
+    k.g1 = sf * (c1 * k3 * y / a1 - p5 * m);
+  }
+  if (!P.use_cv) { k.g0 = 0.f; k.g1 = 0.f; }
+}
+
+template <int KIND>
+__device__ __forceinline__ float u_f32(const ProblemDev& P, float x, float y) {
+  if (KIND == PK_POISSON_SINCOS) {
+    float sx, cx, sy, cy;
+    __sincosf(3.14159265358979f * x, &sx, &cx);
+    __sincosf(3.14159265358979f * y, &sy, &cy);
+    return sx * cy + x * y;
+  } else if (KIND == PK_HELMHOLTZ) {
+    return __sinf((float)P.p[0] * x) * __cosf((float)P.p[1] * y);
+  } else if (KIND == PK_VARCOEF) {
+    return __expf(x) * __cosf(2.f * y) + 1.f;
+  } else {
+    const float q = 1.f + 0.01f * x * x + 0.02f * y * y;
+    return 3.f + 0.333f * (__sinf(sqrtf(q)) + tanhf(__sinf(0.12f * x + 0.05f * y) + __sinf(0.05f * x - 0.12f * y)));
+  }
+}
+
+// ------------------------------------------------------------------ FP64
+// Plain double precision with the CUDA math library (FP64 mode).
+template <int KIND>
+__device__ __forceinline__ void coef_f64(const ProblemDev& P, double x, double y, Coef<double>& k) {
+  const double PI = 3.141592653589793;
+  if (KIND == PK_POISSON_SINCOS) {
+    double sx, cx, sy, cy;
+    sincospi(x, &sx, &cx);
+    sincospi(y, &sy, &cy);
+    k.s00 = 1.4142135623730951; k.s01 = 0.0; k.s10 = 0.0; k.s11 = 1.4142135623730951;
+    k.b0 = 0.0; k.b1 = 0.0; k.c = 0.0;
+    k.f = 19.739208802178716 * (sx * cy);
+    k.g0 = PI * (cx * cy) + y;
+    k.g1 = x - PI * (sx * sy);
+  } else if (KIND == PK_HELMHOLTZ) {
+    const double a = P.p[0], b = P.p[1], c = P.p[2];
+    double sa, ca, sb, cb;
+    sincos(a * x, &sa, &ca);
+    sincos(b * y, &sb, &cb);
+    k.s00 = 1.4142135623730951; k.s01 = 0.0; k.s10 = 0.0; k.s11 = 1.4142135623730951;
+    k.b0 = 0.0; k.b1 = 0.0; k.c = c;
+    k.f = ((a * a + b * b) - c) * (sa * cb);
+    k.g0 = a * (ca * cb);
+    k.g1 = -(b * (sa * sb));
+  } else if (KIND == PK_VARCOEF) {
+    const double s1 = 1.0 + 0.5 * (x * x), s2 = 1.0 + 0.5 * (y * y);
+    double sn, cs;
+    sincos(2.0 * y, &sn, &cs);
+    const double ex = ::exp(x);
+    const double ux = ex * cs, uy = -2.0 * (ex * sn), uxx = ux, uyy = -4.0 * ux;
+    const double c = -(1.0 + x * x + y * y);
+    k.s00 = s1; k.s01 = 0.0; k.s10 = 0.0; k.s11 = s2;
+    k.b0 = y; k.b1 = -x; k.c = c;
+    k.f = -(0.5 * (s1 * s1 * uxx + s2 * s2 * uyy) + (y * ux - x * uy) + c * (ux + 1.0));
+    k.g0 = ux;
+    k.g1 = uy;
+  } else {
+    const double k2 = 0.01, k3 = 0.02, k4 = 0.12, k5 = 0.05, k6 = 0.05, k7 = -0.12, sf = 0.333;
+    const double q = 1.0 + k2 * x * x + k3 * y * y;
+    const double a1 = ::sqrt(q);
+    double s1, c1, sA, cA, sB, cB;
+    sincos(a1, &s1, &c1);
+    sincos(k4 * x + k5 * y, &sA, &cA);
+    sincos(k6 * x + k7 * y, &sB, &cB);
+    const double a2 = ::tanh(sA + sB);
+    const double m = a2 * a2 - 1.0;
+    const double p4 = k4 * cA + k6 * cB, p5 = k5 * cA + k7 * cB;
+    const double dxx = ((k2 / a1) - (k2 * k2 * x * x / (a1 * a1 * a1))) * c1 - (x * x * k2 * k2 / (a1 * a1)) * s1 +
+                       2.0 * p4 * p4 * m * a2 + (k4 * k4 * sA + k6 * k6 * sB) * m;
+    const double dyy = ((k3 / a1) - (k3 * k3 * y * y / (a1 * a1 * a1))) * c1 - (y * y * k3 * k3 / (a1 * a1)) * s1 +
+                       2.0 * p5 * p5 * m * a2 + (k5 * k5 * sA + k7 * k7 * sB) * m;
+    k.s00 = 1.41421356237; k.s01 = 0.0; k.s10 = 0.0; k.s11 = 1.41421356237;
+    k.b0 = 0.0; k.b1 = 0.0; k.c = 0.0;
+    k.f = -sf * dxx - sf * dyy;
+    k.g0 = sf * (c1 * k2 * x / a1 - p4 * m);
+    k.g1 = sf * (c1 * k3 * y / a1 - p5 * m);
+  }
+  if (!P.use_cv) { k.g0 = 0.0; k.g1 = 0.0; }
+}
+
+template <int KIND>
+__device__ __forceinline__ double u_f64(const ProblemDev& P, double x, double y) {
+  if (KIND == PK_POISSON_SINCOS) {
+    double sx, cx, sy, cy;
+    sincospi(x, &sx, &cx);
+    sincospi(y, &sy, &cy);
+    return sx * cy + x * y;
+  } else if (KIND == PK_HELMHOLTZ) {
+    return ::sin(P.p[0] * x) * ::cos(P.p[1] * y);
+  } else if (KIND == PK_VARCOEF) {
+    return ::exp(x) * ::cos(2.0 * y) + 1.0;
+  } else {
+    const double q = 1.0 + 0.01 * x * x + 0.02 * y * y;
+    return 3.0 + 0.333 * (::sin(::sqrt(q)) + ::tanh(::sin(0.12 * x + 0.05 * y) + ::sin(0.05 * x - 0.12 * y)));
+  }
+}
+
+// ------------------------------------------------------------------ rectangle
+// Rectangle2D (BVPs/Domains/rectangle.hpp:7-229) with the same branch table:
+// signed distance (negative inside), projection E onto the nearest side and
+// the outward normal N.  `onmask` reports the sides E lies on (bit d for
+// Dir d) so the exit side can be taken without comparing coordinates.
+template <typename T>
+__device__ __forceinline__ T rect2d(const T* p, T x, T y, T& Ex, T& Ey, T& Nx, T& Ny, int& onmask) {
+  const T c0 = T(0.5) * (p[0] + p[2]), c1 = T(0.5) * (p[1] + p[3]);
+  const T h0 = p[2] - c0, h1 = p[3] - c1;
+  const T d0 = fabs(x - c0), d1 = fabs(y - c1);
+  const bool right = x > c0, top = y > c1;
+  const T ex = right ? (h0 + c0) : (-h0 + c0);
+  const T ey = top ? (h1 + c1) : (-h1 + c1);
+  const T nx = right ? T(1) : T(-1), ny = top ? T(1) : T(-1);
+  const int xside = right ? (1 << 2) : (1 << 3);   // E : W
+  const int yside = top ? (1 << 0) : (1 << 1);     // N : S
+  Ex = x; Ey = y;
+  if (d0 <= h0 && d1 <= h1) {
+    if (d0 - h0 > d1 - h1) { Ex = ex; Nx = nx; Ny = T(0); onmask = xside; return d0 - h0; }
+    Ey = ey; Nx = T(0); Ny = ny; onmask = yside; return d1 - h1;
+  }
+  if (d0 > h0) {
+    if (d1 > h1) {
+      const T diag = T(0.70710678118f);
+      Ex = ex; Ey = ey; Nx = right ? diag : -diag; Ny = top ? diag : -diag;
+      onmask = xside | yside;
+      return sqrt((d0 - h0) * (d0 - h0) + (d1 - h1) * (d1 - h1));
+    }
+    Ex = ex; Nx = nx; Ny = T(0); onmask = xside;
+    return d0 - h0;
+  }
+  Ey = ey; Nx = T(0); Ny = ny; onmask = yside;
+  return d1 - h1;
+}
+
+// Exit side by the reference's priority S, N, W, E (G_update, stencil.cpp:246-301).
+__device__ __forceinline__ int exit_side(int onmask) {
+  if (onmask & (1 << 1)) return 1;  // S
+  if (onmask & (1 << 0)) return 0;  // N
+  if (onmask & (1 << 3)) return 3;  // W
+  if (onmask & (1 << 2)) return 2;  // E
+  return -1;
+}
+
+// Cubic Lagrange weights for nodes -1, 0, 1, 2 at offset u in [0, 1).
+__device__ __forceinline__ void cubic_weights(float u, float& w0, float& w1, float& w2, float& w3) {
+  const float um1 = u - 1.f, um2 = u - 2.f, up1 = u + 1.f;
+  w0 = -u * um1 * um2 * (1.f / 6.f);
+  w1 = up1 * um1 * um2 * 0.5f;
+  w2 = -up1 * u * um2 * 0.5f;
+  w3 = up1 * u * um1 * (1.f / 6.f);
+}
+
+}  // namespace pdds

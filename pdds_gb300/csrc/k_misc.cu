@@ -1,0 +1,85 @@
+// Boundary knots and the per-knot finalisation of B, BB and G_var.
+//   Solve_OMP_Analytic boundary shortcut  Solvers/EMFKACSolver.hpp:720-727 (B = g, BB = B^2)
+//   B = b/N, BB = bb/N                     Solvers/EMFKACSolver.hpp:570-571
+//   var_G = GG/N - (G/N)^2                 Meshes/stencil.cpp:403
+#include "kernels.h"
+
+namespace pdds {
+
+namespace {
+
+template <int KIND>
+__device__ double g_port(const ProblemDev& P, double x, double y) {
+  if (KIND == PK_POISSON_SINCOS) {
+    double sx, cx, sy, cy;
+    pm::sincos(pm::PI * x, &sx, &cx);
+    pm::sincos(pm::PI * y, &sy, &cy);
+    return sx * cy + x * y;
+  } else if (KIND == PK_HELMHOLTZ) {
+    double sa, ca, sb, cb;
+    pm::sincos(P.p[0] * x, &sa, &ca);
+    pm::sincos(P.p[1] * y, &sb, &cb);
+    return sa * cb;
+  } else if (KIND == PK_VARCOEF) {
+    double s2, c2;
+    pm::sincos(2.0 * y, &s2, &c2);
+    return pm::exp(x) * c2 + 1.0;
+  }
+  return u_f64<PK_MONEGROS>(P, x, y);
+}
+
+template <int KIND>
+__global__ void k_boundary(const DevLayout L, const ProblemDev P, int portable, const int* knots,
+                           int n, double* B, double* BB) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int k = knots[t];
+  const double x = L.kx[k], y = L.ky[k];
+  const double g = portable ? g_port<KIND>(P, x, y) : u_f64<KIND>(P, x, y);
+  B[k] = g;
+  BB[k] = g * g;
+}
+
+__global__ void k_finalize_b(const int* mc, int n, int N, const double* Bsum, const double* BBsum,
+                             double* B, double* BB) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int k = mc[t];
+  B[k] = Bsum[k] / N;
+  BB[k] = BBsum[k] / N;
+}
+
+__global__ void k_finalize_var(int64_t nnz, const double* G, double* GG) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nnz) return;
+  GG[e] = GG[e] - G[e] * G[e];
+}
+
+}  // namespace
+
+cudaError_t launch_boundary_b(const DevLayout& L, const ProblemDev& P, int mode, const int* knots,
+                              int n, double* B, double* BB, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  const int portable = (mode == 0 && P.kind != PK_MONEGROS) ? 1 : 0;
+  const int g = (n + 127) / 128;
+  switch (P.kind) {
+    case PK_POISSON_SINCOS: k_boundary<PK_POISSON_SINCOS><<<g, 128, 0, s>>>(L, P, portable, knots, n, B, BB); break;
+    case PK_MONEGROS: k_boundary<PK_MONEGROS><<<g, 128, 0, s>>>(L, P, 0, knots, n, B, BB); break;
+    case PK_HELMHOLTZ: k_boundary<PK_HELMHOLTZ><<<g, 128, 0, s>>>(L, P, portable, knots, n, B, BB); break;
+    default: k_boundary<PK_VARCOEF><<<g, 128, 0, s>>>(L, P, portable, knots, n, B, BB); break;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_finalize(const int* mc_knots, int n_mc, int N, const double* Bsum,
+                            const double* BBsum, double* B, double* BB, const int64_t* row_ptr,
+                            int64_t nnz, const double* G, double* GG_to_var, int want_var,
+                            cudaStream_t s) {
+  (void)row_ptr;
+  if (n_mc > 0) k_finalize_b<<<(n_mc + 127) / 128, 128, 0, s>>>(mc_knots, n_mc, N, Bsum, BBsum, B, BB);
+  if (want_var && nnz > 0)
+    k_finalize_var<<<(unsigned)((nnz + 255) / 256), 256, 0, s>>>(nnz, G, GG_to_var);
+  return cudaGetLastError();
+}
+
+}  // namespace pdds

@@ -1,0 +1,154 @@
+// FP64 factorisation of the Gaussian RBF interpolation matrices and the
+// cardinal-function tables used by the MIXED kernel.
+//
+// The reference inverts Psi_ij = exp(-|p_i - p_j|^2 / c^2) for every side of
+// every knot with Eigen's FullPivLU (Meshes/stencil.cpp:115-184, 211-243).
+// Here one CTA inverts one side shape (sides that are translates of each
+// other share Psi) by Gauss-Jordan elimination with partial pivoting in
+// shared memory, in FP64: cond(Psi) reaches 1e9..1e11, so the inverse needs
+// double precision.  The tables H[b][i] = sum_j Psi^-1(j,i) exp(-(t_j - s_b)^2/c^2)
+// on the exit-bin grid s_b are accumulated in FP64 and stored in FP32: the
+// cardinal functions are bounded by ~1, so storing them in FP32 costs 6e-8
+// relative and no amplification.
+#include "kernels.h"
+
+namespace pdds {
+
+namespace {
+
+constexpr int RBF_THREADS = 256;
+
+__global__ void __launch_bounds__(RBF_THREADS) k_invert(const DevLayout L, double* ipsi_out,
+                                                        unsigned* err_flags) {
+  extern __shared__ double A[];  // n x n, row-major, then column k of the current step
+  __shared__ int s_piv;
+  __shared__ double s_val[RBF_THREADS];
+  __shared__ int s_idx[RBF_THREADS];
+  __shared__ int perm[512];
+  const int sh = blockIdx.x, tid = threadIdx.x;
+  const int n = L.sh_n[sh];
+  const double c = L.sh_c[sh];
+  const double* t = L.sh_t + L.sh_t_off[sh];
+  const double ic2 = 1.0 / (c * c);
+  double* fcol = A + n * n;
+  for (int e = tid; e < n * n; e += RBF_THREADS) {
+    const int i = e / n, j = e % n;
+    const double d = t[i] - t[j];
+    A[e] = exp(-(d * d) * ic2);
+  }
+  __syncthreads();
+  for (int k = 0; k < n; k++) {
+    // pivot: largest |A[i][k]| for i >= k (lowest index on ties)
+    double best = -1.0;
+    int bi = k;
+    for (int i = k + tid; i < n; i += RBF_THREADS) {
+      const double v = fabs(A[i * n + k]);
+      if (v > best) { best = v; bi = i; }
+    }
+    s_val[tid] = best;
+    s_idx[tid] = bi;
+    __syncthreads();
+    for (int o = RBF_THREADS / 2; o > 0; o >>= 1) {
+      if (tid < o) {
+        const double v2 = s_val[tid + o];
+        const int i2 = s_idx[tid + o];
+        if (v2 > s_val[tid] || (v2 == s_val[tid] && i2 < s_idx[tid])) { s_val[tid] = v2; s_idx[tid] = i2; }
+      }
+      __syncthreads();
+    }
+    if (tid == 0) {
+      s_piv = s_idx[0];
+      perm[k] = s_idx[0];
+      if (!(s_val[0] > 1e-300)) atomicOr(err_flags, ERR_FLAG_SINGULAR);
+    }
+    __syncthreads();
+    const int p = s_piv;
+    if (p != k)
+      for (int j = tid; j < n; j += RBF_THREADS) {
+        const double tmp = A[k * n + j];
+        A[k * n + j] = A[p * n + j];
+        A[p * n + j] = tmp;
+      }
+    __syncthreads();
+    const double piv = A[k * n + k];
+    const double ipiv = 1.0 / piv;
+    __syncthreads();
+    for (int j = tid; j < n; j += RBF_THREADS) A[k * n + j] = (j == k) ? ipiv : A[k * n + j] * ipiv;
+    for (int i = tid; i < n; i += RBF_THREADS) fcol[i] = A[i * n + k];
+    __syncthreads();
+    for (int e = tid; e < n * n; e += RBF_THREADS) {
+      const int i = e / n, j = e % n;
+      if (i == k) continue;
+      const double f = fcol[i];
+      if (j == k) A[e] = -f * ipiv;
+      else A[e] = A[e] - f * A[k * n + j];
+    }
+    __syncthreads();
+  }
+  // undo the row exchanges as column exchanges, in reverse order
+  for (int k = n - 1; k >= 0; k--) {
+    const int p = perm[k];
+    if (p != k)
+      for (int i = tid; i < n; i += RBF_THREADS) {
+        const double tmp = A[i * n + k];
+        A[i * n + k] = A[i * n + p];
+        A[i * n + p] = tmp;
+      }
+    __syncthreads();
+  }
+  double* out = ipsi_out + L.sh_ipsi_off[sh];
+  for (int e = tid; e < n * n; e += RBF_THREADS) out[e] = A[e];
+}
+
+// H[b][i] for one shape and a tile of bins.
+constexpr int TAB_TILE = 16;
+__global__ void __launch_bounds__(RBF_THREADS) k_tables(const DevLayout L, const double* ipsi,
+                                                        float* tab) {
+  extern __shared__ double r[];  // [TAB_TILE][n]
+  const int sh = blockIdx.y, tid = threadIdx.x;
+  const int n = L.sh_n[sh], nb = L.sh_nbins[sh];
+  const int b0 = blockIdx.x * TAB_TILE;
+  if (b0 >= nb) return;
+  const int nt = min(TAB_TILE, nb - b0);
+  const double c = L.sh_c[sh], ic2 = 1.0 / (c * c);
+  const double* t = L.sh_t + L.sh_t_off[sh];
+  const double delta = L.sh_delta[sh];
+  const double s0 = L.sh_lo[sh] - delta;
+  for (int e = tid; e < nt * n; e += RBF_THREADS) {
+    const int q = e / n, j = e % n;
+    const double s = s0 + (double)(b0 + q) * delta;
+    const double d = t[j] - s;
+    r[e] = exp(-(d * d) * ic2);
+  }
+  __syncthreads();
+  const double* ip = ipsi + L.sh_ipsi_off[sh];
+  float* out = tab + L.sh_tab_off[sh];
+  for (int e = tid; e < nt * n; e += RBF_THREADS) {
+    const int q = e / n, i = e % n;
+    double acc = 0.0;
+    for (int j = 0; j < n; j++) acc += ip[(int64_t)j * n + i] * r[q * n + j];
+    out[(int64_t)(b0 + q) * n + i] = (float)acc;
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_rbf_setup(const DevLayout& L, int max_n, int max_nbins, double* ipsi, float* tab,
+                             unsigned* err_flags, cudaStream_t s) {
+  if (L.P == 0) return cudaSuccess;
+  if (max_n > 160) return cudaErrorInvalidValue;
+  const size_t smem = (size_t)(max_n * max_n + max_n) * sizeof(double);
+  cudaFuncSetAttribute(k_invert, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_invert<<<L.P, RBF_THREADS, smem, s>>>(L, ipsi, err_flags);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  if (tab) {
+    const size_t smem2 = (size_t)TAB_TILE * max_n * sizeof(double);
+    dim3 grid((max_nbins + TAB_TILE - 1) / TAB_TILE, L.P);
+    k_tables<<<grid, RBF_THREADS, smem2, s>>>(L, ipsi, tab);
+    e = cudaGetLastError();
+  }
+  return e;
+}
+
+}  // namespace pdds

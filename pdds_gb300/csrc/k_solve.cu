@@ -1,0 +1,407 @@
+// Interface solve (I + G) u = B on the device.
+//
+// The reference assembles the COO triplets into an Eigen SparseMatrix, adds
+// the identity and runs Jacobi-preconditioned BiCGSTAB in FP64 from a zero
+// guess (PDDAlgorithms/PDDSparseGM.cpp:3168-3246).  G is produced here
+// directly in CSR (rows sorted by column), and the diagonal of I + G is 1
+// (a knot never belongs to its own stencil sides), so the Jacobi
+// preconditioner is the identity.  Two methods:
+//   BiCGSTAB in FP64 (van der Vorst 1992), the reference's method;
+//   GMRES(m) in FP32 (Saad & Schultz 1986, classical Gram-Schmidt with one
+//   re-orthogonalisation pass) as the inner solver of FP64 iterative
+//   refinement: residuals are formed in FP64 and each refinement step restarts
+//   GMRES on the normalised residual.
+// Reductions are deterministic (fixed-shape two-stage sums).
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cmath>
+#include <vector>
+
+#include "solve.h"
+
+namespace pdds {
+
+namespace {
+
+constexpr int SPMV_THREADS = 256;
+constexpr int RED_THREADS = 256;
+constexpr int RED_BLOCKS = 256;
+constexpr int MDOT_THREADS = 128;
+
+template <typename T>
+__global__ void k_spmv(int K, const int64_t* __restrict__ rp, const int* __restrict__ col,
+                       const T* __restrict__ val, const T* __restrict__ x, T* __restrict__ y) {
+  const int lane = threadIdx.x & 31;
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  for (int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < K; row += warps) {
+    const int64_t e0 = rp[row], e1 = rp[row + 1];
+    T acc = T(0);
+    for (int64_t e = e0 + lane; e < e1; e += 32) acc += val[e] * x[col[e]];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) y[row] = x[row] + acc;
+  }
+}
+
+// Stage 1 of up to two dot products: per-block partial sums (FP64).
+template <typename T>
+__global__ void k_dot2_part(int n, const T* a, const T* b, const T* c, const T* d, double* part) {
+  __shared__ double s1[RED_THREADS], s2[RED_THREADS];
+  double p1 = 0.0, p2 = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    p1 += (double)a[i] * (double)b[i];
+    if (c) p2 += (double)c[i] * (double)d[i];
+  }
+  s1[threadIdx.x] = p1;
+  s2[threadIdx.x] = p2;
+  __syncthreads();
+  for (int o = RED_THREADS / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      s1[threadIdx.x] += s1[threadIdx.x + o];
+      s2[threadIdx.x] += s2[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = s1[0];
+    part[2 * blockIdx.x + 1] = s2[0];
+  }
+}
+
+__global__ void k_dot2_final(int nb, const double* part, double* out1, double* out2) {
+  __shared__ double s1[RED_THREADS], s2[RED_THREADS];
+  double p1 = 0.0, p2 = 0.0;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+    p1 += part[2 * i];
+    p2 += part[2 * i + 1];
+  }
+  s1[threadIdx.x] = p1;
+  s2[threadIdx.x] = p2;
+  __syncthreads();
+  for (int o = RED_THREADS / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      s1[threadIdx.x] += s1[threadIdx.x + o];
+      s2[threadIdx.x] += s2[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    *out1 = s1[0];
+    if (out2) *out2 = s2[0];
+  }
+}
+
+// BiCGSTAB scalars, in one device array.
+enum { S_RR = 0, S_RHO_NEW, S_RHO, S_ALPHA, S_W, S_BETA, S_R0V, S_TS, S_TT, S_COUNT };
+
+__global__ void k_bicg_scal1(double* sc) {  // after <r,r>, <r0,r>
+  const double rho_old = sc[S_RHO];
+  sc[S_RHO] = sc[S_RHO_NEW];
+  sc[S_BETA] = (sc[S_RHO] / rho_old) * (sc[S_ALPHA] / sc[S_W]);
+}
+__global__ void k_bicg_scal2(double* sc) { sc[S_ALPHA] = sc[S_RHO] / sc[S_R0V]; }
+__global__ void k_bicg_scal3(double* sc) { sc[S_W] = (sc[S_TT] > 0.0) ? sc[S_TS] / sc[S_TT] : 0.0; }
+
+__global__ void k_bicg_p(int n, const double* r, double* p, const double* v, const double* sc) {
+  const double beta = sc[S_BETA], w = sc[S_W];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    p[i] = r[i] + beta * (p[i] - w * v[i]);
+}
+__global__ void k_bicg_s(int n, const double* r, const double* v, double* s, const double* sc) {
+  const double alpha = sc[S_ALPHA];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    s[i] = r[i] - alpha * v[i];
+}
+__global__ void k_bicg_x(int n, double* x, const double* p, const double* s, double* r,
+                         const double* t, const double* sc) {
+  const double alpha = sc[S_ALPHA], w = sc[S_W];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    x[i] += alpha * p[i] + w * s[i];
+    r[i] = s[i] - w * t[i];
+  }
+}
+
+__global__ void k_fill(int n, double* a, double v) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) a[i] = v;
+}
+__global__ void k_copy(int n, const double* a, double* b) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) b[i] = a[i];
+}
+__global__ void k_init_scal(double* sc) {
+  sc[S_RHO] = 1.0; sc[S_ALPHA] = 1.0; sc[S_W] = 1.0;
+}
+
+// ---------------------------------------------------------------- GMRES
+__global__ void k_to_f32(int64_t n, const double* a, float* b) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+// r = b - A x in FP64 from y = A x
+__global__ void k_resid(int n, const double* b, const double* Ax, double* r) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) r[i] = b[i] - Ax[i];
+}
+__global__ void k_scale_to_f32(int n, const double* r, const double* nrm, float* v) {
+  const double inv = 1.0 / sqrt(*nrm);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v[i] = (float)(r[i] * inv);
+}
+// partial dots of w with V[0..j]: part[blk][i]
+__global__ void k_mdot_part(int n, int nv, const float* V, const float* w, double* part) {
+  extern __shared__ double sh[];  // [nv][MDOT_THREADS]
+  for (int i = 0; i < nv; i++) sh[i * MDOT_THREADS + threadIdx.x] = 0.0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const float wk = w[k];
+    for (int i = 0; i < nv; i++) sh[i * MDOT_THREADS + threadIdx.x] += (double)(V[(int64_t)i * n + k] * wk);
+  }
+  __syncthreads();
+  for (int o = MDOT_THREADS / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o)
+      for (int i = 0; i < nv; i++) sh[i * MDOT_THREADS + threadIdx.x] += sh[i * MDOT_THREADS + threadIdx.x + o];
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < nv; i += blockDim.x) part[(int64_t)blockIdx.x * nv + i] = sh[i * MDOT_THREADS];
+}
+__global__ void k_mdot_final(int nb, int nv, const double* part, double* h, int accumulate) {
+  const int i = threadIdx.x;
+  if (i >= nv) return;
+  double s = 0.0;
+  for (int b = 0; b < nb; b++) s += part[(int64_t)b * nv + i];
+  h[i] = accumulate ? h[i] + s : s;
+}
+__global__ void k_mdot_sub(int n, int nv, const float* V, const double* hsub, float* w) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    float acc = w[k];
+    for (int i = 0; i < nv; i++) acc -= (float)hsub[i] * V[(int64_t)i * n + k];
+    w[k] = acc;
+  }
+}
+__global__ void k_normalize(int n, const double* nrm2, const float* w, float* v) {
+  const float inv = (float)(1.0 / sqrt(*nrm2));
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) v[k] = w[k] * inv;
+}
+// Givens update of Hessenberg column j; H is (m+1) x m column-major in hs,
+// cs/sn the rotations, g the rotated right-hand side (g[0] = 1 initially).
+__global__ void k_givens(int m, int j, double* H, const double* hcol, const double* nrm2, double* cs,
+                         double* sn, double* g) {
+  double* col = H + (int64_t)j * (m + 1);
+  for (int i = 0; i <= j; i++) col[i] = hcol[i];
+  col[j + 1] = sqrt(*nrm2);
+  for (int i = 0; i < j; i++) {
+    const double a = col[i], b = col[i + 1];
+    col[i] = cs[i] * a + sn[i] * b;
+    col[i + 1] = -sn[i] * a + cs[i] * b;
+  }
+  const double a = col[j], b = col[j + 1];
+  const double r = sqrt(a * a + b * b);
+  cs[j] = (r > 0.0) ? a / r : 1.0;
+  sn[j] = (r > 0.0) ? b / r : 0.0;
+  col[j] = r;
+  col[j + 1] = 0.0;
+  g[j + 1] = -sn[j] * g[j];
+  g[j] = cs[j] * g[j];
+}
+__global__ void k_backsolve(int m, int jdim, const double* H, const double* g, double* y) {
+  for (int i = jdim - 1; i >= 0; i--) {
+    double s = g[i];
+    for (int k = i + 1; k < jdim; k++) s -= H[(int64_t)k * (m + 1) + i] * y[k];
+    y[i] = s / H[(int64_t)i * (m + 1) + i];
+  }
+}
+// x += scale * sum_i y_i V_i, in FP64
+__global__ void k_update_x(int n, int jdim, const float* V, const double* y, const double* nrm2r,
+                           double* x) {
+  const double scale = sqrt(*nrm2r);
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    for (int i = 0; i < jdim; i++) acc += y[i] * (double)V[(int64_t)i * n + k];
+    x[k] += scale * acc;
+  }
+}
+__global__ void k_gmres_init(double* g, int m) {
+  for (int i = 0; i <= m; i++) g[i] = 0.0;
+  g[0] = 1.0;
+}
+
+inline int vgrid(int n) { return std::max(1, std::min(1024, (n + 255) / 256)); }
+
+}  // namespace
+
+// ---------------------------------------------------------------- drivers
+static void dot2(cudaStream_t s, int n, const double* a, const double* b, const double* c,
+                 const double* d, double* part, double* o1, double* o2, int* cnt) {
+  *cnt += 2;
+  const int nb = std::min(RED_BLOCKS, std::max(1, (n + RED_THREADS - 1) / RED_THREADS));
+  k_dot2_part<double><<<nb, RED_THREADS, 0, s>>>(n, a, b, c, d, part);
+  k_dot2_final<<<1, RED_THREADS, 0, s>>>(nb, part, o1, o2);
+}
+
+cudaError_t solve_bicgstab(const SolveCsr& A, const double* b, double* x, SolveWork& w,
+                           int max_iter, double tol, int* iters, double* relres, cudaStream_t s) {
+  w.launches = 0;
+  const int n = A.K;
+  const int sg = std::max(1, std::min(4096, (n * 32 + SPMV_THREADS - 1) / SPMV_THREADS));
+  const int vg = vgrid(n);
+  double* r = w.v64[0];
+  double* r0 = w.v64[1];
+  double* p = w.v64[2];
+  double* v = w.v64[3];
+  double* sv = w.v64[4];
+  double* t = w.v64[5];
+  double* sc = w.scal;
+  ++w.launches;
+  k_fill<<<vg, 256, 0, s>>>(n, x, 0.0);
+  ++w.launches;
+  k_copy<<<vg, 256, 0, s>>>(n, b, r);
+  ++w.launches;
+  k_copy<<<vg, 256, 0, s>>>(n, b, r0);
+  ++w.launches;
+  k_fill<<<vg, 256, 0, s>>>(n, p, 0.0);
+  ++w.launches;
+  k_fill<<<vg, 256, 0, s>>>(n, v, 0.0);
+  ++w.launches;
+  k_init_scal<<<1, 1, 0, s>>>(sc);
+  dot2(s, n, b, b, nullptr, nullptr, w.part, sc + S_COUNT, nullptr, &w.launches);
+  double rhs_sq = 0.0;
+  cudaMemcpyAsync(&rhs_sq, sc + S_COUNT, sizeof(double), cudaMemcpyDeviceToHost, s);
+  cudaStreamSynchronize(s);
+  *iters = 0;
+  *relres = 0.0;
+  if (rhs_sq == 0.0) return cudaGetLastError();
+  const double tol2 = tol * tol * rhs_sq;
+  int it = 0;
+  double rr = rhs_sq;
+  while (it < max_iter) {
+    dot2(s, n, r, r, r0, r, w.part, sc + S_RR, sc + S_RHO_NEW, &w.launches);
+    cudaMemcpyAsync(w.host_rr, sc + S_RR, sizeof(double), cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    rr = *w.host_rr;
+    if (!(rr > tol2)) break;
+    ++w.launches;
+    k_bicg_scal1<<<1, 1, 0, s>>>(sc);
+    ++w.launches;
+    k_bicg_p<<<vg, 256, 0, s>>>(n, r, p, v, sc);
+    ++w.launches;
+    k_spmv<double><<<sg, SPMV_THREADS, 0, s>>>(n, A.row_ptr, A.col, A.val64, p, v);
+    dot2(s, n, r0, v, nullptr, nullptr, w.part, sc + S_R0V, nullptr, &w.launches);
+    ++w.launches;
+    k_bicg_scal2<<<1, 1, 0, s>>>(sc);
+    ++w.launches;
+    k_bicg_s<<<vg, 256, 0, s>>>(n, r, v, sv, sc);
+    ++w.launches;
+    k_spmv<double><<<sg, SPMV_THREADS, 0, s>>>(n, A.row_ptr, A.col, A.val64, sv, t);
+    dot2(s, n, t, sv, t, t, w.part, sc + S_TS, sc + S_TT, &w.launches);
+    ++w.launches;
+    k_bicg_scal3<<<1, 1, 0, s>>>(sc);
+    ++w.launches;
+    k_bicg_x<<<vg, 256, 0, s>>>(n, x, p, sv, r, t, sc);
+    ++it;
+  }
+  if (it == max_iter) {
+    dot2(s, n, r, r, nullptr, nullptr, w.part, sc + S_RR, nullptr, &w.launches);
+    cudaMemcpyAsync(w.host_rr, sc + S_RR, sizeof(double), cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    rr = *w.host_rr;
+  }
+  *iters = it;
+  *relres = std::sqrt(rr / rhs_sq);
+  return cudaGetLastError();
+}
+
+cudaError_t solve_gmres_ir(const SolveCsr& A, const double* b, double* x, SolveWork& w, int m,
+                           int max_iter, int max_refine, double tol, int* iters, int* refines,
+                           double* relres, cudaStream_t s) {
+  w.launches = 0;
+  const int n = A.K;
+  const int sg = std::max(1, std::min(4096, (n * 32 + SPMV_THREADS - 1) / SPMV_THREADS));
+  const int vg = vgrid(n);
+  double* r = w.v64[0];
+  double* Ax = w.v64[1];
+  double* sc = w.scal;
+  double* bb = sc + 0;     // <b,b>
+  double* rr = sc + 1;     // <r,r>
+  double* nrm = sc + 2;    // <w,w>
+  double* H = w.hess;
+  double* cs = H + (m + 1) * m;
+  double* sn = cs + m;
+  double* g = sn + m;
+  double* hcol = g + (m + 1);
+  double* y = hcol + (m + 1);
+  float* V = w.V32;
+  float* wv = w.w32;
+  const int nb = std::min(RED_BLOCKS, std::max(1, (n + RED_THREADS - 1) / RED_THREADS));
+  ++w.launches;
+  k_to_f32<<<vgrid((int)std::min<int64_t>(A.nnz, 1 << 28)), 256, 0, s>>>(A.nnz, A.val64, w.val32);
+  ++w.launches;
+  k_fill<<<vg, 256, 0, s>>>(n, x, 0.0);
+  dot2(s, n, b, b, nullptr, nullptr, w.part, bb, nullptr, &w.launches);
+  double hb = 0.0;
+  cudaMemcpyAsync(&hb, bb, sizeof(double), cudaMemcpyDeviceToHost, s);
+  cudaStreamSynchronize(s);
+  *iters = 0;
+  *refines = 0;
+  *relres = 0.0;
+  if (hb == 0.0) return cudaGetLastError();
+  const double tol2 = tol * tol * hb;
+  int total = 0, ref = 0;
+  double hr = hb;
+  for (; ref <= max_refine; ref++) {
+    // FP64 residual
+    ++w.launches;
+    k_spmv<double><<<sg, SPMV_THREADS, 0, s>>>(n, A.row_ptr, A.col, A.val64, x, Ax);
+    ++w.launches;
+    k_resid<<<vg, 256, 0, s>>>(n, b, Ax, r);
+    dot2(s, n, r, r, nullptr, nullptr, w.part, rr, nullptr, &w.launches);
+    cudaMemcpyAsync(w.host_rr, rr, sizeof(double), cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    hr = *w.host_rr;
+    if (!(hr > tol2) || ref == max_refine || total >= max_iter) break;
+    // FP32 GMRES(m) on A d = r / |r|
+    ++w.launches;
+    k_scale_to_f32<<<vg, 256, 0, s>>>(n, r, rr, V);
+    ++w.launches;
+    k_gmres_init<<<1, 1, 0, s>>>(g, m);
+    int j = 0;
+    const double inner_tol = 1e-6;
+    for (; j < m; j++) {
+      ++w.launches;
+      k_spmv<float><<<sg, SPMV_THREADS, 0, s>>>(n, A.row_ptr, A.col, w.val32, V + (int64_t)j * n, wv);
+      const int nv = j + 1;
+      const size_t shm = (size_t)nv * MDOT_THREADS * sizeof(double);
+      // classical Gram-Schmidt, twice
+      ++w.launches;
+      k_mdot_part<<<nb, MDOT_THREADS, shm, s>>>(n, nv, V, wv, w.part);
+      ++w.launches;
+      k_mdot_final<<<1, 64, 0, s>>>(nb, nv, w.part, hcol, 0);
+      ++w.launches;
+      k_mdot_sub<<<vg, 256, 0, s>>>(n, nv, V, hcol, wv);
+      ++w.launches;
+      k_mdot_part<<<nb, MDOT_THREADS, shm, s>>>(n, nv, V, wv, w.part);
+      ++w.launches;
+      k_mdot_final<<<1, 64, 0, s>>>(nb, nv, w.part, y, 0);
+      ++w.launches;
+      k_mdot_sub<<<vg, 256, 0, s>>>(n, nv, V, y, wv);
+      ++w.launches;
+      k_mdot_final<<<1, 64, 0, s>>>(nb, nv, w.part, hcol, 1);
+      k_dot2_part<float><<<nb, RED_THREADS, 0, s>>>(n, wv, wv, nullptr, nullptr, w.part);
+      k_dot2_final<<<1, RED_THREADS, 0, s>>>(nb, w.part, nrm, nullptr);
+      ++w.launches;
+      k_normalize<<<vg, 256, 0, s>>>(n, nrm, wv, V + (int64_t)(j + 1) * n);
+      ++w.launches;
+      k_givens<<<1, 1, 0, s>>>(m, j, H, hcol, nrm, cs, sn, g);
+      ++total;
+      double gres = 0.0;
+      cudaMemcpyAsync(&gres, g + j + 1, sizeof(double), cudaMemcpyDeviceToHost, s);
+      cudaStreamSynchronize(s);
+      if (std::fabs(gres) < inner_tol || total >= max_iter) { j++; break; }
+    }
+    ++w.launches;
+    k_backsolve<<<1, 1, 0, s>>>(m, j, H, g, y);
+    ++w.launches;
+    k_update_x<<<vg, 256, 0, s>>>(n, j, V, y, rr, x);
+  }
+  *iters = total;
+  *refines = ref;
+  *relres = std::sqrt(hr / hb);
+  return cudaGetLastError();
+}
+
+}  // namespace pdds

@@ -1,0 +1,108 @@
+// Launch arguments and entry points of the device kernels (host-visible).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "dev_common.cuh"
+
+namespace pdds {
+
+constexpr int MIXED_THREADS = 256;
+constexpr int FP64_THREADS = 256;
+constexpr unsigned ERR_FLAG_STEP_LIMIT = 1u;
+constexpr unsigned ERR_FLAG_EXIT_SIDE = 2u;
+constexpr unsigned ERR_FLAG_SINGULAR = 4u;
+
+struct MixedArgs {
+  DevLayout L;
+  ProblemDev P;
+  int N;                 // paths per knot
+  float h, sqrth;
+  double inv_N;
+  uint64_t seed;
+  uint32_t instance;
+  int chunks, paths_per_chunk, n_items;
+  int want_var, dup_sum;
+  long long max_steps;
+  const int* mc_knots;   // knots that need paths, in hand-out order
+  int* item_counter;
+  double* G;             // [nnz] accumulates -sum Y H / N
+  double* GG;            // [nnz] accumulates sum (Y H)^2 / N
+  double* Bsum;          // [K]
+  double* BBsum;         // [K]
+  unsigned long long* stats;  // [0] steps [1] unused [2] global exits [3] stencil exits
+  unsigned* err_flags;
+};
+
+struct Fp64Args {
+  DevLayout L;
+  ProblemDev P;
+  int N;
+  double h, sqrth, inv_N;
+  uint64_t seed;
+  uint32_t instance;
+  int chunks, paths_per_chunk, n_items;
+  int dup_sum;
+  long long max_steps;
+  const int* mc_knots;
+  int* item_counter;
+  double* G;
+  double* Bsum;
+  double* BBsum;
+  unsigned long long* stats;
+  unsigned* err_flags;
+};
+
+struct ReplayArgs {
+  DevLayout L;
+  ProblemDev P;
+  int N;
+  double h, sqrth;
+  uint64_t seed;
+  uint32_t instance;
+  int sublinear;
+  long long max_steps;
+  const int* mc_knots;   // knots with paths
+  int n_mc;
+  // per-knot side data for the reduction (actual positions, ipsi per knot)
+  const int64_t* knot_ipsi_off;  // [n_mc][4] offset into ipsi_knot, -1 if none
+  const double* ipsi_knot;
+  // exit records [n_mc * N]
+  double* ex;
+  double* ey;
+  double* eY;
+  double* eZ;
+  double* exi;
+  int* eside;            // -1 global, 0..3 stencil side, -2 no side
+  int* esteps_l;
+  int* esteps_s;
+  // outputs
+  double* G;             // [nnz] final values
+  double* GG;            // [nnz] final GG/N values (before - G^2)
+  double* B;             // [K]
+  double* BB;            // [K]
+  int dup_sum;
+  unsigned* err_flags;
+};
+
+cudaError_t launch_paths_mixed(const MixedArgs& a, int kind, int grid, size_t smem, cudaStream_t s);
+int mixed_blocks_per_sm(int kind, size_t smem);
+cudaError_t launch_paths_fp64(const Fp64Args& a, int kind, int grid, size_t smem, cudaStream_t s);
+int fp64_blocks_per_sm(int kind, size_t smem);
+cudaError_t launch_replay_paths(const ReplayArgs& a, int kind, cudaStream_t s);
+cudaError_t launch_replay_reduce(const ReplayArgs& a, int kind, const int* task_m, const int* task_d,
+                                 const int* task_i, int ntask, const int64_t* task_out,
+                                 const int64_t* knot_task_off, double* Gside, double* GGside,
+                                 cudaStream_t s);
+// FP64 factorisation of every shape's Psi and the cardinal-function tables.
+cudaError_t launch_rbf_setup(const DevLayout& L, int max_n, int max_nbins, double* ipsi, float* tab,
+                             unsigned* err_flags, cudaStream_t s);
+// B = g(x0) for boundary knots; finalisation of B, BB, G_var.
+cudaError_t launch_boundary_b(const DevLayout& L, const ProblemDev& P, int mode, const int* knots,
+                              int n, double* B, double* BB, cudaStream_t s);
+cudaError_t launch_finalize(const int* mc_knots, int n_mc, int N, const double* Bsum,
+                            const double* BBsum, double* B, double* BB, const int64_t* row_ptr,
+                            int64_t nnz, const double* G, double* GG_to_var, int want_var,
+                            cudaStream_t s);
+
+}  // namespace pdds

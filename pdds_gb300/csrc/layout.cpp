@@ -1,0 +1,427 @@
+// Host-side layout of the PDDSparse interface system: knots, stencils, stencil
+// sides and side shapes.  Follows the reference's construction exactly,
+// including its floating-point order, so knot coordinates are bit-identical:
+//   Fullfill_interfaces      PDDAlgorithms/PDDSparseGM.cpp:346-689 (INTERSECTIONS_YES)
+//   server hand-out order    PDDAlgorithms/PDDSparseGM.cpp:705-756
+//   Get_Interfaces, Labels_Stencil  PDDAlgorithms/PDDSparseGM.cpp:1316-1433
+//   Compute_Stencil          PDDAlgorithms/PDDSparseGM.cpp:1845-2041 (STEN_ELONG 0.5)
+//   Interface::N/S/E/W       Meshes/interface.cpp:16-93
+//   Stencil::Init            Meshes/stencil.cpp:11-85
+//   G_return_withrep order   Meshes/stencil.cpp:343-406 (sides N, S, E, W; later overwrites)
+// The reference rebuilds a stencil for every knot; here knots that belong to
+// the same interface (or the same cross point) share one stencil record, and
+// stencil sides with identical knot lists share one side record.
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <tuple>
+
+#include "pdds_internal.h"
+
+namespace pdds {
+
+namespace {
+
+struct Lab {
+  int a, b;
+};
+
+// Position of interface [a, b] in the reference's interfaces vector, or -1.
+int lab_id(int nsub, Lab l) {
+  if (l.b >= 0 && (l.b % 2) == 1) {  // horizontal [j, 2i+1]
+    const int i = (l.b - 1) / 2, j = l.a;
+    if (i < 0 || i > nsub - 2 || j < 0 || j > nsub - 1) return -1;
+    return 2 * (i * nsub + j);
+  }
+  if (l.b >= 0 && (l.b % 2) == 0) {  // vertical [i, 2j]
+    const int i = l.a, j = l.b / 2;
+    if (i < 0 || i > nsub - 2 || j < 0 || j > nsub - 1) return -1;
+    return 2 * (i * nsub + j) + 1;
+  }
+  return -1;
+}
+
+// Interface::N/S/E/W; label[1] % 2 == 0 means vertical.
+void lab_N(Lab l, std::vector<Lab>& o) {
+  o.clear();
+  if (l.b % 2 == 0) { o.push_back({l.a, l.b + 1}); o.push_back({l.a + 1, l.b + 1}); }
+  else o.push_back({l.a, l.b + 2});
+}
+void lab_S(Lab l, std::vector<Lab>& o) {
+  o.clear();
+  if (l.b % 2 == 0) { o.push_back({l.a, l.b - 1}); o.push_back({l.a + 1, l.b - 1}); }
+  else o.push_back({l.a, l.b - 2});
+}
+void lab_E(Lab l, std::vector<Lab>& o) {
+  o.clear();
+  if (l.b % 2 == 0) o.push_back({l.a + 1, l.b});
+  else { o.push_back({l.a, l.b - 1}); o.push_back({l.a, l.b + 1}); }
+}
+void lab_W(Lab l, std::vector<Lab>& o) {
+  o.clear();
+  if (l.b % 2 == 0) o.push_back({l.a - 1, l.b});
+  else { o.push_back({l.a - 1, l.b - 1}); o.push_back({l.a - 1, l.b + 1}); }
+}
+
+struct Iface {
+  Lab label;
+  std::vector<int> index;
+  std::vector<double> px, py;
+};
+
+// Rectangle2D signed distance (BVPs/Domains/rectangle.hpp:7-229), distance only.
+double rect_dist(const double* p, double x, double y) {
+  const double c0 = 0.5 * (p[0] + p[2]), c1 = 0.5 * (p[1] + p[3]);
+  const double h0 = p[2] - c0, h1 = p[3] - c1;
+  const double d0 = std::fabs(x - c0), d1 = std::fabs(y - c1);
+  if (d0 <= h0 && d1 <= h1) return (d0 - h0 > d1 - h1) ? d0 - h0 : d1 - h1;
+  if (d0 > h0) {
+    if (d1 > h1) return std::sqrt((d0 - h0) * (d0 - h0) + (d1 - h1) * (d1 - h1));
+    return d0 - h0;
+  }
+  return d1 - h1;
+}
+
+}  // namespace
+
+void set_shape_bins(HostLayout& L, int bps) {
+  if (bps <= 0) bps = 16;
+  int64_t tab = 0;
+  for (auto& sh : L.shapes) {
+    const double gap = (sh.n > 1) ? (sh.t[1] - sh.t[0]) : 1.0;
+    sh.delta = gap / bps;
+    const int inner = (int)std::ceil((sh.hi - sh.lo) / sh.delta - 1e-9);
+    sh.nbins = inner + 4;  // grid covers [lo - delta, hi + 2 delta]
+    sh.tab_off = tab;
+    tab += (int64_t)sh.nbins * sh.n;
+  }
+}
+
+std::string build_rect_layout(HostLayout& L, const double sw[2], const double ne[2], int nsub,
+                              int nnode, const double fac[4], int bps) {
+  if (nsub < 2 || nnode < 3) return "layout needs nsub >= 2 and nnode >= 3";
+  if (!(ne[0] > sw[0] && ne[1] > sw[1])) return "layout needs NE > SW";
+  L = HostLayout();
+  for (int i = 0; i < 2; i++) { L.sw[i] = sw[i]; L.ne[i] = ne[i]; }
+  for (int i = 0; i < 4; i++) L.fac[i] = fac[i];
+  L.nsub = nsub;
+  L.nnode = nnode;
+  const int iN = nsub, nN = nnode;
+  const int nif = iN * (iN - 1) * 2;
+  std::vector<Iface> ifs(nif);
+  std::vector<double> sx(nif), sy(nif), ex(nif), ey(nif);
+  // interface end points (PDDSparseGM.cpp:363-437); P0 accumulates in y, P1 in x
+  const double lx = (ne[0] - sw[0]) / (1.0 * iN), ly = (ne[1] - sw[1]) / (1.0 * iN);
+  double P0[2] = {sw[0], sw[1]}, P1[2] = {sw[0], sw[1]};
+  P0[0] += 0.0; P0[1] += ly;
+  P1[0] += lx; P1[1] += 0.0;
+  int cen = 0;
+  for (int i = 0; i < iN - 1; i++) {
+    for (int j = 0; j < iN; j++) {
+      sx[cen] = P0[0] + lx * j; sy[cen] = P0[1] + 0.0 * j;
+      ex[cen] = P0[0] + lx * (j + 1); ey[cen] = P0[1] + 0.0 * (j + 1);
+      ifs[cen].label = {j, 2 * i + 1};
+      cen++;
+      sx[cen] = P1[0] + 0.0 * j; sy[cen] = P1[1] + ly * j;
+      ex[cen] = P1[0] + 0.0 * (j + 1); ey[cen] = P1[1] + ly * (j + 1);
+      ifs[cen].label = {i, 2 * j};
+      cen++;
+    }
+    P0[0] += 0.0; P0[1] += ly;
+    P1[0] += lx; P1[1] += 0.0;
+  }
+  // knot numbering with shared cross points (:493-543)
+  std::vector<int> cross((iN - 1) * (iN - 1), 0);
+  int knot = 0, cc = 0;
+  for (int i = 0; i < iN - 1; i++)
+    for (int j = 0; j <= 2 * iN - 2; j += 2) {
+      Iface& f = ifs[lab_id(iN, {i, j})];
+      f.index.push_back(knot);
+      if (j != 0) cross[(j / 2 - 1) * (iN - 1) + i] = knot;
+      for (int k = 0; k < nN - 1; k++) f.index.push_back(++knot);
+      if (j == 2 * iN - 2) knot++;
+    }
+  for (int j = 1; j <= 2 * iN - 3; j += 2)
+    for (int i = 0; i < iN; i++) {
+      Iface& f = ifs[lab_id(iN, {i, j})];
+      if (i != 0) f.index.push_back(cross[cc++]);
+      else f.index.push_back(knot++);
+      for (int k = 1; k < nN - 1; k++) f.index.push_back(knot++);
+      if (i != iN - 1) f.index.push_back(cross[cc]);
+      else f.index.push_back(knot++);
+    }
+  L.K = knot;
+  // positions by repeated addition (:641-686)
+  for (int id = 0; id < nif; id++) {
+    Iface& f = ifs[id];
+    const size_t n = f.index.size();
+    const double den = (double)(n - 1);
+    const double ix = (ex[id] - sx[id]) / den, iy = (ey[id] - sy[id]) / den;
+    double vx = sx[id], vy = sy[id];
+    f.px.resize(n);
+    f.py.resize(n);
+    for (size_t k = 0; k < n; k++) {
+      f.px[k] = vx;
+      f.py[k] = vy;
+      vx += ix;
+      vy += iy;
+    }
+  }
+  // hand-out order and the positions sent with the knots (:705-756)
+  L.kx.assign(L.K, 0.0);
+  L.ky.assign(L.K, 0.0);
+  for (int Iy = 0; Iy <= 2 * iN - 2; Iy++) {
+    const bool vert = (Iy % 2 == 0);
+    for (int Ix = 0; Ix <= (vert ? iN - 2 : iN - 1); Ix++) {
+      const Iface& f = ifs[lab_id(iN, {Ix, Iy})];
+      size_t b = 1, e = f.index.size();
+      if (vert) { if (Iy == 0) b = 0; }
+      else {
+        if (Ix == 0) { b = 0; e = f.index.size() - 1; }
+        else if (Ix != iN - 1) e = f.index.size() - 1;
+      }
+      for (size_t k = b; k < e; k++) {
+        L.order.push_back(f.index[k]);
+        L.kx[f.index[k]] = f.px[k];
+        L.ky[f.index[k]] = f.py[k];
+      }
+    }
+  }
+  if ((int)L.order.size() != L.K) return "internal: hand-out list does not cover all knots";
+  // interfaces of every knot, in interface-vector order (Get_Interfaces)
+  std::vector<std::vector<int>> knot_ifs(L.K);
+  for (int id = 0; id < nif; id++)
+    for (int v : ifs[id].index)
+      if (knot_ifs[v].empty() || knot_ifs[v].back() != id) knot_ifs[v].push_back(id);
+
+  const double gparams[4] = {sw[0], sw[1], ne[0], ne[1]};
+  std::map<std::vector<int>, int> stencil_key;
+  std::map<std::pair<int, std::vector<int>>, int> side_key;
+  L.knot_stencil.assign(L.K, -1);
+  L.knot_boundary.assign(L.K, 0);
+  std::vector<Lab> tmp;
+  const double STEN_ELONG = 0.5;
+  for (int v = 0; v < L.K; v++) {
+    const std::vector<int>& ki = knot_ifs[v];
+    auto it = stencil_key.find(ki);
+    if (it != stencil_key.end()) {
+      L.knot_stencil[v] = it->second;
+      continue;
+    }
+    // Labels_Stencil
+    std::vector<Lab> lab[4];
+    auto push_if = [&](int d, Lab l) { if (lab_id(iN, l) >= 0) lab[d].push_back(l); };
+    if (ki.size() == 1) {
+      const Lab l = ifs[ki[0]].label;
+      lab_N(l, tmp); for (auto& a : tmp) push_if(DIR_N, a);
+      lab_S(l, tmp); for (auto& a : tmp) push_if(DIR_S, a);
+      lab_E(l, tmp); for (auto& a : tmp) push_if(DIR_E, a);
+      lab_W(l, tmp); for (auto& a : tmp) push_if(DIR_W, a);
+    } else if (ki.size() == 4) {
+      int max_h = -1 << 30, max_v = -1 << 30;
+      for (int q = 0; q < 4; q++) {
+        max_h = std::max(max_h, ifs[ki[q]].label.a);
+        max_v = std::max(max_v, ifs[ki[q]].label.b);
+      }
+      Lab ie{0, 0}, iw{0, 0}, in{0, 0}, is{0, 0};
+      for (int q = 0; q < 4; q++) {
+        const Lab l = ifs[ki[q]].label;
+        if (l.b % 2 == 1) { if (l.a == max_h) ie = l; else iw = l; }
+        else { if (l.b == max_v) in = l; else is = l; }
+      }
+      lab_N(iw, tmp); push_if(DIR_N, tmp[0]);
+      lab_N(ie, tmp); push_if(DIR_N, tmp[0]);
+      lab_S(iw, tmp); push_if(DIR_S, tmp[0]);
+      lab_S(ie, tmp); push_if(DIR_S, tmp[0]);
+      lab_E(is, tmp); push_if(DIR_E, tmp[0]);
+      lab_E(in, tmp); push_if(DIR_E, tmp[0]);
+      lab_W(is, tmp); push_if(DIR_W, tmp[0]);
+      lab_W(in, tmp); push_if(DIR_W, tmp[0]);
+    } else {
+      return "internal: knot on " + std::to_string(ki.size()) + " interfaces";
+    }
+    auto IF = [&](Lab l) -> const Iface& { return ifs[lab_id(iN, l)]; };
+    // Compute_Stencil
+    StencilRec st;
+    for (int i = 0; i < 4; i++) st.rect[i] = gparams[i];
+    if (!lab[DIR_S].empty()) st.rect[1] = IF(lab[DIR_S][0]).py[0];
+    if (!lab[DIR_W].empty()) st.rect[0] = IF(lab[DIR_W][0]).px[0];
+    if (!lab[DIR_N].empty()) st.rect[3] = IF(lab[DIR_N].back()).py.back();
+    if (!lab[DIR_E].empty()) st.rect[2] = IF(lab[DIR_E].back()).px.back();
+    std::vector<int> sidx[4];
+    std::vector<double> spx[4], spy[4];
+    int kind[4] = {-3, -3, -3, -3};
+    for (int d = 0; d < 4; d++) {
+      if (lab[d].empty()) continue;
+      const bool horiz = (d == DIR_N || d == DIR_S);
+      auto add = [&](const Iface& f, int from, int to) {
+        for (int k = from; k < to; k++) {
+          sidx[d].push_back(f.index[k]);
+          spx[d].push_back(f.px[k]);
+          spy[d].push_back(f.py[k]);
+        }
+      };
+      Lab first = lab[d][0];
+      Lab pre = horiz ? Lab{first.a - 1, first.b} : Lab{first.a, first.b - 2};
+      if (lab_id(iN, pre) >= 0) {
+        kind[d]++;
+        const Iface& a = IF(pre);
+        add(a, (int)((1 - STEN_ELONG) * (a.index.size() - 1)), (int)a.index.size());
+      }
+      for (const Lab& l : lab[d]) {
+        add(IF(l), 0, (int)IF(l).index.size());
+        kind[d] += 2;
+      }
+      Lab last = lab[d].back();
+      Lab post = horiz ? Lab{last.a + 1, last.b} : Lab{last.a, last.b + 2};
+      if (lab_id(iN, post) >= 0) {
+        const Iface& a = IF(post);
+        kind[d]++;
+        add(a, 0, (int)(STEN_ELONG * (a.index.size())));
+      }
+    }
+    // Stencil::Init: keep the last written position of an index; drop
+    // consecutive repeats of an index
+    for (int d = 0; d < 4; d++) {
+      st.kind[d] = kind[d];
+      st.side[d] = -1;
+      if (sidx[d].empty()) continue;
+      std::map<int, std::pair<double, double>> pos;
+      for (size_t q = 0; q < sidx[d].size(); q++) pos[sidx[d][q]] = {spx[d][q], spy[d][q]};
+      std::vector<int> idx = sidx[d];
+      idx.erase(std::unique(idx.begin(), idx.end()), idx.end());
+      int kd = kind[d];
+      if (kd < 0 || kd > 3) return "internal: stencil side kind out of range";
+      auto key = std::make_pair(kd, idx);
+      auto sit = side_key.find(key);
+      if (sit == side_key.end()) {
+        SideRec sr;
+        sr.n = (int)idx.size();
+        sr.orient = (d == DIR_N || d == DIR_S) ? 0 : 1;
+        sr.kind = kd;
+        sr.c = fac[kd];
+        sr.shape = -1;
+        sr.knot_off = (int64_t)L.side_knot.size();
+        for (int v2 : idx) {
+          L.side_knot.push_back(v2);
+          L.side_px.push_back(pos[v2].first);
+          L.side_py.push_back(pos[v2].second);
+        }
+        sr.origin = (sr.orient == 0) ? L.side_px[sr.knot_off] : L.side_py[sr.knot_off];
+        sr.fixed = (sr.orient == 0) ? L.side_py[sr.knot_off] : L.side_px[sr.knot_off];
+        L.max_side = std::max(L.max_side, sr.n);
+        side_key[key] = (int)L.sides.size();
+        st.side[d] = (int)L.sides.size();
+        L.sides.push_back(sr);
+      } else {
+        st.side[d] = sit->second;
+      }
+    }
+    // global-boundary flags of the rect sides: midpoint within 1e-8 of the
+    // domain boundary (Reduce_Analytic's test, EMFKACSolver.hpp:559)
+    {
+      const double mx = 0.5 * (st.rect[0] + st.rect[2]), my = 0.5 * (st.rect[1] + st.rect[3]);
+      st.glob[DIR_N] = rect_dist(gparams, mx, st.rect[3]) >= -1e-08;
+      st.glob[DIR_S] = rect_dist(gparams, mx, st.rect[1]) >= -1e-08;
+      st.glob[DIR_E] = rect_dist(gparams, st.rect[2], my) >= -1e-08;
+      st.glob[DIR_W] = rect_dist(gparams, st.rect[0], my) >= -1e-08;
+    }
+    // G row: sorted union of side indices
+    std::vector<int> cols;
+    for (int d = 0; d < 4; d++)
+      if (st.side[d] >= 0) {
+        const SideRec& sr = L.sides[st.side[d]];
+        for (int q = 0; q < sr.n; q++) cols.push_back(L.side_knot[sr.knot_off + q]);
+      }
+    std::sort(cols.begin(), cols.end());
+    cols.erase(std::unique(cols.begin(), cols.end()), cols.end());
+    st.cols = cols;
+    st.row_len = (int)cols.size();
+    st.map_off = (int64_t)L.map_pos.size();
+    std::map<int, int64_t> last_writer;
+    for (int d = 0; d < 4; d++) {
+      if (st.side[d] < 0) continue;
+      const SideRec& sr = L.sides[st.side[d]];
+      for (int q = 0; q < sr.n; q++) {
+        const int v2 = L.side_knot[sr.knot_off + q];
+        const int p = (int)(std::lower_bound(cols.begin(), cols.end(), v2) - cols.begin());
+        last_writer[v2] = (int64_t)L.map_pos.size();
+        L.map_pos.push_back(p);
+        L.map_owner.push_back(0);
+      }
+    }
+    for (auto& kv : last_writer) L.map_owner[kv.second] = 1;
+    const int sid = (int)L.stencils.size();
+    stencil_key[ki] = sid;
+    L.knot_stencil[v] = sid;
+    L.stencils.push_back(st);
+  }
+  // boundary knots (Solve_OMP_Analytic: |dist| <= 1e-8 -> B = g, no row)
+  L.row_ptr.assign(L.K + 1, 0);
+  for (int v = 0; v < L.K; v++) {
+    L.knot_boundary[v] = !(std::fabs(rect_dist(gparams, L.kx[v], L.ky[v])) > 1e-08);
+    L.nboundary += L.knot_boundary[v];
+    const int len = L.knot_boundary[v] ? 0 : L.stencils[L.knot_stencil[v]].row_len;
+    L.row_ptr[v + 1] = L.row_ptr[v] + len;
+  }
+  L.col.resize(L.row_ptr[L.K]);
+  for (int v = 0; v < L.K; v++) {
+    if (L.knot_boundary[v]) continue;
+    const auto& cols = L.stencils[L.knot_stencil[v]].cols;
+    std::copy(cols.begin(), cols.end(), L.col.begin() + L.row_ptr[v]);
+  }
+  // side shapes: translates with equal knot spacing, size, c and exit extent
+  std::map<std::tuple<int, long long, long long, long long, long long>, int> shape_key;
+  std::vector<std::vector<std::pair<int, int>>> uses(L.sides.size());  // (stencil, dir)
+  for (size_t s = 0; s < L.stencils.size(); s++)
+    for (int d = 0; d < 4; d++)
+      if (L.stencils[s].side[d] >= 0) uses[L.stencils[s].side[d]].push_back({(int)s, d});
+  for (size_t sd = 0; sd < L.sides.size(); sd++) {
+    SideRec& sr = L.sides[sd];
+    std::vector<double> t(sr.n);
+    const double* crd = (sr.orient == 0) ? &L.side_px[sr.knot_off] : &L.side_py[sr.knot_off];
+    for (int q = 0; q < sr.n; q++) t[q] = crd[q] - sr.origin;
+    const double gap = sr.n > 1 ? t[1] - t[0] : 1.0;
+    bool uniform = true;
+    for (int q = 0; q < sr.n; q++)
+      if (std::fabs(t[q] - q * gap) > 1e-9 * (1.0 + std::fabs(t[q]))) uniform = false;
+    double lo = 1e300, hi = -1e300;
+    for (auto& u : uses[sd]) {
+      const StencilRec& st = L.stencils[u.first];
+      const double a = (sr.orient == 0) ? st.rect[0] : st.rect[1];
+      const double b = (sr.orient == 0) ? st.rect[2] : st.rect[3];
+      lo = std::min(lo, a - sr.origin);
+      hi = std::max(hi, b - sr.origin);
+    }
+    auto key = std::make_tuple(sr.n, (long long)std::llround(gap * 1e12),
+                               (long long)std::llround(sr.c * 1e12),
+                               (long long)std::llround(lo / gap * 1e6),
+                               uniform ? (long long)std::llround(hi / gap * 1e6) : -1 - (long long)sd);
+    auto it = shape_key.find(key);
+    if (it == shape_key.end()) {
+      ShapeRec sh;
+      sh.n = sr.n;
+      sh.c = sr.c;
+      sh.t = t;
+      sh.lo = lo;
+      sh.hi = hi;
+      shape_key[key] = (int)L.shapes.size();
+      sr.shape = (int)L.shapes.size();
+      L.shapes.push_back(sh);
+    } else {
+      sr.shape = it->second;
+      ShapeRec& sh = L.shapes[it->second];
+      sh.lo = std::min(sh.lo, lo);
+      sh.hi = std::max(sh.hi, hi);
+    }
+  }
+  int64_t ip = 0;
+  for (auto& sh : L.shapes) {
+    sh.ipsi_off = ip;
+    ip += (int64_t)sh.n * sh.n;
+  }
+  set_shape_bins(L, bps);
+  return "";
+}
+
+}  // namespace pdds

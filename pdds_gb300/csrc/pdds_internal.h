@@ -1,0 +1,87 @@
+// Internal data model of the pdds_gb300 library (host side).
+//
+// HBM layout (struct-of-arrays, all device copies made once per layout):
+//   knots    K      : x, y (FP64 and FP32), stencil id, boundary flag, row offset
+//   stencils S      : rect {x0,y0,x1,y1} (FP64 and FP32), global-side flags,
+//                     side id per direction N,S,E,W (-1 = none), row length,
+//                     offset into the (side knot -> row column) map
+//   sides    D      : shape id, orientation, origin (coordinate of side knot 0),
+//                     knot offset into side_knot/side_px/side_py
+//   shapes   P      : side knots that are translates of each other share one
+//                     shape: n, c, local knot coordinates t_j, exit extent,
+//                     bin grid, FP64 inverse of Psi and the FP32 table of
+//                     cardinal functions H[b][i] on the bin grid.
+#pragma once
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+namespace pdds {
+
+enum Dir { DIR_N = 0, DIR_S = 1, DIR_E = 2, DIR_W = 3 };
+
+struct StencilRec {
+  double rect[4];
+  int32_t side[4];   // side id per Dir, -1 if the side has no knots
+  int32_t kind[4];   // reference's kind per Dir (-3 .. 3)
+  int32_t glob[4];   // 1 if that rect side lies on the domain boundary
+  int32_t row_len;   // entries of the G row (sorted unique knot indices)
+  int64_t map_off;   // offset of per-(side, knot) row positions, 4 blocks of n_side
+  std::vector<int32_t> cols;  // sorted unique columns
+};
+
+struct SideRec {
+  int32_t n;
+  int32_t orient;    // 0: horizontal side (N/S), coordinate along = x; 1: vertical (E/W), along = y
+  int32_t shape;
+  int32_t kind;
+  double c;          // RBF shape parameter (fac[kind])
+  double origin;     // coordinate along the side of knot 0
+  double fixed;      // the other coordinate (constant along the side)
+  int64_t knot_off;  // into side_knot / side_px / side_py
+};
+
+struct ShapeRec {
+  int32_t n;
+  double c;
+  std::vector<double> t;  // local coordinates of the knots (representative side)
+  double lo, hi;          // exit extent in local coordinates (union over its sides)
+  double delta;           // bin spacing
+  int32_t nbins;          // grid points lo - delta + b*delta, b = 0 .. nbins-1
+  int64_t tab_off;        // FP32 table offset: H[b*n + i]
+  int64_t ipsi_off;       // FP64 inverse offset: ipsi[j*n + i]
+};
+
+struct HostLayout {
+  double sw[2], ne[2];
+  int32_t nsub = 0, nnode = 0;
+  double fac[4];
+  int32_t K = 0;
+  std::vector<double> kx, ky;
+  std::vector<int32_t> order;          // reference hand-out order
+  std::vector<int32_t> knot_stencil;
+  std::vector<uint8_t> knot_boundary;
+  std::vector<int64_t> row_ptr;        // K+1
+  std::vector<int32_t> col;            // nnz
+  std::vector<StencilRec> stencils;
+  std::vector<SideRec> sides;
+  std::vector<int32_t> side_knot;
+  std::vector<double> side_px, side_py;
+  std::vector<int32_t> map_pos;        // per stencil, per side, per side knot: row position
+  std::vector<uint8_t> map_owner;      // 1 if this (side, knot) writes the entry (overwrite rule)
+  std::vector<ShapeRec> shapes;
+  int32_t max_side = 0;
+  int32_t nboundary = 0;
+};
+
+// Builds the rectangular layout of PDDSparseGM (Fullfill_interfaces,
+// Labels_Stencil, Compute_Stencil, Stencil::Init) and the derived tables.
+// Returns an empty string on success, else the error text.
+std::string build_rect_layout(HostLayout& L, const double sw[2], const double ne[2], int nsub,
+                              int nnode, const double fac[4], int bins_per_gap);
+
+// Re-derives the shape bin grids for a new bins-per-gap value.
+void set_shape_bins(HostLayout& L, int bins_per_gap);
+
+}  // namespace pdds
