@@ -78,8 +78,10 @@ def test_replay_varcoef_bit_exact():
 
 
 def test_device_factorisation_matches_oracle_inverse():
-    """Replay with the library's own FP64 Gauss-Jordan inverses (shared per
-    side shape) stays within the conditioning of Psi of the oracle's result."""
+    """Replay with the library's own FP64 LU inverses (shared per side shape)
+    stays within the conditioning of Psi (cond up to 3e11 here) of the
+    oracle's full-pivot inverses: cardinal weights of two backward-stable
+    inverses differ by up to ~2e-5 on the worst side shape."""
     nsub, nnode, N = 4, 11, 300
     fac = fac_rule(2.0, nsub, nnode)
     L = O.Layout(SW, NE, nsub, nnode)
@@ -87,7 +89,10 @@ def test_device_factorisation_matches_oracle_inverse():
         est = pd.estimate(P.BVP.poisson_sincos(), N, 1e-3, mode=P.MODE_REPLAY_FP64, seed=3)
     ref = L.run(O.make_problem(O.POISSON_SINCOS),
                 O.make_params(N, 1e-3, seed=3, fac=fac, portable=True))
-    _rows_equal(est, ref, exact=False, atol=2e-6)
+    _rows_equal(est, ref, exact=False, atol=5e-5)
+    d = np.concatenate([est.val[est.row_ptr[int(k)]:est.row_ptr[int(k) + 1]] -
+                        ref["g"][ref["row_ptr"][i]:ref["row_ptr"][i + 1]] for i, k in enumerate(ref["knots"])])
+    assert np.median(np.abs(d)) < 1e-6
     b = ref["B"]
     np.testing.assert_array_equal(est.B[ref["knots"]], b)
 
