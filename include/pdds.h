@@ -169,6 +169,27 @@ typedef struct {
 pdds_status pdds_solve_interface(pdds_ctx* ctx, const pdds_solve_desc* desc, double* u,
                                  pdds_solve_info* info);
 
+/* ---------------------------------------------------------------- allocation-free solve
+ * No counterpart in the reference.  For callers that cannot let a library
+ * allocate GPU memory (memory owned by another allocator, serving loops where
+ * cudaMalloc/cudaFree would synchronise or stall, foreign-language hosts that
+ * only lend device buffers): solves (I + G) u = B with the FP64 BiCGSTAB of
+ * pdds_solve_interface on caller-owned DEVICE buffers -- G in CSR without the
+ * unit diagonal (row_ptr[K+1], col[nnz], val[nnz]), B[K], u[K] -- and takes
+ * its work vectors from a static device array instead of allocating.
+ * K must not exceed PDDS_STATIC_SOLVE_MAX_K.  The array (6.3 MB) is held on
+ * every GPU that loads the library until the process exits; all calls share
+ * it, so calls that overlap on the GPU race.  The first call on a device
+ * looks up the array's address; make it before any stream capture on that
+ * device.  stream may be NULL (legacy default stream); err, if given,
+ * receives a message of at most err_len bytes. */
+#define PDDS_STATIC_SOLVE_MAX_K 131072
+pdds_status pdds_solve_bicgstab_static(int device, int32_t K, int64_t nnz, const int64_t* row_ptr,
+                                       const int32_t* col, const double* val, const double* B,
+                                       double* u, double tol, int32_t max_iter, void* stream,
+                                       int32_t* iterations, double* rel_residual, char* err,
+                                       int32_t err_len);
+
 #ifdef __cplusplus
 }
 #endif

@@ -25,8 +25,9 @@ SOLVE_BICGSTAB_FP64, SOLVE_GMRES_FP32_IR = 0, 1
 EXPORTS = [
     "pdds_create", "pdds_destroy", "pdds_last_error", "pdds_version", "pdds_problem_set",
     "pdds_layout_build", "pdds_layout_knots", "pdds_layout_csr", "pdds_layout_stencil",
-    "pdds_estimate", "pdds_solve_interface",
+    "pdds_estimate", "pdds_solve_interface", "pdds_solve_bicgstab_static",
 ]
+STATIC_SOLVE_MAX_K = 131072
 
 
 class ProblemDesc(C.Structure):
@@ -95,6 +96,8 @@ def load(path: str = LIB_PATH):
                                       C.POINTER(C.c_int32), C.c_int32]
     L.pdds_estimate.argtypes = [vp, C.POINTER(EstimateDesc), dp, dp, dp, dp, C.POINTER(EstimateInfo)]
     L.pdds_solve_interface.argtypes = [vp, C.POINTER(SolveDesc), dp, C.POINTER(SolveInfo)]
+    L.pdds_solve_bicgstab_static.argtypes = [C.c_int, C.c_int32, C.c_int64, vp, vp, vp, vp, vp, C.c_double,
+                                             C.c_int32, vp, C.POINTER(C.c_int32), dp, C.c_char_p, C.c_int32]
     for name in EXPORTS:
         if not hasattr(L, name):
             raise RuntimeError("missing export " + name)

@@ -30,6 +30,7 @@ UNITS = {
     "k_misc.cu": ["-fmad=false"],
     "k_solve.cu": [],
     "layout.cpp": ["-x", "cu"],
+    "noalloc.cu": [],
 }
 
 
