@@ -1,11 +1,14 @@
 """Benchmark of the GB300 PDDSparse hot path (one JSON line on rank 0).
 
 A step is one pass of the hot path over one batch of synthetic input: the
-Feynman-Kac estimation of every knot's G row and B entry followed by the
-interface solve (I + G) u = B, on the 12x12-subdomain / 43-knot Poisson
-workload (10,989 knots, 2e4 paths per knot, h = 5e-4) in the MIXED form
-(FP32 paths, FP64 accumulation, FP64 RBF factorisation, FP32 GMRES under
-FP64 refinement).
+RBF factorisation of the stencil sides, the Feynman-Kac estimation of every
+knot's G row and B entry, and the interface solve (I + G) u = B, on the
+12x12-subdomain / 43-knot Poisson workload (10,989 knots, 2e4 paths per knot,
+h = 5e-4) in the MIXED form (FP32 paths, FP64 accumulation, FP64 RBF
+factorisation, FP32 GMRES under FP64 refinement) with the per-knot adaptive
+step and the Richardson pair (h/2, h) that bring the interface RMSE under
+2e-3.  The same step without them (the reference's plain method) and the
+plain FP64 GPU form are measured beside it.
 
   value  path-steps/s of the device-timed step (inputs resident in HBM),
          CUDA events on the library's stream, L2 flushed between steps
@@ -163,15 +166,10 @@ def run_reference(args, workload, fac):
     print(json.dumps(line), flush=True)
 
 
-def contraction_fma(pd) -> int:
-    """FMAs of the G contraction per knot summed over knots (sum over sides of n * nbins)."""
-    return int(pd.layout_info.get("_contraction_fma", 0))
-
-
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="poisson_12x12_n43")
@@ -211,9 +209,13 @@ def main():
     exact = bvp.u(pd.x, pd.y)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
-    def step(instance):
-        est = pd.estimate(bvp, N, h, mode=P.MODE_MIXED, seed=1234, instance=instance)
-        u, sinfo = pd.solve_interface(P.SOLVE_GMRES_FP32_IR, tol=1e-10)
+    OPTS = dict(adaptive_h=True, richardson=True)
+
+    def step(instance, mode=P.MODE_MIXED, method=P.SOLVE_GMRES_FP32_IR, **opts):
+        o = dict(OPTS)
+        o.update(opts)
+        est = pd.estimate(bvp, N, h, mode=mode, seed=1234, instance=instance, **o)
+        u, sinfo = pd.solve_interface(method, tol=1e-10)
         return est, u, sinfo
 
     for w in range(args.warmup):
@@ -252,13 +254,18 @@ def main():
     value = steps_all / t_dev
 
     extra = {}
+    # the reference's plain method (no adaptive step, no extrapolation), MIXED
+    if rank == 0:
+        estp, up, sp = step(999, adaptive_h=False, richardson=False)
+        tp = (estp.info["ms_setup"] + estp.info["ms_paths"] + sp["ms"]) / 1000.0
+        extra["plain_method"] = {"path_steps_per_s": estp.info["path_steps"] / tp, "ms_per_step": 1000 * tp,
+                                 "path_steps": estp.info["path_steps"],
+                                 "rmse_vs_analytic": float(np.sqrt(np.mean((up - exact) ** 2)))}
     # plain FP64 GPU form on the same workload (the >= 3x comparison)
     if not args.no_fp64 and rank == 0:
-        est64 = pd.estimate(bvp, N, h, mode=P.MODE_FP64, seed=1234, instance=7)
-        u64, s64 = pd.solve_interface(P.SOLVE_BICGSTAB_FP64, tol=1e-10)
+        est64, u64, s64 = step(7, mode=P.MODE_FP64, method=P.SOLVE_BICGSTAB_FP64)
         t64 = (est64.info["ms_setup"] + est64.info["ms_paths"] + s64["ms"]) / 1000.0
-        estm = pd.estimate(bvp, N, h, mode=P.MODE_MIXED, seed=1234, instance=7)
-        um, sm = pd.solve_interface(P.SOLVE_GMRES_FP32_IR, tol=1e-10)
+        estm, um, sm = step(7)
         extra["fp64"] = {
             "path_steps_per_s": est64.info["path_steps"] / t64,
             "ms_per_step": 1000 * t64,
@@ -281,7 +288,7 @@ def main():
         for s in range(max(1, min(args.steps, 3))):
             with P.PDDSparseGM(workload["sw"], workload["ne"], workload["nsub"], workload["nnode"], fac,
                                device=local) as q:
-                u2, est2, si2 = q.Solve(bvp, N, h, mode=P.MODE_MIXED, seed=1234, instance=50 + s)
+                u2, est2, si2 = q.Solve(bvp, N, h, mode=P.MODE_MIXED, seed=1234, instance=50 + s, **OPTS)
                 e2e_steps += est2.info["path_steps"]
                 K, nnz = q.K, q.nnz
         dt = time.perf_counter() - t0
@@ -305,21 +312,20 @@ def main():
     f_mhz = clk.get("sm_mhz") or 1920.0
     peak = sm_count * 4 * 32 * f_mhz * 1e6  # thread-instructions per second
     t_paths = sum(ms_paths) / 1000.0
-    contr = pd.layout_info.get("nnz", 0)  # placeholder replaced below
     work = steps_done * W_STEP + exits * W_EXIT
     achieved = work / t_paths if t_paths > 0 else 0.0
     roof = {"bound": "issue", "achieved": achieved / 1e9, "peak": peak / 1e9, "unit": "Ginst/s",
             "frac": achieved / peak, "traffic": None,
             "peak_source": f"{sm_count} SMs x 128 issue lanes x median SM clock {f_mhz:.0f} MHz under load",
             "kernel": "k_paths_mixed", "kernel_ms_per_launch": 1000 * t_paths / args.steps}
-    del contr
 
     line = {
         "metric": METRIC, "value": value, "unit": "path-steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000 * t_dev / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
         "config": {"workload": workload["name"], "knots": pd.K, "paths_per_knot": N, "h": h,
-                   "mode": "MIXED", "solver": "GMRES(30) FP32 + FP64 refinement", "l2": "flushed (256 MB write)"},
+                   "mode": "MIXED", "adaptive_h": True, "richardson": "h/2,h",
+                   "solver": "GMRES(30) FP32 + FP64 refinement", "l2": "flushed (256 MB write)"},
         "interface_solves_per_s": args.steps / t_dev,
         "rmse_vs_analytic": float(np.mean(rmses)),
         "solve_ms": float(np.mean(solve_ms)),

@@ -125,6 +125,19 @@ typedef struct {
    * (j,i) = ipsi(j,i) of the reference; NULL = factorise on the device. */
   const double* ipsi_override;
   int64_t ipsi_override_len;
+  /* 1: per-knot step h_k = min(h, (d_k / (2 * 0.5826 * |N^T sigma(x_k)|))^2) for
+   * knots at distance d_k <= -1e-4 inside their stencil, the adaptive step of
+   * the reference's iterative solvers (PDDSparseGM.cpp:4026-4028) */
+  int32_t adaptive_h;
+  /* MIXED and FP64 only, 1: Richardson extrapolation in the step.  Every path
+   * is a pair driven by one Brownian motion, a fine level of step h/2 and a
+   * coarse level of step h; G and B estimate 2 E[fine] - E[coarse], which
+   * cancels the O(h) bias of the Gobet-shifted scheme.  Both levels' steps
+   * count as path steps.  G_var then omits the fine/coarse covariance. */
+  int32_t richardson;
+  /* 1: keep the RBF factorisation and tables of the previous call on this
+   * layout (they depend only on the layout and bins_per_gap); 0: recompute */
+  int32_t reuse_tables;
 } pdds_estimate_desc;
 
 typedef struct {

@@ -40,6 +40,7 @@ class Params(C.Structure):
         ("threads", C.c_int),
         ("fac", C.c_double * 4),
         ("max_steps", C.c_int64),
+        ("adaptive_h", C.c_int),
     ]
 
 
@@ -99,7 +100,7 @@ def make_problem(kind: int, *params: float) -> Problem:
 
 
 def make_params(N, h, seed=1234, fac=(1.0, 1.0, 1.0, 1.0), portable=False, sublinear=True,
-                dup_sum=False, threads=None, instance=0, max_steps=10**8) -> Params:
+                dup_sum=False, threads=None, instance=0, max_steps=10**8, adaptive_h=False) -> Params:
     prm = Params()
     prm.N = int(N)
     prm.h = float(h)
@@ -112,6 +113,7 @@ def make_params(N, h, seed=1234, fac=(1.0, 1.0, 1.0, 1.0), portable=False, subli
     for i in range(4):
         prm.fac[i] = float(fac[i])
     prm.max_steps = int(max_steps)
+    prm.adaptive_h = int(bool(adaptive_h))
     return prm
 
 

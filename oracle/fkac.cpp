@@ -17,6 +17,7 @@
 // replaced by Philox-4x32-10 + Box-Muller (pdds_portable.h), keyed by
 // (seed, instance, knot, path, step pair), so runs are reproducible.
 #include <cmath>
+#include <algorithm>
 #include <cstring>
 #include <limits>
 #include <map>
@@ -401,7 +402,21 @@ int knot_impl(const Layout& L, const orc_problem* P, const orc_params* prm, int 
     return status;
   }
   const int N = prm->N;
-  const double h = prm->h, sqrth = std::sqrt(h);
+  double h = prm->h;
+  if (prm->adaptive_h) {
+    // adaptive step of the reference's iterative solvers (PDDSparseGM.cpp:4026-4028)
+    const double d = rect2d(st.params, x0, y0, E, Nn);
+    if (d <= -1E-04) {
+      Coef k0;
+      pb.coef(x0, y0, k0);
+      const double w0 = Nn[0] * k0.s[0] + Nn[1] * k0.s[2];
+      const double w1 = Nn[0] * k0.s[1] + Nn[1] * k0.s[3];
+      const double q = d / (std::sqrt(w0 * w0 + w1 * w1) * 2 * 0.5826);
+      const double ha = q * q;
+      h = std::min(h, ha);
+    }
+  }
+  const double sqrth = std::sqrt(h);
   std::vector<PathOut> paths(N);
 #if defined(_OPENMP)
 #pragma omp parallel for schedule(static) num_threads(prm->threads > 0 ? prm->threads : 1)

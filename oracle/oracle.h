@@ -34,6 +34,7 @@ typedef struct {
   int threads;         /* OpenMP threads for the path loop                      */
   double fac[4];       /* RBF shape c per side kind (c2[kind] in the reference) */
   int64_t max_steps;   /* per path, per leg; exceeded -> status 3               */
+  int adaptive_h;      /* 1: per-knot h of PDDSparseGM.cpp:4026-4028             */
 } orc_params;
 
 /* ---- layout ---------------------------------------------------------------*/

@@ -49,7 +49,8 @@ class EstimateDesc(C.Structure):
     _fields_ = [("mode", C.c_int32), ("npaths", C.c_int32), ("h", C.c_double), ("seed", C.c_uint64),
                 ("instance", C.c_uint32), ("dup_sum", C.c_int32), ("want_var", C.c_int32),
                 ("bins_per_gap", C.c_int32), ("max_steps", C.c_int64),
-                ("ipsi_override", C.POINTER(C.c_double)), ("ipsi_override_len", C.c_int64)]
+                ("ipsi_override", C.POINTER(C.c_double)), ("ipsi_override_len", C.c_int64),
+                ("adaptive_h", C.c_int32), ("richardson", C.c_int32), ("reuse_tables", C.c_int32)]
 
 
 class EstimateInfo(C.Structure):

@@ -219,7 +219,8 @@ class PDDSparseGM:
 
     def estimate(self, bvp: BVP, npaths: int, h: float, mode: int = capi.MODE_MIXED, seed: int = 1234,
                  instance: int = 0, dup_sum: bool = False, want_var: bool = False,
-                 bins_per_gap: int = 0, max_steps: int = 0, ipsi_override=None) -> Estimate:
+                 bins_per_gap: int = 0, max_steps: int = 0, ipsi_override=None,
+                 adaptive_h: bool = False, richardson: bool = False, reuse_tables: bool = False) -> Estimate:
         """Runs the Feynman-Kac estimation of every knot's G row and B entry."""
         self._check(self._lib.pdds_problem_set(self._ctx, C.byref(bvp.desc())))
         d = capi.EstimateDesc()
@@ -232,6 +233,9 @@ class PDDSparseGM:
         d.want_var = int(bool(want_var))
         d.bins_per_gap = int(bins_per_gap)
         d.max_steps = int(max_steps)
+        d.adaptive_h = int(bool(adaptive_h))
+        d.richardson = int(bool(richardson))
+        d.reuse_tables = int(bool(reuse_tables))
         keep = None
         if ipsi_override is not None:
             keep = np.ascontiguousarray(ipsi_override, np.float64)

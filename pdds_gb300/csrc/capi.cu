@@ -395,6 +395,8 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
   if (desc->npaths < 1 || !(desc->h > 0.0)) return fail(ctx, PDDS_ERR_INVALID, "npaths >= 1 and h > 0 required");
   const int mode = desc->mode;
   if (mode < 0 || mode > 2) return fail(ctx, PDDS_ERR_INVALID, "unknown mode");
+  if (mode == PDDS_MODE_REPLAY_FP64 && desc->richardson)
+    return fail(ctx, PDDS_ERR_INVALID, "the replay mode follows the reference and has no Richardson form");
   if (mode == PDDS_MODE_REPLAY_FP64 && ctx->prob.kind == PDDS_MONEGROS)
     return fail(ctx, PDDS_ERR_INVALID, "the Monegros problem has no replay form");
   CK(cudaSetDevice(ctx->device));
@@ -416,7 +418,7 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
   CK(cudaMemsetAsync(ctx->errf.p, 0, sizeof(unsigned), s));
   CK(cudaMemsetAsync(ctx->stats.p, 0, 8 * sizeof(unsigned long long), s));
   const bool need_ipsi = !(mode == PDDS_MODE_REPLAY_FP64 && desc->ipsi_override);
-  if (need_ipsi && !ctx->tables_ready) {
+  if (need_ipsi && (!ctx->tables_ready || !desc->reuse_tables)) {
     int max_n = 0;
     for (auto& sh : L.shapes) max_n = std::max(max_n, sh.n);
     CK(launch_rbf_setup(ctx->dl, max_n, ctx->max_nbins, ctx->ipsi.p, ctx->tab.p, ctx->errf.p, s));
@@ -486,6 +488,7 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
     a.seed = desc->seed;
     a.instance = desc->instance;
     a.sublinear = 1;
+    a.adaptive_h = desc->adaptive_h ? 1 : 0;
     a.max_steps = max_steps;
     a.mc_knots = ctx->mc_knots.p;
     a.n_mc = n_mc;
@@ -542,6 +545,9 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
       a.n_items = n_items;
       a.want_var = desc->want_var ? 1 : 0;
       a.dup_sum = desc->dup_sum;
+      a.adaptive_h = desc->adaptive_h ? 1 : 0;
+      a.richardson = desc->richardson ? 1 : 0;
+      a.h64 = desc->h;
       a.max_steps = max_steps;
       a.mc_knots = ctx->mc_knots.p;
       a.item_counter = ctx->counter.p;
@@ -553,7 +559,7 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
       a.err_flags = ctx->errf.p;
       const size_t smem = ctx->mixed_smem * (a.want_var ? 2 : 1);
       if (smem > 200 * 1024) return fail(ctx, PDDS_ERR_INVALID, "exit histograms exceed shared memory; lower bins_per_gap");
-      int bps = mixed_blocks_per_sm(P.kind, smem);
+      int bps = mixed_blocks_per_sm(P.kind, smem, a.richardson);
       if (bps < 1) bps = 1;
       const int grid = std::max(1, std::min(n_items, bps * ctx->num_sms));
       if (n_items > 0) {
@@ -574,6 +580,8 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
       a.paths_per_chunk = ppc;
       a.n_items = n_items;
       a.dup_sum = desc->dup_sum;
+      a.adaptive_h = desc->adaptive_h ? 1 : 0;
+      a.richardson = desc->richardson ? 1 : 0;
       a.max_steps = max_steps;
       a.mc_knots = ctx->mc_knots.p;
       a.item_counter = ctx->counter.p;
@@ -585,7 +593,7 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
       const size_t smem = ctx->fp64_smem;
       cudaFuncAttributes fa;
       (void)fa;
-      int bps = fp64_blocks_per_sm(P.kind, smem);
+      int bps = fp64_blocks_per_sm(P.kind, smem, a.richardson);
       if (bps < 1) bps = 1;
       const int grid = std::max(1, std::min(n_items, bps * ctx->num_sms));
       if (n_items > 0) {

@@ -257,6 +257,22 @@ __device__ __forceinline__ T rect2d(const T* p, T x, T y, T& Ex, T& Ey, T& Nx, T
   return d1 - h1;
 }
 
+// Adaptive step of a knot (PDDSparseGM.cpp:4026-4028):
+// h_k = min(h0, (d / (|N^T sigma(x0)| * 2 * 0.5826))^2) when d <= -1e-4.
+template <typename T>
+__device__ __forceinline__ double adaptive_step(const double* rect, double x0, double y0, double h0,
+                                                const Coef<T>& k) {
+  double Ex, Ey, Nx, Ny;
+  int om;
+  const double d = rect2d<double>(rect, x0, y0, Ex, Ey, Nx, Ny, om);
+  if (!(d <= -1e-04)) return h0;
+  const double w0 = Nx * (double)k.s00 + Ny * (double)k.s10;
+  const double w1 = Nx * (double)k.s01 + Ny * (double)k.s11;
+  const double q = d / (sqrt(w0 * w0 + w1 * w1) * 2 * 0.5826);
+  const double ha = q * q;
+  return h0 < ha ? h0 : ha;
+}
+
 // Exit side by the reference's priority S, N, W, E (G_update, stencil.cpp:246-301).
 __device__ __forceinline__ int exit_side(int onmask) {
   if (onmask & (1 << 1)) return 1;  // S

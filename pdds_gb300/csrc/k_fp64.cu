@@ -29,19 +29,35 @@ struct ItemSide64 {
 
 constexpr unsigned FULL = 0xffffffffu;
 
-template <int KIND>
+struct Lvl64 {
+  double x, y, Y, Z, xi;
+  Coef<double> k;
+  unsigned steps;
+};
+
+// Box-Muller in FP64: z0 = rho cos(2 pi u1), z1 = rho sin(2 pi u1).
+__device__ __forceinline__ void normals_f64(uint32_t ua, uint32_t ub, double& z0, double& z1) {
+  const double u0 = u01_fp64(ua), u1 = u01_fp64(ub);
+  const double rho = ::sqrt(-2.0 * ::log(u0));
+  double sn, cs;
+  sincospi(2.0 * u1, &sn, &cs);
+  z0 = rho * cs;
+  z1 = rho * sn;
+}
+
+template <int KIND, bool RICH>
 __global__ void __launch_bounds__(FP64_THREADS)
 k_paths_fp64(const Fp64Args a) {
   extern __shared__ double Ssum[];  // [sum n] per-side RBF sums, then [sum n] local t
   __shared__ ItemSide64 s_side[4];
   __shared__ double s_rect[4];
   __shared__ int s_item, s_knot, s_path_end, s_nall;
+  __shared__ double s_h;
   __shared__ unsigned s_next_path;
   __shared__ double s_red[FP64_THREADS / 32][2];
   __shared__ unsigned long long s_redi[FP64_THREADS / 32][3];
   const DevLayout& L = a.L;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const double h = a.h, sqrth = a.sqrth;
 
   for (;;) {
     if (tid == 0) s_item = atomicAdd(a.item_counter, 1);
@@ -57,6 +73,12 @@ k_paths_fp64(const Fp64Args a) {
       s_next_path = (unsigned)(p0 + FP64_THREADS);
       const int st = L.knot_stencil[k];
       for (int q = 0; q < 4; q++) s_rect[q] = L.st_rect[4 * st + q];
+      s_h = a.h;
+      if (a.adaptive_h) {
+        Coef<double> kd;
+        coef_f64<KIND>(a.P, L.kx[k], L.ky[k], kd);
+        s_h = adaptive_step<double>(L.st_rect + 4 * st, L.kx[k], L.ky[k], a.h, kd);
+      }
       int off = 0;
       int64_t moff = L.st_map_off[st];
       for (int d = 0; d < 4; d++) {
@@ -86,6 +108,7 @@ k_paths_fp64(const Fp64Args a) {
     }
     __syncthreads();
     const int knot = s_knot, path_end = s_path_end, nall = s_nall;
+    const double h = s_h, sqrth = ::sqrt(s_h);
     double* tloc = Ssum + nall;
     for (int i = tid; i < nall; i += FP64_THREADS) Ssum[i] = 0.0;
     for (int d = 0; d < 4; d++)
@@ -100,72 +123,102 @@ k_paths_fp64(const Fp64Args a) {
     const int chunk = item % a.chunks;
     unsigned path = (unsigned)(chunk * a.paths_per_chunk + tid);
     bool active = (int)path < path_end;
-    double x = x0, y = y0, Y = 1.0, Z = 0.0, xi = 0.0;
-    Coef<double> k = k0;
-    unsigned step = 0;
-    u32x4 blk;
-    blk.v[0] = blk.v[1] = blk.v[2] = blk.v[3] = 0;
     double b = 0.0, bb = 0.0;
     unsigned long long nsteps = 0, nglob = 0, nsten = 0;
-    while (__any_sync(FULL, active)) {
-      if (!active) continue;
-      if ((step & 1u) == 0) blk = path_block(a.seed, a.instance, (uint32_t)knot, path, step >> 1);
-      const uint32_t ua = (step & 1u) ? blk.v[2] : blk.v[0];
-      const uint32_t ub = (step & 1u) ? blk.v[3] : blk.v[1];
-      const double u0 = u01_fp64(ua), u1 = u01_fp64(ub);
-      const double rho = ::sqrt(-2.0 * ::log(u0));
-      double sn, cs;
-      sincospi(2.0 * u1, &sn, &cs);
-      const double i0 = sqrth * (rho * cs), i1 = sqrth * (rho * sn);
-      const double v0 = -(k.s00 * k.g0 + k.s10 * k.g1);
-      const double v1 = -(k.s01 * k.g0 + k.s11 * k.g1);
-      xi += Y * (v0 * i0 + v1 * i1);
-      Z += k.f * Y * h;
-      Y += k.c * Y * h;
-      x += k.b0 * h + (k.s00 * i0 + k.s01 * i1);
-      y += k.b1 * h + (k.s10 * i0 + k.s11 * i1);
-      ++step;
-      coef_f64<KIND>(a.P, x, y, k);
+    auto exit_level = [&](const Lvl64& s, double wgt, double Ex, double Ey, int onmask) -> double {
+      const int d = exit_side(onmask);
+      const bool glob = ((onmask & 1) && s_side[0].glob) || ((onmask & 2) && s_side[1].glob) ||
+                        ((onmask & 4) && s_side[2].glob) || ((onmask & 8) && s_side[3].glob);
+      if (glob) {
+        ++nglob;
+        return s.Z + s.Y * u_f64<KIND>(a.P, Ex, Ey) + s.xi;
+      }
+      ++nsten;
+      if (d < 0) {
+        atomicOr(a.err_flags, ERR_FLAG_EXIT_SIDE);
+      } else {
+        const ItemSide64& is = s_side[d];
+        const double sc = (is.orient == 0 ? Ex : Ey) - is.origin;
+        const double yw = wgt * s.Y;
+        for (int j = 0; j < is.n; j++) {
+          const double dt = tloc[is.s_off + j] - sc;
+          atomicAdd(Ssum + is.s_off + j, yw * ::exp(-(dt * dt) * is.inv_c2));
+        }
+      }
+      return s.Z + s.xi;
+    };
+    auto step_level = [&](Lvl64& s, double i0, double i1, double hh, double sq, double wgt,
+                          double& val) -> bool {
+      const double v0 = -(s.k.s00 * s.k.g0 + s.k.s10 * s.k.g1);
+      const double v1 = -(s.k.s01 * s.k.g0 + s.k.s11 * s.k.g1);
+      s.xi += s.Y * (v0 * i0 + v1 * i1);
+      s.Z += s.k.f * s.Y * hh;
+      s.Y += s.k.c * s.Y * hh;
+      s.x += s.k.b0 * hh + (s.k.s00 * i0 + s.k.s01 * i1);
+      s.y += s.k.b1 * hh + (s.k.s10 * i0 + s.k.s11 * i1);
+      ++s.steps;
+      coef_f64<KIND>(a.P, s.x, s.y, s.k);
       double Ex, Ey, Nx, Ny;
       int onmask;
-      const double dist = rect2d<double>(rect, x, y, Ex, Ey, Nx, Ny, onmask);
-      const double w0 = Nx * k.s00 + Ny * k.s10, w1 = Nx * k.s01 + Ny * k.s11;
-      const double thr = -0.5826 * ::sqrt(w0 * w0 + w1 * w1) * sqrth;
-      const bool capped = step >= (unsigned)a.max_steps;
-      if (dist < thr && !capped) continue;
-      nsteps += step;
-      if (capped && dist < thr) {
+      const double dist = rect2d<double>(rect, s.x, s.y, Ex, Ey, Nx, Ny, onmask);
+      const double w0 = Nx * s.k.s00 + Ny * s.k.s10, w1 = Nx * s.k.s01 + Ny * s.k.s11;
+      const double thr = -0.5826 * ::sqrt(w0 * w0 + w1 * w1) * sq;
+      if (dist < thr) {
+        if (s.steps < (unsigned)a.max_steps) return false;
         atomicOr(a.err_flags, ERR_FLAG_STEP_LIMIT);
+        val = 0.0;
+        return true;
+      }
+      val = exit_level(s, wgt, Ex, Ey, onmask);
+      return true;
+    };
+    Lvl64 fine, coarse;
+    auto reset = [&]() {
+      fine.x = x0; fine.y = y0; fine.Y = 1.0; fine.Z = 0.0; fine.xi = 0.0; fine.k = k0; fine.steps = 0;
+      coarse = fine;
+    };
+    reset();
+    bool fine_alive = active, coarse_alive = RICH && active;
+    double val_f = 0.0, val_c = 0.0;
+    unsigned m = 0;
+    u32x4 blk;
+    blk.v[0] = blk.v[1] = blk.v[2] = blk.v[3] = 0;
+    while (__any_sync(FULL, active)) {
+      if (!active) continue;
+      if (RICH) {
+        blk = path_block(a.seed, a.instance, (uint32_t)knot, path, m++);
+        double za0, za1, zb0, zb1;
+        normals_f64(blk.v[0], blk.v[1], za0, za1);
+        normals_f64(blk.v[2], blk.v[3], zb0, zb1);
+        const double hf = 0.5 * h, sqf = ::sqrt(hf);
+        if (fine_alive) fine_alive = !step_level(fine, sqf * za0, sqf * za1, hf, sqf, 2.0, val_f);
+        if (fine_alive) fine_alive = !step_level(fine, sqf * zb0, sqf * zb1, hf, sqf, 2.0, val_f);
+        if (coarse_alive)
+          coarse_alive = !step_level(coarse, sqf * (za0 + zb0), sqf * (za1 + zb1), h, sqrth, -1.0, val_c);
+        if (fine_alive || coarse_alive) continue;
+        const double v = 2.0 * val_f - val_c;
+        b += v;
+        bb += v * v;
+        nsteps += fine.steps + coarse.steps;
       } else {
-        const int d = exit_side(onmask);
-        const bool glob = ((onmask & 1) && s_side[0].glob) || ((onmask & 2) && s_side[1].glob) ||
-                          ((onmask & 4) && s_side[2].glob) || ((onmask & 8) && s_side[3].glob);
-        double val;
-        if (glob) {
-          val = Z + Y * u_f64<KIND>(a.P, Ex, Ey) + xi;
-          ++nglob;
-        } else {
-          val = Z + xi;
-          ++nsten;
-          if (d < 0) {
-            atomicOr(a.err_flags, ERR_FLAG_EXIT_SIDE);
-          } else {
-            const ItemSide64& is = s_side[d];
-            const double s = (is.orient == 0 ? Ex : Ey) - is.origin;
-            for (int j = 0; j < is.n; j++) {
-              const double dt = tloc[is.s_off + j] - s;
-              atomicAdd(Ssum + is.s_off + j, Y * ::exp(-(dt * dt) * is.inv_c2));
-            }
-          }
-        }
-        b += val;
-        bb += val * val;
+        if ((m & 1u) == 0) blk = path_block(a.seed, a.instance, (uint32_t)knot, path, m >> 1);
+        double z0, z1;
+        if (m & 1u) normals_f64(blk.v[2], blk.v[3], z0, z1);
+        else normals_f64(blk.v[0], blk.v[1], z0, z1);
+        ++m;
+        if (!step_level(fine, sqrth * z0, sqrth * z1, h, sqrth, 1.0, val_f)) continue;
+        b += val_f;
+        bb += val_f * val_f;
+        nsteps += fine.steps;
       }
       path = atomicAdd(&s_next_path, 1u);
       if ((int)path >= path_end) {
         active = false;
       } else {
-        x = x0; y = y0; Y = 1.0; Z = 0.0; xi = 0.0; step = 0; k = k0;
+        reset();
+        fine_alive = true;
+        coarse_alive = RICH;
+        m = 0;
       }
     }
 #pragma unroll
@@ -216,13 +269,13 @@ k_paths_fp64(const Fp64Args a) {
 
 }  // namespace
 
-#define PDDS_FP64_CASE(KK)                                                                        \
-  case KK:                                                                                        \
-    cudaFuncSetAttribute(k_paths_fp64<KK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
-    k_paths_fp64<KK><<<grid, FP64_THREADS, smem, s>>>(a);                                         \
+template <bool RICH>
+static cudaError_t launch_fp64_t(const Fp64Args& a, int kind, int grid, size_t smem, cudaStream_t s) {
+#define PDDS_FP64_CASE(KK)                                                                           \
+  case KK:                                                                                           \
+    cudaFuncSetAttribute(k_paths_fp64<KK, RICH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+    k_paths_fp64<KK, RICH><<<grid, FP64_THREADS, smem, s>>>(a);                                      \
     break;
-
-cudaError_t launch_paths_fp64(const Fp64Args& a, int kind, int grid, size_t smem, cudaStream_t s) {
   switch (kind) {
     PDDS_FP64_CASE(0)
     PDDS_FP64_CASE(1)
@@ -230,18 +283,28 @@ cudaError_t launch_paths_fp64(const Fp64Args& a, int kind, int grid, size_t smem
     PDDS_FP64_CASE(3)
     default: return cudaErrorInvalidValue;
   }
+#undef PDDS_FP64_CASE
   return cudaGetLastError();
 }
 
-int fp64_blocks_per_sm(int kind, size_t smem) {
+cudaError_t launch_paths_fp64(const Fp64Args& a, int kind, int grid, size_t smem, cudaStream_t s) {
+  return a.richardson ? launch_fp64_t<true>(a, kind, grid, smem, s) : launch_fp64_t<false>(a, kind, grid, smem, s);
+}
+
+template <bool RICH>
+static int blocks64_t(int kind, size_t smem) {
   int nb = 0;
   switch (kind) {
-    case 0: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_paths_fp64<0>, FP64_THREADS, smem); break;
-    case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_paths_fp64<1>, FP64_THREADS, smem); break;
-    case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_paths_fp64<2>, FP64_THREADS, smem); break;
-    default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_paths_fp64<3>, FP64_THREADS, smem); break;
+    case 0: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_paths_fp64<0, RICH>, FP64_THREADS, smem); break;
+    case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_paths_fp64<1, RICH>, FP64_THREADS, smem); break;
+    case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_paths_fp64<2, RICH>, FP64_THREADS, smem); break;
+    default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_paths_fp64<3, RICH>, FP64_THREADS, smem); break;
   }
   return nb;
+}
+
+int fp64_blocks_per_sm(int kind, size_t smem, int richardson) {
+  return richardson ? blocks64_t<true>(kind, smem) : blocks64_t<false>(kind, smem);
 }
 
 }  // namespace pdds

@@ -34,19 +34,38 @@ struct ItemSide {
 
 constexpr unsigned FULL = 0xffffffffu;
 
-template <int KIND>
+struct Lvl {
+  float x, y, Y, Z, xi;
+  Coef<float> k;
+  unsigned steps;
+};
+
+// Box-Muller in FP32 from two Philox words: z0 = rho cos(2 pi u1),
+// z1 = rho sin(2 pi u1), evaluated as -rho cos/sin(2 pi u1 - pi) so the fast
+// intrinsics see an argument in [-pi, pi).
+__device__ __forceinline__ void normals_f32(uint32_t ua, uint32_t ub, float& z0, float& z1) {
+  const float u0 = fmaf((float)ua, 2.3283064e-10f, 1.1641532e-10f);
+  const float u1 = fmaf((float)ub, 2.3283064e-10f, 1.1641532e-10f);
+  const float rho = sqrtf(-2.f * __logf(u0));
+  float sn, cs;
+  __sincosf(6.28318531f * (u1 - 0.5f), &sn, &cs);
+  z0 = -rho * cs;
+  z1 = -rho * sn;
+}
+
+template <int KIND, bool RICH>
 __global__ void __launch_bounds__(MIXED_THREADS)
 k_paths_mixed(const MixedArgs a) {
   extern __shared__ float hist[];  // [sum nbins] (and the Y^2 histogram after it)
   __shared__ ItemSide s_side[4];
   __shared__ float s_rect[4];
   __shared__ int s_item, s_knot, s_path_end, s_hist_len;
+  __shared__ float s_h, s_sqrth;
   __shared__ unsigned s_next_path;
   __shared__ double s_red[MIXED_THREADS / 32][4];
   __shared__ unsigned long long s_redi[MIXED_THREADS / 32][3];
   const DevLayout& L = a.L;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const float h = a.h, sqrth = a.sqrth;
 
   for (;;) {
     if (tid == 0) s_item = atomicAdd(a.item_counter, 1);
@@ -62,6 +81,15 @@ k_paths_mixed(const MixedArgs a) {
       s_next_path = (unsigned)(p0 + MIXED_THREADS);
       const int st = L.knot_stencil[k];
       for (int q = 0; q < 4; q++) s_rect[q] = (float)L.st_rect[4 * st + q];
+      s_h = a.h;
+      s_sqrth = a.sqrth;
+      if (a.adaptive_h) {
+        Coef<double> kd;
+        coef_f64<KIND>(a.P, L.kx[k], L.ky[k], kd);
+        const double hk = adaptive_step<double>(L.st_rect + 4 * st, L.kx[k], L.ky[k], a.h64, kd);
+        s_h = (float)hk;
+        s_sqrth = (float)sqrt(hk);
+      }
       int off = 0;
       for (int d = 0; d < 4; d++) {
         const int sd = L.st_side[4 * st + d];
@@ -94,6 +122,7 @@ k_paths_mixed(const MixedArgs a) {
     }
     __syncthreads();
     const int knot = s_knot, path_end = s_path_end, hist_len = s_hist_len;
+    const float h = s_h, sqrth = s_sqrth;
     const int nh = a.want_var ? 2 * hist_len : hist_len;
     for (int i = tid; i < nh; i += MIXED_THREADS) hist[i] = 0.f;
     float* hist2 = hist + hist_len;
@@ -107,90 +136,122 @@ k_paths_mixed(const MixedArgs a) {
     const int chunk = item % a.chunks;
     unsigned path = (unsigned)(chunk * a.paths_per_chunk + tid);
     bool active = (int)path < path_end;
-    float x = x0, y = y0, Y = 1.f, Z = 0.f, xi = 0.f;
-    Coef<float> k = k0;
-    unsigned step = 0;
-    u32x4 blk;
-    blk.v[0] = blk.v[1] = blk.v[2] = blk.v[3] = 0;
     double b = 0.0, bb = 0.0;
     unsigned long long nsteps = 0, nglob = 0, nsten = 0;
-    while (__any_sync(FULL, active)) {
-      if (!active) continue;
-      // Step, control-variate variant (FKACIntegrator.hpp:46-57)
-      if ((step & 1u) == 0) blk = path_block(a.seed, a.instance, (uint32_t)knot, path, step >> 1);
-      const uint32_t ua = (step & 1u) ? blk.v[2] : blk.v[0];
-      const uint32_t ub = (step & 1u) ? blk.v[3] : blk.v[1];
-      const float u0 = fmaf((float)ua, 2.3283064e-10f, 1.1641532e-10f);
-      const float u1 = fmaf((float)ub, 2.3283064e-10f, 1.1641532e-10f);
-      const float rho = sqrtf(-2.f * __logf(u0));
-      float sn, cs;
-      __sincosf(6.28318531f * (u1 - 0.5f), &sn, &cs);  // angle 2 pi u1 - pi
-      const float i0 = -rho * cs * sqrth, i1 = -rho * sn * sqrth;
-      const float v0 = -(k.s00 * k.g0 + k.s10 * k.g1);
-      const float v1 = -(k.s01 * k.g0 + k.s11 * k.g1);
-      xi += Y * (v0 * i0 + v1 * i1);
-      Z += k.f * Y * h;
-      Y += k.c * Y * h;
-      x += k.b0 * h + (k.s00 * i0 + k.s01 * i1);
-      y += k.b1 * h + (k.s10 * i0 + k.s11 * i1);
-      ++step;
-      // Inside with the Gobet-Menozzi shift (FKACIntegrator.hpp:168-222)
-      coef_f32<KIND>(a.P, x, y, k);
-      float Ex, Ey, Nx, Ny;
-      int onmask;
-      const float dist = rect2d<float>(rect, x, y, Ex, Ey, Nx, Ny, onmask);
-      const float w0 = Nx * k.s00 + Ny * k.s10, w1 = Nx * k.s01 + Ny * k.s11;
-      const float thr = -0.5826f * sqrtf(w0 * w0 + w1 * w1) * sqrth;
-      const bool capped = step >= (unsigned)a.max_steps;
-      if (dist < thr && !capped) continue;
-      // ---------------------------------------------------------- exit
-      nsteps += step;
-      if (capped && dist < thr) {
-        atomicOr(a.err_flags, ERR_FLAG_STEP_LIMIT);
+    // Exit of one level: B value, and the RBF deposit with weight wgt * Y.
+    auto exit_level = [&](const Lvl& s, float wgt, float Ex, float Ey, int onmask) -> float {
+      const int d = exit_side(onmask);
+      const bool glob = ((onmask & 1) && s_side[0].glob) || ((onmask & 2) && s_side[1].glob) ||
+                        ((onmask & 4) && s_side[2].glob) || ((onmask & 8) && s_side[3].glob);
+      if (glob) {
+        ++nglob;
+        return s.Z + s.Y * u_f32<KIND>(a.P, Ex, Ey) + s.xi;
+      }
+      ++nsten;
+      if (d < 0) {
+        atomicOr(a.err_flags, ERR_FLAG_EXIT_SIDE);
       } else {
-        const int d = exit_side(onmask);
-        const bool glob = ((onmask & 1) && s_side[0].glob) || ((onmask & 2) && s_side[1].glob) ||
-                          ((onmask & 4) && s_side[2].glob) || ((onmask & 8) && s_side[3].glob);
-        float val;
-        if (glob) {
-          val = Z + Y * u_f32<KIND>(a.P, Ex, Ey) + xi;
-          ++nglob;
-        } else {
-          val = Z + xi;
-          ++nsten;
-          if (d < 0) {
-            atomicOr(a.err_flags, ERR_FLAG_EXIT_SIDE);
-          } else {
-            const ItemSide& is = s_side[d];
-            if (is.n > 0) {
-              const float s = is.orient == 0 ? Ex : Ey;
-              const float u = (s - is.base) * is.inv_delta;
-              int b0 = (int)floorf(u);
-              b0 = max(1, min(b0, is.nbins - 3));
-              const float fu = u - (float)b0;
-              float w[4];
-              cubic_weights(fu, w[0], w[1], w[2], w[3]);
-              float* hp = hist + is.hist_off + b0 - 1;
+        const ItemSide& is = s_side[d];
+        if (is.n > 0) {
+          const float sc = is.orient == 0 ? Ex : Ey;
+          const float u = (sc - is.base) * is.inv_delta;
+          int b0 = (int)floorf(u);
+          b0 = max(1, min(b0, is.nbins - 3));
+          const float fu = u - (float)b0;
+          float w[4];
+          cubic_weights(fu, w[0], w[1], w[2], w[3]);
+          const float yw = wgt * s.Y;
+          float* hp = hist + is.hist_off + b0 - 1;
 #pragma unroll
-              for (int q = 0; q < 4; q++) atomicAdd(hp + q, Y * w[q]);
-              if (a.want_var) {
-                float* hq = hist2 + is.hist_off + b0 - 1;
-                const float y2 = Y * Y;
+          for (int q = 0; q < 4; q++) atomicAdd(hp + q, yw * w[q]);
+          if (a.want_var) {
+            float* hq = hist2 + is.hist_off + b0 - 1;
+            const float y2 = yw * yw;
 #pragma unroll
-                for (int q = 0; q < 4; q++) atomicAdd(hq + q, y2 * w[q]);
-              }
-            }
+            for (int q = 0; q < 4; q++) atomicAdd(hq + q, y2 * w[q]);
           }
         }
-        b += (double)val;
-        bb += (double)val * (double)val;
+      }
+      return s.Z + s.xi;
+    };
+    // One Euler-Maruyama step of a level (Step, control-variate variant,
+    // FKACIntegrator.hpp:46-57) and the Gobet-shifted exit test (Inside,
+    // :168-222).  Returns true when the level has exited (val set).
+    auto step_level = [&](Lvl& s, float i0, float i1, float hh, float sq, float wgt, float& val) -> bool {
+      const float v0 = -(s.k.s00 * s.k.g0 + s.k.s10 * s.k.g1);
+      const float v1 = -(s.k.s01 * s.k.g0 + s.k.s11 * s.k.g1);
+      s.xi += s.Y * (v0 * i0 + v1 * i1);
+      s.Z += s.k.f * s.Y * hh;
+      s.Y += s.k.c * s.Y * hh;
+      s.x += s.k.b0 * hh + (s.k.s00 * i0 + s.k.s01 * i1);
+      s.y += s.k.b1 * hh + (s.k.s10 * i0 + s.k.s11 * i1);
+      ++s.steps;
+      coef_f32<KIND>(a.P, s.x, s.y, s.k);
+      float Ex, Ey, Nx, Ny;
+      int onmask;
+      const float dist = rect2d<float>(rect, s.x, s.y, Ex, Ey, Nx, Ny, onmask);
+      const float w0 = Nx * s.k.s00 + Ny * s.k.s10, w1 = Nx * s.k.s01 + Ny * s.k.s11;
+      const float thr = -0.5826f * sqrtf(w0 * w0 + w1 * w1) * sq;
+      if (dist < thr) {
+        if (s.steps < (unsigned)a.max_steps) return false;
+        atomicOr(a.err_flags, ERR_FLAG_STEP_LIMIT);
+        val = 0.f;
+        return true;
+      }
+      val = exit_level(s, wgt, Ex, Ey, onmask);
+      return true;
+    };
+    Lvl fine, coarse;
+    auto reset = [&]() {
+      fine.x = x0; fine.y = y0; fine.Y = 1.f; fine.Z = 0.f; fine.xi = 0.f; fine.k = k0; fine.steps = 0;
+      coarse = fine;
+    };
+    reset();
+    bool fine_alive = active, coarse_alive = RICH && active;
+    float val_f = 0.f, val_c = 0.f;
+    unsigned m = 0;  // Philox block index of the path
+    u32x4 blk;
+    blk.v[0] = blk.v[1] = blk.v[2] = blk.v[3] = 0;
+    while (__any_sync(FULL, active)) {
+      if (!active) continue;
+      if (RICH) {
+        // Richardson pair: one coarse step of h and two fine steps of h/2 on
+        // the same Brownian increments (dW_coarse = dW_fine1 + dW_fine2);
+        // the estimator 2 E[fine] - E[coarse] cancels the O(h) bias
+        blk = path_block(a.seed, a.instance, (uint32_t)knot, path, m++);
+        float za0, za1, zb0, zb1;
+        normals_f32(blk.v[0], blk.v[1], za0, za1);
+        normals_f32(blk.v[2], blk.v[3], zb0, zb1);
+        const float hf = 0.5f * h, sqf = sqrth * 0.70710678f;
+        if (fine_alive) fine_alive = !step_level(fine, sqf * za0, sqf * za1, hf, sqf, 2.f, val_f);
+        if (fine_alive) fine_alive = !step_level(fine, sqf * zb0, sqf * zb1, hf, sqf, 2.f, val_f);
+        if (coarse_alive)
+          coarse_alive = !step_level(coarse, sqf * (za0 + zb0), sqf * (za1 + zb1), h, sqrth, -1.f, val_c);
+        if (fine_alive || coarse_alive) continue;
+        const double v = 2.0 * (double)val_f - (double)val_c;
+        b += v;
+        bb += v * v;
+        nsteps += fine.steps + coarse.steps;
+      } else {
+        if ((m & 1u) == 0) blk = path_block(a.seed, a.instance, (uint32_t)knot, path, m >> 1);
+        float z0, z1;
+        if (m & 1u) normals_f32(blk.v[2], blk.v[3], z0, z1);
+        else normals_f32(blk.v[0], blk.v[1], z0, z1);
+        ++m;
+        if (!step_level(fine, sqrth * z0, sqrth * z1, h, sqrth, 1.f, val_f)) continue;
+        b += (double)val_f;
+        bb += (double)val_f * (double)val_f;
+        nsteps += fine.steps;
       }
       // refill from the item's path counter
       path = atomicAdd(&s_next_path, 1u);
       if ((int)path >= path_end) {
         active = false;
       } else {
-        x = x0; y = y0; Y = 1.f; Z = 0.f; xi = 0.f; step = 0; k = k0;
+        reset();
+        fine_alive = true;
+        coarse_alive = RICH;
+        m = 0;
       }
     }
     // ------------------------------------------------------------ reduce B
@@ -257,45 +318,49 @@ k_paths_mixed(const MixedArgs a) {
 
 }  // namespace
 
-cudaError_t launch_paths_mixed(const MixedArgs& a, int kind, int grid, size_t smem, cudaStream_t s) {
+template <bool RICH>
+static cudaError_t launch_mixed_t(const MixedArgs& a, int kind, int grid, size_t smem, cudaStream_t s) {
+#define PDDS_MIXED_CASE(KK)                                                                           \
+  case KK:                                                                                            \
+    cudaFuncSetAttribute(k_paths_mixed<KK, RICH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+    k_paths_mixed<KK, RICH><<<grid, MIXED_THREADS, smem, s>>>(a);                                     \
+    break;
   switch (kind) {
-    case 0: {
-      cudaFuncSetAttribute(k_paths_mixed<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      k_paths_mixed<0><<<grid, MIXED_THREADS, smem, s>>>(a);
-      break;
-    }
-    case 1: {
-      cudaFuncSetAttribute(k_paths_mixed<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      k_paths_mixed<1><<<grid, MIXED_THREADS, smem, s>>>(a);
-      break;
-    }
-    case 2: {
-      cudaFuncSetAttribute(k_paths_mixed<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      k_paths_mixed<2><<<grid, MIXED_THREADS, smem, s>>>(a);
-      break;
-    }
-    default: {
-      cudaFuncSetAttribute(k_paths_mixed<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      k_paths_mixed<3><<<grid, MIXED_THREADS, smem, s>>>(a);
-      break;
-    }
+    PDDS_MIXED_CASE(0)
+    PDDS_MIXED_CASE(1)
+    PDDS_MIXED_CASE(2)
+    PDDS_MIXED_CASE(3)
+    default: return cudaErrorInvalidValue;
   }
+#undef PDDS_MIXED_CASE
   return cudaGetLastError();
 }
 
-int mixed_blocks_per_sm(int kind, size_t smem) {
+cudaError_t launch_paths_mixed(const MixedArgs& a, int kind, int grid, size_t smem, cudaStream_t s) {
+  return a.richardson ? launch_mixed_t<true>(a, kind, grid, smem, s) : launch_mixed_t<false>(a, kind, grid, smem, s);
+}
+
+template <bool RICH>
+static int blocks_t(int kind, size_t smem) {
   int nb = 0;
+#define PDDS_OCC(KK)                                                                                 \
+  case KK:                                                                                           \
+    cudaFuncSetAttribute(k_paths_mixed<KK, RICH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_paths_mixed<KK, RICH>, MIXED_THREADS, smem); \
+    break;
   switch (kind) {
-    case 0: cudaFuncSetAttribute(k_paths_mixed<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_paths_mixed<0>, MIXED_THREADS, smem); break;
-    case 1: cudaFuncSetAttribute(k_paths_mixed<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_paths_mixed<1>, MIXED_THREADS, smem); break;
-    case 2: cudaFuncSetAttribute(k_paths_mixed<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_paths_mixed<2>, MIXED_THREADS, smem); break;
-    default: cudaFuncSetAttribute(k_paths_mixed<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_paths_mixed<3>, MIXED_THREADS, smem); break;
+    PDDS_OCC(0)
+    PDDS_OCC(1)
+    PDDS_OCC(2)
+    default:
+    PDDS_OCC(3)
   }
+#undef PDDS_OCC
   return nb;
+}
+
+int mixed_blocks_per_sm(int kind, size_t smem, int richardson) {
+  return richardson ? blocks_t<true>(kind, smem) : blocks_t<false>(kind, smem);
 }
 
 }  // namespace pdds

@@ -142,6 +142,12 @@ __global__ void k_replay_paths(const ReplayArgs a) {
   ps.Y = 1.0; ps.Z = 0.0; ps.xi = 0.0; ps.E0 = ps.X0; ps.E1 = ps.X1;
   ps.h = a.h;
   ps.sqrth = a.sqrth;
+  if (a.adaptive_h) {
+    Coef<double> k0;
+    coef_port<KIND>(a.P, ps.X0, ps.X1, k0);
+    ps.h = adaptive_step<double>(sp, ps.X0, ps.X1, a.h, k0);
+    ps.sqrth = ::sqrt(ps.h);
+  }
   ps.seed = a.seed;
   ps.inst = a.instance;
   ps.knot = (uint32_t)knot;

@@ -23,6 +23,9 @@ struct MixedArgs {
   uint32_t instance;
   int chunks, paths_per_chunk, n_items;
   int want_var, dup_sum;
+  int adaptive_h;
+  int richardson;        // 1: common-random-number Richardson pair (h/2, h)
+  double h64;            // h in FP64 (for the adaptive step)
   long long max_steps;
   const int* mc_knots;   // knots that need paths, in hand-out order
   int* item_counter;
@@ -43,6 +46,8 @@ struct Fp64Args {
   uint32_t instance;
   int chunks, paths_per_chunk, n_items;
   int dup_sum;
+  int adaptive_h;
+  int richardson;
   long long max_steps;
   const int* mc_knots;
   int* item_counter;
@@ -61,6 +66,7 @@ struct ReplayArgs {
   uint64_t seed;
   uint32_t instance;
   int sublinear;
+  int adaptive_h;
   long long max_steps;
   const int* mc_knots;   // knots with paths
   int n_mc;
@@ -86,9 +92,9 @@ struct ReplayArgs {
 };
 
 cudaError_t launch_paths_mixed(const MixedArgs& a, int kind, int grid, size_t smem, cudaStream_t s);
-int mixed_blocks_per_sm(int kind, size_t smem);
+int mixed_blocks_per_sm(int kind, size_t smem, int richardson);
 cudaError_t launch_paths_fp64(const Fp64Args& a, int kind, int grid, size_t smem, cudaStream_t s);
-int fp64_blocks_per_sm(int kind, size_t smem);
+int fp64_blocks_per_sm(int kind, size_t smem, int richardson);
 cudaError_t launch_replay_paths(const ReplayArgs& a, int kind, cudaStream_t s);
 cudaError_t launch_replay_reduce(const ReplayArgs& a, int kind, const int* task_m, const int* task_d,
                                  const int* task_i, int ntask, const int64_t* task_out,

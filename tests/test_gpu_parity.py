@@ -188,3 +188,40 @@ def test_errors_are_reported_not_faulted():
         # the context stays usable afterwards
         est = pd.estimate(P.BVP.poisson_sincos(), 64, 1e-3, mode=P.MODE_MIXED)
         assert np.all(np.isfinite(est.val))
+
+
+def test_replay_bit_exact_adaptive_step():
+    """Per-knot adaptive step (PDDSparseGM.cpp:4026-4028) in replay and oracle."""
+    nsub, nnode, N, h = 4, 9, 150, 1e-3
+    fac = fac_rule(2.0, nsub, nnode)
+    L = O.Layout(SW, NE, nsub, nnode)
+    ip, _ = O.replay_ipsi(L, fac)
+    with P.PDDSparseGM(SW, NE, nsub, nnode, fac) as pd:
+        est = pd.estimate(P.BVP.poisson_sincos(), N, h, mode=P.MODE_REPLAY_FP64, seed=8, want_var=True,
+                          ipsi_override=ip, adaptive_h=True)
+    ref = L.run(O.make_problem(O.POISSON_SINCOS),
+                O.make_params(N, h, seed=8, fac=fac, portable=True, adaptive_h=True))
+    _rows_equal(est, ref, exact=True)
+    assert est.info["path_steps"] == ref["stats"][0]
+
+
+def test_richardson_mixed_matches_fp64_and_beats_plain():
+    """Richardson pair (h/2, h) on one Brownian motion: MIXED equals the FP64
+    form on the same stream within a fraction of a standard error, and the
+    extrapolated interface solution is closer to the analytic one."""
+    nsub, nnode, N, h = 4, 11, 10_000, 1e-3
+    fac = fac_rule(2.0, nsub, nnode)
+    bvp = P.BVP.poisson_sincos()
+    with P.PDDSparseGM(SW, NE, nsub, nnode, fac) as pd:
+        m = pd.estimate(bvp, N, h, mode=P.MODE_MIXED, seed=5, want_var=True, adaptive_h=True, richardson=True)
+        u_r, _ = pd.solve_interface()
+        f = pd.estimate(bvp, N, h, mode=P.MODE_FP64, seed=5, adaptive_h=True, richardson=True)
+        p = pd.estimate(bvp, N, h, mode=P.MODE_MIXED, seed=5, adaptive_h=True)
+        u_p, _ = pd.solve_interface()
+        ex = bvp.u(pd.x, pd.y)
+    se = np.sqrt(np.maximum(m.var, 1e-12) / N)
+    assert np.max(np.abs(m.val - f.val) / se) < 0.5
+    assert m.info["path_steps"] > 1.4 * p.info["path_steps"]
+    rmse_r = np.sqrt(np.mean((u_r - ex) ** 2))
+    rmse_p = np.sqrt(np.mean((u_p - ex) ** 2))
+    assert rmse_r < 2e-3 and rmse_r < 0.6 * rmse_p, (rmse_r, rmse_p)
