@@ -81,6 +81,7 @@ struct pdds_ctx {
   // solve scratch
   DBuf<double> sv64, sscal, spart, shess, su;
   DBuf<float> sV32, sw32, sval32;
+  DBuf<unsigned> sctl;
   double* host_rr = nullptr;
   int solve_m = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
@@ -304,6 +305,7 @@ pdds_status pdds_destroy(pdds_ctx* ctx) {
     ctx->sV32.release();
     ctx->sw32.release();
     ctx->sval32.release();
+    ctx->sctl.release();
     if (ctx->host_rr) cudaFreeHost(ctx->host_rr);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -647,8 +649,9 @@ pdds_status pdds_solve_interface(pdds_ctx* ctx, const pdds_solve_desc* desc, dou
   const int m = std::max(2, std::min(desc->restart > 0 ? desc->restart : 30, 40));
   CK(ctx->sv64.resize((size_t)6 * K));
   CK(ctx->sscal.resize(64));
-  CK(ctx->spart.resize(64 * 256 + 1024));
-  CK(ctx->shess.resize((size_t)(m + 1) * m + 2 * m + 3 * (m + 1) + 16));
+  CK(ctx->spart.resize(std::max<size_t>(64 * 256 + 1024, (size_t)((K + 1023) / 1024) * 48 + 64)));
+  CK(ctx->shess.resize((size_t)(m + 1) * m + 2 * m + 4 * (m + 1) + 16));
+  CK(ctx->sctl.resize(8));
   CK(ctx->su.resize(std::max(K, 1)));
   SolveCsr A{K, nnz, ctx->row_ptr.p, ctx->col.p, ctx->G.p};
   SolveWork w;
@@ -657,6 +660,7 @@ pdds_status pdds_solve_interface(pdds_ctx* ctx, const pdds_solve_desc* desc, dou
   w.part = ctx->spart.p;
   w.hess = ctx->shess.p;
   w.host_rr = ctx->host_rr;
+  w.ctl = ctx->sctl.p;
   int iters = 0, refines = 0;
   double relres = 0.0;
   const double tol = desc->tol > 0 ? desc->tol : 1e-10;

@@ -128,6 +128,31 @@ __device__ __forceinline__ void coef_f32(const ProblemDev& P, float x, float y, 
   if (!P.use_cv) { k.g0 = 0.f; k.g1 = 0.f; }
 }
 
+// sigma alone (for the exit threshold)
+template <int KIND>
+__device__ __forceinline__ void sigma_f32(float x, float y, float& s00, float& s01, float& s10, float& s11) {
+  if (KIND == PK_VARCOEF) {
+    s00 = 1.f + 0.5f * (x * x); s01 = 0.f; s10 = 0.f; s11 = 1.f + 0.5f * (y * y);
+  } else if (KIND == PK_MONEGROS) {
+    s00 = 1.41421356237f; s01 = 0.f; s10 = 0.f; s11 = 1.41421356237f;
+  } else {
+    s00 = 1.41421356f; s01 = 0.f; s10 = 0.f; s11 = 1.41421356f;
+  }
+}
+
+// |N^T sigma| for the x normal (1,0) and the y normal (0,1) (diagonal sigma)
+template <int KIND>
+__device__ __forceinline__ void sigma_normals_f32(float x, float y, float& nx, float& ny) {
+  if (KIND == PK_VARCOEF) {
+    nx = 1.f + 0.5f * (x * x);
+    ny = 1.f + 0.5f * (y * y);
+  } else if (KIND == PK_MONEGROS) {
+    nx = ny = 1.41421356237f;
+  } else {
+    nx = ny = 1.41421356f;
+  }
+}
+
 template <int KIND>
 __device__ __forceinline__ float u_f32(const ProblemDev& P, float x, float y) {
   if (KIND == PK_POISSON_SINCOS) {

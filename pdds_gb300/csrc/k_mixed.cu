@@ -36,9 +36,17 @@ constexpr unsigned FULL = 0xffffffffu;
 
 struct Lvl {
   float x, y, Y, Z, xi;
-  Coef<float> k;
   unsigned steps;
 };
+
+// A pending exit deposit: histogram index of the first of the 4 cubic
+// nodes, offset in the bin, and the signed weight * Y.
+struct QEntry {
+  int idx;
+  float fu;
+  float yw;
+};
+constexpr int QCAP = 96;  // <= 31 left over + 2 deposits x 32 lanes
 
 // Box-Muller in FP32 from two Philox words: z0 = rho cos(2 pi u1),
 // z1 = rho sin(2 pi u1), evaluated as -rho cos/sin(2 pi u1 - pi) so the fast
@@ -54,7 +62,7 @@ __device__ __forceinline__ void normals_f32(uint32_t ua, uint32_t ub, float& z0,
 }
 
 template <int KIND, bool RICH>
-__global__ void __launch_bounds__(MIXED_THREADS)
+__global__ void __launch_bounds__(MIXED_THREADS, 4)
 k_paths_mixed(const MixedArgs a) {
   extern __shared__ float hist[];  // [sum nbins] (and the Y^2 histogram after it)
   __shared__ ItemSide s_side[4];
@@ -64,6 +72,7 @@ k_paths_mixed(const MixedArgs a) {
   __shared__ unsigned s_next_path;
   __shared__ double s_red[MIXED_THREADS / 32][4];
   __shared__ unsigned long long s_redi[MIXED_THREADS / 32][3];
+  __shared__ QEntry s_queue[MIXED_THREADS / 32][QCAP];
   const DevLayout& L = a.L;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
@@ -129,131 +138,189 @@ k_paths_mixed(const MixedArgs a) {
     __syncthreads();
 
     // ------------------------------------------------------------ paths
+    // Every iteration of a lane: one Philox block, two Box-Muller pairs, and
+    // a fixed sequence of steps -- (fine A, fine B, coarse) for the
+    // Richardson pair, (A, B) otherwise -- so the warp's control flow stays
+    // uniform while path lengths differ.  Exit deposits go through a
+    // per-warp queue in shared memory and are applied 32 at a time by the
+    // whole warp; finished lanes refill with a warp-aggregated atomic.
     const float x0 = (float)L.kx[knot], y0 = (float)L.ky[knot];
     const float rect[4] = {s_rect[0], s_rect[1], s_rect[2], s_rect[3]};
-    Coef<float> k0;
-    coef_f32<KIND>(a.P, x0, y0, k0);
+    const float cx = 0.5f * (rect[0] + rect[2]), cy = 0.5f * (rect[1] + rect[3]);
+    const float hx = rect[2] - cx, hy = rect[3] - cy;
     const int chunk = item % a.chunks;
     unsigned path = (unsigned)(chunk * a.paths_per_chunk + tid);
     bool active = (int)path < path_end;
     double b = 0.0, bb = 0.0;
     unsigned long long nsteps = 0, nglob = 0, nsten = 0;
-    // Exit of one level: B value, and the RBF deposit with weight wgt * Y.
-    auto exit_level = [&](const Lvl& s, float wgt, float Ex, float Ey, int onmask) -> float {
+    QEntry* q = s_queue[warp];
+    int qcount = 0;  // warp-uniform
+    const unsigned lt = (1u << lane) - 1u;
+
+    auto apply = [&](const QEntry& e) {
+      float w[4];
+      cubic_weights(e.fu, w[0], w[1], w[2], w[3]);
+      float* hp = hist + e.idx;
+#pragma unroll
+      for (int r = 0; r < 4; r++) atomicAdd(hp + r, e.yw * w[r]);
+      if (a.want_var) {
+        float* hq = hist2 + e.idx;
+        const float y2 = e.yw * e.yw;
+#pragma unroll
+        for (int r = 0; r < 4; r++) atomicAdd(hq + r, y2 * w[r]);
+      }
+    };
+    // One step of a level (Step, control-variate variant,
+    // FKACIntegrator.hpp:46-57) and the Gobet-shifted exit test (Inside,
+    // :168-222), branch-free: with dx = |x - cx| - hx, dy = |y - cy| - hy the
+    // reference's signed distance is max(dx, dy) except in the outer corner
+    // region (where both are positive and the path exits anyway), and its
+    // normal is the x normal exactly when dx > dy.
+    auto advance = [&](Lvl& s, float i0, float i1, float hh, float sq) -> bool {
+      Coef<float> k;
+      coef_f32<KIND>(a.P, s.x, s.y, k);
+      const float v0 = -(k.s00 * k.g0 + k.s10 * k.g1);
+      const float v1 = -(k.s01 * k.g0 + k.s11 * k.g1);
+      s.xi += s.Y * (v0 * i0 + v1 * i1);
+      s.Z += k.f * s.Y * hh;
+      s.Y += k.c * s.Y * hh;
+      s.x += k.b0 * hh + (k.s00 * i0 + k.s01 * i1);
+      s.y += k.b1 * hh + (k.s10 * i0 + k.s11 * i1);
+      ++s.steps;
+      const float dx = fabsf(s.x - cx) - hx, dy = fabsf(s.y - cy) - hy;
+      float nx, ny;  // |N^T sigma| for the x and y normals
+      sigma_normals_f32<KIND>(s.x, s.y, nx, ny);
+      const float thr = -0.5826f * sq * (dx > dy ? nx : ny);
+      return !(fmaxf(dx, dy) < thr) || s.steps >= (unsigned)a.max_steps;
+    };
+    // Exit of a level: B value and, on an interior side, the deposit.
+    auto on_exit = [&](const Lvl& s, float wgt, float& val, bool& dep, QEntry& de) {
+      float Ex, Ey, Nx, Ny;
+      int onmask;
+      const float dist = rect2d<float>(rect, s.x, s.y, Ex, Ey, Nx, Ny, onmask);
+      (void)dist;
+      if (s.steps >= (unsigned)a.max_steps) {
+        float g00, g01, g10, g11;
+        sigma_f32<KIND>(s.x, s.y, g00, g01, g10, g11);
+        const float w0 = Nx * g00 + Ny * g10, w1 = Nx * g01 + Ny * g11;
+        if (dist < -0.5826f * sqrtf(w0 * w0 + w1 * w1) * (wgt < 0.f ? sqrth : (RICH ? sqrth * 0.70710678f : sqrth))) {
+          atomicOr(a.err_flags, ERR_FLAG_STEP_LIMIT);
+          val = 0.f;
+          return;
+        }
+      }
       const int d = exit_side(onmask);
       const bool glob = ((onmask & 1) && s_side[0].glob) || ((onmask & 2) && s_side[1].glob) ||
                         ((onmask & 4) && s_side[2].glob) || ((onmask & 8) && s_side[3].glob);
       if (glob) {
         ++nglob;
-        return s.Z + s.Y * u_f32<KIND>(a.P, Ex, Ey) + s.xi;
+        val = s.Z + s.Y * u_f32<KIND>(a.P, Ex, Ey) + s.xi;
+        return;
       }
       ++nsten;
+      val = s.Z + s.xi;
       if (d < 0) {
         atomicOr(a.err_flags, ERR_FLAG_EXIT_SIDE);
-      } else {
-        const ItemSide& is = s_side[d];
-        if (is.n > 0) {
-          const float sc = is.orient == 0 ? Ex : Ey;
-          const float u = (sc - is.base) * is.inv_delta;
-          int b0 = (int)floorf(u);
-          b0 = max(1, min(b0, is.nbins - 3));
-          const float fu = u - (float)b0;
-          float w[4];
-          cubic_weights(fu, w[0], w[1], w[2], w[3]);
-          const float yw = wgt * s.Y;
-          float* hp = hist + is.hist_off + b0 - 1;
-#pragma unroll
-          for (int q = 0; q < 4; q++) atomicAdd(hp + q, yw * w[q]);
-          if (a.want_var) {
-            float* hq = hist2 + is.hist_off + b0 - 1;
-            const float y2 = yw * yw;
-#pragma unroll
-            for (int q = 0; q < 4; q++) atomicAdd(hq + q, y2 * w[q]);
-          }
-        }
+        return;
       }
-      return s.Z + s.xi;
-    };
-    // One Euler-Maruyama step of a level (Step, control-variate variant,
-    // FKACIntegrator.hpp:46-57) and the Gobet-shifted exit test (Inside,
-    // :168-222).  Returns true when the level has exited (val set).
-    auto step_level = [&](Lvl& s, float i0, float i1, float hh, float sq, float wgt, float& val) -> bool {
-      const float v0 = -(s.k.s00 * s.k.g0 + s.k.s10 * s.k.g1);
-      const float v1 = -(s.k.s01 * s.k.g0 + s.k.s11 * s.k.g1);
-      s.xi += s.Y * (v0 * i0 + v1 * i1);
-      s.Z += s.k.f * s.Y * hh;
-      s.Y += s.k.c * s.Y * hh;
-      s.x += s.k.b0 * hh + (s.k.s00 * i0 + s.k.s01 * i1);
-      s.y += s.k.b1 * hh + (s.k.s10 * i0 + s.k.s11 * i1);
-      ++s.steps;
-      coef_f32<KIND>(a.P, s.x, s.y, s.k);
-      float Ex, Ey, Nx, Ny;
-      int onmask;
-      const float dist = rect2d<float>(rect, s.x, s.y, Ex, Ey, Nx, Ny, onmask);
-      const float w0 = Nx * s.k.s00 + Ny * s.k.s10, w1 = Nx * s.k.s01 + Ny * s.k.s11;
-      const float thr = -0.5826f * sqrtf(w0 * w0 + w1 * w1) * sq;
-      if (dist < thr) {
-        if (s.steps < (unsigned)a.max_steps) return false;
-        atomicOr(a.err_flags, ERR_FLAG_STEP_LIMIT);
-        val = 0.f;
-        return true;
+      const ItemSide& is = s_side[d];
+      if (is.n > 0) {
+        const float sc = is.orient == 0 ? Ex : Ey;
+        const float u = (sc - is.base) * is.inv_delta;
+        int b0 = (int)floorf(u);
+        b0 = max(1, min(b0, is.nbins - 3));
+        de.idx = is.hist_off + b0 - 1;
+        de.fu = u - (float)b0;
+        de.yw = wgt * s.Y;
+        dep = true;
       }
-      val = exit_level(s, wgt, Ex, Ey, onmask);
-      return true;
     };
-    Lvl fine, coarse;
+    Lvl F, Cs;
     auto reset = [&]() {
-      fine.x = x0; fine.y = y0; fine.Y = 1.f; fine.Z = 0.f; fine.xi = 0.f; fine.k = k0; fine.steps = 0;
-      coarse = fine;
+      F.x = x0; F.y = y0; F.Y = 1.f; F.Z = 0.f; F.xi = 0.f; F.steps = 0;
+      Cs = F;
     };
     reset();
-    bool fine_alive = active, coarse_alive = RICH && active;
+    bool f_alive = active, c_alive = RICH && active;
     float val_f = 0.f, val_c = 0.f;
-    unsigned m = 0;  // Philox block index of the path
-    u32x4 blk;
-    blk.v[0] = blk.v[1] = blk.v[2] = blk.v[3] = 0;
+    unsigned m = 0;
     while (__any_sync(FULL, active)) {
-      if (!active) continue;
-      if (RICH) {
-        // Richardson pair: one coarse step of h and two fine steps of h/2 on
-        // the same Brownian increments (dW_coarse = dW_fine1 + dW_fine2);
-        // the estimator 2 E[fine] - E[coarse] cancels the O(h) bias
-        blk = path_block(a.seed, a.instance, (uint32_t)knot, path, m++);
+      bool dep0 = false, dep1 = false;
+      QEntry e0, e1;
+      bool fx = false, cx_ = false;  // exits in this iteration
+      if (active) {
+        const u32x4 blk = path_block(a.seed, a.instance, (uint32_t)knot, path, m++);
         float za0, za1, zb0, zb1;
         normals_f32(blk.v[0], blk.v[1], za0, za1);
         normals_f32(blk.v[2], blk.v[3], zb0, zb1);
-        const float hf = 0.5f * h, sqf = sqrth * 0.70710678f;
-        if (fine_alive) fine_alive = !step_level(fine, sqf * za0, sqf * za1, hf, sqf, 2.f, val_f);
-        if (fine_alive) fine_alive = !step_level(fine, sqf * zb0, sqf * zb1, hf, sqf, 2.f, val_f);
-        if (coarse_alive)
-          coarse_alive = !step_level(coarse, sqf * (za0 + zb0), sqf * (za1 + zb1), h, sqrth, -1.f, val_c);
-        if (fine_alive || coarse_alive) continue;
-        const double v = 2.0 * (double)val_f - (double)val_c;
+        if (RICH) {
+          // Richardson pair: two fine steps of h/2 and one coarse step of h
+          // on the same Brownian increments (dW_coarse = dW_fine1 + dW_fine2);
+          // 2 E[fine] - E[coarse] cancels the O(h) bias
+          const float hf = 0.5f * h, sqf = sqrth * 0.70710678f;
+          if (f_alive) fx = advance(F, sqf * za0, sqf * za1, hf, sqf);
+          if (f_alive && !fx) fx = advance(F, sqf * zb0, sqf * zb1, hf, sqf);
+          if (c_alive) cx_ = advance(Cs, sqf * (za0 + zb0), sqf * (za1 + zb1), h, sqrth);
+        } else {
+          fx = advance(F, sqrth * za0, sqrth * za1, h, sqrth);
+          if (!fx) fx = advance(F, sqrth * zb0, sqrth * zb1, h, sqrth);
+        }
+      }
+      if (fx) {
+        on_exit(F, RICH ? 2.f : 1.f, val_f, dep0, e0);
+        f_alive = false;
+      }
+      if (RICH && cx_) {
+        on_exit(Cs, -1.f, val_c, dep1, e1);
+        c_alive = false;
+      }
+      // deposit queue (warp-synchronous)
+      {
+        const unsigned mk = __ballot_sync(FULL, dep0);
+        if (dep0) q[qcount + __popc(mk & lt)] = e0;
+        qcount += __popc(mk);
+      }
+      if (RICH) {
+        const unsigned mk = __ballot_sync(FULL, dep1);
+        if (dep1) q[qcount + __popc(mk & lt)] = e1;
+        qcount += __popc(mk);
+      }
+      __syncwarp();
+      while (qcount >= 32) {
+        const QEntry e = q[qcount - 32 + lane];
+        __syncwarp();
+        apply(e);
+        qcount -= 32;
+      }
+      // finished pairs: B and refill
+      const bool done = active && !f_alive && !c_alive;
+      if (done) {
+        const double v = RICH ? 2.0 * (double)val_f - (double)val_c : (double)val_f;
         b += v;
         bb += v * v;
-        nsteps += fine.steps + coarse.steps;
-      } else {
-        if ((m & 1u) == 0) blk = path_block(a.seed, a.instance, (uint32_t)knot, path, m >> 1);
-        float z0, z1;
-        if (m & 1u) normals_f32(blk.v[2], blk.v[3], z0, z1);
-        else normals_f32(blk.v[0], blk.v[1], z0, z1);
-        ++m;
-        if (!step_level(fine, sqrth * z0, sqrth * z1, h, sqrth, 1.f, val_f)) continue;
-        b += (double)val_f;
-        bb += (double)val_f * (double)val_f;
-        nsteps += fine.steps;
+        nsteps += F.steps + (RICH ? Cs.steps : 0u);
       }
-      // refill from the item's path counter
-      path = atomicAdd(&s_next_path, 1u);
-      if ((int)path >= path_end) {
-        active = false;
-      } else {
-        reset();
-        fine_alive = true;
-        coarse_alive = RICH;
-        m = 0;
+      const unsigned dm = __ballot_sync(FULL, done);
+      if (dm) {
+        const int leader = __ffs(dm) - 1;
+        unsigned base = 0;
+        if (lane == leader) base = atomicAdd(&s_next_path, (unsigned)__popc(dm));
+        base = __shfl_sync(FULL, base, leader);
+        if (done) {
+          path = base + __popc(dm & lt);
+          if ((int)path >= path_end) {
+            active = false;
+          } else {
+            reset();
+            f_alive = true;
+            c_alive = RICH;
+            m = 0;
+          }
+        }
       }
     }
+    __syncwarp();
+    if (lane < qcount) apply(q[lane]);
     // ------------------------------------------------------------ reduce B
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {

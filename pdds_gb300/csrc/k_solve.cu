@@ -306,27 +306,229 @@ cudaError_t solve_bicgstab(const SolveCsr& A, const double* b, double* x, SolveW
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------- fused GMRES
+// One Arnoldi step is five launches and no host synchronisation: SpMV,
+// dots with the basis, subtract + re-orthogonalising dots, subtract + norm
+// (whose last block also applies the Givens rotations and tests
+// convergence), normalise.  Reductions finish in the last block to arrive
+// (a ticket counter, no waiting), and every kernel returns at once after
+// the device-side convergence flag is set.
+namespace {
+
+constexpr int GM_THREADS = 256;
+constexpr int GM_CHUNK = 1024;   // elements per block
+constexpr int GM_MAXV = 48;      // basis vectors (m + 1 <= 41)
+
+struct GmCtl {
+  unsigned ticket;
+  unsigned converged;
+  unsigned jdim;
+  unsigned pad;
+};
+
+// last-block ticket: returns true in the block that finishes last
+__device__ __forceinline__ bool gm_last_block(GmCtl* ctl) {
+  __shared__ bool last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned t = atomicAdd(&ctl->ticket, 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (last) __threadfence();
+  return last;
+}
+
+__global__ void k_gm_spmv(int K, const int64_t* __restrict__ rp, const int* __restrict__ col,
+                          const float* __restrict__ val, const float* __restrict__ x, float* __restrict__ y,
+                          const GmCtl* ctl) {
+  if (ctl->converged) return;
+  const int lane = threadIdx.x & 31;
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  for (int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < K; row += warps) {
+    const int64_t e0 = rp[row], e1 = rp[row + 1];
+    float acc = 0.f;
+    for (int64_t e = e0 + lane; e < e1; e += 32) acc += val[e] * x[col[e]];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) y[row] = x[row] + acc;
+  }
+}
+
+// partial dots of the chunk of wc (shared) with V[0..nv): one warp per vector
+__device__ __forceinline__ void gm_chunk_dots(int n, int nv, const float* V, const float* wc, int k0, int cn,
+                                              double* part) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int i = warp; i < nv; i += GM_THREADS / 32) {
+    const float* vi = V + (int64_t)i * n + k0;
+    float acc = 0.f;
+    for (int k = lane; k < cn; k += 32) acc += vi[k] * wc[k];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) part[(int64_t)blockIdx.x * GM_MAXV + i] = (double)acc;
+  }
+}
+
+__device__ __forceinline__ void gm_finish_dots(int nv, const double* part, double* out, bool accumulate) {
+  for (int i = threadIdx.x; i < nv; i += blockDim.x) {
+    double s = 0.0;
+    for (int b = 0; b < (int)gridDim.x; b++) s += part[(int64_t)b * GM_MAXV + i];
+    out[i] = accumulate ? out[i] + s : s;
+  }
+}
+
+// h = V^T w
+__global__ void k_gm_dots(int n, int nv, const float* V, const float* w, double* part, double* h, GmCtl* ctl) {
+  if (ctl->converged) return;
+  __shared__ float wc[GM_CHUNK];
+  const int k0 = blockIdx.x * GM_CHUNK, cn = min(GM_CHUNK, n - k0);
+  for (int k = threadIdx.x; k < cn; k += GM_THREADS) wc[k] = w[k0 + k];
+  __syncthreads();
+  gm_chunk_dots(n, nv, V, wc, k0, cn, part);
+  if (gm_last_block(ctl)) {
+    gm_finish_dots(nv, part, h, false);
+    if (threadIdx.x == 0) ctl->ticket = 0;
+  }
+}
+
+// w -= V h1; h2 = V^T w; h1 += h2
+__global__ void k_gm_sub_dots(int n, int nv, const float* V, double* h1, double* h2, float* w, double* part,
+                              GmCtl* ctl) {
+  if (ctl->converged) return;
+  __shared__ float wc[GM_CHUNK];
+  __shared__ float hs[GM_MAXV];
+  for (int i = threadIdx.x; i < nv; i += GM_THREADS) hs[i] = (float)h1[i];
+  __syncthreads();
+  const int k0 = blockIdx.x * GM_CHUNK, cn = min(GM_CHUNK, n - k0);
+  for (int k = threadIdx.x; k < cn; k += GM_THREADS) {
+    float acc = w[k0 + k];
+    for (int i = 0; i < nv; i++) acc -= hs[i] * V[(int64_t)i * n + k0 + k];
+    wc[k] = acc;
+    w[k0 + k] = acc;
+  }
+  __syncthreads();
+  gm_chunk_dots(n, nv, V, wc, k0, cn, part);
+  if (gm_last_block(ctl)) {
+    gm_finish_dots(nv, part, h2, false);
+    __syncthreads();
+    for (int i = threadIdx.x; i < nv; i += blockDim.x) h1[i] += h2[i];
+    if (threadIdx.x == 0) ctl->ticket = 0;
+  }
+}
+
+// w -= V h2; |w|; last block: Givens rotation of column j, convergence test
+__global__ void k_gm_sub_norm(int n, int nv, const float* V, const double* h2, float* w, double* part,
+                              GmCtl* ctl, int m, int j, const double* hcol, double* H, double* cs,
+                              double* sn, double* g, double* inv_norm, double inner_tol) {
+  if (ctl->converged) return;
+  __shared__ float hs[GM_MAXV];
+  __shared__ double red[GM_THREADS];
+  for (int i = threadIdx.x; i < nv; i += GM_THREADS) hs[i] = (float)h2[i];
+  __syncthreads();
+  const int k0 = blockIdx.x * GM_CHUNK, cn = min(GM_CHUNK, n - k0);
+  double ss = 0.0;
+  for (int k = threadIdx.x; k < cn; k += GM_THREADS) {
+    float acc = w[k0 + k];
+    for (int i = 0; i < nv; i++) acc -= hs[i] * V[(int64_t)i * n + k0 + k];
+    w[k0 + k] = acc;
+    ss += (double)acc * (double)acc;
+  }
+  red[threadIdx.x] = ss;
+  __syncthreads();
+  for (int o = GM_THREADS / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[(int64_t)blockIdx.x * GM_MAXV] = red[0];
+  if (gm_last_block(ctl) && threadIdx.x == 0) {
+    double nrm2 = 0.0;
+    for (int b = 0; b < (int)gridDim.x; b++) nrm2 += part[(int64_t)b * GM_MAXV];
+    const double nrm = sqrt(nrm2);
+    double* colj = H + (int64_t)j * (m + 1);
+    for (int i = 0; i <= j; i++) colj[i] = hcol[i];
+    colj[j + 1] = nrm;
+    for (int i = 0; i < j; i++) {
+      const double x0 = colj[i], x1 = colj[i + 1];
+      colj[i] = cs[i] * x0 + sn[i] * x1;
+      colj[i + 1] = -sn[i] * x0 + cs[i] * x1;
+    }
+    const double x0 = colj[j], x1 = colj[j + 1];
+    const double r = sqrt(x0 * x0 + x1 * x1);
+    cs[j] = (r > 0.0) ? x0 / r : 1.0;
+    sn[j] = (r > 0.0) ? x1 / r : 0.0;
+    colj[j] = r;
+    colj[j + 1] = 0.0;
+    g[j + 1] = -sn[j] * g[j];
+    g[j] = cs[j] * g[j];
+    *inv_norm = (nrm > 0.0) ? 1.0 / nrm : 0.0;
+    ctl->jdim = (unsigned)(j + 1);
+    if (fabs(g[j + 1]) < inner_tol || !(nrm > 0.0)) ctl->converged = 1u;
+    ctl->ticket = 0;
+  }
+}
+
+__global__ void k_gm_normalize(int n, const float* w, const double* inv_norm, float* vnext, const GmCtl* ctl) {
+  if (ctl->converged) return;
+  const float s = (float)*inv_norm;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) vnext[k] = w[k] * s;
+}
+
+__global__ void k_gm_init(double* g, int m, GmCtl* ctl) {
+  for (int i = 0; i <= m; i++) g[i] = 0.0;
+  g[0] = 1.0;
+  ctl->ticket = 0;
+  ctl->converged = 0;
+  ctl->jdim = 0;
+}
+
+__global__ void k_gm_backsolve(int m, const double* H, const double* g, double* y, const GmCtl* ctl,
+                               double* jdim_out) {
+  const int jd = (int)ctl->jdim;
+  for (int i = jd - 1; i >= 0; i--) {
+    double s = g[i];
+    for (int k = i + 1; k < jd; k++) s -= H[(int64_t)k * (m + 1) + i] * y[k];
+    y[i] = s / H[(int64_t)i * (m + 1) + i];
+  }
+  *jdim_out = (double)jd;
+}
+
+__global__ void k_gm_update_x(int n, int m, const float* V, const double* y, const double* nrm2r, double* x,
+                              const GmCtl* ctl) {
+  const int jd = (int)ctl->jdim;
+  const double scale = sqrt(*nrm2r);
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    for (int i = 0; i < jd; i++) acc += y[i] * (double)V[(int64_t)i * n + k];
+    x[k] += scale * acc;
+  }
+}
+
+}  // namespace
+
 cudaError_t solve_gmres_ir(const SolveCsr& A, const double* b, double* x, SolveWork& w, int m,
                            int max_iter, int max_refine, double tol, int* iters, int* refines,
                            double* relres, cudaStream_t s) {
   w.launches = 0;
   const int n = A.K;
+  if (m + 1 > GM_MAXV) m = GM_MAXV - 1;
   const int sg = std::max(1, std::min(4096, (n * 32 + SPMV_THREADS - 1) / SPMV_THREADS));
   const int vg = vgrid(n);
+  const int gb = (n + GM_CHUNK - 1) / GM_CHUNK;
   double* r = w.v64[0];
   double* Ax = w.v64[1];
   double* sc = w.scal;
-  double* bb = sc + 0;     // <b,b>
-  double* rr = sc + 1;     // <r,r>
-  double* nrm = sc + 2;    // <w,w>
+  double* bb = sc + 0;       // <b,b>
+  double* rr = sc + 1;       // <r,r>, then jdim of the last cycle at sc[2]
+  double* inv_norm = sc + 3;
   double* H = w.hess;
   double* cs = H + (m + 1) * m;
   double* sn = cs + m;
   double* g = sn + m;
   double* hcol = g + (m + 1);
   double* y = hcol + (m + 1);
+  double* h2 = y + (m + 1);
   float* V = w.V32;
   float* wv = w.w32;
+  GmCtl* ctl = reinterpret_cast<GmCtl*>(w.ctl);
   const int nb = std::min(RED_BLOCKS, std::max(1, (n + RED_THREADS - 1) / RED_THREADS));
   ++w.launches;
   k_to_f32<<<vgrid((int)std::min<int64_t>(A.nnz, 1 << 28)), 256, 0, s>>>(A.nnz, A.val64, w.val32);
@@ -344,59 +546,37 @@ cudaError_t solve_gmres_ir(const SolveCsr& A, const double* b, double* x, SolveW
   int total = 0, ref = 0;
   double hr = hb;
   for (; ref <= max_refine; ref++) {
-    // FP64 residual
+    // FP64 residual; also reads back the size of the previous cycle
     ++w.launches;
     k_spmv<double><<<sg, SPMV_THREADS, 0, s>>>(n, A.row_ptr, A.col, A.val64, x, Ax);
     ++w.launches;
     k_resid<<<vg, 256, 0, s>>>(n, b, Ax, r);
     dot2(s, n, r, r, nullptr, nullptr, w.part, rr, nullptr, &w.launches);
-    cudaMemcpyAsync(w.host_rr, rr, sizeof(double), cudaMemcpyDeviceToHost, s);
+    double hv[2] = {0.0, 0.0};
+    cudaMemcpyAsync(hv, rr, 2 * sizeof(double), cudaMemcpyDeviceToHost, s);
     cudaStreamSynchronize(s);
-    hr = *w.host_rr;
+    hr = hv[0];
+    if (ref > 0) total += (int)hv[1];
     if (!(hr > tol2) || ref == max_refine || total >= max_iter) break;
     // FP32 GMRES(m) on A d = r / |r|
     ++w.launches;
     k_scale_to_f32<<<vg, 256, 0, s>>>(n, r, rr, V);
     ++w.launches;
-    k_gmres_init<<<1, 1, 0, s>>>(g, m);
-    int j = 0;
+    k_gm_init<<<1, 1, 0, s>>>(g, m, ctl);
     const double inner_tol = 1e-6;
-    for (; j < m; j++) {
-      ++w.launches;
-      k_spmv<float><<<sg, SPMV_THREADS, 0, s>>>(n, A.row_ptr, A.col, w.val32, V + (int64_t)j * n, wv);
+    for (int j = 0; j < m; j++) {
       const int nv = j + 1;
-      const size_t shm = (size_t)nv * MDOT_THREADS * sizeof(double);
-      // classical Gram-Schmidt, twice
-      ++w.launches;
-      k_mdot_part<<<nb, MDOT_THREADS, shm, s>>>(n, nv, V, wv, w.part);
-      ++w.launches;
-      k_mdot_final<<<1, 64, 0, s>>>(nb, nv, w.part, hcol, 0);
-      ++w.launches;
-      k_mdot_sub<<<vg, 256, 0, s>>>(n, nv, V, hcol, wv);
-      ++w.launches;
-      k_mdot_part<<<nb, MDOT_THREADS, shm, s>>>(n, nv, V, wv, w.part);
-      ++w.launches;
-      k_mdot_final<<<1, 64, 0, s>>>(nb, nv, w.part, y, 0);
-      ++w.launches;
-      k_mdot_sub<<<vg, 256, 0, s>>>(n, nv, V, y, wv);
-      ++w.launches;
-      k_mdot_final<<<1, 64, 0, s>>>(nb, nv, w.part, hcol, 1);
-      k_dot2_part<float><<<nb, RED_THREADS, 0, s>>>(n, wv, wv, nullptr, nullptr, w.part);
-      k_dot2_final<<<1, RED_THREADS, 0, s>>>(nb, w.part, nrm, nullptr);
-      ++w.launches;
-      k_normalize<<<vg, 256, 0, s>>>(n, nrm, wv, V + (int64_t)(j + 1) * n);
-      ++w.launches;
-      k_givens<<<1, 1, 0, s>>>(m, j, H, hcol, nrm, cs, sn, g);
-      ++total;
-      double gres = 0.0;
-      cudaMemcpyAsync(&gres, g + j + 1, sizeof(double), cudaMemcpyDeviceToHost, s);
-      cudaStreamSynchronize(s);
-      if (std::fabs(gres) < inner_tol || total >= max_iter) { j++; break; }
+      k_gm_spmv<<<sg, SPMV_THREADS, 0, s>>>(n, A.row_ptr, A.col, w.val32, V + (int64_t)j * n, wv, ctl);
+      k_gm_dots<<<gb, GM_THREADS, 0, s>>>(n, nv, V, wv, w.part, hcol, ctl);
+      k_gm_sub_dots<<<gb, GM_THREADS, 0, s>>>(n, nv, V, hcol, h2, wv, w.part, ctl);
+      k_gm_sub_norm<<<gb, GM_THREADS, 0, s>>>(n, nv, V, h2, wv, w.part, ctl, m, j, hcol, H, cs, sn, g, inv_norm,
+                                              inner_tol);
+      k_gm_normalize<<<vg, 256, 0, s>>>(n, wv, inv_norm, V + (int64_t)(j + 1) * n, ctl);
+      w.launches += 5;
     }
-    ++w.launches;
-    k_backsolve<<<1, 1, 0, s>>>(m, j, H, g, y);
-    ++w.launches;
-    k_update_x<<<vg, 256, 0, s>>>(n, j, V, y, rr, x);
+    k_gm_backsolve<<<1, 1, 0, s>>>(m, H, g, y, ctl, sc + 2);
+    k_gm_update_x<<<vg, 256, 0, s>>>(n, m, V, y, rr, x, ctl);
+    w.launches += 2;
   }
   *iters = total;
   *refines = ref;

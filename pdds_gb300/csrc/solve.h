@@ -16,12 +16,13 @@ struct SolveCsr {
 struct SolveWork {
   double* v64[6];   // K doubles each
   double* scal;     // 32 doubles
-  double* part;     // reduction partials, >= 2*256 and 64*256 doubles
-  double* hess;     // (m+1)m + 2m + 3(m+1) doubles
+  double* part;     // reduction partials, >= 2*256 and 48*64 doubles
+  double* hess;     // (m+1)m + 2m + 4(m+1) doubles
   float* V32;       // (m+1) K floats
   float* w32;       // K floats
   float* val32;     // nnz floats
   double* host_rr;  // pinned host scalar
+  unsigned* ctl;    // 4 unsigned: GMRES ticket, convergence flag, basis size
   int launches;     // kernels launched by the last solve
 };
 
