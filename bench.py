@@ -130,7 +130,13 @@ def cpu_baseline(workload: dict, fac, n_knots: int, seed: int = 1234, npaths=Non
     N = npaths or workload["npaths"]
     threads = os.cpu_count() or 1
     prm = O.make_params(N, workload["h"], seed=seed, fac=fac, sublinear=True, threads=threads)
-    prob = O.make_problem(O.POISSON_SINCOS)
+    if workload.get("problem") == "varcoef_lut":
+        from pdds_gb300.config import varcoef_tables
+        O.set_lut(*varcoef_tables(workload["lut_n"], (workload["sw"][0], workload["sw"][1],
+                                                      workload["ne"][0], workload["ne"][1])))
+        prob = O.make_problem(O.LUT)
+    else:
+        prob = O.make_problem(O.POISSON_SINCOS)
     t0 = time.perf_counter()
     res = L.run(prob, prm, knots=sel)
     dt = time.perf_counter() - t0
@@ -203,7 +209,11 @@ def main():
     torch.cuda.set_device(local)
     import pdds_gb300 as P
 
-    bvp = P.BVP.poisson_sincos()
+    if workload.get("problem") == "varcoef_lut":
+        bvp = P.BVP.varcoef_lut(workload["lut_n"], (workload["sw"][0], workload["sw"][1],
+                                                     workload["ne"][0], workload["ne"][1]))
+    else:
+        bvp = P.BVP.poisson_sincos()
     N, h = workload["npaths"], workload["h"]
     pd = P.PDDSparseGM(workload["sw"], workload["ne"], workload["nsub"], workload["nnode"], fac, device=local)
     exact = bvp.u(pd.x, pd.y)

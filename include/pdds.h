@@ -58,8 +58,9 @@ typedef enum {
   PDDS_POISSON_SINCOS = 0, /* u = sin(pi x)cos(pi y) + x y, sigma = sqrt2 I, f = -Lap u  */
   PDDS_MONEGROS = 1,       /* the reference's Monegros Poisson test problem            */
   PDDS_HELMHOLTZ = 2,      /* u = sin(a x)cos(b y); p = {a, b, c}, c <= 0               */
-  PDDS_VARCOEF = 3         /* sigma = diag(1+x^2/2, 1+y^2/2), b = (y,-x),
+  PDDS_VARCOEF = 3,        /* sigma = diag(1+x^2/2, 1+y^2/2), b = (y,-x),
                               c = -(1+x^2+y^2), u = e^x cos 2y + 1                      */
+  PDDS_LUT = 4             /* diagonal sigma, b, c, f, grad u and g served from tables  */
 } pdds_problem_kind;
 
 typedef struct {
@@ -69,6 +70,16 @@ typedef struct {
 } pdds_problem_desc;
 
 pdds_status pdds_problem_set(pdds_ctx* ctx, const pdds_problem_desc* desc);
+
+/* Tables of the PDDS_LUT problem (replaces the reference's LUT coefficient
+ * sources: GSL splines, BVPs/EDPs/Monegros_Helmhotz.hpp:50-61, and the CUDA
+ * LUT texture, BVPs/LUT2.cuh:11-92).  coef is host memory [ny][nx][8] FP32,
+ * fields (sigma11, sigma22, b1, b2, c, f, du/dx, du/dy) on the grid
+ * x_i = bounds[0] + i (bounds[2]-bounds[0])/(nx-1), y_j likewise; g is
+ * [ny][nx] FP32 boundary values.  Sampled with bicubic Catmull-Rom
+ * interpolation, clamped at the table edges.  Copied to the device. */
+pdds_status pdds_problem_set_lut(pdds_ctx* ctx, const float* coef, const float* g, int32_t nx, int32_t ny,
+                                 const double bounds[4]);
 
 /* ---------------------------------------------------------------- layout
  * Rectangular domain [SW, NE] split into nsub x nsub subdomains with nnode

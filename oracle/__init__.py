@@ -21,7 +21,7 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
 
-POISSON_SINCOS, MONEGROS, HELMHOLTZ, VARCOEF = 0, 1, 2, 3
+POISSON_SINCOS, MONEGROS, HELMHOLTZ, VARCOEF, LUT = 0, 1, 2, 3, 4
 
 
 class Problem(C.Structure):
@@ -81,6 +81,7 @@ def lib():
         L.orc_run.argtypes = [vp, C.POINTER(Problem), C.POINTER(Params), ip, dp, dp, C.c_int, ip,
                               ip, dp, dp, C.c_int64, dp, dp, i64p]
         L.orc_bicgstab.argtypes = [C.c_int, C.c_int64, ip, ip, dp, dp, dp, C.c_int, C.c_double, ip, dp]
+        L.orc_set_lut.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int, C.c_int, dp]
         L.orc_problem_u.restype = C.c_double
         L.orc_problem_u.argtypes = [C.POINTER(Problem), C.c_double, C.c_double]
         _lib = L
@@ -274,6 +275,15 @@ def bicgstab(K, rows, cols, vals, b, maxit=None, tol=2.220446049250313e-16):
                        _p(b, C.c_double), _p(x, C.c_double), int(maxit if maxit else 2 * K), float(tol),
                        C.byref(it), C.byref(err))
     return x, it.value, err.value
+
+
+def set_lut(coef, g, bounds):
+    """Tables of the LUT problem (coef [ny][nx][8], g [ny][nx] float32)."""
+    coef = np.ascontiguousarray(coef, np.float32)
+    g = np.ascontiguousarray(g, np.float32)
+    b = np.ascontiguousarray(bounds, np.float64)
+    ny, nx = g.shape
+    lib().orc_set_lut(_p(coef, C.c_float), _p(g, C.c_float), nx, ny, _p(b, C.c_double))
 
 
 def problem_u(problem: Problem, x, y):

@@ -59,6 +59,69 @@ const double SQRT2 = 1.4142135623730951;
 const double PI = pdds::pm::PI;
 const double TWO_PI_SQ = 19.739208802178716;  // 2 pi^2
 
+// Tables of the LUT problem (orc_set_lut): bicubic Catmull-Rom in FP64 from
+// FP32 nodes, clamped at the edges, in the operation order of the device
+// sampler so the replay mode stays bit-exact.
+struct LutTables {
+  std::vector<float> coef, g;  // [ny][nx][8], [ny][nx]
+  int nx = 0, ny = 0;
+  double x0 = 0, y0 = 0, inv_dx = 0, inv_dy = 0;
+};
+LutTables g_lut;
+
+void cr_w(double t, double* w) {
+  const double t2 = t * t, t3 = t2 * t;
+  w[0] = 0.5 * ((2.0 * t2 - t3) - t);
+  w[1] = 0.5 * ((3.0 * t3 - 5.0 * t2) + 2.0);
+  w[2] = 0.5 * ((4.0 * t2 - 3.0 * t3) + t);
+  w[3] = 0.5 * (t3 - t2);
+}
+void lut_c(double x, double x0, double inv, int n, int& i, double& t) {
+  double g = (x - x0) * inv;
+  g = g < 0.0 ? 0.0 : g;
+  g = g > (double)(n - 1) ? (double)(n - 1) : g;
+  i = (int)std::floor(g);
+  if (i > n - 2) i = n - 2;
+  t = g - (double)i;
+}
+int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+void lut_sample8(double x, double y, double* out) {
+  const LutTables& L = g_lut;
+  int ix, iy;
+  double tx, ty, wx[4], wy[4];
+  lut_c(x, L.x0, L.inv_dx, L.nx, ix, tx);
+  lut_c(y, L.y0, L.inv_dy, L.ny, iy, ty);
+  cr_w(tx, wx);
+  cr_w(ty, wy);
+  for (int f = 0; f < 8; f++) out[f] = 0.0;
+  for (int r = 0; r < 4; r++) {
+    const float* row = &L.coef[(size_t)8 * clampi(iy - 1 + r, 0, L.ny - 1) * L.nx];
+    double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int c = 0; c < 4; c++) {
+      const float* v = row + 8 * clampi(ix - 1 + c, 0, L.nx - 1);
+      for (int f = 0; f < 8; f++) acc[f] += wx[c] * (double)v[f];
+    }
+    for (int f = 0; f < 8; f++) out[f] += wy[r] * acc[f];
+  }
+}
+double lut_sample_g(double x, double y) {
+  const LutTables& L = g_lut;
+  int ix, iy;
+  double tx, ty, wx[4], wy[4];
+  lut_c(x, L.x0, L.inv_dx, L.nx, ix, tx);
+  lut_c(y, L.y0, L.inv_dy, L.ny, iy, ty);
+  cr_w(tx, wx);
+  cr_w(ty, wy);
+  double out = 0.0;
+  for (int r = 0; r < 4; r++) {
+    const float* row = &L.g[(size_t)clampi(iy - 1 + r, 0, L.ny - 1) * L.nx];
+    double acc = 0.0;
+    for (int c = 0; c < 4; c++) acc += wx[c] * (double)row[clampi(ix - 1 + c, 0, L.nx - 1)];
+    out += wy[r] * acc;
+  }
+  return out;
+}
+
 // Coefficients at one point: sigma (row-major 2x2), drift b, reaction c,
 // source f, gradient of u (control variate).
 struct Coef {
@@ -130,12 +193,20 @@ struct Problem {
         M::sincos(2.0 * y, &s2, &c2);
         return M::exp(x) * c2 + 1.0;
       }
+      case ORC_LUT: return lut_sample_g(x, y);
     }
     return 0.0;
   }
   double g(double x, double y) const { return u(x, y); }
   void coef(double x, double y, Coef& k) const {
     switch (P->kind) {
+      case ORC_LUT: {
+        double v[8];
+        lut_sample8(x, y, v);
+        k.s[0] = v[0]; k.s[1] = 0.0; k.s[2] = 0.0; k.s[3] = v[1];
+        k.b[0] = v[2]; k.b[1] = v[3]; k.c = v[4]; k.f = v[5]; k.gr[0] = v[6]; k.gr[1] = v[7];
+        return;
+      }
       case ORC_POISSON_SINCOS: {
         double sx, cx, sy, cy;
         M::sincos(PI * x, &sx, &cx);
@@ -691,6 +762,17 @@ int orc_bicgstab(int K, int64_t nnz, const int* ri, const int* ci, const double*
   *iters = i;
   *err = std::sqrt(dot(r, r) / rhs_sq);
   return 0;
+}
+
+void orc_set_lut(const float* coef, const float* g, int nx, int ny, const double* bounds) {
+  g_lut.coef.assign(coef, coef + (size_t)8 * nx * ny);
+  g_lut.g.assign(g, g + (size_t)nx * ny);
+  g_lut.nx = nx;
+  g_lut.ny = ny;
+  g_lut.x0 = bounds[0];
+  g_lut.y0 = bounds[1];
+  g_lut.inv_dx = 1.0 / ((bounds[2] - bounds[0]) / (nx - 1));
+  g_lut.inv_dy = 1.0 / ((bounds[3] - bounds[1]) / (ny - 1));
 }
 
 double orc_problem_u(const orc_problem* P, double x, double y) {

@@ -15,7 +15,8 @@ enum {
   ORC_POISSON_SINCOS = 0, /* u = sin(pi x)cos(pi y) + xy, sigma = sqrt2 I        */
   ORC_MONEGROS = 1,       /* BVPs/EDPs/Monegros_Poisson_CPP.hpp (libm only)      */
   ORC_HELMHOLTZ = 2,      /* u = sin(a x)cos(b y), c const; p = {a, b, c}       */
-  ORC_VARCOEF = 3         /* sigma = diag(1+x^2/2, 1+y^2/2), b = (y,-x), ...    */
+  ORC_VARCOEF = 3,        /* sigma = diag(1+x^2/2, 1+y^2/2), b = (y,-x), ...    */
+  ORC_LUT = 4             /* coefficients and g from tables (orc_set_lut)       */
 };
 
 typedef struct {
@@ -78,6 +79,10 @@ int orc_run(const void* L, const orc_problem* P, const orc_params* prm, const in
  * BiCGSTAB with zero start (PDDSparseGM.cpp:3168-3246). */
 int orc_bicgstab(int K, int64_t nnz, const int* ri, const int* ci, const double* v,
                  const double* b, double* x, int maxit, double tol, int* iters, double* err);
+
+/* Tables of ORC_LUT: coef [ny][nx][8] = (sigma11, sigma22, b1, b2, c, f,
+ * du/dx, du/dy), g [ny][nx]; bounds {x0, y0, x1, y1}.  Copied. */
+void orc_set_lut(const float* coef, const float* g, int nx, int ny, const double* bounds);
 
 /* ---- problem functions (for analytic checks) ------------------------------*/
 double orc_problem_u(const orc_problem* P, double x, double y);

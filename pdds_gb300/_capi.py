@@ -18,12 +18,12 @@ STATUS_NAMES = {0: "PDDS_OK", 1: "PDDS_ERR_INVALID", 2: "PDDS_ERR_CUDA", 3: "PDD
                 4: "PDDS_ERR_TIMEOUT", 5: "PDDS_ERR_ILL_CONDITIONED", 6: "PDDS_ERR_NOT_CONVERGED",
                 7: "PDDS_ERR_NO_MEMORY", 8: "PDDS_ERR_EXIT_SIDE"}
 
-POISSON_SINCOS, MONEGROS, HELMHOLTZ, VARCOEF = 0, 1, 2, 3
+POISSON_SINCOS, MONEGROS, HELMHOLTZ, VARCOEF, LUT = 0, 1, 2, 3, 4
 MODE_REPLAY_FP64, MODE_FP64, MODE_MIXED = 0, 1, 2
 SOLVE_BICGSTAB_FP64, SOLVE_GMRES_FP32_IR = 0, 1
 
 EXPORTS = [
-    "pdds_create", "pdds_destroy", "pdds_last_error", "pdds_version", "pdds_problem_set",
+    "pdds_create", "pdds_destroy", "pdds_last_error", "pdds_version", "pdds_problem_set", "pdds_problem_set_lut",
     "pdds_layout_build", "pdds_layout_knots", "pdds_layout_csr", "pdds_layout_stencil",
     "pdds_estimate", "pdds_solve_interface", "pdds_solve_bicgstab_static",
 ]
@@ -90,6 +90,8 @@ def load(path: str = LIB_PATH):
     L.pdds_last_error.argtypes = [vp]
     L.pdds_version.restype = C.c_char_p
     L.pdds_problem_set.argtypes = [vp, C.POINTER(ProblemDesc)]
+    L.pdds_problem_set_lut.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int32, C.c_int32,
+                                       C.POINTER(C.c_double)]
     L.pdds_layout_build.argtypes = [vp, C.POINTER(LayoutDesc), C.POINTER(LayoutInfo)]
     L.pdds_layout_knots.argtypes = [vp, dp, dp, C.POINTER(C.c_int32)]
     L.pdds_layout_csr.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int32)]

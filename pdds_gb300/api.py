@@ -33,11 +33,14 @@ class BVP:
     MONEGROS = capi.MONEGROS
     HELMHOLTZ = capi.HELMHOLTZ
     VARCOEF = capi.VARCOEF
+    LUT = capi.LUT
 
-    def __init__(self, kind: int, params=(), use_cv: bool = True):
+    def __init__(self, kind: int, params=(), use_cv: bool = True, tables=None, exact=None):
         self.kind = int(kind)
         self.params = tuple(float(v) for v in params)
         self.use_cv = bool(use_cv)
+        self.tables = tables      # (coef [ny][nx][8], g [ny][nx], bounds) for LUT problems
+        self.exact = exact        # optional exact solution u(x, y) for LUT problems
 
     @classmethod
     def poisson_sincos(cls):
@@ -57,6 +60,21 @@ class BVP:
     def varcoef(cls):
         return cls(cls.VARCOEF)
 
+    @classmethod
+    def lut(cls, coef, g, bounds, exact=None):
+        """Problem with diagonal sigma, b, c, f, grad u and g served from FP32
+        tables (bicubic Catmull-Rom); coef [ny][nx][8], g [ny][nx]."""
+        import numpy as np
+        return cls(cls.LUT, tables=(np.ascontiguousarray(coef, np.float32),
+                                    np.ascontiguousarray(g, np.float32), tuple(bounds)), exact=exact)
+
+    @classmethod
+    def varcoef_lut(cls, n: int = 1024, bounds=(0.0, 0.0, 1.0, 1.0)):
+        """The variable-coefficient problem served from n x n tables."""
+        from .config import varcoef_tables
+        coef, g, b = varcoef_tables(n, bounds)
+        return cls.lut(coef, g, b, exact=lambda x, y: np.exp(x) * np.cos(2 * y) + 1.0)
+
     def desc(self) -> capi.ProblemDesc:
         d = capi.ProblemDesc()
         d.kind = self.kind
@@ -69,6 +87,10 @@ class BVP:
         """Exact solution (numpy, FP64)."""
         x = np.asarray(x, np.float64)
         y = np.asarray(y, np.float64)
+        if self.kind == self.LUT:
+            if self.exact is None:
+                raise ValueError("no exact solution attached to this table problem")
+            return self.exact(x, y)
         if self.kind == self.POISSON_SINCOS:
             return np.sin(np.pi * x) * np.cos(np.pi * y) + x * y
         if self.kind == self.HELMHOLTZ:
@@ -222,6 +244,13 @@ class PDDSparseGM:
                  bins_per_gap: int = 0, max_steps: int = 0, ipsi_override=None,
                  adaptive_h: bool = False, richardson: bool = False, reuse_tables: bool = False) -> Estimate:
         """Runs the Feynman-Kac estimation of every knot's G row and B entry."""
+        if bvp.kind == BVP.LUT and getattr(self, "_lut_owner", None) is not bvp.tables:
+            coef, g, bounds = bvp.tables
+            ny, nx = g.shape
+            b = np.ascontiguousarray(bounds, np.float64)
+            self._check(self._lib.pdds_problem_set_lut(self._ctx, _p(coef, C.c_float), _p(g, C.c_float), nx, ny,
+                                                       _p(b, C.c_double)))
+            self._lut_owner = bvp.tables
         self._check(self._lib.pdds_problem_set(self._ctx, C.byref(bvp.desc())))
         d = capi.EstimateDesc()
         d.mode = int(mode)

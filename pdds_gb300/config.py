@@ -33,6 +33,32 @@ WORKLOADS = {
     "poisson_4x4_n11": dict(sw=(-1.0, -1.0), ne=(1.0, 1.0), nsub=4, nnode=11, npaths=10_000, h=1e-3),
     # the same problem scaled up: 12x12 subdomains, 43 knots per segment
     "poisson_12x12_n43": dict(sw=(-1.0, -1.0), ne=(1.0, 1.0), nsub=12, nnode=43, npaths=20_000, h=5e-4),
-    # variable coefficients on [0,1]^2, 8x8 subdomains, 31 knots per segment
-    "varcoef_8x8_n31": dict(sw=(0.0, 0.0), ne=(1.0, 1.0), nsub=8, nnode=31, npaths=50_000, h=5e-4),
+    # variable coefficients on [0,1]^2 served from 1024^2 FP32 tables, 8x8 subdomains, 31 knots per segment
+    "varcoef_lut_8x8_n31": dict(sw=(0.0, 0.0), ne=(1.0, 1.0), nsub=8, nnode=31, npaths=50_000, h=5e-4,
+                                problem="varcoef_lut", lut_n=1024),
 }
+
+
+def varcoef_tables(n: int = 1024, bounds=(0.0, 0.0, 1.0, 1.0)):
+    """Coefficient and boundary tables of the variable-coefficient problem
+    0.5 sum (sigma sigma^T)_ij d_ij u + b.grad u + c u + f = 0 with
+    sigma = diag(1 + x^2/2, 1 + y^2/2), b = (y, -x), c = -(1 + x^2 + y^2),
+    u = exp(x) cos(2y) + 1 and f derived from u, sampled on an n x n grid
+    over bounds (x0, y0, x1, y1) in FP32.  Fields per node: sigma11, sigma22,
+    b1, b2, c, f, du/dx, du/dy.  Returns (coef [n][n][8], g [n][n], bounds)."""
+    import numpy as np
+    x0, y0, x1, y1 = bounds
+    xs = x0 + (x1 - x0) * np.arange(n) / (n - 1)
+    ys = y0 + (y1 - y0) * np.arange(n) / (n - 1)
+    X, Y = np.meshgrid(xs, ys)  # [ny][nx]
+    s1 = 1.0 + 0.5 * X * X
+    s2 = 1.0 + 0.5 * Y * Y
+    ex = np.exp(X)
+    ux = ex * np.cos(2 * Y)
+    uy = -2.0 * ex * np.sin(2 * Y)
+    uxx, uyy = ux, -4.0 * ux
+    c = -(1.0 + X * X + Y * Y)
+    u = ux + 1.0
+    f = -(0.5 * (s1 * s1 * uxx + s2 * s2 * uyy) + (Y * ux - X * uy) + c * u)
+    coef = np.stack([s1, s2, Y, -X, c, f, ux, uy], axis=-1).astype(np.float32)
+    return np.ascontiguousarray(coef), np.ascontiguousarray(u.astype(np.float32)), tuple(float(b) for b in bounds)

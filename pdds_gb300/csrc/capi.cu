@@ -53,6 +53,9 @@ struct pdds_ctx {
   std::string err;
   bool has_problem = false;
   pdds_problem_desc prob{};
+  DBuf<float> lut_coef, lut_g;
+  int lut_nx = 0, lut_ny = 0;
+  double lut_bounds[4] = {0, 0, 0, 0};
   bool has_layout = false;
   HostLayout L;
   int bins = 16;
@@ -229,11 +232,20 @@ pdds_status upload_layout(pdds_ctx* ctx) {
   return PDDS_OK;
 }
 
-ProblemDev problem_dev(const pdds_problem_desc& p) {
+ProblemDev problem_dev(const pdds_ctx* ctx) {
+  const pdds_problem_desc& p = ctx->prob;
   ProblemDev d;
   d.kind = p.kind;
   d.use_cv = p.use_cv;
   for (int i = 0; i < 8; i++) d.p[i] = p.p[i];
+  d.lut.coef = reinterpret_cast<const float4*>(ctx->lut_coef.p);
+  d.lut.g = ctx->lut_g.p;
+  d.lut.nx = ctx->lut_nx;
+  d.lut.ny = ctx->lut_ny;
+  d.lut.x0 = ctx->lut_bounds[0];
+  d.lut.y0 = ctx->lut_bounds[1];
+  d.lut.inv_dx = ctx->lut_nx > 1 ? 1.0 / ((ctx->lut_bounds[2] - ctx->lut_bounds[0]) / (ctx->lut_nx - 1)) : 0.0;
+  d.lut.inv_dy = ctx->lut_ny > 1 ? 1.0 / ((ctx->lut_bounds[3] - ctx->lut_bounds[1]) / (ctx->lut_ny - 1)) : 0.0;
   return d;
 }
 
@@ -300,6 +312,8 @@ pdds_status pdds_destroy(pdds_ctx* ctx) {
     for (auto* b : dl) b->release();
     ctx->map_owner.release();
     ctx->tab.release();
+    ctx->lut_coef.release();
+    ctx->lut_g.release();
     ctx->stats.release();
     ctx->errf.release();
     ctx->sV32.release();
@@ -320,11 +334,32 @@ const char* pdds_last_error(const pdds_ctx* ctx) { return ctx ? ctx->err.c_str()
 
 pdds_status pdds_problem_set(pdds_ctx* ctx, const pdds_problem_desc* desc) {
   if (!ctx || !desc) return PDDS_ERR_INVALID;
-  if (desc->kind < 0 || desc->kind > 3) return fail(ctx, PDDS_ERR_INVALID, "unknown problem kind");
+  if (desc->kind < 0 || desc->kind > 4) return fail(ctx, PDDS_ERR_INVALID, "unknown problem kind");
+  if (desc->kind == PDDS_LUT && ctx->lut_nx < 4)
+    return fail(ctx, PDDS_ERR_INVALID, "PDDS_LUT needs pdds_problem_set_lut first");
   if (desc->kind == PDDS_HELMHOLTZ && desc->p[2] > 0.0)
     return fail(ctx, PDDS_ERR_INVALID, "Helmholtz reaction c must be <= 0");
   ctx->prob = *desc;
   ctx->has_problem = true;
+  return PDDS_OK;
+}
+
+pdds_status pdds_problem_set_lut(pdds_ctx* ctx, const float* coef, const float* g, int32_t nx, int32_t ny,
+                                 const double bounds[4]) {
+  if (!ctx || !coef || !g || !bounds) return PDDS_ERR_INVALID;
+  if (nx < 4 || ny < 4) return fail(ctx, PDDS_ERR_INVALID, "tables need at least 4 x 4 nodes");
+  if (!(bounds[2] > bounds[0] && bounds[3] > bounds[1])) return fail(ctx, PDDS_ERR_INVALID, "bad table bounds");
+  if (ctx->device < 0) return fail(ctx, PDDS_ERR_INVALID, "context has no device");
+  CK(cudaSetDevice(ctx->device));
+  const size_t n = (size_t)nx * ny;
+  CK(ctx->lut_coef.resize(8 * n));
+  CK(ctx->lut_g.resize(n));
+  CK(cudaMemcpyAsync(ctx->lut_coef.p, coef, 8 * n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->lut_g.p, g, n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->lut_nx = nx;
+  ctx->lut_ny = ny;
+  for (int q = 0; q < 4; q++) ctx->lut_bounds[q] = bounds[q];
   return PDDS_OK;
 }
 
@@ -413,7 +448,7 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
   }
   const int64_t nnz = L.row_ptr[L.K];
   const long long max_steps = desc->max_steps > 0 ? desc->max_steps : 1000000LL;
-  const ProblemDev P = problem_dev(ctx->prob);
+  const ProblemDev P = problem_dev(ctx);
   const int N = desc->npaths;
   int launches = 0;
   CK(cudaEventRecord(ctx->ev0, s));

@@ -51,13 +51,100 @@ struct DevLayout {
   const double* ipsi;
 };
 
+// Coefficient tables of the PK_LUT problem: node (i, j) of an nx x ny grid
+// over [x0, x0 + (nx-1) dx] x [y0, y0 + (ny-1) dy] holds two float4,
+// (sigma11, sigma22, b1, b2) and (c, f, du/dx, du/dy); g holds the
+// boundary/solution values on the same grid.
+struct LutDev {
+  const float4* coef;
+  const float* g;
+  int nx, ny;
+  double x0, y0, inv_dx, inv_dy;
+};
+
 struct ProblemDev {
   int kind;
   int use_cv;
   double p[8];
+  LutDev lut;
 };
 
-enum { PK_POISSON_SINCOS = 0, PK_MONEGROS = 1, PK_HELMHOLTZ = 2, PK_VARCOEF = 3 };
+enum { PK_POISSON_SINCOS = 0, PK_MONEGROS = 1, PK_HELMHOLTZ = 2, PK_VARCOEF = 3, PK_LUT = 4 };
+
+// ------------------------------------------------------------------ tables
+// Bicubic Catmull-Rom (Keys cubic convolution, a = -1/2) interpolation,
+// clamped to the table edges like the reference's clamp-addressed LUT
+// texture (BVPs/LUT2.cuh:11-45).  The same arithmetic is used in FP32
+// (MIXED), FP64 (FP64 mode) and, compiled without FMA contraction, in the
+// replay kernels and the host restatement.
+template <typename T>
+__host__ __device__ __forceinline__ void cr_weights(T t, T* w) {
+  const T t2 = t * t, t3 = t2 * t;
+  w[0] = T(0.5) * ((T(2) * t2 - t3) - t);
+  w[1] = T(0.5) * ((T(3) * t3 - T(5) * t2) + T(2));
+  w[2] = T(0.5) * ((T(4) * t2 - T(3) * t3) + t);
+  w[3] = T(0.5) * (t3 - t2);
+}
+template <typename T>
+__host__ __device__ __forceinline__ void lut_coord(T x, T x0, T inv_dx, int n, int& i, T& t) {
+  T g = (x - x0) * inv_dx;
+  g = g < T(0) ? T(0) : g;
+  g = g > T(n - 1) ? T(n - 1) : g;
+  i = (int)floor(g);
+  if (i > n - 2) i = n - 2;
+  t = g - T(i);
+}
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// all eight fields (nf = 8) or the first four (nf = 4: sigma11, sigma22, b1, b2)
+template <typename T, int NF>
+__device__ __forceinline__ void lut_sample(const LutDev& L, T x, T y, T* out) {
+  int ix, iy;
+  T tx, ty, wx[4], wy[4];
+  lut_coord<T>(x, (T)L.x0, (T)L.inv_dx, L.nx, ix, tx);
+  lut_coord<T>(y, (T)L.y0, (T)L.inv_dy, L.ny, iy, ty);
+  cr_weights<T>(tx, wx);
+  cr_weights<T>(ty, wy);
+#pragma unroll
+  for (int f = 0; f < NF; f++) out[f] = T(0);
+#pragma unroll
+  for (int r = 0; r < 4; r++) {
+    const float4* row = L.coef + (int64_t)2 * clampi(iy - 1 + r, 0, L.ny - 1) * L.nx;
+    T acc[NF];
+#pragma unroll
+    for (int f = 0; f < NF; f++) acc[f] = T(0);
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+      const int xx = clampi(ix - 1 + c, 0, L.nx - 1);
+      const float4 a = __ldg(row + 2 * xx);
+      acc[0] += wx[c] * (T)a.x; acc[1] += wx[c] * (T)a.y; acc[2] += wx[c] * (T)a.z; acc[3] += wx[c] * (T)a.w;
+      if (NF == 8) {
+        const float4 b = __ldg(row + 2 * xx + 1);
+        acc[NF > 4 ? 4 : 0] += wx[c] * (T)b.x; acc[NF > 5 ? 5 : 0] += wx[c] * (T)b.y;
+        acc[NF > 6 ? 6 : 0] += wx[c] * (T)b.z; acc[NF > 7 ? 7 : 0] += wx[c] * (T)b.w;
+      }
+    }
+#pragma unroll
+    for (int f = 0; f < NF; f++) out[f] += wy[r] * acc[f];
+  }
+}
+template <typename T>
+__device__ __forceinline__ T lut_sample_g(const LutDev& L, T x, T y) {
+  int ix, iy;
+  T tx, ty, wx[4], wy[4];
+  lut_coord<T>(x, (T)L.x0, (T)L.inv_dx, L.nx, ix, tx);
+  lut_coord<T>(y, (T)L.y0, (T)L.inv_dy, L.ny, iy, ty);
+  cr_weights<T>(tx, wx);
+  cr_weights<T>(ty, wy);
+  T out = T(0);
+  for (int r = 0; r < 4; r++) {
+    const float* row = L.g + (int64_t)clampi(iy - 1 + r, 0, L.ny - 1) * L.nx;
+    T acc = T(0);
+    for (int c = 0; c < 4; c++) acc += wx[c] * (T)__ldg(row + clampi(ix - 1 + c, 0, L.nx - 1));
+    out += wy[r] * acc;
+  }
+  return out;
+}
 
 template <typename T>
 struct Coef {
@@ -73,7 +160,12 @@ struct Coef {
 template <int KIND>
 __device__ __forceinline__ void coef_f32(const ProblemDev& P, float x, float y, Coef<float>& k) {
   const float PI = 3.14159265358979f;
-  if (KIND == PK_POISSON_SINCOS) {
+  if (KIND == PK_LUT) {
+    float v[8];
+    lut_sample<float, 8>(P.lut, x, y, v);
+    k.s00 = v[0]; k.s01 = 0.f; k.s10 = 0.f; k.s11 = v[1];
+    k.b0 = v[2]; k.b1 = v[3]; k.c = v[4]; k.f = v[5]; k.g0 = v[6]; k.g1 = v[7];
+  } else if (KIND == PK_POISSON_SINCOS) {
     float sx, cx, sy, cy;
     __sincosf(PI * x, &sx, &cx);
     __sincosf(PI * y, &sy, &cy);
@@ -130,8 +222,13 @@ __device__ __forceinline__ void coef_f32(const ProblemDev& P, float x, float y, 
 
 // sigma alone (for the exit threshold)
 template <int KIND>
-__device__ __forceinline__ void sigma_f32(float x, float y, float& s00, float& s01, float& s10, float& s11) {
-  if (KIND == PK_VARCOEF) {
+__device__ __forceinline__ void sigma_f32(const ProblemDev& P, float x, float y, float& s00, float& s01,
+                                          float& s10, float& s11) {
+  if (KIND == PK_LUT) {
+    float v[4];
+    lut_sample<float, 4>(P.lut, x, y, v);
+    s00 = v[0]; s01 = 0.f; s10 = 0.f; s11 = v[1];
+  } else if (KIND == PK_VARCOEF) {
     s00 = 1.f + 0.5f * (x * x); s01 = 0.f; s10 = 0.f; s11 = 1.f + 0.5f * (y * y);
   } else if (KIND == PK_MONEGROS) {
     s00 = 1.41421356237f; s01 = 0.f; s10 = 0.f; s11 = 1.41421356237f;
@@ -142,8 +239,13 @@ __device__ __forceinline__ void sigma_f32(float x, float y, float& s00, float& s
 
 // |N^T sigma| for the x normal (1,0) and the y normal (0,1) (diagonal sigma)
 template <int KIND>
-__device__ __forceinline__ void sigma_normals_f32(float x, float y, float& nx, float& ny) {
-  if (KIND == PK_VARCOEF) {
+__device__ __forceinline__ void sigma_normals_f32(const ProblemDev& P, float x, float y, float& nx, float& ny) {
+  if (KIND == PK_LUT) {
+    float v[4];
+    lut_sample<float, 4>(P.lut, x, y, v);
+    nx = fabsf(v[0]);
+    ny = fabsf(v[1]);
+  } else if (KIND == PK_VARCOEF) {
     nx = 1.f + 0.5f * (x * x);
     ny = 1.f + 0.5f * (y * y);
   } else if (KIND == PK_MONEGROS) {
@@ -155,7 +257,9 @@ __device__ __forceinline__ void sigma_normals_f32(float x, float y, float& nx, f
 
 template <int KIND>
 __device__ __forceinline__ float u_f32(const ProblemDev& P, float x, float y) {
-  if (KIND == PK_POISSON_SINCOS) {
+  if (KIND == PK_LUT) {
+    return lut_sample_g<float>(P.lut, x, y);
+  } else if (KIND == PK_POISSON_SINCOS) {
     float sx, cx, sy, cy;
     __sincosf(3.14159265358979f * x, &sx, &cx);
     __sincosf(3.14159265358979f * y, &sy, &cy);
@@ -175,7 +279,12 @@ __device__ __forceinline__ float u_f32(const ProblemDev& P, float x, float y) {
 template <int KIND>
 __device__ __forceinline__ void coef_f64(const ProblemDev& P, double x, double y, Coef<double>& k) {
   const double PI = 3.141592653589793;
-  if (KIND == PK_POISSON_SINCOS) {
+  if (KIND == PK_LUT) {
+    double v[8];
+    lut_sample<double, 8>(P.lut, x, y, v);
+    k.s00 = v[0]; k.s01 = 0.0; k.s10 = 0.0; k.s11 = v[1];
+    k.b0 = v[2]; k.b1 = v[3]; k.c = v[4]; k.f = v[5]; k.g0 = v[6]; k.g1 = v[7];
+  } else if (KIND == PK_POISSON_SINCOS) {
     double sx, cx, sy, cy;
     sincospi(x, &sx, &cx);
     sincospi(y, &sy, &cy);
@@ -232,7 +341,9 @@ __device__ __forceinline__ void coef_f64(const ProblemDev& P, double x, double y
 
 template <int KIND>
 __device__ __forceinline__ double u_f64(const ProblemDev& P, double x, double y) {
-  if (KIND == PK_POISSON_SINCOS) {
+  if (KIND == PK_LUT) {
+    return lut_sample_g<double>(P.lut, x, y);
+  } else if (KIND == PK_POISSON_SINCOS) {
     double sx, cx, sy, cy;
     sincospi(x, &sx, &cx);
     sincospi(y, &sy, &cy);

@@ -281,6 +281,7 @@ static cudaError_t launch_fp64_t(const Fp64Args& a, int kind, int grid, size_t s
     PDDS_FP64_CASE(1)
     PDDS_FP64_CASE(2)
     PDDS_FP64_CASE(3)
+    PDDS_FP64_CASE(4)
     default: return cudaErrorInvalidValue;
   }
 #undef PDDS_FP64_CASE
@@ -298,6 +299,7 @@ static int blocks64_t(int kind, size_t smem) {
     case 0: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_paths_fp64<0, RICH>, FP64_THREADS, smem); break;
     case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_paths_fp64<1, RICH>, FP64_THREADS, smem); break;
     case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_paths_fp64<2, RICH>, FP64_THREADS, smem); break;
+    case 4: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_paths_fp64<4, RICH>, FP64_THREADS, smem); break;
     default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_paths_fp64<3, RICH>, FP64_THREADS, smem); break;
   }
   return nb;

@@ -24,6 +24,8 @@ __device__ double g_port(const ProblemDev& P, double x, double y) {
     double s2, c2;
     pm::sincos(2.0 * y, &s2, &c2);
     return pm::exp(x) * c2 + 1.0;
+  } else if (KIND == PK_LUT) {
+    return lut_sample_g<double>(P.lut, x, y);
   }
   return u_f64<PK_MONEGROS>(P, x, y);
 }
@@ -66,6 +68,7 @@ cudaError_t launch_boundary_b(const DevLayout& L, const ProblemDev& P, int mode,
     case PK_POISSON_SINCOS: k_boundary<PK_POISSON_SINCOS><<<g, 128, 0, s>>>(L, P, portable, knots, n, B, BB); break;
     case PK_MONEGROS: k_boundary<PK_MONEGROS><<<g, 128, 0, s>>>(L, P, 0, knots, n, B, BB); break;
     case PK_HELMHOLTZ: k_boundary<PK_HELMHOLTZ><<<g, 128, 0, s>>>(L, P, portable, knots, n, B, BB); break;
+    case PK_LUT: k_boundary<PK_LUT><<<g, 128, 0, s>>>(L, P, portable, knots, n, B, BB); break;
     default: k_boundary<PK_VARCOEF><<<g, 128, 0, s>>>(L, P, portable, knots, n, B, BB); break;
   }
   return cudaGetLastError();

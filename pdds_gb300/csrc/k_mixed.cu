@@ -189,7 +189,7 @@ k_paths_mixed(const MixedArgs a) {
       ++s.steps;
       const float dx = fabsf(s.x - cx) - hx, dy = fabsf(s.y - cy) - hy;
       float nx, ny;  // |N^T sigma| for the x and y normals
-      sigma_normals_f32<KIND>(s.x, s.y, nx, ny);
+      sigma_normals_f32<KIND>(a.P, s.x, s.y, nx, ny);
       const float thr = -0.5826f * sq * (dx > dy ? nx : ny);
       return !(fmaxf(dx, dy) < thr) || s.steps >= (unsigned)a.max_steps;
     };
@@ -201,7 +201,7 @@ k_paths_mixed(const MixedArgs a) {
       (void)dist;
       if (s.steps >= (unsigned)a.max_steps) {
         float g00, g01, g10, g11;
-        sigma_f32<KIND>(s.x, s.y, g00, g01, g10, g11);
+        sigma_f32<KIND>(a.P, s.x, s.y, g00, g01, g10, g11);
         const float w0 = Nx * g00 + Ny * g10, w1 = Nx * g01 + Ny * g11;
         if (dist < -0.5826f * sqrtf(w0 * w0 + w1 * w1) * (wgt < 0.f ? sqrth : (RICH ? sqrth * 0.70710678f : sqrth))) {
           atomicOr(a.err_flags, ERR_FLAG_STEP_LIMIT);
@@ -397,6 +397,7 @@ static cudaError_t launch_mixed_t(const MixedArgs& a, int kind, int grid, size_t
     PDDS_MIXED_CASE(1)
     PDDS_MIXED_CASE(2)
     PDDS_MIXED_CASE(3)
+    PDDS_MIXED_CASE(4)
     default: return cudaErrorInvalidValue;
   }
 #undef PDDS_MIXED_CASE
@@ -419,6 +420,7 @@ static int blocks_t(int kind, size_t smem) {
     PDDS_OCC(0)
     PDDS_OCC(1)
     PDDS_OCC(2)
+    PDDS_OCC(4)
     default:
     PDDS_OCC(3)
   }

@@ -23,7 +23,12 @@ constexpr int DIR_N_ = 0, DIR_S_ = 1, DIR_E_ = 2, DIR_W_ = 3;
 template <int KIND>
 __device__ void coef_port(const ProblemDev& P, double x, double y, Coef<double>& k) {
   const double PI = pm::PI;
-  if (KIND == PK_POISSON_SINCOS) {
+  if (KIND == PK_LUT) {
+    double v[8];
+    lut_sample<double, 8>(P.lut, x, y, v);
+    k.s00 = v[0]; k.s01 = 0.0; k.s10 = 0.0; k.s11 = v[1];
+    k.b0 = v[2]; k.b1 = v[3]; k.c = v[4]; k.f = v[5]; k.g0 = v[6]; k.g1 = v[7];
+  } else if (KIND == PK_POISSON_SINCOS) {
     double sx, cx, sy, cy;
     pm::sincos(PI * x, &sx, &cx);
     pm::sincos(PI * y, &sy, &cy);
@@ -61,7 +66,9 @@ __device__ void coef_port(const ProblemDev& P, double x, double y, Coef<double>&
 
 template <int KIND>
 __device__ double u_port(const ProblemDev& P, double x, double y) {
-  if (KIND == PK_POISSON_SINCOS) {
+  if (KIND == PK_LUT) {
+    return lut_sample_g<double>(P.lut, x, y);
+  } else if (KIND == PK_POISSON_SINCOS) {
     double sx, cx, sy, cy;
     pm::sincos(pm::PI * x, &sx, &cx);
     pm::sincos(pm::PI * y, &sy, &cy);
@@ -288,6 +295,7 @@ cudaError_t launch_replay_paths(const ReplayArgs& a, int kind, cudaStream_t s) {
     case PK_POISSON_SINCOS: k_replay_paths<PK_POISSON_SINCOS><<<grid, th, 0, s>>>(a); break;
     case PK_HELMHOLTZ: k_replay_paths<PK_HELMHOLTZ><<<grid, th, 0, s>>>(a); break;
     case PK_VARCOEF: k_replay_paths<PK_VARCOEF><<<grid, th, 0, s>>>(a); break;
+    case PK_LUT: k_replay_paths<PK_LUT><<<grid, th, 0, s>>>(a); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
@@ -303,6 +311,7 @@ cudaError_t launch_replay_reduce(const ReplayArgs& a, int kind, const int* task_
     case PK_POISSON_SINCOS: k_replay_b<PK_POISSON_SINCOS><<<gb, 128, 0, s>>>(a); break;
     case PK_HELMHOLTZ: k_replay_b<PK_HELMHOLTZ><<<gb, 128, 0, s>>>(a); break;
     case PK_VARCOEF: k_replay_b<PK_VARCOEF><<<gb, 128, 0, s>>>(a); break;
+    case PK_LUT: k_replay_b<PK_LUT><<<gb, 128, 0, s>>>(a); break;
     default: return cudaErrorInvalidValue;
   }
   if (ntask > 0)
