@@ -684,7 +684,7 @@ pdds_status pdds_solve_interface(pdds_ctx* ctx, const pdds_solve_desc* desc, dou
   const int m = std::max(2, std::min(desc->restart > 0 ? desc->restart : 30, 40));
   CK(ctx->sv64.resize((size_t)6 * K));
   CK(ctx->sscal.resize(64));
-  CK(ctx->spart.resize(std::max<size_t>(64 * 256 + 1024, (size_t)((K + 1023) / 1024) * 48 + 64)));
+  CK(ctx->spart.resize(std::max<size_t>(64 * 256 + 1024, (size_t)((K + 127) / 128) * 48 + 64)));
   CK(ctx->shess.resize((size_t)(m + 1) * m + 2 * m + 4 * (m + 1) + 16));
   CK(ctx->sctl.resize(8));
   CK(ctx->su.resize(std::max(K, 1)));

@@ -61,8 +61,10 @@ __device__ __forceinline__ void normals_f32(uint32_t ua, uint32_t ub, float& z0,
   z1 = -rho * sn;
 }
 
+// Table-served coefficients (PK_LUT) need more live registers for the
+// bicubic accumulation: two CTAs per SM there, four otherwise.
 template <int KIND, bool RICH>
-__global__ void __launch_bounds__(MIXED_THREADS, 4)
+__global__ void __launch_bounds__(MIXED_THREADS, KIND == PK_LUT ? 2 : 4)
 k_paths_mixed(const MixedArgs a) {
   extern __shared__ float hist[];  // [sum nbins] (and the Y^2 histogram after it)
   __shared__ ItemSide s_side[4];

@@ -27,7 +27,6 @@ namespace {
 constexpr int SPMV_THREADS = 256;
 constexpr int RED_THREADS = 256;
 constexpr int RED_BLOCKS = 256;
-constexpr int MDOT_THREADS = 128;
 
 template <typename T>
 __global__ void k_spmv(int K, const int64_t* __restrict__ rp, const int* __restrict__ col,
@@ -144,82 +143,6 @@ __global__ void k_scale_to_f32(int n, const double* r, const double* nrm, float*
   const double inv = 1.0 / sqrt(*nrm);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v[i] = (float)(r[i] * inv);
 }
-// partial dots of w with V[0..j]: part[blk][i]
-__global__ void k_mdot_part(int n, int nv, const float* V, const float* w, double* part) {
-  extern __shared__ double sh[];  // [nv][MDOT_THREADS]
-  for (int i = 0; i < nv; i++) sh[i * MDOT_THREADS + threadIdx.x] = 0.0;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-    const float wk = w[k];
-    for (int i = 0; i < nv; i++) sh[i * MDOT_THREADS + threadIdx.x] += (double)(V[(int64_t)i * n + k] * wk);
-  }
-  __syncthreads();
-  for (int o = MDOT_THREADS / 2; o > 0; o >>= 1) {
-    if (threadIdx.x < o)
-      for (int i = 0; i < nv; i++) sh[i * MDOT_THREADS + threadIdx.x] += sh[i * MDOT_THREADS + threadIdx.x + o];
-    __syncthreads();
-  }
-  for (int i = threadIdx.x; i < nv; i += blockDim.x) part[(int64_t)blockIdx.x * nv + i] = sh[i * MDOT_THREADS];
-}
-__global__ void k_mdot_final(int nb, int nv, const double* part, double* h, int accumulate) {
-  const int i = threadIdx.x;
-  if (i >= nv) return;
-  double s = 0.0;
-  for (int b = 0; b < nb; b++) s += part[(int64_t)b * nv + i];
-  h[i] = accumulate ? h[i] + s : s;
-}
-__global__ void k_mdot_sub(int n, int nv, const float* V, const double* hsub, float* w) {
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-    float acc = w[k];
-    for (int i = 0; i < nv; i++) acc -= (float)hsub[i] * V[(int64_t)i * n + k];
-    w[k] = acc;
-  }
-}
-__global__ void k_normalize(int n, const double* nrm2, const float* w, float* v) {
-  const float inv = (float)(1.0 / sqrt(*nrm2));
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) v[k] = w[k] * inv;
-}
-// Givens update of Hessenberg column j; H is (m+1) x m column-major in hs,
-// cs/sn the rotations, g the rotated right-hand side (g[0] = 1 initially).
-__global__ void k_givens(int m, int j, double* H, const double* hcol, const double* nrm2, double* cs,
-                         double* sn, double* g) {
-  double* col = H + (int64_t)j * (m + 1);
-  for (int i = 0; i <= j; i++) col[i] = hcol[i];
-  col[j + 1] = sqrt(*nrm2);
-  for (int i = 0; i < j; i++) {
-    const double a = col[i], b = col[i + 1];
-    col[i] = cs[i] * a + sn[i] * b;
-    col[i + 1] = -sn[i] * a + cs[i] * b;
-  }
-  const double a = col[j], b = col[j + 1];
-  const double r = sqrt(a * a + b * b);
-  cs[j] = (r > 0.0) ? a / r : 1.0;
-  sn[j] = (r > 0.0) ? b / r : 0.0;
-  col[j] = r;
-  col[j + 1] = 0.0;
-  g[j + 1] = -sn[j] * g[j];
-  g[j] = cs[j] * g[j];
-}
-__global__ void k_backsolve(int m, int jdim, const double* H, const double* g, double* y) {
-  for (int i = jdim - 1; i >= 0; i--) {
-    double s = g[i];
-    for (int k = i + 1; k < jdim; k++) s -= H[(int64_t)k * (m + 1) + i] * y[k];
-    y[i] = s / H[(int64_t)i * (m + 1) + i];
-  }
-}
-// x += scale * sum_i y_i V_i, in FP64
-__global__ void k_update_x(int n, int jdim, const float* V, const double* y, const double* nrm2r,
-                           double* x) {
-  const double scale = sqrt(*nrm2r);
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-    double acc = 0.0;
-    for (int i = 0; i < jdim; i++) acc += y[i] * (double)V[(int64_t)i * n + k];
-    x[k] += scale * acc;
-  }
-}
-__global__ void k_gmres_init(double* g, int m) {
-  for (int i = 0; i <= m; i++) g[i] = 0.0;
-  g[0] = 1.0;
-}
 
 inline int vgrid(int n) { return std::max(1, std::min(1024, (n + 255) / 256)); }
 
@@ -316,7 +239,7 @@ cudaError_t solve_bicgstab(const SolveCsr& A, const double* b, double* x, SolveW
 namespace {
 
 constexpr int GM_THREADS = 256;
-constexpr int GM_CHUNK = 1024;   // elements per block
+constexpr int GM_CHUNK = 128;    // elements per block
 constexpr int GM_MAXV = 48;      // basis vectors (m + 1 <= 41)
 
 struct GmCtl {
