@@ -54,6 +54,13 @@ METRIC = "path-steps/s & interface solves/s at RMSE<=2e-3, mixed+batched vs plai
 W_STEP = 94
 W_EXIT = 42
 
+# DRAM bytes (read + write) of one k_paths_mixed launch, from one ncu capture
+# of the same workload (dram__bytes_read.sum + dram__bytes_write.sum); the
+# captures and their commands are summarised under profiles/.
+PATH_KERNEL_DRAM_BYTES = {
+    "poisson_12x12_n43": 36_007_936,
+}
+
 
 def _env_rank():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), \
@@ -325,7 +332,7 @@ def main():
     work = steps_done * W_STEP + exits * W_EXIT
     achieved = work / t_paths if t_paths > 0 else 0.0
     roof = {"bound": "issue", "achieved": achieved / 1e9, "peak": peak / 1e9, "unit": "Ginst/s",
-            "frac": achieved / peak, "traffic": None,
+            "frac": achieved / peak, "traffic": PATH_KERNEL_DRAM_BYTES.get(workload["name"]),
             "peak_source": f"{sm_count} SMs x 128 issue lanes x median SM clock {f_mhz:.0f} MHz under load",
             "kernel": "k_paths_mixed", "kernel_ms_per_launch": 1000 * t_paths / args.steps}
 

@@ -1,4 +1,4 @@
-// MIXED mode: FP32 Euler-Maruyama paths, FP64 per-knot accumulation.
+// MIXED mode: FP32 Euler-Maruyama paths, compensated per-lane sums, FP64 per-knot accumulation.
 //
 // One persistent CTA per slot processes work items (knot, chunk of paths).
 // Lanes step paths in FP32 with Philox-4x32-10 normals held in registers and
@@ -34,9 +34,19 @@ struct ItemSide {
 
 constexpr unsigned FULL = 0xffffffffu;
 
+// State of one level of a path.  With table-served coefficients the level
+// also carries the 8 table fields at its position: the end-of-step sample
+// gives sigma for the exit test and the coefficients of the next step.
+template <int KIND>
 struct Lvl {
   float x, y, Y, Z, xi;
   unsigned steps;
+};
+template <>
+struct Lvl<PK_LUT> {
+  float x, y, Y, Z, xi;
+  unsigned steps;
+  float cf[8];
 };
 
 // A pending exit deposit: histogram index of the first of the 4 cubic
@@ -47,6 +57,15 @@ struct QEntry {
   float yw;
 };
 constexpr int QCAP = 96;  // <= 31 left over + 2 deposits x 32 lanes
+
+// Kahan step: s + c tracks the exact sum to O(eps^2); c holds the negated
+// rounding error of the running sum.
+__device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
+  const float y = __fsub_rn(x, c);
+  const float t = __fadd_rn(s, y);
+  c = __fsub_rn(__fsub_rn(t, s), y);
+  s = t;
+}
 
 // Box-Muller in FP32 from two Philox words: z0 = rho cos(2 pi u1),
 // z1 = rho sin(2 pi u1), evaluated as -rho cos/sin(2 pi u1 - pi) so the fast
@@ -150,11 +169,17 @@ k_paths_mixed(const MixedArgs a) {
     const float rect[4] = {s_rect[0], s_rect[1], s_rect[2], s_rect[3]};
     const float cx = 0.5f * (rect[0] + rect[2]), cy = 0.5f * (rect[1] + rect[3]);
     const float hx = rect[2] - cx, hy = rect[3] - cy;
+    // bit d set when stencil side d lies on the global boundary
+    const int globmask = (s_side[0].glob ? 1 : 0) | (s_side[1].glob ? 2 : 0) | (s_side[2].glob ? 4 : 0) |
+                         (s_side[3].glob ? 8 : 0);
     const int chunk = item % a.chunks;
     unsigned path = (unsigned)(chunk * a.paths_per_chunk + tid);
     bool active = (int)path < path_end;
-    double b = 0.0, bb = 0.0;
-    unsigned long long nsteps = 0, nglob = 0, nsten = 0;
+    // per-lane B sums in compensated FP32 (Kahan), folded into FP64 per item:
+    // the error is at most 2 eps_32 sum |v| over the lane's paths of the item
+    float bs = 0.f, bc = 0.f, bbs = 0.f, bbc = 0.f;
+    unsigned long long nsteps = 0;
+    unsigned nglob = 0, nsten = 0;  // exits of the lane in this item (<= 2 N)
     QEntry* q = s_queue[warp];
     int qcount = 0;  // warp-uniform
     const unsigned lt = (1u << lane) - 1u;
@@ -178,9 +203,16 @@ k_paths_mixed(const MixedArgs a) {
     // reference's signed distance is max(dx, dy) except in the outer corner
     // region (where both are positive and the path exits anyway), and its
     // normal is the x normal exactly when dx > dy.
-    auto advance = [&](Lvl& s, float i0, float i1, float hh, float sq) -> bool {
+    auto advance = [&](Lvl<KIND>& s, float i0, float i1, float hh, float sq) -> bool {
       Coef<float> k;
-      coef_f32<KIND>(a.P, s.x, s.y, k);
+      if constexpr (KIND == PK_LUT) {
+        k.s00 = s.cf[0]; k.s01 = 0.f; k.s10 = 0.f; k.s11 = s.cf[1];
+        k.b0 = s.cf[2]; k.b1 = s.cf[3]; k.c = s.cf[4]; k.f = s.cf[5];
+        k.g0 = a.P.use_cv ? s.cf[6] : 0.f;
+        k.g1 = a.P.use_cv ? s.cf[7] : 0.f;
+      } else {
+        coef_f32<KIND>(a.P, s.x, s.y, k);
+      }
       const float v0 = -(k.s00 * k.g0 + k.s10 * k.g1);
       const float v1 = -(k.s01 * k.g0 + k.s11 * k.g1);
       s.xi += s.Y * (v0 * i0 + v1 * i1);
@@ -191,17 +223,27 @@ k_paths_mixed(const MixedArgs a) {
       ++s.steps;
       const float dx = fabsf(s.x - cx) - hx, dy = fabsf(s.y - cy) - hy;
       float nx, ny;  // |N^T sigma| for the x and y normals
-      sigma_normals_f32<KIND>(a.P, s.x, s.y, nx, ny);
+      if constexpr (KIND == PK_LUT) {
+        lut_sample<float, 8>(a.P.lut, s.x, s.y, s.cf);
+        nx = fabsf(s.cf[0]);
+        ny = fabsf(s.cf[1]);
+      } else {
+        sigma_normals_f32<KIND>(a.P, s.x, s.y, nx, ny);
+      }
       const float thr = -0.5826f * sq * (dx > dy ? nx : ny);
       return !(fmaxf(dx, dy) < thr) || s.steps >= (unsigned)a.max_steps;
     };
     // Exit of a level: B value and, on an interior side, the deposit.
-    auto on_exit = [&](const Lvl& s, float wgt, float& val, bool& dep, QEntry& de) {
-      float Ex, Ey, Nx, Ny;
-      int onmask;
-      const float dist = rect2d<float>(rect, s.x, s.y, Ex, Ey, Nx, Ny, onmask);
-      (void)dist;
+    // Projection (Rectangle2D, rectangle.hpp:7-229) as selects: the x side is
+    // taken exactly when dx > dy, the other coordinate is clamped to the
+    // rectangle (the identity inside, the corner outside both slabs), and the
+    // sides the projection lies on are read off by equality, first match in
+    // the order S, N, W, E as in G_update (stencil.cpp:246-301).
+    auto on_exit = [&](const Lvl<KIND>& s, float wgt, float& val, bool& dep, QEntry& de) {
       if (s.steps >= (unsigned)a.max_steps) {
+        float Ex, Ey, Nx, Ny;
+        int om;
+        const float dist = rect2d<float>(rect, s.x, s.y, Ex, Ey, Nx, Ny, om);
         float g00, g01, g10, g11;
         sigma_f32<KIND>(a.P, s.x, s.y, g00, g01, g10, g11);
         const float w0 = Nx * g00 + Ny * g10, w1 = Nx * g01 + Ny * g11;
@@ -211,20 +253,20 @@ k_paths_mixed(const MixedArgs a) {
           return;
         }
       }
-      const int d = exit_side(onmask);
-      const bool glob = ((onmask & 1) && s_side[0].glob) || ((onmask & 2) && s_side[1].glob) ||
-                        ((onmask & 4) && s_side[2].glob) || ((onmask & 8) && s_side[3].glob);
-      if (glob) {
+      const float dx = fabsf(s.x - cx) - hx, dy = fabsf(s.y - cy) - hy;
+      const bool xs = dx > dy;
+      const float Ex = xs ? (s.x > cx ? rect[2] : rect[0]) : fminf(fmaxf(s.x, rect[0]), rect[2]);
+      const float Ey = xs ? fminf(fmaxf(s.y, rect[1]), rect[3]) : (s.y > cy ? rect[3] : rect[1]);
+      const bool onS = Ey == rect[1], onN = Ey == rect[3], onW = Ex == rect[0], onE = Ex == rect[2];
+      const int onmask = (onN ? 1 : 0) | (onS ? 2 : 0) | (onE ? 4 : 0) | (onW ? 8 : 0);
+      if (onmask & globmask) {
         ++nglob;
         val = s.Z + s.Y * u_f32<KIND>(a.P, Ex, Ey) + s.xi;
         return;
       }
       ++nsten;
       val = s.Z + s.xi;
-      if (d < 0) {
-        atomicOr(a.err_flags, ERR_FLAG_EXIT_SIDE);
-        return;
-      }
+      const int d = onS ? 1 : (onN ? 0 : (onW ? 3 : 2));
       const ItemSide& is = s_side[d];
       if (is.n > 0) {
         const float sc = is.orient == 0 ? Ex : Ey;
@@ -237,9 +279,15 @@ k_paths_mixed(const MixedArgs a) {
         dep = true;
       }
     };
-    Lvl F, Cs;
+    Lvl<KIND> F, Cs;
+    float cf0[8];  // table fields at the knot (PK_LUT)
+    if constexpr (KIND == PK_LUT) lut_sample<float, 8>(a.P.lut, x0, y0, cf0);
     auto reset = [&]() {
       F.x = x0; F.y = y0; F.Y = 1.f; F.Z = 0.f; F.xi = 0.f; F.steps = 0;
+      if constexpr (KIND == PK_LUT) {
+#pragma unroll
+        for (int f = 0; f < 8; f++) F.cf[f] = cf0[f];
+      }
       Cs = F;
     };
     reset();
@@ -297,9 +345,9 @@ k_paths_mixed(const MixedArgs a) {
       // finished pairs: B and refill
       const bool done = active && !f_alive && !c_alive;
       if (done) {
-        const double v = RICH ? 2.0 * (double)val_f - (double)val_c : (double)val_f;
-        b += v;
-        bb += v * v;
+        const float v = RICH ? 2.f * val_f - val_c : val_f;
+        kahan_add(bs, bc, v);
+        kahan_add(bbs, bbc, v * v);
         nsteps += F.steps + (RICH ? Cs.steps : 0u);
       }
       const unsigned dm = __ballot_sync(FULL, done);
@@ -324,6 +372,7 @@ k_paths_mixed(const MixedArgs a) {
     __syncwarp();
     if (lane < qcount) apply(q[lane]);
     // ------------------------------------------------------------ reduce B
+    double b = (double)bs - (double)bc, bb = (double)bbs - (double)bbc;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       b += __shfl_xor_sync(FULL, b, o);
