@@ -29,6 +29,7 @@ UNITS = {
     "k_rbf.cu": [],
     "k_misc.cu": ["-fmad=false"],
     "k_solve.cu": [],
+    "k_gmres_cluster.cu": [],
     "layout.cpp": ["-x", "cu"],
     "noalloc.cu": [],
 }

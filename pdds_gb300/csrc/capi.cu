@@ -712,7 +712,11 @@ pdds_status pdds_solve_interface(pdds_ctx* ctx, const pdds_solve_desc* desc, dou
     w.val32 = ctx->sval32.p;
     const int maxit = desc->max_iter > 0 ? desc->max_iter : 1000;
     const int maxref = desc->max_refine > 0 ? desc->max_refine : 30;
-    CK(solve_gmres_ir(A, ctx->B.p, ctx->su.p, w, m, maxit, maxref, tol, &iters, &refines, &relres, s));
+    bool used = false;
+    CK(solve_gmres_ir_cluster(A, ctx->B.p, ctx->su.p, w, m, maxit, maxref, tol, &iters, &refines, &relres, s,
+                              &used));
+    if (!used)
+      CK(solve_gmres_ir(A, ctx->B.p, ctx->su.p, w, m, maxit, maxref, tol, &iters, &refines, &relres, s));
   } else {
     return fail(ctx, PDDS_ERR_INVALID, "unknown solve method");
   }

@@ -507,4 +507,60 @@ cudaError_t solve_gmres_ir(const SolveCsr& A, const double* b, double* x, SolveW
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------- cluster GMRES
+__global__ void k_cl_single_rows(int* sys_row0, int K) {
+  sys_row0[0] = 0;
+  sys_row0[1] = K;
+}
+
+cudaError_t solve_gmres_ir_cluster(const SolveCsr& A, const double* b, double* x, SolveWork& w, int m,
+                                   int max_iter, int max_refine, double tol, int* iters, int* refines,
+                                   double* relres, cudaStream_t s, bool* used) {
+  *used = false;
+  w.launches = 0;
+  const int n = A.K;
+  if (m < 2 || m > GMRES_CLUSTER_MAX_M) return cudaSuccess;
+  const int cl = gmres_cluster_pick(n);
+  if (cl <= 0) return cudaSuccess;
+  *used = true;
+  int* ctl = reinterpret_cast<int*>(w.ctl);  // [0..1] rows, [2] iterations, [3] refinements
+  ++w.launches;
+  k_to_f32<<<vgrid((int)std::min<int64_t>(A.nnz, 1 << 28)), 256, 0, s>>>(A.nnz, A.val64, w.val32);
+  ++w.launches;
+  k_cl_single_rows<<<1, 1, 0, s>>>(ctl, n);
+  ClusterGmresArgs a;
+  a.n_sys = 1;
+  a.sys_row0 = ctl;
+  a.K = n;
+  a.row_ptr = A.row_ptr;
+  a.col = A.col;
+  a.val64 = A.val64;
+  a.val32 = w.val32;
+  a.b = b;
+  a.x = x;
+  a.r64 = w.v64[0];
+  a.V = w.V32;
+  a.m = m;
+  a.max_iter = max_iter;
+  a.max_refine = max_refine;
+  a.tol = tol;
+  a.inner_tol = 1e-6;
+  a.out_iters = ctl + 2;
+  a.out_refines = ctl + 3;
+  a.out_relres = w.scal;
+  a.out_t_end = nullptr;
+  ++w.launches;
+  cudaError_t e = launch_gmres_cluster(a, cl, n, s);
+  if (e != cudaSuccess) return e;
+  int hi[2] = {0, 0};
+  double hr = 0.0;
+  cudaMemcpyAsync(hi, ctl + 2, 2 * sizeof(int), cudaMemcpyDeviceToHost, s);
+  cudaMemcpyAsync(&hr, w.scal, sizeof(double), cudaMemcpyDeviceToHost, s);
+  e = cudaStreamSynchronize(s);
+  *iters = hi[0];
+  *refines = hi[1];
+  *relres = hr;
+  return e == cudaSuccess ? cudaGetLastError() : e;
+}
+
 }  // namespace pdds

@@ -26,6 +26,47 @@ struct SolveWork {
   int launches;     // kernels launched by the last solve
 };
 
+// One-launch GMRES(m)-IR, one thread-block cluster per system (k_gmres_cluster.cu).
+// Systems are row ranges [sys_row0[s], sys_row0[s+1]) of one CSR whose
+// columns stay inside the system's range (a block-diagonal batch).
+constexpr int GMRES_CLUSTER_MAX_M = 40;
+constexpr size_t CG_SMEM_CAP = 200 * 1024;  // dynamic shared memory per CTA
+
+struct ClusterGmresArgs {
+  int n_sys;
+  const int* sys_row0;   // n_sys + 1
+  int64_t K;             // rows of the whole CSR (stride of the basis)
+  const int64_t* row_ptr;
+  const int* col;
+  const double* val64;
+  const float* val32;
+  const double* b;
+  double* x;
+  double* r64;           // K
+  float* V;              // (m + 1) K
+  int m;
+  int max_iter;
+  int max_refine;
+  double tol;
+  double inner_tol;
+  int* out_iters;        // per system
+  int* out_refines;
+  double* out_relres;
+  unsigned long long* out_t_end;  // optional: %globaltimer when the system finished
+};
+
+// Cluster size for systems of at most max_rows rows (about 512 rows per CTA,
+// <= 16 CTAs, placeable on the device), 0 when a system of that size does not
+// fit the kernel's shared-memory staging (8 max_rows + 4 max_rows / cluster bytes).
+int gmres_cluster_pick(int max_rows);
+cudaError_t launch_gmres_cluster(const ClusterGmresArgs& a, int cluster, int max_rows, cudaStream_t s);
+
+// The same solve through k_gmres_cluster for one system; *used is false (and
+// nothing ran) when the system does not fit the cluster kernel.
+cudaError_t solve_gmres_ir_cluster(const SolveCsr& A, const double* b, double* x, SolveWork& w, int m,
+                                   int max_iter, int max_refine, double tol, int* iters, int* refines,
+                                   double* relres, cudaStream_t s, bool* used);
+
 cudaError_t solve_bicgstab(const SolveCsr& A, const double* b, double* x, SolveWork& w,
                            int max_iter, double tol, int* iters, double* relres, cudaStream_t s);
 cudaError_t solve_gmres_ir(const SolveCsr& A, const double* b, double* x, SolveWork& w, int m,
