@@ -154,6 +154,40 @@ def cpu_baseline(workload: dict, fac, n_knots: int, seed: int = 1234, npaths=Non
             "seconds": dt, "knots": len(sel), "path_steps": steps}
 
 
+def many_instance_batch(local: int, n_inst: int = 256, reps: int = 3, npaths: int = 10_000, h: float = 1e-3):
+    """256 independent Helmholtz instances on [0,1]^2 (random g x g grids,
+    g in 4..16, 11..41 knots per segment, a, b ~ U[1,4], c ~ U[-4,0]),
+    1e4 paths per knot, h = 1e-3, MIXED with the adaptive step, every
+    instance solved by the cluster GMRES; the sequence is one CUDA graph."""
+    import pdds_gb300 as P
+    from pdds_gb300.config import batch_instances
+    insts = batch_instances(n_inst, seed=1234)
+    t0 = time.perf_counter()
+    bt = P.Batch(P.BVP.HELMHOLTZ, insts, device=local)
+    t_build = time.perf_counter() - t0
+    bt.run(npaths, h, seed=1234, instance=0, use_graph=True)  # capture + warm-up
+    runs = [bt.run(npaths, h, seed=1234, instance=1000 * (r + 1), use_graph=True) for r in range(reps)]
+    lat, rmse, iters = [], [], []
+    for i, ins in enumerate(insts):
+        r = bt.result(i)
+        x, y = bt.knots(i)
+        bvp = P.BVP.helmholtz(*ins.params)
+        rmse.append(float(np.sqrt(np.mean((r["u"] - bvp.u(x, y)) ** 2))))
+        lat.append(r["latency_ms"])
+        iters.append(r["iterations"])
+    ms = float(np.mean([r["ms"] for r in runs]))
+    out = {"instances": n_inst, "knots": int(bt.info["nknots"]), "nnz": int(bt.info["nnz"]),
+           "paths_per_knot": npaths, "h": h, "ms_per_batch": ms, "solves_per_s": n_inst / (ms / 1000.0),
+           "path_steps_per_s": float(np.mean([r["path_steps"] / (r["ms"] / 1000.0) for r in runs])),
+           "latency_ms_p50": float(np.percentile(lat, 50)), "latency_ms_p99": float(np.percentile(lat, 99)),
+           "rmse_vs_analytic_mean": float(np.mean(rmse)), "rmse_vs_analytic_max": float(np.max(rmse)),
+           "solver_iterations_max": int(max(iters)), "unconverged": int(max(r["unconverged"] for r in runs)),
+           "kernel_launches_per_batch": int(runs[-1]["kernel_launches"]), "graph_replayed": int(runs[-1]["graph_replayed"]),
+           "host_build_s": t_build}
+    bt.close()
+    return out
+
+
 def run_reference(args, workload, fac):
     rank, world, _ = _env_rank()
     if rank != 0:
@@ -191,6 +225,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
     args = ap.parse_args()
 
     from pdds_gb300.config import WORKLOADS, fac_rule
@@ -315,6 +350,9 @@ def main():
         d2h = nnz * 16 + K * 24
         e2e = {"value": e2e_steps / dt, "unit": "path-steps/s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "ms_per_step": 1000 * dt / ns}
+
+    if not args.no_batch and rank == 0:
+        extra["many_instance_batch"] = many_instance_batch(local)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

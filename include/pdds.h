@@ -193,6 +193,62 @@ typedef struct {
 pdds_status pdds_solve_interface(pdds_ctx* ctx, const pdds_solve_desc* desc, double* u,
                                  pdds_solve_info* info);
 
+/* ---------------------------------------------------------------- batch
+ * No counterpart in the reference, whose driver solves one problem per run
+ * (PDDSparseGM::Solve, PDDAlgorithms/PDDSparseGM.cpp:691-851).  Many
+ * independent instances of one problem kind (the kind and use_cv of
+ * pdds_problem_set) with their own layouts and parameters run as one
+ * sequence: one RBF factorisation launch, one path-kernel launch over the
+ * knots of all instances, and one launch of the cluster GMRES that solves
+ * every instance's (I + G) u = B with its own convergence test.  The layout
+ * of the context becomes the block-diagonal union of the instances (instance
+ * i's knots follow instance i-1's).  Instance i draws from Philox instance
+ * word estimate.instance + i with its own knot numbering, so its random
+ * stream is the one of a single-layout run of that instance. */
+typedef struct {
+  pdds_layout_desc layout; /* the instance's domain, grid and RBF shapes */
+  double p[8];             /* the instance's problem parameters            */
+} pdds_instance_desc;
+
+typedef struct {
+  int32_t ninstances;
+  int32_t max_knots;     /* knots of the largest instance */
+  int64_t nknots;        /* knots of all instances        */
+  int64_t nnz;           /* G entries of all instances    */
+} pdds_batch_info;
+
+pdds_status pdds_batch_build(pdds_ctx* ctx, const pdds_instance_desc* inst, int32_t n, pdds_batch_info* info);
+
+typedef struct {
+  pdds_estimate_desc estimate; /* mode must be PDDS_MODE_MIXED                */
+  pdds_solve_desc solve;       /* method must be PDDS_SOLVE_GMRES_FP32_IR    */
+  int32_t use_graph;           /* 1: capture the sequence in a CUDA graph on
+                                  the first run and replay it while the batch
+                                  and the descriptor stay the same          */
+} pdds_batch_run_desc;
+
+typedef struct {
+  double ms;                   /* device time of the whole sequence          */
+  int64_t path_steps;
+  int64_t paths;
+  int64_t exits_global;
+  int64_t exits_stencil;
+  int32_t kernel_launches;     /* kernels in the sequence                    */
+  int32_t graph_replayed;      /* 1: this run replayed a captured graph      */
+  int32_t max_iterations;      /* over instances                             */
+  int32_t unconverged;         /* instances that missed the tolerance        */
+  double max_rel_residual;
+} pdds_batch_run_info;
+
+pdds_status pdds_batch_run(pdds_ctx* ctx, const pdds_batch_run_desc* desc, pdds_batch_run_info* info);
+
+/* Results of instance i after pdds_batch_run, in the instance's own knot
+ * numbering (the one pdds_layout_build of its layout gives).  Any pointer
+ * may be NULL; x, y, u, B hold nknots values.  latency_ms: time from the
+ * start of the sequence until the instance's solution was complete. */
+pdds_status pdds_batch_instance(pdds_ctx* ctx, int32_t i, int32_t* nknots, double* x, double* y, double* u,
+                                double* B, int32_t* iterations, double* rel_residual, double* latency_ms);
+
 /* ---------------------------------------------------------------- allocation-free solve
  * No counterpart in the reference.  For callers that cannot let a library
  * allocate GPU memory (memory owned by another allocator, serving loops where

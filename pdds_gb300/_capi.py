@@ -25,7 +25,8 @@ SOLVE_BICGSTAB_FP64, SOLVE_GMRES_FP32_IR = 0, 1
 EXPORTS = [
     "pdds_create", "pdds_destroy", "pdds_last_error", "pdds_version", "pdds_problem_set", "pdds_problem_set_lut",
     "pdds_layout_build", "pdds_layout_knots", "pdds_layout_csr", "pdds_layout_stencil",
-    "pdds_estimate", "pdds_solve_interface", "pdds_solve_bicgstab_static",
+    "pdds_estimate", "pdds_solve_interface", "pdds_batch_build", "pdds_batch_run", "pdds_batch_instance",
+    "pdds_solve_bicgstab_static",
 ]
 STATIC_SOLVE_MAX_K = 131072
 
@@ -69,6 +70,25 @@ class SolveInfo(C.Structure):
                 ("ms", C.c_double), ("kernel_launches", C.c_int32)]
 
 
+class InstanceDesc(C.Structure):
+    _fields_ = [("layout", LayoutDesc), ("p", C.c_double * 8)]
+
+
+class BatchInfo(C.Structure):
+    _fields_ = [("ninstances", C.c_int32), ("max_knots", C.c_int32), ("nknots", C.c_int64), ("nnz", C.c_int64)]
+
+
+class BatchRunDesc(C.Structure):
+    _fields_ = [("estimate", EstimateDesc), ("solve", SolveDesc), ("use_graph", C.c_int32)]
+
+
+class BatchRunInfo(C.Structure):
+    _fields_ = [("ms", C.c_double), ("path_steps", C.c_int64), ("paths", C.c_int64),
+                ("exits_global", C.c_int64), ("exits_stencil", C.c_int64), ("kernel_launches", C.c_int32),
+                ("graph_replayed", C.c_int32), ("max_iterations", C.c_int32), ("unconverged", C.c_int32),
+                ("max_rel_residual", C.c_double)]
+
+
 _lib = None
 
 
@@ -99,6 +119,10 @@ def load(path: str = LIB_PATH):
                                       C.POINTER(C.c_int32), C.c_int32]
     L.pdds_estimate.argtypes = [vp, C.POINTER(EstimateDesc), dp, dp, dp, dp, C.POINTER(EstimateInfo)]
     L.pdds_solve_interface.argtypes = [vp, C.POINTER(SolveDesc), dp, C.POINTER(SolveInfo)]
+    L.pdds_batch_build.argtypes = [vp, C.POINTER(InstanceDesc), C.c_int32, C.POINTER(BatchInfo)]
+    L.pdds_batch_run.argtypes = [vp, C.POINTER(BatchRunDesc), C.POINTER(BatchRunInfo)]
+    L.pdds_batch_instance.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), dp, dp, dp, dp, C.POINTER(C.c_int32), dp,
+                                      dp]
     L.pdds_solve_bicgstab_static.argtypes = [C.c_int, C.c_int32, C.c_int64, vp, vp, vp, vp, vp, C.c_double,
                                              C.c_int32, vp, C.POINTER(C.c_int32), dp, C.c_char_p, C.c_int32]
     for name in EXPORTS:

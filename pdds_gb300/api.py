@@ -301,3 +301,125 @@ class PDDSparseGM:
         est = self.estimate(bvp, npaths, h, mode=mode, seed=seed, **kw)
         u, sinfo = self.solve_interface(method=method, tol=tol)
         return u, est, sinfo
+
+
+@dataclass
+class Instance:
+    """One BVP instance of a batch: its layout and problem parameters."""
+
+    sw: tuple
+    ne: tuple
+    nsub: int
+    nnode: int
+    fac: tuple
+    params: tuple = ()
+
+
+class Batch:
+    """Many independent instances of one problem kind solved as one sequence.
+
+    No counterpart in the reference, whose PDDSparseGM solves one problem per
+    run.  All instances' knots are estimated by one path-kernel launch and all
+    interface systems are solved by one cluster-GMRES launch; with
+    use_graph=True the sequence is captured once in a CUDA graph and replayed.
+    Instance i uses Philox instance word `instance + i` and its own knot
+    numbering, so its random stream equals the one of a PDDSparseGM run of
+    that instance alone with instance word `instance + i`."""
+
+    def __init__(self, kind: int, instances, use_cv: bool = True, device: int = 0):
+        self._lib = capi.load()
+        self._ctx = C.c_void_p()
+        st = self._lib.pdds_create(C.byref(self._ctx), int(device), 0)
+        if st != capi.OK:
+            raise PDDSError(st, "pdds_create failed (device %d)" % device)
+        self.kind = int(kind)
+        self.use_cv = bool(use_cv)
+        self.instances = list(instances)
+        n = len(self.instances)
+        arr = (capi.InstanceDesc * n)()
+        for i, ins in enumerate(self.instances):
+            d = arr[i]
+            d.layout.sw[0], d.layout.sw[1] = float(ins.sw[0]), float(ins.sw[1])
+            d.layout.ne[0], d.layout.ne[1] = float(ins.ne[0]), float(ins.ne[1])
+            d.layout.nsub = int(ins.nsub)
+            d.layout.nnode = int(ins.nnode)
+            for q in range(4):
+                d.layout.fac[q] = float(ins.fac[q])
+            for q, v in enumerate(ins.params):
+                d.p[q] = float(v)
+        info = capi.BatchInfo()
+        self._check(self._lib.pdds_batch_build(self._ctx, arr, n, C.byref(info)))
+        self.info = {f: getattr(info, f) for f, _ in capi.BatchInfo._fields_}
+        pd = capi.ProblemDesc()
+        pd.kind = self.kind
+        pd.use_cv = int(self.use_cv)
+        self._check(self._lib.pdds_problem_set(self._ctx, C.byref(pd)))
+
+    def _check(self, st):
+        if st != capi.OK:
+            msg = self._lib.pdds_last_error(self._ctx).decode() if self._ctx else ""
+            raise PDDSError(st, msg)
+
+    def close(self):
+        if getattr(self, "_ctx", None) and self._ctx.value:
+            self._lib.pdds_destroy(self._ctx)
+            self._ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def run(self, npaths: int, h: float, seed: int = 1234, instance: int = 0, adaptive_h: bool = True,
+            richardson: bool = False, tol: float = 1e-10, restart: int = 30, use_graph: bool = True,
+            bins_per_gap: int = 0, reuse_tables: bool = False) -> dict:
+        """Estimates and solves every instance; returns the run counters."""
+        d = capi.BatchRunDesc()
+        e = d.estimate
+        e.mode = capi.MODE_MIXED
+        e.npaths = int(npaths)
+        e.h = float(h)
+        e.seed = int(seed)
+        e.instance = int(instance)
+        e.bins_per_gap = int(bins_per_gap)
+        e.adaptive_h = int(bool(adaptive_h))
+        e.richardson = int(bool(richardson))
+        e.reuse_tables = int(bool(reuse_tables))
+        d.solve.method = capi.SOLVE_GMRES_FP32_IR
+        d.solve.restart = int(restart)
+        d.solve.tol = float(tol)
+        d.use_graph = int(bool(use_graph))
+        info = capi.BatchRunInfo()
+        self._check(self._lib.pdds_batch_run(self._ctx, C.byref(d), C.byref(info)))
+        return {f: getattr(info, f) for f, _ in capi.BatchRunInfo._fields_}
+
+    def knots(self, i: int):
+        n = C.c_int32()
+        self._check(self._lib.pdds_batch_instance(self._ctx, int(i), C.byref(n), None, None, None, None, None,
+                                                  None, None))
+        x = np.zeros(n.value)
+        y = np.zeros(n.value)
+        self._check(self._lib.pdds_batch_instance(self._ctx, int(i), None, _p(x, C.c_double), _p(y, C.c_double),
+                                                  None, None, None, None, None))
+        return x, y
+
+    def result(self, i: int) -> dict:
+        """u, B, solver iterations, relative residual and latency (ms) of instance i."""
+        n = C.c_int32()
+        self._check(self._lib.pdds_batch_instance(self._ctx, int(i), C.byref(n), None, None, None, None, None,
+                                                  None, None))
+        u = np.zeros(n.value)
+        B = np.zeros(n.value)
+        it = C.c_int32()
+        rr = C.c_double()
+        lat = C.c_double()
+        self._check(self._lib.pdds_batch_instance(self._ctx, int(i), None, None, None, _p(u, C.c_double),
+                                                  _p(B, C.c_double), C.byref(it), C.byref(rr), C.byref(lat)))
+        return {"u": u, "B": B, "iterations": it.value, "rel_residual": rr.value, "latency_ms": lat.value}

@@ -30,6 +30,7 @@ UNITS = {
     "k_misc.cu": ["-fmad=false"],
     "k_solve.cu": [],
     "k_gmres_cluster.cu": [],
+    "batch.cu": [],
     "layout.cpp": ["-x", "cu"],
     "noalloc.cu": [],
 }

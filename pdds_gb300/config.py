@@ -62,3 +62,23 @@ def varcoef_tables(n: int = 1024, bounds=(0.0, 0.0, 1.0, 1.0)):
     f = -(0.5 * (s1 * s1 * uxx + s2 * s2 * uyy) + (Y * ux - X * uy) + c * u)
     coef = np.stack([s1, s2, Y, -X, c, f, ux, uy], axis=-1).astype(np.float32)
     return np.ascontiguousarray(coef), np.ascontiguousarray(u.astype(np.float32)), tuple(float(b) for b in bounds)
+
+
+def batch_instances(n: int = 256, seed: int = 1234, grid=(4, 16), nodes=(11, 41)):
+    """The many-instance workload: n Helmholtz problems Lap u + c u + f = 0
+    on [0,1]^2 with u = sin(a x) cos(b y), a, b ~ U[1,4], c ~ U[-4,0], each
+    on its own g x g subdomain grid, g ~ U{4..16}, with k ~ U{11..41} knots
+    per segment (seeded).  The grids are square: the reference's layout
+    (Fullfill_interfaces and its configuration reader) takes one subdomain
+    count for both directions."""
+    import numpy as np
+    from .api import Instance
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        g = int(rng.integers(grid[0], grid[1] + 1))
+        k = int(rng.integers(nodes[0], nodes[1] + 1))
+        a, b = rng.uniform(1.0, 4.0, size=2)
+        c = -rng.uniform(0.0, 4.0)
+        out.append(Instance((0.0, 0.0), (1.0, 1.0), g, k, fac_rule(1.0, g, k), (float(a), float(b), float(c))))
+    return out

@@ -1,0 +1,259 @@
+// Batches of independent instances (include/pdds.h, "batch"): layout union,
+// the one-sequence run (estimation of every instance in one path-kernel
+// launch, every instance's interface solve in one cluster-GMRES launch),
+// CUDA-graph capture and replay of that sequence, per-instance results.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/pdds.h"
+#include "ctx.h"
+#include "kernels.h"
+#include "pdds_internal.h"
+#include "solve.h"
+
+using namespace pdds;
+
+namespace {
+
+// The whole batch step on ctx->stream, without host synchronisation.
+pdds_status enqueue_batch(pdds_ctx* ctx, const pdds_batch_run_desc* d, int cluster, int* launches) {
+  cudaStream_t s = ctx->stream;
+  const int n = ctx->n_inst;
+  const int64_t K = ctx->L.K;
+  const int64_t nnz = ctx->L.row_ptr[ctx->L.K];
+  CK(launch_stamp(ctx->b_tend.p + n, s));
+  ++*launches;
+  pdds_status st = enqueue_mixed(ctx, &d->estimate, launches);
+  if (st != PDDS_OK) return st;
+  CK(launch_to_f32(ctx->G.p, ctx->sval32.p, nnz, s));
+  ++*launches;
+  ClusterGmresArgs a;
+  a.n_sys = n;
+  a.sys_row0 = ctx->inst_knot0.p;
+  a.K = K;
+  a.row_ptr = ctx->row_ptr.p;
+  a.col = ctx->col.p;
+  a.val64 = ctx->G.p;
+  a.val32 = ctx->sval32.p;
+  a.b = ctx->B.p;
+  a.x = ctx->su.p;
+  a.r64 = ctx->sv64.p;
+  a.V = ctx->sV32.p;
+  a.m = std::max(2, std::min(d->solve.restart > 0 ? d->solve.restart : 30, GMRES_CLUSTER_MAX_M));
+  a.max_iter = d->solve.max_iter > 0 ? d->solve.max_iter : 1000;
+  a.max_refine = d->solve.max_refine > 0 ? d->solve.max_refine : 30;
+  a.tol = d->solve.tol > 0 ? d->solve.tol : 1e-10;
+  a.inner_tol = 1e-6;
+  a.out_iters = ctx->b_iters.p;
+  a.out_refines = ctx->b_refines.p;
+  a.out_relres = ctx->b_relres.p;
+  a.out_t_end = ctx->b_tend.p;
+  CK(launch_gmres_cluster(a, cluster, ctx->max_inst_knots, s));
+  ++*launches;
+  return PDDS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+pdds_status pdds_batch_build(pdds_ctx* ctx, const pdds_instance_desc* inst, int32_t n, pdds_batch_info* info) {
+  if (!ctx || !inst || n < 1) return fail(ctx, PDDS_ERR_INVALID, "a batch needs n >= 1 instances");
+  std::vector<HostLayout> parts(n);
+  for (int i = 0; i < n; i++) {
+    const pdds_layout_desc& ld = inst[i].layout;
+    for (int q = 0; q < 4; q++)
+      if (!(ld.fac[q] > 0.0)) return fail(ctx, PDDS_ERR_INVALID, "instance " + std::to_string(i) + ": fac must be positive");
+    const std::string e = build_rect_layout(parts[i], ld.sw, ld.ne, ld.nsub, ld.nnode, ld.fac, ctx->bins);
+    if (!e.empty()) return fail(ctx, PDDS_ERR_INVALID, "instance " + std::to_string(i) + ": " + e);
+  }
+  if (ctx->device >= 0) {
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  drop_graph(ctx);
+  const std::string e = merge_layouts(ctx->L, parts, ctx->bins);
+  if (!e.empty()) return fail(ctx, PDDS_ERR_INVALID, e);
+  ctx->n_inst = n;
+  ctx->inst_k0.assign(n + 1, 0);
+  ctx->inst_nnz0.assign(n + 1, 0);
+  ctx->inst_p.assign((size_t)8 * n, 0.0);
+  ctx->max_inst_knots = 0;
+  for (int i = 0; i < n; i++) {
+    ctx->inst_k0[i + 1] = ctx->inst_k0[i] + parts[i].K;
+    ctx->inst_nnz0[i + 1] = ctx->inst_nnz0[i] + parts[i].row_ptr[parts[i].K];
+    for (int q = 0; q < 8; q++) ctx->inst_p[8 * i + q] = inst[i].p[q];
+    ctx->max_inst_knots = std::max(ctx->max_inst_knots, parts[i].K);
+  }
+  ctx->is_batch = true;
+  ctx->has_layout = true;
+  ctx->has_estimate = false;
+  ctx->has_batch_run = false;
+  if (ctx->device >= 0) {
+    std::vector<int> knot_inst(ctx->L.K);
+    for (int i = 0; i < n; i++)
+      for (int k = ctx->inst_k0[i]; k < ctx->inst_k0[i + 1]; k++) knot_inst[k] = i;
+    cudaStream_t s = ctx->stream;
+    CK(ctx->knot_inst.upload(knot_inst, s));
+    CK(ctx->inst_knot0.upload(ctx->inst_k0, s));
+    CK(ctx->inst_pd.upload(ctx->inst_p, s));
+    CK(ctx->b_iters.resize(n));
+    CK(ctx->b_refines.resize(n));
+    CK(ctx->b_relres.resize(n));
+    CK(ctx->b_tend.resize(n + 1));
+    pdds_status st = upload_layout(ctx);
+    if (st != PDDS_OK) return st;
+    CK(cudaStreamSynchronize(s));
+  }
+  if (info) {
+    info->ninstances = n;
+    info->max_knots = ctx->max_inst_knots;
+    info->nknots = ctx->L.K;
+    info->nnz = ctx->L.row_ptr[ctx->L.K];
+  }
+  return PDDS_OK;
+}
+
+pdds_status pdds_batch_run(pdds_ctx* ctx, const pdds_batch_run_desc* desc, pdds_batch_run_info* info) {
+  if (!ctx || !desc) return PDDS_ERR_INVALID;
+  if (ctx->device < 0) return fail(ctx, PDDS_ERR_INVALID, "context has no device");
+  if (!ctx->is_batch) return fail(ctx, PDDS_ERR_INVALID, "no batch built");
+  if (!ctx->has_problem) return fail(ctx, PDDS_ERR_INVALID, "no problem set");
+  const pdds_estimate_desc& ed = desc->estimate;
+  if (ed.mode != PDDS_MODE_MIXED) return fail(ctx, PDDS_ERR_INVALID, "batches run in PDDS_MODE_MIXED");
+  if (ed.npaths < 1 || !(ed.h > 0.0)) return fail(ctx, PDDS_ERR_INVALID, "npaths >= 1 and h > 0 required");
+  if (ed.ipsi_override) return fail(ctx, PDDS_ERR_INVALID, "ipsi_override is a replay option");
+  if (desc->solve.method != PDDS_SOLVE_GMRES_FP32_IR)
+    return fail(ctx, PDDS_ERR_INVALID, "batches solve with PDDS_SOLVE_GMRES_FP32_IR");
+  if (desc->solve.restart > GMRES_CLUSTER_MAX_M) return fail(ctx, PDDS_ERR_INVALID, "restart must be <= 40");
+  CK(cudaSetDevice(ctx->device));
+  cudaStream_t s = ctx->stream;
+  HostLayout& L = ctx->L;
+  const int bins = ed.bins_per_gap > 0 ? ed.bins_per_gap : 16;
+  if (bins != ctx->bins) {
+    drop_graph(ctx);
+    ctx->bins = bins;
+    set_shape_bins(L, bins);
+    pdds_status st = upload_layout(ctx);
+    if (st != PDDS_OK) return st;
+  }
+  const int cluster = gmres_cluster_pick(ctx->max_inst_knots);
+  if (cluster <= 0)
+    return fail(ctx, PDDS_ERR_INVALID, "largest instance (" + std::to_string(ctx->max_inst_knots) +
+                                           " knots) exceeds the batched solve's shared-memory staging");
+  const int64_t K = L.K;
+  const int64_t nnz = L.row_ptr[L.K];
+  const int m = std::max(2, std::min(desc->solve.restart > 0 ? desc->solve.restart : 30, GMRES_CLUSTER_MAX_M));
+  // buffers first: a captured graph holds their addresses
+  const void* before[4] = {ctx->sV32.p, ctx->sval32.p, ctx->sv64.p, ctx->su.p};
+  CK(ctx->sV32.resize((size_t)(m + 1) * K));
+  CK(ctx->sval32.resize(std::max<int64_t>(nnz, 1)));
+  CK(ctx->sv64.resize(std::max<int64_t>(K, 1) * 6));
+  CK(ctx->su.resize(std::max<int64_t>(K, 1)));
+  const void* after[4] = {ctx->sV32.p, ctx->sval32.p, ctx->sv64.p, ctx->su.p};
+  if (std::memcmp(before, after, sizeof(before)) != 0) drop_graph(ctx);
+  // the graph is reused while the descriptor, the cluster size and the solve
+  // scratch (which pdds_solve_interface may also reallocate) are unchanged;
+  // layout, problem and table changes drop it where they happen
+  std::vector<unsigned char> key(sizeof(pdds_batch_run_desc) + sizeof(int) + sizeof(after));
+  std::memcpy(key.data(), desc, sizeof(pdds_batch_run_desc));
+  std::memcpy(key.data() + sizeof(pdds_batch_run_desc), &cluster, sizeof(int));
+  std::memcpy(key.data() + sizeof(pdds_batch_run_desc) + sizeof(int), after, sizeof(after));
+  int launches = 0;
+  bool replayed = false;
+  if (desc->use_graph) {
+    if (!ctx->graph_exec || ctx->graph_key != key) {
+      drop_graph(ctx);
+      CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+      int nl = 0;
+      pdds_status st = enqueue_batch(ctx, desc, cluster, &nl);
+      cudaGraph_t g = nullptr;
+      cudaError_t ce = cudaStreamEndCapture(s, &g);
+      if (st != PDDS_OK) {
+        if (g) cudaGraphDestroy(g);
+        return st;
+      }
+      if (ce != cudaSuccess) return fail(ctx, PDDS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+      ctx->graph = g;
+      CK(cudaGraphInstantiate(&ctx->graph_exec, ctx->graph, 0));
+      ctx->graph_key = key;
+      ctx->graph_launches = nl;
+    } else {
+      replayed = true;
+    }
+    launches = ctx->graph_launches;
+    CK(cudaEventRecord(ctx->ev0, s));
+    CK(cudaGraphLaunch(ctx->graph_exec, s));
+    CK(cudaEventRecord(ctx->ev1, s));
+  } else {
+    CK(cudaEventRecord(ctx->ev0, s));
+    pdds_status st = enqueue_batch(ctx, desc, cluster, &launches);
+    if (st != PDDS_OK) return st;
+    CK(cudaEventRecord(ctx->ev1, s));
+  }
+  unsigned long long stats[8] = {0};
+  CK(cudaMemcpyAsync(stats, ctx->stats.p, sizeof(stats), cudaMemcpyDeviceToHost, s));
+  std::vector<int> it(ctx->n_inst);
+  std::vector<double> rr(ctx->n_inst);
+  CK(cudaMemcpyAsync(it.data(), ctx->b_iters.p, ctx->n_inst * sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(rr.data(), ctx->b_relres.p, ctx->n_inst * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  ctx->has_estimate = true;
+  ctx->has_batch_run = true;
+  const double tol = desc->solve.tol > 0 ? desc->solve.tol : 1e-10;
+  if (info) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    info->ms = ms;
+    info->path_steps = (int64_t)stats[0];
+    info->paths = (int64_t)ctx->n_mc * ed.npaths;
+    info->exits_global = (int64_t)stats[2];
+    info->exits_stencil = (int64_t)stats[3];
+    info->kernel_launches = launches;
+    info->graph_replayed = replayed ? 1 : 0;
+    info->max_iterations = 0;
+    info->unconverged = 0;
+    info->max_rel_residual = 0.0;
+    for (int i = 0; i < ctx->n_inst; i++) {
+      info->max_iterations = std::max(info->max_iterations, it[i]);
+      info->max_rel_residual = std::max(info->max_rel_residual, rr[i]);
+      if (!(rr[i] <= tol * 1.0000001) && rr[i] != 0.0) info->unconverged++;
+    }
+  }
+  return check_err_flags(ctx);
+}
+
+pdds_status pdds_batch_instance(pdds_ctx* ctx, int32_t i, int32_t* nknots, double* x, double* y, double* u,
+                                double* B, int32_t* iterations, double* rel_residual, double* latency_ms) {
+  if (!ctx || !ctx->is_batch) return fail(ctx, PDDS_ERR_INVALID, "no batch built");
+  if (i < 0 || i >= ctx->n_inst) return fail(ctx, PDDS_ERR_INVALID, "instance out of range");
+  const int k0 = ctx->inst_k0[i], nk = ctx->inst_k0[i + 1] - k0;
+  if (nknots) *nknots = nk;
+  if (x) std::copy(ctx->L.kx.begin() + k0, ctx->L.kx.begin() + k0 + nk, x);
+  if (y) std::copy(ctx->L.ky.begin() + k0, ctx->L.ky.begin() + k0 + nk, y);
+  if (!(u || B || iterations || rel_residual || latency_ms)) return PDDS_OK;
+  if (!ctx->has_batch_run) return fail(ctx, PDDS_ERR_INVALID, "no batch run yet");
+  CK(cudaSetDevice(ctx->device));
+  cudaStream_t s = ctx->stream;
+  int it = 0;
+  double rr = 0.0;
+  unsigned long long t[2] = {0, 0};
+  if (u) CK(cudaMemcpyAsync(u, ctx->su.p + k0, nk * sizeof(double), cudaMemcpyDeviceToHost, s));
+  if (B) CK(cudaMemcpyAsync(B, ctx->B.p + k0, nk * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(&it, ctx->b_iters.p + i, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(&rr, ctx->b_relres.p + i, sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(&t[0], ctx->b_tend.p + i, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(&t[1], ctx->b_tend.p + ctx->n_inst, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (iterations) *iterations = it;
+  if (rel_residual) *rel_residual = rr;
+  if (latency_ms) *latency_ms = t[0] >= t[1] ? (double)(t[0] - t[1]) * 1e-6 : 0.0;
+  return PDDS_OK;
+}
+
+}  // extern "C"

@@ -10,101 +10,31 @@
 #include <vector>
 
 #include "../../include/pdds.h"
+#include "ctx.h"
 #include "kernels.h"
 #include "pdds_internal.h"
 #include "solve.h"
 
 using namespace pdds;
 
-namespace {
-
-template <typename T>
-struct DBuf {
-  T* p = nullptr;
-  size_t n = 0;
-  cudaError_t resize(size_t count) {
-    if (count <= n && p) return cudaSuccess;
-    if (p) cudaFree(p);
-    p = nullptr;
-    n = 0;
-    if (count == 0) return cudaSuccess;
-    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
-    if (e == cudaSuccess) n = count;
-    return e;
-  }
-  cudaError_t upload(const std::vector<T>& v, cudaStream_t s) {
-    cudaError_t e = resize(std::max<size_t>(v.size(), 1));
-    if (e != cudaSuccess || v.empty()) return e;
-    return cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s);
-  }
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    n = 0;
-  }
-};
-
-}  // namespace
-
-struct pdds_ctx {
-  int device = -1;
-  cudaStream_t stream = nullptr;
-  int num_sms = 0;
-  std::string err;
-  bool has_problem = false;
-  pdds_problem_desc prob{};
-  DBuf<float> lut_coef, lut_g;
-  int lut_nx = 0, lut_ny = 0;
-  double lut_bounds[4] = {0, 0, 0, 0};
-  bool has_layout = false;
-  HostLayout L;
-  int bins = 16;
-  bool tables_ready = false;
-  // device layout
-  DBuf<double> kx, ky, st_rect, sd_c, sd_origin, side_px, side_py, sh_c, sh_lo, sh_delta, sh_t, ipsi;
-  DBuf<int> knot_stencil, st_side, st_glob, map_pos, sd_n, sd_orient, sd_shape, side_knot, sh_n,
-      sh_nbins, col, mc_knots, bnd_knots;
-  DBuf<int64_t> row_ptr, st_map_off, sd_knot_off, sh_tab_off, sh_ipsi_off, sh_t_off;
-  DBuf<unsigned char> map_owner;
-  DBuf<float> tab;
-  DevLayout dl{};
-  int n_mc = 0, n_bnd = 0;
-  size_t mixed_smem = 0, fp64_smem = 0;
-  int max_nbins = 0;
-  // results and scratch
-  DBuf<double> G, GG, B, BB, Bsum, BBsum;
-  DBuf<unsigned long long> stats;
-  DBuf<unsigned> errf;
-  DBuf<int> counter;
-  bool has_estimate = false;
-  // replay scratch
-  DBuf<double> rx, ry, rY, rZ, rxi, Gside, GGside, ipsi_knot;
-  DBuf<int> rside, rsl, rss, task_m, task_d, task_i;
-  DBuf<int64_t> task_out, knot_task_off, knot_ipsi_off;
-  // solve scratch
-  DBuf<double> sv64, sscal, spart, shess, su;
-  DBuf<float> sV32, sw32, sval32;
-  DBuf<unsigned> sctl;
-  double* host_rr = nullptr;
-  int solve_m = 0;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
-};
-
-namespace {
+namespace pdds {
 
 pdds_status fail(pdds_ctx* c, pdds_status s, const std::string& msg) {
   if (c) c->err = msg;
   return s;
 }
 
-#define CK(call)                                                                         \
-  do {                                                                                   \
-    cudaError_t e_ = (call);                                                             \
-    if (e_ != cudaSuccess)                                                               \
-      return fail(ctx, PDDS_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
-  } while (0)
+void drop_graph(pdds_ctx* ctx) {
+  if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+  if (ctx->graph) cudaGraphDestroy(ctx->graph);
+  ctx->graph_exec = nullptr;
+  ctx->graph = nullptr;
+  ctx->graph_key.clear();
+  ctx->graph_launches = 0;
+}
 
 pdds_status upload_layout(pdds_ctx* ctx) {
+  drop_graph(ctx);  // the buffers below may move
   HostLayout& L = ctx->L;
   cudaStream_t s = ctx->stream;
   std::vector<double> st_rect;
@@ -228,6 +158,9 @@ pdds_status upload_layout(pdds_ctx* ctx) {
   d.sh_t_off = ctx->sh_t_off.p; d.sh_t = ctx->sh_t.p;
   d.tab = ctx->tab.p;
   d.ipsi = ctx->ipsi.p;
+  d.knot_inst = ctx->is_batch ? ctx->knot_inst.p : nullptr;
+  d.inst_knot0 = ctx->is_batch ? ctx->inst_knot0.p : nullptr;
+  d.inst_p = ctx->is_batch ? ctx->inst_pd.p : nullptr;
   ctx->tables_ready = false;
   return PDDS_OK;
 }
@@ -259,7 +192,106 @@ pdds_status check_err_flags(pdds_ctx* ctx) {
   return PDDS_OK;
 }
 
-}  // namespace
+pdds_status enqueue_prefix(pdds_ctx* ctx, const pdds_estimate_desc* desc, const ProblemDev& P, bool events,
+                           int* launches) {
+  cudaStream_t s = ctx->stream;
+  HostLayout& L = ctx->L;
+  const int mode = desc->mode;
+  const int64_t nnz = L.row_ptr[L.K];
+  if (events) CK(cudaEventRecord(ctx->ev0, s));
+  CK(cudaMemsetAsync(ctx->errf.p, 0, sizeof(unsigned), s));
+  CK(cudaMemsetAsync(ctx->stats.p, 0, 8 * sizeof(unsigned long long), s));
+  const bool need_ipsi = !(mode == PDDS_MODE_REPLAY_FP64 && desc->ipsi_override);
+  if (need_ipsi && (!ctx->tables_ready || !desc->reuse_tables)) {
+    int max_n = 0;
+    for (auto& sh : L.shapes) max_n = std::max(max_n, sh.n);
+    CK(launch_rbf_setup(ctx->dl, max_n, ctx->max_nbins, ctx->ipsi.p, ctx->tab.p, ctx->errf.p, s));
+    *launches += 2;
+    ctx->tables_ready = true;
+  }
+  if (events) CK(cudaEventRecord(ctx->ev1, s));
+  CK(cudaMemsetAsync(ctx->G.p, 0, std::max<int64_t>(nnz, 1) * sizeof(double), s));
+  CK(cudaMemsetAsync(ctx->GG.p, 0, std::max<int64_t>(nnz, 1) * sizeof(double), s));
+  CK(cudaMemsetAsync(ctx->Bsum.p, 0, L.K * sizeof(double), s));
+  CK(cudaMemsetAsync(ctx->BBsum.p, 0, L.K * sizeof(double), s));
+  CK(launch_boundary_b(ctx->dl, P, mode, ctx->bnd_knots.p, ctx->n_bnd, ctx->B.p, ctx->BB.p, s));
+  *launches += ctx->n_bnd > 0;
+  return PDDS_OK;
+}
+
+// Items are (knot, chunk of paths): enough chunks per knot to give every SM
+// several items, but at least 256 paths per chunk.
+void item_split(const pdds_ctx* ctx, int N, int* chunks_out, int* ppc_out) {
+  const int n_mc = ctx->n_mc;
+  const int target = 4 * std::max(ctx->num_sms, 1) * 4;
+  int chunks = std::max(1, (target + std::max(n_mc, 1) - 1) / std::max(n_mc, 1));
+  chunks = std::min(chunks, std::max(1, N / 256));
+  const int ppc = (N + chunks - 1) / chunks;
+  *chunks_out = (N + ppc - 1) / ppc;
+  *ppc_out = ppc;
+}
+
+pdds_status enqueue_mixed_paths(pdds_ctx* ctx, const pdds_estimate_desc* desc, const ProblemDev& P, int chunks,
+                                int ppc, int* launches) {
+  cudaStream_t s = ctx->stream;
+  const int N = desc->npaths;
+  const int n_items = ctx->n_mc * chunks;
+  const long long max_steps = desc->max_steps > 0 ? desc->max_steps : 1000000LL;
+  CK(cudaMemsetAsync(ctx->counter.p, 0, sizeof(int), s));
+  MixedArgs a;
+  a.L = ctx->dl;
+  a.P = P;
+  a.N = N;
+  a.h = (float)desc->h;
+  a.sqrth = (float)std::sqrt(desc->h);
+  a.inv_N = 1.0 / N;
+  a.seed = desc->seed;
+  a.instance = desc->instance;
+  a.chunks = chunks;
+  a.paths_per_chunk = ppc;
+  a.n_items = n_items;
+  a.want_var = desc->want_var ? 1 : 0;
+  a.dup_sum = desc->dup_sum;
+  a.adaptive_h = desc->adaptive_h ? 1 : 0;
+  a.richardson = desc->richardson ? 1 : 0;
+  a.h64 = desc->h;
+  a.max_steps = max_steps;
+  a.mc_knots = ctx->mc_knots.p;
+  a.item_counter = ctx->counter.p;
+  a.G = ctx->G.p;
+  a.GG = ctx->GG.p;
+  a.Bsum = ctx->Bsum.p;
+  a.BBsum = ctx->BBsum.p;
+  a.stats = ctx->stats.p;
+  a.err_flags = ctx->errf.p;
+  const size_t smem = ctx->mixed_smem * (a.want_var ? 2 : 1);
+  if (smem > 200 * 1024) return fail(ctx, PDDS_ERR_INVALID, "exit histograms exceed shared memory; lower bins_per_gap");
+  int bps = mixed_blocks_per_sm(P.kind, smem, a.richardson);
+  if (bps < 1) bps = 1;
+  const int grid = std::max(1, std::min(n_items, bps * ctx->num_sms));
+  if (n_items > 0) {
+    CK(launch_paths_mixed(a, P.kind, grid, smem, s));
+    ++*launches;
+  }
+  return PDDS_OK;
+}
+
+pdds_status enqueue_mixed(pdds_ctx* ctx, const pdds_estimate_desc* desc, int* launches) {
+  const ProblemDev P = problem_dev(ctx);
+  pdds_status st = enqueue_prefix(ctx, desc, P, false, launches);
+  if (st != PDDS_OK) return st;
+  int chunks = 1, ppc = 1;
+  item_split(ctx, desc->npaths, &chunks, &ppc);
+  st = enqueue_mixed_paths(ctx, desc, P, chunks, ppc, launches);
+  if (st != PDDS_OK) return st;
+  const int64_t nnz = ctx->L.row_ptr[ctx->L.K];
+  CK(launch_finalize(ctx->mc_knots.p, ctx->n_mc, desc->npaths, ctx->Bsum.p, ctx->BBsum.p, ctx->B.p, ctx->BB.p,
+                     ctx->row_ptr.p, nnz, ctx->G.p, ctx->GG.p, desc->want_var ? 1 : 0, ctx->stream));
+  *launches += 1 + (desc->want_var ? 1 : 0);
+  return PDDS_OK;
+}
+
+}  // namespace pdds
 
 extern "C" {
 
@@ -320,6 +352,14 @@ pdds_status pdds_destroy(pdds_ctx* ctx) {
     ctx->sw32.release();
     ctx->sval32.release();
     ctx->sctl.release();
+    drop_graph(ctx);
+    ctx->knot_inst.release();
+    ctx->inst_knot0.release();
+    ctx->b_iters.release();
+    ctx->b_refines.release();
+    ctx->inst_pd.release();
+    ctx->b_relres.release();
+    ctx->b_tend.release();
     if (ctx->host_rr) cudaFreeHost(ctx->host_rr);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -339,6 +379,7 @@ pdds_status pdds_problem_set(pdds_ctx* ctx, const pdds_problem_desc* desc) {
     return fail(ctx, PDDS_ERR_INVALID, "PDDS_LUT needs pdds_problem_set_lut first");
   if (desc->kind == PDDS_HELMHOLTZ && desc->p[2] > 0.0)
     return fail(ctx, PDDS_ERR_INVALID, "Helmholtz reaction c must be <= 0");
+  drop_graph(ctx);  // a captured batch sequence holds the problem by value
   ctx->prob = *desc;
   ctx->has_problem = true;
   return PDDS_OK;
@@ -351,6 +392,8 @@ pdds_status pdds_problem_set_lut(pdds_ctx* ctx, const float* coef, const float* 
   if (!(bounds[2] > bounds[0] && bounds[3] > bounds[1])) return fail(ctx, PDDS_ERR_INVALID, "bad table bounds");
   if (ctx->device < 0) return fail(ctx, PDDS_ERR_INVALID, "context has no device");
   CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  drop_graph(ctx);
   const size_t n = (size_t)nx * ny;
   CK(ctx->lut_coef.resize(8 * n));
   CK(ctx->lut_g.resize(n));
@@ -367,6 +410,14 @@ pdds_status pdds_layout_build(pdds_ctx* ctx, const pdds_layout_desc* desc, pdds_
   if (!ctx || !desc) return PDDS_ERR_INVALID;
   for (int q = 0; q < 4; q++)
     if (!(desc->fac[q] > 0.0)) return fail(ctx, PDDS_ERR_INVALID, "fac must be positive");
+  if (ctx->device >= 0) {
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  drop_graph(ctx);
+  ctx->is_batch = false;
+  ctx->n_inst = 0;
+  ctx->has_batch_run = false;
   const std::string e = build_rect_layout(ctx->L, desc->sw, desc->ne, desc->nsub, desc->nnode, desc->fac,
                                           ctx->bins);
   if (!e.empty()) return fail(ctx, PDDS_ERR_INVALID, e);
@@ -451,24 +502,10 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
   const ProblemDev P = problem_dev(ctx);
   const int N = desc->npaths;
   int launches = 0;
-  CK(cudaEventRecord(ctx->ev0, s));
-  CK(cudaMemsetAsync(ctx->errf.p, 0, sizeof(unsigned), s));
-  CK(cudaMemsetAsync(ctx->stats.p, 0, 8 * sizeof(unsigned long long), s));
-  const bool need_ipsi = !(mode == PDDS_MODE_REPLAY_FP64 && desc->ipsi_override);
-  if (need_ipsi && (!ctx->tables_ready || !desc->reuse_tables)) {
-    int max_n = 0;
-    for (auto& sh : L.shapes) max_n = std::max(max_n, sh.n);
-    CK(launch_rbf_setup(ctx->dl, max_n, ctx->max_nbins, ctx->ipsi.p, ctx->tab.p, ctx->errf.p, s));
-    launches += 2;
-    ctx->tables_ready = true;
+  {
+    pdds_status st = enqueue_prefix(ctx, desc, P, true, &launches);
+    if (st != PDDS_OK) return st;
   }
-  CK(cudaEventRecord(ctx->ev1, s));
-  CK(cudaMemsetAsync(ctx->G.p, 0, std::max<int64_t>(nnz, 1) * sizeof(double), s));
-  CK(cudaMemsetAsync(ctx->GG.p, 0, std::max<int64_t>(nnz, 1) * sizeof(double), s));
-  CK(cudaMemsetAsync(ctx->Bsum.p, 0, L.K * sizeof(double), s));
-  CK(cudaMemsetAsync(ctx->BBsum.p, 0, L.K * sizeof(double), s));
-  CK(launch_boundary_b(ctx->dl, P, mode, ctx->bnd_knots.p, ctx->n_bnd, ctx->B.p, ctx->BB.p, s));
-  launches += ctx->n_bnd > 0;
   const int n_mc = ctx->n_mc;
   if (mode == PDDS_MODE_REPLAY_FP64) {
     const int64_t total = (int64_t)n_mc * N;
@@ -560,49 +597,13 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
       info->exits_stencil = nsn;
     }
   } else {
-    const int target = 4 * std::max(ctx->num_sms, 1) * 4;
-    int chunks = std::max(1, (target + std::max(n_mc, 1) - 1) / std::max(n_mc, 1));
-    chunks = std::min(chunks, std::max(1, N / 256));
-    const int ppc = (N + chunks - 1) / chunks;
-    chunks = (N + ppc - 1) / ppc;
+    int chunks = 1, ppc = 1;
+    item_split(ctx, N, &chunks, &ppc);
     const int n_items = n_mc * chunks;
     CK(cudaMemsetAsync(ctx->counter.p, 0, sizeof(int), s));
     if (mode == PDDS_MODE_MIXED) {
-      MixedArgs a;
-      a.L = ctx->dl;
-      a.P = P;
-      a.N = N;
-      a.h = (float)desc->h;
-      a.sqrth = (float)std::sqrt(desc->h);
-      a.inv_N = 1.0 / N;
-      a.seed = desc->seed;
-      a.instance = desc->instance;
-      a.chunks = chunks;
-      a.paths_per_chunk = ppc;
-      a.n_items = n_items;
-      a.want_var = desc->want_var ? 1 : 0;
-      a.dup_sum = desc->dup_sum;
-      a.adaptive_h = desc->adaptive_h ? 1 : 0;
-      a.richardson = desc->richardson ? 1 : 0;
-      a.h64 = desc->h;
-      a.max_steps = max_steps;
-      a.mc_knots = ctx->mc_knots.p;
-      a.item_counter = ctx->counter.p;
-      a.G = ctx->G.p;
-      a.GG = ctx->GG.p;
-      a.Bsum = ctx->Bsum.p;
-      a.BBsum = ctx->BBsum.p;
-      a.stats = ctx->stats.p;
-      a.err_flags = ctx->errf.p;
-      const size_t smem = ctx->mixed_smem * (a.want_var ? 2 : 1);
-      if (smem > 200 * 1024) return fail(ctx, PDDS_ERR_INVALID, "exit histograms exceed shared memory; lower bins_per_gap");
-      int bps = mixed_blocks_per_sm(P.kind, smem, a.richardson);
-      if (bps < 1) bps = 1;
-      const int grid = std::max(1, std::min(n_items, bps * ctx->num_sms));
-      if (n_items > 0) {
-        CK(launch_paths_mixed(a, P.kind, grid, smem, s));
-        launches++;
-      }
+      pdds_status st = enqueue_mixed_paths(ctx, desc, P, chunks, ppc, &launches);
+      if (st != PDDS_OK) return st;
     } else {
       Fp64Args a;
       a.L = ctx->dl;

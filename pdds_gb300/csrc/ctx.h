@@ -1,0 +1,129 @@
+// Context of the C ABI (internal to the library): device buffers of the
+// layout, the problem, results and scratch, shared by capi.cu and batch.cu.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/pdds.h"
+#include "kernels.h"
+#include "pdds_internal.h"
+
+namespace pdds {
+
+template <typename T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  cudaError_t resize(size_t count) {
+    if (count <= n && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    if (count == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    if (e == cudaSuccess) n = count;
+    return e;
+  }
+  cudaError_t upload(const std::vector<T>& v, cudaStream_t s) {
+    cudaError_t e = resize(std::max<size_t>(v.size(), 1));
+    if (e != cudaSuccess || v.empty()) return e;
+    return cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s);
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+}  // namespace pdds
+
+using pdds::DBuf;
+using pdds::DevLayout;
+using pdds::HostLayout;
+
+struct pdds_ctx {
+  int device = -1;
+  cudaStream_t stream = nullptr;
+  int num_sms = 0;
+  std::string err;
+  bool has_problem = false;
+  pdds_problem_desc prob{};
+  DBuf<float> lut_coef, lut_g;
+  int lut_nx = 0, lut_ny = 0;
+  double lut_bounds[4] = {0, 0, 0, 0};
+  bool has_layout = false;
+  HostLayout L;
+  int bins = 16;
+  bool tables_ready = false;
+  // device layout
+  DBuf<double> kx, ky, st_rect, sd_c, sd_origin, side_px, side_py, sh_c, sh_lo, sh_delta, sh_t, ipsi;
+  DBuf<int> knot_stencil, st_side, st_glob, map_pos, sd_n, sd_orient, sd_shape, side_knot, sh_n,
+      sh_nbins, col, mc_knots, bnd_knots;
+  DBuf<int64_t> row_ptr, st_map_off, sd_knot_off, sh_tab_off, sh_ipsi_off, sh_t_off;
+  DBuf<unsigned char> map_owner;
+  DBuf<float> tab;
+  DevLayout dl{};
+  int n_mc = 0, n_bnd = 0;
+  size_t mixed_smem = 0, fp64_smem = 0;
+  int max_nbins = 0;
+  // results and scratch
+  DBuf<double> G, GG, B, BB, Bsum, BBsum;
+  DBuf<unsigned long long> stats;
+  DBuf<unsigned> errf;
+  DBuf<int> counter;
+  bool has_estimate = false;
+  // replay scratch
+  DBuf<double> rx, ry, rY, rZ, rxi, Gside, GGside, ipsi_knot;
+  DBuf<int> rside, rsl, rss, task_m, task_d, task_i;
+  DBuf<int64_t> task_out, knot_task_off, knot_ipsi_off;
+  // solve scratch
+  DBuf<double> sv64, sscal, spart, shess, su;
+  DBuf<float> sV32, sw32, sval32;
+  DBuf<unsigned> sctl;
+  double* host_rr = nullptr;
+  int solve_m = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
+  // batch of independent instances (pdds_batch_build): the layout above is
+  // the block-diagonal union of the instances' layouts
+  bool is_batch = false;
+  int n_inst = 0;
+  std::vector<int> inst_k0;         // first knot of each instance, n_inst + 1
+  std::vector<int64_t> inst_nnz0;   // first G entry of each instance, n_inst + 1
+  std::vector<double> inst_p;       // 8 problem parameters per instance
+  DBuf<int> knot_inst, inst_knot0, b_iters, b_refines;
+  DBuf<double> inst_pd, b_relres;
+  DBuf<unsigned long long> b_tend;  // per instance, then the start stamp
+  int max_inst_knots = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  std::vector<unsigned char> graph_key;
+  int graph_launches = 0;
+  bool has_batch_run = false;
+};
+
+namespace pdds {
+
+pdds_status fail(pdds_ctx* c, pdds_status s, const std::string& msg);
+// Uploads ctx->L into the device layout buffers and fills ctx->dl.
+pdds_status upload_layout(pdds_ctx* ctx);
+ProblemDev problem_dev(const pdds_ctx* ctx);
+// Reads the device error flags (synchronises the stream).
+pdds_status check_err_flags(pdds_ctx* ctx);
+// Enqueues the MIXED estimation on ctx->stream: RBF factorisation and tables
+// (unless reused), zeroing, boundary knots, the path kernel and the
+// finalisation.  No host synchronisation, so it can be graph-captured.
+pdds_status enqueue_mixed(pdds_ctx* ctx, const pdds_estimate_desc* desc, int* launches);
+// Destroys the captured batch graph (its kernels hold buffer addresses).
+void drop_graph(pdds_ctx* ctx);
+
+}  // namespace pdds
+
+#define CK(call)                                                                         \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess)                                                               \
+      return fail(ctx, PDDS_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)

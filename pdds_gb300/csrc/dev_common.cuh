@@ -49,6 +49,11 @@ struct DevLayout {
   const double* sh_t;
   const float* tab;
   const double* ipsi;
+  // batch of independent instances (null for one layout): instance of each
+  // knot, first knot of each instance, 8 problem parameters per instance
+  const int* knot_inst;
+  const int* inst_knot0;
+  const double* inst_p;
 };
 
 // Coefficient tables of the PK_LUT problem: node (i, j) of an nx x ny grid
@@ -70,6 +75,20 @@ struct ProblemDev {
 };
 
 enum { PK_POISSON_SINCOS = 0, PK_MONEGROS = 1, PK_HELMHOLTZ = 2, PK_VARCOEF = 3, PK_LUT = 4 };
+
+// Problem parameters of the instance that owns knot k (batches), else P's own.
+__device__ __forceinline__ void instance_params(const DevLayout& L, int k, ProblemDev& P, uint32_t& rng_inst,
+                                                uint32_t& rng_knot) {
+  if (L.knot_inst) {
+    const int i = L.knot_inst[k];
+#pragma unroll
+    for (int q = 0; q < 8; q++) P.p[q] = L.inst_p[8 * i + q];
+    rng_inst += (uint32_t)i;
+    rng_knot = (uint32_t)(k - L.inst_knot0[i]);
+  } else {
+    rng_knot = (uint32_t)k;
+  }
+}
 
 // ------------------------------------------------------------------ tables
 // Bicubic Catmull-Rom (Keys cubic convolution, a = -1/2) interpolation,

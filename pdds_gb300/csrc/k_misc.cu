@@ -37,7 +37,10 @@ __global__ void k_boundary(const DevLayout L, const ProblemDev P, int portable, 
   if (t >= n) return;
   const int k = knots[t];
   const double x = L.kx[k], y = L.ky[k];
-  const double g = portable ? g_port<KIND>(P, x, y) : u_f64<KIND>(P, x, y);
+  ProblemDev Pk = P;
+  uint32_t ri = 0, rk = 0;
+  instance_params(L, k, Pk, ri, rk);
+  const double g = portable ? g_port<KIND>(Pk, x, y) : u_f64<KIND>(Pk, x, y);
   B[k] = g;
   BB[k] = g * g;
 }

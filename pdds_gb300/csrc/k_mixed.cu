@@ -114,8 +114,11 @@ k_paths_mixed(const MixedArgs a) {
       s_h = a.h;
       s_sqrth = a.sqrth;
       if (a.adaptive_h) {
+        ProblemDev Pk = a.P;
+        uint32_t ri = 0, rk = 0;
+        instance_params(L, k, Pk, ri, rk);
         Coef<double> kd;
-        coef_f64<KIND>(a.P, L.kx[k], L.ky[k], kd);
+        coef_f64<KIND>(Pk, L.kx[k], L.ky[k], kd);
         const double hk = adaptive_step<double>(L.st_rect + 4 * st, L.kx[k], L.ky[k], a.h64, kd);
         s_h = (float)hk;
         s_sqrth = (float)sqrt(hk);
@@ -152,6 +155,10 @@ k_paths_mixed(const MixedArgs a) {
     }
     __syncthreads();
     const int knot = s_knot, path_end = s_path_end, hist_len = s_hist_len;
+    // the problem of this knot's instance, and its Philox instance and knot words
+    ProblemDev P = a.P;
+    uint32_t rng_inst = a.instance, rng_knot = 0;
+    instance_params(L, knot, P, rng_inst, rng_knot);
     const float h = s_h, sqrth = s_sqrth;
     const int nh = a.want_var ? 2 * hist_len : hist_len;
     for (int i = tid; i < nh; i += MIXED_THREADS) hist[i] = 0.f;
@@ -208,10 +215,10 @@ k_paths_mixed(const MixedArgs a) {
       if constexpr (KIND == PK_LUT) {
         k.s00 = s.cf[0]; k.s01 = 0.f; k.s10 = 0.f; k.s11 = s.cf[1];
         k.b0 = s.cf[2]; k.b1 = s.cf[3]; k.c = s.cf[4]; k.f = s.cf[5];
-        k.g0 = a.P.use_cv ? s.cf[6] : 0.f;
-        k.g1 = a.P.use_cv ? s.cf[7] : 0.f;
+        k.g0 = P.use_cv ? s.cf[6] : 0.f;
+        k.g1 = P.use_cv ? s.cf[7] : 0.f;
       } else {
-        coef_f32<KIND>(a.P, s.x, s.y, k);
+        coef_f32<KIND>(P, s.x, s.y, k);
       }
       const float v0 = -(k.s00 * k.g0 + k.s10 * k.g1);
       const float v1 = -(k.s01 * k.g0 + k.s11 * k.g1);
@@ -224,11 +231,11 @@ k_paths_mixed(const MixedArgs a) {
       const float dx = fabsf(s.x - cx) - hx, dy = fabsf(s.y - cy) - hy;
       float nx, ny;  // |N^T sigma| for the x and y normals
       if constexpr (KIND == PK_LUT) {
-        lut_sample<float, 8>(a.P.lut, s.x, s.y, s.cf);
+        lut_sample<float, 8>(P.lut, s.x, s.y, s.cf);
         nx = fabsf(s.cf[0]);
         ny = fabsf(s.cf[1]);
       } else {
-        sigma_normals_f32<KIND>(a.P, s.x, s.y, nx, ny);
+        sigma_normals_f32<KIND>(P, s.x, s.y, nx, ny);
       }
       const float thr = -0.5826f * sq * (dx > dy ? nx : ny);
       return !(fmaxf(dx, dy) < thr) || s.steps >= (unsigned)a.max_steps;
@@ -245,7 +252,7 @@ k_paths_mixed(const MixedArgs a) {
         int om;
         const float dist = rect2d<float>(rect, s.x, s.y, Ex, Ey, Nx, Ny, om);
         float g00, g01, g10, g11;
-        sigma_f32<KIND>(a.P, s.x, s.y, g00, g01, g10, g11);
+        sigma_f32<KIND>(P, s.x, s.y, g00, g01, g10, g11);
         const float w0 = Nx * g00 + Ny * g10, w1 = Nx * g01 + Ny * g11;
         if (dist < -0.5826f * sqrtf(w0 * w0 + w1 * w1) * (wgt < 0.f ? sqrth : (RICH ? sqrth * 0.70710678f : sqrth))) {
           atomicOr(a.err_flags, ERR_FLAG_STEP_LIMIT);
@@ -261,7 +268,7 @@ k_paths_mixed(const MixedArgs a) {
       const int onmask = (onN ? 1 : 0) | (onS ? 2 : 0) | (onE ? 4 : 0) | (onW ? 8 : 0);
       if (onmask & globmask) {
         ++nglob;
-        val = s.Z + s.Y * u_f32<KIND>(a.P, Ex, Ey) + s.xi;
+        val = s.Z + s.Y * u_f32<KIND>(P, Ex, Ey) + s.xi;
         return;
       }
       ++nsten;
@@ -281,7 +288,7 @@ k_paths_mixed(const MixedArgs a) {
     };
     Lvl<KIND> F, Cs;
     float cf0[8];  // table fields at the knot (PK_LUT)
-    if constexpr (KIND == PK_LUT) lut_sample<float, 8>(a.P.lut, x0, y0, cf0);
+    if constexpr (KIND == PK_LUT) lut_sample<float, 8>(P.lut, x0, y0, cf0);
     auto reset = [&]() {
       F.x = x0; F.y = y0; F.Y = 1.f; F.Z = 0.f; F.xi = 0.f; F.steps = 0;
       if constexpr (KIND == PK_LUT) {
@@ -299,7 +306,7 @@ k_paths_mixed(const MixedArgs a) {
       QEntry e0, e1;
       bool fx = false, cx_ = false;  // exits in this iteration
       if (active) {
-        const u32x4 blk = path_block(a.seed, a.instance, (uint32_t)knot, path, m++);
+        const u32x4 blk = path_block(a.seed, rng_inst, rng_knot, path, m++);
         float za0, za1, zb0, zb1;
         normals_f32(blk.v[0], blk.v[1], za0, za1);
         normals_f32(blk.v[2], blk.v[3], zb0, zb1);

@@ -563,4 +563,10 @@ cudaError_t solve_gmres_ir_cluster(const SolveCsr& A, const double* b, double* x
   return e == cudaSuccess ? cudaGetLastError() : e;
 }
 
+cudaError_t launch_to_f32(const double* a, float* b, int64_t n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_to_f32<<<vgrid((int)std::min<int64_t>(n, 1 << 28)), 256, 0, s>>>(n, a, b);
+  return cudaGetLastError();
+}
+
 }  // namespace pdds

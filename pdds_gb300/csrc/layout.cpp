@@ -12,6 +12,8 @@
 // the same interface (or the same cross point) share one stencil record, and
 // stencil sides with identical knot lists share one side record.
 #include <algorithm>
+#include <climits>
+#include <cstdint>
 #include <cmath>
 #include <map>
 #include <tuple>
@@ -421,6 +423,62 @@ std::string build_rect_layout(HostLayout& L, const double sw[2], const double ne
     ip += (int64_t)sh.n * sh.n;
   }
   set_shape_bins(L, bps);
+  return "";
+}
+
+std::string merge_layouts(HostLayout& out, const std::vector<HostLayout>& parts, int bps) {
+  out = HostLayout();
+  if (parts.empty()) return "a batch needs at least one instance";
+  const HostLayout& p0 = parts[0];
+  for (int i = 0; i < 2; i++) { out.sw[i] = p0.sw[i]; out.ne[i] = p0.ne[i]; }
+  for (int i = 0; i < 4; i++) out.fac[i] = p0.fac[i];
+  out.nsub = p0.nsub;
+  out.nnode = p0.nnode;
+  out.row_ptr.push_back(0);
+  for (const HostLayout& P : parts) {
+    const int k0 = out.K;
+    const int s0 = (int)out.stencils.size();
+    const int d0 = (int)out.sides.size();
+    const int h0 = (int)out.shapes.size();
+    const int64_t e0 = out.row_ptr.back();
+    const int64_t sk0 = (int64_t)out.side_knot.size();
+    const int64_t m0 = (int64_t)out.map_pos.size();
+    if ((int64_t)out.K + P.K > (int64_t)INT32_MAX) return "batch has more than 2^31 knots";
+    out.K += P.K;
+    out.kx.insert(out.kx.end(), P.kx.begin(), P.kx.end());
+    out.ky.insert(out.ky.end(), P.ky.begin(), P.ky.end());
+    for (int v : P.order) out.order.push_back(v + k0);
+    for (int v : P.knot_stencil) out.knot_stencil.push_back(v + s0);
+    out.knot_boundary.insert(out.knot_boundary.end(), P.knot_boundary.begin(), P.knot_boundary.end());
+    out.nboundary += P.nboundary;
+    for (int v = 0; v < P.K; v++) out.row_ptr.push_back(e0 + P.row_ptr[v + 1]);
+    for (int c : P.col) out.col.push_back(c + k0);
+    for (StencilRec st : P.stencils) {
+      for (int d = 0; d < 4; d++)
+        if (st.side[d] >= 0) st.side[d] += d0;
+      st.map_off += m0;
+      for (int& c : st.cols) c += k0;
+      out.stencils.push_back(std::move(st));
+    }
+    for (SideRec sr : P.sides) {
+      sr.shape += h0;
+      sr.knot_off += sk0;
+      out.sides.push_back(sr);
+    }
+    for (int v : P.side_knot) out.side_knot.push_back(v + k0);
+    out.side_px.insert(out.side_px.end(), P.side_px.begin(), P.side_px.end());
+    out.side_py.insert(out.side_py.end(), P.side_py.begin(), P.side_py.end());
+    out.map_pos.insert(out.map_pos.end(), P.map_pos.begin(), P.map_pos.end());
+    out.map_owner.insert(out.map_owner.end(), P.map_owner.begin(), P.map_owner.end());
+    out.shapes.insert(out.shapes.end(), P.shapes.begin(), P.shapes.end());
+    out.max_side = std::max(out.max_side, P.max_side);
+  }
+  int64_t ip = 0;
+  for (auto& sh : out.shapes) {
+    sh.ipsi_off = ip;
+    ip += (int64_t)sh.n * sh.n;
+  }
+  set_shape_bins(out, bps);
   return "";
 }
 

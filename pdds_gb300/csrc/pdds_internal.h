@@ -81,6 +81,11 @@ struct HostLayout {
 std::string build_rect_layout(HostLayout& L, const double sw[2], const double ne[2], int nsub,
                               int nnode, const double fac[4], int bins_per_gap);
 
+// Block-diagonal union of independent layouts (a batch of instances): knots,
+// stencils, sides and shapes of part i follow those of part i-1 with all
+// indices shifted; G columns stay inside their part's knot range.
+std::string merge_layouts(HostLayout& out, const std::vector<HostLayout>& parts, int bins_per_gap);
+
 // Re-derives the shape bin grids for a new bins-per-gap value.
 void set_shape_bins(HostLayout& L, int bins_per_gap);
 

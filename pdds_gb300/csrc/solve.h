@@ -60,6 +60,10 @@ struct ClusterGmresArgs {
 // fit the kernel's shared-memory staging (8 max_rows + 4 max_rows / cluster bytes).
 int gmres_cluster_pick(int max_rows);
 cudaError_t launch_gmres_cluster(const ClusterGmresArgs& a, int cluster, int max_rows, cudaStream_t s);
+// Writes %globaltimer (ns) to *t when the stream reaches it.
+cudaError_t launch_stamp(unsigned long long* t, cudaStream_t s);
+// b[i] = (float)a[i]
+cudaError_t launch_to_f32(const double* a, float* b, int64_t n, cudaStream_t s);
 
 // The same solve through k_gmres_cluster for one system; *used is false (and
 // nothing ran) when the system does not fit the cluster kernel.

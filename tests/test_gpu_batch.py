@@ -1,0 +1,68 @@
+"""Many-instance batches on the GPU: every instance of a batch gets the
+answer a run of that instance alone gets (same random stream, agreement far
+inside the Monte Carlo error), each converges to its own tolerance and
+approaches its analytic solution, and the CUDA-graph replay of the sequence
+equals the directly launched sequence."""
+import numpy as np
+import pytest
+
+import pdds_gb300 as P
+from pdds_gb300.config import batch_instances, fac_rule
+
+pytestmark = pytest.mark.gpu
+
+N, H = 2000, 1e-3
+
+
+def small_instances():
+    return [P.Instance((0.0, 0.0), (1.0, 1.0), g, k, fac_rule(1.0, g, k), (a, b, c))
+            for g, k, a, b, c in [(4, 11, 1.5, 2.0, -1.0), (6, 9, 3.0, 1.2, 0.0), (5, 13, 2.2, 3.7, -3.5)]]
+
+
+def test_batch_instance_equals_single_run():
+    insts = small_instances()
+    with P.Batch(P.BVP.HELMHOLTZ, insts) as bt:
+        info = bt.run(N, H, seed=11, instance=100, adaptive_h=True, use_graph=False)
+        assert info["unconverged"] == 0
+        res = [bt.result(i) for i in range(len(insts))]
+    for i, ins in enumerate(insts):
+        with P.PDDSparseGM(ins.sw, ins.ne, ins.nsub, ins.nnode, ins.fac) as pd:
+            bvp = P.BVP.helmholtz(*ins.params)
+            est = pd.estimate(bvp, N, H, mode=P.MODE_MIXED, seed=11, instance=100 + i, adaptive_h=True)
+            u, _ = pd.solve_interface(P.SOLVE_GMRES_FP32_IR, tol=1e-10)
+            # same Philox streams: only the order of the FP32/FP64 sums differs
+            assert np.max(np.abs(res[i]["B"] - est.B)) < 1e-5
+            assert np.max(np.abs(res[i]["u"] - u)) < 1e-4
+            rmse = np.sqrt(np.mean((res[i]["u"] - bvp.u(pd.x, pd.y)) ** 2))
+            assert rmse < 5e-2, rmse
+
+
+def test_batch_graph_replay_matches_direct_launch():
+    insts = small_instances()
+    with P.Batch(P.BVP.HELMHOLTZ, insts) as bt:
+        bt.run(N, H, seed=5, use_graph=False)
+        direct = [bt.result(i)["u"] for i in range(len(insts))]
+        first = bt.run(N, H, seed=5, use_graph=True)
+        second = bt.run(N, H, seed=5, use_graph=True)
+        assert first["graph_replayed"] == 0 and second["graph_replayed"] == 1
+        assert second["kernel_launches"] == first["kernel_launches"] > 0
+        replay = [bt.result(i) for i in range(len(insts))]
+    for d, r in zip(direct, replay):
+        assert np.max(np.abs(d - r["u"])) < 1e-6
+        assert r["latency_ms"] > 0.0 and r["iterations"] > 0
+
+
+def test_batch_many_instances_converge():
+    insts = batch_instances(24, seed=3, grid=(4, 10), nodes=(11, 25))
+    with P.Batch(P.BVP.HELMHOLTZ, insts) as bt:
+        info = bt.run(1000, H, seed=2, use_graph=True)
+        assert info["unconverged"] == 0
+        assert info["max_rel_residual"] <= 1e-10 * 1.0000001
+        lat = []
+        for i, ins in enumerate(insts):
+            r = bt.result(i)
+            x, y = bt.knots(i)
+            bvp = P.BVP.helmholtz(*ins.params)
+            assert np.sqrt(np.mean((r["u"] - bvp.u(x, y)) ** 2)) < 0.1  # N = 1e3, plain step
+            lat.append(r["latency_ms"])
+        assert 0.0 < min(lat) <= max(lat) <= info["ms"] * 1.5
