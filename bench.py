@@ -157,16 +157,25 @@ def cpu_baseline(workload: dict, fac, n_knots: int, seed: int = 1234, npaths=Non
 def many_instance_batch(local: int, n_inst: int = 256, reps: int = 3, npaths: int = 10_000, h: float = 1e-3):
     """256 independent Helmholtz instances on [0,1]^2 (random g x g grids,
     g in 4..16, 11..41 knots per segment, a, b ~ U[1,4], c ~ U[-4,0]),
-    1e4 paths per knot, h = 1e-3, MIXED with the adaptive step, every
-    instance solved by the cluster GMRES; the sequence is one CUDA graph."""
+    1e4 paths per knot, h = 1e-3, MIXED with the adaptive step and the
+    Richardson pair (as the headline step), every instance solved by the
+    cluster GMRES; the sequence is one CUDA graph, replayed with a new Philox
+    instance word each run.  The plain method (no Richardson) is timed too."""
     import pdds_gb300 as P
     from pdds_gb300.config import batch_instances
     insts = batch_instances(n_inst, seed=1234)
     t0 = time.perf_counter()
     bt = P.Batch(P.BVP.HELMHOLTZ, insts, device=local)
     t_build = time.perf_counter() - t0
-    bt.run(npaths, h, seed=1234, instance=0, use_graph=True)  # capture + warm-up
-    runs = [bt.run(npaths, h, seed=1234, instance=1000 * (r + 1), use_graph=True) for r in range(reps)]
+    bt.run(npaths, h, seed=1234, instance=0, use_graph=True, richardson=False)
+    plain = bt.run(npaths, h, seed=1234, instance=500, use_graph=True, richardson=False)
+    plain_rmse = []
+    for i, ins in enumerate(insts):
+        x, y = bt.knots(i)
+        plain_rmse.append(float(np.sqrt(np.mean((bt.result(i)["u"] - P.BVP.helmholtz(*ins.params).u(x, y)) ** 2))))
+    bt.run(npaths, h, seed=1234, instance=0, use_graph=True, richardson=True)  # capture + warm-up
+    runs = [bt.run(npaths, h, seed=1234, instance=1000 * (r + 1), use_graph=True, richardson=True)
+            for r in range(reps)]
     lat, rmse, iters = [], [], []
     for i, ins in enumerate(insts):
         r = bt.result(i)
@@ -183,7 +192,10 @@ def many_instance_batch(local: int, n_inst: int = 256, reps: int = 3, npaths: in
            "rmse_vs_analytic_mean": float(np.mean(rmse)), "rmse_vs_analytic_max": float(np.max(rmse)),
            "solver_iterations_max": int(max(iters)), "unconverged": int(max(r["unconverged"] for r in runs)),
            "kernel_launches_per_batch": int(runs[-1]["kernel_launches"]), "graph_replayed": int(runs[-1]["graph_replayed"]),
-           "host_build_s": t_build}
+           "host_build_s": t_build,
+           "plain_method": {"ms_per_batch": plain["ms"], "solves_per_s": n_inst / (plain["ms"] / 1000.0),
+                            "rmse_vs_analytic_mean": float(np.mean(plain_rmse)),
+                            "rmse_vs_analytic_max": float(np.max(plain_rmse))}}
     bt.close()
     return out
 

@@ -28,7 +28,9 @@ pdds_status enqueue_batch(pdds_ctx* ctx, const pdds_batch_run_desc* d, int clust
   const int64_t nnz = ctx->L.row_ptr[ctx->L.K];
   CK(launch_stamp(ctx->b_tend.p + n, s));
   ++*launches;
+  ctx->rng_override = ctx->rng_dev.p;
   pdds_status st = enqueue_mixed(ctx, &d->estimate, launches);
+  ctx->rng_override = nullptr;
   if (st != PDDS_OK) return st;
   CK(launch_to_f32(ctx->G.p, ctx->sval32.p, nnz, s));
   ++*launches;
@@ -106,6 +108,8 @@ pdds_status pdds_batch_build(pdds_ctx* ctx, const pdds_instance_desc* inst, int3
     CK(ctx->b_refines.resize(n));
     CK(ctx->b_relres.resize(n));
     CK(ctx->b_tend.resize(n + 1));
+    CK(ctx->rng_dev.resize(2));
+    if (!ctx->rng_host) CK(cudaMallocHost(&ctx->rng_host, 2 * sizeof(unsigned long long)));
     pdds_status st = upload_layout(ctx);
     if (st != PDDS_OK) return st;
     CK(cudaStreamSynchronize(s));
@@ -160,12 +164,19 @@ pdds_status pdds_batch_run(pdds_ctx* ctx, const pdds_batch_run_desc* desc, pdds_
   // the graph is reused while the descriptor, the cluster size and the solve
   // scratch (which pdds_solve_interface may also reallocate) are unchanged;
   // layout, problem and table changes drop it where they happen
+  // seed and instance live in device memory (rng_dev), not in the graph
+  pdds_batch_run_desc kd = *desc;
+  kd.estimate.seed = 0;
+  kd.estimate.instance = 0;
   std::vector<unsigned char> key(sizeof(pdds_batch_run_desc) + sizeof(int) + sizeof(after));
-  std::memcpy(key.data(), desc, sizeof(pdds_batch_run_desc));
+  std::memcpy(key.data(), &kd, sizeof(pdds_batch_run_desc));
   std::memcpy(key.data() + sizeof(pdds_batch_run_desc), &cluster, sizeof(int));
   std::memcpy(key.data() + sizeof(pdds_batch_run_desc) + sizeof(int), after, sizeof(after));
   int launches = 0;
   bool replayed = false;
+  ctx->rng_host[0] = ed.seed;
+  ctx->rng_host[1] = ed.instance;
+  CK(cudaMemcpyAsync(ctx->rng_dev.p, ctx->rng_host, 2 * sizeof(unsigned long long), cudaMemcpyHostToDevice, s));
   if (desc->use_graph) {
     if (!ctx->graph_exec || ctx->graph_key != key) {
       drop_graph(ctx);

@@ -264,6 +264,7 @@ pdds_status enqueue_mixed_paths(pdds_ctx* ctx, const pdds_estimate_desc* desc, c
   a.BBsum = ctx->BBsum.p;
   a.stats = ctx->stats.p;
   a.err_flags = ctx->errf.p;
+  a.rng_dev = ctx->rng_override;
   const size_t smem = ctx->mixed_smem * (a.want_var ? 2 : 1);
   if (smem > 200 * 1024) return fail(ctx, PDDS_ERR_INVALID, "exit histograms exceed shared memory; lower bins_per_gap");
   int bps = mixed_blocks_per_sm(P.kind, smem, a.richardson);
@@ -360,6 +361,8 @@ pdds_status pdds_destroy(pdds_ctx* ctx) {
     ctx->inst_pd.release();
     ctx->b_relres.release();
     ctx->b_tend.release();
+    ctx->rng_dev.release();
+    if (ctx->rng_host) cudaFreeHost(ctx->rng_host);
     if (ctx->host_rr) cudaFreeHost(ctx->host_rr);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);

@@ -102,6 +102,10 @@ struct pdds_ctx {
   std::vector<unsigned char> graph_key;
   int graph_launches = 0;
   bool has_batch_run = false;
+  // {seed, instance} read by the path kernel of a batch sequence
+  DBuf<unsigned long long> rng_dev;
+  unsigned long long* rng_host = nullptr;  // pinned staging of rng_dev
+  const unsigned long long* rng_override = nullptr;
 };
 
 namespace pdds {

@@ -157,7 +157,8 @@ k_paths_mixed(const MixedArgs a) {
     const int knot = s_knot, path_end = s_path_end, hist_len = s_hist_len;
     // the problem of this knot's instance, and its Philox instance and knot words
     ProblemDev P = a.P;
-    uint32_t rng_inst = a.instance, rng_knot = 0;
+    const uint64_t seed = a.rng_dev ? (uint64_t)a.rng_dev[0] : a.seed;
+    uint32_t rng_inst = a.rng_dev ? (uint32_t)a.rng_dev[1] : a.instance, rng_knot = 0;
     instance_params(L, knot, P, rng_inst, rng_knot);
     const float h = s_h, sqrth = s_sqrth;
     const int nh = a.want_var ? 2 * hist_len : hist_len;
@@ -306,7 +307,7 @@ k_paths_mixed(const MixedArgs a) {
       QEntry e0, e1;
       bool fx = false, cx_ = false;  // exits in this iteration
       if (active) {
-        const u32x4 blk = path_block(a.seed, rng_inst, rng_knot, path, m++);
+        const u32x4 blk = path_block(seed, rng_inst, rng_knot, path, m++);
         float za0, za1, zb0, zb1;
         normals_f32(blk.v[0], blk.v[1], za0, za1);
         normals_f32(blk.v[2], blk.v[3], zb0, zb1);

@@ -35,6 +35,9 @@ struct MixedArgs {
   double* BBsum;         // [K]
   unsigned long long* stats;  // [0] steps [1] unused [2] global exits [3] stencil exits
   unsigned* err_flags;
+  // optional {seed, instance} in device memory, read instead of seed and
+  // instance (a replayed graph draws fresh numbers when the host updates it)
+  const unsigned long long* rng_dev;
 };
 
 struct Fp64Args {

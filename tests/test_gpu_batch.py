@@ -47,9 +47,14 @@ def test_batch_graph_replay_matches_direct_launch():
         assert first["graph_replayed"] == 0 and second["graph_replayed"] == 1
         assert second["kernel_launches"] == first["kernel_launches"] > 0
         replay = [bt.result(i) for i in range(len(insts))]
+        # a new seed replays the same graph: seed and instance are read from device memory
+        third = bt.run(N, H, seed=6, use_graph=True)
+        assert third["graph_replayed"] == 1
+        other = [bt.result(i)["u"] for i in range(len(insts))]
     for d, r in zip(direct, replay):
         assert np.max(np.abs(d - r["u"])) < 1e-6
         assert r["latency_ms"] > 0.0 and r["iterations"] > 0
+    assert max(np.max(np.abs(d - o)) for d, o in zip(direct, other)) > 1e-6
 
 
 def test_batch_many_instances_converge():
