@@ -149,6 +149,15 @@ typedef struct {
   /* 1: keep the RBF factorisation and tables of the previous call on this
    * layout (they depend only on the layout and bins_per_gap); 0: recompute */
   int32_t reuse_tables;
+  /* MIXED only, 1: variance-adaptive paths per knot, the rule of the
+   * reference's Compute_h_N (PDDSparseGM.cpp:4338-4395): a pilot of npaths
+   * paths per knot estimates the variance V_k of the knot's score, then
+   * N_k = 4 V_k / (0.66666 target_stderr)^2 rounded up to a multiple of 256
+   * and clamped to [npaths, npaths_max]; knots continue with paths
+   * npaths .. N_k-1 of the same Philox streams (pdds_estimate_knot_paths). */
+  int32_t adaptive_n;
+  int32_t npaths_max;
+  double target_stderr;
 } pdds_estimate_desc;
 
 typedef struct {
@@ -166,6 +175,8 @@ typedef struct {
  * B[K], BB[K] (mean of the squared score, as Reduce_Analytic's BB). */
 pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double* val, double* var,
                           double* B, double* BB, pdds_estimate_info* info);
+/* Paths per knot of the last pdds_estimate (npaths[K]; 0 for boundary knots). */
+pdds_status pdds_estimate_knot_paths(pdds_ctx* ctx, int32_t* npaths);
 
 /* ---------------------------------------------------------------- solve */
 typedef enum {

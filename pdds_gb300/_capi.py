@@ -25,7 +25,7 @@ SOLVE_BICGSTAB_FP64, SOLVE_GMRES_FP32_IR = 0, 1
 EXPORTS = [
     "pdds_create", "pdds_destroy", "pdds_last_error", "pdds_version", "pdds_problem_set", "pdds_problem_set_lut",
     "pdds_layout_build", "pdds_layout_knots", "pdds_layout_csr", "pdds_layout_stencil",
-    "pdds_estimate", "pdds_solve_interface", "pdds_batch_build", "pdds_batch_run", "pdds_batch_instance",
+    "pdds_estimate", "pdds_estimate_knot_paths", "pdds_solve_interface", "pdds_batch_build", "pdds_batch_run", "pdds_batch_instance",
     "pdds_solve_bicgstab_static",
 ]
 STATIC_SOLVE_MAX_K = 131072
@@ -51,7 +51,8 @@ class EstimateDesc(C.Structure):
                 ("instance", C.c_uint32), ("dup_sum", C.c_int32), ("want_var", C.c_int32),
                 ("bins_per_gap", C.c_int32), ("max_steps", C.c_int64),
                 ("ipsi_override", C.POINTER(C.c_double)), ("ipsi_override_len", C.c_int64),
-                ("adaptive_h", C.c_int32), ("richardson", C.c_int32), ("reuse_tables", C.c_int32)]
+                ("adaptive_h", C.c_int32), ("richardson", C.c_int32), ("reuse_tables", C.c_int32),
+                ("adaptive_n", C.c_int32), ("npaths_max", C.c_int32), ("target_stderr", C.c_double)]
 
 
 class EstimateInfo(C.Structure):
@@ -118,6 +119,7 @@ def load(path: str = LIB_PATH):
     L.pdds_layout_stencil.argtypes = [vp, C.c_int32, dp, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                       C.POINTER(C.c_int32), C.c_int32]
     L.pdds_estimate.argtypes = [vp, C.POINTER(EstimateDesc), dp, dp, dp, dp, C.POINTER(EstimateInfo)]
+    L.pdds_estimate_knot_paths.argtypes = [vp, C.POINTER(C.c_int32)]
     L.pdds_solve_interface.argtypes = [vp, C.POINTER(SolveDesc), dp, C.POINTER(SolveInfo)]
     L.pdds_batch_build.argtypes = [vp, C.POINTER(InstanceDesc), C.c_int32, C.POINTER(BatchInfo)]
     L.pdds_batch_run.argtypes = [vp, C.POINTER(BatchRunDesc), C.POINTER(BatchRunInfo)]

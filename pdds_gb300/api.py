@@ -150,6 +150,7 @@ class Estimate:
     B: np.ndarray
     BB: np.ndarray
     info: dict = field(default_factory=dict)
+    npaths: np.ndarray = None  # paths per knot (0 for boundary knots)
 
     @property
     def B_var(self):
@@ -242,8 +243,13 @@ class PDDSparseGM:
     def estimate(self, bvp: BVP, npaths: int, h: float, mode: int = capi.MODE_MIXED, seed: int = 1234,
                  instance: int = 0, dup_sum: bool = False, want_var: bool = False,
                  bins_per_gap: int = 0, max_steps: int = 0, ipsi_override=None,
-                 adaptive_h: bool = False, richardson: bool = False, reuse_tables: bool = False) -> Estimate:
-        """Runs the Feynman-Kac estimation of every knot's G row and B entry."""
+                 adaptive_h: bool = False, richardson: bool = False, reuse_tables: bool = False,
+                 adaptive_n: bool = False, npaths_max: int = 0, target_stderr: float = 0.0) -> Estimate:
+        """Runs the Feynman-Kac estimation of every knot's G row and B entry.
+
+        adaptive_n: npaths is the pilot per knot; each knot then runs
+        N_k = 4 Var_k / (0.66666 target_stderr)^2 paths (multiple of 256,
+        clamped to [npaths, npaths_max]); Estimate.npaths holds N_k."""
         if bvp.kind == BVP.LUT and getattr(self, "_lut_owner", None) is not bvp.tables:
             coef, g, bounds = bvp.tables
             ny, nx = g.shape
@@ -265,6 +271,9 @@ class PDDSparseGM:
         d.adaptive_h = int(bool(adaptive_h))
         d.richardson = int(bool(richardson))
         d.reuse_tables = int(bool(reuse_tables))
+        d.adaptive_n = int(bool(adaptive_n))
+        d.npaths_max = int(npaths_max)
+        d.target_stderr = float(target_stderr)
         keep = None
         if ipsi_override is not None:
             keep = np.ascontiguousarray(ipsi_override, np.float64)
@@ -278,8 +287,10 @@ class PDDSparseGM:
         self._check(self._lib.pdds_estimate(self._ctx, C.byref(d), _p(val, C.c_double), _p(var, C.c_double),
                                             _p(B, C.c_double), _p(BB, C.c_double), C.byref(info)))
         del keep
+        kn = np.zeros(self.K, np.int32)
+        self._check(self._lib.pdds_estimate_knot_paths(self._ctx, _p(kn, C.c_int32)))
         return Estimate(self.row_ptr, self.col, val[:self.nnz], var[:self.nnz], B, BB,
-                        {f: getattr(info, f) for f, _ in capi.EstimateInfo._fields_})
+                        {f: getattr(info, f) for f, _ in capi.EstimateInfo._fields_}, kn)
 
     def solve_interface(self, method: int = capi.SOLVE_GMRES_FP32_IR, tol: float = 1e-10,
                         restart: int = 30, max_iter: int = 0, max_refine: int = 0):

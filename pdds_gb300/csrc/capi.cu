@@ -231,11 +231,20 @@ void item_split(const pdds_ctx* ctx, int N, int* chunks_out, int* ppc_out) {
   *ppc_out = ppc;
 }
 
+// explicit work items of a continuation pass (variance-adaptive paths)
+struct ItemList {
+  const int* knot;
+  const int* p0;
+  const int* p1;
+  int n;
+  const double* knot_invN;
+};
+
 pdds_status enqueue_mixed_paths(pdds_ctx* ctx, const pdds_estimate_desc* desc, const ProblemDev& P, int chunks,
-                                int ppc, int* launches) {
+                                int ppc, int* launches, const ItemList* items = nullptr) {
   cudaStream_t s = ctx->stream;
   const int N = desc->npaths;
-  const int n_items = ctx->n_mc * chunks;
+  const int n_items = items ? items->n : ctx->n_mc * chunks;
   const long long max_steps = desc->max_steps > 0 ? desc->max_steps : 1000000LL;
   CK(cudaMemsetAsync(ctx->counter.p, 0, sizeof(int), s));
   MixedArgs a;
@@ -265,6 +274,10 @@ pdds_status enqueue_mixed_paths(pdds_ctx* ctx, const pdds_estimate_desc* desc, c
   a.stats = ctx->stats.p;
   a.err_flags = ctx->errf.p;
   a.rng_dev = ctx->rng_override;
+  a.item_knot = items ? items->knot : nullptr;
+  a.item_p0 = items ? items->p0 : nullptr;
+  a.item_p1 = items ? items->p1 : nullptr;
+  a.knot_invN = items ? items->knot_invN : nullptr;
   const size_t smem = ctx->mixed_smem * (a.want_var ? 2 : 1);
   if (smem > 200 * 1024) return fail(ctx, PDDS_ERR_INVALID, "exit histograms exceed shared memory; lower bins_per_gap");
   int bps = mixed_blocks_per_sm(P.kind, smem, a.richardson);
@@ -273,6 +286,60 @@ pdds_status enqueue_mixed_paths(pdds_ctx* ctx, const pdds_estimate_desc* desc, c
   if (n_items > 0) {
     CK(launch_paths_mixed(a, P.kind, grid, smem, s));
     ++*launches;
+  }
+  return PDDS_OK;
+}
+
+// Variance-adaptive paths per knot after a pilot of desc->npaths paths
+// (Compute_h_N, PDDSparseGM.cpp:4338-4395): N_k = 4 V_k / (0.66666 eps)^2,
+// rounded up to the next multiple of 256 as the reference rounds to N_job,
+// clamped to [N0, npaths_max]; paths N0 .. N_k-1 continue the knot's Philox
+// streams.  Synchronises once to read the pilot's sums.
+pdds_status adaptive_continue(pdds_ctx* ctx, const pdds_estimate_desc* desc, const ProblemDev& P, int* launches) {
+  cudaStream_t s = ctx->stream;
+  const HostLayout& L = ctx->L;
+  const int K = L.K;
+  const int N0 = desc->npaths;
+  const int nmax = std::max(N0, desc->npaths_max > 0 ? desc->npaths_max : 100000);
+  const double eps = desc->target_stderr > 0 ? desc->target_stderr : 1e-3;
+  std::vector<double> bs(K), bbs(K);
+  CK(cudaMemcpyAsync(bs.data(), ctx->Bsum.p, K * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(bbs.data(), ctx->BBsum.p, K * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  std::vector<int> kn(K, 0), ik, ip0, ip1;
+  std::vector<double> scale(K, 1.0), inv(K, 0.0);
+  const int granule = 256, ppc = 2048;
+  for (int v : L.order) {
+    if (L.knot_boundary[v]) continue;
+    const double mean = bs[v] / N0;
+    const double var = std::max(0.0, bbs[v] / N0 - mean * mean);
+    const double want = 4.0 * var / ((eps * 0.66666) * (eps * 0.66666));
+    long long nk = want < 2e9 ? (long long)want : 2000000000LL;
+    nk = (1 + nk / granule) * granule;
+    nk = std::max<long long>(N0, std::min<long long>(nmax, nk));
+    kn[v] = (int)nk;
+    scale[v] = (double)N0 / (double)nk;
+    inv[v] = 1.0 / (double)nk;
+    for (long long p = N0; p < nk; p += ppc) {
+      ik.push_back(v);
+      ip0.push_back((int)p);
+      ip1.push_back((int)std::min<long long>(nk, p + ppc));
+    }
+  }
+  ctx->last_knot_N = kn;
+  CK(ctx->knot_N.upload(kn, s));
+  CK(ctx->knot_scale.upload(scale, s));
+  CK(ctx->knot_invN.upload(inv, s));
+  CK(launch_scale_rows(ctx->mc_knots.p, ctx->n_mc, ctx->row_ptr.p, ctx->knot_scale.p, ctx->G.p,
+                       desc->want_var ? ctx->GG.p : nullptr, s));
+  ++*launches;
+  if (!ik.empty()) {
+    CK(ctx->item_knot.upload(ik, s));
+    CK(ctx->item_p0.upload(ip0, s));
+    CK(ctx->item_p1.upload(ip1, s));
+    ItemList items{ctx->item_knot.p, ctx->item_p0.p, ctx->item_p1.p, (int)ik.size(), ctx->knot_invN.p};
+    pdds_status st = enqueue_mixed_paths(ctx, desc, P, 1, ppc, launches, &items);
+    if (st != PDDS_OK) return st;
   }
   return PDDS_OK;
 }
@@ -362,6 +429,12 @@ pdds_status pdds_destroy(pdds_ctx* ctx) {
     ctx->b_relres.release();
     ctx->b_tend.release();
     ctx->rng_dev.release();
+    ctx->knot_N.release();
+    ctx->item_knot.release();
+    ctx->item_p0.release();
+    ctx->item_p1.release();
+    ctx->knot_scale.release();
+    ctx->knot_invN.release();
     if (ctx->rng_host) cudaFreeHost(ctx->rng_host);
     if (ctx->host_rr) cudaFreeHost(ctx->host_rr);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
@@ -490,6 +563,9 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
     return fail(ctx, PDDS_ERR_INVALID, "the replay mode follows the reference and has no Richardson form");
   if (mode == PDDS_MODE_REPLAY_FP64 && ctx->prob.kind == PDDS_MONEGROS)
     return fail(ctx, PDDS_ERR_INVALID, "the Monegros problem has no replay form");
+  if (desc->adaptive_n && mode != PDDS_MODE_MIXED)
+    return fail(ctx, PDDS_ERR_INVALID, "variance-adaptive paths (adaptive_n) run in PDDS_MODE_MIXED");
+  if (desc->adaptive_n && desc->target_stderr < 0.0) return fail(ctx, PDDS_ERR_INVALID, "target_stderr < 0");
   CK(cudaSetDevice(ctx->device));
   cudaStream_t s = ctx->stream;
   HostLayout& L = ctx->L;
@@ -607,6 +683,10 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
     if (mode == PDDS_MODE_MIXED) {
       pdds_status st = enqueue_mixed_paths(ctx, desc, P, chunks, ppc, &launches);
       if (st != PDDS_OK) return st;
+      if (desc->adaptive_n) {
+        st = adaptive_continue(ctx, desc, P, &launches);
+        if (st != PDDS_OK) return st;
+      }
     } else {
       Fp64Args a;
       a.L = ctx->dl;
@@ -642,12 +722,21 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
         launches++;
       }
     }
-    CK(launch_finalize(ctx->mc_knots.p, n_mc, N, ctx->Bsum.p, ctx->BBsum.p, ctx->B.p, ctx->BB.p,
-                       ctx->row_ptr.p, nnz, ctx->G.p, ctx->GG.p,
-                       (mode == PDDS_MODE_MIXED && desc->want_var) ? 1 : 0, s));
+    if (mode == PDDS_MODE_MIXED && desc->adaptive_n)
+      CK(launch_finalize_n(ctx->mc_knots.p, n_mc, ctx->knot_N.p, ctx->Bsum.p, ctx->BBsum.p, ctx->B.p, ctx->BB.p,
+                           nnz, ctx->G.p, ctx->GG.p, desc->want_var ? 1 : 0, s));
+    else
+      CK(launch_finalize(ctx->mc_knots.p, n_mc, N, ctx->Bsum.p, ctx->BBsum.p, ctx->B.p, ctx->BB.p,
+                         ctx->row_ptr.p, nnz, ctx->G.p, ctx->GG.p,
+                         (mode == PDDS_MODE_MIXED && desc->want_var) ? 1 : 0, s));
     launches += 1 + ((mode == PDDS_MODE_MIXED && desc->want_var) ? 1 : 0);
   }
   CK(cudaEventRecord(ctx->ev2, s));
+  if (!(mode == PDDS_MODE_MIXED && desc->adaptive_n)) {
+    ctx->last_knot_N.assign(L.K, 0);
+    for (int v = 0; v < L.K; v++)
+      if (!L.knot_boundary[v]) ctx->last_knot_N[v] = N;
+  }
   if (val && nnz) CK(cudaMemcpyAsync(val, ctx->G.p, nnz * sizeof(double), cudaMemcpyDeviceToHost, s));
   if (var && nnz) {
     if (mode == PDDS_MODE_FP64) std::fill(var, var + nnz, 0.0);
@@ -666,7 +755,13 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
     info->ms_setup = ms_setup;
     info->ms_paths = ms_paths;
     info->kernel_launches = launches;
-    info->paths = (int64_t)n_mc * N;
+    if (mode == PDDS_MODE_MIXED && desc->adaptive_n) {
+      int64_t tot = 0;
+      for (int v : ctx->last_knot_N) tot += v;
+      info->paths = tot;
+    } else {
+      info->paths = (int64_t)n_mc * N;
+    }
     if (mode != PDDS_MODE_REPLAY_FP64) {
       info->path_steps = (int64_t)st[0];
       info->exits_global = (int64_t)st[2];
@@ -674,6 +769,14 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
     }
   }
   return check_err_flags(ctx);
+}
+
+pdds_status pdds_estimate_knot_paths(pdds_ctx* ctx, int32_t* npaths) {
+  if (!ctx || !npaths) return PDDS_ERR_INVALID;
+  if (!ctx->has_estimate || ctx->last_knot_N.size() != (size_t)ctx->L.K)
+    return fail(ctx, PDDS_ERR_INVALID, "no estimate on this layout");
+  std::copy(ctx->last_knot_N.begin(), ctx->last_knot_N.end(), npaths);
+  return PDDS_OK;
 }
 
 pdds_status pdds_solve_interface(pdds_ctx* ctx, const pdds_solve_desc* desc, double* u,

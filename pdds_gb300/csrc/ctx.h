@@ -102,6 +102,10 @@ struct pdds_ctx {
   std::vector<unsigned char> graph_key;
   int graph_launches = 0;
   bool has_batch_run = false;
+  // variance-adaptive paths (pdds_estimate with adaptive_n)
+  DBuf<int> knot_N, item_knot, item_p0, item_p1;
+  DBuf<double> knot_scale, knot_invN;
+  std::vector<int> last_knot_N;  // paths per knot of the last estimate
   // {seed, instance} read by the path kernel of a batch sequence
   DBuf<unsigned long long> rng_dev;
   unsigned long long* rng_host = nullptr;  // pinned staging of rng_dev

@@ -54,6 +54,31 @@ __global__ void k_finalize_b(const int* mc, int n, int N, const double* Bsum, co
   BB[k] = BBsum[k] / N;
 }
 
+// Per-knot path counts (variance-adaptive N): B = b / N_k, BB = bb / N_k.
+__global__ void k_finalize_b_n(const int* mc, int n, const int* knot_N, const double* Bsum, const double* BBsum,
+                               double* B, double* BB) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int k = mc[t];
+  const double inv = 1.0 / (double)knot_N[k];
+  B[k] = Bsum[k] * inv;
+  BB[k] = BBsum[k] * inv;
+}
+
+// G and GG rows of the given knots scaled by scale[k] (one warp per knot):
+// the pilot's entries, normalised by its N, renormalised to the final N_k.
+__global__ void k_scale_rows(const int* mc, int n, const int64_t* row_ptr, const double* scale, double* G,
+                             double* GG) {
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (w >= n) return;
+  const int k = mc[w];
+  const double f = scale[k];
+  for (int64_t e = row_ptr[k] + lane; e < row_ptr[k + 1]; e += 32) {
+    G[e] *= f;
+    if (GG) GG[e] *= f;
+  }
+}
+
 __global__ void k_finalize_var(int64_t nnz, const double* G, double* GG) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= nnz) return;
@@ -83,6 +108,22 @@ cudaError_t launch_finalize(const int* mc_knots, int n_mc, int N, const double* 
                             cudaStream_t s) {
   (void)row_ptr;
   if (n_mc > 0) k_finalize_b<<<(n_mc + 127) / 128, 128, 0, s>>>(mc_knots, n_mc, N, Bsum, BBsum, B, BB);
+  if (want_var && nnz > 0)
+    k_finalize_var<<<(unsigned)((nnz + 255) / 256), 256, 0, s>>>(nnz, G, GG_to_var);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scale_rows(const int* mc, int n, const int64_t* row_ptr, const double* scale, double* G,
+                              double* GG, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_scale_rows<<<(n + 7) / 8, 256, 0, s>>>(mc, n, row_ptr, scale, G, GG);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_finalize_n(const int* mc_knots, int n_mc, const int* knot_N, const double* Bsum,
+                              const double* BBsum, double* B, double* BB, int64_t nnz, const double* G,
+                              double* GG_to_var, int want_var, cudaStream_t s) {
+  if (n_mc > 0) k_finalize_b_n<<<(n_mc + 127) / 128, 128, 0, s>>>(mc_knots, n_mc, knot_N, Bsum, BBsum, B, BB);
   if (want_var && nnz > 0)
     k_finalize_var<<<(unsigned)((nnz + 255) / 256), 256, 0, s>>>(nnz, G, GG_to_var);
   return cudaGetLastError();

@@ -88,7 +88,7 @@ k_paths_mixed(const MixedArgs a) {
   extern __shared__ float hist[];  // [sum nbins] (and the Y^2 histogram after it)
   __shared__ ItemSide s_side[4];
   __shared__ float s_rect[4];
-  __shared__ int s_item, s_knot, s_path_end, s_hist_len;
+  __shared__ int s_item, s_knot, s_p0, s_path_end, s_hist_len;
   __shared__ float s_h, s_sqrth;
   __shared__ unsigned s_next_path;
   __shared__ double s_red[MIXED_THREADS / 32][4];
@@ -103,11 +103,19 @@ k_paths_mixed(const MixedArgs a) {
     const int item = s_item;
     if (item >= a.n_items) break;
     if (tid == 0) {
-      const int k = a.mc_knots[item / a.chunks];
-      const int chunk = item % a.chunks;
+      int k, p0, p1;
+      if (a.item_knot) {
+        k = a.item_knot[item];
+        p0 = a.item_p0[item];
+        p1 = a.item_p1[item];
+      } else {
+        k = a.mc_knots[item / a.chunks];
+        p0 = (item % a.chunks) * a.paths_per_chunk;
+        p1 = min(a.N, p0 + a.paths_per_chunk);
+      }
       s_knot = k;
-      const int p0 = chunk * a.paths_per_chunk;
-      s_path_end = min(a.N, p0 + a.paths_per_chunk);
+      s_p0 = p0;
+      s_path_end = p1;
       s_next_path = (unsigned)(p0 + MIXED_THREADS);
       const int st = L.knot_stencil[k];
       for (int q = 0; q < 4; q++) s_rect[q] = (float)L.st_rect[4 * st + q];
@@ -180,8 +188,7 @@ k_paths_mixed(const MixedArgs a) {
     // bit d set when stencil side d lies on the global boundary
     const int globmask = (s_side[0].glob ? 1 : 0) | (s_side[1].glob ? 2 : 0) | (s_side[2].glob ? 4 : 0) |
                          (s_side[3].glob ? 8 : 0);
-    const int chunk = item % a.chunks;
-    unsigned path = (unsigned)(chunk * a.paths_per_chunk + tid);
+    unsigned path = (unsigned)(s_p0 + tid);
     bool active = (int)path < path_end;
     // per-lane B sums in compensated FP32 (Kahan), folded into FP64 per item:
     // the error is at most 2 eps_32 sum |v| over the lane's paths of the item
@@ -412,6 +419,7 @@ k_paths_mixed(const MixedArgs a) {
     }
     // ------------------------------------------------------------ contract G
     const int64_t row0 = L.row_ptr[knot];
+    const double invN = a.knot_invN ? a.knot_invN[knot] : a.inv_N;
     const int n_all = s_side[0].n + s_side[1].n + s_side[2].n + s_side[3].n;
     for (int pr = tid; pr < n_all; pr += MIXED_THREADS) {
       int d = 0, i = pr;
@@ -435,8 +443,8 @@ k_paths_mixed(const MixedArgs a) {
         acc2 += (double)part2;
       }
       const int64_t e = row0 + L.map_pos[m];
-      atomicAdd(a.G + e, -acc * a.inv_N);
-      if (a.want_var) atomicAdd(a.GG + e, acc2 * a.inv_N);
+      atomicAdd(a.G + e, -acc * invN);
+      if (a.want_var) atomicAdd(a.GG + e, acc2 * invN);
     }
     __syncthreads();
   }

@@ -38,6 +38,12 @@ struct MixedArgs {
   // optional {seed, instance} in device memory, read instead of seed and
   // instance (a replayed graph draws fresh numbers when the host updates it)
   const unsigned long long* rng_dev;
+  // optional explicit items (knot, paths [p0, p1)) instead of n_mc x chunks,
+  // and per-knot 1/N_k instead of inv_N (variance-adaptive paths)
+  const int* item_knot;
+  const int* item_p0;
+  const int* item_p1;
+  const double* knot_invN;
 };
 
 struct Fp64Args {
@@ -109,6 +115,12 @@ cudaError_t launch_rbf_setup(const DevLayout& L, int max_n, int max_nbins, doubl
 // B = g(x0) for boundary knots; finalisation of B, BB, G_var.
 cudaError_t launch_boundary_b(const DevLayout& L, const ProblemDev& P, int mode, const int* knots,
                               int n, double* B, double* BB, cudaStream_t s);
+// Variance-adaptive paths: rescale the pilot's G/GG rows, finalise with per-knot N.
+cudaError_t launch_scale_rows(const int* mc, int n, const int64_t* row_ptr, const double* scale, double* G,
+                              double* GG, cudaStream_t s);
+cudaError_t launch_finalize_n(const int* mc_knots, int n_mc, const int* knot_N, const double* Bsum,
+                              const double* BBsum, double* B, double* BB, int64_t nnz, const double* G,
+                              double* GG_to_var, int want_var, cudaStream_t s);
 cudaError_t launch_finalize(const int* mc_knots, int n_mc, int N, const double* Bsum,
                             const double* BBsum, double* B, double* BB, const int64_t* row_ptr,
                             int64_t nnz, const double* G, double* GG_to_var, int want_var,

@@ -1,0 +1,56 @@
+"""Variance-adaptive paths per knot (the reference's Compute_h_N rule,
+PDDSparseGM.cpp:4338-4395): N_k = 4 V_k / (0.66666 eps)^2 from a pilot,
+rounded up to the next multiple of 256 and clamped; the continuation runs
+paths N0 .. N_k-1 of the same Philox streams, so a knot's result equals a
+uniform run with N = N_k."""
+import numpy as np
+import pytest
+
+import pdds_gb300 as P
+from pdds_gb300.config import fac_rule
+
+pytestmark = pytest.mark.gpu
+
+SW, NE, NSUB, NNODE, H = (-1.0, -1.0), (1.0, 1.0), 4, 11, 1e-3
+N0, NMAX, EPS = 512, 16384, 0.01
+
+
+def expected_n(B, BB):
+    var = np.maximum(BB - B * B, 0.0)
+    n = (4.0 * var / (EPS * 0.66666) ** 2).astype(np.int64)
+    n = (1 + n // 256) * 256
+    return np.clip(n, N0, NMAX)
+
+
+def test_adaptive_paths_follow_the_rule_and_continue_streams():
+    fac = fac_rule(2.0, NSUB, NNODE)
+    bvp = P.BVP.poisson_sincos()
+    with P.PDDSparseGM(SW, NE, NSUB, NNODE, fac) as pd:
+        pilot = pd.estimate(bvp, N0, H, mode=P.MODE_MIXED, seed=9, adaptive_h=True)
+        ad = pd.estimate(bvp, N0, H, mode=P.MODE_MIXED, seed=9, adaptive_h=True, adaptive_n=True, npaths_max=NMAX,
+                         target_stderr=EPS)
+        mc = pilot.npaths > 0
+        assert np.all(ad.npaths[~mc] == 0)
+        nk = ad.npaths[mc]
+        assert np.all(nk % 256 == 0) and nk.min() >= N0 and nk.max() <= NMAX
+        assert len(np.unique(nk)) > 3, "the workload should spread N_k"
+        want = expected_n(pilot.B[mc], pilot.BB[mc])
+        # the pilot is recomputed: summation order may move a knot across a rounding edge
+        assert np.mean(nk == want) > 0.95 and np.max(np.abs(nk - want)) <= 256
+        assert ad.info["paths"] == int(ad.npaths.sum())
+        # a knot with N_k = M matches the uniform run with M paths (paths 0 .. M-1)
+        M = int(np.bincount(nk // 256).argmax() * 256)
+        uni = pd.estimate(bvp, M, H, mode=P.MODE_MIXED, seed=9, adaptive_h=True)
+        sel = np.where(mc)[0][nk == M]
+        assert len(sel) > 0
+        assert np.max(np.abs(ad.B[sel] - uni.B[sel])) < 1e-9
+        for k in sel[:20]:
+            a, b = pd.row_ptr[k], pd.row_ptr[k + 1]
+            assert np.max(np.abs(ad.val[a:b] - uni.val[a:b])) < 1e-5  # FP32 histograms, other chunking
+        # standard error of B at or below the target where N_k is not clamped
+        free = (nk > N0) & (nk < NMAX)
+        var = np.maximum(ad.BB[mc] - ad.B[mc] ** 2, 0.0)
+        se = np.sqrt(var[free] / nk[free])
+        assert np.quantile(se, 0.95) < 0.5 * EPS
+        u, _ = pd.solve_interface()
+        assert np.sqrt(np.mean((u - bvp.u(pd.x, pd.y)) ** 2)) < 3e-2
