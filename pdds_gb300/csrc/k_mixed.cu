@@ -3,9 +3,12 @@
 // One persistent CTA per slot processes work items (knot, chunk of paths).
 // Lanes step paths in FP32 with Philox-4x32-10 normals held in registers and
 // refill from the item's path counter the moment their path exits, so a warp
-// keeps stepping while path lengths vary.  An exit on an interior stencil side
-// deposits Y with cubic Lagrange weights into a per-side histogram of the exit
-// coordinate in shared memory (4 FP32 atomics, O(1) per exit).  At the end of
+// keeps stepping while path lengths vary.  A level that exits pushes its final
+// state to a per-warp queue in shared memory; the warp processes the queue 32
+// exits at a time, one per lane, so exit handling runs at full width.  An exit
+// on an interior stencil side deposits Y with cubic Lagrange weights into a
+// per-side histogram of the exit coordinate in shared memory (4 FP32 atomics,
+// O(1) per exit).  At the end of
 // the item the histograms are contracted with the FP32 table of cardinal
 // functions H_i(s) = sum_j Psi^-1(j,i) exp(-(t_j - s)^2 / c^2), computed in
 // FP64 from the factorised RBF matrix, and added into the G row in FP64.
@@ -49,14 +52,14 @@ struct Lvl<PK_LUT> {
   float cf[8];
 };
 
-// A pending exit deposit: histogram index of the first of the 4 cubic
-// nodes, offset in the bin, and the signed weight * Y.
-struct QEntry {
-  int idx;
-  float fu;
-  float yw;
-};
-constexpr int QCAP = 96;  // <= 31 left over + 2 deposits x 32 lanes
+// Exit queue of a warp: a level that leaves its stencil pushes (x, y, Y,
+// Z + xi, meta) and the warp processes 32 exits at a time, one per lane.
+// meta = owner lane | level << 5 | pair slot << 6 | step-limit << 8.
+// <= 31 left over + one push of 32 (the queue drains between the pushes).
+constexpr int XQCAP = 64;
+// Pair slots per lane: a Richardson pair's two exits meet in the slot of
+// its owner lane (halves outstanding, first half's weighted value).
+constexpr int NSLOT = 4;
 
 // Kahan step: s + c tracks the exact sum to O(eps^2); c holds the negated
 // rounding error of the running sum.
@@ -93,7 +96,11 @@ k_paths_mixed(const MixedArgs a) {
   __shared__ unsigned s_next_path;
   __shared__ double s_red[MIXED_THREADS / 32][4];
   __shared__ unsigned long long s_redi[MIXED_THREADS / 32][3];
-  __shared__ QEntry s_queue[MIXED_THREADS / 32][QCAP];
+  __shared__ float s_qx[MIXED_THREADS / 32][XQCAP], s_qy[MIXED_THREADS / 32][XQCAP];
+  __shared__ float s_qY[MIXED_THREADS / 32][XQCAP], s_qS[MIXED_THREADS / 32][XQCAP];
+  __shared__ unsigned s_qm[MIXED_THREADS / 32][XQCAP];
+  __shared__ float s_pv[MIXED_THREADS / 32][NSLOT][32];
+  __shared__ int s_pst[MIXED_THREADS / 32][NSLOT][32];
   const DevLayout& L = a.L;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
@@ -195,23 +202,16 @@ k_paths_mixed(const MixedArgs a) {
     float bs = 0.f, bc = 0.f, bbs = 0.f, bbc = 0.f;
     unsigned long long nsteps = 0;
     unsigned nglob = 0, nsten = 0;  // exits of the lane in this item (<= 2 N)
-    QEntry* q = s_queue[warp];
     int qcount = 0;  // warp-uniform
     const unsigned lt = (1u << lane) - 1u;
+    float* qx = s_qx[warp];
+    float* qy = s_qy[warp];
+    float* qY = s_qY[warp];
+    float* qS = s_qS[warp];
+    unsigned* qm = s_qm[warp];
+    for (int q = 0; q < NSLOT; q++) s_pst[warp][q][lane] = 0;
+    const int halves = RICH ? 2 : 1;
 
-    auto apply = [&](const QEntry& e) {
-      float w[4];
-      cubic_weights(e.fu, w[0], w[1], w[2], w[3]);
-      float* hp = hist + e.idx;
-#pragma unroll
-      for (int r = 0; r < 4; r++) atomicAdd(hp + r, e.yw * w[r]);
-      if (a.want_var) {
-        float* hq = hist2 + e.idx;
-        const float y2 = e.yw * e.yw;
-#pragma unroll
-        for (int r = 0; r < 4; r++) atomicAdd(hq + r, y2 * w[r]);
-      }
-    };
     // One step of a level (Step, control-variate variant,
     // FKACIntegrator.hpp:46-57) and the Gobet-shifted exit test (Inside,
     // :168-222), branch-free: with dx = |x - cx| - hx, dy = |y - cy| - hy the
@@ -248,52 +248,114 @@ k_paths_mixed(const MixedArgs a) {
       const float thr = -0.5826f * sq * (dx > dy ? nx : ny);
       return !(fmaxf(dx, dy) < thr) || s.steps >= (unsigned)a.max_steps;
     };
-    // Exit of a level: B value and, on an interior side, the deposit.
+    // Push the exits of one level (warp-synchronous) and drain 32 if full.
+    auto push = [&](bool ex, const Lvl<KIND>& s, unsigned meta) {
+      const unsigned mk = __ballot_sync(FULL, ex);
+      if (ex) {
+        const int i = qcount + __popc(mk & lt);
+        qx[i] = s.x;
+        qy[i] = s.y;
+        qY[i] = s.Y;
+        qS[i] = s.Z + s.xi;
+        qm[i] = meta | (s.steps >= (unsigned)a.max_steps ? 256u : 0u);
+      }
+      qcount += __popc(mk);
+    };
+    // Process the exit at queue index i (lane-parallel): projection onto the
+    // stencil rectangle, value of the score, deposit on an interior side, and
+    // the pair's B contribution once both of its exits are processed.
     // Projection (Rectangle2D, rectangle.hpp:7-229) as selects: the x side is
     // taken exactly when dx > dy, the other coordinate is clamped to the
     // rectangle (the identity inside, the corner outside both slabs), and the
     // sides the projection lies on are read off by equality, first match in
     // the order S, N, W, E as in G_update (stencil.cpp:246-301).
-    auto on_exit = [&](const Lvl<KIND>& s, float wgt, float& val, bool& dep, QEntry& de) {
-      if (s.steps >= (unsigned)a.max_steps) {
-        float Ex, Ey, Nx, Ny;
-        int om;
-        const float dist = rect2d<float>(rect, s.x, s.y, Ex, Ey, Nx, Ny, om);
-        float g00, g01, g10, g11;
-        sigma_f32<KIND>(P, s.x, s.y, g00, g01, g10, g11);
-        const float w0 = Nx * g00 + Ny * g10, w1 = Nx * g01 + Ny * g11;
-        if (dist < -0.5826f * sqrtf(w0 * w0 + w1 * w1) * (wgt < 0.f ? sqrth : (RICH ? sqrth * 0.70710678f : sqrth))) {
-          atomicOr(a.err_flags, ERR_FLAG_STEP_LIMIT);
-          val = 0.f;
-          return;
+    auto process = [&](int i, bool valid) {
+      float wv = 0.f;
+      int old = 0, slot = 0, owner = 0;
+      if (valid) {
+        const float x = qx[i], y = qy[i], Y = qY[i];
+        const unsigned meta = qm[i];
+        owner = (int)(meta & 31u);
+        const int lvl = (int)((meta >> 5) & 1u);
+        slot = (int)((meta >> 6) & 3u);
+        const float wgt = RICH ? (lvl ? -1.f : 2.f) : 1.f;
+        float val = qS[i];
+        bool ok = true;
+        if (meta & 256u) {  // step limit reached: an error unless the path had exited anyway
+          float Ex, Ey, Nx, Ny;
+          int om;
+          const float dist = rect2d<float>(rect, x, y, Ex, Ey, Nx, Ny, om);
+          float g00, g01, g10, g11;
+          sigma_f32<KIND>(P, x, y, g00, g01, g10, g11);
+          const float w0 = Nx * g00 + Ny * g10, w1 = Nx * g01 + Ny * g11;
+          if (dist < -0.5826f * sqrtf(w0 * w0 + w1 * w1) * ((RICH && lvl == 0) ? sqrth * 0.70710678f : sqrth)) {
+            atomicOr(a.err_flags, ERR_FLAG_STEP_LIMIT);
+            ok = false;
+            val = 0.f;
+          }
         }
+        if (ok) {
+          const float dx = fabsf(x - cx) - hx, dy = fabsf(y - cy) - hy;
+          const bool xs = dx > dy;
+          const float Ex = xs ? (x > cx ? rect[2] : rect[0]) : fminf(fmaxf(x, rect[0]), rect[2]);
+          const float Ey = xs ? fminf(fmaxf(y, rect[1]), rect[3]) : (y > cy ? rect[3] : rect[1]);
+          const bool onS = Ey == rect[1], onN = Ey == rect[3], onW = Ex == rect[0], onE = Ex == rect[2];
+          const int onmask = (onN ? 1 : 0) | (onS ? 2 : 0) | (onE ? 4 : 0) | (onW ? 8 : 0);
+          if (onmask & globmask) {
+            ++nglob;
+            val += Y * u_f32<KIND>(P, Ex, Ey);
+          } else {
+            ++nsten;
+            const int d = onS ? 1 : (onN ? 0 : (onW ? 3 : 2));
+            const ItemSide& is = s_side[d];
+            if (is.n > 0) {
+              const float sc = is.orient == 0 ? Ex : Ey;
+              const float uu = (sc - is.base) * is.inv_delta;
+              int b0 = (int)floorf(uu);
+              b0 = max(1, min(b0, is.nbins - 3));
+              float w[4];
+              cubic_weights(uu - (float)b0, w[0], w[1], w[2], w[3]);
+              const float yw = wgt * Y;
+              float* hp = hist + is.hist_off + b0 - 1;
+#pragma unroll
+              for (int r = 0; r < 4; r++) atomicAdd(hp + r, yw * w[r]);
+              if (a.want_var) {
+                float* hq = hist2 + is.hist_off + b0 - 1;
+                const float y2 = yw * yw;
+#pragma unroll
+                for (int r = 0; r < 4; r++) atomicAdd(hq + r, y2 * w[r]);
+              }
+            }
+          }
+        }
+        wv = wgt * val;
+        old = atomicSub(&s_pst[warp][slot][owner], 1);
+        if (RICH && old == 2) s_pv[warp][slot][owner] = wv;
       }
-      const float dx = fabsf(s.x - cx) - hx, dy = fabsf(s.y - cy) - hy;
-      const bool xs = dx > dy;
-      const float Ex = xs ? (s.x > cx ? rect[2] : rect[0]) : fminf(fmaxf(s.x, rect[0]), rect[2]);
-      const float Ey = xs ? fminf(fmaxf(s.y, rect[1]), rect[3]) : (s.y > cy ? rect[3] : rect[1]);
-      const bool onS = Ey == rect[1], onN = Ey == rect[3], onW = Ex == rect[0], onE = Ex == rect[2];
-      const int onmask = (onN ? 1 : 0) | (onS ? 2 : 0) | (onE ? 4 : 0) | (onW ? 8 : 0);
-      if (onmask & globmask) {
-        ++nglob;
-        val = s.Z + s.Y * u_f32<KIND>(P, Ex, Ey) + s.xi;
-        return;
-      }
-      ++nsten;
-      val = s.Z + s.xi;
-      const int d = onS ? 1 : (onN ? 0 : (onW ? 3 : 2));
-      const ItemSide& is = s_side[d];
-      if (is.n > 0) {
-        const float sc = is.orient == 0 ? Ex : Ey;
-        const float u = (sc - is.base) * is.inv_delta;
-        int b0 = (int)floorf(u);
-        b0 = max(1, min(b0, is.nbins - 3));
-        de.idx = is.hist_off + b0 - 1;
-        de.fu = u - (float)b0;
-        de.yw = wgt * s.Y;
-        dep = true;
+      __syncwarp();
+      if (valid && old == 1) {
+        const float v = RICH ? wv + s_pv[warp][slot][owner] : wv;
+        kahan_add(bs, bc, v);
+        kahan_add(bbs, bbc, v * v);
       }
     };
+    auto drain_full = [&]() {
+      __syncwarp();
+      while (qcount >= 32) {
+        process(qcount - 32 + lane, true);
+        __syncwarp();
+        qcount -= 32;
+      }
+    };
+    auto drain_all = [&]() {
+      drain_full();
+      if (qcount > 0) {
+        process(lane, lane < qcount);
+        __syncwarp();
+        qcount = 0;
+      }
+    };
+
     Lvl<KIND> F, Cs;
     float cf0[8];  // table fields at the knot (PK_LUT)
     if constexpr (KIND == PK_LUT) lut_sample<float, 8>(P.lut, x0, y0, cf0);
@@ -306,12 +368,12 @@ k_paths_mixed(const MixedArgs a) {
       Cs = F;
     };
     reset();
+    int gen = 0;  // pair slot of the lane's current pair
+    __syncwarp();
+    if (active) s_pst[warp][0][lane] = halves;
     bool f_alive = active, c_alive = RICH && active;
-    float val_f = 0.f, val_c = 0.f;
     unsigned m = 0;
     while (__any_sync(FULL, active)) {
-      bool dep0 = false, dep1 = false;
-      QEntry e0, e1;
       bool fx = false, cx_ = false;  // exits in this iteration
       if (active) {
         const u32x4 blk = path_block(seed, rng_inst, rng_knot, path, m++);
@@ -331,40 +393,20 @@ k_paths_mixed(const MixedArgs a) {
           if (!fx) fx = advance(F, sqrth * zb0, sqrth * zb1, h, sqrth);
         }
       }
-      if (fx) {
-        on_exit(F, RICH ? 2.f : 1.f, val_f, dep0, e0);
-        f_alive = false;
-      }
-      if (RICH && cx_) {
-        on_exit(Cs, -1.f, val_c, dep1, e1);
-        c_alive = false;
-      }
-      // deposit queue (warp-synchronous)
-      {
-        const unsigned mk = __ballot_sync(FULL, dep0);
-        if (dep0) q[qcount + __popc(mk & lt)] = e0;
-        qcount += __popc(mk);
-      }
+      const unsigned meta0 = (unsigned)lane | ((unsigned)gen << 6);
+      push(fx, F, meta0);
+      drain_full();
       if (RICH) {
-        const unsigned mk = __ballot_sync(FULL, dep1);
-        if (dep1) q[qcount + __popc(mk & lt)] = e1;
-        qcount += __popc(mk);
+        push(cx_, Cs, meta0 | 32u);
+        drain_full();
       }
-      __syncwarp();
-      while (qcount >= 32) {
-        const QEntry e = q[qcount - 32 + lane];
-        __syncwarp();
-        apply(e);
-        qcount -= 32;
-      }
-      // finished pairs: B and refill
+      f_alive = f_alive && !fx;
+      c_alive = c_alive && !cx_;
+      // finished pairs: steps, and refill into the next pair slot
       const bool done = active && !f_alive && !c_alive;
-      if (done) {
-        const float v = RICH ? 2.f * val_f - val_c : val_f;
-        kahan_add(bs, bc, v);
-        kahan_add(bbs, bbc, v * v);
-        nsteps += F.steps + (RICH ? Cs.steps : 0u);
-      }
+      if (done) nsteps += F.steps + (RICH ? Cs.steps : 0u);
+      const int ngen = (gen + 1) & (NSLOT - 1);
+      if (__any_sync(FULL, done && s_pst[warp][ngen][lane] != 0)) drain_all();
       const unsigned dm = __ballot_sync(FULL, done);
       if (dm) {
         const int leader = __ffs(dm) - 1;
@@ -377,15 +419,17 @@ k_paths_mixed(const MixedArgs a) {
             active = false;
           } else {
             reset();
+            gen = ngen;
+            s_pst[warp][gen][lane] = halves;
             f_alive = true;
             c_alive = RICH;
             m = 0;
           }
         }
       }
+      __syncwarp();
     }
-    __syncwarp();
-    if (lane < qcount) apply(q[lane]);
+    drain_all();
     // ------------------------------------------------------------ reduce B
     double b = (double)bs - (double)bc, bb = (double)bbs - (double)bbc;
 #pragma unroll
