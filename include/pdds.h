@@ -60,7 +60,8 @@ typedef enum {
   PDDS_HELMHOLTZ = 2,      /* u = sin(a x)cos(b y); p = {a, b, c}, c <= 0               */
   PDDS_VARCOEF = 3,        /* sigma = diag(1+x^2/2, 1+y^2/2), b = (y,-x),
                               c = -(1+x^2+y^2), u = e^x cos 2y + 1                      */
-  PDDS_LUT = 4             /* diagonal sigma, b, c, f, grad u and g served from tables  */
+  PDDS_LUT = 4,            /* diagonal sigma, b, c, f, grad u and g served from tables  */
+  PDDS_CIRCLE_POISSON = 5  /* u = r^2 sin(3 theta) + cos x, sigma = sqrt2 I, f = -Lap u  */
 } pdds_problem_kind;
 
 typedef struct {
@@ -104,6 +105,27 @@ typedef struct {
 } pdds_layout_info;
 
 pdds_status pdds_layout_build(pdds_ctx* ctx, const pdds_layout_desc* desc, pdds_layout_info* info);
+
+/* Disk of the given radius centred at the origin, split into nrings x
+ * nsectors annular sectors (a CircleMesh; the reference's Circle* meshes are
+ * empty stubs, its layouts are rectangular).  Knots on the arcs between
+ * rings and the rays between sectors, nnode per segment, none at the centre;
+ * stencils are the polar rectangles of the subdomains next to a knot's
+ * interfaces, sides elongated by half a segment as on rectangles; the RBF
+ * shape of a side is kappa[kind] times its knot spacing (chord).  MIXED and
+ * FP64 modes (no replay form); problems with sigma = sqrt2 I (PDDS_POISSON_SINCOS,
+ * PDDS_CIRCLE_POISSON).  pdds_layout_stencil reports rect = {rho0, phi0,
+ * rho1, phi1} with sides N = outer arc, S = inner arc, E = ray at phi1,
+ * W = ray at phi0. */
+typedef struct {
+  double radius;
+  int32_t nrings;
+  int32_t nsectors;
+  int32_t nnode;
+  double kappa[4];
+} pdds_circle_desc;
+
+pdds_status pdds_layout_build_circle(pdds_ctx* ctx, const pdds_circle_desc* desc, pdds_layout_info* info);
 /* Knot i's position (the one the reference hands to its worker) and the
  * hand-out order of the reference's server loop. */
 pdds_status pdds_layout_knots(pdds_ctx* ctx, double* x, double* y, int32_t* order);
@@ -177,6 +199,32 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
                           double* B, double* BB, pdds_estimate_info* info);
 /* Paths per knot of the last pdds_estimate (npaths[K]; 0 for boundary knots). */
 pdds_status pdds_estimate_knot_paths(pdds_ctx* ctx, int32_t* npaths);
+/* Euler-Maruyama steps per knot of the last MIXED pdds_estimate, summed
+ * over its paths (both levels of a Richardson pair): steps[K]. */
+pdds_status pdds_estimate_knot_steps(pdds_ctx* ctx, int64_t* steps);
+
+/* Autotuner of the MIXED path kernel (no counterpart in the reference):
+ * times the kernel on a sample of knots of the current layout and problem
+ * for candidate launch shapes -- persistent CTAs per SM (1 .. the occupancy
+ * limit) and paths per work item (256 .. npaths) -- and keeps the fastest
+ * for later pdds_estimate calls with the same problem kind and Richardson
+ * setting.  Lanes refill from the work item's path counter the moment their
+ * path exits (a refill threshold of one lane), so the refill needs no knob.
+ * sample_knots <= 0 times the whole layout; a smaller sample runs on a grid
+ * scaled by the sampled fraction of knots, so each CTA sees as many work
+ * items as in the full run.  Overwrites the device results of the last
+ * estimate. */
+typedef struct {
+  int32_t blocks_per_sm;     /* chosen persistent CTAs per SM            */
+  int32_t paths_per_item;    /* chosen paths per work item (knot, chunk) */
+  int32_t candidates;        /* launch shapes timed                      */
+  int32_t sample_knots;      /* knots in the timing sample               */
+  double best_ms;            /* sample time with the chosen shape        */
+  double default_ms;         /* sample time with the default shape       */
+} pdds_tune_info;
+
+pdds_status pdds_autotune(pdds_ctx* ctx, const pdds_estimate_desc* desc, int32_t sample_knots,
+                          pdds_tune_info* info);
 
 /* ---------------------------------------------------------------- solve */
 typedef enum {

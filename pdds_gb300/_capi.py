@@ -18,14 +18,14 @@ STATUS_NAMES = {0: "PDDS_OK", 1: "PDDS_ERR_INVALID", 2: "PDDS_ERR_CUDA", 3: "PDD
                 4: "PDDS_ERR_TIMEOUT", 5: "PDDS_ERR_ILL_CONDITIONED", 6: "PDDS_ERR_NOT_CONVERGED",
                 7: "PDDS_ERR_NO_MEMORY", 8: "PDDS_ERR_EXIT_SIDE"}
 
-POISSON_SINCOS, MONEGROS, HELMHOLTZ, VARCOEF, LUT = 0, 1, 2, 3, 4
+POISSON_SINCOS, MONEGROS, HELMHOLTZ, VARCOEF, LUT, CIRCLE_POISSON = 0, 1, 2, 3, 4, 5
 MODE_REPLAY_FP64, MODE_FP64, MODE_MIXED = 0, 1, 2
 SOLVE_BICGSTAB_FP64, SOLVE_GMRES_FP32_IR = 0, 1
 
 EXPORTS = [
     "pdds_create", "pdds_destroy", "pdds_last_error", "pdds_version", "pdds_problem_set", "pdds_problem_set_lut",
-    "pdds_layout_build", "pdds_layout_knots", "pdds_layout_csr", "pdds_layout_stencil",
-    "pdds_estimate", "pdds_estimate_knot_paths", "pdds_solve_interface", "pdds_batch_build", "pdds_batch_run", "pdds_batch_instance",
+    "pdds_layout_build", "pdds_layout_build_circle", "pdds_layout_knots", "pdds_layout_csr", "pdds_layout_stencil",
+    "pdds_estimate", "pdds_estimate_knot_paths", "pdds_estimate_knot_steps", "pdds_autotune", "pdds_solve_interface", "pdds_batch_build", "pdds_batch_run", "pdds_batch_instance",
     "pdds_solve_bicgstab_static",
 ]
 STATIC_SOLVE_MAX_K = 131072
@@ -38,6 +38,11 @@ class ProblemDesc(C.Structure):
 class LayoutDesc(C.Structure):
     _fields_ = [("sw", C.c_double * 2), ("ne", C.c_double * 2), ("nsub", C.c_int32),
                 ("nnode", C.c_int32), ("fac", C.c_double * 4)]
+
+
+class CircleDesc(C.Structure):
+    _fields_ = [("radius", C.c_double), ("nrings", C.c_int32), ("nsectors", C.c_int32), ("nnode", C.c_int32),
+                ("kappa", C.c_double * 4)]
 
 
 class LayoutInfo(C.Structure):
@@ -59,6 +64,11 @@ class EstimateInfo(C.Structure):
     _fields_ = [("path_steps", C.c_int64), ("paths", C.c_int64), ("exits_global", C.c_int64),
                 ("exits_stencil", C.c_int64), ("ms_setup", C.c_double), ("ms_paths", C.c_double),
                 ("kernel_launches", C.c_int32)]
+
+
+class TuneInfo(C.Structure):
+    _fields_ = [("blocks_per_sm", C.c_int32), ("paths_per_item", C.c_int32), ("candidates", C.c_int32),
+                ("sample_knots", C.c_int32), ("best_ms", C.c_double), ("default_ms", C.c_double)]
 
 
 class SolveDesc(C.Structure):
@@ -114,11 +124,14 @@ def load(path: str = LIB_PATH):
     L.pdds_problem_set_lut.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int32, C.c_int32,
                                        C.POINTER(C.c_double)]
     L.pdds_layout_build.argtypes = [vp, C.POINTER(LayoutDesc), C.POINTER(LayoutInfo)]
+    L.pdds_layout_build_circle.argtypes = [vp, C.POINTER(CircleDesc), C.POINTER(LayoutInfo)]
     L.pdds_layout_knots.argtypes = [vp, dp, dp, C.POINTER(C.c_int32)]
     L.pdds_layout_csr.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int32)]
     L.pdds_layout_stencil.argtypes = [vp, C.c_int32, dp, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                       C.POINTER(C.c_int32), C.c_int32]
     L.pdds_estimate.argtypes = [vp, C.POINTER(EstimateDesc), dp, dp, dp, dp, C.POINTER(EstimateInfo)]
+    L.pdds_autotune.argtypes = [vp, C.POINTER(EstimateDesc), C.c_int32, C.POINTER(TuneInfo)]
+    L.pdds_estimate_knot_steps.argtypes = [vp, C.POINTER(C.c_int64)]
     L.pdds_estimate_knot_paths.argtypes = [vp, C.POINTER(C.c_int32)]
     L.pdds_solve_interface.argtypes = [vp, C.POINTER(SolveDesc), dp, C.POINTER(SolveInfo)]
     L.pdds_batch_build.argtypes = [vp, C.POINTER(InstanceDesc), C.c_int32, C.POINTER(BatchInfo)]

@@ -34,6 +34,7 @@ class BVP:
     HELMHOLTZ = capi.HELMHOLTZ
     VARCOEF = capi.VARCOEF
     LUT = capi.LUT
+    CIRCLE_POISSON = capi.CIRCLE_POISSON
 
     def __init__(self, kind: int, params=(), use_cv: bool = True, tables=None, exact=None):
         self.kind = int(kind)
@@ -46,6 +47,11 @@ class BVP:
     def poisson_sincos(cls):
         """Lap u = f on the domain with u = sin(pi x)cos(pi y) + x y (sigma = sqrt2 I)."""
         return cls(cls.POISSON_SINCOS)
+
+    @classmethod
+    def circle_poisson(cls):
+        """Lap u = f on the unit disk with u = r^2 sin(3 theta) + cos x (sigma = sqrt2 I)."""
+        return cls(cls.CIRCLE_POISSON)
 
     @classmethod
     def monegros(cls):
@@ -97,6 +103,9 @@ class BVP:
             return np.sin(self.params[0] * x) * np.cos(self.params[1] * y)
         if self.kind == self.VARCOEF:
             return np.exp(x) * np.cos(2 * y) + 1.0
+        if self.kind == self.CIRCLE_POISSON:
+            r = np.hypot(x, y)
+            return r * r * np.sin(3.0 * np.arctan2(y, x)) + np.cos(x)
         q = 1.0 + 0.01 * x * x + 0.02 * y * y
         return 3.0 + 0.333 * (np.sin(np.sqrt(q)) +
                               np.tanh(np.sin(0.12 * x + 0.05 * y) + np.sin(0.05 * x - 0.12 * y)))
@@ -169,22 +178,32 @@ class PDDSparseGM:
     (the reference's c2[kind], Meshes/stencil.cpp:211-243)."""
 
     def __init__(self, sw=(-1.0, -1.0), ne=(1.0, 1.0), nsub: int = 4, nnode: int = 11,
-                 fac=(1.0, 1.0, 1.0, 1.0), device: int = 0):
+                 fac=(1.0, 1.0, 1.0, 1.0), device: int = 0, circle=None):
         self._lib = capi.load()
         self._ctx = C.c_void_p()
         st = self._lib.pdds_create(C.byref(self._ctx), int(device), 0)
         if st != capi.OK:
             raise PDDSError(st, "pdds_create failed (device %d)" % device)
         self.device = device
-        d = capi.LayoutDesc()
-        d.sw[0], d.sw[1] = float(sw[0]), float(sw[1])
-        d.ne[0], d.ne[1] = float(ne[0]), float(ne[1])
-        d.nsub = int(nsub)
-        d.nnode = int(nnode)
-        for i in range(4):
-            d.fac[i] = float(fac[i])
         info = capi.LayoutInfo()
-        self._check(self._lib.pdds_layout_build(self._ctx, C.byref(d), C.byref(info)))
+        if circle is not None:
+            radius, nrings, nsectors, kappa = circle
+            d = capi.CircleDesc()
+            d.radius, d.nrings, d.nsectors, d.nnode = float(radius), int(nrings), int(nsectors), int(nnode)
+            for i in range(4):
+                d.kappa[i] = float(kappa[i])
+            self._check(self._lib.pdds_layout_build_circle(self._ctx, C.byref(d), C.byref(info)))
+            sw, ne, nsub, fac = (-radius, -radius), (radius, radius), nrings, tuple(kappa)
+        else:
+            d = capi.LayoutDesc()
+            d.sw[0], d.sw[1] = float(sw[0]), float(sw[1])
+            d.ne[0], d.ne[1] = float(ne[0]), float(ne[1])
+            d.nsub = int(nsub)
+            d.nnode = int(nnode)
+            for i in range(4):
+                d.fac[i] = float(fac[i])
+            self._check(self._lib.pdds_layout_build(self._ctx, C.byref(d), C.byref(info)))
+        self.circle = circle
         self.sw, self.ne, self.nsub, self.nnode, self.fac = tuple(sw), tuple(ne), nsub, nnode, tuple(fac)
         self.layout_info = {f: getattr(info, f) for f, _ in capi.LayoutInfo._fields_}
         K = info.nknots
@@ -200,6 +219,14 @@ class PDDSparseGM:
                                               _p(self.col, C.c_int32)))
         self.col = self.col[:info.nnz]
         self.nnz = int(info.nnz)
+
+    @classmethod
+    def circle_mesh(cls, radius: float = 1.0, nrings: int = 6, nsectors: int = 16, nnode: int = 11,
+                    kappa=(3.164, 3.164, 3.164, 3.164), device: int = 0):
+        """Disk of the given radius split into nrings x nsectors annular
+        sectors (MIXED mode, sigma = sqrt2 I problems); kappa[kind] scales
+        the RBF shape to each side's knot spacing."""
+        return cls(nnode=nnode, device=device, circle=(radius, nrings, nsectors, kappa))
 
     @classmethod
     def from_configuration(cls, path: str, device: int = 0):
@@ -291,6 +318,37 @@ class PDDSparseGM:
         self._check(self._lib.pdds_estimate_knot_paths(self._ctx, _p(kn, C.c_int32)))
         return Estimate(self.row_ptr, self.col, val[:self.nnz], var[:self.nnz], B, BB,
                         {f: getattr(info, f) for f, _ in capi.EstimateInfo._fields_}, kn)
+
+    def autotune(self, bvp: BVP, npaths: int, h: float, sample_knots: int = 0, seed: int = 1234,
+                 adaptive_h: bool = False, richardson: bool = False, want_var: bool = False) -> dict:
+        """Times the MIXED path kernel's launch shapes on a sample of knots and
+        keeps the fastest for later estimates of this problem kind."""
+        self._check(self._lib.pdds_problem_set(self._ctx, C.byref(bvp.desc())))
+        d = capi.EstimateDesc()
+        d.mode = capi.MODE_MIXED
+        d.npaths = int(npaths)
+        d.h = float(h)
+        d.seed = int(seed)
+        d.adaptive_h = int(bool(adaptive_h))
+        d.richardson = int(bool(richardson))
+        d.want_var = int(bool(want_var))
+        info = capi.TuneInfo()
+        self._check(self._lib.pdds_autotune(self._ctx, C.byref(d), int(sample_knots), C.byref(info)))
+        return {f: getattr(info, f) for f, _ in capi.TuneInfo._fields_}
+
+    def knot_steps(self):
+        """Path steps per knot of the last MIXED estimate (both Richardson levels)."""
+        st = np.zeros(self.K, np.int64)
+        self._check(self._lib.pdds_estimate_knot_steps(self._ctx, _p(st, C.c_int64)))
+        return st
+
+    def write_outputs(self, directory: str, est: "Estimate", u, bvp: BVP):
+        """Writes Output/solution.csv and Output/Debug/{G,G_var,B,B_var}.csv
+        under directory in the reference's format (Compute_Solution,
+        PDDSparseGM.cpp:3176-3244)."""
+        from .output_files import write_outputs
+        write_outputs(directory, self.x, self.y, self.row_ptr, self.col, est.val, est.var, est.B, est.BB, u,
+                      bvp.u(self.x, self.y))
 
     def solve_interface(self, method: int = capi.SOLVE_GMRES_FP32_IR, tol: float = 1e-10,
                         restart: int = 30, max_iter: int = 0, max_refine: int = 0):

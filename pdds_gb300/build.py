@@ -32,6 +32,7 @@ UNITS = {
     "k_gmres_cluster.cu": [],
     "batch.cu": [],
     "layout.cpp": ["-x", "cu"],
+    "layout_circle.cpp": ["-x", "cu"],
     "noalloc.cu": [],
 }
 

@@ -60,7 +60,7 @@ pdds_status upload_layout(pdds_ctx* ctx) {
     sd_knot_off.push_back(sd.knot_off);
   }
   std::vector<int> sh_n, sh_nbins;
-  std::vector<double> sh_c, sh_lo, sh_delta, sh_t;
+  std::vector<double> sh_c, sh_lo, sh_delta, sh_t, sh_R;
   std::vector<int64_t> sh_tab_off, sh_ipsi_off, sh_t_off;
   int64_t ipsi_len = 0, tab_len = 0;
   int max_n = 0;
@@ -69,6 +69,7 @@ pdds_status upload_layout(pdds_ctx* ctx) {
     sh_n.push_back(sh.n);
     sh_nbins.push_back(sh.nbins);
     sh_c.push_back(sh.c);
+    sh_R.push_back(sh.R);
     sh_lo.push_back(sh.lo);
     sh_delta.push_back(sh.delta);
     sh_tab_off.push_back(sh.tab_off);
@@ -124,6 +125,7 @@ pdds_status upload_layout(pdds_ctx* ctx) {
   CK(ctx->sh_n.upload(sh_n, s));
   CK(ctx->sh_nbins.upload(sh_nbins, s));
   CK(ctx->sh_c.upload(sh_c, s));
+  CK(ctx->sh_R.upload(sh_R, s));
   CK(ctx->sh_lo.upload(sh_lo, s));
   CK(ctx->sh_delta.upload(sh_delta, s));
   CK(ctx->sh_tab_off.upload(sh_tab_off, s));
@@ -141,12 +143,16 @@ pdds_status upload_layout(pdds_ctx* ctx) {
   CK(ctx->BB.resize(std::max(L.K, 1)));
   CK(ctx->Bsum.resize(std::max(L.K, 1)));
   CK(ctx->BBsum.resize(std::max(L.K, 1)));
+  CK(ctx->knot_steps.resize(std::max(L.K, 1)));
   DevLayout& d = ctx->dl;
   d.K = L.K;
   d.S = (int)L.stencils.size();
   d.D = (int)L.sides.size();
   d.P = (int)L.shapes.size();
   d.dom[0] = L.sw[0]; d.dom[1] = L.sw[1]; d.dom[2] = L.ne[0]; d.dom[3] = L.ne[1];
+  d.geom = L.geom;
+  d.radius = L.radius;
+  d.sh_R = ctx->sh_R.p;
   d.kx = ctx->kx.p; d.ky = ctx->ky.p; d.knot_stencil = ctx->knot_stencil.p; d.row_ptr = ctx->row_ptr.p;
   d.st_rect = ctx->st_rect.p; d.st_side = ctx->st_side.p; d.st_glob = ctx->st_glob.p;
   d.st_map_off = ctx->st_map_off.p; d.map_pos = ctx->map_pos.p; d.map_owner = ctx->map_owner.p;
@@ -189,6 +195,7 @@ pdds_status check_err_flags(pdds_ctx* ctx) {
   if (f & ERR_FLAG_SINGULAR) return fail(ctx, PDDS_ERR_ILL_CONDITIONED, "RBF matrix numerically singular");
   if (f & ERR_FLAG_STEP_LIMIT) return fail(ctx, PDDS_ERR_STEP_LIMIT, "a path exceeded max_steps");
   if (f & ERR_FLAG_EXIT_SIDE) return fail(ctx, PDDS_ERR_EXIT_SIDE, "an exit matched no stencil side");
+  if (f & ERR_FLAG_TIMEOUT) return fail(ctx, PDDS_ERR_TIMEOUT, "a grid barrier of the interface solve timed out");
   return PDDS_OK;
 }
 
@@ -214,6 +221,8 @@ pdds_status enqueue_prefix(pdds_ctx* ctx, const pdds_estimate_desc* desc, const 
   CK(cudaMemsetAsync(ctx->GG.p, 0, std::max<int64_t>(nnz, 1) * sizeof(double), s));
   CK(cudaMemsetAsync(ctx->Bsum.p, 0, L.K * sizeof(double), s));
   CK(cudaMemsetAsync(ctx->BBsum.p, 0, L.K * sizeof(double), s));
+  CK(cudaMemsetAsync(ctx->knot_steps.p, 0, L.K * sizeof(unsigned long long), s));
+  ctx->has_knot_steps = (mode == PDDS_MODE_MIXED);
   CK(launch_boundary_b(ctx->dl, P, mode, ctx->bnd_knots.p, ctx->n_bnd, ctx->B.p, ctx->BB.p, s));
   *launches += ctx->n_bnd > 0;
   return PDDS_OK;
@@ -221,7 +230,17 @@ pdds_status enqueue_prefix(pdds_ctx* ctx, const pdds_estimate_desc* desc, const 
 
 // Items are (knot, chunk of paths): enough chunks per knot to give every SM
 // several items, but at least 256 paths per chunk.
-void item_split(const pdds_ctx* ctx, int N, int* chunks_out, int* ppc_out) {
+bool tuned_for(const pdds_ctx* ctx, const pdds_estimate_desc* desc) {
+  return ctx->tune_ppc > 0 && ctx->tune_kind == ctx->prob.kind && ctx->tune_rich == (desc->richardson ? 1 : 0);
+}
+
+void item_split(const pdds_ctx* ctx, int N, int* chunks_out, int* ppc_out, int tuned_ppc = 0) {
+  if (tuned_ppc > 0) {
+    const int ppc = std::max(1, std::min(N, tuned_ppc));
+    *chunks_out = (N + ppc - 1) / ppc;
+    *ppc_out = ppc;
+    return;
+  }
   const int n_mc = ctx->n_mc;
   const int target = 4 * std::max(ctx->num_sms, 1) * 4;
   int chunks = std::max(1, (target + std::max(n_mc, 1) - 1) / std::max(n_mc, 1));
@@ -278,11 +297,16 @@ pdds_status enqueue_mixed_paths(pdds_ctx* ctx, const pdds_estimate_desc* desc, c
   a.item_p0 = items ? items->p0 : nullptr;
   a.item_p1 = items ? items->p1 : nullptr;
   a.knot_invN = items ? items->knot_invN : nullptr;
+  a.knot_steps = ctx->knot_steps.p;
   const size_t smem = ctx->mixed_smem * (a.want_var ? 2 : 1);
   if (smem > 200 * 1024) return fail(ctx, PDDS_ERR_INVALID, "exit histograms exceed shared memory; lower bins_per_gap");
   int bps = mixed_blocks_per_sm(P.kind, smem, a.richardson);
   if (bps < 1) bps = 1;
-  const int grid = std::max(1, std::min(n_items, bps * ctx->num_sms));
+  if (ctx->force_bps > 0) bps = std::min(bps, ctx->force_bps);
+  else if (tuned_for(ctx, desc)) bps = std::min(bps, ctx->tune_bps);
+  int grid = std::max(1, std::min(n_items, bps * ctx->num_sms));
+  if (ctx->force_grid_frac > 0.0 && ctx->force_grid_frac < 1.0)
+    grid = std::max(1, std::min(grid, (int)std::lround(ctx->force_grid_frac * bps * ctx->num_sms)));
   if (n_items > 0) {
     CK(launch_paths_mixed(a, P.kind, grid, smem, s));
     ++*launches;
@@ -349,7 +373,7 @@ pdds_status enqueue_mixed(pdds_ctx* ctx, const pdds_estimate_desc* desc, int* la
   pdds_status st = enqueue_prefix(ctx, desc, P, false, launches);
   if (st != PDDS_OK) return st;
   int chunks = 1, ppc = 1;
-  item_split(ctx, desc->npaths, &chunks, &ppc);
+  item_split(ctx, desc->npaths, &chunks, &ppc, tuned_for(ctx, desc) ? ctx->tune_ppc : 0);
   st = enqueue_mixed_paths(ctx, desc, P, chunks, ppc, launches);
   if (st != PDDS_OK) return st;
   const int64_t nnz = ctx->L.row_ptr[ctx->L.K];
@@ -396,7 +420,7 @@ pdds_status pdds_destroy(pdds_ctx* ctx) {
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     DBuf<double>* d64[] = {&ctx->kx, &ctx->ky, &ctx->st_rect, &ctx->sd_c, &ctx->sd_origin, &ctx->side_px,
-                           &ctx->side_py, &ctx->sh_c, &ctx->sh_lo, &ctx->sh_delta, &ctx->sh_t, &ctx->ipsi,
+                           &ctx->side_py, &ctx->sh_c, &ctx->sh_R, &ctx->sh_lo, &ctx->sh_delta, &ctx->sh_t, &ctx->ipsi,
                            &ctx->G, &ctx->GG, &ctx->B, &ctx->BB, &ctx->Bsum, &ctx->BBsum, &ctx->rx,
                            &ctx->ry, &ctx->rY, &ctx->rZ, &ctx->rxi, &ctx->Gside, &ctx->GGside,
                            &ctx->ipsi_knot, &ctx->sv64, &ctx->sscal, &ctx->spart, &ctx->shess, &ctx->su};
@@ -420,6 +444,8 @@ pdds_status pdds_destroy(pdds_ctx* ctx) {
     ctx->sw32.release();
     ctx->sval32.release();
     ctx->sctl.release();
+    ctx->sgpart.release();
+    ctx->sbar.release();
     drop_graph(ctx);
     ctx->knot_inst.release();
     ctx->inst_knot0.release();
@@ -430,6 +456,7 @@ pdds_status pdds_destroy(pdds_ctx* ctx) {
     ctx->b_tend.release();
     ctx->rng_dev.release();
     ctx->knot_N.release();
+    ctx->knot_steps.release();
     ctx->item_knot.release();
     ctx->item_p0.release();
     ctx->item_p1.release();
@@ -450,7 +477,7 @@ const char* pdds_last_error(const pdds_ctx* ctx) { return ctx ? ctx->err.c_str()
 
 pdds_status pdds_problem_set(pdds_ctx* ctx, const pdds_problem_desc* desc) {
   if (!ctx || !desc) return PDDS_ERR_INVALID;
-  if (desc->kind < 0 || desc->kind > 4) return fail(ctx, PDDS_ERR_INVALID, "unknown problem kind");
+  if (desc->kind < 0 || desc->kind > 5) return fail(ctx, PDDS_ERR_INVALID, "unknown problem kind");
   if (desc->kind == PDDS_LUT && ctx->lut_nx < 4)
     return fail(ctx, PDDS_ERR_INVALID, "PDDS_LUT needs pdds_problem_set_lut first");
   if (desc->kind == PDDS_HELMHOLTZ && desc->p[2] > 0.0)
@@ -496,6 +523,39 @@ pdds_status pdds_layout_build(pdds_ctx* ctx, const pdds_layout_desc* desc, pdds_
   ctx->has_batch_run = false;
   const std::string e = build_rect_layout(ctx->L, desc->sw, desc->ne, desc->nsub, desc->nnode, desc->fac,
                                           ctx->bins);
+  if (!e.empty()) return fail(ctx, PDDS_ERR_INVALID, e);
+  ctx->has_layout = true;
+  ctx->has_estimate = false;
+  if (ctx->device >= 0) {
+    pdds_status st = upload_layout(ctx);
+    if (st != PDDS_OK) return st;
+  }
+  if (info) {
+    info->nknots = ctx->L.K;
+    info->nboundary = ctx->L.nboundary;
+    info->nstencils = (int)ctx->L.stencils.size();
+    info->nsides = (int)ctx->L.sides.size();
+    info->nshapes = (int)ctx->L.shapes.size();
+    info->max_side = ctx->L.max_side;
+    info->nnz = ctx->L.row_ptr[ctx->L.K];
+  }
+  return PDDS_OK;
+}
+
+pdds_status pdds_layout_build_circle(pdds_ctx* ctx, const pdds_circle_desc* desc, pdds_layout_info* info) {
+  if (!ctx || !desc) return PDDS_ERR_INVALID;
+  for (int q = 0; q < 4; q++)
+    if (!(desc->kappa[q] > 0.0)) return fail(ctx, PDDS_ERR_INVALID, "kappa must be positive");
+  if (ctx->device >= 0) {
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  drop_graph(ctx);
+  ctx->is_batch = false;
+  ctx->n_inst = 0;
+  ctx->has_batch_run = false;
+  const std::string e = build_circle_layout(ctx->L, desc->radius, desc->nrings, desc->nsectors, desc->nnode,
+                                            desc->kappa, ctx->bins);
   if (!e.empty()) return fail(ctx, PDDS_ERR_INVALID, e);
   ctx->has_layout = true;
   ctx->has_estimate = false;
@@ -563,6 +623,12 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
     return fail(ctx, PDDS_ERR_INVALID, "the replay mode follows the reference and has no Richardson form");
   if (mode == PDDS_MODE_REPLAY_FP64 && ctx->prob.kind == PDDS_MONEGROS)
     return fail(ctx, PDDS_ERR_INVALID, "the Monegros problem has no replay form");
+  if (ctx->L.geom == 1 && mode == PDDS_MODE_REPLAY_FP64)
+    return fail(ctx, PDDS_ERR_INVALID, "circle layouts have no replay form (MIXED and FP64 modes)");
+  if (ctx->L.geom == 1 && ctx->prob.kind != PDDS_POISSON_SINCOS && ctx->prob.kind != PDDS_CIRCLE_POISSON)
+    return fail(ctx, PDDS_ERR_INVALID, "circle layouts take the sigma = sqrt2 I problems");
+  if (mode == PDDS_MODE_REPLAY_FP64 && ctx->prob.kind == PDDS_CIRCLE_POISSON)
+    return fail(ctx, PDDS_ERR_INVALID, "the circle problem has no replay form");
   if (desc->adaptive_n && mode != PDDS_MODE_MIXED)
     return fail(ctx, PDDS_ERR_INVALID, "variance-adaptive paths (adaptive_n) run in PDDS_MODE_MIXED");
   if (desc->adaptive_n && desc->target_stderr < 0.0) return fail(ctx, PDDS_ERR_INVALID, "target_stderr < 0");
@@ -677,7 +743,7 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
     }
   } else {
     int chunks = 1, ppc = 1;
-    item_split(ctx, N, &chunks, &ppc);
+    item_split(ctx, N, &chunks, &ppc, (mode == PDDS_MODE_MIXED && tuned_for(ctx, desc)) ? ctx->tune_ppc : 0);
     const int n_items = n_mc * chunks;
     CK(cudaMemsetAsync(ctx->counter.p, 0, sizeof(int), s));
     if (mode == PDDS_MODE_MIXED) {
@@ -771,6 +837,120 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
   return check_err_flags(ctx);
 }
 
+pdds_status pdds_autotune(pdds_ctx* ctx, const pdds_estimate_desc* desc, int32_t sample_knots,
+                          pdds_tune_info* info) {
+  if (!ctx || !desc) return PDDS_ERR_INVALID;
+  if (ctx->device < 0) return fail(ctx, PDDS_ERR_INVALID, "context has no device");
+  if (!ctx->has_problem || !ctx->has_layout) return fail(ctx, PDDS_ERR_INVALID, "problem and layout needed");
+  if (desc->mode != PDDS_MODE_MIXED) return fail(ctx, PDDS_ERR_INVALID, "the autotuner tunes PDDS_MODE_MIXED");
+  if (desc->npaths < 1 || !(desc->h > 0.0)) return fail(ctx, PDDS_ERR_INVALID, "npaths >= 1 and h > 0 required");
+  CK(cudaSetDevice(ctx->device));
+  cudaStream_t s = ctx->stream;
+  const HostLayout& L = ctx->L;
+  const ProblemDev P = problem_dev(ctx);
+  const int N = desc->npaths;
+  // sample: knots spread evenly through the hand-out order
+  std::vector<int> mc;
+  for (int v : L.order)
+    if (!L.knot_boundary[v]) mc.push_back(v);
+  if (mc.empty()) return fail(ctx, PDDS_ERR_INVALID, "layout has no knots with paths");
+  // the whole layout by default; a sample runs on a proportionally smaller
+  // grid so every CTA sees as many work items as in the full run
+  const int ns = std::max(1, std::min<int>(sample_knots > 0 ? sample_knots : (int)mc.size(), (int)mc.size()));
+  const double frac = (double)ns / (double)mc.size();
+  std::vector<int> sample(ns);
+  for (int i = 0; i < ns; i++) sample[i] = mc[(size_t)i * mc.size() / ns];
+  pdds_estimate_desc d = *desc;
+  d.adaptive_n = 0;
+  int launches = 0;
+  pdds_status st = enqueue_prefix(ctx, &d, P, false, &launches);
+  if (st != PDDS_OK) return st;
+  const size_t smem = ctx->mixed_smem * (d.want_var ? 2 : 1);
+  const int occ = std::max(1, mixed_blocks_per_sm(P.kind, smem, d.richardson));
+  std::vector<int> bps_c;
+  for (int b = 1; b <= occ; b++) bps_c.push_back(b);
+  std::vector<int> ppc_c;
+  for (int p = 256; p < N; p *= 4) ppc_c.push_back(p);
+  ppc_c.push_back(N);
+  int def_chunks = 1, def_ppc = 1;
+  item_split(ctx, N, &def_chunks, &def_ppc);
+  ppc_c.push_back(def_ppc);
+  std::sort(ppc_c.begin(), ppc_c.end());
+  ppc_c.erase(std::unique(ppc_c.begin(), ppc_c.end()), ppc_c.end());
+  auto time_shape = [&](int bps, int ppc, float* ms_out) -> pdds_status {
+    std::vector<int> ik, ip0, ip1;
+    for (int k : sample)
+      for (int p = 0; p < N; p += ppc) {
+        ik.push_back(k);
+        ip0.push_back(p);
+        ip1.push_back(std::min(N, p + ppc));
+      }
+    CK(ctx->item_knot.upload(ik, s));
+    CK(ctx->item_p0.upload(ip0, s));
+    CK(ctx->item_p1.upload(ip1, s));
+    ItemList items{ctx->item_knot.p, ctx->item_p0.p, ctx->item_p1.p, (int)ik.size(), nullptr};
+    float best = 1e30f;
+    for (int rep = 0; rep < 2; rep++) {
+      ctx->force_bps = bps;
+      ctx->force_grid_frac = frac;
+      CK(cudaEventRecord(ctx->ev0, s));
+      int nl = 0;
+      pdds_status e = enqueue_mixed_paths(ctx, &d, P, 1, ppc, &nl, &items);
+      ctx->force_bps = 0;
+      ctx->force_grid_frac = 0.0;
+      if (e != PDDS_OK) return e;
+      CK(cudaEventRecord(ctx->ev1, s));
+      CK(cudaEventSynchronize(ctx->ev1));
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+      best = std::min(best, ms);
+    }
+    *ms_out = best;
+    return PDDS_OK;
+  };
+  float best_ms = 1e30f, def_ms = 0.f;
+  int best_bps = occ, best_ppc = def_ppc, ncand = 0;
+  st = time_shape(occ, def_ppc, &def_ms);
+  if (st != PDDS_OK) return st;
+  for (int b : bps_c)
+    for (int p : ppc_c) {
+      float ms = 0.f;
+      st = time_shape(b, p, &ms);
+      if (st != PDDS_OK) return st;
+      ++ncand;
+      if (ms < best_ms) {
+        best_ms = ms;
+        best_bps = b;
+        best_ppc = p;
+      }
+    }
+  st = check_err_flags(ctx);
+  if (st != PDDS_OK) return st;
+  ctx->tune_bps = best_bps;
+  ctx->tune_ppc = best_ppc;
+  ctx->tune_kind = ctx->prob.kind;
+  ctx->tune_rich = d.richardson ? 1 : 0;
+  ctx->has_estimate = false;
+  if (info) {
+    info->blocks_per_sm = best_bps;
+    info->paths_per_item = best_ppc;
+    info->candidates = ncand;
+    info->sample_knots = ns;
+    info->best_ms = best_ms;
+    info->default_ms = def_ms;
+  }
+  return PDDS_OK;
+}
+
+pdds_status pdds_estimate_knot_steps(pdds_ctx* ctx, int64_t* steps) {
+  if (!ctx || !steps) return PDDS_ERR_INVALID;
+  if (!ctx->has_estimate || !ctx->has_knot_steps) return fail(ctx, PDDS_ERR_INVALID, "no MIXED estimate on this layout");
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaMemcpyAsync(steps, ctx->knot_steps.p, ctx->L.K * sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return PDDS_OK;
+}
+
 pdds_status pdds_estimate_knot_paths(pdds_ctx* ctx, int32_t* npaths) {
   if (!ctx || !npaths) return PDDS_ERR_INVALID;
   if (!ctx->has_estimate || ctx->last_knot_N.size() != (size_t)ctx->L.K)
@@ -794,15 +974,21 @@ pdds_status pdds_solve_interface(pdds_ctx* ctx, const pdds_solve_desc* desc, dou
   CK(ctx->spart.resize(std::max<size_t>(64 * 256 + 1024, (size_t)((K + 127) / 128) * 48 + 64)));
   CK(ctx->shess.resize((size_t)(m + 1) * m + 2 * m + 4 * (m + 1) + 16));
   CK(ctx->sctl.resize(8));
+  CK(ctx->sgpart.resize((size_t)2 * std::max(ctx->num_sms, 1) * (GMRES_CLUSTER_MAX_M + 3)));
+  CK(ctx->sbar.resize(2));
   CK(ctx->su.resize(std::max(K, 1)));
   SolveCsr A{K, nnz, ctx->row_ptr.p, ctx->col.p, ctx->G.p};
   SolveWork w;
+  w.err = ctx->errf.p;
+  CK(cudaMemsetAsync(ctx->errf.p, 0, sizeof(unsigned), s));
   for (int q = 0; q < 6; q++) w.v64[q] = ctx->sv64.p + (size_t)q * K;
   w.scal = ctx->sscal.p;
   w.part = ctx->spart.p;
   w.hess = ctx->shess.p;
   w.host_rr = ctx->host_rr;
   w.ctl = ctx->sctl.p;
+  w.gpart = ctx->sgpart.p;
+  w.bar = ctx->sbar.p;
   int iters = 0, refines = 0;
   double relres = 0.0;
   const double tol = desc->tol > 0 ? desc->tol : 1e-10;
@@ -838,6 +1024,10 @@ pdds_status pdds_solve_interface(pdds_ctx* ctx, const pdds_solve_desc* desc, dou
     info->rel_residual = relres;
     info->ms = ms;
     info->kernel_launches = w.launches;
+  }
+  {
+    pdds_status st = check_err_flags(ctx);
+    if (st != PDDS_OK) return st;
   }
   if (!(relres <= tol * 1.0000001) && !(relres == 0.0))
     return fail(ctx, PDDS_ERR_NOT_CONVERGED, "interface solve reached " + std::to_string(relres));

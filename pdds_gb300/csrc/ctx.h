@@ -59,7 +59,7 @@ struct pdds_ctx {
   int bins = 16;
   bool tables_ready = false;
   // device layout
-  DBuf<double> kx, ky, st_rect, sd_c, sd_origin, side_px, side_py, sh_c, sh_lo, sh_delta, sh_t, ipsi;
+  DBuf<double> kx, ky, st_rect, sd_c, sd_origin, side_px, side_py, sh_c, sh_R, sh_lo, sh_delta, sh_t, ipsi;
   DBuf<int> knot_stencil, st_side, st_glob, map_pos, sd_n, sd_orient, sd_shape, side_knot, sh_n,
       sh_nbins, col, mc_knots, bnd_knots;
   DBuf<int64_t> row_ptr, st_map_off, sd_knot_off, sh_tab_off, sh_ipsi_off, sh_t_off;
@@ -82,7 +82,8 @@ struct pdds_ctx {
   // solve scratch
   DBuf<double> sv64, sscal, spart, shess, su;
   DBuf<float> sV32, sw32, sval32;
-  DBuf<unsigned> sctl;
+  DBuf<unsigned> sctl, sbar;
+  DBuf<double> sgpart;
   double* host_rr = nullptr;
   int solve_m = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
@@ -102,10 +103,16 @@ struct pdds_ctx {
   std::vector<unsigned char> graph_key;
   int graph_launches = 0;
   bool has_batch_run = false;
+  // autotuned launch shape of the MIXED path kernel (0 = defaults)
+  int tune_bps = 0, tune_ppc = 0, tune_kind = -1, tune_rich = -1;
+  int force_bps = 0;             // CTAs per SM imposed while the autotuner times a shape
+  double force_grid_frac = 0.0;  // grid scaled to a knot sample while it times
   // variance-adaptive paths (pdds_estimate with adaptive_n)
   DBuf<int> knot_N, item_knot, item_p0, item_p1;
   DBuf<double> knot_scale, knot_invN;
   std::vector<int> last_knot_N;  // paths per knot of the last estimate
+  DBuf<unsigned long long> knot_steps;  // path steps per knot of the last MIXED estimate
+  bool has_knot_steps = false;
   // {seed, instance} read by the path kernel of a batch sequence
   DBuf<unsigned long long> rng_dev;
   unsigned long long* rng_host = nullptr;  // pinned staging of rng_dev

@@ -15,6 +15,11 @@ namespace pdds {
 struct DevLayout {
   int K, S, D, P;
   double dom[4];  // domain rectangle {SW.x, SW.y, NE.x, NE.y}
+  // 0: rectangular stencils {x0, y0, x1, y1}; 1: polar stencils
+  // {rho0, phi0, rho1, phi1} on a disk of radius `radius` (arcs and rays)
+  int geom;
+  double radius;
+  const double* sh_R;  // per shape: arc radius (RBF distance = chord), 0 for straight sides
   // knots
   const double* kx;
   const double* ky;
@@ -74,7 +79,7 @@ struct ProblemDev {
   LutDev lut;
 };
 
-enum { PK_POISSON_SINCOS = 0, PK_MONEGROS = 1, PK_HELMHOLTZ = 2, PK_VARCOEF = 3, PK_LUT = 4 };
+enum { PK_POISSON_SINCOS = 0, PK_MONEGROS = 1, PK_HELMHOLTZ = 2, PK_VARCOEF = 3, PK_LUT = 4, PK_CIRCLE = 5 };
 
 // Problem parameters of the instance that owns knot k (batches), else P's own.
 __device__ __forceinline__ void instance_params(const DevLayout& L, int k, ProblemDev& P, uint32_t& rng_inst,
@@ -215,6 +220,22 @@ __device__ __forceinline__ void coef_f32(const ProblemDev& P, float x, float y, 
     k.f = -(0.5f * (s1 * s1 * uxx + s2 * s2 * uyy) + (y * ux - x * uy) + c * (ux + 1.f));
     k.g0 = ux;
     k.g1 = uy;
+  } else if (KIND == PK_CIRCLE) {
+    // u = r^2 sin 3t + cos x: with c = x / r, s = y / r, sin 3t = 3s - 4s^3,
+    // cos 3t = 4c^3 - 3c; f = -Lap u = 5 sin 3t + cos x (bounded, continuous
+    // away from r = 0); grad u = (2r sin3t c - 3r cos3t s - sin x,
+    // 2r sin3t s + 3r cos3t c)
+    const float r = sqrtf(x * x + y * y);
+    const float ir = r > 1e-30f ? 1.f / r : 0.f;
+    const float c1 = r > 1e-30f ? x * ir : 1.f, s1 = y * ir;
+    const float s3 = s1 * (3.f - 4.f * s1 * s1), c3 = c1 * (4.f * c1 * c1 - 3.f);
+    float sx, cx;
+    __sincosf(x, &sx, &cx);
+    k.s00 = 1.41421356f; k.s01 = 0.f; k.s10 = 0.f; k.s11 = 1.41421356f;
+    k.b0 = 0.f; k.b1 = 0.f; k.c = 0.f;
+    k.f = 5.f * s3 + cx;
+    k.g0 = r * (2.f * s3 * c1 - 3.f * c3 * s1) - sx;
+    k.g1 = r * (2.f * s3 * s1 + 3.f * c3 * c1);
   } else {  // PK_MONEGROS (BVPs/EDPs/Monegros_Poisson_CPP.hpp)
     const float k2 = 0.01f, k3 = 0.02f, k4 = 0.12f, k5 = 0.05f, k6 = 0.05f, k7 = -0.12f, sf = 0.333f;
     const float q = 1.f + k2 * x * x + k3 * y * y;
@@ -287,6 +308,10 @@ __device__ __forceinline__ float u_f32(const ProblemDev& P, float x, float y) {
     return __sinf((float)P.p[0] * x) * __cosf((float)P.p[1] * y);
   } else if (KIND == PK_VARCOEF) {
     return __expf(x) * __cosf(2.f * y) + 1.f;
+  } else if (KIND == PK_CIRCLE) {
+    const float r = sqrtf(x * x + y * y);
+    const float s1 = r > 1e-30f ? y / r : 0.f;
+    return r * r * (s1 * (3.f - 4.f * s1 * s1)) + __cosf(x);
   } else {
     const float q = 1.f + 0.01f * x * x + 0.02f * y * y;
     return 3.f + 0.333f * (__sinf(sqrtf(q)) + tanhf(__sinf(0.12f * x + 0.05f * y) + __sinf(0.05f * x - 0.12f * y)));
@@ -334,6 +359,17 @@ __device__ __forceinline__ void coef_f64(const ProblemDev& P, double x, double y
     k.f = -(0.5 * (s1 * s1 * uxx + s2 * s2 * uyy) + (y * ux - x * uy) + c * (ux + 1.0));
     k.g0 = ux;
     k.g1 = uy;
+  } else if (KIND == PK_CIRCLE) {
+    const double r = ::sqrt(x * x + y * y);
+    const double c1 = r > 1e-300 ? x / r : 1.0, s1 = r > 1e-300 ? y / r : 0.0;
+    const double s3 = s1 * (3.0 - 4.0 * s1 * s1), c3 = c1 * (4.0 * c1 * c1 - 3.0);
+    double sx, cx;
+    sincos(x, &sx, &cx);
+    k.s00 = 1.4142135623730951; k.s01 = 0.0; k.s10 = 0.0; k.s11 = 1.4142135623730951;
+    k.b0 = 0.0; k.b1 = 0.0; k.c = 0.0;
+    k.f = 5.0 * s3 + cx;
+    k.g0 = r * (2.0 * s3 * c1 - 3.0 * c3 * s1) - sx;
+    k.g1 = r * (2.0 * s3 * s1 + 3.0 * c3 * c1);
   } else {
     const double k2 = 0.01, k3 = 0.02, k4 = 0.12, k5 = 0.05, k6 = 0.05, k7 = -0.12, sf = 0.333;
     const double q = 1.0 + k2 * x * x + k3 * y * y;
@@ -371,6 +407,10 @@ __device__ __forceinline__ double u_f64(const ProblemDev& P, double x, double y)
     return ::sin(P.p[0] * x) * ::cos(P.p[1] * y);
   } else if (KIND == PK_VARCOEF) {
     return ::exp(x) * ::cos(2.0 * y) + 1.0;
+  } else if (KIND == PK_CIRCLE) {
+    const double r = ::sqrt(x * x + y * y);
+    const double s1 = r > 1e-300 ? y / r : 0.0;
+    return r * r * (s1 * (3.0 - 4.0 * s1 * s1)) + ::cos(x);
   } else {
     const double q = 1.0 + 0.01 * x * x + 0.02 * y * y;
     return 3.0 + 0.333 * (::sin(::sqrt(q)) + ::tanh(::sin(0.12 * x + 0.05 * y) + ::sin(0.05 * x - 0.12 * y)));
@@ -424,6 +464,23 @@ __device__ __forceinline__ double adaptive_step(const double* rect, double x0, d
   const double w0 = Nx * (double)k.s00 + Ny * (double)k.s10;
   const double w1 = Nx * (double)k.s01 + Ny * (double)k.s11;
   const double q = d / (sqrt(w0 * w0 + w1 * w1) * 2 * 0.5826);
+  const double ha = q * q;
+  return h0 < ha ? h0 : ha;
+}
+
+// The same step on a polar stencil {rho0, phi0, rho1, phi1} (isotropic
+// sigma): d = the largest outside distance to the inner arc (none at the
+// centre), the outer arc and the two rays, as in the polar exit test.
+template <typename T>
+__device__ __forceinline__ double adaptive_step_polar(const double* rect, double x0, double y0, double h0,
+                                                      const Coef<T>& k) {
+  const double rho = sqrt(x0 * x0 + y0 * y0);
+  double d = rho - rect[2];
+  if (rect[0] > 0.0) d = fmax(d, rect[0] - rho);
+  d = fmax(d, sin(rect[1]) * x0 - cos(rect[1]) * y0);
+  d = fmax(d, cos(rect[3]) * y0 - sin(rect[3]) * x0);
+  if (!(d <= -1e-04)) return h0;
+  const double q = d / (fabs((double)k.s00) * 2 * 0.5826);
   const double ha = q * q;
   return h0 < ha ? h0 : ha;
 }

@@ -25,6 +25,7 @@ struct ItemSide64 {
   int64_t t_off;     // shape's local knot coordinates
   int64_t ipsi_off;
   int64_t map_off;
+  double R;          // arc radius (polar stencils): RBF distance = chord 2 R sin(dt / 2)
 };
 
 constexpr unsigned FULL = 0xffffffffu;
@@ -45,7 +46,7 @@ __device__ __forceinline__ void normals_f64(uint32_t ua, uint32_t ub, double& z0
   z1 = rho * sn;
 }
 
-template <int KIND, bool RICH>
+template <int KIND, bool RICH, int GEOM>
 __global__ void __launch_bounds__(FP64_THREADS)
 k_paths_fp64(const Fp64Args a) {
   extern __shared__ double Ssum[];  // [sum n] per-side RBF sums, then [sum n] local t
@@ -77,7 +78,8 @@ k_paths_fp64(const Fp64Args a) {
       if (a.adaptive_h) {
         Coef<double> kd;
         coef_f64<KIND>(a.P, L.kx[k], L.ky[k], kd);
-        s_h = adaptive_step<double>(L.st_rect + 4 * st, L.kx[k], L.ky[k], a.h, kd);
+        s_h = GEOM == 1 ? adaptive_step_polar(L.st_rect + 4 * st, L.kx[k], L.ky[k], a.h, kd)
+                        : adaptive_step<double>(L.st_rect + 4 * st, L.kx[k], L.ky[k], a.h, kd);
       }
       int off = 0;
       int64_t moff = L.st_map_off[st];
@@ -88,13 +90,18 @@ k_paths_fp64(const Fp64Args a) {
         is.map_off = moff;
         if (sd < 0) {
           is.n = 0; is.orient = 0; is.s_off = off; is.origin = 0.0; is.inv_c2 = 0.0;
-          is.t_off = 0; is.ipsi_off = 0;
+          is.t_off = 0; is.ipsi_off = 0; is.R = 0.0;
         } else {
           const int sh = L.sd_shape[sd];
           is.n = L.sd_n[sd];
           is.orient = L.sd_orient[sd];
           is.s_off = off;
           is.origin = L.sd_origin[sd];
+          is.R = L.sh_R ? L.sh_R[sh] : 0.0;
+          if (GEOM == 1 && is.orient == 0) {  // arc: the side's angles in this stencil's turn
+            const double tw = 6.283185307179586;
+            is.origin += tw * nearbyint((L.st_rect[4 * st + 1] - is.origin) / tw);
+          }
           const double c = L.sh_c[sh];
           is.inv_c2 = 1.0 / (c * c);
           is.t_off = L.sh_t_off[sh];
@@ -118,6 +125,8 @@ k_paths_fp64(const Fp64Args a) {
 
     const double x0 = L.kx[knot], y0 = L.ky[knot];
     const double rect[4] = {s_rect[0], s_rect[1], s_rect[2], s_rect[3]};
+    const double pa0 = GEOM == 1 ? ::cos(rect[1]) : 0.0, pa1 = GEOM == 1 ? ::sin(rect[1]) : 0.0;
+    const double pb0 = GEOM == 1 ? ::cos(rect[3]) : 0.0, pb1 = GEOM == 1 ? ::sin(rect[3]) : 0.0;
     Coef<double> k0;
     coef_f64<KIND>(a.P, x0, y0, k0);
     const int chunk = item % a.chunks;
@@ -125,10 +134,10 @@ k_paths_fp64(const Fp64Args a) {
     bool active = (int)path < path_end;
     double b = 0.0, bb = 0.0;
     unsigned long long nsteps = 0, nglob = 0, nsten = 0;
-    auto exit_level = [&](const Lvl64& s, double wgt, double Ex, double Ey, int onmask) -> double {
-      const int d = exit_side(onmask);
-      const bool glob = ((onmask & 1) && s_side[0].glob) || ((onmask & 2) && s_side[1].glob) ||
-                        ((onmask & 4) && s_side[2].glob) || ((onmask & 8) && s_side[3].glob);
+    // exit on side d at side coordinate `along` (x or y on rectangles, angle
+    // or radius on polar stencils), projection (Ex, Ey)
+    auto exit_level = [&](const Lvl64& s, double wgt, double Ex, double Ey, int d, bool glob,
+                          double along) -> double {
       if (glob) {
         ++nglob;
         return s.Z + s.Y * u_f64<KIND>(a.P, Ex, Ey) + s.xi;
@@ -138,10 +147,11 @@ k_paths_fp64(const Fp64Args a) {
         atomicOr(a.err_flags, ERR_FLAG_EXIT_SIDE);
       } else {
         const ItemSide64& is = s_side[d];
-        const double sc = (is.orient == 0 ? Ex : Ey) - is.origin;
+        const double sc = along - is.origin;
         const double yw = wgt * s.Y;
         for (int j = 0; j < is.n; j++) {
-          const double dt = tloc[is.s_off + j] - sc;
+          const double dt0 = tloc[is.s_off + j] - sc;
+          const double dt = is.R > 0.0 ? 2.0 * is.R * ::sin(0.5 * dt0) : dt0;
           atomicAdd(Ssum + is.s_off + j, yw * ::exp(-(dt * dt) * is.inv_c2));
         }
       }
@@ -158,19 +168,55 @@ k_paths_fp64(const Fp64Args a) {
       s.y += s.k.b1 * hh + (s.k.s10 * i0 + s.k.s11 * i1);
       ++s.steps;
       coef_f64<KIND>(a.P, s.x, s.y, s.k);
-      double Ex, Ey, Nx, Ny;
-      int onmask;
-      const double dist = rect2d<double>(rect, s.x, s.y, Ex, Ey, Nx, Ny, onmask);
-      const double w0 = Nx * s.k.s00 + Ny * s.k.s10, w1 = Nx * s.k.s01 + Ny * s.k.s11;
-      const double thr = -0.5826 * ::sqrt(w0 * w0 + w1 * w1) * sq;
-      if (dist < thr) {
-        if (s.steps < (unsigned)a.max_steps) return false;
-        atomicOr(a.err_flags, ERR_FLAG_STEP_LIMIT);
-        val = 0.0;
+      if constexpr (GEOM == 1) {
+        // polar stencil, isotropic sigma: outside distances beyond the inner
+        // arc (none at the centre), the outer arc and the two rays
+        const double rho = ::sqrt(s.x * s.x + s.y * s.y);
+        const double d_in = rect[0] > 0.0 ? rect[0] - rho : -1e300;
+        const double d_out = rho - rect[2];
+        const double d_a = pa1 * s.x - pa0 * s.y, d_b = pb0 * s.y - pb1 * s.x;
+        int d = 1;
+        double mx = d_in;
+        if (d_out > mx) { mx = d_out; d = 0; }
+        if (d_a > mx) { mx = d_a; d = 3; }
+        if (d_b > mx) { mx = d_b; d = 2; }
+        if (mx < -0.5826 * ::fabs(s.k.s00) * sq) {
+          if (s.steps < (unsigned)a.max_steps) return false;
+          atomicOr(a.err_flags, ERR_FLAG_STEP_LIMIT);
+          val = 0.0;
+          return true;
+        }
+        double along, Ex = 0.0, Ey = 0.0;
+        if (d <= 1) {
+          const double rel = ::atan2(pa0 * s.y - pa1 * s.x, pa0 * s.x + pa1 * s.y);
+          along = rect[1] + ::fmin(::fmax(rel, 0.0), rect[3] - rect[1]);
+          ::sincos(along, &Ey, &Ex);
+          Ex *= rect[d == 0 ? 2 : 0];
+          Ey *= rect[d == 0 ? 2 : 0];
+        } else {
+          const double t = d == 3 ? pa0 * s.x + pa1 * s.y : pb0 * s.x + pb1 * s.y;
+          along = ::fmin(::fmax(t, rect[0]), rect[2]);
+        }
+        val = exit_level(s, wgt, Ex, Ey, d, d == 0 && s_side[0].glob, along);
+        return true;
+      } else {
+        double Ex, Ey, Nx, Ny;
+        int onmask;
+        const double dist = rect2d<double>(rect, s.x, s.y, Ex, Ey, Nx, Ny, onmask);
+        const double w0 = Nx * s.k.s00 + Ny * s.k.s10, w1 = Nx * s.k.s01 + Ny * s.k.s11;
+        const double thr = -0.5826 * ::sqrt(w0 * w0 + w1 * w1) * sq;
+        if (dist < thr) {
+          if (s.steps < (unsigned)a.max_steps) return false;
+          atomicOr(a.err_flags, ERR_FLAG_STEP_LIMIT);
+          val = 0.0;
+          return true;
+        }
+        const int d = exit_side(onmask);
+        const bool glob = ((onmask & 1) && s_side[0].glob) || ((onmask & 2) && s_side[1].glob) ||
+                          ((onmask & 4) && s_side[2].glob) || ((onmask & 8) && s_side[3].glob);
+        val = exit_level(s, wgt, Ex, Ey, d, glob, d >= 0 && s_side[d].orient == 0 ? Ex : Ey);
         return true;
       }
-      val = exit_level(s, wgt, Ex, Ey, onmask);
-      return true;
     };
     Lvl64 fine, coarse;
     auto reset = [&]() {
@@ -271,18 +317,27 @@ k_paths_fp64(const Fp64Args a) {
 
 template <bool RICH>
 static cudaError_t launch_fp64_t(const Fp64Args& a, int kind, int grid, size_t smem, cudaStream_t s) {
-#define PDDS_FP64_CASE(KK)                                                                           \
-  case KK:                                                                                           \
-    cudaFuncSetAttribute(k_paths_fp64<KK, RICH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
-    k_paths_fp64<KK, RICH><<<grid, FP64_THREADS, smem, s>>>(a);                                      \
+#define PDDS_FP64_CASE(KK, GG)                                                                           \
+  case KK:                                                                                               \
+    cudaFuncSetAttribute(k_paths_fp64<KK, RICH, GG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+    k_paths_fp64<KK, RICH, GG><<<grid, FP64_THREADS, smem, s>>>(a);                                      \
     break;
-  switch (kind) {
-    PDDS_FP64_CASE(0)
-    PDDS_FP64_CASE(1)
-    PDDS_FP64_CASE(2)
-    PDDS_FP64_CASE(3)
-    PDDS_FP64_CASE(4)
-    default: return cudaErrorInvalidValue;
+  if (a.L.geom == 1) {
+    switch (kind) {
+      PDDS_FP64_CASE(0, 1)
+      PDDS_FP64_CASE(5, 1)
+      default: return cudaErrorInvalidValue;
+    }
+  } else {
+    switch (kind) {
+      PDDS_FP64_CASE(0, 0)
+      PDDS_FP64_CASE(1, 0)
+      PDDS_FP64_CASE(2, 0)
+      PDDS_FP64_CASE(3, 0)
+      PDDS_FP64_CASE(4, 0)
+      PDDS_FP64_CASE(5, 0)
+      default: return cudaErrorInvalidValue;
+    }
   }
 #undef PDDS_FP64_CASE
   return cudaGetLastError();
@@ -296,11 +351,12 @@ template <bool RICH>
 static int blocks64_t(int kind, size_t smem) {
   int nb = 0;
   switch (kind) {
-    case 0: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_paths_fp64<0, RICH>, FP64_THREADS, smem); break;
-    case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_paths_fp64<1, RICH>, FP64_THREADS, smem); break;
-    case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_paths_fp64<2, RICH>, FP64_THREADS, smem); break;
-    case 4: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_paths_fp64<4, RICH>, FP64_THREADS, smem); break;
-    default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_paths_fp64<3, RICH>, FP64_THREADS, smem); break;
+    case 0: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_paths_fp64<0, RICH, 0>, FP64_THREADS, smem); break;
+    case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_paths_fp64<1, RICH, 0>, FP64_THREADS, smem); break;
+    case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_paths_fp64<2, RICH, 0>, FP64_THREADS, smem); break;
+    case 4: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_paths_fp64<4, RICH, 0>, FP64_THREADS, smem); break;
+    case 5: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_paths_fp64<5, RICH, 0>, FP64_THREADS, smem); break;
+    default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_paths_fp64<3, RICH, 0>, FP64_THREADS, smem); break;
   }
   return nb;
 }

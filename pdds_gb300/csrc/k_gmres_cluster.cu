@@ -54,10 +54,98 @@ __device__ __forceinline__ unsigned long long global_ns() {
   return t;
 }
 
-__global__ void __launch_bounds__(CG_THREADS, 1) k_gmres_cluster(const ClusterGmresArgs a) {
-  cg::cluster_group cl = cg::this_cluster();
-  const unsigned crank = cl.block_rank(), csize = cl.num_blocks();
-  const int sys = blockIdx.x / csize;  // uniform within the cluster
+// The CTAs that own one system: a thread-block cluster (hardware barrier,
+// partials read through distributed shared memory), or the whole grid of a
+// cooperative launch (a counting barrier in global memory whose wait is
+// bounded, partials published in global memory).  reduce() sums the CTAs'
+// partials slot[0 .. nv) in rank order into out in every CTA; sync() and
+// reduce() return false only when a grid barrier timed out.
+struct ClusterGroup {
+  cg::cluster_group cl;
+  __device__ ClusterGroup() : cl(cg::this_cluster()) {}
+  __device__ unsigned rank() const { return cl.block_rank(); }
+  __device__ unsigned size() const { return cl.num_blocks(); }
+  __device__ int system() const { return (int)(blockIdx.x / cl.num_blocks()); }
+  __device__ bool sync() {
+    cl.sync();
+    return true;
+  }
+  // one warp per value, lanes over ranks, a fixed shuffle tree: the same
+  // order in every CTA
+  __device__ bool reduce(double* slot, int nv, double* out, int) {
+    cl.sync();
+    const unsigned lane = threadIdx.x & 31, n = cl.num_blocks();
+    for (int i = threadIdx.x >> 5; i < nv; i += CG_WARPS) {
+      double s = 0.0;
+      for (unsigned rk = lane; rk < n; rk += 32) s += cl.map_shared_rank(slot, rk)[i];
+      s = warp_sum(s);
+      if (lane == 0) out[i] = s;
+    }
+    __syncthreads();
+    return true;
+  }
+};
+
+constexpr unsigned GRID_SPIN_LIMIT = 1u << 24;  // ~1 s of polling
+
+struct GridGroup {
+  unsigned* count;  // arrivals at the current barrier (zeroed before the launch)
+  unsigned* gen;    // barrier generation
+  unsigned* err;    // ERR_FLAG_TIMEOUT on a wait that ran out
+  double* gpart;    // [2][gridDim.x][CG_MAXV + 2] published partials
+  __device__ unsigned rank() const { return blockIdx.x; }
+  __device__ unsigned size() const { return gridDim.x; }
+  __device__ int system() const { return 0; }
+  __device__ bool sync() {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      volatile unsigned* vg = gen;
+      const unsigned g = *vg;
+      __threadfence();
+      int ok = 1;
+      if (atomicAdd(count, 1u) == gridDim.x - 1) {
+        atomicExch(count, 0u);
+        __threadfence();
+        atomicAdd(gen, 1u);
+      } else {
+        unsigned spins = 0;
+        while (*vg == g) {
+          if (++spins > GRID_SPIN_LIMIT) {
+            atomicOr(err, ERR_FLAG_TIMEOUT);
+            ok = 0;
+            break;
+          }
+          __nanosleep(32);
+        }
+      }
+      __threadfence();
+      s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+  }
+  __device__ bool reduce(double* slot, int nv, double* out, int parity) {
+    double* mine = gpart + ((size_t)parity * gridDim.x + blockIdx.x) * (CG_MAXV + 2);
+    for (int i = threadIdx.x; i < nv; i += CG_THREADS) mine[i] = slot[i];
+    const bool ok = sync();
+    const unsigned lane = threadIdx.x & 31;
+    for (int i = threadIdx.x >> 5; i < nv; i += CG_WARPS) {
+      double s = 0.0;
+      for (unsigned rk = lane; rk < gridDim.x; rk += 32)
+        s += __ldcg(gpart + ((size_t)parity * gridDim.x + rk) * (CG_MAXV + 2) + i);
+      s = warp_sum(s);
+      if (lane == 0) out[i] = s;
+    }
+    __syncthreads();
+    return ok;
+  }
+};
+
+template <class Group>
+__device__ __forceinline__ void gmres_body(const ClusterGmresArgs& a, Group& grp) {
+  const unsigned crank = grp.rank(), csize = grp.size();
+  const int sys = grp.system();  // uniform within the group
   if (sys >= a.n_sys) return;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int R0 = a.sys_row0[sys], R1 = a.sys_row0[sys + 1];
@@ -82,16 +170,11 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_gmres_cluster(const ClusterGm
   __shared__ int s_flag[2];
   int parity = 0;
 
-  // cluster all-reduce of s_slot[parity][0 .. nv) into s_red
+  bool alive = true;  // false once a grid barrier timed out: the CTA winds down
+  // group all-reduce of s_slot[parity][0 .. nv) into s_red
   auto allreduce = [&](int nv) {
-    cl.sync();
-    for (int i = tid; i < nv; i += CG_THREADS) {
-      double s = 0.0;
-      for (unsigned rk = 0; rk < csize; rk++) s += cl.map_shared_rank(&s_slot[parity][0], rk)[i];
-      s_red[i] = s;
-    }
+    alive = grp.reduce(&s_slot[parity][0], nv, s_red, parity) && alive;
     parity ^= 1;
-    __syncthreads();
   };
   // CTA sum of up to two per-thread values into s_slot[parity][0..1]
   auto block_sum2 = [&](double v0, double v1) {
@@ -142,7 +225,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_gmres_cluster(const ClusterGm
   const double bnorm2 = s_red[0];
   int total = 0, ref = 0;
   double rr = bnorm2;
-  if (bnorm2 > 0.0) {
+  if (bnorm2 > 0.0 && alive) {
     const double tol2 = a.tol * a.tol * bnorm2;
     for (ref = 0;; ref++) {
       // FP64 residual r = b - x - G x of the own rows (x complete after the barrier above / below)
@@ -168,7 +251,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_gmres_cluster(const ClusterGm
       block_sum2(prr, 0.0);
       allreduce(1);
       rr = s_red[0];
-      if (!(rr > tol2) || ref >= a.max_refine || total >= a.max_iter) break;
+      if (!(rr > tol2) || ref >= a.max_refine || total >= a.max_iter || !alive) break;
       // v0 = r / |r|
       const double beta = sqrt(rr);
       for (int r = r0 + tid; r < r1; r += CG_THREADS) a.V[r] = (float)(a.r64[r] / beta);
@@ -178,7 +261,8 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_gmres_cluster(const ClusterGm
       }
       int jdim = 0;
       for (int j = 0; j < m; j++) {
-        cl.sync();  // V[j] complete in every CTA
+        alive = grp.sync() && alive;  // V[j] complete in every CTA
+        if (!alive) break;
         // w = (I + G32) V[j], own rows
         const float* vj = a.V + (int64_t)j * K + R0;
         for (int i = tid; i < nr; i += CG_THREADS) s_vf[i] = __ldcg(vj + i);
@@ -243,7 +327,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_gmres_cluster(const ClusterGm
           float* vn = a.V + (int64_t)(j + 1) * K;
           for (int r = tid; r < nown; r += CG_THREADS) vn[r0 + r] = s_w[r] * inv;
         }
-        if (s_flag[0] || total >= a.max_iter) break;
+        if (s_flag[0] || total >= a.max_iter || !alive) break;
       }
       // y = H^-1 g (upper triangular), x += beta V y in FP64
       if (tid == 0) {
@@ -260,16 +344,28 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_gmres_cluster(const ClusterGm
         for (int i = 0; i < jdim; i++) acc += s_y[i] * (double)__ldcg(a.V + (int64_t)i * K + r);
         a.x[r] += beta * acc;
       }
-      cl.sync();  // x complete before the next residual
+      alive = grp.sync() && alive;  // x complete before the next residual
     }
   }
-  cl.sync();  // no CTA leaves while another may still read its shared memory
+  if (alive) grp.sync();  // no CTA leaves while another may still read its shared memory
   if (crank == 0 && tid == 0) {
     a.out_iters[sys] = total;
     a.out_refines[sys] = ref;
-    a.out_relres[sys] = bnorm2 > 0.0 ? sqrt(rr / bnorm2) : 0.0;
+    a.out_relres[sys] = !alive ? -1.0 : (bnorm2 > 0.0 ? sqrt(rr / bnorm2) : 0.0);
     if (a.out_t_end) a.out_t_end[sys] = global_ns();
   }
+}
+
+__global__ void __launch_bounds__(CG_THREADS, 1) k_gmres_cluster(const ClusterGmresArgs a) {
+  ClusterGroup grp;
+  gmres_body(a, grp);
+}
+
+// One system over the whole grid (cooperative launch, one CTA per SM).
+__global__ void __launch_bounds__(CG_THREADS, 1) k_gmres_grid(const ClusterGmresArgs a, unsigned* bar,
+                                                              unsigned* err, double* gpart) {
+  GridGroup grp{bar, bar + 1, err, gpart};
+  gmres_body(a, grp);
 }
 
 __global__ void k_stamp(unsigned long long* t) { *t = global_ns(); }
@@ -314,6 +410,40 @@ int gmres_cluster_pick(int max_rows) {
     cudaGetLastError();
   }
   return 0;
+}
+
+int gmres_grid_blocks(int max_rows) {
+  static int sms = -1;
+  if (sms < 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int coop = 0;
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    if (!coop) sms = 0;
+    cudaFuncSetAttribute(k_gmres_grid, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CG_SMEM_CAP);
+  }
+  if (sms <= 0) return 0;
+  const size_t smem = gmres_cluster_smem(max_rows, sms);
+  if (smem > CG_SMEM_CAP) return 0;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gmres_grid, CG_THREADS, smem) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return per_sm >= 1 ? sms : 0;
+}
+
+cudaError_t launch_gmres_grid(const ClusterGmresArgs& a, int blocks, int max_rows, unsigned* bar, unsigned* err,
+                              double* gpart, cudaStream_t s) {
+  if (a.n_sys != 1 || a.m < 2 || a.m > CG_MAXM || blocks < 1) return cudaErrorInvalidValue;
+  const size_t smem = gmres_cluster_smem(max_rows, blocks);
+  if (smem > CG_SMEM_CAP) return cudaErrorInvalidValue;
+  cudaError_t e = cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), s);
+  if (e != cudaSuccess) return e;
+  ClusterGmresArgs aa = a;
+  void* args[] = {&aa, &bar, &err, &gpart};
+  return cudaLaunchCooperativeKernel((const void*)k_gmres_grid, dim3(blocks), dim3(CG_THREADS), args, smem, s);
 }
 
 cudaError_t launch_gmres_cluster(const ClusterGmresArgs& a, int cluster, int max_rows, cudaStream_t s) {

@@ -85,12 +85,13 @@ __device__ __forceinline__ void normals_f32(uint32_t ua, uint32_t ub, float& z0,
 
 // Table-served coefficients (PK_LUT) need more live registers for the
 // bicubic accumulation: two CTAs per SM there, four otherwise.
-template <int KIND, bool RICH>
+template <int KIND, bool RICH, int GEOM>
 __global__ void __launch_bounds__(MIXED_THREADS, KIND == PK_LUT ? 2 : 4)
 k_paths_mixed(const MixedArgs a) {
   extern __shared__ float hist[];  // [sum nbins] (and the Y^2 histogram after it)
   __shared__ ItemSide s_side[4];
   __shared__ float s_rect[4];
+  __shared__ float s_dir[4];  // polar stencils: (cos, sin) of phi0 and phi1
   __shared__ int s_item, s_knot, s_p0, s_path_end, s_hist_len;
   __shared__ float s_h, s_sqrth;
   __shared__ unsigned s_next_path;
@@ -126,6 +127,12 @@ k_paths_mixed(const MixedArgs a) {
       s_next_path = (unsigned)(p0 + MIXED_THREADS);
       const int st = L.knot_stencil[k];
       for (int q = 0; q < 4; q++) s_rect[q] = (float)L.st_rect[4 * st + q];
+      if (GEOM == 1) {
+        s_dir[0] = (float)cos(L.st_rect[4 * st + 1]);
+        s_dir[1] = (float)sin(L.st_rect[4 * st + 1]);
+        s_dir[2] = (float)cos(L.st_rect[4 * st + 3]);
+        s_dir[3] = (float)sin(L.st_rect[4 * st + 3]);
+      }
       s_h = a.h;
       s_sqrth = a.sqrth;
       if (a.adaptive_h) {
@@ -134,7 +141,8 @@ k_paths_mixed(const MixedArgs a) {
         instance_params(L, k, Pk, ri, rk);
         Coef<double> kd;
         coef_f64<KIND>(Pk, L.kx[k], L.ky[k], kd);
-        const double hk = adaptive_step<double>(L.st_rect + 4 * st, L.kx[k], L.ky[k], a.h64, kd);
+        const double hk = GEOM == 1 ? adaptive_step_polar(L.st_rect + 4 * st, L.kx[k], L.ky[k], a.h64, kd)
+                                    : adaptive_step<double>(L.st_rect + 4 * st, L.kx[k], L.ky[k], a.h64, kd);
         s_h = (float)hk;
         s_sqrth = (float)sqrt(hk);
       }
@@ -153,7 +161,12 @@ k_paths_mixed(const MixedArgs a) {
           is.hist_off = off;
           is.orient = L.sd_orient[sd];
           const double delta = L.sh_delta[sh];
-          is.base = (float)(L.sd_origin[sd] + L.sh_lo[sh] - delta);
+          double origin = L.sd_origin[sd];
+          if (GEOM == 1 && is.orient == 0) {  // arc: the side's angles in this stencil's turn
+            const double tw = 6.283185307179586;
+            origin += tw * nearbyint((L.st_rect[4 * st + 1] - origin) / tw);
+          }
+          is.base = (float)(origin + L.sh_lo[sh] - delta);
           is.inv_delta = (float)(1.0 / delta);
           is.tab_off = L.sh_tab_off[sh];
           off += is.nbins;
@@ -192,6 +205,18 @@ k_paths_mixed(const MixedArgs a) {
     const float rect[4] = {s_rect[0], s_rect[1], s_rect[2], s_rect[3]};
     const float cx = 0.5f * (rect[0] + rect[2]), cy = 0.5f * (rect[1] + rect[3]);
     const float hx = rect[2] - cx, hy = rect[3] - cy;
+    // polar stencils: outside distances beyond the inner arc (none at the
+    // centre), the outer arc, the ray at phi0 and the ray at phi1 (straight
+    // lines through the centre: the wedge is narrower than pi)
+    const float ua0 = s_dir[0], ua1 = s_dir[1], ub0 = s_dir[2], ub1 = s_dir[3];
+    const bool has_inner = rect[0] > 0.f;
+    auto polar_out = [&](float x, float y, float& d_in, float& d_out, float& d_a, float& d_b) {
+      const float rho = sqrtf(x * x + y * y);
+      d_in = has_inner ? rect[0] - rho : -3.0e38f;
+      d_out = rho - rect[2];
+      d_a = ua1 * x - ua0 * y;
+      d_b = ub0 * y - ub1 * x;
+    };
     // bit d set when stencil side d lies on the global boundary
     const int globmask = (s_side[0].glob ? 1 : 0) | (s_side[1].glob ? 2 : 0) | (s_side[2].glob ? 4 : 0) |
                          (s_side[3].glob ? 8 : 0);
@@ -236,17 +261,24 @@ k_paths_mixed(const MixedArgs a) {
       s.x += k.b0 * hh + (k.s00 * i0 + k.s01 * i1);
       s.y += k.b1 * hh + (k.s10 * i0 + k.s11 * i1);
       ++s.steps;
-      const float dx = fabsf(s.x - cx) - hx, dy = fabsf(s.y - cy) - hy;
-      float nx, ny;  // |N^T sigma| for the x and y normals
-      if constexpr (KIND == PK_LUT) {
-        lut_sample<float, 8>(P.lut, s.x, s.y, s.cf);
-        nx = fabsf(s.cf[0]);
-        ny = fabsf(s.cf[1]);
+      if constexpr (GEOM == 1) {  // isotropic sigma (sqrt2 I): |N^T sigma| = sqrt2 for every normal
+        float d_in, d_out, d_a, d_b;
+        polar_out(s.x, s.y, d_in, d_out, d_a, d_b);
+        const float dist = fmaxf(fmaxf(d_in, d_out), fmaxf(d_a, d_b));
+        return !(dist < -0.5826f * 1.41421356f * sq) || s.steps >= (unsigned)a.max_steps;
       } else {
-        sigma_normals_f32<KIND>(P, s.x, s.y, nx, ny);
+        const float dx = fabsf(s.x - cx) - hx, dy = fabsf(s.y - cy) - hy;
+        float nx, ny;  // |N^T sigma| for the x and y normals
+        if constexpr (KIND == PK_LUT) {
+          lut_sample<float, 8>(P.lut, s.x, s.y, s.cf);
+          nx = fabsf(s.cf[0]);
+          ny = fabsf(s.cf[1]);
+        } else {
+          sigma_normals_f32<KIND>(P, s.x, s.y, nx, ny);
+        }
+        const float thr = -0.5826f * sq * (dx > dy ? nx : ny);
+        return !(fmaxf(dx, dy) < thr) || s.steps >= (unsigned)a.max_steps;
       }
-      const float thr = -0.5826f * sq * (dx > dy ? nx : ny);
-      return !(fmaxf(dx, dy) < thr) || s.steps >= (unsigned)a.max_steps;
     };
     // Push the exits of one level (warp-synchronous) and drain 32 if full.
     auto push = [&](bool ex, const Lvl<KIND>& s, unsigned meta) {
@@ -282,19 +314,79 @@ k_paths_mixed(const MixedArgs a) {
         float val = qS[i];
         bool ok = true;
         if (meta & 256u) {  // step limit reached: an error unless the path had exited anyway
-          float Ex, Ey, Nx, Ny;
-          int om;
-          const float dist = rect2d<float>(rect, x, y, Ex, Ey, Nx, Ny, om);
-          float g00, g01, g10, g11;
-          sigma_f32<KIND>(P, x, y, g00, g01, g10, g11);
-          const float w0 = Nx * g00 + Ny * g10, w1 = Nx * g01 + Ny * g11;
-          if (dist < -0.5826f * sqrtf(w0 * w0 + w1 * w1) * ((RICH && lvl == 0) ? sqrth * 0.70710678f : sqrth)) {
+          const float sql = (RICH && lvl == 0) ? sqrth * 0.70710678f : sqrth;
+          float dist, wn;
+          if constexpr (GEOM == 1) {
+            float d_in, d_out, d_a, d_b;
+            polar_out(x, y, d_in, d_out, d_a, d_b);
+            dist = fmaxf(fmaxf(d_in, d_out), fmaxf(d_a, d_b));
+            wn = 1.41421356f;
+          } else {
+            float Ex, Ey, Nx, Ny;
+            int om;
+            dist = rect2d<float>(rect, x, y, Ex, Ey, Nx, Ny, om);
+            float g00, g01, g10, g11;
+            sigma_f32<KIND>(P, x, y, g00, g01, g10, g11);
+            const float w0 = Nx * g00 + Ny * g10, w1 = Nx * g01 + Ny * g11;
+            wn = sqrtf(w0 * w0 + w1 * w1);
+          }
+          if (dist < -0.5826f * wn * sql) {
             atomicOr(a.err_flags, ERR_FLAG_STEP_LIMIT);
             ok = false;
             val = 0.f;
           }
         }
-        if (ok) {
+        if (ok && GEOM == 1) {
+          // polar stencil: the side with the largest outside distance (ties
+          // S, N, W, E); arcs are parameterised by the angle (measured from
+          // phi0, clamped to the stencil), rays by the radius (clamped)
+          float d_in, d_out, d_a, d_b;
+          polar_out(x, y, d_in, d_out, d_a, d_b);
+          int d = 1;
+          float mx = d_in;
+          if (d_out > mx) { mx = d_out; d = 0; }
+          if (d_a > mx) { mx = d_a; d = 3; }
+          if (d_b > mx) { mx = d_b; d = 2; }
+          float sc;
+          bool glob = false;
+          if (d <= 1) {
+            const float rel = atan2f(ua0 * y - ua1 * x, ua0 * x + ua1 * y);
+            const float ang = rect[1] + fminf(fmaxf(rel, 0.f), rect[3] - rect[1]);
+            sc = ang;
+            if (d == 0 && (globmask & 1)) {
+              glob = true;
+              float sa, ca;
+              sincosf(ang, &sa, &ca);
+              val += Y * u_f32<KIND>(P, rect[2] * ca, rect[2] * sa);
+            }
+          } else {
+            const float t = d == 3 ? ua0 * x + ua1 * y : ub0 * x + ub1 * y;
+            sc = fminf(fmaxf(t, rect[0]), rect[2]);
+          }
+          if (glob) {
+            ++nglob;
+          } else {
+            ++nsten;
+            const ItemSide& is = s_side[d];
+            if (is.n > 0) {
+              const float uu = (sc - is.base) * is.inv_delta;
+              int b0 = (int)floorf(uu);
+              b0 = max(1, min(b0, is.nbins - 3));
+              float w[4];
+              cubic_weights(uu - (float)b0, w[0], w[1], w[2], w[3]);
+              const float yw = wgt * Y;
+              float* hp = hist + is.hist_off + b0 - 1;
+#pragma unroll
+              for (int r = 0; r < 4; r++) atomicAdd(hp + r, yw * w[r]);
+              if (a.want_var) {
+                float* hq = hist2 + is.hist_off + b0 - 1;
+                const float y2 = yw * yw;
+#pragma unroll
+                for (int r = 0; r < 4; r++) atomicAdd(hq + r, y2 * w[r]);
+              }
+            }
+          }
+        } else if (ok) {
           const float dx = fabsf(x - cx) - hx, dy = fabsf(y - cy) - hy;
           const bool xs = dx > dy;
           const float Ex = xs ? (x > cx ? rect[2] : rect[0]) : fminf(fmaxf(x, rect[0]), rect[2]);
@@ -458,6 +550,7 @@ k_paths_mixed(const MixedArgs a) {
       atomicAdd(a.Bsum + knot, tb);
       atomicAdd(a.BBsum + knot, tbb);
       atomicAdd(a.stats + 0, ts);
+      if (a.knot_steps) atomicAdd(a.knot_steps + knot, ts);
       atomicAdd(a.stats + 2, tg);
       atomicAdd(a.stats + 3, tt);
     }
@@ -496,20 +589,30 @@ k_paths_mixed(const MixedArgs a) {
 
 }  // namespace
 
+// Polar stencils are instantiated for the isotropic problems only.
 template <bool RICH>
 static cudaError_t launch_mixed_t(const MixedArgs& a, int kind, int grid, size_t smem, cudaStream_t s) {
-#define PDDS_MIXED_CASE(KK)                                                                           \
-  case KK:                                                                                            \
-    cudaFuncSetAttribute(k_paths_mixed<KK, RICH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
-    k_paths_mixed<KK, RICH><<<grid, MIXED_THREADS, smem, s>>>(a);                                     \
+#define PDDS_MIXED_CASE(KK, GG)                                                                           \
+  case KK:                                                                                                \
+    cudaFuncSetAttribute(k_paths_mixed<KK, RICH, GG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+    k_paths_mixed<KK, RICH, GG><<<grid, MIXED_THREADS, smem, s>>>(a);                                     \
     break;
-  switch (kind) {
-    PDDS_MIXED_CASE(0)
-    PDDS_MIXED_CASE(1)
-    PDDS_MIXED_CASE(2)
-    PDDS_MIXED_CASE(3)
-    PDDS_MIXED_CASE(4)
-    default: return cudaErrorInvalidValue;
+  if (a.L.geom == 1) {
+    switch (kind) {
+      PDDS_MIXED_CASE(0, 1)
+      PDDS_MIXED_CASE(5, 1)
+      default: return cudaErrorInvalidValue;
+    }
+  } else {
+    switch (kind) {
+      PDDS_MIXED_CASE(0, 0)
+      PDDS_MIXED_CASE(1, 0)
+      PDDS_MIXED_CASE(2, 0)
+      PDDS_MIXED_CASE(3, 0)
+      PDDS_MIXED_CASE(4, 0)
+      PDDS_MIXED_CASE(5, 0)
+      default: return cudaErrorInvalidValue;
+    }
   }
 #undef PDDS_MIXED_CASE
   return cudaGetLastError();
@@ -522,16 +625,17 @@ cudaError_t launch_paths_mixed(const MixedArgs& a, int kind, int grid, size_t sm
 template <bool RICH>
 static int blocks_t(int kind, size_t smem) {
   int nb = 0;
-#define PDDS_OCC(KK)                                                                                 \
-  case KK:                                                                                           \
-    cudaFuncSetAttribute(k_paths_mixed<KK, RICH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_paths_mixed<KK, RICH>, MIXED_THREADS, smem); \
+#define PDDS_OCC(KK)                                                                                    \
+  case KK:                                                                                              \
+    cudaFuncSetAttribute(k_paths_mixed<KK, RICH, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_paths_mixed<KK, RICH, 0>, MIXED_THREADS, smem); \
     break;
   switch (kind) {
     PDDS_OCC(0)
     PDDS_OCC(1)
     PDDS_OCC(2)
     PDDS_OCC(4)
+    PDDS_OCC(5)
     default:
     PDDS_OCC(3)
   }

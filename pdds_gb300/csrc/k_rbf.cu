@@ -33,9 +33,10 @@ __global__ void __launch_bounds__(RBF_THREADS) k_invert(const DevLayout L, doubl
   const double c = L.sh_c[sh];
   const double* t = L.sh_t + L.sh_t_off[sh];
   const double ic2 = 1.0 / (c * c);
+  const double Rarc = L.sh_R ? L.sh_R[sh] : 0.0;  // arcs: chord 2 R sin(dphi / 2)
   for (int e = tid; e < n * n; e += RBF_THREADS) {
     const int i = e / n, j = e % n;
-    const double d = t[i] - t[j];
+    const double d = Rarc > 0.0 ? 2.0 * Rarc * sin(0.5 * (t[i] - t[j])) : t[i] - t[j];
     A[e] = exp(-(d * d) * ic2);
   }
   for (int i = tid; i < n; i += RBF_THREADS) prow[i] = i;
@@ -118,10 +119,11 @@ __global__ void __launch_bounds__(RBF_THREADS) k_tables(const DevLayout L, const
   const double* t = L.sh_t + L.sh_t_off[sh];
   const double delta = L.sh_delta[sh];
   const double s0 = L.sh_lo[sh] - delta;
+  const double Rarc = L.sh_R ? L.sh_R[sh] : 0.0;
   for (int e = tid; e < nt * n; e += RBF_THREADS) {
     const int q = e / n, j = e % n;
     const double s = s0 + (double)(b0 + q) * delta;
-    const double d = t[j] - s;
+    const double d = Rarc > 0.0 ? 2.0 * Rarc * sin(0.5 * (t[j] - s)) : t[j] - s;
     r[e] = exp(-(d * d) * ic2);
   }
   __syncthreads();

@@ -520,8 +520,10 @@ cudaError_t solve_gmres_ir_cluster(const SolveCsr& A, const double* b, double* x
   w.launches = 0;
   const int n = A.K;
   if (m < 2 || m > GMRES_CLUSTER_MAX_M) return cudaSuccess;
-  const int cl = gmres_cluster_pick(n);
-  if (cl <= 0) return cudaSuccess;
+  // large systems: the whole GPU with grid barriers; small ones: one cluster
+  const int gb = (n >= 4096 && w.bar && w.gpart && w.err) ? gmres_grid_blocks(n) : 0;
+  const int cl = gb > 0 ? 0 : gmres_cluster_pick(n);
+  if (gb <= 0 && cl <= 0) return cudaSuccess;
   *used = true;
   int* ctl = reinterpret_cast<int*>(w.ctl);  // [0..1] rows, [2] iterations, [3] refinements
   ++w.launches;
@@ -550,7 +552,7 @@ cudaError_t solve_gmres_ir_cluster(const SolveCsr& A, const double* b, double* x
   a.out_relres = w.scal;
   a.out_t_end = nullptr;
   ++w.launches;
-  cudaError_t e = launch_gmres_cluster(a, cl, n, s);
+  cudaError_t e = gb > 0 ? launch_gmres_grid(a, gb, n, w.bar, w.err, w.gpart, s) : launch_gmres_cluster(a, cl, n, s);
   if (e != cudaSuccess) return e;
   int hi[2] = {0, 0};
   double hr = 0.0;

@@ -12,6 +12,7 @@ constexpr int FP64_THREADS = 256;
 constexpr unsigned ERR_FLAG_STEP_LIMIT = 1u;
 constexpr unsigned ERR_FLAG_EXIT_SIDE = 2u;
 constexpr unsigned ERR_FLAG_SINGULAR = 4u;
+constexpr unsigned ERR_FLAG_TIMEOUT = 8u;  // a bounded device wait ran out
 
 struct MixedArgs {
   DevLayout L;
@@ -44,6 +45,7 @@ struct MixedArgs {
   const int* item_p0;
   const int* item_p1;
   const double* knot_invN;
+  unsigned long long* knot_steps;  // optional: path steps per knot (both levels)
 };
 
 struct Fp64Args {

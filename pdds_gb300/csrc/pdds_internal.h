@@ -14,6 +14,7 @@
 #pragma once
 #include <stdint.h>
 
+#include <array>
 #include <string>
 #include <vector>
 
@@ -45,6 +46,7 @@ struct SideRec {
 struct ShapeRec {
   int32_t n;
   double c;
+  double R = 0.0;         // 0: straight side (distance |t_i - t_j|); > 0: arc of radius R, t in radians
   std::vector<double> t;  // local coordinates of the knots (representative side)
   double lo, hi;          // exit extent in local coordinates (union over its sides)
   double delta;           // bin spacing
@@ -54,6 +56,14 @@ struct ShapeRec {
 };
 
 struct HostLayout {
+  // 0: rectangle split into nsub x nsub subdomains (the reference's layout);
+  // 1: disk of radius `radius` split into nrings x nsectors annular sectors,
+  //    stencils are polar rectangles rect = {rho0, phi0, rho1, phi1}, sides
+  //    are arcs (orient 0, coordinate along = angle) and rays (orient 1,
+  //    coordinate along = radius)
+  int32_t geom = 0;
+  double radius = 0.0;
+  int32_t nrings = 0, nsectors = 0;
   double sw[2], ne[2];
   int32_t nsub = 0, nnode = 0;
   double fac[4];
@@ -68,6 +78,7 @@ struct HostLayout {
   std::vector<SideRec> sides;
   std::vector<int32_t> side_knot;
   std::vector<double> side_px, side_py;
+  std::vector<double> side_along;      // polar layouts: coordinate along the side (angle or radius) - origin
   std::vector<int32_t> map_pos;        // per stencil, per side, per side knot: row position
   std::vector<uint8_t> map_owner;      // 1 if this (side, knot) writes the entry (overwrite rule)
   std::vector<ShapeRec> shapes;
@@ -80,6 +91,16 @@ struct HostLayout {
 // Returns an empty string on success, else the error text.
 std::string build_rect_layout(HostLayout& L, const double sw[2], const double ne[2], int nsub,
                               int nnode, const double fac[4], int bins_per_gap);
+
+// Disk of radius R split into nrings x nsectors annular sectors (a
+// CircleMesh): knots on the arcs between rings and on the rays between
+// sectors, nnode knots per segment (shared end points; no knot at the
+// centre), stencils = the union of the subdomains next to a knot's
+// interfaces, sides elongated by half a segment as the rectangular rule
+// does.  kappa[kind] scales the RBF shape to the side's knot spacing:
+// c = kappa[kind] * chord between neighbouring side knots.
+std::string build_circle_layout(HostLayout& L, double R, int nrings, int nsectors, int nnode,
+                                const double kappa[4], int bins_per_gap);
 
 // Block-diagonal union of independent layouts (a batch of instances): knots,
 // stencils, sides and shapes of part i follow those of part i-1 with all

@@ -14,6 +14,7 @@ struct SolveCsr {
 };
 
 struct SolveWork {
+  unsigned* err;    // device error flags (grid barrier timeouts)
   double* v64[6];   // K doubles each
   double* scal;     // 32 doubles
   double* part;     // reduction partials, >= 2*256 and 48*64 doubles
@@ -23,6 +24,8 @@ struct SolveWork {
   float* val32;     // nnz floats
   double* host_rr;  // pinned host scalar
   unsigned* ctl;    // 4 unsigned: GMRES ticket, convergence flag, basis size
+  unsigned* bar;    // 2 unsigned: grid barrier count and generation
+  double* gpart;    // grid-reduction partials, 2 * SMs * (GMRES_CLUSTER_MAX_M + 3)
   int launches;     // kernels launched by the last solve
 };
 
@@ -60,6 +63,14 @@ struct ClusterGmresArgs {
 // fit the kernel's shared-memory staging (8 max_rows + 4 max_rows / cluster bytes).
 int gmres_cluster_pick(int max_rows);
 cudaError_t launch_gmres_cluster(const ClusterGmresArgs& a, int cluster, int max_rows, cudaStream_t s);
+// One system over the whole GPU: a cooperative launch of one CTA per SM that
+// runs the same GMRES with grid barriers (bounded waits; a wait that runs out
+// sets ERR_FLAG_TIMEOUT in *err and the kernel returns).  gmres_grid_blocks
+// gives the grid (0 when the device or the system size does not allow it);
+// bar holds 2 words, gpart 2 * blocks * (GMRES_CLUSTER_MAX_M + 3) doubles.
+int gmres_grid_blocks(int max_rows);
+cudaError_t launch_gmres_grid(const ClusterGmresArgs& a, int blocks, int max_rows, unsigned* bar, unsigned* err,
+                              double* gpart, cudaStream_t s);
 // Writes %globaltimer (ns) to *t when the stream reaches it.
 cudaError_t launch_stamp(unsigned long long* t, cudaStream_t s);
 // b[i] = (float)a[i]

@@ -54,3 +54,19 @@ def test_adaptive_paths_follow_the_rule_and_continue_streams():
         assert np.quantile(se, 0.95) < 0.5 * EPS
         u, _ = pd.solve_interface()
         assert np.sqrt(np.mean((u - bvp.u(pd.x, pd.y)) ** 2)) < 3e-2
+
+
+def test_autotuner_keeps_results_and_picks_a_valid_shape():
+    """The tuned launch shape changes only the work split: every (knot, path)
+    keeps its Philox stream, so the estimate equals the untuned one up to
+    summation order."""
+    fac = fac_rule(2.0, NSUB, NNODE)
+    bvp = P.BVP.poisson_sincos()
+    with P.PDDSparseGM(SW, NE, NSUB, NNODE, fac) as pd:
+        before = pd.estimate(bvp, 3000, H, mode=P.MODE_MIXED, seed=4, adaptive_h=True, richardson=True)
+        t = pd.autotune(bvp, 3000, H, sample_knots=64, adaptive_h=True, richardson=True)
+        assert 1 <= t["blocks_per_sm"] <= 8 and 1 <= t["paths_per_item"] <= 3000
+        assert t["candidates"] >= 2 and 0 < t["best_ms"] <= t["default_ms"] * 1.2  # timing noise
+        after = pd.estimate(bvp, 3000, H, mode=P.MODE_MIXED, seed=4, adaptive_h=True, richardson=True)
+        assert np.max(np.abs(after.B - before.B)) < 1e-9
+        assert np.max(np.abs(after.val - before.val)) < 1e-5
