@@ -200,6 +200,50 @@ def many_instance_batch(local: int, n_inst: int = 256, reps: int = 3, npaths: in
     return out
 
 
+def circle_uneven(local: int, reps: int = 3, h: float = 1e-3):
+    """Uneven path lengths on the unit disk: 6 rings x 16 sectors (the central
+    ring one disk subdomain), 11 knots per segment, Poisson with
+    u = r^2 sin(3 theta) + cos x; per-knot adaptive step (knots near their
+    stencil side take steps down to ~1e-6, so mean path lengths span orders
+    of magnitude), Richardson pair, variance-adaptive paths per knot
+    N_k in [1e3, 1e5] for a score standard error of 1e-3, the launch shape
+    picked by the autotuner.  The FP64 form runs the same layout with 1e3
+    paths per knot for the MIXED/FP64 comparison."""
+    import pdds_gb300 as P
+    bvp = P.BVP.circle_poisson()
+    pd = P.PDDSparseGM.circle_mesh(1.0, 6, 16, 11, device=local)
+    ex = bvp.u(pd.x, pd.y)
+    opts = dict(adaptive_h=True, richardson=True, dup_sum=True)
+    tune = pd.autotune(bvp, 1000, h, adaptive_h=True, richardson=True)
+    runs = []
+    for r in range(reps + 1):
+        est = pd.estimate(bvp, 1000, h, mode=P.MODE_MIXED, seed=1234, instance=r, adaptive_n=True,
+                          npaths_max=100_000, target_stderr=1e-3, **opts)
+        u, si = pd.solve_interface()
+        if r > 0:
+            runs.append((est, u, si))
+    est, u, si = runs[-1]
+    steps = pd.knot_steps().astype(np.float64)
+    mc = est.npaths > 0
+    per_path = steps[mc] / (2.0 * est.npaths[mc])  # both levels of the pair count; per level
+    ms = [e.info["ms_setup"] + e.info["ms_paths"] + s_["ms"] for e, _, s_ in runs]
+    out = {"knots": int(pd.K), "paths_per_knot_min": int(est.npaths[mc].min()),
+           "paths_per_knot_max": int(est.npaths[mc].max()), "paths": int(est.info["paths"]),
+           "path_steps": int(est.info["path_steps"]), "ms_per_step": float(np.mean(ms)),
+           "path_steps_per_s": float(np.mean([e.info["path_steps"] / (m / 1000.0) for (e, _, _), m in zip(runs, ms)])),
+           "mean_steps_per_path_min": float(per_path.min()), "mean_steps_per_path_max": float(per_path.max()),
+           "rmse_vs_analytic": float(np.sqrt(np.mean((u - ex) ** 2))), "solver_iterations": int(si["iterations"]),
+           "autotune": tune}
+    m = pd.estimate(bvp, 1000, h, mode=P.MODE_MIXED, seed=77, **opts)
+    f = pd.estimate(bvp, 1000, h, mode=P.MODE_FP64, seed=77, **opts)
+    tm = m.info["ms_setup"] + m.info["ms_paths"]
+    tf = f.info["ms_setup"] + f.info["ms_paths"]
+    out["fp64"] = {"ms_estimate": tf, "mixed_ms_estimate": tm, "mixed_over_fp64": tf / tm,
+                   "G_max_abs": float(np.max(np.abs(m.val - f.val))), "B_max_abs": float(np.max(np.abs(m.B - f.B)))}
+    pd.close()
+    return out
+
+
 def run_reference(args, workload, fac):
     rank, world, _ = _env_rank()
     if rank != 0:
@@ -238,6 +282,7 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-circle", action="store_true")
     args = ap.parse_args()
 
     from pdds_gb300.config import WORKLOADS, fac_rule
@@ -365,6 +410,8 @@ def main():
 
     if not args.no_batch and rank == 0:
         extra["many_instance_batch"] = many_instance_batch(local)
+    if not args.no_circle and rank == 0:
+        extra["circle_uneven_lengths"] = circle_uneven(local)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

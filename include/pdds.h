@@ -112,8 +112,13 @@ pdds_status pdds_layout_build(pdds_ctx* ctx, const pdds_layout_desc* desc, pdds_
  * rings and the rays between sectors, nnode per segment, none at the centre;
  * stencils are the polar rectangles of the subdomains next to a knot's
  * interfaces, sides elongated by half a segment as on rectangles; the RBF
- * shape of a side is kappa[kind] times its knot spacing (chord).  MIXED and
- * FP64 modes (no replay form); problems with sigma = sqrt2 I (PDDS_POISSON_SINCOS,
+ * shape of a side is kappa[kind] times its knot spacing (chord).  The central
+ * ring is one disk subdomain (no rays): the stencil of a knot on its boundary
+ * is the disk of radius 2R/nrings with one periodic side.  A knot shared by
+ * two sides of a stencil gets both sides' weights (dup_sum is implied: the
+ * overwrite of the rectangular reference leaves cond(I + G) ~100 here but
+ * biases G).  MIXED and FP64 modes (no replay form); problems with
+ * sigma = sqrt2 I (PDDS_POISSON_SINCOS,
  * PDDS_CIRCLE_POISSON).  pdds_layout_stencil reports rect = {rho0, phi0,
  * rho1, phi1} with sides N = outer arc, S = inner arc, E = ray at phi1,
  * W = ray at phi0. */

@@ -279,7 +279,7 @@ pdds_status enqueue_mixed_paths(pdds_ctx* ctx, const pdds_estimate_desc* desc, c
   a.paths_per_chunk = ppc;
   a.n_items = n_items;
   a.want_var = desc->want_var ? 1 : 0;
-  a.dup_sum = desc->dup_sum;
+  a.dup_sum = ctx->L.geom == 1 ? 1 : desc->dup_sum;  // circle layouts sum shared side knots
   a.adaptive_h = desc->adaptive_h ? 1 : 0;
   a.richardson = desc->richardson ? 1 : 0;
   a.h64 = desc->h;
@@ -719,7 +719,7 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
     a.GG = ctx->GG.p;
     a.B = ctx->B.p;
     a.BB = ctx->BB.p;
-    a.dup_sum = desc->dup_sum;
+    a.dup_sum = ctx->L.geom == 1 ? 1 : desc->dup_sum;  // circle layouts sum shared side knots
     a.err_flags = ctx->errf.p;
     CK(launch_replay_paths(a, P.kind, s));
     CK(launch_replay_reduce(a, P.kind, ctx->task_m.p, ctx->task_d.p, ctx->task_i.p, (int)tm.size(),
@@ -766,7 +766,7 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
       a.chunks = chunks;
       a.paths_per_chunk = ppc;
       a.n_items = n_items;
-      a.dup_sum = desc->dup_sum;
+      a.dup_sum = ctx->L.geom == 1 ? 1 : desc->dup_sum;  // circle layouts sum shared side knots
       a.adaptive_h = desc->adaptive_h ? 1 : 0;
       a.richardson = desc->richardson ? 1 : 0;
       a.max_steps = max_steps;

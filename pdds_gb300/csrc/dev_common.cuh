@@ -477,8 +477,10 @@ __device__ __forceinline__ double adaptive_step_polar(const double* rect, double
   const double rho = sqrt(x0 * x0 + y0 * y0);
   double d = rho - rect[2];
   if (rect[0] > 0.0) d = fmax(d, rect[0] - rho);
-  d = fmax(d, sin(rect[1]) * x0 - cos(rect[1]) * y0);
-  d = fmax(d, cos(rect[3]) * y0 - sin(rect[3]) * x0);
+  if (rect[3] - rect[1] < 6.2) {  // a full disk has no rays
+    d = fmax(d, sin(rect[1]) * x0 - cos(rect[1]) * y0);
+    d = fmax(d, cos(rect[3]) * y0 - sin(rect[3]) * x0);
+  }
   if (!(d <= -1e-04)) return h0;
   const double q = d / (fabs((double)k.s00) * 2 * 0.5826);
   const double ha = q * q;

@@ -174,7 +174,9 @@ k_paths_fp64(const Fp64Args a) {
         const double rho = ::sqrt(s.x * s.x + s.y * s.y);
         const double d_in = rect[0] > 0.0 ? rect[0] - rho : -1e300;
         const double d_out = rho - rect[2];
-        const double d_a = pa1 * s.x - pa0 * s.y, d_b = pb0 * s.y - pb1 * s.x;
+        const bool has_rays = rect[3] - rect[1] < 6.2;  // a full disk has one side, its arc
+        const double d_a = has_rays ? pa1 * s.x - pa0 * s.y : -1e300;
+        const double d_b = has_rays ? pb0 * s.y - pb1 * s.x : -1e300;
         int d = 1;
         double mx = d_in;
         if (d_out > mx) { mx = d_out; d = 0; }
@@ -189,7 +191,8 @@ k_paths_fp64(const Fp64Args a) {
         double along, Ex = 0.0, Ey = 0.0;
         if (d <= 1) {
           const double rel = ::atan2(pa0 * s.y - pa1 * s.x, pa0 * s.x + pa1 * s.y);
-          along = rect[1] + ::fmin(::fmax(rel, 0.0), rect[3] - rect[1]);
+          along = rect[1] + (has_rays ? ::fmin(::fmax(rel, 0.0), rect[3] - rect[1])
+                                      : (rel < 0.0 ? rel + 6.283185307179586 : rel));
           ::sincos(along, &Ey, &Ex);
           Ex *= rect[d == 0 ? 2 : 0];
           Ey *= rect[d == 0 ? 2 : 0];

@@ -210,12 +210,13 @@ k_paths_mixed(const MixedArgs a) {
     // lines through the centre: the wedge is narrower than pi)
     const float ua0 = s_dir[0], ua1 = s_dir[1], ub0 = s_dir[2], ub1 = s_dir[3];
     const bool has_inner = rect[0] > 0.f;
+    const bool has_rays = rect[3] - rect[1] < 6.2f;  // a full disk has one side, its arc
     auto polar_out = [&](float x, float y, float& d_in, float& d_out, float& d_a, float& d_b) {
       const float rho = sqrtf(x * x + y * y);
       d_in = has_inner ? rect[0] - rho : -3.0e38f;
       d_out = rho - rect[2];
-      d_a = ua1 * x - ua0 * y;
-      d_b = ub0 * y - ub1 * x;
+      d_a = has_rays ? ua1 * x - ua0 * y : -3.0e38f;
+      d_b = has_rays ? ub0 * y - ub1 * x : -3.0e38f;
     };
     // bit d set when stencil side d lies on the global boundary
     const int globmask = (s_side[0].glob ? 1 : 0) | (s_side[1].glob ? 2 : 0) | (s_side[2].glob ? 4 : 0) |
@@ -351,7 +352,8 @@ k_paths_mixed(const MixedArgs a) {
           bool glob = false;
           if (d <= 1) {
             const float rel = atan2f(ua0 * y - ua1 * x, ua0 * x + ua1 * y);
-            const float ang = rect[1] + fminf(fmaxf(rel, 0.f), rect[3] - rect[1]);
+            const float ang = rect[1] + (has_rays ? fminf(fmaxf(rel, 0.f), rect[3] - rect[1])
+                                                  : (rel < 0.f ? rel + 6.28318531f : rel));
             sc = ang;
             if (d == 0 && (globmask & 1)) {
               glob = true;

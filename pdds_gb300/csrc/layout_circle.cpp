@@ -4,8 +4,12 @@
 // PDDAlgorithms/PDDSparseGM.cpp:346-689; its Circle* mesh files are empty
 // stubs).  This layout applies the same rules in polar coordinates:
 //   * interfaces are the arcs rho = rho_i between rings (one per sector) and
-//     the rays phi = theta_j between sectors (one per ring), nnode knots per
-//     segment with shared end points (cross points), no knot at the centre;
+//     the rays phi = theta_j between sectors (one per ring outside the
+//     central disk, which is one subdomain: sectors meeting at the centre make
+//     (I + G) nearly singular, cond ~1e4 against ~30 on rectangles), nnode
+//     knots per segment with shared end points (cross points);
+//   * knots on the central disk's boundary take the disk of radius rho_2 as
+//     stencil, whose one side is the whole second arc (periodic);
 //   * a knot's stencil is the union of the subdomains next to its
 //     interfaces (two for a segment knot, four for a cross point), a polar
 //     rectangle {rho0, phi0, rho1, phi1};
@@ -94,7 +98,7 @@ std::string circle_stencils(HostLayout& L, double R, int NR, int NS, int n, cons
     Pending P;
     const double ang = dth * jj;
     const int j = wrap(jj);
-    if (p >= 1) {
+    if (p >= 2) {  // ring 0 has no rays
       const PolarIface& a = rays[(size_t)(p - 1) * NS + j];
       P.kind++;
       add_from(P, a, 0.0, (int)((1 - STEN_ELONG) * (a.index.size() - 1)), (int)a.index.size(), false, ang);
@@ -122,6 +126,7 @@ std::string circle_stencils(HostLayout& L, double R, int NR, int NS, int n, cons
       continue;
     }
     const int p = st4[0], q = st4[1], s = st4[2], w = st4[3];
+    const bool full = (w == NS);  // the disk of radius rho_q: one periodic arc side
     StencilRec st;
     st.rect[0] = drho * p;
     st.rect[1] = dth * s;
@@ -130,12 +135,21 @@ std::string circle_stencils(HostLayout& L, double R, int NR, int NS, int n, cons
     Pending sides[4];
     bool has[4] = {false, false, false, false};
     for (int d = 0; d < 4; d++) st.glob[d] = 0;
-    if (q < NR) { sides[DIR_N] = arc_side(q, s, w); has[DIR_N] = true; } else { st.glob[DIR_N] = 1; }
-    if (p > 0) { sides[DIR_S] = arc_side(p, s, w); has[DIR_S] = true; }
-    sides[DIR_E] = ray_side(p, q, s + w);
-    has[DIR_E] = true;
-    sides[DIR_W] = ray_side(p, q, s);
-    has[DIR_W] = true;
+    if (full) {
+      if (q >= NR) return "internal: full-circle stencil on the boundary";
+      Pending& P = sides[DIR_N];
+      for (int jj = 0; jj < NS; jj++) add_from(P, arcs[(size_t)q * NS + jj], 0.0, 0,
+                                               (int)arcs[(size_t)q * NS + jj].index.size() - 1, true, drho * q);
+      P.kind = 3;
+      has[DIR_N] = true;
+    } else {
+      if (q < NR) { sides[DIR_N] = arc_side(q, s, w); has[DIR_N] = true; } else { st.glob[DIR_N] = 1; }
+      if (p > 0) { sides[DIR_S] = arc_side(p, s, w); has[DIR_S] = true; }
+      sides[DIR_E] = ray_side(p, q, s + w);
+      has[DIR_E] = true;
+      sides[DIR_W] = ray_side(p, q, s);
+      has[DIR_W] = true;
+    }
     for (int d = 0; d < 4; d++) {
       st.side[d] = -1;
       st.kind[d] = has[d] ? sides[d].kind : -3;
@@ -313,13 +327,11 @@ std::string build_circle_layout(HostLayout& L, double R, int NR, int NS, int n, 
     }
   std::vector<int> bnd(NS);
   for (int j = 0; j < NS; j++) bnd[j] = add_knot(R, theta(j));
-  for (int i = 0; i < NR; i++)
+  for (int i = 1; i < NR; i++)  // the central disk (ring 0) has no rays
     for (int j = 0; j < NS; j++) {
       PolarIface& f = rays[(size_t)i * NS + j];
-      if (i > 0) {
-        f.index.push_back(cross[(size_t)i * NS + j]);
-        f.along.push_back(rho(i));
-      }
+      f.index.push_back(cross[(size_t)i * NS + j]);
+      f.along.push_back(rho(i));
       for (int k = 1; k < n - 1; k++) {
         const double r = rho(i) + drho * k / (n - 1);
         f.index.push_back(add_knot(r, theta(j)));
@@ -338,17 +350,20 @@ std::string build_circle_layout(HostLayout& L, double R, int NR, int NS, int n, 
   L.nboundary = NS;
   // ---- stencil of every knot: rings [p, q), sectors [s, s + w)
   std::vector<std::array<int, 4>> kst(K, {-1, -1, -1, -1});
+  // knots on the first arc (the central disk's boundary): the disk of radius
+  // rho_2 (the central disk and the first ring), a stencil with one side,
+  // the whole second arc
   for (int i = 1; i < NR; i++)
     for (int j = 0; j < NS; j++) {
       const PolarIface& f = arcs[(size_t)i * NS + j];
-      for (size_t k = 1; k + 1 < f.index.size(); k++) kst[f.index[k]] = {i - 1, i + 1, j, 1};
-      kst[cross[(size_t)i * NS + j]] = {i - 1, i + 1, j - 1, 2};
+      for (size_t k = 1; k + 1 < f.index.size(); k++) kst[f.index[k]] = i == 1 ? std::array<int, 4>{0, 2, 0, NS}
+                                                                               : std::array<int, 4>{i - 1, i + 1, j, 1};
+      kst[cross[(size_t)i * NS + j]] = i == 1 ? std::array<int, 4>{0, 2, 0, NS} : std::array<int, 4>{i - 1, i + 1, j - 1, 2};
     }
-  for (int i = 0; i < NR; i++)
+  for (int i = 1; i < NR; i++)
     for (int j = 0; j < NS; j++) {
       const PolarIface& f = rays[(size_t)i * NS + j];
-      const size_t b = (i > 0) ? 1 : 0;
-      for (size_t k = b; k + 1 < f.index.size(); k++) kst[f.index[k]] = {i, i + 1, j - 1, 2};
+      for (size_t k = 1; k + 1 < f.index.size(); k++) kst[f.index[k]] = {i, i + 1, j - 1, 2};
       if (i == NR - 1) kst[f.index.back()] = {i, i + 1, j - 1, 2};  // boundary knot: no paths, B = g
     }
   return circle_stencils(L, R, NR, NS, n, kappa, bps, arcs, rays, kst);

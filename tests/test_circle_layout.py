@@ -22,14 +22,16 @@ def pd():
 def polar_outside(rect, x, y):
     r0, p0, r1, p1 = rect
     rho = np.hypot(x, y)
-    d = [rho - r1, np.sin(p0) * x - np.cos(p0) * y, np.cos(p1) * y - np.sin(p1) * x]
+    d = [rho - r1]
+    if p1 - p0 < 6.2:
+        d += [np.sin(p0) * x - np.cos(p0) * y, np.cos(p1) * y - np.sin(p1) * x]
     if r0 > 0:
         d.append(r0 - rho)
     return max(d)
 
 
 def test_knots(pd):
-    K = (NR - 1) * NS * (N - 1) + NR * NS * (N - 2) + NS
+    K = (NR - 1) * NS * (N - 1) + (NR - 1) * NS * (N - 2) + NS  # no rays in the central disk
     assert pd.K == K
     r = np.hypot(pd.x, pd.y)
     assert r.max() <= 1.0 + 1e-12 and r.min() > 0.0
@@ -63,6 +65,8 @@ def test_stencils_and_rows(pd):
         a, b = pd.row_ptr[k], pd.row_ptr[k + 1]
         assert sorted(cols) == pd.col[a:b].tolist()
         assert (r0 == 0.0) == (len(sides[1]) == 0)     # no inner arc at the centre
+        if p1 - p0 > 6.2:  # the central disk's stencil: one periodic arc, no rays
+            assert len(sides[2]) == 0 and len(sides[3]) == 0 and len(sides[0]) == NS * (N - 1)
         assert (abs(r1 - 1.0) < 1e-12) == (len(sides[0]) == 0)  # outer arc on the boundary: no knots
 
 
