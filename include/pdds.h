@@ -313,6 +313,21 @@ pdds_status pdds_batch_run(pdds_ctx* ctx, const pdds_batch_run_desc* desc, pdds_
 pdds_status pdds_batch_instance(pdds_ctx* ctx, int32_t i, int32_t* nknots, double* x, double* y, double* u,
                                 double* B, int32_t* iterations, double* rel_residual, double* latency_ms);
 
+/* ---------------------------------------------------------------- subdomain solve
+ * Interior solution of every subdomain of a rectangular layout from the
+ * interface solution (the reference hands each subdomain's four interfaces
+ * to an Octave spectral solver, Subdomain::Solve, Meshes/subdomain.cpp:80-122).
+ * For problems whose operator is Lap + c with constant c (PDDS_POISSON_SINCOS,
+ * PDDS_MONEGROS, PDDS_HELMHOLTZ): one CTA per subdomain solves the 5-point
+ * finite-difference problem on an m x m interior grid (2 <= m <= 64) by the
+ * sine transform, in FP64, with Dirichlet data = the interface solution
+ * interpolated along each edge (cubic Lagrange through its knots) and g on
+ * the domain boundary.  u: interface values u[K] (host), or NULL for those of
+ * the last pdds_solve_interface.  out[nsub*nsub][m][m]: subdomain
+ * s = column + nsub * row, value [j][i] at x = x0 + (i+1) lx/(m+1),
+ * y = y0 + (j+1) ly/(m+1) of its rectangle [x0, x0+lx] x [y0, y0+ly]. */
+pdds_status pdds_subdomain_solve(pdds_ctx* ctx, int32_t m, const double* u, double* out);
+
 /* ---------------------------------------------------------------- allocation-free solve
  * No counterpart in the reference.  For callers that cannot let a library
  * allocate GPU memory (memory owned by another allocator, serving loops where

@@ -25,7 +25,7 @@ SOLVE_BICGSTAB_FP64, SOLVE_GMRES_FP32_IR = 0, 1
 EXPORTS = [
     "pdds_create", "pdds_destroy", "pdds_last_error", "pdds_version", "pdds_problem_set", "pdds_problem_set_lut",
     "pdds_layout_build", "pdds_layout_build_circle", "pdds_layout_knots", "pdds_layout_csr", "pdds_layout_stencil",
-    "pdds_estimate", "pdds_estimate_knot_paths", "pdds_estimate_knot_steps", "pdds_autotune", "pdds_solve_interface", "pdds_batch_build", "pdds_batch_run", "pdds_batch_instance",
+    "pdds_estimate", "pdds_estimate_knot_paths", "pdds_estimate_knot_steps", "pdds_autotune", "pdds_solve_interface", "pdds_subdomain_solve", "pdds_batch_build", "pdds_batch_run", "pdds_batch_instance",
     "pdds_solve_bicgstab_static",
 ]
 STATIC_SOLVE_MAX_K = 131072
@@ -133,6 +133,7 @@ def load(path: str = LIB_PATH):
     L.pdds_autotune.argtypes = [vp, C.POINTER(EstimateDesc), C.c_int32, C.POINTER(TuneInfo)]
     L.pdds_estimate_knot_steps.argtypes = [vp, C.POINTER(C.c_int64)]
     L.pdds_estimate_knot_paths.argtypes = [vp, C.POINTER(C.c_int32)]
+    L.pdds_subdomain_solve.argtypes = [vp, C.c_int32, dp, dp]
     L.pdds_solve_interface.argtypes = [vp, C.POINTER(SolveDesc), dp, C.POINTER(SolveInfo)]
     L.pdds_batch_build.argtypes = [vp, C.POINTER(InstanceDesc), C.c_int32, C.POINTER(BatchInfo)]
     L.pdds_batch_run.argtypes = [vp, C.POINTER(BatchRunDesc), C.POINTER(BatchRunInfo)]

@@ -342,6 +342,23 @@ class PDDSparseGM:
         self._check(self._lib.pdds_estimate_knot_steps(self._ctx, _p(st, C.c_int64)))
         return st
 
+    def subdomain_solve(self, m: int = 32, u=None):
+        """Interior solution of every subdomain (the reference's Subdomain::Solve):
+        returns (x, y, v) with v[row, col, j, i] at x[col, i], y[row, j] on an
+        m x m interior grid per subdomain.  u: interface values (default: the
+        last solve_interface)."""
+        ns = self.nsub
+        out = np.zeros((ns * ns, m, m))
+        keep = None if u is None else np.ascontiguousarray(u, np.float64)
+        self._check(self._lib.pdds_subdomain_solve(self._ctx, int(m), None if keep is None else _p(keep, C.c_double),
+                                                   _p(out, C.c_double)))
+        lx = (self.ne[0] - self.sw[0]) / ns
+        ly = (self.ne[1] - self.sw[1]) / ns
+        t = (np.arange(m) + 1.0) / (m + 1)
+        x = self.sw[0] + (np.arange(ns)[:, None] + t[None, :]) * lx
+        y = self.sw[1] + (np.arange(ns)[:, None] + t[None, :]) * ly
+        return x, y, out.reshape(ns, ns, m, m)
+
     def write_outputs(self, directory: str, est: "Estimate", u, bvp: BVP):
         """Writes Output/solution.csv and Output/Debug/{G,G_var,B,B_var}.csv
         under directory in the reference's format (Compute_Solution,

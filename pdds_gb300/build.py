@@ -31,6 +31,7 @@ UNITS = {
     "k_solve.cu": [],
     "k_gmres_cluster.cu": [],
     "batch.cu": [],
+    "k_subdomain.cu": [],
     "layout.cpp": ["-x", "cu"],
     "layout_circle.cpp": ["-x", "cu"],
     "noalloc.cu": [],

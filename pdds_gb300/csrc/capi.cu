@@ -35,6 +35,8 @@ void drop_graph(pdds_ctx* ctx) {
 
 pdds_status upload_layout(pdds_ctx* ctx) {
   drop_graph(ctx);  // the buffers below may move
+  ctx->edges_ready = false;
+  ctx->has_solution = false;
   HostLayout& L = ctx->L;
   cudaStream_t s = ctx->stream;
   std::vector<double> st_rect;
@@ -457,6 +459,9 @@ pdds_status pdds_destroy(pdds_ctx* ctx) {
     ctx->rng_dev.release();
     ctx->knot_N.release();
     ctx->knot_steps.release();
+    ctx->edge_knots.release();
+    ctx->sub_u.release();
+    ctx->sub_out.release();
     ctx->item_knot.release();
     ctx->item_p0.release();
     ctx->item_p1.release();
@@ -942,6 +947,65 @@ pdds_status pdds_autotune(pdds_ctx* ctx, const pdds_estimate_desc* desc, int32_t
   return PDDS_OK;
 }
 
+pdds_status pdds_subdomain_solve(pdds_ctx* ctx, int32_t m, const double* u, double* out) {
+  if (!ctx || !out) return PDDS_ERR_INVALID;
+  if (ctx->device < 0) return fail(ctx, PDDS_ERR_INVALID, "context has no device");
+  if (!ctx->has_layout || ctx->L.geom != 0 || ctx->is_batch)
+    return fail(ctx, PDDS_ERR_INVALID, "subdomain solves need a rectangular layout");
+  if (!ctx->has_problem) return fail(ctx, PDDS_ERR_INVALID, "no problem set");
+  const int kind = ctx->prob.kind;
+  if (kind != PDDS_POISSON_SINCOS && kind != PDDS_MONEGROS && kind != PDDS_HELMHOLTZ)
+    return fail(ctx, PDDS_ERR_INVALID, "subdomain solves take operators Lap + c (Poisson, Monegros, Helmholtz)");
+  if (m < 2 || m > 64) return fail(ctx, PDDS_ERR_INVALID, "2 <= m <= 64");
+  if (!u && !ctx->has_solution) return fail(ctx, PDDS_ERR_INVALID, "no interface solution");
+  CK(cudaSetDevice(ctx->device));
+  cudaStream_t s = ctx->stream;
+  const HostLayout& L = ctx->L;
+  const int ns = L.nsub, n = L.nnode, S = ns * ns;
+  if (!ctx->edges_ready) {
+    // knots of every subdomain edge, ordered along it, from the knot positions
+    const double lx = (L.ne[0] - L.sw[0]) / ns, ly = (L.ne[1] - L.sw[1]) / ns;
+    const double tol = 1e-9 * std::max(lx, ly);
+    std::vector<int> ek((size_t)S * 4 * n, -1);
+    for (int b = 0; b < ns; b++)
+      for (int a = 0; a < ns; a++) {
+        const int sub = a + ns * b;
+        const double x0 = L.sw[0] + a * lx, y0 = L.sw[1] + b * ly;
+        for (int d = 0; d < 4; d++) {
+          const bool on_bnd = (d == 0 && b == 0) || (d == 1 && b == ns - 1) || (d == 2 && a == 0) || (d == 3 && a == ns - 1);
+          if (on_bnd) continue;
+          std::vector<std::pair<double, int>> hit;
+          for (int v = 0; v < L.K; v++) {
+            const double x = L.kx[v], y = L.ky[v];
+            if (d <= 1) {
+              const double yl = d == 0 ? y0 : y0 + ly;
+              if (std::fabs(y - yl) < tol && x > x0 - tol && x < x0 + lx + tol) hit.push_back({x, v});
+            } else {
+              const double xl = d == 2 ? x0 : x0 + lx;
+              if (std::fabs(x - xl) < tol && y > y0 - tol && y < y0 + ly + tol) hit.push_back({y, v});
+            }
+          }
+          if ((int)hit.size() != n) return fail(ctx, PDDS_ERR_INVALID, "internal: subdomain edge knot count");
+          std::sort(hit.begin(), hit.end());
+          for (int q = 0; q < n; q++) ek[((size_t)sub * 4 + d) * n + q] = hit[q].second;
+        }
+      }
+    CK(ctx->edge_knots.upload(ek, s));
+    ctx->edges_ready = true;
+  }
+  const double* ud = ctx->su.p;
+  if (u) {
+    CK(ctx->sub_u.resize(std::max(L.K, 1)));
+    CK(cudaMemcpyAsync(ctx->sub_u.p, u, L.K * sizeof(double), cudaMemcpyHostToDevice, s));
+    ud = ctx->sub_u.p;
+  }
+  CK(ctx->sub_out.resize((size_t)S * m * m));
+  CK(launch_subdomain(ctx->dl, problem_dev(ctx), ns, m, n, ctx->edge_knots.p, ud, ctx->sub_out.p, s));
+  CK(cudaMemcpyAsync(out, ctx->sub_out.p, (size_t)S * m * m * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return PDDS_OK;
+}
+
 pdds_status pdds_estimate_knot_steps(pdds_ctx* ctx, int64_t* steps) {
   if (!ctx || !steps) return PDDS_ERR_INVALID;
   if (!ctx->has_estimate || !ctx->has_knot_steps) return fail(ctx, PDDS_ERR_INVALID, "no MIXED estimate on this layout");
@@ -1016,6 +1080,7 @@ pdds_status pdds_solve_interface(pdds_ctx* ctx, const pdds_solve_desc* desc, dou
   CK(cudaEventRecord(ctx->ev1, s));
   if (u) CK(cudaMemcpyAsync(u, ctx->su.p, K * sizeof(double), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
+  ctx->has_solution = true;
   if (info) {
     float ms = 0.f;
     cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);

@@ -103,6 +103,11 @@ struct pdds_ctx {
   std::vector<unsigned char> graph_key;
   int graph_launches = 0;
   bool has_batch_run = false;
+  // subdomain solves: knots of each subdomain edge (S, N, W, E; -1 = domain boundary)
+  DBuf<int> edge_knots;
+  DBuf<double> sub_u, sub_out;
+  bool edges_ready = false;
+  bool has_solution = false;
   // autotuned launch shape of the MIXED path kernel (0 = defaults)
   int tune_bps = 0, tune_ppc = 0, tune_kind = -1, tune_rich = -1;
   int force_bps = 0;             // CTAs per SM imposed while the autotuner times a shape

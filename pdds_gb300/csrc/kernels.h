@@ -123,6 +123,10 @@ cudaError_t launch_scale_rows(const int* mc, int n, const int64_t* row_ptr, cons
 cudaError_t launch_finalize_n(const int* mc_knots, int n_mc, const int* knot_N, const double* Bsum,
                               const double* BBsum, double* B, double* BB, int64_t nnz, const double* G,
                               double* GG_to_var, int want_var, cudaStream_t s);
+// Subdomain interior solves (k_subdomain.cu).
+size_t subdomain_smem(int m);
+cudaError_t launch_subdomain(const DevLayout& L, const ProblemDev& P, int nsub, int m, int n, const int* edge_knots,
+                             const double* u, double* out, cudaStream_t s);
 cudaError_t launch_finalize(const int* mc_knots, int n_mc, int N, const double* Bsum,
                             const double* BBsum, double* B, double* BB, const int64_t* row_ptr,
                             int64_t nnz, const double* G, double* GG_to_var, int want_var,
