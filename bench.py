@@ -168,13 +168,13 @@ def many_instance_batch(local: int, n_inst: int = 256, reps: int = 3, npaths: in
     bt = P.Batch(P.BVP.HELMHOLTZ, insts, device=local)
     t_build = time.perf_counter() - t0
     bt.run(npaths, h, seed=1234, instance=0, use_graph=True, richardson=False)
-    plain = bt.run(npaths, h, seed=1234, instance=500, use_graph=True, richardson=False)
+    plain = bt.run(npaths, h, seed=1234, instance=500, use_graph=True, richardson=False)  # reference's weight rule
     plain_rmse = []
     for i, ins in enumerate(insts):
         x, y = bt.knots(i)
         plain_rmse.append(float(np.sqrt(np.mean((bt.result(i)["u"] - P.BVP.helmholtz(*ins.params).u(x, y)) ** 2))))
-    bt.run(npaths, h, seed=1234, instance=0, use_graph=True, richardson=True)  # capture + warm-up
-    runs = [bt.run(npaths, h, seed=1234, instance=1000 * (r + 1), use_graph=True, richardson=True)
+    bt.run(npaths, h, seed=1234, instance=0, use_graph=True, richardson=True, dup_sum=True)  # capture + warm-up
+    runs = [bt.run(npaths, h, seed=1234, instance=1000 * (r + 1), use_graph=True, richardson=True, dup_sum=True)
             for r in range(reps)]
     lat, rmse, iters = [], [], []
     for i, ins in enumerate(insts):
@@ -318,7 +318,9 @@ def main():
     exact = bvp.u(pd.x, pd.y)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
-    OPTS = dict(adaptive_h=True, richardson=True)
+    # the consistent weight rule for knots shared by two stencil sides (the
+    # reference's overwrite is the API default, checked by the parity tests)
+    OPTS = dict(adaptive_h=True, richardson=True, dup_sum=True)
 
     def step(instance, mode=P.MODE_MIXED, method=P.SOLVE_GMRES_FP32_IR, **opts):
         o = dict(OPTS)
@@ -365,7 +367,7 @@ def main():
     extra = {}
     # the reference's plain method (no adaptive step, no extrapolation), MIXED
     if rank == 0:
-        estp, up, sp = step(999, adaptive_h=False, richardson=False)
+        estp, up, sp = step(999, adaptive_h=False, richardson=False, dup_sum=False)
         tp = (estp.info["ms_setup"] + estp.info["ms_paths"] + sp["ms"]) / 1000.0
         extra["plain_method"] = {"path_steps_per_s": estp.info["path_steps"] / tp, "ms_per_step": 1000 * tp,
                                  "path_steps": estp.info["path_steps"],
@@ -439,7 +441,8 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
         "config": {"workload": workload["name"], "knots": pd.K, "paths_per_knot": N, "h": h,
                    "mode": "MIXED", "adaptive_h": True, "richardson": "h/2,h",
-                   "solver": "GMRES(30) FP32 + FP64 refinement", "l2": "flushed (256 MB write)"},
+                   "solver": "GMRES(30) FP32 + FP64 refinement", "l2": "flushed (256 MB write)",
+                   "shared_side_knots": "weights summed (dup_sum)"},
         "interface_solves_per_s": args.steps / t_dev,
         "rmse_vs_analytic": float(np.mean(rmses)),
         "solve_ms": float(np.mean(solve_ms)),

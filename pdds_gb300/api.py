@@ -465,7 +465,7 @@ class Batch:
 
     def run(self, npaths: int, h: float, seed: int = 1234, instance: int = 0, adaptive_h: bool = True,
             richardson: bool = False, tol: float = 1e-10, restart: int = 30, use_graph: bool = True,
-            bins_per_gap: int = 0, reuse_tables: bool = False) -> dict:
+            bins_per_gap: int = 0, reuse_tables: bool = False, dup_sum: bool = False) -> dict:
         """Estimates and solves every instance; returns the run counters."""
         d = capi.BatchRunDesc()
         e = d.estimate
@@ -478,6 +478,7 @@ class Batch:
         e.adaptive_h = int(bool(adaptive_h))
         e.richardson = int(bool(richardson))
         e.reuse_tables = int(bool(reuse_tables))
+        e.dup_sum = int(bool(dup_sum))
         d.solve.method = capi.SOLVE_GMRES_FP32_IR
         d.solve.restart = int(restart)
         d.solve.tol = float(tol)

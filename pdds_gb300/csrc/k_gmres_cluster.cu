@@ -168,6 +168,7 @@ __device__ __forceinline__ void gmres_body(const ClusterGmresArgs& a, Group& grp
   __shared__ double s_cs[CG_MAXM], s_sn[CG_MAXM], s_g[CG_MAXV], s_y[CG_MAXM];
   __shared__ double s_bsum[CG_WARPS][2];
   __shared__ int s_flag[2];
+  __shared__ double s_hn;
   int parity = 0;
 
   bool alive = true;  // false once a grid barrier timed out: the CTA winds down
@@ -290,16 +291,31 @@ __device__ __forceinline__ void gmres_body(const ClusterGmresArgs& a, Group& grp
         for (int i = tid; i < nv; i += CG_THREADS) s_h[i] = s_red[i];
         __syncthreads();
         subtract(nv, s_h);
-        basis_dots(nv);
-        allreduce(nv);
-        // second pass: w -= V h2, h += h2, then |w|^2
-        subtract(nv, s_red);
+        // second pass: h2 = V^T w and |w|^2 in one reduction; then w -= V h2,
+        // h += h2 and |w - V h2|^2 = |w|^2 - |h2|^2 (V orthonormal)
+        {
+          double pn = 0.0;
+          for (int r = tid; r < nown; r += CG_THREADS) pn += (double)s_w[r] * (double)s_w[r];
+          pn = warp_sum(pn);
+          if (lane == 0) s_bsum[warp][0] = pn;
+        }
+        basis_dots(nv);  // ends with __syncthreads: s_bsum complete
+        if (tid == 0) {
+          double t0 = 0.0;
+          for (int q = 0; q < CG_WARPS; q++) t0 += s_bsum[q][0];
+          s_slot[parity][nv] = t0;
+        }
+        __syncthreads();
+        allreduce(nv + 1);
+        subtract(nv, s_red);  // ends with __syncthreads
+        if (tid == 0) {  // one thread: FP64 throughput is scarce on this GPU
+          double h2sq = 0.0;
+          for (int i = 0; i < nv; i++) h2sq += s_red[i] * s_red[i];
+          s_hn = sqrt(fmax(s_red[nv] - h2sq, 0.0));
+        }
         for (int i = tid; i < nv; i += CG_THREADS) s_h[i] += s_red[i];
-        double pn = 0.0;
-        for (int r = tid; r < nown; r += CG_THREADS) pn += (double)s_w[r] * (double)s_w[r];
-        block_sum2(pn, 0.0);
-        allreduce(1);
-        const double hn = sqrt(s_red[0]);
+        __syncthreads();
+        const double hn = s_hn;
         if (tid == 0) {
           double* col = s_H + j * (m + 1);
           for (int i = 0; i <= j; i++) col[i] = s_h[i];
