@@ -203,6 +203,8 @@ std::string build_rect_layout(HostLayout& L, const double sw[2], const double ne
   L.knot_boundary.assign(L.K, 0);
   std::vector<Lab> tmp;
   const double STEN_ELONG = 0.5;
+  std::vector<int> lastq(L.K, -1);            // scratch: last insertion of a knot on a side
+  std::vector<int64_t> last_writer(L.K, -1);  // scratch: last (side, knot) map entry of a knot
   for (int v = 0; v < L.K; v++) {
     const std::vector<int>& ki = knot_ifs[v];
     auto it = stencil_key.find(ki);
@@ -288,8 +290,6 @@ std::string build_rect_layout(HostLayout& L, const double sw[2], const double ne
       st.kind[d] = kind[d];
       st.side[d] = -1;
       if (sidx[d].empty()) continue;
-      std::map<int, std::pair<double, double>> pos;
-      for (size_t q = 0; q < sidx[d].size(); q++) pos[sidx[d][q]] = {spx[d][q], spy[d][q]};
       std::vector<int> idx = sidx[d];
       idx.erase(std::unique(idx.begin(), idx.end()), idx.end());
       int kd = kind[d];
@@ -304,11 +304,14 @@ std::string build_rect_layout(HostLayout& L, const double sw[2], const double ne
         sr.c = fac[kd];
         sr.shape = -1;
         sr.knot_off = (int64_t)L.side_knot.size();
+        // the last written position of each index (scratch array over knots)
+        for (size_t q = 0; q < sidx[d].size(); q++) lastq[sidx[d][q]] = (int)q;
         for (int v2 : idx) {
           L.side_knot.push_back(v2);
-          L.side_px.push_back(pos[v2].first);
-          L.side_py.push_back(pos[v2].second);
+          L.side_px.push_back(spx[d][lastq[v2]]);
+          L.side_py.push_back(spy[d][lastq[v2]]);
         }
+        for (int v2 : sidx[d]) lastq[v2] = -1;
         sr.origin = (sr.orient == 0) ? L.side_px[sr.knot_off] : L.side_py[sr.knot_off];
         sr.fixed = (sr.orient == 0) ? L.side_py[sr.knot_off] : L.side_px[sr.knot_off];
         L.max_side = std::max(L.max_side, sr.n);
@@ -340,7 +343,6 @@ std::string build_rect_layout(HostLayout& L, const double sw[2], const double ne
     st.cols = cols;
     st.row_len = (int)cols.size();
     st.map_off = (int64_t)L.map_pos.size();
-    std::map<int, int64_t> last_writer;
     for (int d = 0; d < 4; d++) {
       if (st.side[d] < 0) continue;
       const SideRec& sr = L.sides[st.side[d]];
@@ -352,7 +354,10 @@ std::string build_rect_layout(HostLayout& L, const double sw[2], const double ne
         L.map_owner.push_back(0);
       }
     }
-    for (auto& kv : last_writer) L.map_owner[kv.second] = 1;
+    for (int v2 : cols) {  // the last side that wrote a knot owns its entry
+      L.map_owner[last_writer[v2]] = 1;
+      last_writer[v2] = -1;
+    }
     const int sid = (int)L.stencils.size();
     stencil_key[ki] = sid;
     L.knot_stencil[v] = sid;
