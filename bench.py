@@ -394,21 +394,32 @@ def main():
     e2e = None
     if not args.no_e2e:
         h2d = d2h = 0
+        ph = {"layout": 0.0, "estimate": 0.0, "solve": 0.0, "close": 0.0}
         t0 = time.perf_counter()
         e2e_steps = 0
         for s in range(max(1, min(args.steps, 3))):
-            with P.PDDSparseGM(workload["sw"], workload["ne"], workload["nsub"], workload["nnode"], fac,
-                               device=local) as q:
-                u2, est2, si2 = q.Solve(bvp, N, h, mode=P.MODE_MIXED, seed=1234, instance=50 + s, **OPTS)
-                e2e_steps += est2.info["path_steps"]
-                K, nnz = q.K, q.nnz
+            ta = time.perf_counter()
+            q = P.PDDSparseGM(workload["sw"], workload["ne"], workload["nsub"], workload["nnode"], fac,
+                              device=local)
+            tb = time.perf_counter()
+            est2 = q.estimate(bvp, N, h, mode=P.MODE_MIXED, seed=1234, instance=50 + s, **OPTS)
+            tc = time.perf_counter()
+            u2, si2 = q.solve_interface()
+            td = time.perf_counter()
+            e2e_steps += est2.info["path_steps"]
+            K, nnz = q.K, q.nnz
+            q.close()
+            te = time.perf_counter()
+            for k, v in zip(ph, (tb - ta, tc - tb, td - tc, te - td)):
+                ph[k] += v
         dt = time.perf_counter() - t0
         ns = max(1, min(args.steps, 3))
         # layout arrays uploaded (knots, stencils, sides, shapes, CSR) and results read back
         h2d = K * (8 + 8 + 4 + 8) + nnz * 4 + 4096
         d2h = nnz * 16 + K * 24
         e2e = {"value": e2e_steps / dt, "unit": "path-steps/s", "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h), "ms_per_step": 1000 * dt / ns}
+               "d2h_bytes_per_step": int(d2h), "ms_per_step": 1000 * dt / ns,
+               "phases_ms": {k: round(1000 * v / ns, 2) for k, v in ph.items()}}
 
     if not args.no_batch and rank == 0:
         extra["many_instance_batch"] = many_instance_batch(local)

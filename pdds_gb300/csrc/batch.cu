@@ -28,9 +28,7 @@ pdds_status enqueue_batch(pdds_ctx* ctx, const pdds_batch_run_desc* d, int clust
   const int64_t nnz = ctx->L.row_ptr[ctx->L.K];
   CK(launch_stamp(ctx->b_tend.p + n, s));
   ++*launches;
-  ctx->rng_override = ctx->rng_dev.p;
   pdds_status st = enqueue_mixed(ctx, &d->estimate, launches);
-  ctx->rng_override = nullptr;
   if (st != PDDS_OK) return st;
   CK(launch_to_f32(ctx->G.p, ctx->sval32.p, nnz, s));
   ++*launches;
@@ -108,8 +106,6 @@ pdds_status pdds_batch_build(pdds_ctx* ctx, const pdds_instance_desc* inst, int3
     CK(ctx->b_refines.resize(n));
     CK(ctx->b_relres.resize(n));
     CK(ctx->b_tend.resize(n + 1));
-    CK(ctx->rng_dev.resize(2));
-    if (!ctx->rng_host) CK(cudaMallocHost(&ctx->rng_host, 2 * sizeof(unsigned long long)));
     pdds_status st = upload_layout(ctx);
     if (st != PDDS_OK) return st;
     CK(cudaStreamSynchronize(s));
@@ -165,7 +161,8 @@ pdds_status pdds_batch_run(pdds_ctx* ctx, const pdds_batch_run_desc* desc, pdds_
   // the graph is reused while the descriptor, the cluster size and the solve
   // scratch (which pdds_solve_interface may also reallocate) are unchanged;
   // layout, problem and table changes drop it where they happen
-  // seed and instance live in device memory (rng_dev), not in the graph
+  // seed and instance are not part of the key: a replay re-keys the
+  // path-kernel nodes' parameters
   pdds_batch_run_desc kd = *desc;
   kd.estimate.seed = 0;
   kd.estimate.instance = 0;
@@ -175,9 +172,6 @@ pdds_status pdds_batch_run(pdds_ctx* ctx, const pdds_batch_run_desc* desc, pdds_
   std::memcpy(key.data() + sizeof(pdds_batch_run_desc) + sizeof(int), after, sizeof(after));
   int launches = 0;
   bool replayed = false;
-  ctx->rng_host[0] = ed.seed;
-  ctx->rng_host[1] = ed.instance;
-  CK(cudaMemcpyAsync(ctx->rng_dev.p, ctx->rng_host, 2 * sizeof(unsigned long long), cudaMemcpyHostToDevice, s));
   if (desc->use_graph) {
     if (!ctx->graph_exec || ctx->graph_key != key) {
       drop_graph(ctx);
@@ -195,8 +189,31 @@ pdds_status pdds_batch_run(pdds_ctx* ctx, const pdds_batch_run_desc* desc, pdds_
       CK(cudaGraphInstantiate(&ctx->graph_exec, ctx->graph, 0));
       ctx->graph_key = key;
       ctx->graph_launches = nl;
+      size_t nn = 0;
+      CK(cudaGraphGetNodes(g, nullptr, &nn));
+      std::vector<cudaGraphNode_t> nodes(nn);
+      if (nn) CK(cudaGraphGetNodes(g, nodes.data(), &nn));
+      for (cudaGraphNode_t nd : nodes) {
+        cudaGraphNodeType ty;
+        CK(cudaGraphNodeGetType(nd, &ty));
+        if (ty != cudaGraphNodeTypeKernel) continue;
+        cudaKernelNodeParams p;
+        CK(cudaGraphKernelNodeGetParams(nd, &p));
+        if (is_mixed_path_kernel(p.func)) ctx->graph_path_nodes.push_back(nd);
+      }
     } else {
       replayed = true;
+      // the path kernels of this run draw the streams of its seed and instance
+      for (cudaGraphNode_t nd : ctx->graph_path_nodes) {
+        cudaKernelNodeParams p;
+        CK(cudaGraphKernelNodeGetParams(nd, &p));
+        MixedArgs ma = *static_cast<const MixedArgs*>(p.kernelParams[0]);
+        mixed_set_rng(ma, ed.seed, (uint32_t)ed.instance);
+        void* args[1] = {&ma};
+        p.kernelParams = args;
+        p.extra = nullptr;
+        CK(cudaGraphExecKernelNodeSetParams(ctx->graph_exec, nd, &p));
+      }
     }
     launches = ctx->graph_launches;
     CK(cudaEventRecord(ctx->ev0, s));

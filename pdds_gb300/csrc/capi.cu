@@ -31,6 +31,7 @@ void drop_graph(pdds_ctx* ctx) {
   ctx->graph = nullptr;
   ctx->graph_key.clear();
   ctx->graph_launches = 0;
+  ctx->graph_path_nodes.clear();
 }
 
 pdds_status upload_layout(pdds_ctx* ctx) {
@@ -275,8 +276,7 @@ pdds_status enqueue_mixed_paths(pdds_ctx* ctx, const pdds_estimate_desc* desc, c
   a.h = (float)desc->h;
   a.sqrth = (float)std::sqrt(desc->h);
   a.inv_N = 1.0 / N;
-  a.seed = desc->seed;
-  a.instance = desc->instance;
+  mixed_set_rng(a, desc->seed, desc->instance);
   a.chunks = chunks;
   a.paths_per_chunk = ppc;
   a.n_items = n_items;
@@ -294,7 +294,6 @@ pdds_status enqueue_mixed_paths(pdds_ctx* ctx, const pdds_estimate_desc* desc, c
   a.BBsum = ctx->BBsum.p;
   a.stats = ctx->stats.p;
   a.err_flags = ctx->errf.p;
-  a.rng_dev = ctx->rng_override;
   a.item_knot = items ? items->knot : nullptr;
   a.item_p0 = items ? items->p0 : nullptr;
   a.item_p1 = items ? items->p1 : nullptr;
@@ -456,7 +455,6 @@ pdds_status pdds_destroy(pdds_ctx* ctx) {
     ctx->inst_pd.release();
     ctx->b_relres.release();
     ctx->b_tend.release();
-    ctx->rng_dev.release();
     ctx->knot_N.release();
     ctx->knot_steps.release();
     ctx->edge_knots.release();
@@ -467,7 +465,6 @@ pdds_status pdds_destroy(pdds_ctx* ctx) {
     ctx->item_p1.release();
     ctx->knot_scale.release();
     ctx->knot_invN.release();
-    if (ctx->rng_host) cudaFreeHost(ctx->rng_host);
     if (ctx->host_rr) cudaFreeHost(ctx->host_rr);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);

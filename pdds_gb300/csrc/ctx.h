@@ -102,6 +102,7 @@ struct pdds_ctx {
   cudaGraphExec_t graph_exec = nullptr;
   std::vector<unsigned char> graph_key;
   int graph_launches = 0;
+  std::vector<cudaGraphNode_t> graph_path_nodes;  // path-kernel nodes, re-keyed per run
   bool has_batch_run = false;
   // subdomain solves: knots of each subdomain edge (S, N, W, E; -1 = domain boundary)
   DBuf<int> edge_knots;
@@ -118,10 +119,6 @@ struct pdds_ctx {
   std::vector<int> last_knot_N;  // paths per knot of the last estimate
   DBuf<unsigned long long> knot_steps;  // path steps per knot of the last MIXED estimate
   bool has_knot_steps = false;
-  // {seed, instance} read by the path kernel of a batch sequence
-  DBuf<unsigned long long> rng_dev;
-  unsigned long long* rng_host = nullptr;  // pinned staging of rng_dev
-  const unsigned long long* rng_override = nullptr;
 };
 
 namespace pdds {

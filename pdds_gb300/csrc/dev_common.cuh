@@ -170,6 +170,24 @@ __device__ __forceinline__ T lut_sample_g(const LutDev& L, T x, T y) {
   return out;
 }
 
+// Single-precision approximations (the PTX .approx forms, flush-to-zero) for
+// the FP32 path, whose Euler step error is far above their rounding.
+__device__ __forceinline__ float sqrt_approx(float x) {
+  float y;
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float rsqrt_approx(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float lg2_approx(float x) {
+  float y;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 template <typename T>
 struct Coef {
   T s00, s01, s10, s11;  // sigma, row-major
@@ -225,9 +243,10 @@ __device__ __forceinline__ void coef_f32(const ProblemDev& P, float x, float y, 
     // cos 3t = 4c^3 - 3c; f = -Lap u = 5 sin 3t + cos x (bounded, continuous
     // away from r = 0); grad u = (2r sin3t c - 3r cos3t s - sin x,
     // 2r sin3t s + 3r cos3t c)
-    const float r = sqrtf(x * x + y * y);
-    const float ir = r > 1e-30f ? 1.f / r : 0.f;
-    const float c1 = r > 1e-30f ? x * ir : 1.f, s1 = y * ir;
+    const float r2 = x * x + y * y;
+    const float ir = r2 > 1e-30f ? rsqrt_approx(r2) : 0.f;
+    const float r = r2 * ir;
+    const float c1 = r2 > 1e-30f ? x * ir : 1.f, s1 = y * ir;
     const float s3 = s1 * (3.f - 4.f * s1 * s1), c3 = c1 * (4.f * c1 * c1 - 3.f);
     float sx, cx;
     __sincosf(x, &sx, &cx);
@@ -239,7 +258,8 @@ __device__ __forceinline__ void coef_f32(const ProblemDev& P, float x, float y, 
   } else {  // PK_MONEGROS (BVPs/EDPs/Monegros_Poisson_CPP.hpp)
     const float k2 = 0.01f, k3 = 0.02f, k4 = 0.12f, k5 = 0.05f, k6 = 0.05f, k7 = -0.12f, sf = 0.333f;
     const float q = 1.f + k2 * x * x + k3 * y * y;
-    const float a1 = sqrtf(q);
+    const float ia1 = rsqrt_approx(q);  // q >= 1
+    const float a1 = q * ia1;
     float s1, c1, sA, cA, sB, cB;
     __sincosf(a1, &s1, &c1);
     __sincosf(k4 * x + k5 * y, &sA, &cA);
@@ -247,18 +267,30 @@ __device__ __forceinline__ void coef_f32(const ProblemDev& P, float x, float y, 
     const float a2 = tanhf(sA + sB);
     const float m = a2 * a2 - 1.f;
     const float p4 = k4 * cA + k6 * cB, p5 = k5 * cA + k7 * cB;
-    const float dxx = ((k2 / a1) - (k2 * k2 * x * x / (a1 * a1 * a1))) * c1 - (x * x * k2 * k2 / (a1 * a1)) * s1 +
+    const float ia2 = ia1 * ia1, ia3 = ia2 * ia1;
+    const float dxx = ((k2 * ia1) - (k2 * k2 * x * x * ia3)) * c1 - (x * x * k2 * k2 * ia2) * s1 +
                       2.f * p4 * p4 * m * a2 + (k4 * k4 * sA + k6 * k6 * sB) * m;
-    const float dyy = ((k3 / a1) - (k3 * k3 * y * y / (a1 * a1 * a1))) * c1 - (y * y * k3 * k3 / (a1 * a1)) * s1 +
+    const float dyy = ((k3 * ia1) - (k3 * k3 * y * y * ia3)) * c1 - (y * y * k3 * k3 * ia2) * s1 +
                       2.f * p5 * p5 * m * a2 + (k5 * k5 * sA + k7 * k7 * sB) * m;
     k.s00 = 1.41421356237f; k.s01 = 0.f; k.s10 = 0.f; k.s11 = 1.41421356237f;
     k.b0 = 0.f; k.b1 = 0.f; k.c = 0.f;
     k.f = -sf * dxx - sf * dyy;
-    k.g0 = sf * (c1 * k2 * x / a1 - p4 * m);
-    k.g1 = sf * (c1 * k3 * y / a1 - p5 * m);
+    k.g0 = sf * (c1 * k2 * x * ia1 - p4 * m);
+    k.g1 = sf * (c1 * k3 * y * ia1 - p5 * m);
   }
-  if (!P.use_cv) { k.g0 = 0.f; k.g1 = 0.f; }
+  // the control variate is switched off by the caller (P.use_cv), which
+  // drops the accumulated xi at the exit instead of zeroing g every step
 }
+
+// Terms of the FP32 step that a problem kind has, known at compile time:
+// sigma is diagonal for every kind; iso kinds have sigma = sqrt2 I and no
+// drift; react kinds have a reaction term c.
+template <int KIND>
+struct KindTraits {
+  static constexpr bool iso =
+      KIND == PK_POISSON_SINCOS || KIND == PK_MONEGROS || KIND == PK_HELMHOLTZ || KIND == PK_CIRCLE;
+  static constexpr bool react = KIND == PK_HELMHOLTZ || KIND == PK_VARCOEF || KIND == PK_LUT;
+};
 
 // sigma alone (for the exit threshold)
 template <int KIND>

@@ -71,16 +71,40 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
 }
 
 // Box-Muller in FP32 from two Philox words: z0 = rho cos(2 pi u1),
-// z1 = rho sin(2 pi u1), evaluated as -rho cos/sin(2 pi u1 - pi) so the fast
-// intrinsics see an argument in [-pi, pi).
+// z1 = rho sin(2 pi u1) with rho = sqrt(-2 ln u0), u = (word + 1/2) 2^-32,
+// evaluated as -rho cos/sin(a) at a = 2 pi u1 - pi in [-pi, pi], which the
+// fast intrinsics take directly (a is formed from the word in one FMA).
 __device__ __forceinline__ void normals_f32(uint32_t ua, uint32_t ub, float& z0, float& z1) {
   const float u0 = fmaf((float)ua, 2.3283064e-10f, 1.1641532e-10f);
-  const float u1 = fmaf((float)ub, 2.3283064e-10f, 1.1641532e-10f);
-  const float rho = sqrtf(-2.f * __logf(u0));
+  const float rho = sqrt_approx(-1.38629436f * lg2_approx(u0));  // -2 ln u0 = -2 ln2 log2 u0
+  const float ang = fmaf((float)ub, 1.46291808e-9f, -3.14159265f);
   float sn, cs;
-  __sincosf(6.28318531f * (u1 - 0.5f), &sn, &cs);
+  __sincosf(ang, &sn, &cs);
   z0 = -rho * cs;
   z1 = -rho * sn;
+}
+
+// path_block (counter = (step pair, path, knot, instance)) with the key
+// schedule read from the kernel parameters: the same stream.
+__device__ __forceinline__ u32x4 path_block_rk(const uint32_t (&rk)[20], uint32_t instance, uint32_t knot,
+                                               uint32_t path, uint32_t step_pair) {
+  u32x4 c;
+  c.v[0] = step_pair;
+  c.v[1] = path;
+  c.v[2] = knot;
+  c.v[3] = instance;
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint32_t hi0 = __umulhi(0xD2511F53u, c.v[0]), lo0 = 0xD2511F53u * c.v[0];
+    const uint32_t hi1 = __umulhi(0xCD9E8D57u, c.v[2]), lo1 = 0xCD9E8D57u * c.v[2];
+    u32x4 n;
+    n.v[0] = hi1 ^ c.v[1] ^ rk[2 * r];
+    n.v[1] = lo1;
+    n.v[2] = hi0 ^ c.v[3] ^ rk[2 * r + 1];
+    n.v[3] = lo0;
+    c = n;
+  }
+  return c;
 }
 
 // Table-served coefficients (PK_LUT) need more live registers for the
@@ -185,8 +209,7 @@ k_paths_mixed(const MixedArgs a) {
     const int knot = s_knot, path_end = s_path_end, hist_len = s_hist_len;
     // the problem of this knot's instance, and its Philox instance and knot words
     ProblemDev P = a.P;
-    const uint64_t seed = a.rng_dev ? (uint64_t)a.rng_dev[0] : a.seed;
-    uint32_t rng_inst = a.rng_dev ? (uint32_t)a.rng_dev[1] : a.instance, rng_knot = 0;
+    uint32_t rng_inst = a.instance, rng_knot = 0;
     instance_params(L, knot, P, rng_inst, rng_knot);
     const float h = s_h, sqrth = s_sqrth;
     const int nh = a.want_var ? 2 * hist_len : hist_len;
@@ -212,7 +235,7 @@ k_paths_mixed(const MixedArgs a) {
     const bool has_inner = rect[0] > 0.f;
     const bool has_rays = rect[3] - rect[1] < 6.2f;  // a full disk has one side, its arc
     auto polar_out = [&](float x, float y, float& d_in, float& d_out, float& d_a, float& d_b) {
-      const float rho = sqrtf(x * x + y * y);
+      const float rho = sqrt_approx(x * x + y * y);
       d_in = has_inner ? rect[0] - rho : -3.0e38f;
       d_out = rho - rect[2];
       d_a = has_rays ? ua1 * x - ua0 * y : -3.0e38f;
@@ -237,6 +260,13 @@ k_paths_mixed(const MixedArgs a) {
     unsigned* qm = s_qm[warp];
     for (int q = 0; q < NSLOT; q++) s_pst[warp][q][lane] = 0;
     const int halves = RICH ? 2 : 1;
+    const bool use_cv = P.use_cv != 0;
+    // increment scales (sqrt2 sqrt(h) for iso kinds, sqrt(h) otherwise) and
+    // Gobet thresholds of the fine (h/2) and coarse (h) levels
+    const float hf = 0.5f * h;
+    const float scc = KindTraits<KIND>::iso ? 1.41421356f * sqrth : sqrth;
+    const float scf = scc * 0.70710678f;
+    const float thrc = -0.5826f * scc, thrf = -0.5826f * scf;
 
     // One step of a level (Step, control-variate variant,
     // FKACIntegrator.hpp:46-57) and the Gobet-shifted exit test (Inside,
@@ -244,41 +274,50 @@ k_paths_mixed(const MixedArgs a) {
     // reference's signed distance is max(dx, dy) except in the outer corner
     // region (where both are positive and the path exits anyway), and its
     // normal is the x normal exactly when dx > dy.
-    auto advance = [&](Lvl<KIND>& s, float i0, float i1, float hh, float sq) -> bool {
+    // Every kind has a diagonal sigma.  For iso kinds (sigma = sqrt2 I) e is
+    // the diffusion increment sqrt2 dW and thr the shift -0.5826 sqrt2 sqrt(h);
+    // otherwise e = dW and thr = -0.5826 sqrt(h), scaled by |N^T sigma| here.
+    // The control-variate sum xi = -sum Y grad u . sigma dW is always
+    // accumulated; the exit drops it when the control variate is off.
+    auto advance = [&](Lvl<KIND>& s, float e0, float e1, float hh, float thr) -> bool {
       Coef<float> k;
       if constexpr (KIND == PK_LUT) {
-        k.s00 = s.cf[0]; k.s01 = 0.f; k.s10 = 0.f; k.s11 = s.cf[1];
+        k.s00 = s.cf[0]; k.s11 = s.cf[1];
         k.b0 = s.cf[2]; k.b1 = s.cf[3]; k.c = s.cf[4]; k.f = s.cf[5];
-        k.g0 = P.use_cv ? s.cf[6] : 0.f;
-        k.g1 = P.use_cv ? s.cf[7] : 0.f;
+        k.g0 = s.cf[6]; k.g1 = s.cf[7];
       } else {
         coef_f32<KIND>(P, s.x, s.y, k);
       }
-      const float v0 = -(k.s00 * k.g0 + k.s10 * k.g1);
-      const float v1 = -(k.s01 * k.g0 + k.s11 * k.g1);
-      s.xi += s.Y * (v0 * i0 + v1 * i1);
+      float d0 = e0, d1 = e1;
+      if constexpr (!KindTraits<KIND>::iso) { d0 = k.s00 * e0; d1 = k.s11 * e1; }
+      s.xi -= s.Y * (k.g0 * d0 + k.g1 * d1);
       s.Z += k.f * s.Y * hh;
-      s.Y += k.c * s.Y * hh;
-      s.x += k.b0 * hh + (k.s00 * i0 + k.s01 * i1);
-      s.y += k.b1 * hh + (k.s10 * i0 + k.s11 * i1);
+      if constexpr (KindTraits<KIND>::react) s.Y += k.c * s.Y * hh;
+      if constexpr (KindTraits<KIND>::iso) {
+        s.x += d0;
+        s.y += d1;
+      } else {
+        s.x += k.b0 * hh + d0;
+        s.y += k.b1 * hh + d1;
+      }
       ++s.steps;
-      if constexpr (GEOM == 1) {  // isotropic sigma (sqrt2 I): |N^T sigma| = sqrt2 for every normal
+      if constexpr (GEOM == 1) {  // iso kinds only: |N^T sigma| = sqrt2 for every normal
         float d_in, d_out, d_a, d_b;
         polar_out(s.x, s.y, d_in, d_out, d_a, d_b);
         const float dist = fmaxf(fmaxf(d_in, d_out), fmaxf(d_a, d_b));
-        return !(dist < -0.5826f * 1.41421356f * sq) || s.steps >= (unsigned)a.max_steps;
+        return !(dist < thr) || s.steps >= (unsigned)a.max_steps;
       } else {
         const float dx = fabsf(s.x - cx) - hx, dy = fabsf(s.y - cy) - hy;
-        float nx, ny;  // |N^T sigma| for the x and y normals
+        float t = thr;
         if constexpr (KIND == PK_LUT) {
           lut_sample<float, 8>(P.lut, s.x, s.y, s.cf);
-          nx = fabsf(s.cf[0]);
-          ny = fabsf(s.cf[1]);
-        } else {
+          t *= dx > dy ? fabsf(s.cf[0]) : fabsf(s.cf[1]);
+        } else if constexpr (!KindTraits<KIND>::iso) {
+          float nx, ny;  // |N^T sigma| for the x and y normals
           sigma_normals_f32<KIND>(P, s.x, s.y, nx, ny);
+          t *= dx > dy ? nx : ny;
         }
-        const float thr = -0.5826f * sq * (dx > dy ? nx : ny);
-        return !(fmaxf(dx, dy) < thr) || s.steps >= (unsigned)a.max_steps;
+        return !(fmaxf(dx, dy) < t) || s.steps >= (unsigned)a.max_steps;
       }
     };
     // Push the exits of one level (warp-synchronous) and drain 32 if full.
@@ -289,7 +328,7 @@ k_paths_mixed(const MixedArgs a) {
         qx[i] = s.x;
         qy[i] = s.y;
         qY[i] = s.Y;
-        qS[i] = s.Z + s.xi;
+        qS[i] = use_cv ? s.Z + s.xi : s.Z;
         qm[i] = meta | (s.steps >= (unsigned)a.max_steps ? 256u : 0u);
       }
       qcount += __popc(mk);
@@ -470,7 +509,7 @@ k_paths_mixed(const MixedArgs a) {
     while (__any_sync(FULL, active)) {
       bool fx = false, cx_ = false;  // exits in this iteration
       if (active) {
-        const u32x4 blk = path_block(seed, rng_inst, rng_knot, path, m++);
+        const u32x4 blk = path_block_rk(a.rk, rng_inst, rng_knot, path, m++);
         float za0, za1, zb0, zb1;
         normals_f32(blk.v[0], blk.v[1], za0, za1);
         normals_f32(blk.v[2], blk.v[3], zb0, zb1);
@@ -478,13 +517,13 @@ k_paths_mixed(const MixedArgs a) {
           // Richardson pair: two fine steps of h/2 and one coarse step of h
           // on the same Brownian increments (dW_coarse = dW_fine1 + dW_fine2);
           // 2 E[fine] - E[coarse] cancels the O(h) bias
-          const float hf = 0.5f * h, sqf = sqrth * 0.70710678f;
-          if (f_alive) fx = advance(F, sqf * za0, sqf * za1, hf, sqf);
-          if (f_alive && !fx) fx = advance(F, sqf * zb0, sqf * zb1, hf, sqf);
-          if (c_alive) cx_ = advance(Cs, sqf * (za0 + zb0), sqf * (za1 + zb1), h, sqrth);
+          const float ea0 = scf * za0, ea1 = scf * za1, eb0 = scf * zb0, eb1 = scf * zb1;
+          if (f_alive) fx = advance(F, ea0, ea1, hf, thrf);
+          if (f_alive && !fx) fx = advance(F, eb0, eb1, hf, thrf);
+          if (c_alive) cx_ = advance(Cs, ea0 + eb0, ea1 + eb1, h, thrc);
         } else {
-          fx = advance(F, sqrth * za0, sqrth * za1, h, sqrth);
-          if (!fx) fx = advance(F, sqrth * zb0, sqrth * zb1, h, sqrth);
+          fx = advance(F, scc * za0, scc * za1, h, thrc);
+          if (!fx) fx = advance(F, scc * zb0, scc * zb1, h, thrc);
         }
       }
       const unsigned meta0 = (unsigned)lane | ((unsigned)gen << 6);
@@ -619,6 +658,27 @@ static cudaError_t launch_mixed_t(const MixedArgs& a, int kind, int grid, size_t
 #undef PDDS_MIXED_CASE
   return cudaGetLastError();
 }
+
+void mixed_set_rng(MixedArgs& a, uint64_t seed, uint32_t instance) {
+  uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+  for (int r = 0; r < 10; r++) {
+    a.rk[2 * r] = k0;
+    a.rk[2 * r + 1] = k1;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  a.instance = instance;
+}
+
+template <bool RICH>
+static bool is_mixed_t(const void* f) {
+  return f == (const void*)k_paths_mixed<0, RICH, 0> || f == (const void*)k_paths_mixed<1, RICH, 0> ||
+         f == (const void*)k_paths_mixed<2, RICH, 0> || f == (const void*)k_paths_mixed<3, RICH, 0> ||
+         f == (const void*)k_paths_mixed<4, RICH, 0> || f == (const void*)k_paths_mixed<5, RICH, 0> ||
+         f == (const void*)k_paths_mixed<0, RICH, 1> || f == (const void*)k_paths_mixed<5, RICH, 1>;
+}
+
+bool is_mixed_path_kernel(const void* func) { return is_mixed_t<true>(func) || is_mixed_t<false>(func); }
 
 cudaError_t launch_paths_mixed(const MixedArgs& a, int kind, int grid, size_t smem, cudaStream_t s) {
   return a.richardson ? launch_mixed_t<true>(a, kind, grid, smem, s) : launch_mixed_t<false>(a, kind, grid, smem, s);

@@ -20,7 +20,10 @@ struct MixedArgs {
   int N;                 // paths per knot
   float h, sqrth;
   double inv_N;
-  uint64_t seed;
+  // Philox-4x32-10 round keys of the seed (k0 + r W0, k1 + r W1 for rounds
+  // r = 0..9, set by mixed_set_rng): kernel parameters, so every round's key
+  // is an operand of its XOR instead of a key-schedule addition per call
+  uint32_t rk[20];
   uint32_t instance;
   int chunks, paths_per_chunk, n_items;
   int want_var, dup_sum;
@@ -36,9 +39,6 @@ struct MixedArgs {
   double* BBsum;         // [K]
   unsigned long long* stats;  // [0] steps [1] unused [2] global exits [3] stencil exits
   unsigned* err_flags;
-  // optional {seed, instance} in device memory, read instead of seed and
-  // instance (a replayed graph draws fresh numbers when the host updates it)
-  const unsigned long long* rng_dev;
   // optional explicit items (knot, paths [p0, p1)) instead of n_mc x chunks,
   // and per-knot 1/N_k instead of inv_N (variance-adaptive paths)
   const int* item_knot;
@@ -103,6 +103,11 @@ struct ReplayArgs {
 };
 
 cudaError_t launch_paths_mixed(const MixedArgs& a, int kind, int grid, size_t smem, cudaStream_t s);
+// Sets the Philox key schedule (rk) of `seed` and the instance word.
+void mixed_set_rng(MixedArgs& a, uint64_t seed, uint32_t instance);
+// True when `func` is one of the MIXED path kernels (a captured graph's
+// nodes are re-keyed with a new seed through their parameters).
+bool is_mixed_path_kernel(const void* func);
 int mixed_blocks_per_sm(int kind, size_t smem, int richardson);
 cudaError_t launch_paths_fp64(const Fp64Args& a, int kind, int grid, size_t smem, cudaStream_t s);
 int fp64_blocks_per_sm(int kind, size_t smem, int richardson);

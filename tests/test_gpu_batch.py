@@ -47,14 +47,19 @@ def test_batch_graph_replay_matches_direct_launch():
         assert first["graph_replayed"] == 0 and second["graph_replayed"] == 1
         assert second["kernel_launches"] == first["kernel_launches"] > 0
         replay = [bt.result(i) for i in range(len(insts))]
-        # a new seed replays the same graph: seed and instance are read from device memory
-        third = bt.run(N, H, seed=6, use_graph=True)
+        # a new seed and instance replay the same graph, its path-kernel
+        # nodes re-keyed: the results equal a direct launch with them
+        third = bt.run(N, H, seed=6, instance=3, use_graph=True)
         assert third["graph_replayed"] == 1
         other = [bt.result(i)["u"] for i in range(len(insts))]
+        bt.run(N, H, seed=6, instance=3, use_graph=False)
+        direct6 = [bt.result(i)["u"] for i in range(len(insts))]
     for d, r in zip(direct, replay):
         assert np.max(np.abs(d - r["u"])) < 1e-6
         assert r["latency_ms"] > 0.0 and r["iterations"] > 0
     assert max(np.max(np.abs(d - o)) for d, o in zip(direct, other)) > 1e-6
+    for d, o in zip(direct6, other):
+        assert np.max(np.abs(d - o)) < 1e-6
 
 
 def test_batch_many_instances_converge():
