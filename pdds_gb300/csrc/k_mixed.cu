@@ -3,9 +3,11 @@
 // One persistent CTA per slot processes work items (knot, chunk of paths).
 // Lanes step paths in FP32 with Philox-4x32-10 normals held in registers and
 // refill from the item's path counter the moment their path exits, so a warp
-// keeps stepping while path lengths vary.  A level that exits pushes its final
-// state to a per-warp queue in shared memory; the warp processes the queue 32
-// exits at a time, one per lane, so exit handling runs at full width.  An exit
+// keeps stepping while path lengths vary.  A level that exits keeps its exit
+// state; when both levels of a lane's Richardson pair have exited, the lane
+// pushes the pair to a per-warp queue in shared memory, and the warp
+// processes the queue 32 pairs at a time, one per lane, so exit handling runs
+// at full width and needs no bookkeeping across lanes.  An exit
 // on an interior stencil side deposits Y with cubic Lagrange weights into a
 // per-side histogram of the exit coordinate in shared memory (4 FP32 atomics,
 // O(1) per exit).  At the end of
@@ -52,14 +54,12 @@ struct Lvl<PK_LUT> {
   float cf[8];
 };
 
-// Exit queue of a warp: a level that leaves its stencil pushes (x, y, Y,
-// Z + xi, meta) and the warp processes 32 exits at a time, one per lane.
-// meta = owner lane | level << 5 | pair slot << 6 | step-limit << 8.
-// <= 31 left over + one push of 32 (the queue drains between the pushes).
+// Exit queue of a warp: a lane whose path pair has finished pushes both
+// levels' exit states (x, y, Y, Z + xi of the fine level, then of the coarse
+// level, then the step-limit flags) and the warp processes 32 pairs at a
+// time, one per lane.  <= 31 left over + one push of 32; slot XQCAP is the
+// spare slot written by lanes that push nothing.
 constexpr int XQCAP = 64;
-// Pair slots per lane: a Richardson pair's two exits meet in the slot of
-// its owner lane (halves outstanding, first half's weighted value).
-constexpr int NSLOT = 4;
 
 // Kahan step: s + c tracks the exact sum to O(eps^2); c holds the negated
 // rounding error of the running sum.
@@ -121,11 +121,9 @@ k_paths_mixed(const MixedArgs a) {
   __shared__ unsigned s_next_path;
   __shared__ double s_red[MIXED_THREADS / 32][4];
   __shared__ unsigned long long s_redi[MIXED_THREADS / 32][3];
-  __shared__ float s_qx[MIXED_THREADS / 32][XQCAP], s_qy[MIXED_THREADS / 32][XQCAP];
-  __shared__ float s_qY[MIXED_THREADS / 32][XQCAP], s_qS[MIXED_THREADS / 32][XQCAP];
-  __shared__ unsigned s_qm[MIXED_THREADS / 32][XQCAP];
-  __shared__ float s_pv[MIXED_THREADS / 32][NSLOT][32];
-  __shared__ int s_pst[MIXED_THREADS / 32][NSLOT][32];
+  // exit queue of each warp: word w of slot i at s_q[warp][w][i]
+  constexpr int QW = RICH ? 9 : 5;
+  __shared__ float s_q[MIXED_THREADS / 32][QW][XQCAP + 1];
   const DevLayout& L = a.L;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
@@ -253,13 +251,7 @@ k_paths_mixed(const MixedArgs a) {
     unsigned nglob = 0, nsten = 0;  // exits of the lane in this item (<= 2 N)
     int qcount = 0;  // warp-uniform
     const unsigned lt = (1u << lane) - 1u;
-    float* qx = s_qx[warp];
-    float* qy = s_qy[warp];
-    float* qY = s_qY[warp];
-    float* qS = s_qS[warp];
-    unsigned* qm = s_qm[warp];
-    for (int q = 0; q < NSLOT; q++) s_pst[warp][q][lane] = 0;
-    const int halves = RICH ? 2 : 1;
+    float (*q)[XQCAP + 1] = s_q[warp];
     const bool use_cv = P.use_cv != 0;
     // increment scales (sqrt2 sqrt(h) for iso kinds, sqrt(h) otherwise) and
     // Gobet thresholds of the fine (h/2) and coarse (h) levels
@@ -267,6 +259,7 @@ k_paths_mixed(const MixedArgs a) {
     const float scc = KindTraits<KIND>::iso ? 1.41421356f * sqrth : sqrth;
     const float scf = scc * 0.70710678f;
     const float thrc = -0.5826f * scc, thrf = -0.5826f * scf;
+    const unsigned maxs = (unsigned)a.max_steps;
 
     // One step of a level (Step, control-variate variant,
     // FKACIntegrator.hpp:46-57) and the Gobet-shifted exit test (Inside,
@@ -320,154 +313,163 @@ k_paths_mixed(const MixedArgs a) {
         return !(fmaxf(dx, dy) < t) || s.steps >= (unsigned)a.max_steps;
       }
     };
-    // Push the exits of one level (warp-synchronous) and drain 32 if full.
-    auto push = [&](bool ex, const Lvl<KIND>& s, unsigned meta) {
-      const unsigned mk = __ballot_sync(FULL, ex);
-      if (ex) {
-        const int i = qcount + __popc(mk & lt);
-        qx[i] = s.x;
-        qy[i] = s.y;
-        qY[i] = s.Y;
-        qS[i] = use_cv ? s.Z + s.xi : s.Z;
-        qm[i] = meta | (s.steps >= (unsigned)a.max_steps ? 256u : 0u);
-      }
-      qcount += __popc(mk);
-    };
-    // Process the exit at queue index i (lane-parallel): projection onto the
-    // stencil rectangle, value of the score, deposit on an interior side, and
-    // the pair's B contribution once both of its exits are processed.
-    // Projection (Rectangle2D, rectangle.hpp:7-229) as selects: the x side is
-    // taken exactly when dx > dy, the other coordinate is clamped to the
-    // rectangle (the identity inside, the corner outside both slabs), and the
-    // sides the projection lies on are read off by equality, first match in
-    // the order S, N, W, E as in G_update (stencil.cpp:246-301).
-    auto process = [&](int i, bool valid) {
-      float wv = 0.f;
-      int old = 0, slot = 0, owner = 0;
-      if (valid) {
-        const float x = qx[i], y = qy[i], Y = qY[i];
-        const unsigned meta = qm[i];
-        owner = (int)(meta & 31u);
-        const int lvl = (int)((meta >> 5) & 1u);
-        slot = (int)((meta >> 6) & 3u);
-        const float wgt = RICH ? (lvl ? -1.f : 2.f) : 1.f;
-        float val = qS[i];
-        bool ok = true;
-        if (meta & 256u) {  // step limit reached: an error unless the path had exited anyway
-          const float sql = (RICH && lvl == 0) ? sqrth * 0.70710678f : sqrth;
-          float dist, wn;
-          if constexpr (GEOM == 1) {
-            float d_in, d_out, d_a, d_b;
-            polar_out(x, y, d_in, d_out, d_a, d_b);
-            dist = fmaxf(fmaxf(d_in, d_out), fmaxf(d_a, d_b));
-            wn = 1.41421356f;
-          } else {
-            float Ex, Ey, Nx, Ny;
-            int om;
-            dist = rect2d<float>(rect, x, y, Ex, Ey, Nx, Ny, om);
-            float g00, g01, g10, g11;
-            sigma_f32<KIND>(P, x, y, g00, g01, g10, g11);
-            const float w0 = Nx * g00 + Ny * g10, w1 = Nx * g01 + Ny * g11;
-            wn = sqrtf(w0 * w0 + w1 * w1);
-          }
-          if (dist < -0.5826f * wn * sql) {
-            atomicOr(a.err_flags, ERR_FLAG_STEP_LIMIT);
-            ok = false;
-            val = 0.f;
-          }
-        }
-        if (ok && GEOM == 1) {
-          // polar stencil: the side with the largest outside distance (ties
-          // S, N, W, E); arcs are parameterised by the angle (measured from
-          // phi0, clamped to the stencil), rays by the radius (clamped)
+    // Value of one exit of a level, weighted: projection onto the stencil
+    // (Rectangle2D, rectangle.hpp:7-229) as selects -- the x side is taken
+    // exactly when dx > dy, the other coordinate is clamped to the rectangle
+    // (the identity inside, the corner outside both slabs), and the sides the
+    // projection lies on are read off by equality, first match in the order
+    // S, N, W, E as in G_update (stencil.cpp:246-301) -- then g at a global
+    // side or a deposit of wgt Y on an interior side.  Returns wgt (Z + xi +
+    // Y g) for the pair's B contribution.  `limit`: the level stopped at the
+    // step limit, an error unless it had exited anyway.
+    auto score = [&](float x, float y, float Y, float val, float wgt, bool limit, float sql) -> float {
+      bool ok = true;
+      if (limit) {  // step limit reached: an error unless the path had exited anyway
+        float dist, wn;
+        if constexpr (GEOM == 1) {
           float d_in, d_out, d_a, d_b;
           polar_out(x, y, d_in, d_out, d_a, d_b);
-          int d = 1;
-          float mx = d_in;
-          if (d_out > mx) { mx = d_out; d = 0; }
-          if (d_a > mx) { mx = d_a; d = 3; }
-          if (d_b > mx) { mx = d_b; d = 2; }
-          float sc;
-          bool glob = false;
-          if (d <= 1) {
-            const float rel = atan2f(ua0 * y - ua1 * x, ua0 * x + ua1 * y);
-            const float ang = rect[1] + (has_rays ? fminf(fmaxf(rel, 0.f), rect[3] - rect[1])
-                                                  : (rel < 0.f ? rel + 6.28318531f : rel));
-            sc = ang;
-            if (d == 0 && (globmask & 1)) {
-              glob = true;
-              float sa, ca;
-              sincosf(ang, &sa, &ca);
-              val += Y * u_f32<KIND>(P, rect[2] * ca, rect[2] * sa);
-            }
-          } else {
-            const float t = d == 3 ? ua0 * x + ua1 * y : ub0 * x + ub1 * y;
-            sc = fminf(fmaxf(t, rect[0]), rect[2]);
+          dist = fmaxf(fmaxf(d_in, d_out), fmaxf(d_a, d_b));
+          wn = 1.41421356f;
+        } else {
+          float Ex, Ey, Nx, Ny;
+          int om;
+          dist = rect2d<float>(rect, x, y, Ex, Ey, Nx, Ny, om);
+          float g00, g01, g10, g11;
+          sigma_f32<KIND>(P, x, y, g00, g01, g10, g11);
+          const float w0 = Nx * g00 + Ny * g10, w1 = Nx * g01 + Ny * g11;
+          wn = sqrtf(w0 * w0 + w1 * w1);
+        }
+        if (dist < -0.5826f * wn * sql) {
+          atomicOr(a.err_flags, ERR_FLAG_STEP_LIMIT);
+          ok = false;
+          val = 0.f;
+        }
+      }
+      if (ok && GEOM == 1) {
+        // polar stencil: the side with the largest outside distance (ties
+        // S, N, W, E); arcs are parameterised by the angle (measured from
+        // phi0, clamped to the stencil), rays by the radius (clamped)
+        float d_in, d_out, d_a, d_b;
+        polar_out(x, y, d_in, d_out, d_a, d_b);
+        int d = 1;
+        float mx = d_in;
+        if (d_out > mx) { mx = d_out; d = 0; }
+        if (d_a > mx) { mx = d_a; d = 3; }
+        if (d_b > mx) { mx = d_b; d = 2; }
+        float sc;
+        bool glob = false;
+        if (d <= 1) {
+          const float rel = atan2f(ua0 * y - ua1 * x, ua0 * x + ua1 * y);
+          const float ang = rect[1] + (has_rays ? fminf(fmaxf(rel, 0.f), rect[3] - rect[1])
+                                                : (rel < 0.f ? rel + 6.28318531f : rel));
+          sc = ang;
+          if (d == 0 && (globmask & 1)) {
+            glob = true;
+            float sa, ca;
+            sincosf(ang, &sa, &ca);
+            val += Y * u_f32<KIND>(P, rect[2] * ca, rect[2] * sa);
           }
-          if (glob) {
-            ++nglob;
-          } else {
-            ++nsten;
-            const ItemSide& is = s_side[d];
-            if (is.n > 0) {
-              const float uu = (sc - is.base) * is.inv_delta;
-              int b0 = (int)floorf(uu);
-              b0 = max(1, min(b0, is.nbins - 3));
-              float w[4];
-              cubic_weights(uu - (float)b0, w[0], w[1], w[2], w[3]);
-              const float yw = wgt * Y;
-              float* hp = hist + is.hist_off + b0 - 1;
+        } else {
+          const float t = d == 3 ? ua0 * x + ua1 * y : ub0 * x + ub1 * y;
+          sc = fminf(fmaxf(t, rect[0]), rect[2]);
+        }
+        if (glob) {
+          ++nglob;
+        } else {
+          ++nsten;
+          const ItemSide& is = s_side[d];
+          if (is.n > 0) {
+            const float uu = (sc - is.base) * is.inv_delta;
+            int b0 = (int)floorf(uu);
+            b0 = max(1, min(b0, is.nbins - 3));
+            float w[4];
+            cubic_weights(uu - (float)b0, w[0], w[1], w[2], w[3]);
+            const float yw = wgt * Y;
+            float* hp = hist + is.hist_off + b0 - 1;
 #pragma unroll
-              for (int r = 0; r < 4; r++) atomicAdd(hp + r, yw * w[r]);
-              if (a.want_var) {
-                float* hq = hist2 + is.hist_off + b0 - 1;
-                const float y2 = yw * yw;
+            for (int r = 0; r < 4; r++) atomicAdd(hp + r, yw * w[r]);
+            if (a.want_var) {
+              float* hq = hist2 + is.hist_off + b0 - 1;
+              const float y2 = yw * yw;
 #pragma unroll
-                for (int r = 0; r < 4; r++) atomicAdd(hq + r, y2 * w[r]);
-              }
-            }
-          }
-        } else if (ok) {
-          const float dx = fabsf(x - cx) - hx, dy = fabsf(y - cy) - hy;
-          const bool xs = dx > dy;
-          const float Ex = xs ? (x > cx ? rect[2] : rect[0]) : fminf(fmaxf(x, rect[0]), rect[2]);
-          const float Ey = xs ? fminf(fmaxf(y, rect[1]), rect[3]) : (y > cy ? rect[3] : rect[1]);
-          const bool onS = Ey == rect[1], onN = Ey == rect[3], onW = Ex == rect[0], onE = Ex == rect[2];
-          const int onmask = (onN ? 1 : 0) | (onS ? 2 : 0) | (onE ? 4 : 0) | (onW ? 8 : 0);
-          if (onmask & globmask) {
-            ++nglob;
-            val += Y * u_f32<KIND>(P, Ex, Ey);
-          } else {
-            ++nsten;
-            const int d = onS ? 1 : (onN ? 0 : (onW ? 3 : 2));
-            const ItemSide& is = s_side[d];
-            if (is.n > 0) {
-              const float sc = is.orient == 0 ? Ex : Ey;
-              const float uu = (sc - is.base) * is.inv_delta;
-              int b0 = (int)floorf(uu);
-              b0 = max(1, min(b0, is.nbins - 3));
-              float w[4];
-              cubic_weights(uu - (float)b0, w[0], w[1], w[2], w[3]);
-              const float yw = wgt * Y;
-              float* hp = hist + is.hist_off + b0 - 1;
-#pragma unroll
-              for (int r = 0; r < 4; r++) atomicAdd(hp + r, yw * w[r]);
-              if (a.want_var) {
-                float* hq = hist2 + is.hist_off + b0 - 1;
-                const float y2 = yw * yw;
-#pragma unroll
-                for (int r = 0; r < 4; r++) atomicAdd(hq + r, y2 * w[r]);
-              }
+              for (int r = 0; r < 4; r++) atomicAdd(hq + r, y2 * w[r]);
             }
           }
         }
-        wv = wgt * val;
-        old = atomicSub(&s_pst[warp][slot][owner], 1);
-        if (RICH && old == 2) s_pv[warp][slot][owner] = wv;
+      } else if (ok) {
+        const float dx = fabsf(x - cx) - hx, dy = fabsf(y - cy) - hy;
+        const bool xs = dx > dy;
+        const float Ex = xs ? (x > cx ? rect[2] : rect[0]) : fminf(fmaxf(x, rect[0]), rect[2]);
+        const float Ey = xs ? fminf(fmaxf(y, rect[1]), rect[3]) : (y > cy ? rect[3] : rect[1]);
+        const bool onS = Ey == rect[1], onN = Ey == rect[3], onW = Ex == rect[0], onE = Ex == rect[2];
+        const int onmask = (onN ? 1 : 0) | (onS ? 2 : 0) | (onE ? 4 : 0) | (onW ? 8 : 0);
+        if (onmask & globmask) {
+          ++nglob;
+          val += Y * u_f32<KIND>(P, Ex, Ey);
+        } else {
+          ++nsten;
+          const int d = onS ? 1 : (onN ? 0 : (onW ? 3 : 2));
+          const ItemSide& is = s_side[d];
+          if (is.n > 0) {
+            const float sc = is.orient == 0 ? Ex : Ey;
+            const float uu = (sc - is.base) * is.inv_delta;
+            int b0 = (int)floorf(uu);
+            b0 = max(1, min(b0, is.nbins - 3));
+            float w[4];
+            cubic_weights(uu - (float)b0, w[0], w[1], w[2], w[3]);
+            const float yw = wgt * Y;
+            float* hp = hist + is.hist_off + b0 - 1;
+#pragma unroll
+            for (int r = 0; r < 4; r++) atomicAdd(hp + r, yw * w[r]);
+            if (a.want_var) {
+              float* hq = hist2 + is.hist_off + b0 - 1;
+              const float y2 = yw * yw;
+#pragma unroll
+              for (int r = 0; r < 4; r++) atomicAdd(hq + r, y2 * w[r]);
+            }
+          }
+        }
       }
-      __syncwarp();
-      if (valid && old == 1) {
-        const float v = RICH ? wv + s_pv[warp][slot][owner] : wv;
+      return wgt * val;
+    };
+    Lvl<KIND> F, Cs;  // fine (or only) and coarse level of the lane's pair
+    // Push the finished pairs of the warp (both levels' exit states; the
+    // warp-synchronous ballot gives each its slot) and return their mask.
+    // Lanes without a finished pair write the spare slot XQCAP instead of
+    // branching around the stores.
+    auto push = [&](bool ex) -> unsigned {
+      const unsigned mk = __ballot_sync(FULL, ex);
+      const int i = ex ? qcount + __popc(mk & lt) : XQCAP;
+      q[0][i] = F.x;
+      q[1][i] = F.y;
+      q[2][i] = F.Y;
+      q[3][i] = use_cv ? F.Z + F.xi : F.Z;
+      unsigned meta = F.steps >= maxs ? 1u : 0u;
+      if (RICH) {
+        q[4][i] = Cs.x;
+        q[5][i] = Cs.y;
+        q[6][i] = Cs.Y;
+        q[7][i] = use_cv ? Cs.Z + Cs.xi : Cs.Z;
+        meta |= Cs.steps >= maxs ? 2u : 0u;
+      }
+      q[QW - 1][i] = __uint_as_float(meta);
+      qcount += __popc(mk);
+      return mk;
+    };
+    // Process the pair at queue index i (lane-parallel): both exits scored,
+    // B += 2 v_fine - v_coarse (v otherwise) in the lane's compensated sums.
+    auto process = [&](int i, bool valid) {
+      if (valid) {
+        const unsigned meta = __float_as_uint(q[QW - 1][i]);
+        float v = 0.f;
+#pragma unroll 1
+        for (int lv = 0; lv < (RICH ? 2 : 1); lv++) {
+          const int o = 4 * lv;
+          const float wgt = RICH ? (lv ? -1.f : 2.f) : 1.f;
+          const float sql = (RICH && lv == 0) ? sqrth * 0.70710678f : sqrth;
+          v += score(q[o][i], q[o + 1][i], q[o + 2][i], q[o + 3][i], wgt, ((meta >> lv) & 1u) != 0, sql);
+        }
         kahan_add(bs, bc, v);
         kahan_add(bbs, bbc, v * v);
       }
@@ -489,7 +491,6 @@ k_paths_mixed(const MixedArgs a) {
       }
     };
 
-    Lvl<KIND> F, Cs;
     float cf0[8];  // table fields at the knot (PK_LUT)
     if constexpr (KIND == PK_LUT) lut_sample<float, 8>(P.lut, x0, y0, cf0);
     auto reset = [&]() {
@@ -501,13 +502,9 @@ k_paths_mixed(const MixedArgs a) {
       Cs = F;
     };
     reset();
-    int gen = 0;  // pair slot of the lane's current pair
-    __syncwarp();
-    if (active) s_pst[warp][0][lane] = halves;
     bool f_alive = active, c_alive = RICH && active;
     unsigned m = 0;
     while (__any_sync(FULL, active)) {
-      bool fx = false, cx_ = false;  // exits in this iteration
       if (active) {
         const u32x4 blk = path_block_rk(a.rk, rng_inst, rng_knot, path, m++);
         float za0, za1, zb0, zb1;
@@ -516,51 +513,41 @@ k_paths_mixed(const MixedArgs a) {
         if (RICH) {
           // Richardson pair: two fine steps of h/2 and one coarse step of h
           // on the same Brownian increments (dW_coarse = dW_fine1 + dW_fine2);
-          // 2 E[fine] - E[coarse] cancels the O(h) bias
+          // 2 E[fine] - E[coarse] cancels the O(h) bias.  A level that has
+          // exited keeps its exit state until the pair is pushed.
           const float ea0 = scf * za0, ea1 = scf * za1, eb0 = scf * zb0, eb1 = scf * zb1;
-          if (f_alive) fx = advance(F, ea0, ea1, hf, thrf);
-          if (f_alive && !fx) fx = advance(F, eb0, eb1, hf, thrf);
-          if (c_alive) cx_ = advance(Cs, ea0 + eb0, ea1 + eb1, h, thrc);
+          if (f_alive) {
+            bool fx = advance(F, ea0, ea1, hf, thrf);
+            if (!fx) fx = advance(F, eb0, eb1, hf, thrf);
+            f_alive = !fx;
+          }
+          if (c_alive) c_alive = !advance(Cs, ea0 + eb0, ea1 + eb1, h, thrc);
         } else {
-          fx = advance(F, scc * za0, scc * za1, h, thrc);
+          bool fx = advance(F, scc * za0, scc * za1, h, thrc);
           if (!fx) fx = advance(F, scc * zb0, scc * zb1, h, thrc);
+          f_alive = !fx;
         }
       }
-      const unsigned meta0 = (unsigned)lane | ((unsigned)gen << 6);
-      push(fx, F, meta0);
-      drain_full();
-      if (RICH) {
-        push(cx_, Cs, meta0 | 32u);
-        drain_full();
-      }
-      f_alive = f_alive && !fx;
-      c_alive = c_alive && !cx_;
-      // finished pairs: steps, and refill into the next pair slot
+      // finished pairs: queue both exits, then refill from the item's
+      // path counter with one warp-aggregated atomic
       const bool done = active && !f_alive && !c_alive;
-      if (done) nsteps += F.steps + (RICH ? Cs.steps : 0u);
-      const int ngen = (gen + 1) & (NSLOT - 1);
-      if (__any_sync(FULL, done && s_pst[warp][ngen][lane] != 0)) drain_all();
-      const unsigned dm = __ballot_sync(FULL, done);
+      const unsigned dm = push(done);
+      drain_full();
       if (dm) {
         const int leader = __ffs(dm) - 1;
         unsigned base = 0;
         if (lane == leader) base = atomicAdd(&s_next_path, (unsigned)__popc(dm));
         base = __shfl_sync(FULL, base, leader);
         if (done) {
+          nsteps += F.steps + (RICH ? Cs.steps : 0u);
           path = base + __popc(dm & lt);
-          if ((int)path >= path_end) {
-            active = false;
-          } else {
-            reset();
-            gen = ngen;
-            s_pst[warp][gen][lane] = halves;
-            f_alive = true;
-            c_alive = RICH;
-            m = 0;
-          }
+          active = (int)path < path_end;
+          reset();
+          f_alive = active;
+          c_alive = RICH && active;
+          m = 0;
         }
       }
-      __syncwarp();
     }
     drain_all();
     // ------------------------------------------------------------ reduce B
