@@ -311,7 +311,10 @@ class PDDSparseGM:
         B = np.zeros(self.K)
         BB = np.zeros(self.K)
         info = capi.EstimateInfo()
-        self._check(self._lib.pdds_estimate(self._ctx, C.byref(d), _p(val, C.c_double), _p(var, C.c_double),
+        # G_var is only computed by the replay mode and by MIXED with want_var;
+        # otherwise var stays the zero array and nothing is read back into it
+        var_out = _p(var, C.c_double) if (want_var or mode == capi.MODE_REPLAY_FP64) else None
+        self._check(self._lib.pdds_estimate(self._ctx, C.byref(d), _p(val, C.c_double), var_out,
                                             _p(B, C.c_double), _p(BB, C.c_double), C.byref(info)))
         del keep
         kn = np.zeros(self.K, np.int32)
