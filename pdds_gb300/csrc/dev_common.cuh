@@ -120,6 +120,15 @@ __host__ __device__ __forceinline__ void lut_coord(T x, T x0, T inv_dx, int n, i
 }
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
+// One table node, its 8 fields as two float4 (32 bytes, 32-byte aligned: the
+// table comes from cudaMalloc and nodes are 32 bytes apart), in one 256-bit
+// read-only load: half the L1 requests of two 128-bit loads.
+__device__ __forceinline__ void ldg_node(const float4* p, float4& a, float4& b) {
+  asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+      : "l"(p));
+}
+
 // all eight fields (nf = 8) or the first four (nf = 4: sigma11, sigma22, b1, b2)
 template <typename T, int NF>
 __device__ __forceinline__ void lut_sample(const LutDev& L, T x, T y, T* out) {
@@ -140,10 +149,11 @@ __device__ __forceinline__ void lut_sample(const LutDev& L, T x, T y, T* out) {
 #pragma unroll
     for (int c = 0; c < 4; c++) {
       const int xx = clampi(ix - 1 + c, 0, L.nx - 1);
-      const float4 a = __ldg(row + 2 * xx);
+      float4 a, b;
+      if (NF == 8) ldg_node(row + 2 * xx, a, b);
+      else a = __ldg(row + 2 * xx);
       acc[0] += wx[c] * (T)a.x; acc[1] += wx[c] * (T)a.y; acc[2] += wx[c] * (T)a.z; acc[3] += wx[c] * (T)a.w;
       if (NF == 8) {
-        const float4 b = __ldg(row + 2 * xx + 1);
         acc[NF > 4 ? 4 : 0] += wx[c] * (T)b.x; acc[NF > 5 ? 5 : 0] += wx[c] * (T)b.y;
         acc[NF > 6 ? 6 : 0] += wx[c] * (T)b.z; acc[NF > 7 ? 7 : 0] += wx[c] * (T)b.w;
       }
