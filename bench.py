@@ -200,6 +200,30 @@ def many_instance_batch(local: int, n_inst: int = 256, reps: int = 3, npaths: in
     return out
 
 
+def semilinear_newton(local: int, iterations: int = 4, npaths: int = 20_000, h: float = 5e-4, m: int = 32):
+    """The semilinear outer loop (Solve_SemiLin_numVR + subdomain solves):
+    Lap u - u^3 + F = 0 on [0,1]^2, u = 1.1 + sin(pi x) sin(pi y), 8 x 8
+    subdomains, 21 knots per segment, Newton steps from the constant 1.1, each
+    one Newton-table build on the device, a MIXED estimate (Richardson pair,
+    adaptive step, summed weights), the interface solve and the table-served
+    subdomain solves on 32 x 32 grids; wall time per step and the RMSE
+    against the analytic solution after each step."""
+    import pdds_gb300 as P
+    from pdds_gb300.config import fac_rule
+    pd = P.PDDSparseGM((0.0, 0.0), (1.0, 1.0), 8, 21, fac_rule(1.0, 8, 21), device=local)
+    pd.solve_semilinear(1, 256, h, m=m)  # warm-up (module load, allocations)
+    t0 = time.perf_counter()
+    its = pd.solve_semilinear(iterations, npaths, h, m=m, seed=7, adaptive_h=True, richardson=True, dup_sum=True)
+    dt = time.perf_counter() - t0
+    out = {"knots": int(pd.K), "paths_per_knot": npaths, "h": h, "subdomain_grid": m, "newton_steps": iterations,
+           "ms_per_newton_step": 1000.0 * dt / iterations,
+           "rmse_knots": [round(it["rmse_knots"], 6) for it in its],
+           "rmse_grid": [round(it["rmse_grid"], 6) for it in its],
+           "path_steps_per_s": float(sum(it["estimate"].info["path_steps"] for it in its) / dt)}
+    pd.close()
+    return out
+
+
 def circle_uneven(local: int, reps: int = 3, h: float = 1e-3):
     """Uneven path lengths on the unit disk: 6 rings x 16 sectors (the central
     ring one disk subdomain), 11 knots per segment, Poisson with
@@ -277,12 +301,14 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="poisson_12x12_n43")
     ap.add_argument("--npaths", type=int, default=0)
-    ap.add_argument("--ref-knots", type=int, default=3)
+    ap.add_argument("--ref-knots", type=int, default=8, help="knots per step of the reference arm")
+    ap.add_argument("--cpu-knots", type=int, default=16, help="knots of the cpu_baseline sample (about 10 s)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-circle", action="store_true")
+    ap.add_argument("--no-semilinear", action="store_true")
     args = ap.parse_args()
 
     from pdds_gb300.config import WORKLOADS, fac_rule
@@ -425,11 +451,13 @@ def main():
         extra["many_instance_batch"] = many_instance_batch(local)
     if not args.no_circle and rank == 0:
         extra["circle_uneven_lengths"] = circle_uneven(local)
+    if not args.no_semilinear and rank == 0:
+        extra["semilinear_newton"] = semilinear_newton(local)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
-            cpu = cpu_baseline(workload, fac, args.ref_knots)
+            cpu = cpu_baseline(workload, fac, args.cpu_knots)
         except Exception as exc:  # report, do not fail the bench
             cpu = {"value": None, "unit": "path-steps/s", "cores": os.cpu_count(), "kind": "port",
                    "sample": f"failed: {exc}"}

@@ -322,11 +322,42 @@ pdds_status pdds_batch_instance(pdds_ctx* ctx, int32_t i, int32_t* nknots, doubl
  * finite-difference problem on an m x m interior grid (2 <= m <= 64) by the
  * sine transform, in FP64, with Dirichlet data = the interface solution
  * interpolated along each edge (cubic Lagrange through its knots) and g on
- * the domain boundary.  u: interface values u[K] (host), or NULL for those of
- * the last pdds_solve_interface.  out[nsub*nsub][m][m]: subdomain
- * s = column + nsub * row, value [j][i] at x = x0 + (i+1) lx/(m+1),
- * y = y0 + (j+1) ly/(m+1) of its rectangle [x0, x0+lx] x [y0, y0+ly]. */
+ * the domain boundary.  Table-served problems (PDDS_LUT, including the
+ * tables of pdds_semilinear_tables) have variable coefficients
+ * sigma11^2/2 v_xx + sigma22^2/2 v_yy + b.grad v + c v + f = 0 sampled at the
+ * grid nodes, central differences, solved by BiCGSTAB preconditioned with the
+ * sine-transform solve of the subdomain-mean operator (relative residual
+ * 1e-12, at most 200 iterations, else PDDS_ERR_NOT_CONVERGED).  u: interface
+ * values u[K] (host), or NULL for those of the last pdds_solve_interface.
+ * out[nsub*nsub][m][m]: subdomain s = column + nsub * row, value [j][i] at
+ * x = x0 + (i+1) lx/(m+1), y = y0 + (j+1) ly/(m+1) of its rectangle
+ * [x0, x0+lx] x [y0, y0+ly].  The solution with its edge values is also kept
+ * on the device as one grid of nsub (m+1) + 1 nodes per side for
+ * pdds_semilinear_tables. */
 pdds_status pdds_subdomain_solve(pdds_ctx* ctx, int32_t m, const double* u, double* out);
+
+/* Semilinear outer loop, one Newton step (Solve_SemiLin_numVR,
+ * PDDSparseGM.cpp:3833-4080, with the equation of
+ * BVPs/EDPs/Semilinear_u3_VR.hpp): Lap u - u^3 + F = 0 on the unit square,
+ * u = a + sin(pi x) sin(pi y) (a = 1.1 in the reference), g = a on the
+ * boundary, F = 2 pi^2 sin(pi x) sin(pi y) + u^3.  Builds, on the device, the
+ * tables of the problem linearised around the iterate u_k -- sigma = sqrt2 I,
+ * b = 0, c = -3 u_k^2, f = F + 2 u_k^3 and grad u_k for the control variate
+ * (EquationSM_c_LUT, EquationSM_f_LUT, EquationSM_grad_LUT) -- on the grid of
+ * nsub (m+1) + 1 nodes per side, and makes that table-served problem the
+ * context's problem.  u_k is the last pdds_subdomain_solve (from_solution = 1,
+ * same m) or the constant u0 (the reference's first iteration: c = -3.63,
+ * f = F + 2.662 at u0 = 1.1).  A Newton iteration is then pdds_estimate,
+ * pdds_solve_interface and pdds_subdomain_solve (Solve_Subdomains_SemiLin). */
+typedef struct {
+  int32_t m;              /* interior grid points per subdomain side (2..64)   */
+  int32_t from_solution;  /* 1: around the last subdomain solve; 0: around u0 */
+  int32_t use_cv;         /* control variate with grad u_k                     */
+  int32_t reserved;
+  double u0;              /* constant first iterate                            */
+  double a;               /* u = a + sin(pi x) sin(pi y)                       */
+} pdds_semilinear_desc;
+pdds_status pdds_semilinear_tables(pdds_ctx* ctx, const pdds_semilinear_desc* desc);
 
 /* ---------------------------------------------------------------- allocation-free solve
  * No counterpart in the reference.  For callers that cannot let a library

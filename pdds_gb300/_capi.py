@@ -25,7 +25,8 @@ SOLVE_BICGSTAB_FP64, SOLVE_GMRES_FP32_IR = 0, 1
 EXPORTS = [
     "pdds_create", "pdds_destroy", "pdds_last_error", "pdds_version", "pdds_problem_set", "pdds_problem_set_lut",
     "pdds_layout_build", "pdds_layout_build_circle", "pdds_layout_knots", "pdds_layout_csr", "pdds_layout_stencil",
-    "pdds_estimate", "pdds_estimate_knot_paths", "pdds_estimate_knot_steps", "pdds_autotune", "pdds_solve_interface", "pdds_subdomain_solve", "pdds_batch_build", "pdds_batch_run", "pdds_batch_instance",
+    "pdds_estimate", "pdds_estimate_knot_paths", "pdds_estimate_knot_steps", "pdds_autotune", "pdds_solve_interface",
+    "pdds_subdomain_solve", "pdds_semilinear_tables", "pdds_batch_build", "pdds_batch_run", "pdds_batch_instance",
     "pdds_solve_bicgstab_static",
 ]
 STATIC_SOLVE_MAX_K = 131072
@@ -43,6 +44,11 @@ class LayoutDesc(C.Structure):
 class CircleDesc(C.Structure):
     _fields_ = [("radius", C.c_double), ("nrings", C.c_int32), ("nsectors", C.c_int32), ("nnode", C.c_int32),
                 ("kappa", C.c_double * 4)]
+
+
+class SemilinearDesc(C.Structure):
+    _fields_ = [("m", C.c_int32), ("from_solution", C.c_int32), ("use_cv", C.c_int32), ("reserved", C.c_int32),
+                ("u0", C.c_double), ("a", C.c_double)]
 
 
 class LayoutInfo(C.Structure):

@@ -277,7 +277,7 @@ class PDDSparseGM:
         adaptive_n: npaths is the pilot per knot; each knot then runs
         N_k = 4 Var_k / (0.66666 target_stderr)^2 paths (multiple of 256,
         clamped to [npaths, npaths_max]); Estimate.npaths holds N_k."""
-        if bvp.kind == BVP.LUT and getattr(self, "_lut_owner", None) is not bvp.tables:
+        if bvp.kind == BVP.LUT and bvp.tables is not None and getattr(self, "_lut_owner", None) is not bvp.tables:
             coef, g, bounds = bvp.tables
             ny, nx = g.shape
             b = np.ascontiguousarray(bounds, np.float64)
@@ -361,6 +361,45 @@ class PDDSparseGM:
         x = self.sw[0] + (np.arange(ns)[:, None] + t[None, :]) * lx
         y = self.sw[1] + (np.arange(ns)[:, None] + t[None, :]) * ly
         return x, y, out.reshape(ns, ns, m, m)
+
+    def semilinear_tables(self, m: int = 32, from_solution: bool = False, u0: float = 1.1, a: float = 1.1,
+                          use_cv: bool = True) -> BVP:
+        """One Newton linearisation of Lap u - u^3 + F = 0 on the unit square
+        (the reference's Solve_SemiLin_numVR with Semilinear_u3_VR.hpp):
+        tables of c = -3 u_k^2, f = F + 2 u_k^3 and grad u_k built on the device
+        around the last subdomain_solve(m) (from_solution) or the constant u0.
+        Returns the table-served BVP (tables stay on the device)."""
+        d = capi.SemilinearDesc()
+        d.m = int(m)
+        d.from_solution = int(bool(from_solution))
+        d.use_cv = int(bool(use_cv))
+        d.u0 = float(u0)
+        d.a = float(a)
+        self._check(self._lib.pdds_semilinear_tables(self._ctx, C.byref(d)))
+        self._lut_owner = None
+        return BVP(BVP.LUT, use_cv=use_cv, tables=None,
+                   exact=lambda x, y: a + np.sin(np.pi * x) * np.sin(np.pi * y))
+
+    def solve_semilinear(self, iterations: int, npaths: int, h: float, m: int = 32, u0: float = 1.1,
+                         a: float = 1.1, seed: int = 1234, **opts):
+        """The semilinear outer loop: `iterations` Newton steps, each an
+        estimate and interface solve of the problem linearised around the
+        previous subdomain solution, then the subdomain solves
+        (Solve_SemiLin_numVR + Solve_Subdomains_SemiLin, main_VR.cpp).  Returns
+        a list of per-iteration dicts (interface solution u, subdomain grid
+        (x, y, v), their RMSE against the exact solution)."""
+        out = []
+        for k in range(iterations):
+            bvp = self.semilinear_tables(m, from_solution=k > 0, u0=u0, a=a)
+            est = self.estimate(bvp, npaths, h, mode=capi.MODE_MIXED, seed=seed, instance=k, **opts)
+            u, sinfo = self.solve_interface()
+            x, y, v = self.subdomain_solve(m)
+            ex_knots = bvp.u(self.x, self.y)
+            ex_grid = bvp.u(x[None, :, None, :], y[:, None, :, None])  # [row, col, j, i] like v
+            out.append({"u": u, "grid": (x, y, v), "estimate": est, "solve": sinfo,
+                        "rmse_knots": float(np.sqrt(np.mean((u - ex_knots) ** 2))),
+                        "rmse_grid": float(np.sqrt(np.mean((v - ex_grid) ** 2)))})
+        return out
 
     def write_outputs(self, directory: str, est: "Estimate", u, bvp: BVP):
         """Writes Output/solution.csv and Output/Debug/{G,G_var,B,B_var}.csv

@@ -38,6 +38,7 @@ pdds_status upload_layout(pdds_ctx* ctx) {
   drop_graph(ctx);  // the buffers below may move
   ctx->edges_ready = false;
   ctx->has_solution = false;
+  ctx->ugrid_m = 0;
   HostLayout& L = ctx->L;
   cudaStream_t s = ctx->stream;
   std::vector<double> st_rect;
@@ -198,6 +199,8 @@ pdds_status check_err_flags(pdds_ctx* ctx) {
   if (f & ERR_FLAG_SINGULAR) return fail(ctx, PDDS_ERR_ILL_CONDITIONED, "RBF matrix numerically singular");
   if (f & ERR_FLAG_STEP_LIMIT) return fail(ctx, PDDS_ERR_STEP_LIMIT, "a path exceeded max_steps");
   if (f & ERR_FLAG_EXIT_SIDE) return fail(ctx, PDDS_ERR_EXIT_SIDE, "an exit matched no stencil side");
+  if (f & ERR_FLAG_SUB_NOCONV)
+    return fail(ctx, PDDS_ERR_NOT_CONVERGED, "a subdomain solve missed its tolerance in 200 iterations");
   if (f & ERR_FLAG_TIMEOUT) return fail(ctx, PDDS_ERR_TIMEOUT, "a grid barrier of the interface solve timed out");
   return PDDS_OK;
 }
@@ -460,6 +463,9 @@ pdds_status pdds_destroy(pdds_ctx* ctx) {
     ctx->edge_knots.release();
     ctx->sub_u.release();
     ctx->sub_out.release();
+    ctx->sub_work.release();
+    ctx->sub_iters.release();
+    ctx->ugrid.release();
     ctx->item_knot.release();
     ctx->item_p0.release();
     ctx->item_p1.release();
@@ -951,8 +957,9 @@ pdds_status pdds_subdomain_solve(pdds_ctx* ctx, int32_t m, const double* u, doub
     return fail(ctx, PDDS_ERR_INVALID, "subdomain solves need a rectangular layout");
   if (!ctx->has_problem) return fail(ctx, PDDS_ERR_INVALID, "no problem set");
   const int kind = ctx->prob.kind;
-  if (kind != PDDS_POISSON_SINCOS && kind != PDDS_MONEGROS && kind != PDDS_HELMHOLTZ)
-    return fail(ctx, PDDS_ERR_INVALID, "subdomain solves take operators Lap + c (Poisson, Monegros, Helmholtz)");
+  if (kind != PDDS_POISSON_SINCOS && kind != PDDS_MONEGROS && kind != PDDS_HELMHOLTZ && kind != PDDS_LUT)
+    return fail(ctx, PDDS_ERR_INVALID,
+                "subdomain solves take operators Lap + c (Poisson, Monegros, Helmholtz) or table-served problems");
   if (m < 2 || m > 64) return fail(ctx, PDDS_ERR_INVALID, "2 <= m <= 64");
   if (!u && !ctx->has_solution) return fail(ctx, PDDS_ERR_INVALID, "no interface solution");
   CK(cudaSetDevice(ctx->device));
@@ -997,9 +1004,61 @@ pdds_status pdds_subdomain_solve(pdds_ctx* ctx, int32_t m, const double* u, doub
     ud = ctx->sub_u.p;
   }
   CK(ctx->sub_out.resize((size_t)S * m * m));
-  CK(launch_subdomain(ctx->dl, problem_dev(ctx), ns, m, n, ctx->edge_knots.p, ud, ctx->sub_out.p, s));
+  const int G = ns * (m + 1) + 1;
+  CK(ctx->ugrid.resize((size_t)G * G));
+  if (kind == PDDS_LUT) {
+    CK(ctx->sub_work.resize((size_t)S * 13 * m * m));
+    CK(ctx->sub_iters.resize(S));
+    CK(cudaMemsetAsync(ctx->errf.p, 0, sizeof(unsigned), s));
+    CK(launch_subdomain_lut(ctx->dl, problem_dev(ctx), ns, m, n, ctx->edge_knots.p, ud, ctx->sub_out.p,
+                            ctx->sub_work.p, ctx->ugrid.p, 200, 1e-12, ctx->sub_iters.p, ctx->errf.p, s));
+  } else {
+    CK(launch_subdomain(ctx->dl, problem_dev(ctx), ns, m, n, ctx->edge_knots.p, ud, ctx->sub_out.p, ctx->ugrid.p, s));
+  }
   CK(cudaMemcpyAsync(out, ctx->sub_out.p, (size_t)S * m * m * sizeof(double), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
+  ctx->ugrid_m = m;
+  if (kind == PDDS_LUT) return check_err_flags(ctx);
+  return PDDS_OK;
+}
+
+pdds_status pdds_semilinear_tables(pdds_ctx* ctx, const pdds_semilinear_desc* desc) {
+  if (!ctx || !desc) return PDDS_ERR_INVALID;
+  if (ctx->device < 0) return fail(ctx, PDDS_ERR_INVALID, "context has no device");
+  if (!ctx->has_layout || ctx->L.geom != 0 || ctx->is_batch)
+    return fail(ctx, PDDS_ERR_INVALID, "the semilinear step needs a rectangular layout");
+  const HostLayout& L = ctx->L;
+  if (std::fabs(L.sw[0]) > 1e-12 || std::fabs(L.sw[1]) > 1e-12 || std::fabs(L.ne[0] - 1.0) > 1e-12 ||
+      std::fabs(L.ne[1] - 1.0) > 1e-12)
+    return fail(ctx, PDDS_ERR_INVALID, "the semilinear test equation lives on the unit square [0,1]^2");
+  const int m = desc->m;
+  if (m < 2 || m > 64) return fail(ctx, PDDS_ERR_INVALID, "2 <= m <= 64");
+  if (desc->from_solution && ctx->ugrid_m != m)
+    return fail(ctx, PDDS_ERR_INVALID, "from_solution needs a pdds_subdomain_solve with the same m on this layout");
+  CK(cudaSetDevice(ctx->device));
+  cudaStream_t s = ctx->stream;
+  drop_graph(ctx);
+  const int ns = L.nsub;
+  const int G = ns * (m + 1) + 1;
+  const size_t nn = (size_t)G * G;
+  CK(ctx->lut_coef.resize(8 * nn));
+  CK(ctx->lut_g.resize(nn));
+  const double hg = (L.ne[0] - L.sw[0]) / ns / (m + 1);
+  CK(launch_newton_tables(desc->from_solution ? ctx->ugrid.p : nullptr, G, L.sw[0], L.sw[1], hg, desc->u0, desc->a,
+                          ctx->lut_coef.p, ctx->lut_g.p, s));
+  CK(cudaStreamSynchronize(s));
+  ctx->lut_nx = G;
+  ctx->lut_ny = G;
+  ctx->lut_bounds[0] = L.sw[0];
+  ctx->lut_bounds[1] = L.sw[1];
+  ctx->lut_bounds[2] = L.sw[0] + (G - 1) * hg;
+  ctx->lut_bounds[3] = L.sw[1] + (G - 1) * hg;
+  pdds_problem_desc pd;
+  std::memset(&pd, 0, sizeof(pd));
+  pd.kind = PDDS_LUT;
+  pd.use_cv = desc->use_cv ? 1 : 0;
+  ctx->prob = pd;
+  ctx->has_problem = true;
   return PDDS_OK;
 }
 

@@ -107,6 +107,10 @@ struct pdds_ctx {
   // subdomain solves: knots of each subdomain edge (S, N, W, E; -1 = domain boundary)
   DBuf<int> edge_knots;
   DBuf<double> sub_u, sub_out;
+  DBuf<double> sub_work;          // Krylov vectors of the table-served subdomain solver
+  DBuf<int> sub_iters;            // its iterations per subdomain
+  DBuf<double> ugrid;             // last subdomain solution on the global grid
+  int ugrid_m = 0;                // its interior points per subdomain side (0 = none)
   bool edges_ready = false;
   bool has_solution = false;
   // autotuned launch shape of the MIXED path kernel (0 = defaults)

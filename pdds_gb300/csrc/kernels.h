@@ -13,6 +13,7 @@ constexpr unsigned ERR_FLAG_STEP_LIMIT = 1u;
 constexpr unsigned ERR_FLAG_EXIT_SIDE = 2u;
 constexpr unsigned ERR_FLAG_SINGULAR = 4u;
 constexpr unsigned ERR_FLAG_TIMEOUT = 8u;  // a bounded device wait ran out
+constexpr unsigned ERR_FLAG_SUB_NOCONV = 16u;  // a subdomain solve missed its tolerance
 
 struct MixedArgs {
   DevLayout L;
@@ -130,8 +131,17 @@ cudaError_t launch_finalize_n(const int* mc_knots, int n_mc, const int* knot_N, 
                               double* GG_to_var, int want_var, cudaStream_t s);
 // Subdomain interior solves (k_subdomain.cu).
 size_t subdomain_smem(int m);
+// grid: optional nsub (m + 1) + 1 nodes per side, the solution with its edges
 cudaError_t launch_subdomain(const DevLayout& L, const ProblemDev& P, int nsub, int m, int n, const int* edge_knots,
-                             const double* u, double* out, cudaStream_t s);
+                             const double* u, double* out, double* grid, cudaStream_t s);
+// table-served problems (PK_LUT): BiCGSTAB with a sine-transform preconditioner;
+// work = 13 m^2 doubles per subdomain
+cudaError_t launch_subdomain_lut(const DevLayout& L, const ProblemDev& P, int nsub, int m, int n, const int* edge_knots,
+                                 const double* u, double* out, double* work, double* grid, int max_iter, double tol,
+                                 int* iters, unsigned* err, cudaStream_t s);
+// tables of the semilinear Newton step around the grid (or the constant u0)
+cudaError_t launch_newton_tables(const double* grid, int G, double x0, double y0, double hg, double u0, double A,
+                                 float* coef, float* gtab, cudaStream_t s);
 cudaError_t launch_finalize(const int* mc_knots, int n_mc, int N, const double* Bsum,
                             const double* BBsum, double* B, double* BB, const int64_t* row_ptr,
                             int64_t nnz, const double* G, double* GG_to_var, int want_var,
