@@ -224,6 +224,40 @@ def semilinear_newton(local: int, iterations: int = 4, npaths: int = 20_000, h: 
     return out
 
 
+def varcoef_lut(local: int, reps: int = 2):
+    """The variable-coefficient problem with coefficients served from 1024^2
+    FP32 tables (bicubic), 8 x 8 subdomains, 31 knots per segment, 5e4 paths
+    per knot, h = 5e-4, MIXED with the Richardson pair, adaptive step and
+    summed weights; device time of the path kernel by the library's events.
+    The FP64 form runs the same tables with 2e3 paths per knot for the
+    MIXED/FP64 path-step rate comparison."""
+    import pdds_gb300 as P
+    from pdds_gb300.config import WORKLOADS, fac_rule
+    w = WORKLOADS["varcoef_lut_8x8_n31"]
+    bvp = P.BVP.varcoef_lut(w["lut_n"], (w["sw"][0], w["sw"][1], w["ne"][0], w["ne"][1]))
+    pd = P.PDDSparseGM(w["sw"], w["ne"], w["nsub"], w["nnode"], fac_rule(w["ne"][0] - w["sw"][0], w["nsub"],
+                                                                         w["nnode"]), device=local)
+    opts = dict(adaptive_h=True, richardson=True, dup_sum=True)
+    pd.estimate(bvp, 256, w["h"], mode=P.MODE_MIXED, **opts)  # warm-up, table upload
+    ms, steps = [], 0
+    for r in range(reps):
+        est = pd.estimate(bvp, w["npaths"], w["h"], mode=P.MODE_MIXED, seed=1234, instance=r, **opts)
+        u, si = pd.solve_interface()
+        ms.append(est.info["ms_paths"])
+        steps = est.info["path_steps"]
+    rmse = float(np.sqrt(np.mean((u - bvp.u(pd.x, pd.y)) ** 2)))
+    e64 = pd.estimate(bvp, 2000, w["h"], mode=P.MODE_FP64, seed=1234, **opts)
+    e32 = pd.estimate(bvp, 2000, w["h"], mode=P.MODE_MIXED, seed=1234, **opts)
+    out = {"knots": int(pd.K), "paths_per_knot": w["npaths"], "h": w["h"], "table": "1024^2 x 8 FP32, bicubic",
+           "ms_paths": float(np.mean(ms)), "path_steps_per_s": steps / (1e-3 * float(np.mean(ms))),
+           "rmse_vs_analytic": rmse, "solve_ms": float(si["ms"]),
+           "fp64": {"paths_per_knot": 2000, "ms_paths": e64.info["ms_paths"],
+                    "mixed_over_fp64": (e32.info["path_steps"] / e32.info["ms_paths"]) /
+                                       (e64.info["path_steps"] / e64.info["ms_paths"])}}
+    pd.close()
+    return out
+
+
 def circle_uneven(local: int, reps: int = 3, h: float = 1e-3):
     """Uneven path lengths on the unit disk: 6 rings x 16 sectors (the central
     ring one disk subdomain), 11 knots per segment, Poisson with
@@ -309,6 +343,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-circle", action="store_true")
     ap.add_argument("--no-semilinear", action="store_true")
+    ap.add_argument("--no-lut", action="store_true")
     args = ap.parse_args()
 
     from pdds_gb300.config import WORKLOADS, fac_rule
@@ -451,6 +486,8 @@ def main():
         extra["many_instance_batch"] = many_instance_batch(local)
     if not args.no_circle and rank == 0:
         extra["circle_uneven_lengths"] = circle_uneven(local)
+    if not args.no_lut and rank == 0:
+        extra["varcoef_lut"] = varcoef_lut(local)
     if not args.no_semilinear and rank == 0:
         extra["semilinear_newton"] = semilinear_newton(local)
 
@@ -480,7 +517,7 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
         "config": {"workload": workload["name"], "knots": pd.K, "paths_per_knot": N, "h": h,
                    "mode": "MIXED", "adaptive_h": True, "richardson": "h/2,h",
-                   "solver": "GMRES(30) FP32 + FP64 refinement", "l2": "flushed (256 MB write)",
+                   "solver": "GMRES(20) FP32 + FP64 refinement", "l2": "flushed (256 MB write)",
                    "shared_side_knots": "weights summed (dup_sum)"},
         "interface_solves_per_s": args.steps / t_dev,
         "rmse_vs_analytic": float(np.mean(rmses)),

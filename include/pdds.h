@@ -239,7 +239,7 @@ typedef enum {
 
 typedef struct {
   int32_t method;
-  int32_t restart;       /* GMRES(m), 2 <= m <= 40 (0 = 30) */
+  int32_t restart;       /* GMRES(m), 2 <= m <= 40 (0 = 20) */
   int32_t max_iter;      /* inner iterations per call / refinement step */
   int32_t max_refine;    /* FP64 refinement steps */
   double tol;            /* relative residual in FP64 */

@@ -410,7 +410,7 @@ class PDDSparseGM:
                       bvp.u(self.x, self.y))
 
     def solve_interface(self, method: int = capi.SOLVE_GMRES_FP32_IR, tol: float = 1e-10,
-                        restart: int = 30, max_iter: int = 0, max_refine: int = 0):
+                        restart: int = 20, max_iter: int = 0, max_refine: int = 0):
         """Solves (I + G) u = B for the last estimate; returns (u, info)."""
         d = capi.SolveDesc()
         d.method = int(method)
