@@ -103,7 +103,7 @@ pdds_status upload_layout(pdds_ctx* ctx) {
     fsm = std::max(fsm, nn);
   }
   ctx->mixed_smem = msm * sizeof(float);
-  ctx->fp64_smem = 2 * fsm * sizeof(double);
+  ctx->fp64_smem = (FP64_THREADS / 32 + 1) * fsm * sizeof(double);  // per-warp sums, knot coordinates
   std::vector<unsigned char> owner(L.map_owner.begin(), L.map_owner.end());
   std::vector<int> knot_stencil(L.knot_stencil.begin(), L.knot_stencil.end());
   CK(ctx->kx.upload(L.kx, s));

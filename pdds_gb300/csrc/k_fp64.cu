@@ -4,6 +4,10 @@
 // quantity is FP64 and each stencil exit adds its exact RBF vector
 // Y * r_j(X), r_j = exp(-|p_j - X|^2 / c^2), into per-side FP64 sums S_j in
 // shared memory.  At the end of the item G_i = -(1/N) sum_j ipsi(j,i) S_j.
+// Exits are queued per warp (side, coordinate, weight) and the warp adds
+// their RBF vectors one exit at a time with the side knots spread over the
+// lanes, into its own copy of the sums (no atomics; the copies are added at
+// the end of the item), so the n_s exponentials of an exit run at full width.
 // By linearity this equals the reference's per-exit
 // H_i = sum_j ipsi(j,i) RBF(p_j, X) accumulation (Meshes/stencil.cpp:244-307)
 // with n_s instead of n_s^2 exponentials per exit.  It is the all-FP64 GPU
@@ -49,7 +53,11 @@ __device__ __forceinline__ void normals_f64(uint32_t ua, uint32_t ub, double& z0
 template <int KIND, bool RICH, int GEOM>
 __global__ void __launch_bounds__(FP64_THREADS)
 k_paths_fp64(const Fp64Args a) {
-  extern __shared__ double Ssum[];  // [sum n] per-side RBF sums, then [sum n] local t
+  // [warps][sum n] per-warp per-side RBF sums, then [sum n] local t
+  extern __shared__ double Ssum[];
+  __shared__ double s_qs[FP64_THREADS / 32][FP64_QCAP], s_qy[FP64_THREADS / 32][FP64_QCAP];
+  __shared__ int s_qd[FP64_THREADS / 32][FP64_QCAP];
+  __shared__ int s_qn[FP64_THREADS / 32];
   __shared__ ItemSide64 s_side[4];
   __shared__ double s_rect[4];
   __shared__ int s_item, s_knot, s_path_end, s_nall;
@@ -116,8 +124,11 @@ k_paths_fp64(const Fp64Args a) {
     __syncthreads();
     const int knot = s_knot, path_end = s_path_end, nall = s_nall;
     const double h = s_h, sqrth = ::sqrt(s_h);
-    double* tloc = Ssum + nall;
-    for (int i = tid; i < nall; i += FP64_THREADS) Ssum[i] = 0.0;
+    constexpr int NW = FP64_THREADS / 32;
+    double* tloc = Ssum + NW * nall;
+    double* Sw = Ssum + warp * nall;  // this warp's sums
+    for (int i = tid; i < NW * nall; i += FP64_THREADS) Ssum[i] = 0.0;
+    if (lane == 0) s_qn[warp] = 0;
     for (int d = 0; d < 4; d++)
       for (int i = tid; i < s_side[d].n; i += FP64_THREADS)
         tloc[s_side[d].s_off + i] = L.sh_t[s_side[d].t_off + i];
@@ -146,16 +157,33 @@ k_paths_fp64(const Fp64Args a) {
       if (d < 0) {
         atomicOr(a.err_flags, ERR_FLAG_EXIT_SIDE);
       } else {
-        const ItemSide64& is = s_side[d];
-        const double sc = along - is.origin;
-        const double yw = wgt * s.Y;
-        for (int j = 0; j < is.n; j++) {
-          const double dt0 = tloc[is.s_off + j] - sc;
-          const double dt = is.R > 0.0 ? 2.0 * is.R * ::sin(0.5 * dt0) : dt0;
-          atomicAdd(Ssum + is.s_off + j, yw * ::exp(-(dt * dt) * is.inv_c2));
-        }
+        // queue the exit: < 32 left over + at most 2 exits per lane and
+        // iteration fit in FP64_QCAP
+        const int e = atomicAdd(&s_qn[warp], 1);
+        s_qd[warp][e] = d;
+        s_qs[warp][e] = along - s_side[d].origin;
+        s_qy[warp][e] = wgt * s.Y;
       }
       return s.Z + s.xi;
+    };
+    // Add the queued exits' RBF vectors to this warp's sums (warp-uniform
+    // call; only when at least minq exits are queued).
+    auto flush = [&](int minq) {
+      __syncwarp();
+      const int n = s_qn[warp];
+      if (n < minq) return;
+      for (int e = 0; e < n; e++) {
+        const ItemSide64& is = s_side[s_qd[warp][e]];
+        const double sc = s_qs[warp][e], yw = s_qy[warp][e];
+        for (int j = lane; j < is.n; j += 32) {
+          const double dt0 = tloc[is.s_off + j] - sc;
+          const double dt = is.R > 0.0 ? 2.0 * is.R * ::sin(0.5 * dt0) : dt0;
+          Sw[is.s_off + j] += yw * ::exp(-(dt * dt) * is.inv_c2);
+        }
+      }
+      __syncwarp();
+      if (lane == 0) s_qn[warp] = 0;
+      __syncwarp();
     };
     auto step_level = [&](Lvl64& s, double i0, double i1, double hh, double sq, double wgt,
                           double& val) -> bool {
@@ -233,42 +261,59 @@ k_paths_fp64(const Fp64Args a) {
     u32x4 blk;
     blk.v[0] = blk.v[1] = blk.v[2] = blk.v[3] = 0;
     while (__any_sync(FULL, active)) {
-      if (!active) continue;
-      if (RICH) {
-        blk = path_block(a.seed, a.instance, (uint32_t)knot, path, m++);
-        double za0, za1, zb0, zb1;
-        normals_f64(blk.v[0], blk.v[1], za0, za1);
-        normals_f64(blk.v[2], blk.v[3], zb0, zb1);
-        const double hf = 0.5 * h, sqf = ::sqrt(hf);
-        if (fine_alive) fine_alive = !step_level(fine, sqf * za0, sqf * za1, hf, sqf, 2.0, val_f);
-        if (fine_alive) fine_alive = !step_level(fine, sqf * zb0, sqf * zb1, hf, sqf, 2.0, val_f);
-        if (coarse_alive)
-          coarse_alive = !step_level(coarse, sqf * (za0 + zb0), sqf * (za1 + zb1), h, sqrth, -1.0, val_c);
-        if (fine_alive || coarse_alive) continue;
-        const double v = 2.0 * val_f - val_c;
-        b += v;
-        bb += v * v;
-        nsteps += fine.steps + coarse.steps;
-      } else {
-        if ((m & 1u) == 0) blk = path_block(a.seed, a.instance, (uint32_t)knot, path, m >> 1);
-        double z0, z1;
-        if (m & 1u) normals_f64(blk.v[2], blk.v[3], z0, z1);
-        else normals_f64(blk.v[0], blk.v[1], z0, z1);
-        ++m;
-        if (!step_level(fine, sqrth * z0, sqrth * z1, h, sqrth, 1.0, val_f)) continue;
-        b += val_f;
-        bb += val_f * val_f;
-        nsteps += fine.steps;
+      if (active) {
+        bool fin = false;  // the lane's path (pair) finished in this iteration
+        if (RICH) {
+          blk = path_block(a.seed, a.instance, (uint32_t)knot, path, m++);
+          double za0, za1, zb0, zb1;
+          normals_f64(blk.v[0], blk.v[1], za0, za1);
+          normals_f64(blk.v[2], blk.v[3], zb0, zb1);
+          const double hf = 0.5 * h, sqf = ::sqrt(hf);
+          if (fine_alive) fine_alive = !step_level(fine, sqf * za0, sqf * za1, hf, sqf, 2.0, val_f);
+          if (fine_alive) fine_alive = !step_level(fine, sqf * zb0, sqf * zb1, hf, sqf, 2.0, val_f);
+          if (coarse_alive)
+            coarse_alive = !step_level(coarse, sqf * (za0 + zb0), sqf * (za1 + zb1), h, sqrth, -1.0, val_c);
+          if (!fine_alive && !coarse_alive) {
+            const double v = 2.0 * val_f - val_c;
+            b += v;
+            bb += v * v;
+            nsteps += fine.steps + coarse.steps;
+            fin = true;
+          }
+        } else {
+          if ((m & 1u) == 0) blk = path_block(a.seed, a.instance, (uint32_t)knot, path, m >> 1);
+          double z0, z1;
+          if (m & 1u) normals_f64(blk.v[2], blk.v[3], z0, z1);
+          else normals_f64(blk.v[0], blk.v[1], z0, z1);
+          ++m;
+          if (step_level(fine, sqrth * z0, sqrth * z1, h, sqrth, 1.0, val_f)) {
+            b += val_f;
+            bb += val_f * val_f;
+            nsteps += fine.steps;
+            fin = true;
+          }
+        }
+        if (fin) {
+          path = atomicAdd(&s_next_path, 1u);
+          if ((int)path >= path_end) {
+            active = false;
+          } else {
+            reset();
+            fine_alive = true;
+            coarse_alive = RICH;
+            m = 0;
+          }
+        }
       }
-      path = atomicAdd(&s_next_path, 1u);
-      if ((int)path >= path_end) {
-        active = false;
-      } else {
-        reset();
-        fine_alive = true;
-        coarse_alive = RICH;
-        m = 0;
-      }
+      flush(32);
+    }
+    flush(1);
+    __syncthreads();
+    // S_j: the warps' sums added in a fixed order, into warp 0's copy
+    for (int i = tid; i < nall; i += FP64_THREADS) {
+      double t = Ssum[i];
+      for (int w = 1; w < NW; w++) t += Ssum[w * nall + i];
+      Ssum[i] = t;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
