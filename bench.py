@@ -224,6 +224,36 @@ def semilinear_newton(local: int, iterations: int = 4, npaths: int = 20_000, h: 
     return out
 
 
+def plain_config1(local: int, reps: int = 3):
+    """The CPU-runnable configuration: Poisson on [-1,1]^2, 4 x 4 subdomains,
+    11 knots per segment (237 knots), 1e4 paths per knot, h = 1e-3, the plain
+    method (fixed step, no Richardson pair, the reference's overwrite of shared
+    side knots), seed 1234, in the three modes: the replay mode (FP64, the
+    reference's per-exit weights, bit-exact with the CPU restatement), plain
+    FP64 and MIXED; device time of the estimate and RMSE of the solved
+    interface against the analytic solution."""
+    import pdds_gb300 as P
+    from pdds_gb300.config import WORKLOADS, fac_rule
+    w = WORKLOADS["poisson_4x4_n11"]
+    bvp = P.BVP.poisson_sincos()
+    pd = P.PDDSparseGM(w["sw"], w["ne"], w["nsub"], w["nnode"], fac_rule(w["ne"][0] - w["sw"][0], w["nsub"],
+                                                                         w["nnode"]), device=local)
+    ex = bvp.u(pd.x, pd.y)
+    out = {"knots": int(pd.K), "paths_per_knot": w["npaths"], "h": w["h"]}
+    for name, mode in (("replay_fp64", P.MODE_REPLAY_FP64), ("fp64", P.MODE_FP64), ("mixed", P.MODE_MIXED)):
+        pd.estimate(bvp, 64, w["h"], mode=mode)  # warm-up
+        ms = []
+        for r in range(reps):
+            est = pd.estimate(bvp, w["npaths"], w["h"], mode=mode, seed=1234)
+            ms.append(est.info["ms_setup"] + est.info["ms_paths"])
+        u, si = pd.solve_interface(P.SOLVE_BICGSTAB_FP64, tol=1e-12)
+        out[name] = {"ms_estimate": float(np.median(ms)), "path_steps": int(est.info["path_steps"]),
+                     "path_steps_per_s": est.info["path_steps"] / (1e-3 * float(np.median(ms))),
+                     "rmse_vs_analytic": float(np.sqrt(np.mean((u - ex) ** 2)))}
+    pd.close()
+    return out
+
+
 def varcoef_lut(local: int, reps: int = 2):
     """The variable-coefficient problem with coefficients served from 1024^2
     FP32 tables (bicubic), 8 x 8 subdomains, 31 knots per segment, 5e4 paths
@@ -335,7 +365,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="poisson_12x12_n43")
     ap.add_argument("--npaths", type=int, default=0)
-    ap.add_argument("--ref-knots", type=int, default=8, help="knots per step of the reference arm")
+    ap.add_argument("--ref-knots", type=int, default=4, help="knots per step of the reference arm")
     ap.add_argument("--cpu-knots", type=int, default=16, help="knots of the cpu_baseline sample (about 10 s)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
@@ -344,6 +374,7 @@ def main():
     ap.add_argument("--no-circle", action="store_true")
     ap.add_argument("--no-semilinear", action="store_true")
     ap.add_argument("--no-lut", action="store_true")
+    ap.add_argument("--no-config1", action="store_true")
     args = ap.parse_args()
 
     from pdds_gb300.config import WORKLOADS, fac_rule
@@ -486,6 +517,8 @@ def main():
         extra["many_instance_batch"] = many_instance_batch(local)
     if not args.no_circle and rank == 0:
         extra["circle_uneven_lengths"] = circle_uneven(local)
+    if not args.no_config1 and rank == 0:
+        extra["config1_plain"] = plain_config1(local)
     if not args.no_lut and rank == 0:
         extra["varcoef_lut"] = varcoef_lut(local)
     if not args.no_semilinear and rank == 0:
