@@ -120,10 +120,12 @@ class ClockSampler:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
-def cpu_baseline(workload: dict, fac, n_knots: int, seed: int = 1234, npaths=None):
+def cpu_baseline(workload: dict, fac, n_knots: int, seed: int = 1234, npaths=None, fast: bool = False):
     """The reference's CPU path restated (oracle): OpenMP over paths with every
     host core, serial O(n_s^2) reduction, libm, per-knot factorisation; on a
-    fixed random sample of knots of the workload (seed 1234)."""
+    fixed random sample of knots of the workload (seed 1234).  fast: the
+    linearity form of the reduction (n_s exponentials per exit, exits reduced
+    in parallel) instead of the reference's, a faster CPU form shown beside."""
     import oracle as O
     L = O.Layout(workload["sw"], workload["ne"], workload["nsub"], workload["nnode"])
     rng = np.random.default_rng(seed)
@@ -136,7 +138,7 @@ def cpu_baseline(workload: dict, fac, n_knots: int, seed: int = 1234, npaths=Non
     sel = sorted(rng.choice(inner, size=min(n_knots, len(inner)), replace=False).tolist())
     N = npaths or workload["npaths"]
     threads = os.cpu_count() or 1
-    prm = O.make_params(N, workload["h"], seed=seed, fac=fac, sublinear=True, threads=threads)
+    prm = O.make_params(N, workload["h"], seed=seed, fac=fac, sublinear=True, threads=threads, fast_reduce=fast)
     if workload.get("problem") == "varcoef_lut":
         from pdds_gb300.config import varcoef_tables
         O.set_lut(*varcoef_tables(workload["lut_n"], (workload["sw"][0], workload["sw"][1],
@@ -528,6 +530,12 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
             cpu = cpu_baseline(workload, fac, args.cpu_knots)
+            fast = cpu_baseline(workload, fac, args.cpu_knots, fast=True)
+            extra["cpu_linearity_form"] = {
+                "value": fast["value"], "unit": "path-steps/s", "cores": fast["cores"],
+                "sample": fast["sample"],
+                "form": "the reference's reduction in its linearity form (n_s exponentials per exit, "
+                        "G = -ipsi^T S / N) with the exits reduced in parallel; same paths"}
         except Exception as exc:  # report, do not fail the bench
             cpu = {"value": None, "unit": "path-steps/s", "cores": os.cpu_count(), "kind": "port",
                    "sample": f"failed: {exc}"}

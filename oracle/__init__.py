@@ -41,6 +41,7 @@ class Params(C.Structure):
         ("fac", C.c_double * 4),
         ("max_steps", C.c_int64),
         ("adaptive_h", C.c_int),
+        ("fast_reduce", C.c_int),
     ]
 
 
@@ -101,7 +102,8 @@ def make_problem(kind: int, *params: float) -> Problem:
 
 
 def make_params(N, h, seed=1234, fac=(1.0, 1.0, 1.0, 1.0), portable=False, sublinear=True,
-                dup_sum=False, threads=None, instance=0, max_steps=10**8, adaptive_h=False) -> Params:
+                dup_sum=False, threads=None, instance=0, max_steps=10**8, adaptive_h=False,
+                fast_reduce=False) -> Params:
     prm = Params()
     prm.N = int(N)
     prm.h = float(h)
@@ -115,6 +117,7 @@ def make_params(N, h, seed=1234, fac=(1.0, 1.0, 1.0, 1.0), portable=False, subli
         prm.fac[i] = float(fac[i])
     prm.max_steps = int(max_steps)
     prm.adaptive_h = int(bool(adaptive_h))
+    prm.fast_reduce = int(bool(fast_reduce))
     return prm
 
 

@@ -495,9 +495,65 @@ int knot_impl(const Layout& L, const orc_problem* P, const orc_params* prm, int 
   for (int n = 0; n < N; n++)
     paths[n] = run_path<M>(pb, st.params, x0, y0, h, sqrth, prm->seed, prm->instance,
                            (uint32_t)knot, (uint32_t)n, prm->sublinear != 0, prm->max_steps);
-  // Reduce_Analytic (EMFKACSolver.hpp:514-575), serial
   double b = 0.0, bb = 0.0;
-  for (int n = 0; n < N; n++) {
+  if (prm->fast_reduce) {
+    // linearity form of Reduce_Analytic + G_update: S_j = sum over the exits
+    // on a side of Y r_j(X), per thread, then G_i = -sum_j ipsi(j,i) S_j
+    int off[5] = {0, 0, 0, 0, 0};
+    for (int d = 0; d < 4; d++) off[d + 1] = off[d] + sd[d].n;
+    const int nthr = prm->threads > 0 ? prm->threads : 1;
+    std::vector<double> Sth((size_t)nthr * off[4], 0.0);
+    int64_t s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+    int err = 0;
+#if defined(_OPENMP)
+#pragma omp parallel for schedule(static) num_threads(nthr) reduction(+ : b, bb, s0, s1, s2, s3) reduction(max : err)
+#endif
+    for (int n = 0; n < N; n++) {
+#if defined(_OPENMP)
+      double* S = Sth.data() + (size_t)omp_get_thread_num() * off[4];
+#else
+      double* S = Sth.data();
+#endif
+      const PathOut& o = paths[n];
+      double Ea[2], Na[2];
+      if (o.status) err = std::max(err, o.status);
+      s0 += o.steps_l;
+      s1 += o.steps_s;
+      const double score_vr = o.Z + o.Y * pb.g(o.x, o.y) + o.xi;
+      if (rect2d(st.global, o.x, o.y, Ea, Na) >= -1e-08) {
+        s2++;
+        b += score_vr;
+        bb += score_vr * score_vr;
+        continue;
+      }
+      s3++;
+      int d = -1;
+      if (std::fabs(o.y - st.params[1]) < 1e-8) d = South;
+      else if (std::fabs(o.y - st.params[3]) < 1e-8) d = North;
+      else if (std::fabs(o.x - st.params[0]) < 1e-8) d = West;
+      else if (std::fabs(o.x - st.params[2]) < 1e-8) d = East;
+      if (d < 0) { err = std::max(err, 1); continue; }
+      for (int j = 0; j < sd[d].n; j++)
+        S[off[d] + j] += o.Y * rbf<M>(st.pos[d][j][0], st.pos[d][j][1], o.x, o.y, sd[d].c);
+      b += o.Z + o.xi;
+      bb += (o.Z + o.xi) * (o.Z + o.xi);
+    }
+    if (err) status = err;
+    stats[0] = s0; stats[1] = s1; stats[2] = s2; stats[3] = s3;
+    for (int d = 0; d < 4; d++)
+      for (int i = 0; i < sd[d].n; i++) {
+        double H = 0.0;
+        for (int j = 0; j < sd[d].n; j++) {
+          double Sj = 0.0;
+          for (int t = 0; t < nthr; t++) Sj += Sth[(size_t)t * off[4] + off[d] + j];
+          H += sd[d].ipsi[(size_t)j * sd[d].n + i] * Sj;
+        }
+        sd[d].G[i] = -H;
+        sd[d].GG[i] = 0.0;
+      }
+  }
+  // Reduce_Analytic (EMFKACSolver.hpp:514-575), serial
+  for (int n = 0; n < N && !prm->fast_reduce; n++) {
     const PathOut& o = paths[n];
     if (o.status) status = o.status;
     stats[0] += o.steps_l;

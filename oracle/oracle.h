@@ -36,6 +36,10 @@ typedef struct {
   double fac[4];       /* RBF shape c per side kind (c2[kind] in the reference) */
   int64_t max_steps;   /* per path, per leg; exceeded -> status 3               */
   int adaptive_h;      /* 1: per-knot h of PDDSparseGM.cpp:4026-4028             */
+  int fast_reduce;     /* 1: not the reference's reduction but its linearity form
+                          (n_s exponentials per exit, G = -ipsi^T S / N), exits
+                          reduced in parallel; G_var is not computed.  A faster
+                          CPU form for comparison only, never a parity check. */
 } orc_params;
 
 /* ---- layout ---------------------------------------------------------------*/

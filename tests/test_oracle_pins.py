@@ -188,3 +188,23 @@ def test_bicgstab_reproduces_recorded_solution(ref):
     np.testing.assert_allclose(u, sol[:, 4], rtol=2e-6, atol=0)
     rmse = np.sqrt(np.mean((u - sol[:, 3]) ** 2))
     assert abs(rmse - 0.020935) < 5e-5
+
+
+def test_linearity_form_matches_the_reference_reduction():
+    """The faster CPU form timed beside the faithful one (n_s exponentials per
+    exit, G = -ipsi^T S / N, exits reduced in parallel) gives the same G and B
+    on the same paths, up to rounding amplified by cond(Psi) (~1e9 here: the
+    two forms sum the exponentials in different orders), far below the Monte
+    Carlo error of G (~1e-3)."""
+    L = O.Layout((-1, -1), (1, 1), 4, 11)
+    prob = O.make_problem(O.POISSON_SINCOS)
+    sel = [3, 40, 111]
+    from pdds_gb300.config import fac_rule
+    fac = fac_rule(2.0, 4, 11)
+    ref = L.run(prob, O.make_params(400, 1e-3, seed=9, fac=fac, threads=2), knots=sel)
+    fast = L.run(prob, O.make_params(400, 1e-3, seed=9, fac=fac, threads=2, fast_reduce=True), knots=sel)
+    assert ref["status"] == 0 and fast["status"] == 0
+    assert np.array_equal(ref["gj"], fast["gj"]) and np.array_equal(ref["row_ptr"], fast["row_ptr"])
+    np.testing.assert_allclose(fast["g"], ref["g"], rtol=0, atol=1e-6)
+    np.testing.assert_allclose(fast["B"], ref["B"], rtol=1e-12, atol=1e-12)
+    assert np.array_equal(fast["stats"], ref["stats"])
