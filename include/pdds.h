@@ -61,7 +61,17 @@ typedef enum {
   PDDS_VARCOEF = 3,        /* sigma = diag(1+x^2/2, 1+y^2/2), b = (y,-x),
                               c = -(1+x^2+y^2), u = e^x cos 2y + 1                      */
   PDDS_LUT = 4,            /* diagonal sigma, b, c, f, grad u and g served from tables  */
-  PDDS_CIRCLE_POISSON = 5  /* u = r^2 sin(3 theta) + cos x, sigma = sqrt2 I, f = -Lap u  */
+  PDDS_CIRCLE_POISSON = 5, /* u = r^2 sin(3 theta) + cos x, sigma = sqrt2 I, f = -Lap u  */
+  PDDS_ROBIN_POISSON = 6   /* BVPs/EDPs/poisson_3.hpp: Lap u + f = 0 with
+                              u = sin(pi(0.23x + 0.49y)) + cos(pi(0.331x + 0.667y)),
+                              Dirichlet g = u except on the Robin side p[0] (one of
+                              N 1, S 2, E 4, W 8, or 0 for none; the reference's
+                              Stopping_mix takes W), where du/dn - varphi u = psi with
+                              varphi = -2 + sin(pi y): paths reflect there with
+                              Lepingle's step and carry the local-time terms.
+                              Knots on the Robin side keep B = g as in the
+                              reference's boundary shortcut.  MIXED and FP64
+                              modes, rectangular layouts.                        */
 } pdds_problem_kind;
 
 typedef struct {

@@ -18,7 +18,7 @@ STATUS_NAMES = {0: "PDDS_OK", 1: "PDDS_ERR_INVALID", 2: "PDDS_ERR_CUDA", 3: "PDD
                 4: "PDDS_ERR_TIMEOUT", 5: "PDDS_ERR_ILL_CONDITIONED", 6: "PDDS_ERR_NOT_CONVERGED",
                 7: "PDDS_ERR_NO_MEMORY", 8: "PDDS_ERR_EXIT_SIDE"}
 
-POISSON_SINCOS, MONEGROS, HELMHOLTZ, VARCOEF, LUT, CIRCLE_POISSON = 0, 1, 2, 3, 4, 5
+POISSON_SINCOS, MONEGROS, HELMHOLTZ, VARCOEF, LUT, CIRCLE_POISSON, ROBIN_POISSON = 0, 1, 2, 3, 4, 5, 6
 MODE_REPLAY_FP64, MODE_FP64, MODE_MIXED = 0, 1, 2
 SOLVE_BICGSTAB_FP64, SOLVE_GMRES_FP32_IR = 0, 1
 

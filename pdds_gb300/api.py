@@ -35,6 +35,8 @@ class BVP:
     VARCOEF = capi.VARCOEF
     LUT = capi.LUT
     CIRCLE_POISSON = capi.CIRCLE_POISSON
+    ROBIN_POISSON = capi.ROBIN_POISSON
+    ROBIN_SIDES = {"N": 1, "S": 2, "E": 4, "W": 8}
 
     def __init__(self, kind: int, params=(), use_cv: bool = True, tables=None, exact=None):
         self.kind = int(kind)
@@ -52,6 +54,14 @@ class BVP:
     def circle_poisson(cls):
         """Lap u = f on the unit disk with u = r^2 sin(3 theta) + cos x (sigma = sqrt2 I)."""
         return cls(cls.CIRCLE_POISSON)
+
+    @classmethod
+    def robin_poisson(cls, side: str = "W"):  # side None: Dirichlet everywhere
+        """Lap u + f = 0 with u = sin(pi(0.23x + 0.49y)) + cos(pi(0.331x + 0.667y))
+        (BVPs/EDPs/poisson_3.hpp); on the given side of the layout rectangle the
+        Robin condition du/dn - varphi u = psi, varphi = -2 + sin(pi y), instead
+        of Dirichlet data: paths reflect there (Lepingle's step)."""
+        return cls(cls.ROBIN_POISSON, (float(cls.ROBIN_SIDES[side]) if side else 0.0,))
 
     @classmethod
     def monegros(cls):
@@ -106,6 +116,8 @@ class BVP:
         if self.kind == self.CIRCLE_POISSON:
             r = np.hypot(x, y)
             return r * r * np.sin(3.0 * np.arctan2(y, x)) + np.cos(x)
+        if self.kind == self.ROBIN_POISSON:
+            return np.sin(np.pi * (0.23 * x + 0.49 * y)) + np.cos(np.pi * (0.331 * x + 0.667 * y))
         q = 1.0 + 0.01 * x * x + 0.02 * y * y
         return 3.0 + 0.333 * (np.sin(np.sqrt(q)) +
                               np.tanh(np.sin(0.12 * x + 0.05 * y) + np.sin(0.05 * x - 0.12 * y)))

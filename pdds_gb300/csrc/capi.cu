@@ -485,7 +485,13 @@ const char* pdds_last_error(const pdds_ctx* ctx) { return ctx ? ctx->err.c_str()
 
 pdds_status pdds_problem_set(pdds_ctx* ctx, const pdds_problem_desc* desc) {
   if (!ctx || !desc) return PDDS_ERR_INVALID;
-  if (desc->kind < 0 || desc->kind > 5) return fail(ctx, PDDS_ERR_INVALID, "unknown problem kind");
+  if (desc->kind < 0 || desc->kind > 6) return fail(ctx, PDDS_ERR_INVALID, "unknown problem kind");
+  if (desc->kind == PDDS_ROBIN_POISSON) {
+    const double mk = desc->p[0];
+    if (!(mk == 0.0 || mk == 1.0 || mk == 2.0 || mk == 4.0 || mk == 8.0))
+      return fail(ctx, PDDS_ERR_INVALID,
+                  "PDDS_ROBIN_POISSON: p[0] names at most one Robin side (N 1, S 2, E 4, W 8; 0 none)");
+  }
   if (desc->kind == PDDS_LUT && ctx->lut_nx < 4)
     return fail(ctx, PDDS_ERR_INVALID, "PDDS_LUT needs pdds_problem_set_lut first");
   if (desc->kind == PDDS_HELMHOLTZ && desc->p[2] > 0.0)
@@ -637,6 +643,8 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
     return fail(ctx, PDDS_ERR_INVALID, "circle layouts take the sigma = sqrt2 I problems");
   if (mode == PDDS_MODE_REPLAY_FP64 && ctx->prob.kind == PDDS_CIRCLE_POISSON)
     return fail(ctx, PDDS_ERR_INVALID, "the circle problem has no replay form");
+  if (mode == PDDS_MODE_REPLAY_FP64 && ctx->prob.kind == PDDS_ROBIN_POISSON)
+    return fail(ctx, PDDS_ERR_INVALID, "the Robin problem has no replay form (MIXED and FP64 modes)");
   if (desc->adaptive_n && mode != PDDS_MODE_MIXED)
     return fail(ctx, PDDS_ERR_INVALID, "variance-adaptive paths (adaptive_n) run in PDDS_MODE_MIXED");
   if (desc->adaptive_n && desc->target_stderr < 0.0) return fail(ctx, PDDS_ERR_INVALID, "target_stderr < 0");

@@ -79,7 +79,7 @@ struct ProblemDev {
   LutDev lut;
 };
 
-enum { PK_POISSON_SINCOS = 0, PK_MONEGROS = 1, PK_HELMHOLTZ = 2, PK_VARCOEF = 3, PK_LUT = 4, PK_CIRCLE = 5 };
+enum { PK_POISSON_SINCOS = 0, PK_MONEGROS = 1, PK_HELMHOLTZ = 2, PK_VARCOEF = 3, PK_LUT = 4, PK_CIRCLE = 5, PK_ROBIN = 6 };
 
 // Problem parameters of the instance that owns knot k (batches), else P's own.
 __device__ __forceinline__ void instance_params(const DevLayout& L, int k, ProblemDev& P, uint32_t& rng_inst,
@@ -265,6 +265,17 @@ __device__ __forceinline__ void coef_f32(const ProblemDev& P, float x, float y, 
     k.f = 5.f * s3 + cx;
     k.g0 = r * (2.f * s3 * c1 - 3.f * c3 * s1) - sx;
     k.g1 = r * (2.f * s3 * s1 + 3.f * c3 * c1);
+  } else if (KIND == PK_ROBIN) {
+    // BVPs/EDPs/poisson_3.hpp: u = sin(A) + cos(B), A = pi (0.23 x + 0.49 y),
+    // B = pi (0.331 x + 0.667 y), f = -Lap u
+    float sa, ca, sb, cb;
+    __sincosf(PI * (0.23f * x + 0.49f * y), &sa, &ca);
+    __sincosf(PI * (0.331f * x + 0.667f * y), &sb, &cb);
+    k.s00 = 1.41421356f; k.s01 = 0.f; k.s10 = 0.f; k.s11 = 1.41421356f;
+    k.b0 = 0.f; k.b1 = 0.f; k.c = 0.f;
+    k.f = 9.8696044f * (0.2930f * sa + 0.554450f * cb);
+    k.g0 = PI * (0.23f * ca - 0.331f * sb);
+    k.g1 = PI * (0.49f * ca - 0.667f * sb);
   } else {  // PK_MONEGROS (BVPs/EDPs/Monegros_Poisson_CPP.hpp)
     const float k2 = 0.01f, k3 = 0.02f, k4 = 0.12f, k5 = 0.05f, k6 = 0.05f, k7 = -0.12f, sf = 0.333f;
     const float q = 1.f + k2 * x * x + k3 * y * y;
@@ -297,8 +308,8 @@ __device__ __forceinline__ void coef_f32(const ProblemDev& P, float x, float y, 
 // drift; react kinds have a reaction term c.
 template <int KIND>
 struct KindTraits {
-  static constexpr bool iso =
-      KIND == PK_POISSON_SINCOS || KIND == PK_MONEGROS || KIND == PK_HELMHOLTZ || KIND == PK_CIRCLE;
+  static constexpr bool iso = KIND == PK_POISSON_SINCOS || KIND == PK_MONEGROS || KIND == PK_HELMHOLTZ ||
+                              KIND == PK_CIRCLE || KIND == PK_ROBIN;
   static constexpr bool react = KIND == PK_HELMHOLTZ || KIND == PK_VARCOEF || KIND == PK_LUT;
 };
 
@@ -354,6 +365,8 @@ __device__ __forceinline__ float u_f32(const ProblemDev& P, float x, float y) {
     const float r = sqrtf(x * x + y * y);
     const float s1 = r > 1e-30f ? y / r : 0.f;
     return r * r * (s1 * (3.f - 4.f * s1 * s1)) + __cosf(x);
+  } else if (KIND == PK_ROBIN) {
+    return __sinf(3.14159265f * (0.23f * x + 0.49f * y)) + __cosf(3.14159265f * (0.331f * x + 0.667f * y));
   } else {
     const float q = 1.f + 0.01f * x * x + 0.02f * y * y;
     return 3.f + 0.333f * (__sinf(sqrtf(q)) + tanhf(__sinf(0.12f * x + 0.05f * y) + __sinf(0.05f * x - 0.12f * y)));
@@ -412,6 +425,15 @@ __device__ __forceinline__ void coef_f64(const ProblemDev& P, double x, double y
     k.f = 5.0 * s3 + cx;
     k.g0 = r * (2.0 * s3 * c1 - 3.0 * c3 * s1) - sx;
     k.g1 = r * (2.0 * s3 * s1 + 3.0 * c3 * c1);
+  } else if (KIND == PK_ROBIN) {
+    double sa, ca, sb, cb;
+    sincospi(0.23 * x + 0.49 * y, &sa, &ca);
+    sincospi(0.331 * x + 0.667 * y, &sb, &cb);
+    k.s00 = 1.4142135623730951; k.s01 = 0.0; k.s10 = 0.0; k.s11 = 1.4142135623730951;
+    k.b0 = 0.0; k.b1 = 0.0; k.c = 0.0;
+    k.f = 9.869604401089358 * (0.2930 * sa + 0.554450 * cb);
+    k.g0 = PI * (0.23 * ca - 0.331 * sb);
+    k.g1 = PI * (0.49 * ca - 0.667 * sb);
   } else {
     const double k2 = 0.01, k3 = 0.02, k4 = 0.12, k5 = 0.05, k6 = 0.05, k7 = -0.12, sf = 0.333;
     const double q = 1.0 + k2 * x * x + k3 * y * y;
@@ -453,10 +475,34 @@ __device__ __forceinline__ double u_f64(const ProblemDev& P, double x, double y)
     const double r = ::sqrt(x * x + y * y);
     const double s1 = r > 1e-300 ? y / r : 0.0;
     return r * r * (s1 * (3.0 - 4.0 * s1 * s1)) + ::cos(x);
+  } else if (KIND == PK_ROBIN) {
+    return sinpi(0.23 * x + 0.49 * y) + cospi(0.331 * x + 0.667 * y);
   } else {
     const double q = 1.0 + 0.01 * x * x + 0.02 * y * y;
     return 3.0 + 0.333 * (::sin(::sqrt(q)) + ::tanh(::sin(0.12 * x + 0.05 * y) + ::sin(0.05 * x - 0.12 * y)));
   }
+}
+
+// Robin data of PK_ROBIN (poisson_3.hpp): varphi = -2 + sin(pi y) and
+// psi = n.grad u - varphi u at a boundary point with outward normal n, so
+// that n.grad u - varphi u = psi there; along a reflected path
+// Y += varphi Y dL and Z += psi Y dL with dL the local time.
+template <typename T>
+__device__ __forceinline__ void robin_data(T x, T y, T n0, T n1, T& varphi, T& psi) {
+  const T PI = T(3.141592653589793);
+  T sa, ca, sb, cb, sy;
+  if constexpr (sizeof(T) == 4) {
+    __sincosf(PI * (T(0.23) * x + T(0.49) * y), &sa, &ca);
+    __sincosf(PI * (T(0.331) * x + T(0.667) * y), &sb, &cb);
+    sy = __sinf(PI * y);
+  } else {
+    sincospi(T(0.23) * x + T(0.49) * y, &sa, &ca);
+    sincospi(T(0.331) * x + T(0.667) * y, &sb, &cb);
+    sy = sinpi(y);
+  }
+  const T gx = PI * (T(0.23) * ca - T(0.331) * sb), gy = PI * (T(0.49) * ca - T(0.667) * sb);
+  varphi = T(-2) + sy;
+  psi = n0 * gx + n1 * gy - (sa + cb) * varphi;
 }
 
 // ------------------------------------------------------------------ rectangle

@@ -138,6 +138,16 @@ k_paths_fp64(const Fp64Args a) {
     const double rect[4] = {s_rect[0], s_rect[1], s_rect[2], s_rect[3]};
     const double pa0 = GEOM == 1 ? ::cos(rect[1]) : 0.0, pa1 = GEOM == 1 ? ::sin(rect[1]) : 0.0;
     const double pb0 = GEOM == 1 ? ::cos(rect[3]) : 0.0, pb1 = GEOM == 1 ? ::sin(rect[3]) : 0.0;
+    // PK_ROBIN: the reflecting stencil side (a global side in the Robin set
+    // P.p[0], bits N 1, S 2, E 4, W 8), its line n . (x, y) = rc
+    const int globmask = (s_side[0].glob ? 1 : 0) | (s_side[1].glob ? 2 : 0) | (s_side[2].glob ? 4 : 0) |
+                         (s_side[3].glob ? 8 : 0);
+    const int rmask = KIND == PK_ROBIN ? (globmask & (int)a.P.p[0]) : 0;
+    double rn0 = 0.0, rn1 = 0.0, rc = 0.0;
+    if (rmask & 1) { rn1 = 1.0; rc = rect[3]; }
+    else if (rmask & 2) { rn1 = -1.0; rc = -rect[1]; }
+    else if (rmask & 4) { rn0 = 1.0; rc = rect[2]; }
+    else if (rmask & 8) { rn0 = -1.0; rc = -rect[0]; }
     Coef<double> k0;
     coef_f64<KIND>(a.P, x0, y0, k0);
     const int chunk = item % a.chunks;
@@ -185,15 +195,37 @@ k_paths_fp64(const Fp64Args a) {
       if (lane == 0) s_qn[warp] = 0;
       __syncwarp();
     };
-    auto step_level = [&](Lvl64& s, double i0, double i1, double hh, double sq, double wgt,
-                          double& val) -> bool {
+    // ex: Exp(1) sample of the reflected step (PK_ROBIN), see k_mixed.cu
+    auto step_level = [&](Lvl64& s, double i0, double i1, double hh, double sq, double wgt, double& val,
+                          double ex) -> bool {
       const double v0 = -(s.k.s00 * s.k.g0 + s.k.s10 * s.k.g1);
       const double v1 = -(s.k.s01 * s.k.g0 + s.k.s11 * s.k.g1);
       s.xi += s.Y * (v0 * i0 + v1 * i1);
       s.Z += s.k.f * s.Y * hh;
       s.Y += s.k.c * s.Y * hh;
-      s.x += s.k.b0 * hh + (s.k.s00 * i0 + s.k.s01 * i1);
-      s.y += s.k.b1 * hh + (s.k.s10 * i0 + s.k.s11 * i1);
+      if constexpr (KIND == PK_ROBIN) {
+        const double d0 = s.k.s00 * i0, d1 = s.k.s11 * i1;
+        double dL = 0.0;
+        if (rmask) {
+          const double dR = rn0 * s.x + rn1 * s.y - rc;
+          const double U = rn0 * d0 + rn1 * d1;
+          const double M = 0.5 * (U + ::sqrt(U * U + 4.0 * hh * ex));  // |sigma^T n|^2 = 2
+          dL = ::fmax(0.0, M + dR);
+          if (dL > 0.0) {  // exact in dL, as in k_mixed.cu
+            double vphi, psi;
+            robin_data<double>(s.x - dR * rn0, s.y - dR * rn1, rn0, rn1, vphi, psi);
+            const double t = vphi * dL;
+            const double em1 = ::expm1(t);
+            s.Z += psi * s.Y * (t != 0.0 ? em1 / vphi : dL);
+            s.Y += s.Y * em1;
+          }
+        }
+        s.x += d0 - dL * rn0;
+        s.y += d1 - dL * rn1;
+      } else {
+        s.x += s.k.b0 * hh + (s.k.s00 * i0 + s.k.s01 * i1);
+        s.y += s.k.b1 * hh + (s.k.s10 * i0 + s.k.s11 * i1);
+      }
       ++s.steps;
       coef_f64<KIND>(a.P, s.x, s.y, s.k);
       if constexpr (GEOM == 1) {
@@ -230,6 +262,26 @@ k_paths_fp64(const Fp64Args a) {
         }
         val = exit_level(s, wgt, Ex, Ey, d, d == 0 && s_side[0].glob, along);
         return true;
+      } else if constexpr (KIND == PK_ROBIN) {
+        // absorbing sides only; the exit side is the one with the largest
+        // outside distance (ties S, N, W, E), the other coordinate clamped
+        const double o0 = (rmask & 1) ? -1e300 : s.y - rect[3], o1 = (rmask & 2) ? -1e300 : rect[1] - s.y;
+        const double o2 = (rmask & 4) ? -1e300 : s.x - rect[2], o3 = (rmask & 8) ? -1e300 : rect[0] - s.x;
+        int d = 1;
+        double mx = o1;
+        if (o0 > mx) { mx = o0; d = 0; }
+        if (o3 > mx) { mx = o3; d = 3; }
+        if (o2 > mx) { mx = o2; d = 2; }
+        if (mx < -0.5826 * 1.4142135623730951 * sq) {
+          if (s.steps < (unsigned)a.max_steps) return false;
+          atomicOr(a.err_flags, ERR_FLAG_STEP_LIMIT);
+          val = 0.0;
+          return true;
+        }
+        const double Ex = d == 3 ? rect[0] : (d == 2 ? rect[2] : ::fmin(::fmax(s.x, rect[0]), rect[2]));
+        const double Ey = d == 1 ? rect[1] : (d == 0 ? rect[3] : ::fmin(::fmax(s.y, rect[1]), rect[3]));
+        val = exit_level(s, wgt, Ex, Ey, d, s_side[d].glob != 0, s_side[d].orient == 0 ? Ex : Ey);
+        return true;
       } else {
         double Ex, Ey, Nx, Ny;
         int onmask;
@@ -264,15 +316,24 @@ k_paths_fp64(const Fp64Args a) {
       if (active) {
         bool fin = false;  // the lane's path (pair) finished in this iteration
         if (RICH) {
-          blk = path_block(a.seed, a.instance, (uint32_t)knot, path, m++);
+          const unsigned mi = m++;
+          blk = path_block(a.seed, a.instance, (uint32_t)knot, path, mi);
           double za0, za1, zb0, zb1;
           normals_f64(blk.v[0], blk.v[1], za0, za1);
           normals_f64(blk.v[2], blk.v[3], zb0, zb1);
+          double x0e = 0.0, x1e = 0.0, x2e = 0.0;  // Exp(1) samples of reflected steps
+          if (KIND == PK_ROBIN && rmask) {
+            const u32x4 bx = path_block(a.seed, a.instance, (uint32_t)knot | 0x80000000u, path, mi);
+            x0e = -::log(u01_fp64(bx.v[0]));
+            x1e = -::log(u01_fp64(bx.v[1]));
+            x2e = -::log(u01_fp64(bx.v[2]));
+          }
           const double hf = 0.5 * h, sqf = ::sqrt(hf);
-          if (fine_alive) fine_alive = !step_level(fine, sqf * za0, sqf * za1, hf, sqf, 2.0, val_f);
-          if (fine_alive) fine_alive = !step_level(fine, sqf * zb0, sqf * zb1, hf, sqf, 2.0, val_f);
+          if (fine_alive) fine_alive = !step_level(fine, sqf * za0, sqf * za1, hf, sqf, 2.0, val_f, x0e);
+          if (fine_alive) fine_alive = !step_level(fine, sqf * zb0, sqf * zb1, hf, sqf, 2.0, val_f, x1e);
           if (coarse_alive)
-            coarse_alive = !step_level(coarse, sqf * (za0 + zb0), sqf * (za1 + zb1), h, sqrth, -1.0, val_c);
+            coarse_alive =
+                !step_level(coarse, sqf * (za0 + zb0), sqf * (za1 + zb1), h, sqrth, -1.0, val_c, x2e);
           if (!fine_alive && !coarse_alive) {
             const double v = 2.0 * val_f - val_c;
             b += v;
@@ -285,8 +346,13 @@ k_paths_fp64(const Fp64Args a) {
           double z0, z1;
           if (m & 1u) normals_f64(blk.v[2], blk.v[3], z0, z1);
           else normals_f64(blk.v[0], blk.v[1], z0, z1);
+          double xe = 0.0;
+          if (KIND == PK_ROBIN && rmask) {
+            const u32x4 bx = path_block(a.seed, a.instance, (uint32_t)knot | 0x80000000u, path, m >> 1);
+            xe = -::log(u01_fp64(bx.v[m & 1u]));
+          }
           ++m;
-          if (step_level(fine, sqrth * z0, sqrth * z1, h, sqrth, 1.0, val_f)) {
+          if (step_level(fine, sqrth * z0, sqrth * z1, h, sqrth, 1.0, val_f, xe)) {
             b += val_f;
             bb += val_f * val_f;
             nsteps += fine.steps;
@@ -384,6 +450,7 @@ static cudaError_t launch_fp64_t(const Fp64Args& a, int kind, int grid, size_t s
       PDDS_FP64_CASE(3, 0)
       PDDS_FP64_CASE(4, 0)
       PDDS_FP64_CASE(5, 0)
+      PDDS_FP64_CASE(6, 0)
       default: return cudaErrorInvalidValue;
     }
   }

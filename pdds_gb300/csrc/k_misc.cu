@@ -98,6 +98,7 @@ cudaError_t launch_boundary_b(const DevLayout& L, const ProblemDev& P, int mode,
     case PK_HELMHOLTZ: k_boundary<PK_HELMHOLTZ><<<g, 128, 0, s>>>(L, P, portable, knots, n, B, BB); break;
     case PK_LUT: k_boundary<PK_LUT><<<g, 128, 0, s>>>(L, P, portable, knots, n, B, BB); break;
     case PK_CIRCLE: k_boundary<PK_CIRCLE><<<g, 128, 0, s>>>(L, P, 0, knots, n, B, BB); break;
+    case PK_ROBIN: k_boundary<PK_ROBIN><<<g, 128, 0, s>>>(L, P, 0, knots, n, B, BB); break;
     default: k_boundary<PK_VARCOEF><<<g, 128, 0, s>>>(L, P, portable, knots, n, B, BB); break;
   }
   return cudaGetLastError();

@@ -242,6 +242,23 @@ k_paths_mixed(const MixedArgs a) {
     // bit d set when stencil side d lies on the global boundary
     const int globmask = (s_side[0].glob ? 1 : 0) | (s_side[1].glob ? 2 : 0) | (s_side[2].glob ? 4 : 0) |
                          (s_side[3].glob ? 8 : 0);
+    // PK_ROBIN: the stencil side on the Robin part of the boundary (P.p[0],
+    // bits N 1, S 2, E 4, W 8) reflects instead of absorbing; its line is
+    // n . (x, y) = rc with the outward unit normal n
+    const int rmask = KIND == PK_ROBIN ? (globmask & (int)P.p[0]) : 0;
+    float rn0 = 0.f, rn1 = 0.f, rc = 0.f;
+    if (rmask & 1) { rn1 = 1.f; rc = rect[3]; }
+    else if (rmask & 2) { rn1 = -1.f; rc = -rect[1]; }
+    else if (rmask & 4) { rn0 = 1.f; rc = rect[2]; }
+    else if (rmask & 8) { rn0 = -1.f; rc = -rect[0]; }
+    // outside distances to the absorbing sides (N, S, E, W order of the side
+    // index), the reflecting side excluded
+    auto absorb_out = [&](float x, float y, float* o) {
+      o[0] = (rmask & 1) ? -3.0e38f : y - rect[3];
+      o[1] = (rmask & 2) ? -3.0e38f : rect[1] - y;
+      o[2] = (rmask & 4) ? -3.0e38f : x - rect[2];
+      o[3] = (rmask & 8) ? -3.0e38f : rect[0] - x;
+    };
     unsigned path = (unsigned)(s_p0 + tid);
     bool active = (int)path < path_end;
     // per-lane B sums in compensated FP32 (Kahan), folded into FP64 per item:
@@ -272,7 +289,14 @@ k_paths_mixed(const MixedArgs a) {
     // otherwise e = dW and thr = -0.5826 sqrt(h), scaled by |N^T sigma| here.
     // The control-variate sum xi = -sum Y grad u . sigma dW is always
     // accumulated; the exit drops it when the control variate is off.
-    auto advance = [&](Lvl<KIND>& s, float e0, float e1, float hh, float thr) -> bool {
+    // PK_ROBIN with a reflecting side: Lepingle's reflected Euler step
+    // (FKACIntegrator.hpp:116-165 restated from the published scheme): with
+    // U = n . sigma dW and an Exp(1) sample ex, the largest outward excursion
+    // of the step is M = (U + sqrt(U^2 + 2 |sigma^T n|^2 h ex)) / 2 (the
+    // maximum of the Brownian bridge); the local time dL = max(0, M + d),
+    // d the signed distance to the side (negative inside), pushes the path
+    // back along -n and enters dZ = psi Y dL, dY = varphi Y dL.
+    auto advance = [&](Lvl<KIND>& s, float e0, float e1, float hh, float thr, float ex) -> bool {
       Coef<float> k;
       if constexpr (KIND == PK_LUT) {
         k.s00 = s.cf[0]; k.s11 = s.cf[1];
@@ -286,7 +310,31 @@ k_paths_mixed(const MixedArgs a) {
       s.xi -= s.Y * (k.g0 * d0 + k.g1 * d1);
       s.Z += k.f * s.Y * hh;
       if constexpr (KindTraits<KIND>::react) s.Y += k.c * s.Y * hh;
-      if constexpr (KindTraits<KIND>::iso) {
+      if constexpr (KIND == PK_ROBIN) {
+        float dL = 0.f;
+        if (rmask) {
+          const float dR = rn0 * s.x + rn1 * s.y - rc;
+          const float U = rn0 * d0 + rn1 * d1;
+          const float M = 0.5f * (U + sqrt_approx(U * U + 4.f * hh * ex));  // |sigma^T n|^2 = 2
+          dL = fmaxf(0.f, M + dR);
+          if (dL > 0.f) {
+            // dY = varphi Y dL and dZ = psi Y dL integrated exactly over dL:
+            // an Euler update would leave an O(sqrt h) bias (sum of dL^2)
+            float vphi, psi;
+            robin_data<float>(s.x - dR * rn0, s.y - dR * rn1, rn0, rn1, vphi, psi);
+            const float t = vphi * dL;
+            const float em1 = expm1f(t);
+            s.Z += psi * s.Y * (t != 0.f ? em1 / vphi : dL);
+            s.Y += s.Y * em1;
+          }
+        }
+        s.x += d0 - dL * rn0;
+        s.y += d1 - dL * rn1;
+        ++s.steps;
+        float o[4];
+        absorb_out(s.x, s.y, o);
+        return !(fmaxf(fmaxf(o[0], o[1]), fmaxf(o[2], o[3])) < thr) || s.steps >= (unsigned)a.max_steps;
+      } else if constexpr (KindTraits<KIND>::iso) {
         s.x += d0;
         s.y += d1;
       } else {
@@ -330,6 +378,11 @@ k_paths_mixed(const MixedArgs a) {
           float d_in, d_out, d_a, d_b;
           polar_out(x, y, d_in, d_out, d_a, d_b);
           dist = fmaxf(fmaxf(d_in, d_out), fmaxf(d_a, d_b));
+          wn = 1.41421356f;
+        } else if constexpr (KIND == PK_ROBIN) {
+          float o[4];
+          absorb_out(x, y, o);
+          dist = fmaxf(fmaxf(o[0], o[1]), fmaxf(o[2], o[3]));
           wn = 1.41421356f;
         } else {
           float Ex, Ey, Nx, Ny;
@@ -398,18 +451,35 @@ k_paths_mixed(const MixedArgs a) {
           }
         }
       } else if (ok) {
-        const float dx = fabsf(x - cx) - hx, dy = fabsf(y - cy) - hy;
-        const bool xs = dx > dy;
-        const float Ex = xs ? (x > cx ? rect[2] : rect[0]) : fminf(fmaxf(x, rect[0]), rect[2]);
-        const float Ey = xs ? fminf(fmaxf(y, rect[1]), rect[3]) : (y > cy ? rect[3] : rect[1]);
-        const bool onS = Ey == rect[1], onN = Ey == rect[3], onW = Ex == rect[0], onE = Ex == rect[2];
-        const int onmask = (onN ? 1 : 0) | (onS ? 2 : 0) | (onE ? 4 : 0) | (onW ? 8 : 0);
+        float Ex, Ey;
+        int onmask, d;
+        if constexpr (KIND == PK_ROBIN) {
+          // the absorbing side with the largest outside distance (ties S, N,
+          // W, E), the other coordinate clamped to it
+          float o[4];
+          absorb_out(x, y, o);
+          d = 1;
+          float mx = o[1];
+          if (o[0] > mx) { mx = o[0]; d = 0; }
+          if (o[3] > mx) { mx = o[3]; d = 3; }
+          if (o[2] > mx) { mx = o[2]; d = 2; }
+          Ex = d == 3 ? rect[0] : (d == 2 ? rect[2] : fminf(fmaxf(x, rect[0]), rect[2]));
+          Ey = d == 1 ? rect[1] : (d == 0 ? rect[3] : fminf(fmaxf(y, rect[1]), rect[3]));
+          onmask = 1 << d;
+        } else {
+          const float dx = fabsf(x - cx) - hx, dy = fabsf(y - cy) - hy;
+          const bool xs = dx > dy;
+          Ex = xs ? (x > cx ? rect[2] : rect[0]) : fminf(fmaxf(x, rect[0]), rect[2]);
+          Ey = xs ? fminf(fmaxf(y, rect[1]), rect[3]) : (y > cy ? rect[3] : rect[1]);
+          const bool onS = Ey == rect[1], onN = Ey == rect[3], onW = Ex == rect[0], onE = Ex == rect[2];
+          onmask = (onN ? 1 : 0) | (onS ? 2 : 0) | (onE ? 4 : 0) | (onW ? 8 : 0);
+          d = onS ? 1 : (onN ? 0 : (onW ? 3 : 2));
+        }
         if (onmask & globmask) {
           ++nglob;
           val += Y * u_f32<KIND>(P, Ex, Ey);
         } else {
           ++nsten;
-          const int d = onS ? 1 : (onN ? 0 : (onW ? 3 : 2));
           const ItemSide& is = s_side[d];
           if (is.n > 0) {
             const float sc = is.orient == 0 ? Ex : Ey;
@@ -506,10 +576,20 @@ k_paths_mixed(const MixedArgs a) {
     unsigned m = 0;
     while (__any_sync(FULL, active)) {
       if (active) {
-        const u32x4 blk = path_block_rk(a.rk, rng_inst, rng_knot, path, m++);
+        const unsigned mi = m++;
+        const u32x4 blk = path_block_rk(a.rk, rng_inst, rng_knot, path, mi);
         float za0, za1, zb0, zb1;
         normals_f32(blk.v[0], blk.v[1], za0, za1);
         normals_f32(blk.v[2], blk.v[3], zb0, zb1);
+        // Exp(1) samples of the reflected steps: a second Philox block with
+        // the knot word's top bit set (fine A, fine B, coarse)
+        float x0e = 0.f, x1e = 0.f, x2e = 0.f;
+        if (KIND == PK_ROBIN && rmask) {
+          const u32x4 bx = path_block_rk(a.rk, rng_inst, rng_knot | 0x80000000u, path, mi);
+          x0e = -0.69314718f * lg2_approx(fmaf((float)bx.v[0], 2.3283064e-10f, 1.1641532e-10f));
+          x1e = -0.69314718f * lg2_approx(fmaf((float)bx.v[1], 2.3283064e-10f, 1.1641532e-10f));
+          x2e = -0.69314718f * lg2_approx(fmaf((float)bx.v[2], 2.3283064e-10f, 1.1641532e-10f));
+        }
         if (RICH) {
           // Richardson pair: two fine steps of h/2 and one coarse step of h
           // on the same Brownian increments (dW_coarse = dW_fine1 + dW_fine2);
@@ -517,14 +597,14 @@ k_paths_mixed(const MixedArgs a) {
           // exited keeps its exit state until the pair is pushed.
           const float ea0 = scf * za0, ea1 = scf * za1, eb0 = scf * zb0, eb1 = scf * zb1;
           if (f_alive) {
-            bool fx = advance(F, ea0, ea1, hf, thrf);
-            if (!fx) fx = advance(F, eb0, eb1, hf, thrf);
+            bool fx = advance(F, ea0, ea1, hf, thrf, x0e);
+            if (!fx) fx = advance(F, eb0, eb1, hf, thrf, x1e);
             f_alive = !fx;
           }
-          if (c_alive) c_alive = !advance(Cs, ea0 + eb0, ea1 + eb1, h, thrc);
+          if (c_alive) c_alive = !advance(Cs, ea0 + eb0, ea1 + eb1, h, thrc, x2e);
         } else {
-          bool fx = advance(F, scc * za0, scc * za1, h, thrc);
-          if (!fx) fx = advance(F, scc * zb0, scc * zb1, h, thrc);
+          bool fx = advance(F, scc * za0, scc * za1, h, thrc, x0e);
+          if (!fx) fx = advance(F, scc * zb0, scc * zb1, h, thrc, x1e);
           f_alive = !fx;
         }
       }
@@ -639,6 +719,7 @@ static cudaError_t launch_mixed_t(const MixedArgs& a, int kind, int grid, size_t
       PDDS_MIXED_CASE(3, 0)
       PDDS_MIXED_CASE(4, 0)
       PDDS_MIXED_CASE(5, 0)
+      PDDS_MIXED_CASE(6, 0)
       default: return cudaErrorInvalidValue;
     }
   }
@@ -662,6 +743,7 @@ static bool is_mixed_t(const void* f) {
   return f == (const void*)k_paths_mixed<0, RICH, 0> || f == (const void*)k_paths_mixed<1, RICH, 0> ||
          f == (const void*)k_paths_mixed<2, RICH, 0> || f == (const void*)k_paths_mixed<3, RICH, 0> ||
          f == (const void*)k_paths_mixed<4, RICH, 0> || f == (const void*)k_paths_mixed<5, RICH, 0> ||
+         f == (const void*)k_paths_mixed<6, RICH, 0> ||
          f == (const void*)k_paths_mixed<0, RICH, 1> || f == (const void*)k_paths_mixed<5, RICH, 1>;
 }
 
@@ -685,6 +767,7 @@ static int blocks_t(int kind, size_t smem) {
     PDDS_OCC(2)
     PDDS_OCC(4)
     PDDS_OCC(5)
+    PDDS_OCC(6)
     default:
     PDDS_OCC(3)
   }
