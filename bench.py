@@ -256,6 +256,37 @@ def plain_config1(local: int, reps: int = 3):
     return out
 
 
+def robin_reflected(local: int, reps: int = 3, npaths: int = 20_000, h: float = 5e-4):
+    """The Robin test problem (poisson_3.hpp) on [-1,1]^2, 8 x 8 subdomains,
+    21 knots per segment, Robin condition on the west side (paths reflect
+    there with Lepingle's step), MIXED with the Richardson pair, adaptive step
+    and summed weights; the same layout with Dirichlet data on every side for
+    the cost of the reflection.  Device time of the estimate, RMSE of the
+    solved interface against the analytic solution (all knots and the knots of
+    the subdomain column on the Robin side)."""
+    import pdds_gb300 as P
+    from pdds_gb300.config import fac_rule
+    pd = P.PDDSparseGM((-1.0, -1.0), (1.0, 1.0), 8, 21, fac_rule(2.0, 8, 21), device=local)
+    near = pd.x < -0.75 + 1e-9
+    opts = dict(adaptive_h=True, richardson=True, dup_sum=True)
+    out = {"knots": int(pd.K), "paths_per_knot": npaths, "h": h, "robin_side": "W"}
+    for name, side in (("robin_west", "W"), ("dirichlet", None)):
+        bvp = P.BVP.robin_poisson(side)
+        pd.estimate(bvp, 256, h, mode=P.MODE_MIXED, **opts)  # warm-up
+        ms, steps = [], 0
+        for r in range(reps):
+            est = pd.estimate(bvp, npaths, h, mode=P.MODE_MIXED, seed=1234, instance=r, **opts)
+            ms.append(est.info["ms_paths"])
+            steps = est.info["path_steps"]
+        u, si = pd.solve_interface()
+        err = u - bvp.u(pd.x, pd.y)
+        out[name] = {"ms_paths": float(np.median(ms)), "path_steps_per_s": steps / (1e-3 * float(np.median(ms))),
+                     "rmse_vs_analytic": float(np.sqrt(np.mean(err ** 2))),
+                     "rmse_robin_column": float(np.sqrt(np.mean(err[near] ** 2)))}
+    pd.close()
+    return out
+
+
 def varcoef_lut(local: int, reps: int = 2):
     """The variable-coefficient problem with coefficients served from 1024^2
     FP32 tables (bicubic), 8 x 8 subdomains, 31 knots per segment, 5e4 paths
@@ -377,6 +408,7 @@ def main():
     ap.add_argument("--no-semilinear", action="store_true")
     ap.add_argument("--no-lut", action="store_true")
     ap.add_argument("--no-config1", action="store_true")
+    ap.add_argument("--no-robin", action="store_true")
     args = ap.parse_args()
 
     from pdds_gb300.config import WORKLOADS, fac_rule
@@ -523,6 +555,8 @@ def main():
         extra["config1_plain"] = plain_config1(local)
     if not args.no_lut and rank == 0:
         extra["varcoef_lut"] = varcoef_lut(local)
+    if not args.no_robin and rank == 0:
+        extra["robin_reflected"] = robin_reflected(local)
     if not args.no_semilinear and rank == 0:
         extra["semilinear_newton"] = semilinear_newton(local)
 

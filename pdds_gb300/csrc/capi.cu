@@ -268,6 +268,42 @@ struct ItemList {
 pdds_status enqueue_mixed_paths(pdds_ctx* ctx, const pdds_estimate_desc* desc, const ProblemDev& P, int chunks,
                                 int ppc, int* launches, const ItemList* items = nullptr) {
   cudaStream_t s = ctx->stream;
+  if (!items && P.kind == PK_ROBIN && (int)P.p[0] != 0 && !ctx->is_batch) {
+    // Knots whose stencil has a reflecting side take several times the
+    // steps per path of the others (their paths leave only through the
+    // absorbing sides): they go first, in chunks of an eighth of the paths,
+    // so that no single long item sets the end of the launch.
+    const HostLayout& L = ctx->L;
+    const int rm = (int)P.p[0], N = desc->npaths;
+    const int small = std::max(256, ppc / 8);
+    std::vector<int> ik, ip0, ip1, other;
+    for (int v : L.order) {
+      if (L.knot_boundary[v]) continue;
+      const StencilRec& st = L.stencils[L.knot_stencil[v]];
+      bool refl = false;
+      for (int d = 0; d < 4; d++) refl = refl || (st.glob[d] && (rm & (1 << d)));
+      if (!refl) {
+        other.push_back(v);
+        continue;
+      }
+      for (int p = 0; p < N; p += small) {
+        ik.push_back(v);
+        ip0.push_back(p);
+        ip1.push_back(std::min(N, p + small));
+      }
+    }
+    for (int v : other)
+      for (int p = 0; p < N; p += ppc) {
+        ik.push_back(v);
+        ip0.push_back(p);
+        ip1.push_back(std::min(N, p + ppc));
+      }
+    CK(ctx->item_knot.upload(ik, s));
+    CK(ctx->item_p0.upload(ip0, s));
+    CK(ctx->item_p1.upload(ip1, s));
+    const ItemList il{ctx->item_knot.p, ctx->item_p0.p, ctx->item_p1.p, (int)ik.size(), nullptr};
+    return enqueue_mixed_paths(ctx, desc, P, 1, ppc, launches, &il);
+  }
   const int N = desc->npaths;
   const int n_items = items ? items->n : ctx->n_mc * chunks;
   const long long max_steps = desc->max_steps > 0 ? desc->max_steps : 1000000LL;
