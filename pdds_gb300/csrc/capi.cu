@@ -39,6 +39,7 @@ pdds_status upload_layout(pdds_ctx* ctx) {
   ctx->edges_ready = false;
   ctx->has_solution = false;
   ctx->ugrid_m = 0;
+  ctx->lpt_ready = false;
   HostLayout& L = ctx->L;
   cudaStream_t s = ctx->stream;
   std::vector<double> st_rect;
@@ -325,7 +326,10 @@ pdds_status enqueue_mixed_paths(pdds_ctx* ctx, const pdds_estimate_desc* desc, c
   a.richardson = desc->richardson ? 1 : 0;
   a.h64 = desc->h;
   a.max_steps = max_steps;
-  a.mc_knots = ctx->mc_knots.p;
+  // work items of the default split are handed out heaviest knot first once
+  // an estimate on this layout has counted the steps per knot
+  const bool lpt = !items && !ctx->is_batch;
+  a.mc_knots = (lpt && ctx->lpt_ready) ? ctx->mc_lpt.p : ctx->mc_knots.p;
   a.item_counter = ctx->counter.p;
   a.G = ctx->G.p;
   a.GG = ctx->GG.p;
@@ -350,6 +354,12 @@ pdds_status enqueue_mixed_paths(pdds_ctx* ctx, const pdds_estimate_desc* desc, c
   if (n_items > 0) {
     CK(launch_paths_mixed(a, P.kind, grid, smem, s));
     ++*launches;
+    if (lpt) {
+      CK(ctx->mc_lpt.resize(std::max(ctx->n_mc, 1)));
+      CK(launch_lpt_order(ctx->mc_knots.p, ctx->n_mc, ctx->knot_steps.p, ctx->mc_lpt.p, s));
+      ++*launches;
+      ctx->lpt_ready = true;
+    }
   }
   return PDDS_OK;
 }
@@ -496,6 +506,7 @@ pdds_status pdds_destroy(pdds_ctx* ctx) {
     ctx->b_tend.release();
     ctx->knot_N.release();
     ctx->knot_steps.release();
+    ctx->mc_lpt.release();
     ctx->edge_knots.release();
     ctx->sub_u.release();
     ctx->sub_out.release();

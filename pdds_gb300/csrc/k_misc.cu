@@ -131,4 +131,39 @@ cudaError_t launch_finalize_n(const int* mc_knots, int n_mc, const int* knot_N, 
   return cudaGetLastError();
 }
 
+// Hand-out order of the MIXED work items, heaviest knots first: the knots
+// sorted by the path steps of the last estimate in decreasing groups of a
+// quarter octave (a counting sort in one CTA, key = 4 log2(steps) + the next
+// two bits; order inside a group is arbitrary).  Longest-first hand-out keeps
+// a long item from starting near the end of the launch.
+namespace {
+__device__ __forceinline__ int lpt_key(unsigned long long s) {
+  if (s < 4ull) return (int)s;
+  const int e = 63 - __clzll((long long)s);
+  return 4 * e + (int)((s >> (e - 2)) & 3ull);  // <= 255
+}
+__global__ void k_lpt_order(const int* mc, int n, const unsigned long long* steps, int* out) {
+  __shared__ int cnt[256], off[256];
+  for (int b = threadIdx.x; b < 256; b += blockDim.x) cnt[b] = 0;
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) atomicAdd(&cnt[255 - lpt_key(steps[mc[i]])], 1);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int acc = 0;
+    for (int b = 0; b < 256; b++) {
+      off[b] = acc;
+      acc += cnt[b];
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) out[atomicAdd(&off[255 - lpt_key(steps[mc[i]])], 1)] = mc[i];
+}
+}  // namespace
+
+cudaError_t launch_lpt_order(const int* mc, int n, const unsigned long long* steps, int* out, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_lpt_order<<<1, 1024, 0, s>>>(mc, n, steps, out);
+  return cudaGetLastError();
+}
+
 }  // namespace pdds

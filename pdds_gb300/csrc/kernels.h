@@ -105,6 +105,8 @@ struct ReplayArgs {
 };
 
 cudaError_t launch_paths_mixed(const MixedArgs& a, int kind, int grid, size_t smem, cudaStream_t s);
+// knots mc[n] reordered heaviest first by steps[knot] (quarter-octave groups)
+cudaError_t launch_lpt_order(const int* mc, int n, const unsigned long long* steps, int* out, cudaStream_t s);
 // Sets the Philox key schedule (rk) of `seed` and the instance word.
 void mixed_set_rng(MixedArgs& a, uint64_t seed, uint32_t instance);
 // True when `func` is one of the MIXED path kernels (a captured graph's
