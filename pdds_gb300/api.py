@@ -318,14 +318,23 @@ class PDDSparseGM:
             keep = np.ascontiguousarray(ipsi_override, np.float64)
             d.ipsi_override = _p(keep, C.c_double)
             d.ipsi_override_len = keep.size
-        val = np.zeros(max(self.nnz, 1))
+        # the read-back target is touched on the CPU first: a device-to-host
+        # copy into never-touched pages faults them in one by one from the
+        # copy (tens of ms for the 32 MB of G on the 12x12/43 layout), a CPU
+        # fill costs under a millisecond
+        read_var = want_var or mode == capi.MODE_REPLAY_FP64
+        val = np.empty(max(self.nnz, 1))
+        val.fill(0.0)
         var = np.zeros(max(self.nnz, 1))
+        if read_var:
+            var.fill(0.0)
         B = np.zeros(self.K)
         BB = np.zeros(self.K)
         info = capi.EstimateInfo()
         # G_var is only computed by the replay mode and by MIXED with want_var;
-        # otherwise var stays the zero array and nothing is read back into it
-        var_out = _p(var, C.c_double) if (want_var or mode == capi.MODE_REPLAY_FP64) else None
+        # otherwise var stays the (untouched) zero array and nothing is read
+        # back into it
+        var_out = _p(var, C.c_double) if read_var else None
         self._check(self._lib.pdds_estimate(self._ctx, C.byref(d), _p(val, C.c_double), var_out,
                                             _p(B, C.c_double), _p(BB, C.c_double), C.byref(info)))
         del keep

@@ -326,9 +326,36 @@ pdds_status enqueue_mixed_paths(pdds_ctx* ctx, const pdds_estimate_desc* desc, c
   a.richardson = desc->richardson ? 1 : 0;
   a.h64 = desc->h;
   a.max_steps = max_steps;
-  // work items of the default split are handed out heaviest knot first once
-  // an estimate on this layout has counted the steps per knot
+  // work items of the default split are handed out heaviest knot first: by
+  // the steps per knot that the last estimate on this layout counted, or
+  // before the first one by a geometric estimate of the steps per path
   const bool lpt = !items && !ctx->is_batch;
+  if (lpt && !ctx->lpt_ready && ctx->L.geom == 0) {
+    // E[steps] ~ tau / h_k: tau = tx ty / (tx + ty) combines the expected
+    // exit times a (w - a) / 2 across the stencil in x and in y, h_k is the
+    // knot's step (the adaptive one shrinks with the distance d to the
+    // nearest side).  It ranks the heavy knots (the cross knots of large
+    // stencils and knots close to a side) near the top.
+    const HostLayout& L = ctx->L;
+    std::vector<std::pair<double, int>> cost;
+    for (int v : L.order) {
+      if (L.knot_boundary[v]) continue;
+      const double* r = L.stencils[L.knot_stencil[v]].rect;
+      const double ax = L.kx[v] - r[0], bx = r[2] - L.kx[v], ay = L.ky[v] - r[1], by = r[3] - L.ky[v];
+      const double tx = 0.5 * std::max(ax * bx, 0.0), ty = 0.5 * std::max(ay * by, 0.0);
+      const double tau = tx + ty > 0.0 ? tx * ty / (tx + ty) : 0.0;
+      const double d = std::min(std::min(ax, bx), std::min(ay, by));
+      double hk = desc->h;
+      if (desc->adaptive_h && d > 1e-4) hk = std::min(hk, std::pow(d / (2.0 * 0.5826 * 1.4142135623730951), 2.0));
+      cost.push_back({-tau / hk, v});
+    }
+    std::stable_sort(cost.begin(), cost.end());
+    std::vector<int> ord;
+    ord.reserve(cost.size());
+    for (auto& c : cost) ord.push_back(c.second);
+    CK(ctx->mc_lpt.upload(ord, s));
+    ctx->lpt_ready = true;
+  }
   a.mc_knots = (lpt && ctx->lpt_ready) ? ctx->mc_lpt.p : ctx->mc_knots.p;
   a.item_counter = ctx->counter.p;
   a.G = ctx->G.p;
