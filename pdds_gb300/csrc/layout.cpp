@@ -17,6 +17,7 @@
 #include <cmath>
 #include <map>
 #include <tuple>
+#include <unordered_map>
 
 #include "pdds_internal.h"
 
@@ -198,13 +199,22 @@ std::string build_rect_layout(HostLayout& L, const double sw[2], const double ne
 
   const double gparams[4] = {sw[0], sw[1], ne[0], ne[1]};
   std::map<std::vector<int>, int> stencil_key;
-  std::map<std::pair<int, std::vector<int>>, int> side_key;
+  // side records by (kind, knot list): a hash map, the lists are long
+  struct SideKeyHash {
+    size_t operator()(const std::pair<int, std::vector<int>>& k) const {
+      uint64_t h = 1469598103934665603ull ^ (uint64_t)k.first;
+      for (int v : k.second) h = (h ^ (uint64_t)(uint32_t)v) * 1099511628211ull;
+      return (size_t)h;
+    }
+  };
+  std::unordered_map<std::pair<int, std::vector<int>>, int, SideKeyHash> side_key;
   L.knot_stencil.assign(L.K, -1);
   L.knot_boundary.assign(L.K, 0);
   std::vector<Lab> tmp;
   const double STEN_ELONG = 0.5;
   std::vector<int> lastq(L.K, -1);            // scratch: last insertion of a knot on a side
   std::vector<int64_t> last_writer(L.K, -1);  // scratch: last (side, knot) map entry of a knot
+  std::vector<int> col_pos(L.K, 0);           // scratch: position of a knot in the current G row
   for (int v = 0; v < L.K; v++) {
     const std::vector<int>& ki = knot_ifs[v];
     auto it = stencil_key.find(ki);
@@ -343,14 +353,14 @@ std::string build_rect_layout(HostLayout& L, const double sw[2], const double ne
     st.cols = cols;
     st.row_len = (int)cols.size();
     st.map_off = (int64_t)L.map_pos.size();
+    for (int p = 0; p < (int)cols.size(); p++) col_pos[cols[p]] = p;  // row position of each column
     for (int d = 0; d < 4; d++) {
       if (st.side[d] < 0) continue;
       const SideRec& sr = L.sides[st.side[d]];
       for (int q = 0; q < sr.n; q++) {
         const int v2 = L.side_knot[sr.knot_off + q];
-        const int p = (int)(std::lower_bound(cols.begin(), cols.end(), v2) - cols.begin());
         last_writer[v2] = (int64_t)L.map_pos.size();
-        L.map_pos.push_back(p);
+        L.map_pos.push_back(col_pos[v2]);
         L.map_owner.push_back(0);
       }
     }
