@@ -226,6 +226,30 @@ def semilinear_newton(local: int, iterations: int = 4, npaths: int = 20_000, h: 
     return out
 
 
+def linear_fixed_point(local: int, iterations: int = 6, npaths: int = 20_000, h: float = 5e-4, m: int = 32):
+    """The fixed-point loop of main_LinLoop.cpp (Solve_Iterative_numVR +
+    subdomain solves): Lap u + 20 u + F = 0 on [0,1]^2 split with the shift
+    22 and the time rescale 9 (sigma = sqrt(2/9) I, c = -2/9,
+    f = (F + 22 u_k)/9), u = sin(2 pi x + 1/2) cos(pi^2 (x + y)), 8 x 8
+    subdomains, 21 knots per segment, from u_0 = 0; wall time per step and the
+    RMSE against the analytic solution after each step."""
+    import pdds_gb300 as P
+    from pdds_gb300.config import fac_rule
+    pd = P.PDDSparseGM((0.0, 0.0), (1.0, 1.0), 8, 21, fac_rule(1.0, 8, 21), device=local)
+    pd.solve_linear_iteration(1, 256, h, m=m)  # warm-up (module load, allocations)
+    t0 = time.perf_counter()
+    its = pd.solve_linear_iteration(iterations, npaths, h, m=m, seed=7, adaptive_h=True, richardson=True,
+                                    dup_sum=True)
+    dt = time.perf_counter() - t0
+    out = {"knots": int(pd.K), "paths_per_knot": npaths, "h": h, "subdomain_grid": m, "steps": iterations,
+           "ms_per_step": 1000.0 * dt / iterations,
+           "rmse_knots": [round(it["rmse_knots"], 6) for it in its],
+           "rmse_grid": [round(it["rmse_grid"], 6) for it in its],
+           "path_steps_per_s": float(sum(it["estimate"].info["path_steps"] for it in its) / dt)}
+    pd.close()
+    return out
+
+
 def plain_config1(local: int, reps: int = 3):
     """The CPU-runnable configuration: Poisson on [-1,1]^2, 4 x 4 subdomains,
     11 knots per segment (237 knots), 1e4 paths per knot, h = 1e-3, the plain
@@ -406,6 +430,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-circle", action="store_true")
     ap.add_argument("--no-semilinear", action="store_true")
+    ap.add_argument("--no-linloop", action="store_true")
     ap.add_argument("--no-lut", action="store_true")
     ap.add_argument("--no-config1", action="store_true")
     ap.add_argument("--no-robin", action="store_true")
@@ -559,6 +584,8 @@ def main():
         extra["robin_reflected"] = robin_reflected(local)
     if not args.no_semilinear and rank == 0:
         extra["semilinear_newton"] = semilinear_newton(local)
+    if not args.no_linloop and rank == 0:
+        extra["linear_fixed_point"] = linear_fixed_point(local)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

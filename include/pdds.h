@@ -358,14 +358,32 @@ pdds_status pdds_subdomain_solve(pdds_ctx* ctx, int32_t m, const double* u, doub
  * context's problem.  u_k is the last pdds_subdomain_solve (from_solution = 1,
  * same m) or the constant u0 (the reference's first iteration: c = -3.63,
  * f = F + 2.662 at u0 = 1.1).  A Newton iteration is then pdds_estimate,
- * pdds_solve_interface and pdds_subdomain_solve (Solve_Subdomains_SemiLin). */
+ * pdds_solve_interface and pdds_subdomain_solve (Solve_Subdomains_SemiLin).
+ *
+ * equation = PDDS_OUTER_LINEAR_SHIFT gives instead one step of the
+ * reference's fixed-point loop for a linear problem (Solve_Iterative_numVR,
+ * PDDSparseGM.cpp:4081-4336, with BVPs/EDPs/Salou_Iterative.hpp, main_LinLoop.cpp):
+ * Lap u + c2 u + F = 0 on any rectangle of the layout, u = sin(2 pi x + 1/2)
+ * cos(pi^2 (x + y)), g = u, F = -Lap u - c2 u, split with the shift alpha
+ * and rescaled by k (c2 = 20, alpha = 22, k = 9 in the reference):
+ * sigma = sqrt(2/k) I, b = 0, c = (c2 - alpha)/k, f = (F + alpha u_k)/k and
+ * grad u_k for the control variate (EquationLI_sigma, EquationLI_c_LUT,
+ * EquationLI_f_LUT, EquationLI_grad_LUT).  The reference's first iteration
+ * (Solve with the analytic EquationLI_f) is u0 = 0.  The error's component on
+ * a Dirichlet eigenfunction of -Lap with eigenvalue lambda is multiplied by
+ * alpha / (lambda + alpha - c2) per step, so the loop converges only when the
+ * domain's lowest eigenvalue exceeds c2 (2 pi^2 / L^2 on a square of side L:
+ * L < 0.9935 for c2 = 20). */
+#define PDDS_OUTER_NEWTON_U3 0
+#define PDDS_OUTER_LINEAR_SHIFT 1
 typedef struct {
   int32_t m;              /* interior grid points per subdomain side (2..64)   */
   int32_t from_solution;  /* 1: around the last subdomain solve; 0: around u0 */
   int32_t use_cv;         /* control variate with grad u_k                     */
-  int32_t reserved;
+  int32_t equation;       /* PDDS_OUTER_NEWTON_U3 or PDDS_OUTER_LINEAR_SHIFT   */
   double u0;              /* constant first iterate                            */
-  double a;               /* u = a + sin(pi x) sin(pi y)                       */
+  double a;               /* NEWTON_U3: u = a + sin(pi x) sin(pi y)            */
+  double c2, alpha, k;    /* LINEAR_SHIFT: reaction, shift, time rescale (> 0) */
 } pdds_semilinear_desc;
 pdds_status pdds_semilinear_tables(pdds_ctx* ctx, const pdds_semilinear_desc* desc);
 

@@ -47,8 +47,13 @@ class CircleDesc(C.Structure):
 
 
 class SemilinearDesc(C.Structure):
-    _fields_ = [("m", C.c_int32), ("from_solution", C.c_int32), ("use_cv", C.c_int32), ("reserved", C.c_int32),
-                ("u0", C.c_double), ("a", C.c_double)]
+    _fields_ = [("m", C.c_int32), ("from_solution", C.c_int32), ("use_cv", C.c_int32), ("equation", C.c_int32),
+                ("u0", C.c_double), ("a", C.c_double), ("c2", C.c_double), ("alpha", C.c_double),
+                ("k", C.c_double)]
+
+
+OUTER_NEWTON_U3 = 0
+OUTER_LINEAR_SHIFT = 1
 
 
 class LayoutInfo(C.Structure):

@@ -123,6 +123,12 @@ class BVP:
                               np.tanh(np.sin(0.12 * x + 0.05 * y) + np.sin(0.05 * x - 0.12 * y)))
 
 
+def linear_iteration_u(x, y):
+    """Exact solution of the linear fixed-point loop's test problem
+    (Equation_u, BVPs/EDPs/Salou_Iterative.hpp)."""
+    return np.sin(2.0 * np.pi * x + 0.5) * np.cos(np.pi * np.pi * (x + y))
+
+
 def read_configuration(path: str) -> dict:
     """Key = value configuration file of the reference (ReadFromFile).
 
@@ -394,12 +400,47 @@ class PDDSparseGM:
         d.m = int(m)
         d.from_solution = int(bool(from_solution))
         d.use_cv = int(bool(use_cv))
+        d.equation = capi.OUTER_NEWTON_U3
         d.u0 = float(u0)
         d.a = float(a)
         self._check(self._lib.pdds_semilinear_tables(self._ctx, C.byref(d)))
         self._lut_owner = None
         return BVP(BVP.LUT, use_cv=use_cv, tables=None,
                    exact=lambda x, y: a + np.sin(np.pi * x) * np.sin(np.pi * y))
+
+    def linear_iteration_tables(self, m: int = 32, from_solution: bool = False, u0: float = 0.0,
+                                c2: float = 20.0, alpha: float = 22.0, k: float = 9.0, use_cv: bool = True) -> BVP:
+        """One step of the fixed-point loop for Lap u + c2 u + F = 0 with the
+        shift alpha and time rescale k (the reference's Solve_Iterative_numVR
+        with Salou_Iterative.hpp, u = sin(2 pi x + 1/2) cos(pi^2 (x + y))):
+        tables of sigma = sqrt(2/k) I, c = (c2 - alpha)/k, f = (F + alpha u_k)/k
+        and grad u_k built on the device around the last subdomain_solve(m)
+        (from_solution) or the constant u0 (0 is the reference's first
+        iteration).  Returns the table-served BVP."""
+        d = capi.SemilinearDesc()
+        d.m = int(m)
+        d.from_solution = int(bool(from_solution))
+        d.use_cv = int(bool(use_cv))
+        d.equation = capi.OUTER_LINEAR_SHIFT
+        d.u0 = float(u0)
+        d.c2 = float(c2)
+        d.alpha = float(alpha)
+        d.k = float(k)
+        self._check(self._lib.pdds_semilinear_tables(self._ctx, C.byref(d)))
+        self._lut_owner = None
+        return BVP(BVP.LUT, use_cv=use_cv, tables=None, exact=linear_iteration_u)
+
+    def solve_linear_iteration(self, iterations: int, npaths: int, h: float, m: int = 32, u0: float = 0.0,
+                               c2: float = 20.0, alpha: float = 22.0, k: float = 9.0, seed: int = 1234, **opts):
+        """The fixed-point outer loop of main_LinLoop.cpp: `iterations` steps,
+        each an estimate and interface solve of the problem with the source
+        built from the previous subdomain solution, then the subdomain solves
+        (Solve_Iterative_numVR + Solve_Subdomains_LinIt; the first step, around
+        u0, is the reference's Solve + Solve_Subdomains_LinIt_First).  Returns
+        a list of per-iteration dicts like solve_semilinear."""
+        return self._outer_loop(
+            iterations, npaths, h, m, seed, opts,
+            lambda it: self.linear_iteration_tables(m, from_solution=it > 0, u0=u0, c2=c2, alpha=alpha, k=k))
 
     def solve_semilinear(self, iterations: int, npaths: int, h: float, m: int = 32, u0: float = 1.1,
                          a: float = 1.1, seed: int = 1234, **opts):
@@ -409,9 +450,13 @@ class PDDSparseGM:
         (Solve_SemiLin_numVR + Solve_Subdomains_SemiLin, main_VR.cpp).  Returns
         a list of per-iteration dicts (interface solution u, subdomain grid
         (x, y, v), their RMSE against the exact solution)."""
+        return self._outer_loop(iterations, npaths, h, m, seed, opts,
+                                lambda it: self.semilinear_tables(m, from_solution=it > 0, u0=u0, a=a))
+
+    def _outer_loop(self, iterations, npaths, h, m, seed, opts, tables):
         out = []
         for k in range(iterations):
-            bvp = self.semilinear_tables(m, from_solution=k > 0, u0=u0, a=a)
+            bvp = tables(k)
             est = self.estimate(bvp, npaths, h, mode=capi.MODE_MIXED, seed=seed, instance=k, **opts)
             u, sinfo = self.solve_interface()
             x, y, v = self.subdomain_solve(m)

@@ -1110,9 +1110,16 @@ pdds_status pdds_semilinear_tables(pdds_ctx* ctx, const pdds_semilinear_desc* de
   if (!ctx->has_layout || ctx->L.geom != 0 || ctx->is_batch)
     return fail(ctx, PDDS_ERR_INVALID, "the semilinear step needs a rectangular layout");
   const HostLayout& L = ctx->L;
-  if (std::fabs(L.sw[0]) > 1e-12 || std::fabs(L.sw[1]) > 1e-12 || std::fabs(L.ne[0] - 1.0) > 1e-12 ||
-      std::fabs(L.ne[1] - 1.0) > 1e-12)
+  if (desc->equation != PDDS_OUTER_NEWTON_U3 && desc->equation != PDDS_OUTER_LINEAR_SHIFT)
+    return fail(ctx, PDDS_ERR_INVALID, "unknown outer-loop equation");
+  if (desc->equation == PDDS_OUTER_NEWTON_U3 &&
+      (std::fabs(L.sw[0]) > 1e-12 || std::fabs(L.sw[1]) > 1e-12 || std::fabs(L.ne[0] - 1.0) > 1e-12 ||
+       std::fabs(L.ne[1] - 1.0) > 1e-12))
     return fail(ctx, PDDS_ERR_INVALID, "the semilinear test equation lives on the unit square [0,1]^2");
+  if (desc->equation == PDDS_OUTER_LINEAR_SHIFT &&
+      !(desc->k > 0.0 && std::isfinite(desc->k) && std::isfinite(desc->c2) && std::isfinite(desc->alpha) &&
+        std::isfinite(desc->u0)))
+    return fail(ctx, PDDS_ERR_INVALID, "the linear iteration needs k > 0 and finite c2, alpha, u0");
   const int m = desc->m;
   if (m < 2 || m > 64) return fail(ctx, PDDS_ERR_INVALID, "2 <= m <= 64");
   if (desc->from_solution && ctx->ugrid_m != m)
@@ -1125,16 +1132,23 @@ pdds_status pdds_semilinear_tables(pdds_ctx* ctx, const pdds_semilinear_desc* de
   const size_t nn = (size_t)G * G;
   CK(ctx->lut_coef.resize(8 * nn));
   CK(ctx->lut_g.resize(nn));
-  const double hg = (L.ne[0] - L.sw[0]) / ns / (m + 1);
-  CK(launch_newton_tables(desc->from_solution ? ctx->ugrid.p : nullptr, G, L.sw[0], L.sw[1], hg, desc->u0, desc->a,
+  const double hx = (L.ne[0] - L.sw[0]) / ns / (m + 1), hy = (L.ne[1] - L.sw[1]) / ns / (m + 1);
+  OuterStep eq;
+  eq.equation = desc->equation == PDDS_OUTER_LINEAR_SHIFT ? OUTER_LINEAR_SHIFT : OUTER_NEWTON_U3;
+  eq.u0 = desc->u0;
+  eq.a = desc->a;
+  eq.c2 = desc->c2;
+  eq.alpha = desc->alpha;
+  eq.k = desc->k;
+  CK(launch_newton_tables(desc->from_solution ? ctx->ugrid.p : nullptr, G, L.sw[0], L.sw[1], hx, hy, eq,
                           ctx->lut_coef.p, ctx->lut_g.p, s));
   CK(cudaStreamSynchronize(s));
   ctx->lut_nx = G;
   ctx->lut_ny = G;
   ctx->lut_bounds[0] = L.sw[0];
   ctx->lut_bounds[1] = L.sw[1];
-  ctx->lut_bounds[2] = L.sw[0] + (G - 1) * hg;
-  ctx->lut_bounds[3] = L.sw[1] + (G - 1) * hg;
+  ctx->lut_bounds[2] = L.ne[0];
+  ctx->lut_bounds[3] = L.ne[1];
   pdds_problem_desc pd;
   std::memset(&pd, 0, sizeof(pd));
   pd.kind = PDDS_LUT;

@@ -304,42 +304,70 @@ __global__ void __launch_bounds__(SUB_THREADS) k_subdomain_lut(const DevLayout L
   if (grid) write_grid(grid, G, a, b, m, x, s_edge);
 }
 
-// Tables of the Newton linearisation of the semilinear equation
-// Lap u - u^3 + F = 0 (BVPs/EDPs/Semilinear_u3_VR.hpp: u = A + sin(pi x)
-// sin(pi y), F = 2 pi^2 sin(pi x) sin(pi y) + u^3) around the iterate u_k
-// (EquationSM_c_LUT, EquationSM_f_LUT, EquationSM_grad_LUT): sigma = sqrt2 I,
-// b = 0, c = -3 u_k^2, f = F + 2 u_k^3, grad u_k for the control variate, on
-// the G x G grid of spacing hg from (x0, y0).  u_k = the grid values, or the
-// constant u0 (grad 0) when grid is null; g table = A + sin(pi x) sin(pi y),
-// which is the Dirichlet data on the boundary of the unit square.
-__global__ void k_newton_tables(const double* grid, int G, double x0, double y0, double hg, double u0, double A,
-                                float4* coef, float* gtab) {
+// Tables of one step of an outer loop around the iterate u_k, on the G x G
+// grid of spacings (hx, hy) from (x0, y0); u_k = the grid values, or the
+// constant u0 (grad 0) when grid is null; grad u_k (second-order differences)
+// feeds the control variate.  Two equations:
+//
+// NEWTON_U3: the Newton linearisation of Lap u - u^3 + F = 0
+//   (BVPs/EDPs/Semilinear_u3_VR.hpp: u = A + sin(pi x) sin(pi y),
+//   F = 2 pi^2 sin(pi x) sin(pi y) + u^3; EquationSM_c_LUT, EquationSM_f_LUT,
+//   EquationSM_grad_LUT): sigma = sqrt2 I, b = 0, c = -3 u_k^2,
+//   f = F + 2 u_k^3; g table = A + sin(pi x) sin(pi y), the Dirichlet data on
+//   the boundary of the unit square.
+// LINEAR_SHIFT: the fixed-point splitting of Lap u + C2 u + F = 0 with the
+//   shift alpha and time rescale k (BVPs/EDPs/Salou_Iterative.hpp:
+//   u = sin(2 pi x + 1/2) cos(pi^2 (x + y)), F = -Lap u - C2 u;
+//   EquationLI_sigma, EquationLI_c_LUT, EquationLI_f_LUT):
+//   sigma = sqrt(2/k) I, b = 0, c = (C2 - alpha)/k, f = (F + alpha u_k)/k;
+//   g table = u.
+__global__ void k_newton_tables(const double* grid, int G, double x0, double y0, double hx, double hy,
+                                const OuterStep eq, float4* coef, float* gtab) {
   const int64_t N = (int64_t)G * G;
   for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < N; q += (int64_t)gridDim.x * blockDim.x) {
     const int I = (int)(q % G), J = (int)(q / G);
-    const double X = x0 + I * hg, Y = y0 + J * hg;
-    double uk = u0, gx = 0.0, gy = 0.0;
+    const double X = x0 + I * hx, Y = y0 + J * hy;
+    double uk = eq.u0, gx = 0.0, gy = 0.0;
     if (grid) {
       const double* row = grid + (size_t)J * G;
       uk = row[I];
-      const double i2h = 0.5 / hg;
-      if (I == 0) gx = (-3.0 * row[0] + 4.0 * row[1] - row[2]) * i2h;
-      else if (I == G - 1) gx = (3.0 * row[G - 1] - 4.0 * row[G - 2] + row[G - 3]) * i2h;
-      else gx = (row[I + 1] - row[I - 1]) * i2h;
+      const double i2hx = 0.5 / hx, i2hy = 0.5 / hy;
+      if (I == 0) gx = (-3.0 * row[0] + 4.0 * row[1] - row[2]) * i2hx;
+      else if (I == G - 1) gx = (3.0 * row[G - 1] - 4.0 * row[G - 2] + row[G - 3]) * i2hx;
+      else gx = (row[I + 1] - row[I - 1]) * i2hx;
       const double* col = grid + I;
-      if (J == 0) gy = (-3.0 * col[0] + 4.0 * col[G] - col[2 * (size_t)G]) * i2h;
+      if (J == 0) gy = (-3.0 * col[0] + 4.0 * col[G] - col[2 * (size_t)G]) * i2hy;
       else if (J == G - 1)
-        gy = (3.0 * col[(size_t)(G - 1) * G] - 4.0 * col[(size_t)(G - 2) * G] + col[(size_t)(G - 3) * G]) * i2h;
-      else gy = (col[(size_t)(J + 1) * G] - col[(size_t)(J - 1) * G]) * i2h;
+        gy = (3.0 * col[(size_t)(G - 1) * G] - 4.0 * col[(size_t)(G - 2) * G] + col[(size_t)(G - 3) * G]) * i2hy;
+      else gy = (col[(size_t)(J + 1) * G] - col[(size_t)(J - 1) * G]) * i2hy;
     }
-    double sx, cx, sy, cy;
-    sincospi(X, &sx, &cx);
-    sincospi(Y, &sy, &cy);
-    const double sp = sx * sy, ue = A + sp;
-    const double F = 2.0 * 9.869604401089358 * sp + ue * ue * ue;
-    coef[2 * q] = make_float4(1.41421356f, 1.41421356f, 0.f, 0.f);
-    coef[2 * q + 1] = make_float4((float)(-3.0 * uk * uk), (float)(F + 2.0 * uk * uk * uk), (float)gx, (float)gy);
-    gtab[q] = (float)ue;
+    constexpr double PI = 3.141592653589793, PI2 = 9.869604401089358;
+    if (eq.equation == OUTER_LINEAR_SHIFT) {
+      // u = S C with S = sin(2 pi x + 1/2), C = cos(pi^2 (x + y)):
+      // u_xx = -(4 pi^2 + pi^4) u - 4 pi^3 cos(2 pi x + 1/2) sin(pi^2 (x + y)),
+      // u_yy = -pi^4 u
+      double S, Sc, Cs, C;
+      sincos(2.0 * PI * X + 0.5, &S, &Sc);
+      sincos(PI2 * (X + Y), &Cs, &C);
+      const double ue = S * C;
+      const double lap = -(4.0 * PI2 + 2.0 * PI2 * PI2) * ue - 4.0 * PI2 * PI * Sc * Cs;
+      const double F = -lap - eq.c2 * ue;
+      const double ik = 1.0 / eq.k;
+      const float sg = (float)sqrt(2.0 * ik);
+      coef[2 * q] = make_float4(sg, sg, 0.f, 0.f);
+      coef[2 * q + 1] =
+          make_float4((float)((eq.c2 - eq.alpha) * ik), (float)((F + eq.alpha * uk) * ik), (float)gx, (float)gy);
+      gtab[q] = (float)ue;
+    } else {
+      double sx, cx, sy, cy;
+      sincospi(X, &sx, &cx);
+      sincospi(Y, &sy, &cy);
+      const double sp = sx * sy, ue = eq.a + sp;
+      const double F = 2.0 * PI2 * sp + ue * ue * ue;
+      coef[2 * q] = make_float4(1.41421356f, 1.41421356f, 0.f, 0.f);
+      coef[2 * q + 1] = make_float4((float)(-3.0 * uk * uk), (float)(F + 2.0 * uk * uk * uk), (float)gx, (float)gy);
+      gtab[q] = (float)ue;
+    }
   }
 }
 
@@ -379,11 +407,11 @@ cudaError_t launch_subdomain_lut(const DevLayout& L, const ProblemDev& P, int ns
   return cudaGetLastError();
 }
 
-cudaError_t launch_newton_tables(const double* grid, int G, double x0, double y0, double hg, double u0, double A,
-                                 float* coef, float* gtab, cudaStream_t s) {
+cudaError_t launch_newton_tables(const double* grid, int G, double x0, double y0, double hx, double hy,
+                                 const OuterStep& eq, float* coef, float* gtab, cudaStream_t s) {
   const int64_t N = (int64_t)G * G;
   const int blocks = (int)std::min<int64_t>((N + 255) / 256, 4096);
-  k_newton_tables<<<blocks, 256, 0, s>>>(grid, G, x0, y0, hg, u0, A, reinterpret_cast<float4*>(coef), gtab);
+  k_newton_tables<<<blocks, 256, 0, s>>>(grid, G, x0, y0, hx, hy, eq, reinterpret_cast<float4*>(coef), gtab);
   return cudaGetLastError();
 }
 

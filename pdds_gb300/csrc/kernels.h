@@ -142,9 +142,16 @@ cudaError_t launch_subdomain(const DevLayout& L, const ProblemDev& P, int nsub, 
 cudaError_t launch_subdomain_lut(const DevLayout& L, const ProblemDev& P, int nsub, int m, int n, const int* edge_knots,
                                  const double* u, double* out, double* work, double* grid, int max_iter, double tol,
                                  int* iters, unsigned* err, cudaStream_t s);
-// tables of the semilinear Newton step around the grid (or the constant u0)
-cudaError_t launch_newton_tables(const double* grid, int G, double x0, double y0, double hg, double u0, double A,
-                                 float* coef, float* gtab, cudaStream_t s);
+// tables of one outer-loop step around the grid (or the constant u0)
+enum { OUTER_NEWTON_U3 = 0, OUTER_LINEAR_SHIFT = 1 };
+struct OuterStep {
+  int equation;                  // OUTER_*
+  double u0;                     // constant iterate when there is no grid
+  double a;                      // NEWTON_U3: u = a + sin(pi x) sin(pi y)
+  double c2, alpha, k;           // LINEAR_SHIFT: Lap u + c2 u + F = 0, shift alpha, rescale k
+};
+cudaError_t launch_newton_tables(const double* grid, int G, double x0, double y0, double hx, double hy,
+                                 const OuterStep& eq, float* coef, float* gtab, cudaStream_t s);
 cudaError_t launch_finalize(const int* mc_knots, int n_mc, int N, const double* Bsum,
                             const double* BBsum, double* B, double* BB, const int64_t* row_ptr,
                             int64_t nnz, const double* G, double* GG_to_var, int want_var,

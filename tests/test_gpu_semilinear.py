@@ -8,7 +8,12 @@ reference's Solve_SemiLin_numVR + Solve_Subdomains_SemiLin, main_VR.cpp).
 * The Newton loop on Lap u - u^3 + F = 0 (u = 1.1 + sin(pi x) sin(pi y)):
   the first step around the constant 1.1 is far off, the following steps
   approach the analytic solution at the interface knots and on the subdomain
-  grids (check (c))."""
+  grids (check (c)).
+* The fixed-point loop of main_LinLoop.cpp (Solve_Iterative_numVR,
+  Salou_Iterative.hpp: Lap u + 20 u + F = 0 split with the shift 22, time
+  rescale 9): on [0, 0.5]^2 the error's lowest mode shrinks by
+  22 / (8 pi^2 + 2) = 0.27 per step, so the loop reaches the Monte Carlo floor
+  in a few steps."""
 import numpy as np
 import pytest
 
@@ -88,3 +93,22 @@ def test_semilinear_newton_loop_approaches_the_analytic_solution():
     assert knots[-1] < 0.2 * knots[0] and knots[2] < knots[0], knots
     for it in its:
         assert it["solve"]["rel_residual"] < 1e-10
+
+
+def test_linear_fixed_point_loop_contracts_to_the_analytic_solution():
+    sw, ne = (0.0, 0.0), (0.5, 0.5)
+    with P.PDDSparseGM(sw, ne, 4, 11, fac_rule(0.5, 4, 11)) as pd:
+        its = pd.solve_linear_iteration(4, 20000, 5e-4, m=24, seed=11, adaptive_h=True, richardson=True,
+                                        dup_sum=True)
+    knots = [it["rmse_knots"] for it in its]
+    grid = [it["rmse_grid"] for it in its]
+    print("linear loop rmse knots", knots, "grid", grid)
+    for it in its:
+        assert it["solve"]["rel_residual"] < 1e-10
+    # the first step (u_k = 0) misses the alpha u part of the source: the
+    # same loop on a 97^2 finite-difference grid without Monte Carlo error
+    # gives RMSE 4.5e-2, 5.4e-3, 9.1e-4, 2.8e-4 over the four steps
+    assert knots[0] > 2e-2, knots
+    # contraction down to the Monte Carlo floor (about 1e-3 here)
+    assert knots[1] < 0.25 * knots[0] and knots[2] < 0.7 * knots[1], knots
+    assert knots[-1] < 2.5e-3 and grid[-1] < 2.5e-3, (knots, grid)
