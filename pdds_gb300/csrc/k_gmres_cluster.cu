@@ -20,8 +20,10 @@
 // Per Arnoldi step: FP32 SpMV of the CTA's rows, one classical Gram-Schmidt
 // pass whose reduction also carries |w|^2 (the new norm follows from
 // |w - V h|^2 = |w|^2 - |h|^2), and the Givens update of the Hessenberg
-// column (FP64, replicated per CTA): two group barriers per step.  Lane
-// partial sums are FP32; warp, CTA and cluster sums are FP64.  The outer FP64
+// column (FP32, replicated per CTA): two group barriers per step.  Lane
+// partial sums are FP32; warp, CTA and cluster sums are two-float (hi + lo)
+// sums in FP32 instructions (FP64 issues far slower on this GPU and, in the
+// serial parts of a step, set its length).  The outer FP64
 // residual b - (I + G) x uses the FP64 G, so the refined solution reaches the
 // FP64 tolerance whatever the FP32 inner accuracy; the loss of orthogonality
 // of a single pass only costs inner accuracy, which the refinement absorbs
@@ -44,11 +46,42 @@ constexpr int CG_THREADS = 1024;
 constexpr int CG_WARPS = CG_THREADS / 32;
 constexpr int CG_MAXM = 40;
 constexpr int CG_MAXV = CG_MAXM + 1;
+constexpr int SPMV_U = 8;  // CSR entries per lane in flight in the FP32 product
 static_assert(CG_MAXM == GMRES_CLUSTER_MAX_M, "restart bound");
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Two-float sums.  FP64 instructions issue at a small fraction of the FP32
+// rate on this GPU (a warp-wide FP64 add holds its scheduler for tens of
+// cycles), so the per-step reductions carry each value as an unevaluated
+// sum hi + lo of two floats (Knuth's TwoSum, Dekker's product by FMA):
+// about 48 significant bits with FP32 instructions only.
+__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
+  const float s = a.x + b.x;
+  const float bb = s - a.x;
+  const float e = (a.x - (s - bb)) + (b.x - bb) + (a.y + b.y);
+  const float hi = s + e;
+  return make_float2(hi, e - (hi - s));
+}
+__device__ __forceinline__ float2 df_sq(float a) {  // a^2 exactly as hi + lo
+  const float p = a * a;
+  return make_float2(p, fmaf(a, a, -p));
+}
+__device__ __forceinline__ float2 df_from(double v) {
+  const float hi = (float)v;
+  return make_float2(hi, (float)(v - (double)hi));
+}
+__device__ __forceinline__ double df_val(float2 v) { return (double)v.x + (double)v.y; }
+__device__ __forceinline__ float2 warp_sum_df(float2 v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float2 w = make_float2(__shfl_xor_sync(0xffffffffu, v.x, o), __shfl_xor_sync(0xffffffffu, v.y, o));
+    v = df_add(v, w);
+  }
   return v;
 }
 
@@ -76,13 +109,13 @@ struct ClusterGroup {
   }
   // one warp per value, lanes over ranks, a fixed shuffle tree: the same
   // order in every CTA
-  __device__ bool reduce(double* slot, int nv, double* out, int) {
+  __device__ bool reduce(float2* slot, int nv, float2* out, int) {
     cl.sync();
     const unsigned lane = threadIdx.x & 31, n = cl.num_blocks();
     for (int i = threadIdx.x >> 5; i < nv; i += CG_WARPS) {
-      double s = 0.0;
-      for (unsigned rk = lane; rk < n; rk += 32) s += cl.map_shared_rank(slot, rk)[i];
-      s = warp_sum(s);
+      float2 s = make_float2(0.f, 0.f);
+      for (unsigned rk = lane; rk < n; rk += 32) s = df_add(s, cl.map_shared_rank(slot, rk)[i]);
+      s = warp_sum_df(s);
       if (lane == 0) out[i] = s;
     }
     __syncthreads();
@@ -92,9 +125,13 @@ struct ClusterGroup {
 
 constexpr unsigned GRID_SPIN_LIMIT = 1u << 24;  // ~1 s of polling
 
+// The barrier is one arrival counter that only grows (zeroed before the
+// launch): barrier b of the launch is complete when the counter reaches
+// (b + 1) * gridDim.x, so the last CTA to arrive releases the others with its
+// own arrival and nothing is reset.  The wait polls with acquire loads and
+// gives up after GRID_SPIN_LIMIT polls.
 struct GridGroup {
-  unsigned* count;  // arrivals at the current barrier (zeroed before the launch)
-  unsigned* gen;    // barrier generation
+  unsigned* count;  // arrivals since the launch
   unsigned* err;    // ERR_FLAG_TIMEOUT on a wait that ran out
   double* gpart;    // [2][gridDim.x][CG_MAXV + 2] published partials
   __device__ unsigned rank() const { return blockIdx.x; }
@@ -104,24 +141,20 @@ struct GridGroup {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
-      volatile unsigned* vg = gen;
-      const unsigned g = *vg;
-      __threadfence();
+      __threadfence();  // the CTA's writes (ordered before this by the barrier) before the arrival
+      const unsigned arrived = atomicAdd(count, 1u);
+      const unsigned target = (arrived / gridDim.x + 1u) * gridDim.x;
       int ok = 1;
-      if (atomicAdd(count, 1u) == gridDim.x - 1) {
-        atomicExch(count, 0u);
-        __threadfence();
-        atomicAdd(gen, 1u);
-      } else {
-        unsigned spins = 0;
-        while (*vg == g) {
-          if (++spins > GRID_SPIN_LIMIT) {
-            atomicOr(err, ERR_FLAG_TIMEOUT);
-            ok = 0;
-            break;
-          }
-          __nanosleep(32);
+      unsigned spins = 0, cur;
+      for (;;) {
+        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(count) : "memory");
+        if ((int)(cur - target) >= 0) break;
+        if (++spins > GRID_SPIN_LIMIT) {
+          atomicOr(err, ERR_FLAG_TIMEOUT);
+          ok = 0;
+          break;
         }
+        if (spins > 64) __nanosleep(16);
       }
       __threadfence();
       s_ok = ok;
@@ -129,16 +162,27 @@ struct GridGroup {
     __syncthreads();
     return s_ok != 0;
   }
-  __device__ bool reduce(double* slot, int nv, double* out, int parity) {
-    double* mine = gpart + ((size_t)parity * gridDim.x + blockIdx.x) * (CG_MAXV + 2);
+  // partials of all CTAs, 8 loads in flight per lane
+  __device__ bool reduce(float2* slot, int nv, float2* out, int parity) {
+    float2* part = reinterpret_cast<float2*>(gpart);
+    float2* mine = part + ((size_t)parity * gridDim.x + blockIdx.x) * (CG_MAXV + 2);
     for (int i = threadIdx.x; i < nv; i += CG_THREADS) mine[i] = slot[i];
     const bool ok = sync();
-    const unsigned lane = threadIdx.x & 31;
+    const unsigned lane = threadIdx.x & 31, n = gridDim.x;
+    const float2* base = part + (size_t)parity * n * (CG_MAXV + 2);
     for (int i = threadIdx.x >> 5; i < nv; i += CG_WARPS) {
-      double s = 0.0;
-      for (unsigned rk = lane; rk < gridDim.x; rk += 32)
-        s += __ldcg(gpart + ((size_t)parity * gridDim.x + rk) * (CG_MAXV + 2) + i);
-      s = warp_sum(s);
+      float2 s = make_float2(0.f, 0.f);
+      for (unsigned rk0 = lane; rk0 < n; rk0 += 32 * 8) {
+        float2 t[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+          const unsigned rk = rk0 + 32u * u;
+          t[u] = rk < n ? __ldcg(base + (size_t)rk * (CG_MAXV + 2) + i) : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < 8; u++) s = df_add(s, t[u]);
+      }
+      s = warp_sum_df(s);
       if (lane == 0) out[i] = s;
     }
     __syncthreads();
@@ -165,15 +209,16 @@ __device__ __forceinline__ void gmres_body(const ClusterGmresArgs& a, Group& grp
   const size_t wbytes = ((size_t)per * sizeof(float) + 15) & ~(size_t)15;
   float* s_vf = reinterpret_cast<float*>(s_dyn + wbytes);    // system vector, FP32
   double* s_vd = reinterpret_cast<double*>(s_dyn + wbytes);  // system iterate, FP64
-  __shared__ double s_slot[2][CG_MAXV + 2];
-  __shared__ double s_red[CG_MAXV + 2];
-  __shared__ double s_h[CG_MAXV];
-  __shared__ double s_H[CG_MAXV * CG_MAXM];  // column j at s_H[j * (m + 1)]
-  __shared__ double s_cs[CG_MAXM], s_sn[CG_MAXM], s_g[CG_MAXV], s_y[CG_MAXM];
-  __shared__ double s_bsum[CG_WARPS][2];
+  __shared__ float2 s_slot[2][CG_MAXV + 2];
+  __shared__ float2 s_red[CG_MAXV + 2];
+  __shared__ float s_H[CG_MAXV * CG_MAXM];  // column j at s_H[j * (m + 1)]
+  __shared__ float s_cs[CG_MAXM], s_sn[CG_MAXM], s_g[CG_MAXV], s_y[CG_MAXM];
+  __shared__ float2 s_bsum[CG_WARPS];
   __shared__ int s_flag[2];
-  __shared__ double s_hn;
+  __shared__ float s_hn, s_inv;
+  __shared__ double s_beta[2];
   int parity = 0;
+  static_assert(CG_WARPS == 32, "one warp sums the warps' partials");
 
   bool alive = true;  // false once a grid barrier timed out: the CTA winds down
   // group all-reduce of s_slot[parity][0 .. nv) into s_red
@@ -181,37 +226,32 @@ __device__ __forceinline__ void gmres_body(const ClusterGmresArgs& a, Group& grp
     alive = grp.reduce(&s_slot[parity][0], nv, s_red, parity) && alive;
     parity ^= 1;
   };
-  // CTA sum of up to two per-thread values into s_slot[parity][0..1]
-  auto block_sum2 = [&](double v0, double v1) {
-    v0 = warp_sum(v0);
-    v1 = warp_sum(v1);
-    if (lane == 0) { s_bsum[warp][0] = v0; s_bsum[warp][1] = v1; }
+  // CTA sum of one per-thread value into s_slot[parity][0]
+  auto block_sum = [&](float2 v) {
+    v = warp_sum_df(v);
+    if (lane == 0) s_bsum[warp] = v;
     __syncthreads();
-    if (tid == 0) {
-      double t0 = 0.0, t1 = 0.0;
-      for (int q = 0; q < CG_WARPS; q++) { t0 += s_bsum[q][0]; t1 += s_bsum[q][1]; }
-      s_slot[parity][0] = t0;
-      s_slot[parity][1] = t1;
+    if (warp == 0) {
+      const float2 t = warp_sum_df(s_bsum[lane]);
+      if (lane == 0) s_slot[parity][0] = t;
     }
     __syncthreads();
   };
   // dots of the own rows of w with V[0 .. nv): one warp per basis vector
   auto basis_dots = [&](int nv) {
     for (int i = warp; i < nv; i += CG_WARPS) {
-      const float* Vi = a.V + (int64_t)i * K;
+      const float* Vi = a.V + (int64_t)i * K + r0;
       float acc = 0.f;
-      for (int r = lane; r < nown; r += 32) acc = fmaf(__ldcg(Vi + r0 + r), s_w[r], acc);
-      const double t = warp_sum((double)acc);
+      for (int q = lane; q < nown; q += 32 * 4) {
+        float t[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) t[u] = q + 32 * u < nown ? __ldcg(Vi + q + 32 * u) : 0.f;
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+          if (q + 32 * u < nown) acc = fmaf(t[u], s_w[q + 32 * u], acc);
+      }
+      const float2 t = warp_sum_df(make_float2(acc, 0.f));
       if (lane == 0) s_slot[parity][i] = t;
-    }
-    __syncthreads();
-  };
-  // w -= sum_i h_i V_i over the own rows
-  auto subtract = [&](int nv, const double* h) {
-    for (int r = tid; r < nown; r += CG_THREADS) {
-      float acc = s_w[r];
-      for (int i = 0; i < nv; i++) acc = fmaf(-(float)h[i], __ldcg(a.V + (int64_t)i * K + r0 + r), acc);
-      s_w[r] = acc;
     }
     __syncthreads();
   };
@@ -224,28 +264,43 @@ __device__ __forceinline__ void gmres_body(const ClusterGmresArgs& a, Group& grp
       bb += v * v;
       a.x[r] = 0.0;
     }
-    block_sum2(bb, 0.0);
+    block_sum(df_from(bb));
     allreduce(1);
   }
-  const double bnorm2 = s_red[0];
+  const double bnorm2 = df_val(s_red[0]);
   int total = 0, ref = 0;
   double rr = bnorm2;
   if (bnorm2 > 0.0 && alive) {
     const double tol2 = a.tol * a.tol * bnorm2;
     for (ref = 0;; ref++) {
       // FP64 residual r = b - x - G x of the own rows (x complete after the barrier above / below)
-      for (int i = tid; i < nr; i += CG_THREADS) s_vd[i] = __ldcg(a.x + R0 + i);
+      for (int i0 = tid; i0 < nr; i0 += CG_THREADS * 4) {
+        double t[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) t[u] = i0 + CG_THREADS * u < nr ? __ldcg(a.x + R0 + i0 + CG_THREADS * u) : 0.0;
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+          if (i0 + CG_THREADS * u < nr) s_vd[i0 + CG_THREADS * u] = t[u];
+      }
       __syncthreads();
       double prr = 0.0;
       for (int r = r0 + warp; r < r1; r += CG_WARPS) {
         double acc0 = 0.0, acc1 = 0.0;
         const int64_t e1 = a.row_ptr[r + 1];
-        int64_t e = a.row_ptr[r] + lane;
-        for (; e + 32 < e1; e += 64) {
-          acc0 += a.val64[e] * s_vd[a.col[e] - R0];
-          acc1 += a.val64[e + 32] * s_vd[a.col[e + 32] - R0];
+        for (int64_t e = a.row_ptr[r] + lane; e < e1; e += 32 * 4) {
+          double v[4];
+          int c[4];
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            const bool in = e + 32 * u < e1;
+            v[u] = in ? __ldg(a.val64 + e + 32 * u) : 0.0;
+            c[u] = in ? __ldg(a.col + e + 32 * u) - R0 : 0;
+          }
+          acc0 += v[0] * s_vd[c[0]];
+          acc1 += v[1] * s_vd[c[1]];
+          acc0 += v[2] * s_vd[c[2]];
+          acc1 += v[3] * s_vd[c[3]];
         }
-        if (e < e1) acc0 += a.val64[e] * s_vd[a.col[e] - R0];
         const double acc = warp_sum(acc0 + acc1);
         if (lane == 0) {
           const double rv = a.b[r] - s_vd[r - R0] - acc;
@@ -253,113 +308,141 @@ __device__ __forceinline__ void gmres_body(const ClusterGmresArgs& a, Group& grp
           prr += rv * rv;
         }
       }
-      block_sum2(prr, 0.0);
+      block_sum(df_from(prr));
       allreduce(1);
-      rr = s_red[0];
+      rr = df_val(s_red[0]);
       if (!(rr > tol2) || ref >= a.max_refine || total >= a.max_iter || !alive) break;
       // v0 = r / |r|
-      const double beta = sqrt(rr);
-      for (int r = r0 + tid; r < r1; r += CG_THREADS) a.V[r] = (float)(a.r64[r] / beta);
       if (tid == 0) {
-        for (int i = 0; i <= m; i++) s_g[i] = 0.0;
-        s_g[0] = 1.0;
+        s_beta[0] = sqrt(rr);
+        s_beta[1] = 1.0 / s_beta[0];
+        for (int i = 0; i <= m; i++) s_g[i] = 0.f;
+        s_g[0] = 1.f;
       }
+      __syncthreads();
+      const double beta = s_beta[0], ibeta = s_beta[1];
+      for (int r = r0 + tid; r < r1; r += CG_THREADS) a.V[r] = (float)(a.r64[r] * ibeta);
       int jdim = 0;
       for (int j = 0; j < m; j++) {
         alive = grp.sync() && alive;  // V[j] complete in every CTA
         if (!alive) break;
         // w = (I + G32) V[j], own rows
         const float* vj = a.V + (int64_t)j * K + R0;
-        for (int i = tid; i < nr; i += CG_THREADS) s_vf[i] = __ldcg(vj + i);
+        for (int i0 = tid; i0 < nr; i0 += CG_THREADS * 8) {
+          float t[8];
+#pragma unroll
+          for (int u = 0; u < 8; u++) t[u] = i0 + CG_THREADS * u < nr ? __ldcg(vj + i0 + CG_THREADS * u) : 0.f;
+#pragma unroll
+          for (int u = 0; u < 8; u++)
+            if (i0 + CG_THREADS * u < nr) s_vf[i0 + CG_THREADS * u] = t[u];
+        }
         __syncthreads();
+        // one warp per row, SPMV_U entries per lane loaded before any is used
         for (int r = r0 + warp; r < r1; r += CG_WARPS) {
-          float acc0 = 0.f, acc1 = 0.f, acc2 = 0.f, acc3 = 0.f;
+          float acc0 = 0.f, acc1 = 0.f;
           const int64_t e1 = a.row_ptr[r + 1];
-          int64_t e = a.row_ptr[r] + lane;
-          for (; e + 96 < e1; e += 128) {
-            acc0 = fmaf(a.val32[e], s_vf[a.col[e] - R0], acc0);
-            acc1 = fmaf(a.val32[e + 32], s_vf[a.col[e + 32] - R0], acc1);
-            acc2 = fmaf(a.val32[e + 64], s_vf[a.col[e + 64] - R0], acc2);
-            acc3 = fmaf(a.val32[e + 96], s_vf[a.col[e + 96] - R0], acc3);
+          for (int64_t e = a.row_ptr[r] + lane; e < e1; e += 32 * SPMV_U) {
+            float v[SPMV_U];
+            int c[SPMV_U];
+#pragma unroll
+            for (int u = 0; u < SPMV_U; u++) {
+              const bool in = e + 32 * u < e1;
+              v[u] = in ? __ldg(a.val32 + e + 32 * u) : 0.f;
+              c[u] = in ? __ldg(a.col + e + 32 * u) - R0 : 0;
+            }
+#pragma unroll
+            for (int u = 0; u < SPMV_U; u += 2) {
+              acc0 = fmaf(v[u], s_vf[c[u]], acc0);
+              acc1 = fmaf(v[u + 1], s_vf[c[u + 1]], acc1);
+            }
           }
-          for (; e < e1; e += 32) acc0 = fmaf(a.val32[e], s_vf[a.col[e] - R0], acc0);
-          float acc = (acc0 + acc1) + (acc2 + acc3);
+          float acc = acc0 + acc1;
 #pragma unroll
           for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
           if (lane == 0) s_w[r - r0] = s_vf[r - R0] + acc;
         }
         __syncthreads();
         const int nv = j + 1;
-        for (int i = tid; i < nv; i += CG_THREADS) s_h[i] = 0.0;
-        __syncthreads();
         // h = V^T w and |w|^2 in one reduction; then w -= V h and
         // |w - V h|^2 = |w|^2 - |h|^2 (V orthonormal)
         {
-          double pn = 0.0;
-          for (int r = tid; r < nown; r += CG_THREADS) pn += (double)s_w[r] * (double)s_w[r];
-          pn = warp_sum(pn);
-          if (lane == 0) s_bsum[warp][0] = pn;
+          float2 pn = make_float2(0.f, 0.f);
+          for (int r = tid; r < nown; r += CG_THREADS) pn = df_add(pn, df_sq(s_w[r]));
+          pn = warp_sum_df(pn);
+          if (lane == 0) s_bsum[warp] = pn;
         }
         basis_dots(nv);  // ends with __syncthreads: s_bsum complete
-        if (tid == 0) {
-          double t0 = 0.0;
-          for (int q = 0; q < CG_WARPS; q++) t0 += s_bsum[q][0];
-          s_slot[parity][nv] = t0;
+        if (warp == 0) {
+          const float2 t = warp_sum_df(s_bsum[lane]);
+          if (lane == 0) s_slot[parity][nv] = t;
         }
         __syncthreads();
         allreduce(nv + 1);
-        subtract(nv, s_red);  // ends with __syncthreads
-        if (tid == 0) {  // one thread: FP64 throughput is scarce on this GPU
-          double h2sq = 0.0;
-          for (int i = 0; i < nv; i++) h2sq += s_red[i] * s_red[i];
-          s_hn = sqrt(fmax(s_red[nv] - h2sq, 0.0));
+        // w -= V h over the own rows; the last warp then forms h_{j+1,j}
+        // and, in one lane, the Givens update of the Hessenberg column (FP32)
+        for (int r = tid; r < nown; r += CG_THREADS) {
+          float acc = s_w[r];
+#pragma unroll 4
+          for (int i = 0; i < nv; i++) acc = fmaf(-s_red[i].x, __ldcg(a.V + (int64_t)i * K + r0 + r), acc);
+          s_w[r] = acc;
         }
-        for (int i = tid; i < nv; i += CG_THREADS) s_h[i] += s_red[i];
-        __syncthreads();
-        const double hn = s_hn;
-        if (tid == 0) {
-          double* col = s_H + j * (m + 1);
-          for (int i = 0; i <= j; i++) col[i] = s_h[i];
-          col[j + 1] = hn;
-          for (int i = 0; i < j; i++) {
-            const double p = col[i], q = col[i + 1];
-            col[i] = s_cs[i] * p + s_sn[i] * q;
-            col[i + 1] = -s_sn[i] * p + s_cs[i] * q;
+        if (warp == CG_WARPS - 1) {
+          float2 hh = make_float2(0.f, 0.f);
+          for (int i = lane; i < nv; i += 32) {
+            float2 t = df_sq(s_red[i].x);
+            t.y = fmaf(2.f * s_red[i].x, s_red[i].y, t.y);
+            hh = df_add(hh, t);
           }
-          const double p = col[j], q = col[j + 1];
-          const double rho = sqrt(p * p + q * q);
-          s_cs[j] = rho > 0.0 ? p / rho : 1.0;
-          s_sn[j] = rho > 0.0 ? q / rho : 0.0;
-          col[j] = rho;
-          col[j + 1] = 0.0;
-          s_g[j + 1] = -s_sn[j] * s_g[j];
-          s_g[j] = s_cs[j] * s_g[j];
-          s_flag[0] = (fabs(s_g[j + 1]) <= a.inner_tol || !(hn > 0.0)) ? 1 : 0;
+          hh = warp_sum_df(hh);
+          if (lane == 0) {
+            const float2 d = df_add(s_red[nv], make_float2(-hh.x, -hh.y));
+            const float hn = sqrtf(fmaxf(d.x + d.y, 0.f));
+            float* col = s_H + j * (m + 1);
+            for (int i = 0; i <= j; i++) col[i] = s_red[i].x;
+            col[j + 1] = hn;
+            for (int i = 0; i < j; i++) {
+              const float p = col[i], q = col[i + 1];
+              col[i] = s_cs[i] * p + s_sn[i] * q;
+              col[i + 1] = -s_sn[i] * p + s_cs[i] * q;
+            }
+            const float p = col[j], q = col[j + 1];
+            const float rho = sqrtf(p * p + q * q);
+            s_cs[j] = rho > 0.f ? p / rho : 1.f;
+            s_sn[j] = rho > 0.f ? q / rho : 0.f;
+            col[j] = rho;
+            col[j + 1] = 0.f;
+            s_g[j + 1] = -s_sn[j] * s_g[j];
+            s_g[j] = s_cs[j] * s_g[j];
+            s_flag[0] = (fabsf(s_g[j + 1]) <= (float)a.inner_tol || !(hn > 0.f)) ? 1 : 0;
+            s_hn = hn;
+            s_inv = hn > 0.f ? 1.f / hn : 0.f;
+          }
         }
         __syncthreads();
         ++total;
         jdim = j + 1;
-        if (hn > 0.0 && j + 1 < m) {
-          const float inv = (float)(1.0 / hn);
+        if (s_hn > 0.f && j + 1 < m) {
+          const float inv = s_inv;
           float* vn = a.V + (int64_t)(j + 1) * K;
           for (int r = tid; r < nown; r += CG_THREADS) vn[r0 + r] = s_w[r] * inv;
         }
         if (s_flag[0] || total >= a.max_iter || !alive) break;
       }
-      // y = H^-1 g (upper triangular), x += beta V y in FP64
+      // y = H^-1 g (upper triangular, FP32), x += beta V y (FP64 iterate)
       if (tid == 0) {
         for (int i = jdim - 1; i >= 0; i--) {
-          double sacc = s_g[i];
+          float sacc = s_g[i];
           for (int k = i + 1; k < jdim; k++) sacc -= s_H[k * (m + 1) + i] * s_y[k];
-          const double d = s_H[i * (m + 1) + i];
-          s_y[i] = d != 0.0 ? sacc / d : 0.0;
+          const float d = s_H[i * (m + 1) + i];
+          s_y[i] = d != 0.f ? sacc / d : 0.f;
         }
       }
       __syncthreads();
       for (int r = r0 + tid; r < r1; r += CG_THREADS) {
-        double acc = 0.0;
-        for (int i = 0; i < jdim; i++) acc += s_y[i] * (double)__ldcg(a.V + (int64_t)i * K + r);
-        a.x[r] += beta * acc;
+        float acc = 0.f;
+#pragma unroll 4
+        for (int i = 0; i < jdim; i++) acc = fmaf(s_y[i], __ldcg(a.V + (int64_t)i * K + r), acc);
+        a.x[r] += beta * (double)acc;
       }
       alive = grp.sync() && alive;  // x complete before the next residual
     }
@@ -381,7 +464,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_gmres_cluster(const ClusterGm
 // One system over the whole grid (cooperative launch, one CTA per SM).
 __global__ void __launch_bounds__(CG_THREADS, 1) k_gmres_grid(const ClusterGmresArgs a, unsigned* bar,
                                                               unsigned* err, double* gpart) {
-  GridGroup grp{bar, bar + 1, err, gpart};
+  GridGroup grp{bar, err, gpart};
   gmres_body(a, grp);
 }
 
