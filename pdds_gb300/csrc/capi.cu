@@ -140,6 +140,9 @@ pdds_status upload_layout(pdds_ctx* ctx) {
   CK(ctx->mc_knots.upload(mc, s));
   CK(ctx->bnd_knots.upload(bnd, s));
   CK(ctx->ipsi.resize(std::max<int64_t>(ipsi_len, 1)));
+  CK(ctx->rbf_lu.resize(std::max<int64_t>(ipsi_len, 1)));
+  CK(ctx->rbf_uinv.resize(std::max<size_t>(sh_t.size(), 1)));
+  CK(ctx->rbf_piv.resize(std::max<size_t>(sh_t.size(), 1)));
   CK(ctx->tab.resize(std::max<int64_t>(tab_len, 1)));
   const int64_t nnz = L.row_ptr[L.K];
   CK(ctx->G.resize(std::max<int64_t>(nnz, 1)));
@@ -219,8 +222,9 @@ pdds_status enqueue_prefix(pdds_ctx* ctx, const pdds_estimate_desc* desc, const 
   if (need_ipsi && (!ctx->tables_ready || !desc->reuse_tables)) {
     int max_n = 0;
     for (auto& sh : L.shapes) max_n = std::max(max_n, sh.n);
-    CK(launch_rbf_setup(ctx->dl, max_n, ctx->max_nbins, ctx->ipsi.p, ctx->tab.p, ctx->errf.p, s));
-    *launches += 2;
+    CK(launch_rbf_setup(ctx->dl, max_n, ctx->max_nbins, ctx->ipsi.p, ctx->tab.p, ctx->rbf_lu.p, ctx->rbf_piv.p,
+                        ctx->rbf_uinv.p, ctx->errf.p, s));
+    *launches += 4;
     ctx->tables_ready = true;
   }
   if (events) CK(cudaEventRecord(ctx->ev1, s));
@@ -500,12 +504,13 @@ pdds_status pdds_destroy(pdds_ctx* ctx) {
                            &ctx->side_py, &ctx->sh_c, &ctx->sh_R, &ctx->sh_lo, &ctx->sh_delta, &ctx->sh_t, &ctx->ipsi,
                            &ctx->G, &ctx->GG, &ctx->B, &ctx->BB, &ctx->Bsum, &ctx->BBsum, &ctx->rx,
                            &ctx->ry, &ctx->rY, &ctx->rZ, &ctx->rxi, &ctx->Gside, &ctx->GGside,
-                           &ctx->ipsi_knot, &ctx->sv64, &ctx->sscal, &ctx->spart, &ctx->shess, &ctx->su};
+                           &ctx->ipsi_knot, &ctx->sv64, &ctx->sscal, &ctx->spart, &ctx->shess, &ctx->su,
+                           &ctx->rbf_lu, &ctx->rbf_uinv};
     for (auto* b : d64) b->release();
     DBuf<int>* di[] = {&ctx->knot_stencil, &ctx->st_side, &ctx->st_glob, &ctx->map_pos, &ctx->sd_n,
                        &ctx->sd_orient, &ctx->sd_shape, &ctx->side_knot, &ctx->sh_n, &ctx->sh_nbins,
                        &ctx->col, &ctx->mc_knots, &ctx->bnd_knots, &ctx->counter, &ctx->rside,
-                       &ctx->rsl, &ctx->rss, &ctx->task_m, &ctx->task_d, &ctx->task_i};
+                       &ctx->rsl, &ctx->rss, &ctx->task_m, &ctx->task_d, &ctx->task_i, &ctx->rbf_piv};
     for (auto* b : di) b->release();
     DBuf<int64_t>* dl[] = {&ctx->row_ptr, &ctx->st_map_off, &ctx->sd_knot_off, &ctx->sh_tab_off,
                            &ctx->sh_ipsi_off, &ctx->sh_t_off, &ctx->task_out, &ctx->knot_task_off,

@@ -121,7 +121,9 @@ cudaError_t launch_replay_reduce(const ReplayArgs& a, int kind, const int* task_
                                  const int64_t* knot_task_off, double* Gside, double* GGside,
                                  cudaStream_t s);
 // FP64 factorisation of every shape's Psi and the cardinal-function tables.
+// lu: scratch of the ipsi layout; piv, uinv: scratch of the sh_t layout
 cudaError_t launch_rbf_setup(const DevLayout& L, int max_n, int max_nbins, double* ipsi, float* tab,
+                             double* lu, int* piv, double* uinv,
                              unsigned* err_flags, cudaStream_t s);
 // B = g(x0) for boundary knots; finalisation of B, BB, G_var.
 cudaError_t launch_boundary_b(const DevLayout& L, const ProblemDev& P, int mode, const int* knots,
