@@ -123,6 +123,13 @@ class BVP:
                               np.tanh(np.sin(0.12 * x + 0.05 * y) + np.sin(0.05 * x - 0.12 * y)))
 
 
+def _touched(n: int):
+    """Uninitialised float64 array with every 4 KB page touched."""
+    a = np.empty(n)
+    a[::512] = 0.0
+    return a
+
+
 def linear_iteration_u(x, y):
     """Exact solution of the linear fixed-point loop's test problem
     (Equation_u, BVPs/EDPs/Salou_Iterative.hpp)."""
@@ -324,16 +331,13 @@ class PDDSparseGM:
             keep = np.ascontiguousarray(ipsi_override, np.float64)
             d.ipsi_override = _p(keep, C.c_double)
             d.ipsi_override_len = keep.size
-        # the read-back target is touched on the CPU first: a device-to-host
-        # copy into never-touched pages faults them in one by one from the
-        # copy (tens of ms for the 32 MB of G on the 12x12/43 layout), a CPU
-        # fill costs under a millisecond
+        # the read-back targets are touched on the CPU first, one element per
+        # 4 KB: a device-to-host copy into never-touched pages faults them in
+        # one by one from the copy (tens of ms for the 32 MB of G on the
+        # 12x12/43 layout); the copy then overwrites every element
         read_var = want_var or mode == capi.MODE_REPLAY_FP64
-        val = np.empty(max(self.nnz, 1))
-        val.fill(0.0)
-        var = np.zeros(max(self.nnz, 1))
-        if read_var:
-            var.fill(0.0)
+        val = _touched(max(self.nnz, 1))
+        var = _touched(max(self.nnz, 1)) if read_var else np.zeros(max(self.nnz, 1))
         B = np.zeros(self.K)
         BB = np.zeros(self.K)
         info = capi.EstimateInfo()

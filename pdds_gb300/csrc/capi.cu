@@ -111,7 +111,16 @@ pdds_status upload_layout(pdds_ctx* ctx) {
   CK(ctx->ky.upload(L.ky, s));
   CK(ctx->knot_stencil.upload(knot_stencil, s));
   CK(ctx->row_ptr.upload(L.row_ptr, s));
-  CK(ctx->col.upload(L.col, s));
+  {  // G's column indices, expanded on the device from the stencils' lists
+    std::vector<int64_t> st_col_off;
+    std::vector<int32_t> st_cols;
+    layout_stencil_cols(L, st_col_off, st_cols);
+    CK(ctx->st_col_off.upload(st_col_off, s));
+    CK(ctx->st_cols.upload(st_cols, s));
+    CK(ctx->col.resize(std::max<int64_t>(L.row_ptr[L.K], 1)));
+    CK(launch_expand_cols(L.K, ctx->row_ptr.p, ctx->knot_stencil.p, ctx->st_col_off.p, ctx->st_cols.p, ctx->col.p,
+                          s));
+  }
   CK(ctx->st_rect.upload(st_rect, s));
   CK(ctx->st_side.upload(st_side, s));
   CK(ctx->st_glob.upload(st_glob, s));
@@ -516,6 +525,8 @@ pdds_status pdds_destroy(pdds_ctx* ctx) {
                            &ctx->sh_ipsi_off, &ctx->sh_t_off, &ctx->task_out, &ctx->knot_task_off,
                            &ctx->knot_ipsi_off};
     for (auto* b : dl) b->release();
+    ctx->st_col_off.release();
+    ctx->st_cols.release();
     ctx->map_owner.release();
     ctx->tab.release();
     ctx->lut_coef.release();
@@ -680,7 +691,7 @@ pdds_status pdds_layout_knots(pdds_ctx* ctx, double* x, double* y, int32_t* orde
 pdds_status pdds_layout_csr(pdds_ctx* ctx, int64_t* row_ptr, int32_t* col) {
   if (!ctx || !ctx->has_layout) return fail(ctx, PDDS_ERR_INVALID, "no layout");
   if (row_ptr) std::copy(ctx->L.row_ptr.begin(), ctx->L.row_ptr.end(), row_ptr);
-  if (col) std::copy(ctx->L.col.begin(), ctx->L.col.end(), col);
+  if (col) layout_csr_cols(ctx->L, col);
   return PDDS_OK;
 }
 

@@ -63,6 +63,8 @@ struct pdds_ctx {
   DBuf<int> knot_stencil, st_side, st_glob, map_pos, sd_n, sd_orient, sd_shape, side_knot, sh_n,
       sh_nbins, col, mc_knots, bnd_knots;
   DBuf<double> rbf_lu, rbf_uinv;  // factorisation scratch (ipsi and sh_t layouts)
+  DBuf<int64_t> st_col_off;       // stencils' column lists, expanded into col on the device
+  DBuf<int> st_cols;
   DBuf<int> rbf_piv;
   DBuf<int64_t> row_ptr, st_map_off, sd_knot_off, sh_tab_off, sh_ipsi_off, sh_t_off;
   DBuf<unsigned char> map_owner;

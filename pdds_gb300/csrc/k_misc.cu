@@ -160,6 +160,27 @@ __global__ void k_lpt_order(const int* mc, int n, const unsigned long long* step
 }
 }  // namespace
 
+// CSR column indices of G: row k is its stencil's column list (one warp per knot).
+namespace {
+__global__ void k_expand_cols(int K, const int64_t* row_ptr, const int* knot_stencil, const int64_t* st_off,
+                              const int* st_cols, int* col) {
+  const int k = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+  if (k >= K) return;
+  const int64_t e0 = row_ptr[k], len = row_ptr[k + 1] - e0;
+  if (len == 0) return;
+  const int* src = st_cols + st_off[knot_stencil[k]];
+  for (int64_t q = lane; q < len; q += 32) col[e0 + q] = src[q];
+}
+}  // namespace
+
+cudaError_t launch_expand_cols(int K, const int64_t* row_ptr, const int* knot_stencil, const int64_t* st_off,
+                               const int* st_cols, int* col, cudaStream_t s) {
+  if (K <= 0) return cudaSuccess;
+  k_expand_cols<<<(unsigned)(((int64_t)K * 32 + 255) / 256), 256, 0, s>>>(K, row_ptr, knot_stencil, st_off, st_cols,
+                                                                          col);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_lpt_order(const int* mc, int n, const unsigned long long* steps, int* out, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   k_lpt_order<<<1, 1024, 0, s>>>(mc, n, steps, out);

@@ -125,6 +125,9 @@ cudaError_t launch_replay_reduce(const ReplayArgs& a, int kind, const int* task_
 cudaError_t launch_rbf_setup(const DevLayout& L, int max_n, int max_nbins, double* ipsi, float* tab,
                              double* lu, int* piv, double* uinv,
                              unsigned* err_flags, cudaStream_t s);
+// CSR column indices of G from the stencils' column lists
+cudaError_t launch_expand_cols(int K, const int64_t* row_ptr, const int* knot_stencil, const int64_t* st_off,
+                               const int* st_cols, int* col, cudaStream_t s);
 // B = g(x0) for boundary knots; finalisation of B, BB, G_var.
 cudaError_t launch_boundary_b(const DevLayout& L, const ProblemDev& P, int mode, const int* knots,
                               int n, double* B, double* BB, cudaStream_t s);

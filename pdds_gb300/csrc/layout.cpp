@@ -16,6 +16,8 @@
 #include <cstdint>
 #include <cmath>
 #include <map>
+#include <string>
+#include <thread>
 #include <tuple>
 #include <unordered_map>
 
@@ -70,6 +72,22 @@ struct Iface {
   Lab label;
   std::vector<int> index;
   std::vector<double> px, py;
+};
+
+// One stencil side before side records are shared: its knot list (repeats
+// dropped) and each knot's last written position.
+struct SideWork {
+  bool present = false;
+  std::vector<int> idx;
+  std::vector<double> px, py;
+};
+
+struct StencilWork {
+  std::string err;
+  StencilRec st;
+  SideWork side[4];
+  std::vector<int32_t> map_pos;
+  std::vector<uint8_t> map_owner;
 };
 
 // Rectangle2D signed distance (BVPs/Domains/rectangle.hpp:7-229), distance only.
@@ -198,39 +216,40 @@ std::string build_rect_layout(HostLayout& L, const double sw[2], const double ne
       if (knot_ifs[v].empty() || knot_ifs[v].back() != id) knot_ifs[v].push_back(id);
 
   const double gparams[4] = {sw[0], sw[1], ne[0], ne[1]};
+  // 1. stencil ids in knot order: knots with the same interfaces share one
   std::map<std::vector<int>, int> stencil_key;
-  // side records by (kind, knot list): a hash map, the lists are long
-  struct SideKeyHash {
-    size_t operator()(const std::pair<int, std::vector<int>>& k) const {
-      uint64_t h = 1469598103934665603ull ^ (uint64_t)k.first;
-      for (int v : k.second) h = (h ^ (uint64_t)(uint32_t)v) * 1099511628211ull;
-      return (size_t)h;
-    }
-  };
-  std::unordered_map<std::pair<int, std::vector<int>>, int, SideKeyHash> side_key;
+  std::vector<int> rep;  // first knot of each stencil
   L.knot_stencil.assign(L.K, -1);
   L.knot_boundary.assign(L.K, 0);
-  std::vector<Lab> tmp;
-  const double STEN_ELONG = 0.5;
-  std::vector<int> lastq(L.K, -1);            // scratch: last insertion of a knot on a side
-  std::vector<int64_t> last_writer(L.K, -1);  // scratch: last (side, knot) map entry of a knot
-  std::vector<int> col_pos(L.K, 0);           // scratch: position of a knot in the current G row
   for (int v = 0; v < L.K; v++) {
-    const std::vector<int>& ki = knot_ifs[v];
-    auto it = stencil_key.find(ki);
+    auto it = stencil_key.find(knot_ifs[v]);
     if (it != stencil_key.end()) {
       L.knot_stencil[v] = it->second;
       continue;
     }
+    const int sid = (int)rep.size();
+    stencil_key.emplace(knot_ifs[v], sid);
+    rep.push_back(v);
+    L.knot_stencil[v] = sid;
+  }
+  // 2. every stencil on its own (host threads): rect, sides' knot lists with
+  //    their last written positions, G row, row positions and owner flags
+  const int nst = (int)rep.size();
+  const double STEN_ELONG = 0.5;
+  std::vector<StencilWork> work(nst);
+  auto build_one = [&](int sid, std::vector<Lab>& tmp, std::vector<int>& lastq, std::vector<int>& col_pos,
+                       std::vector<int64_t>& last_writer) {
+    StencilWork& W = work[sid];
+    const std::vector<int>& ki = knot_ifs[rep[sid]];
     // Labels_Stencil
     std::vector<Lab> lab[4];
     auto push_if = [&](int d, Lab l) { if (lab_id(iN, l) >= 0) lab[d].push_back(l); };
     if (ki.size() == 1) {
       const Lab l = ifs[ki[0]].label;
-      lab_N(l, tmp); for (auto& a : tmp) push_if(DIR_N, a);
-      lab_S(l, tmp); for (auto& a : tmp) push_if(DIR_S, a);
-      lab_E(l, tmp); for (auto& a : tmp) push_if(DIR_E, a);
-      lab_W(l, tmp); for (auto& a : tmp) push_if(DIR_W, a);
+      lab_N(l, tmp); for (auto& q : tmp) push_if(DIR_N, q);
+      lab_S(l, tmp); for (auto& q : tmp) push_if(DIR_S, q);
+      lab_E(l, tmp); for (auto& q : tmp) push_if(DIR_E, q);
+      lab_W(l, tmp); for (auto& q : tmp) push_if(DIR_W, q);
     } else if (ki.size() == 4) {
       int max_h = -1 << 30, max_v = -1 << 30;
       for (int q = 0; q < 4; q++) {
@@ -252,85 +271,75 @@ std::string build_rect_layout(HostLayout& L, const double sw[2], const double ne
       lab_W(is, tmp); push_if(DIR_W, tmp[0]);
       lab_W(in, tmp); push_if(DIR_W, tmp[0]);
     } else {
-      return "internal: knot on " + std::to_string(ki.size()) + " interfaces";
+      W.err = "internal: knot on " + std::to_string(ki.size()) + " interfaces";
+      return;
     }
     auto IF = [&](Lab l) -> const Iface& { return ifs[lab_id(iN, l)]; };
     // Compute_Stencil
-    StencilRec st;
+    StencilRec& st = W.st;
     for (int i = 0; i < 4; i++) st.rect[i] = gparams[i];
     if (!lab[DIR_S].empty()) st.rect[1] = IF(lab[DIR_S][0]).py[0];
     if (!lab[DIR_W].empty()) st.rect[0] = IF(lab[DIR_W][0]).px[0];
     if (!lab[DIR_N].empty()) st.rect[3] = IF(lab[DIR_N].back()).py.back();
     if (!lab[DIR_E].empty()) st.rect[2] = IF(lab[DIR_E].back()).px.back();
-    std::vector<int> sidx[4];
-    std::vector<double> spx[4], spy[4];
-    int kind[4] = {-3, -3, -3, -3};
+    std::vector<int> sidx;
+    std::vector<double> spx, spy;
     for (int d = 0; d < 4; d++) {
-      if (lab[d].empty()) continue;
+      int kind = -3;
+      st.side[d] = -1;
+      if (lab[d].empty()) {
+        st.kind[d] = kind;
+        continue;
+      }
+      sidx.clear();
+      spx.clear();
+      spy.clear();
       const bool horiz = (d == DIR_N || d == DIR_S);
       auto add = [&](const Iface& f, int from, int to) {
         for (int k = from; k < to; k++) {
-          sidx[d].push_back(f.index[k]);
-          spx[d].push_back(f.px[k]);
-          spy[d].push_back(f.py[k]);
+          sidx.push_back(f.index[k]);
+          spx.push_back(f.px[k]);
+          spy.push_back(f.py[k]);
         }
       };
       Lab first = lab[d][0];
       Lab pre = horiz ? Lab{first.a - 1, first.b} : Lab{first.a, first.b - 2};
       if (lab_id(iN, pre) >= 0) {
-        kind[d]++;
-        const Iface& a = IF(pre);
-        add(a, (int)((1 - STEN_ELONG) * (a.index.size() - 1)), (int)a.index.size());
+        kind++;
+        const Iface& f = IF(pre);
+        add(f, (int)((1 - STEN_ELONG) * (f.index.size() - 1)), (int)f.index.size());
       }
       for (const Lab& l : lab[d]) {
         add(IF(l), 0, (int)IF(l).index.size());
-        kind[d] += 2;
+        kind += 2;
       }
       Lab last = lab[d].back();
       Lab post = horiz ? Lab{last.a + 1, last.b} : Lab{last.a, last.b + 2};
       if (lab_id(iN, post) >= 0) {
-        const Iface& a = IF(post);
-        kind[d]++;
-        add(a, 0, (int)(STEN_ELONG * (a.index.size())));
+        const Iface& f = IF(post);
+        kind++;
+        add(f, 0, (int)(STEN_ELONG * (f.index.size())));
       }
-    }
-    // Stencil::Init: keep the last written position of an index; drop
-    // consecutive repeats of an index
-    for (int d = 0; d < 4; d++) {
-      st.kind[d] = kind[d];
-      st.side[d] = -1;
-      if (sidx[d].empty()) continue;
-      std::vector<int> idx = sidx[d];
-      idx.erase(std::unique(idx.begin(), idx.end()), idx.end());
-      int kd = kind[d];
-      if (kd < 0 || kd > 3) return "internal: stencil side kind out of range";
-      auto key = std::make_pair(kd, idx);
-      auto sit = side_key.find(key);
-      if (sit == side_key.end()) {
-        SideRec sr;
-        sr.n = (int)idx.size();
-        sr.orient = (d == DIR_N || d == DIR_S) ? 0 : 1;
-        sr.kind = kd;
-        sr.c = fac[kd];
-        sr.shape = -1;
-        sr.knot_off = (int64_t)L.side_knot.size();
-        // the last written position of each index (scratch array over knots)
-        for (size_t q = 0; q < sidx[d].size(); q++) lastq[sidx[d][q]] = (int)q;
-        for (int v2 : idx) {
-          L.side_knot.push_back(v2);
-          L.side_px.push_back(spx[d][lastq[v2]]);
-          L.side_py.push_back(spy[d][lastq[v2]]);
-        }
-        for (int v2 : sidx[d]) lastq[v2] = -1;
-        sr.origin = (sr.orient == 0) ? L.side_px[sr.knot_off] : L.side_py[sr.knot_off];
-        sr.fixed = (sr.orient == 0) ? L.side_py[sr.knot_off] : L.side_px[sr.knot_off];
-        L.max_side = std::max(L.max_side, sr.n);
-        side_key[key] = (int)L.sides.size();
-        st.side[d] = (int)L.sides.size();
-        L.sides.push_back(sr);
-      } else {
-        st.side[d] = sit->second;
+      st.kind[d] = kind;
+      // Stencil::Init: keep the last written position of an index; drop
+      // consecutive repeats of an index
+      if (sidx.empty()) continue;
+      if (kind < 0 || kind > 3) {
+        W.err = "internal: stencil side kind out of range";
+        return;
       }
+      SideWork& S = W.side[d];
+      S.present = true;
+      S.idx = sidx;
+      S.idx.erase(std::unique(S.idx.begin(), S.idx.end()), S.idx.end());
+      for (size_t q = 0; q < sidx.size(); q++) lastq[sidx[q]] = (int)q;
+      S.px.reserve(S.idx.size());
+      S.py.reserve(S.idx.size());
+      for (int v2 : S.idx) {
+        S.px.push_back(spx[lastq[v2]]);
+        S.py.push_back(spy[lastq[v2]]);
+      }
+      for (int v2 : sidx) lastq[v2] = -1;
     }
     // global-boundary flags of the rect sides: midpoint within 1e-8 of the
     // domain boundary (Reduce_Analytic's test, EMFKACSolver.hpp:559)
@@ -342,36 +351,95 @@ std::string build_rect_layout(HostLayout& L, const double sw[2], const double ne
       st.glob[DIR_W] = rect_dist(gparams, st.rect[0], my) >= -1e-08;
     }
     // G row: sorted union of side indices
-    std::vector<int> cols;
+    std::vector<int>& cols = st.cols;
     for (int d = 0; d < 4; d++)
-      if (st.side[d] >= 0) {
-        const SideRec& sr = L.sides[st.side[d]];
-        for (int q = 0; q < sr.n; q++) cols.push_back(L.side_knot[sr.knot_off + q]);
-      }
+      if (W.side[d].present) cols.insert(cols.end(), W.side[d].idx.begin(), W.side[d].idx.end());
     std::sort(cols.begin(), cols.end());
     cols.erase(std::unique(cols.begin(), cols.end()), cols.end());
-    st.cols = cols;
     st.row_len = (int)cols.size();
-    st.map_off = (int64_t)L.map_pos.size();
-    for (int p = 0; p < (int)cols.size(); p++) col_pos[cols[p]] = p;  // row position of each column
+    // row position of every (side, knot) entry, sides in N, S, E, W order;
+    // the last side that wrote a knot owns its entry
+    for (int p = 0; p < (int)cols.size(); p++) col_pos[cols[p]] = p;
     for (int d = 0; d < 4; d++) {
-      if (st.side[d] < 0) continue;
-      const SideRec& sr = L.sides[st.side[d]];
-      for (int q = 0; q < sr.n; q++) {
-        const int v2 = L.side_knot[sr.knot_off + q];
-        last_writer[v2] = (int64_t)L.map_pos.size();
-        L.map_pos.push_back(col_pos[v2]);
-        L.map_owner.push_back(0);
+      if (!W.side[d].present) continue;
+      for (int v2 : W.side[d].idx) {
+        last_writer[v2] = (int64_t)W.map_pos.size();
+        W.map_pos.push_back(col_pos[v2]);
+        W.map_owner.push_back(0);
       }
     }
-    for (int v2 : cols) {  // the last side that wrote a knot owns its entry
-      L.map_owner[last_writer[v2]] = 1;
+    for (int v2 : cols) {
+      W.map_owner[last_writer[v2]] = 1;
       last_writer[v2] = -1;
     }
-    const int sid = (int)L.stencils.size();
-    stencil_key[ki] = sid;
-    L.knot_stencil[v] = sid;
-    L.stencils.push_back(st);
+  };
+  {
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const int nth = std::max(1, std::min({(int)hw, 16, nst / 8}));
+    std::vector<std::string> terr(nth);
+    auto worker = [&](int t) {
+      try {
+        std::vector<Lab> tmp;
+        std::vector<int> lastq(L.K, -1), col_pos(L.K, 0);
+        std::vector<int64_t> last_writer(L.K, -1);
+        for (int sid = t; sid < nst; sid += nth) build_one(sid, tmp, lastq, col_pos, last_writer);
+      } catch (const std::exception& e) {
+        terr[t] = std::string("layout worker: ") + e.what();
+      }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nth; t++) pool.emplace_back(worker, t);
+    worker(0);
+    for (auto& th : pool) th.join();
+    for (auto& e : terr)
+      if (!e.empty()) return e;
+  }
+  // 3. in stencil order: side records shared by equal (kind, knot list), the
+  //    first stencil that meets a side giving its knot positions
+  struct SideKeyHash {
+    size_t operator()(const std::pair<int, std::vector<int>>& k) const {
+      uint64_t h = 1469598103934665603ull ^ (uint64_t)k.first;
+      for (int v : k.second) h = (h ^ (uint64_t)(uint32_t)v) * 1099511628211ull;
+      return (size_t)h;
+    }
+  };
+  std::unordered_map<std::pair<int, std::vector<int>>, int, SideKeyHash> side_key;
+  L.stencils.reserve(nst);
+  for (int sid = 0; sid < nst; sid++) {
+    StencilWork& W = work[sid];
+    if (!W.err.empty()) return W.err;
+    StencilRec& st = W.st;
+    for (int d = 0; d < 4; d++) {
+      SideWork& S = W.side[d];
+      if (!S.present) continue;
+      const int kd = st.kind[d];
+      auto key = std::make_pair(kd, std::move(S.idx));
+      auto sit = side_key.find(key);
+      if (sit != side_key.end()) {
+        st.side[d] = sit->second;
+        continue;
+      }
+      SideRec sr;
+      sr.n = (int)key.second.size();
+      sr.orient = (d == DIR_N || d == DIR_S) ? 0 : 1;
+      sr.kind = kd;
+      sr.c = fac[kd];
+      sr.shape = -1;
+      sr.knot_off = (int64_t)L.side_knot.size();
+      L.side_knot.insert(L.side_knot.end(), key.second.begin(), key.second.end());
+      L.side_px.insert(L.side_px.end(), S.px.begin(), S.px.end());
+      L.side_py.insert(L.side_py.end(), S.py.begin(), S.py.end());
+      sr.origin = (sr.orient == 0) ? L.side_px[sr.knot_off] : L.side_py[sr.knot_off];
+      sr.fixed = (sr.orient == 0) ? L.side_py[sr.knot_off] : L.side_px[sr.knot_off];
+      L.max_side = std::max(L.max_side, sr.n);
+      st.side[d] = (int)L.sides.size();
+      side_key.emplace(std::move(key), (int)L.sides.size());
+      L.sides.push_back(sr);
+    }
+    st.map_off = (int64_t)L.map_pos.size();
+    L.map_pos.insert(L.map_pos.end(), W.map_pos.begin(), W.map_pos.end());
+    L.map_owner.insert(L.map_owner.end(), W.map_owner.begin(), W.map_owner.end());
+    L.stencils.push_back(std::move(st));
   }
   // boundary knots (Solve_OMP_Analytic: |dist| <= 1e-8 -> B = g, no row)
   L.row_ptr.assign(L.K + 1, 0);
@@ -380,12 +448,6 @@ std::string build_rect_layout(HostLayout& L, const double sw[2], const double ne
     L.nboundary += L.knot_boundary[v];
     const int len = L.knot_boundary[v] ? 0 : L.stencils[L.knot_stencil[v]].row_len;
     L.row_ptr[v + 1] = L.row_ptr[v] + len;
-  }
-  L.col.resize(L.row_ptr[L.K]);
-  for (int v = 0; v < L.K; v++) {
-    if (L.knot_boundary[v]) continue;
-    const auto& cols = L.stencils[L.knot_stencil[v]].cols;
-    std::copy(cols.begin(), cols.end(), L.col.begin() + L.row_ptr[v]);
   }
   // side shapes: translates with equal knot spacing, size, c and exit extent
   std::map<std::tuple<int, long long, long long, long long, long long>, int> shape_key;
@@ -441,6 +503,23 @@ std::string build_rect_layout(HostLayout& L, const double sw[2], const double ne
   return "";
 }
 
+void layout_csr_cols(const HostLayout& L, int32_t* out) {
+  for (int v = 0; v < L.K; v++) {
+    const int64_t len = L.row_ptr[v + 1] - L.row_ptr[v];
+    if (len == 0) continue;
+    const auto& cols = L.stencils[L.knot_stencil[v]].cols;
+    std::copy(cols.begin(), cols.begin() + len, out + L.row_ptr[v]);
+  }
+}
+
+void layout_stencil_cols(const HostLayout& L, std::vector<int64_t>& off, std::vector<int32_t>& cols) {
+  off.assign(L.stencils.size() + 1, 0);
+  for (size_t s = 0; s < L.stencils.size(); s++) off[s + 1] = off[s] + (int64_t)L.stencils[s].cols.size();
+  cols.clear();
+  cols.reserve(off.back());
+  for (const auto& st : L.stencils) cols.insert(cols.end(), st.cols.begin(), st.cols.end());
+}
+
 std::string merge_layouts(HostLayout& out, const std::vector<HostLayout>& parts, int bps) {
   out = HostLayout();
   if (parts.empty()) return "a batch needs at least one instance";
@@ -467,7 +546,6 @@ std::string merge_layouts(HostLayout& out, const std::vector<HostLayout>& parts,
     out.knot_boundary.insert(out.knot_boundary.end(), P.knot_boundary.begin(), P.knot_boundary.end());
     out.nboundary += P.nboundary;
     for (int v = 0; v < P.K; v++) out.row_ptr.push_back(e0 + P.row_ptr[v + 1]);
-    for (int c : P.col) out.col.push_back(c + k0);
     for (StencilRec st : P.stencils) {
       for (int d = 0; d < 4; d++)
         if (st.side[d] >= 0) st.side[d] += d0;

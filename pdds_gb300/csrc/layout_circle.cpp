@@ -221,12 +221,6 @@ std::string circle_stencils(HostLayout& L, double R, int NR, int NS, int n, cons
     const int len = L.knot_boundary[v] ? 0 : L.stencils[L.knot_stencil[v]].row_len;
     L.row_ptr[v + 1] = L.row_ptr[v] + len;
   }
-  L.col.resize(L.row_ptr[K]);
-  for (int v = 0; v < K; v++) {
-    if (L.knot_boundary[v]) continue;
-    const auto& cols = L.stencils[L.knot_stencil[v]].cols;
-    std::copy(cols.begin(), cols.end(), L.col.begin() + L.row_ptr[v]);
-  }
   // shapes: sides equal up to rotation (arcs) or translation (rays)
   std::map<std::tuple<int, int, long long, long long, long long, long long, long long>, int> shape_key;
   std::vector<std::vector<std::pair<int, int>>> uses(L.sides.size());

@@ -72,8 +72,7 @@ struct HostLayout {
   std::vector<int32_t> order;          // reference hand-out order
   std::vector<int32_t> knot_stencil;
   std::vector<uint8_t> knot_boundary;
-  std::vector<int64_t> row_ptr;        // K+1
-  std::vector<int32_t> col;            // nnz
+  std::vector<int64_t> row_ptr;        // K+1; the columns of row k are stencils[knot_stencil[k]].cols
   std::vector<StencilRec> stencils;
   std::vector<SideRec> sides;
   std::vector<int32_t> side_knot;
@@ -85,6 +84,12 @@ struct HostLayout {
   int32_t max_side = 0;
   int32_t nboundary = 0;
 };
+
+// CSR column indices of G (nnz = row_ptr[K] values) written into out: row k
+// is its stencil's sorted column list (empty for boundary knots).
+void layout_csr_cols(const HostLayout& L, int32_t* out);
+// Every stencil's column list, concatenated (off: stencils + 1 offsets).
+void layout_stencil_cols(const HostLayout& L, std::vector<int64_t>& off, std::vector<int32_t>& cols);
 
 // Builds the rectangular layout of PDDSparseGM (Fullfill_interfaces,
 // Labels_Stencil, Compute_Stencil, Stencil::Init) and the derived tables.
