@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/pdds.h"
@@ -65,12 +66,29 @@ extern "C" {
 pdds_status pdds_batch_build(pdds_ctx* ctx, const pdds_instance_desc* inst, int32_t n, pdds_batch_info* info) {
   if (!ctx || !inst || n < 1) return fail(ctx, PDDS_ERR_INVALID, "a batch needs n >= 1 instances");
   std::vector<HostLayout> parts(n);
-  for (int i = 0; i < n; i++) {
-    const pdds_layout_desc& ld = inst[i].layout;
+  for (int i = 0; i < n; i++)
     for (int q = 0; q < 4; q++)
-      if (!(ld.fac[q] > 0.0)) return fail(ctx, PDDS_ERR_INVALID, "instance " + std::to_string(i) + ": fac must be positive");
-    const std::string e = build_rect_layout(parts[i], ld.sw, ld.ne, ld.nsub, ld.nnode, ld.fac, ctx->bins);
-    if (!e.empty()) return fail(ctx, PDDS_ERR_INVALID, "instance " + std::to_string(i) + ": " + e);
+      if (!(inst[i].layout.fac[q] > 0.0))
+        return fail(ctx, PDDS_ERR_INVALID, "instance " + std::to_string(i) + ": fac must be positive");
+  {  // the instances' layouts are independent: host threads over instances
+    std::vector<std::string> errs(n);
+    const int nth = std::max(1, std::min<int>({(int)std::thread::hardware_concurrency(), 16, n}));
+    auto worker = [&](int t) {
+      for (int i = t; i < n; i += nth) {
+        const pdds_layout_desc& ld = inst[i].layout;
+        try {
+          errs[i] = build_rect_layout(parts[i], ld.sw, ld.ne, ld.nsub, ld.nnode, ld.fac, ctx->bins, 1);
+        } catch (const std::exception& ex) {
+          errs[i] = ex.what();
+        }
+      }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nth; t++) pool.emplace_back(worker, t);
+    worker(0);
+    for (auto& th : pool) th.join();
+    for (int i = 0; i < n; i++)
+      if (!errs[i].empty()) return fail(ctx, PDDS_ERR_INVALID, "instance " + std::to_string(i) + ": " + errs[i]);
   }
   if (ctx->device >= 0) {
     CK(cudaSetDevice(ctx->device));

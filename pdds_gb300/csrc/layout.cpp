@@ -119,7 +119,7 @@ void set_shape_bins(HostLayout& L, int bps) {
 }
 
 std::string build_rect_layout(HostLayout& L, const double sw[2], const double ne[2], int nsub,
-                              int nnode, const double fac[4], int bps) {
+                              int nnode, const double fac[4], int bps, int max_threads) {
   if (nsub < 2 || nnode < 3) return "layout needs nsub >= 2 and nnode >= 3";
   if (!(ne[0] > sw[0] && ne[1] > sw[1])) return "layout needs NE > SW";
   L = HostLayout();
@@ -375,7 +375,8 @@ std::string build_rect_layout(HostLayout& L, const double sw[2], const double ne
   };
   {
     const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-    const int nth = std::max(1, std::min({(int)hw, 16, nst / 8}));
+    const int cap = max_threads > 0 ? max_threads : 16;
+    const int nth = std::max(1, std::min({(int)hw, cap, nst / 8}));
     std::vector<std::string> terr(nth);
     auto worker = [&](int t) {
       try {

@@ -95,7 +95,7 @@ void layout_stencil_cols(const HostLayout& L, std::vector<int64_t>& off, std::ve
 // Labels_Stencil, Compute_Stencil, Stencil::Init) and the derived tables.
 // Returns an empty string on success, else the error text.
 std::string build_rect_layout(HostLayout& L, const double sw[2], const double ne[2], int nsub,
-                              int nnode, const double fac[4], int bins_per_gap);
+                              int nnode, const double fac[4], int bins_per_gap, int max_threads = 0);
 
 // Disk of radius R split into nrings x nsectors annular sectors (a
 // CircleMesh): knots on the arcs between rings and on the rays between
