@@ -414,6 +414,21 @@ def run_reference(args, workload, fac):
     print(json.dumps(line), flush=True)
 
 
+def aggregate_ranks(t_dev: float, units: float, dist, device: str):
+    """Whole-job figures over the replicas: the slowest rank's timed region
+    and the units (path steps) all ranks processed.  dist: torch.distributed
+    or None for one process; device: where the collective's tensors live
+    ("cuda" under NCCL, "cpu" under gloo)."""
+    if not dist:
+        return float(t_dev), float(units)
+    import torch
+    tt = torch.tensor([float(t_dev)], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    st = torch.tensor([float(units)], dtype=torch.float64, device=device)
+    dist.all_reduce(st)
+    return float(tt.item()), float(st.item())
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -503,16 +518,7 @@ def main():
     torch.cuda.synchronize()
     wall = time.perf_counter() - t_wall0
     clk = clocks.stop()
-    t_dev = sum(ms_dev) / 1000.0
-    if dist:
-        tt = torch.tensor([t_dev], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_dev = float(tt.item())
-        st = torch.tensor([float(steps_done)], device="cuda")
-        dist.all_reduce(st)
-        steps_all = float(st.item())
-    else:
-        steps_all = float(steps_done)
+    t_dev, steps_all = aggregate_ranks(sum(ms_dev) / 1000.0, steps_done, dist, "cuda")
     value = steps_all / t_dev
 
     extra = {}
