@@ -108,9 +108,11 @@ __device__ __forceinline__ u32x4 path_block_rk(const uint32_t (&rk)[20], uint32_
 }
 
 // Table-served coefficients (PK_LUT) need more live registers for the
-// bicubic accumulation: two CTAs per SM there, four otherwise.
+// bicubic accumulation: four CTAs per SM there, eight otherwise (128 threads
+// each: an item's tail, where finished warps wait at the CTA barrier for its
+// longest remaining path, is half as long relative to the item as with 256).
 template <int KIND, bool RICH, int GEOM>
-__global__ void __launch_bounds__(MIXED_THREADS, KIND == PK_LUT ? 2 : 4)
+__global__ void __launch_bounds__(MIXED_THREADS, KIND == PK_LUT ? 4 : 8)
 k_paths_mixed(const MixedArgs a) {
   extern __shared__ float hist[];  // [sum nbins] (and the Y^2 histogram after it)
   __shared__ ItemSide s_side[4];

@@ -7,7 +7,7 @@
 
 namespace pdds {
 
-constexpr int MIXED_THREADS = 256;
+constexpr int MIXED_THREADS = 128;
 constexpr int FP64_THREADS = 256;
 constexpr int FP64_QCAP = 96;  // exits queued per warp in the FP64 kernel
 constexpr unsigned ERR_FLAG_STEP_LIMIT = 1u;
