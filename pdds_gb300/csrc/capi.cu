@@ -261,8 +261,9 @@ void item_split(const pdds_ctx* ctx, int N, int* chunks_out, int* ppc_out, int t
     *ppc_out = ppc;
     return;
   }
+  // about four items per persistent CTA (1024 / threads CTAs per SM)
   const int n_mc = ctx->n_mc;
-  const int target = 4 * std::max(ctx->num_sms, 1) * 4;
+  const int target = 4 * std::max(ctx->num_sms, 1) * (1024 / mixed_threads(n_mc));
   int chunks = std::max(1, (target + std::max(n_mc, 1) - 1) / std::max(n_mc, 1));
   chunks = std::min(chunks, std::max(1, N / 256));
   const int ppc = (N + chunks - 1) / chunks;
@@ -382,9 +383,10 @@ pdds_status enqueue_mixed_paths(pdds_ctx* ctx, const pdds_estimate_desc* desc, c
   a.item_p1 = items ? items->p1 : nullptr;
   a.knot_invN = items ? items->knot_invN : nullptr;
   a.knot_steps = ctx->knot_steps.p;
-  const size_t smem = ctx->mixed_smem * (a.want_var ? 2 : 1);
+  const int threads = mixed_threads(ctx->n_mc);
+  const size_t smem = ctx->mixed_smem * (a.want_var ? 2 : 1) + mixed_queue_smem(threads, a.richardson);
   if (smem > 200 * 1024) return fail(ctx, PDDS_ERR_INVALID, "exit histograms exceed shared memory; lower bins_per_gap");
-  int bps = mixed_blocks_per_sm(P.kind, smem, a.richardson);
+  int bps = mixed_blocks_per_sm(P.kind, smem, a.richardson, threads);
   if (bps < 1) bps = 1;
   if (ctx->force_bps > 0) bps = std::min(bps, ctx->force_bps);
   else if (tuned_for(ctx, desc)) bps = std::min(bps, ctx->tune_bps);
@@ -392,7 +394,7 @@ pdds_status enqueue_mixed_paths(pdds_ctx* ctx, const pdds_estimate_desc* desc, c
   if (ctx->force_grid_frac > 0.0 && ctx->force_grid_frac < 1.0)
     grid = std::max(1, std::min(grid, (int)std::lround(ctx->force_grid_frac * bps * ctx->num_sms)));
   if (n_items > 0) {
-    CK(launch_paths_mixed(a, P.kind, grid, smem, s));
+    CK(launch_paths_mixed(a, P.kind, grid, threads, smem, s));
     ++*launches;
     if (lpt) {
       CK(ctx->mc_lpt.resize(std::max(ctx->n_mc, 1)));
@@ -971,8 +973,9 @@ pdds_status pdds_autotune(pdds_ctx* ctx, const pdds_estimate_desc* desc, int32_t
   int launches = 0;
   pdds_status st = enqueue_prefix(ctx, &d, P, false, &launches);
   if (st != PDDS_OK) return st;
-  const size_t smem = ctx->mixed_smem * (d.want_var ? 2 : 1);
-  const int occ = std::max(1, mixed_blocks_per_sm(P.kind, smem, d.richardson));
+  const int threads = mixed_threads(ctx->n_mc);
+  const size_t smem = ctx->mixed_smem * (d.want_var ? 2 : 1) + mixed_queue_smem(threads, d.richardson);
+  const int occ = std::max(1, mixed_blocks_per_sm(P.kind, smem, d.richardson, threads));
   std::vector<int> bps_c;
   for (int b = 1; b <= occ; b++) bps_c.push_back(b);
   std::vector<int> ppc_c;

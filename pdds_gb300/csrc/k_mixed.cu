@@ -108,24 +108,27 @@ __device__ __forceinline__ u32x4 path_block_rk(const uint32_t (&rk)[20], uint32_
 }
 
 // Table-served coefficients (PK_LUT) need more live registers for the
-// bicubic accumulation: four CTAs per SM there, eight otherwise (128 threads
-// each: an item's tail, where finished warps wait at the CTA barrier for its
-// longest remaining path, is half as long relative to the item as with 256).
+// bicubic accumulation: 128 registers there, 64 otherwise.  The block size
+// is chosen at launch (mixed_threads: 128 or 256 threads), with
+// 2048 / 4096 threads' worth of registers per SM either way.
 template <int KIND, bool RICH, int GEOM>
-__global__ void __launch_bounds__(MIXED_THREADS, KIND == PK_LUT ? 4 : 8)
+__global__ void __launch_bounds__(MIXED_MAX_THREADS, KIND == PK_LUT ? 2 : 4)
 k_paths_mixed(const MixedArgs a) {
-  extern __shared__ float hist[];  // [sum nbins] (and the Y^2 histogram after it)
+  // dynamic shared memory: the warps' exit queues, then the exit histograms
+  // [sum nbins] (and the Y^2 histogram after them)
+  extern __shared__ float dyn[];
   __shared__ ItemSide s_side[4];
   __shared__ float s_rect[4];
   __shared__ float s_dir[4];  // polar stencils: (cos, sin) of phi0 and phi1
   __shared__ int s_item, s_knot, s_p0, s_path_end, s_hist_len;
   __shared__ float s_h, s_sqrth;
   __shared__ unsigned s_next_path;
-  __shared__ double s_red[MIXED_THREADS / 32][4];
-  __shared__ unsigned long long s_redi[MIXED_THREADS / 32][3];
-  // exit queue of each warp: word w of slot i at s_q[warp][w][i]
+  __shared__ double s_red[MIXED_MAX_THREADS / 32][4];
+  __shared__ unsigned long long s_redi[MIXED_MAX_THREADS / 32][3];
+  // exit queue of each warp: word w of slot i at q[w][i]
   constexpr int QW = RICH ? 9 : 5;
-  __shared__ float s_q[MIXED_THREADS / 32][QW][XQCAP + 1];
+  const int nthr = blockDim.x, nwarps = nthr >> 5;
+  float* hist = dyn + nwarps * QW * (XQCAP + 1);
   const DevLayout& L = a.L;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
@@ -148,7 +151,7 @@ k_paths_mixed(const MixedArgs a) {
       s_knot = k;
       s_p0 = p0;
       s_path_end = p1;
-      s_next_path = (unsigned)(p0 + MIXED_THREADS);
+      s_next_path = (unsigned)(p0 + nthr);
       const int st = L.knot_stencil[k];
       for (int q = 0; q < 4; q++) s_rect[q] = (float)L.st_rect[4 * st + q];
       if (GEOM == 1) {
@@ -213,7 +216,7 @@ k_paths_mixed(const MixedArgs a) {
     instance_params(L, knot, P, rng_inst, rng_knot);
     const float h = s_h, sqrth = s_sqrth;
     const int nh = a.want_var ? 2 * hist_len : hist_len;
-    for (int i = tid; i < nh; i += MIXED_THREADS) hist[i] = 0.f;
+    for (int i = tid; i < nh; i += nthr) hist[i] = 0.f;
     float* hist2 = hist + hist_len;
     __syncthreads();
 
@@ -270,7 +273,7 @@ k_paths_mixed(const MixedArgs a) {
     unsigned nglob = 0, nsten = 0;  // exits of the lane in this item (<= 2 N)
     int qcount = 0;  // warp-uniform
     const unsigned lt = (1u << lane) - 1u;
-    float (*q)[XQCAP + 1] = s_q[warp];
+    float (*q)[XQCAP + 1] = reinterpret_cast<float (*)[XQCAP + 1]>(dyn + warp * QW * (XQCAP + 1));
     const bool use_cv = P.use_cv != 0;
     // increment scales (sqrt2 sqrt(h) for iso kinds, sqrt(h) otherwise) and
     // Gobet thresholds of the fine (h/2) and coarse (h) levels
@@ -653,7 +656,7 @@ k_paths_mixed(const MixedArgs a) {
     if (tid == 0) {
       double tb = 0.0, tbb = 0.0;
       unsigned long long ts = 0, tg = 0, tt = 0;
-      for (int w = 0; w < MIXED_THREADS / 32; w++) {
+      for (int w = 0; w < nwarps; w++) {
         tb += s_red[w][0]; tbb += s_red[w][1];
         ts += s_redi[w][0]; tg += s_redi[w][1]; tt += s_redi[w][2];
       }
@@ -668,7 +671,7 @@ k_paths_mixed(const MixedArgs a) {
     const int64_t row0 = L.row_ptr[knot];
     const double invN = a.knot_invN ? a.knot_invN[knot] : a.inv_N;
     const int n_all = s_side[0].n + s_side[1].n + s_side[2].n + s_side[3].n;
-    for (int pr = tid; pr < n_all; pr += MIXED_THREADS) {
+    for (int pr = tid; pr < n_all; pr += nthr) {
       int d = 0, i = pr;
       while (i >= s_side[d].n) { i -= s_side[d].n; ++d; }
       const ItemSide& is = s_side[d];
@@ -701,11 +704,11 @@ k_paths_mixed(const MixedArgs a) {
 
 // Polar stencils are instantiated for the isotropic problems only.
 template <bool RICH>
-static cudaError_t launch_mixed_t(const MixedArgs& a, int kind, int grid, size_t smem, cudaStream_t s) {
+static cudaError_t launch_mixed_t(const MixedArgs& a, int kind, int grid, int threads, size_t smem, cudaStream_t s) {
 #define PDDS_MIXED_CASE(KK, GG)                                                                           \
   case KK:                                                                                                \
     cudaFuncSetAttribute(k_paths_mixed<KK, RICH, GG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
-    k_paths_mixed<KK, RICH, GG><<<grid, MIXED_THREADS, smem, s>>>(a);                                     \
+    k_paths_mixed<KK, RICH, GG><<<grid, threads, smem, s>>>(a);                                           \
     break;
   if (a.L.geom == 1) {
     switch (kind) {
@@ -751,17 +754,23 @@ static bool is_mixed_t(const void* f) {
 
 bool is_mixed_path_kernel(const void* func) { return is_mixed_t<true>(func) || is_mixed_t<false>(func); }
 
-cudaError_t launch_paths_mixed(const MixedArgs& a, int kind, int grid, size_t smem, cudaStream_t s) {
-  return a.richardson ? launch_mixed_t<true>(a, kind, grid, smem, s) : launch_mixed_t<false>(a, kind, grid, smem, s);
+size_t mixed_queue_smem(int threads, int richardson) {
+  return (size_t)(threads / 32) * (richardson ? 9 : 5) * (XQCAP + 1) * sizeof(float);
+}
+
+cudaError_t launch_paths_mixed(const MixedArgs& a, int kind, int grid, int threads, size_t smem, cudaStream_t s) {
+  if (threads != 128 && threads != 256) return cudaErrorInvalidValue;
+  return a.richardson ? launch_mixed_t<true>(a, kind, grid, threads, smem, s)
+                      : launch_mixed_t<false>(a, kind, grid, threads, smem, s);
 }
 
 template <bool RICH>
-static int blocks_t(int kind, size_t smem) {
+static int blocks_t(int kind, size_t smem, int threads) {
   int nb = 0;
 #define PDDS_OCC(KK)                                                                                    \
   case KK:                                                                                              \
     cudaFuncSetAttribute(k_paths_mixed<KK, RICH, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_paths_mixed<KK, RICH, 0>, MIXED_THREADS, smem); \
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_paths_mixed<KK, RICH, 0>, threads, smem);       \
     break;
   switch (kind) {
     PDDS_OCC(0)
@@ -777,8 +786,8 @@ static int blocks_t(int kind, size_t smem) {
   return nb;
 }
 
-int mixed_blocks_per_sm(int kind, size_t smem, int richardson) {
-  return richardson ? blocks_t<true>(kind, smem) : blocks_t<false>(kind, smem);
+int mixed_blocks_per_sm(int kind, size_t smem, int richardson, int threads) {
+  return richardson ? blocks_t<true>(kind, smem, threads) : blocks_t<false>(kind, smem, threads);
 }
 
 }  // namespace pdds

@@ -7,7 +7,11 @@
 
 namespace pdds {
 
-constexpr int MIXED_THREADS = 128;
+constexpr int MIXED_MAX_THREADS = 256;
+// Block size of the MIXED path kernel: 128-thread CTAs (8 per SM) for large
+// layouts, where they were faster (12x12/n43: 27.7 against 28.2 ms), 256
+// (4 per SM) below 8192 Monte Carlo knots, where 128 measured 6-17 % slower.
+inline int mixed_threads(int n_mc) { return n_mc >= 8192 ? 128 : 256; }
 constexpr int FP64_THREADS = 256;
 constexpr int FP64_QCAP = 96;  // exits queued per warp in the FP64 kernel
 constexpr unsigned ERR_FLAG_STEP_LIMIT = 1u;
@@ -104,7 +108,9 @@ struct ReplayArgs {
   unsigned* err_flags;
 };
 
-cudaError_t launch_paths_mixed(const MixedArgs& a, int kind, int grid, size_t smem, cudaStream_t s);
+// smem: mixed_queue_smem(threads, richardson) + the exit histograms
+cudaError_t launch_paths_mixed(const MixedArgs& a, int kind, int grid, int threads, size_t smem, cudaStream_t s);
+size_t mixed_queue_smem(int threads, int richardson);
 // knots mc[n] reordered heaviest first by steps[knot] (quarter-octave groups)
 cudaError_t launch_lpt_order(const int* mc, int n, const unsigned long long* steps, int* out, cudaStream_t s);
 // Sets the Philox key schedule (rk) of `seed` and the instance word.
@@ -112,7 +118,7 @@ void mixed_set_rng(MixedArgs& a, uint64_t seed, uint32_t instance);
 // True when `func` is one of the MIXED path kernels (a captured graph's
 // nodes are re-keyed with a new seed through their parameters).
 bool is_mixed_path_kernel(const void* func);
-int mixed_blocks_per_sm(int kind, size_t smem, int richardson);
+int mixed_blocks_per_sm(int kind, size_t smem, int richardson, int threads);
 cudaError_t launch_paths_fp64(const Fp64Args& a, int kind, int grid, size_t smem, cudaStream_t s);
 int fp64_blocks_per_sm(int kind, size_t smem, int richardson);
 cudaError_t launch_replay_paths(const ReplayArgs& a, int kind, cudaStream_t s);
