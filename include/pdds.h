@@ -195,6 +195,10 @@ typedef struct {
   int32_t adaptive_n;
   int32_t npaths_max;
   double target_stderr;
+  /* MIXED only: threads per CTA of the path kernel, 128 or 256; 0 = by
+   * layout size (128 from 8192 Monte Carlo knots).  Results do not depend
+   * on it beyond FP32 summation order. */
+  int32_t cta_threads;
 } pdds_estimate_desc;
 
 typedef struct {

@@ -68,7 +68,8 @@ class EstimateDesc(C.Structure):
                 ("bins_per_gap", C.c_int32), ("max_steps", C.c_int64),
                 ("ipsi_override", C.POINTER(C.c_double)), ("ipsi_override_len", C.c_int64),
                 ("adaptive_h", C.c_int32), ("richardson", C.c_int32), ("reuse_tables", C.c_int32),
-                ("adaptive_n", C.c_int32), ("npaths_max", C.c_int32), ("target_stderr", C.c_double)]
+                ("adaptive_n", C.c_int32), ("npaths_max", C.c_int32), ("target_stderr", C.c_double),
+                ("cta_threads", C.c_int32)]
 
 
 class EstimateInfo(C.Structure):

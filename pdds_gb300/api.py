@@ -296,7 +296,8 @@ class PDDSparseGM:
                  instance: int = 0, dup_sum: bool = False, want_var: bool = False,
                  bins_per_gap: int = 0, max_steps: int = 0, ipsi_override=None,
                  adaptive_h: bool = False, richardson: bool = False, reuse_tables: bool = False,
-                 adaptive_n: bool = False, npaths_max: int = 0, target_stderr: float = 0.0) -> Estimate:
+                 adaptive_n: bool = False, npaths_max: int = 0, target_stderr: float = 0.0,
+                 cta_threads: int = 0) -> Estimate:
         """Runs the Feynman-Kac estimation of every knot's G row and B entry.
 
         adaptive_n: npaths is the pilot per knot; each knot then runs
@@ -326,6 +327,7 @@ class PDDSparseGM:
         d.adaptive_n = int(bool(adaptive_n))
         d.npaths_max = int(npaths_max)
         d.target_stderr = float(target_stderr)
+        d.cta_threads = int(cta_threads)
         keep = None
         if ipsi_override is not None:
             keep = np.ascontiguousarray(ipsi_override, np.float64)

@@ -254,7 +254,12 @@ bool tuned_for(const pdds_ctx* ctx, const pdds_estimate_desc* desc) {
   return ctx->tune_ppc > 0 && ctx->tune_kind == ctx->prob.kind && ctx->tune_rich == (desc->richardson ? 1 : 0);
 }
 
-void item_split(const pdds_ctx* ctx, int N, int* chunks_out, int* ppc_out, int tuned_ppc = 0) {
+// threads per CTA of the MIXED path kernel for this estimate
+int cta_threads_for(const pdds_ctx* ctx, const pdds_estimate_desc* d) {
+  return (d && d->cta_threads > 0) ? d->cta_threads : mixed_threads(ctx->n_mc);
+}
+
+void item_split(const pdds_ctx* ctx, int N, int* chunks_out, int* ppc_out, int tuned_ppc = 0, int threads = 0) {
   if (tuned_ppc > 0) {
     const int ppc = std::max(1, std::min(N, tuned_ppc));
     *chunks_out = (N + ppc - 1) / ppc;
@@ -263,7 +268,7 @@ void item_split(const pdds_ctx* ctx, int N, int* chunks_out, int* ppc_out, int t
   }
   // about four items per persistent CTA (1024 / threads CTAs per SM)
   const int n_mc = ctx->n_mc;
-  const int target = 4 * std::max(ctx->num_sms, 1) * (1024 / mixed_threads(n_mc));
+  const int target = 4 * std::max(ctx->num_sms, 1) * (1024 / (threads > 0 ? threads : mixed_threads(n_mc)));
   int chunks = std::max(1, (target + std::max(n_mc, 1) - 1) / std::max(n_mc, 1));
   chunks = std::min(chunks, std::max(1, N / 256));
   const int ppc = (N + chunks - 1) / chunks;
@@ -383,7 +388,7 @@ pdds_status enqueue_mixed_paths(pdds_ctx* ctx, const pdds_estimate_desc* desc, c
   a.item_p1 = items ? items->p1 : nullptr;
   a.knot_invN = items ? items->knot_invN : nullptr;
   a.knot_steps = ctx->knot_steps.p;
-  const int threads = mixed_threads(ctx->n_mc);
+  const int threads = cta_threads_for(ctx, desc);
   const size_t smem = ctx->mixed_smem * (a.want_var ? 2 : 1) + mixed_queue_smem(threads, a.richardson);
   if (smem > 200 * 1024) return fail(ctx, PDDS_ERR_INVALID, "exit histograms exceed shared memory; lower bins_per_gap");
   int bps = mixed_blocks_per_sm(P.kind, smem, a.richardson, threads);
@@ -465,7 +470,7 @@ pdds_status enqueue_mixed(pdds_ctx* ctx, const pdds_estimate_desc* desc, int* la
   pdds_status st = enqueue_prefix(ctx, desc, P, false, launches);
   if (st != PDDS_OK) return st;
   int chunks = 1, ppc = 1;
-  item_split(ctx, desc->npaths, &chunks, &ppc, tuned_for(ctx, desc) ? ctx->tune_ppc : 0);
+  item_split(ctx, desc->npaths, &chunks, &ppc, tuned_for(ctx, desc) ? ctx->tune_ppc : 0, cta_threads_for(ctx, desc));
   st = enqueue_mixed_paths(ctx, desc, P, chunks, ppc, launches);
   if (st != PDDS_OK) return st;
   const int64_t nnz = ctx->L.row_ptr[ctx->L.K];
@@ -740,6 +745,8 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
   if (desc->adaptive_n && mode != PDDS_MODE_MIXED)
     return fail(ctx, PDDS_ERR_INVALID, "variance-adaptive paths (adaptive_n) run in PDDS_MODE_MIXED");
   if (desc->adaptive_n && desc->target_stderr < 0.0) return fail(ctx, PDDS_ERR_INVALID, "target_stderr < 0");
+  if (desc->cta_threads != 0 && desc->cta_threads != 128 && desc->cta_threads != 256)
+    return fail(ctx, PDDS_ERR_INVALID, "cta_threads must be 0, 128 or 256");
   CK(cudaSetDevice(ctx->device));
   cudaStream_t s = ctx->stream;
   HostLayout& L = ctx->L;
@@ -851,7 +858,8 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
     }
   } else {
     int chunks = 1, ppc = 1;
-    item_split(ctx, N, &chunks, &ppc, (mode == PDDS_MODE_MIXED && tuned_for(ctx, desc)) ? ctx->tune_ppc : 0);
+    item_split(ctx, N, &chunks, &ppc, (mode == PDDS_MODE_MIXED && tuned_for(ctx, desc)) ? ctx->tune_ppc : 0,
+               cta_threads_for(ctx, desc));
     const int n_items = n_mc * chunks;
     CK(cudaMemsetAsync(ctx->counter.p, 0, sizeof(int), s));
     if (mode == PDDS_MODE_MIXED) {
@@ -973,7 +981,7 @@ pdds_status pdds_autotune(pdds_ctx* ctx, const pdds_estimate_desc* desc, int32_t
   int launches = 0;
   pdds_status st = enqueue_prefix(ctx, &d, P, false, &launches);
   if (st != PDDS_OK) return st;
-  const int threads = mixed_threads(ctx->n_mc);
+  const int threads = cta_threads_for(ctx, &d);
   const size_t smem = ctx->mixed_smem * (d.want_var ? 2 : 1) + mixed_queue_smem(threads, d.richardson);
   const int occ = std::max(1, mixed_blocks_per_sm(P.kind, smem, d.richardson, threads));
   std::vector<int> bps_c;

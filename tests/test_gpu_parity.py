@@ -225,3 +225,25 @@ def test_richardson_mixed_matches_fp64_and_beats_plain():
     rmse_r = np.sqrt(np.mean((u_r - ex) ** 2))
     rmse_p = np.sqrt(np.mean((u_p - ex) ** 2))
     assert rmse_r < 2e-3 and rmse_r < 0.6 * rmse_p, (rmse_r, rmse_p)
+
+
+def test_large_layout_block_sizes_agree():
+    """The 12x12 / 43-knot layout (10,945 Monte Carlo knots) runs the MIXED
+    kernel in 128-thread CTAs by default (the small layouts above use 256):
+    the same estimate with either block size, up to FP32 summation order
+    (exit deposits and lane sums are added in another order), with the
+    Richardson pair and the adaptive step of the benchmark."""
+    nsub, nnode, N, h = 12, 43, 512, 5e-4
+    fac = fac_rule(2.0, nsub, nnode)
+    bvp = P.BVP.poisson_sincos()
+    opts = dict(adaptive_h=True, richardson=True, dup_sum=True)
+    with P.PDDSparseGM(SW, NE, nsub, nnode, fac) as pd:
+        assert pd.K - pd.layout_info["nboundary"] >= 8192
+        m128 = pd.estimate(bvp, N, h, mode=P.MODE_MIXED, seed=21, **opts)
+        m256 = pd.estimate(bvp, N, h, mode=P.MODE_MIXED, seed=21, cta_threads=256, **opts)
+        with pytest.raises(P.PDDSError):
+            pd.estimate(bvp, N, h, mode=P.MODE_MIXED, cta_threads=192, **opts)
+    assert m128.info["path_steps"] == m256.info["path_steps"]
+    gmax = np.max(np.abs(m256.val))
+    np.testing.assert_allclose(m128.val, m256.val, rtol=1e-4, atol=1e-6 * gmax)
+    np.testing.assert_allclose(m128.B, m256.B, rtol=1e-5, atol=1e-7)
