@@ -240,6 +240,7 @@ typedef struct {
   int32_t sample_knots;      /* knots in the timing sample               */
   double best_ms;            /* sample time with the chosen shape        */
   double default_ms;         /* sample time with the default shape       */
+  int32_t cta_threads;       /* chosen threads per CTA (128 or 256)      */
 } pdds_tune_info;
 
 pdds_status pdds_autotune(pdds_ctx* ctx, const pdds_estimate_desc* desc, int32_t sample_knots,

@@ -254,9 +254,12 @@ bool tuned_for(const pdds_ctx* ctx, const pdds_estimate_desc* desc) {
   return ctx->tune_ppc > 0 && ctx->tune_kind == ctx->prob.kind && ctx->tune_rich == (desc->richardson ? 1 : 0);
 }
 
-// threads per CTA of the MIXED path kernel for this estimate
+// threads per CTA of the MIXED path kernel for this estimate: the caller's,
+// else the autotuned one for this problem kind, else by layout size
 int cta_threads_for(const pdds_ctx* ctx, const pdds_estimate_desc* d) {
-  return (d && d->cta_threads > 0) ? d->cta_threads : mixed_threads(ctx->n_mc);
+  if (d && d->cta_threads > 0) return d->cta_threads;
+  if (d && tuned_for(ctx, d) && ctx->tune_threads > 0) return ctx->tune_threads;
+  return mixed_threads(ctx->n_mc);
 }
 
 void item_split(const pdds_ctx* ctx, int N, int* chunks_out, int* ppc_out, int tuned_ppc = 0, int threads = 0) {
@@ -981,11 +984,12 @@ pdds_status pdds_autotune(pdds_ctx* ctx, const pdds_estimate_desc* desc, int32_t
   int launches = 0;
   pdds_status st = enqueue_prefix(ctx, &d, P, false, &launches);
   if (st != PDDS_OK) return st;
-  const int threads = cta_threads_for(ctx, &d);
-  const size_t smem = ctx->mixed_smem * (d.want_var ? 2 : 1) + mixed_queue_smem(threads, d.richardson);
-  const int occ = std::max(1, mixed_blocks_per_sm(P.kind, smem, d.richardson, threads));
-  std::vector<int> bps_c;
-  for (int b = 1; b <= occ; b++) bps_c.push_back(b);
+  d.cta_threads = mixed_threads(ctx->n_mc);  // the default shape first
+  auto occupancy = [&](int threads) {
+    const size_t smem = ctx->mixed_smem * (d.want_var ? 2 : 1) + mixed_queue_smem(threads, d.richardson);
+    return std::max(1, mixed_blocks_per_sm(P.kind, smem, d.richardson, threads));
+  };
+  const int occ = occupancy(d.cta_threads);
   std::vector<int> ppc_c;
   for (int p = 256; p < N; p *= 4) ppc_c.push_back(p);
   ppc_c.push_back(N);
@@ -1026,31 +1030,38 @@ pdds_status pdds_autotune(pdds_ctx* ctx, const pdds_estimate_desc* desc, int32_t
     return PDDS_OK;
   };
   float best_ms = 1e30f, def_ms = 0.f;
-  int best_bps = occ, best_ppc = def_ppc, ncand = 0;
+  int best_bps = occ, best_ppc = def_ppc, best_threads = d.cta_threads, ncand = 0;
   st = time_shape(occ, def_ppc, &def_ms);
   if (st != PDDS_OK) return st;
-  for (int b : bps_c)
-    for (int p : ppc_c) {
-      float ms = 0.f;
-      st = time_shape(b, p, &ms);
-      if (st != PDDS_OK) return st;
-      ++ncand;
-      if (ms < best_ms) {
-        best_ms = ms;
-        best_bps = b;
-        best_ppc = p;
+  for (int th : {128, 256}) {
+    d.cta_threads = th;
+    const int occ_t = occupancy(th);
+    for (int b = 1; b <= occ_t; b++)
+      for (int p : ppc_c) {
+        float ms = 0.f;
+        st = time_shape(b, p, &ms);
+        if (st != PDDS_OK) return st;
+        ++ncand;
+        if (ms < best_ms) {
+          best_ms = ms;
+          best_bps = b;
+          best_ppc = p;
+          best_threads = th;
+        }
       }
-    }
+  }
   st = check_err_flags(ctx);
   if (st != PDDS_OK) return st;
   ctx->tune_bps = best_bps;
   ctx->tune_ppc = best_ppc;
+  ctx->tune_threads = best_threads;
   ctx->tune_kind = ctx->prob.kind;
   ctx->tune_rich = d.richardson ? 1 : 0;
   ctx->has_estimate = false;
   if (info) {
     info->blocks_per_sm = best_bps;
     info->paths_per_item = best_ppc;
+    info->cta_threads = best_threads;
     info->candidates = ncand;
     info->sample_knots = ns;
     info->best_ms = best_ms;

@@ -118,7 +118,7 @@ struct pdds_ctx {
   bool edges_ready = false;
   bool has_solution = false;
   // autotuned launch shape of the MIXED path kernel (0 = defaults)
-  int tune_bps = 0, tune_ppc = 0, tune_kind = -1, tune_rich = -1;
+  int tune_bps = 0, tune_ppc = 0, tune_kind = -1, tune_rich = -1, tune_threads = 0;
   int force_bps = 0;             // CTAs per SM imposed while the autotuner times a shape
   double force_grid_frac = 0.0;  // grid scaled to a knot sample while it times
   // variance-adaptive paths (pdds_estimate with adaptive_n)
