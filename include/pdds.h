@@ -112,6 +112,7 @@ typedef struct {
   int32_t nshapes;       /* distinct side shapes (translates share one)    */
   int32_t max_side;      /* largest side                                   */
   int64_t nnz;           /* entries of G (rows of all knots)               */
+  int64_t h2d_bytes;     /* bytes this call copied from host to device      */
 } pdds_layout_info;
 
 pdds_status pdds_layout_build(pdds_ctx* ctx, const pdds_layout_desc* desc, pdds_layout_info* info);
@@ -209,6 +210,9 @@ typedef struct {
   double ms_setup;       /* factorisation and tables                     */
   double ms_paths;       /* path kernels and reduction                   */
   int32_t kernel_launches;
+  int32_t cta_threads;   /* MIXED: threads per CTA of the path kernel    */
+  int64_t h2d_bytes;     /* bytes this call copied host -> device        */
+  int64_t d2h_bytes;     /* bytes this call copied device -> host        */
 } pdds_estimate_info;
 
 /* Runs the estimation for all knots and keeps G and B on the device.  Any of
@@ -231,8 +235,10 @@ pdds_status pdds_estimate_knot_steps(pdds_ctx* ctx, int64_t* steps);
  * path exits (a refill threshold of one lane), so the refill needs no knob.
  * sample_knots <= 0 times the whole layout; a smaller sample runs on a grid
  * scaled by the sampled fraction of knots, so each CTA sees as many work
- * items as in the full run.  Overwrites the device results of the last
- * estimate. */
+ * items as in the full run.  desc->cta_threads = 128 or 256 keeps that
+ * block size and searches only the other shape parameters; 0 searches both
+ * block sizes.  The tuned shape is forgotten when a new layout or batch is
+ * built.  Overwrites the device results of the last estimate. */
 typedef struct {
   int32_t blocks_per_sm;     /* chosen persistent CTAs per SM            */
   int32_t paths_per_item;    /* chosen paths per work item (knot, chunk) */
@@ -266,6 +272,8 @@ typedef struct {
   double rel_residual;
   double ms;
   int32_t kernel_launches;
+  int64_t h2d_bytes;     /* bytes this call copied host -> device */
+  int64_t d2h_bytes;     /* bytes this call copied device -> host */
 } pdds_solve_info;
 
 /* Solves (I + G) u = B with the G and B of the last pdds_estimate. */
@@ -404,8 +412,10 @@ pdds_status pdds_semilinear_tables(pdds_ctx* ctx, const pdds_semilinear_desc* de
  * every GPU that loads the library until the process exits; all calls share
  * it, so calls that overlap on the GPU race.  The first call on a device
  * looks up the array's address; make it before any stream capture on that
- * device.  stream may be NULL (legacy default stream); err, if given,
- * receives a message of at most err_len bytes. */
+ * device.  The address is kept for the life of the process: after a
+ * cudaDeviceReset of a device, neither this entry point nor any other of the
+ * library may be used on it.  stream may be NULL (legacy default stream);
+ * err, if given, receives a message of at most err_len bytes. */
 #define PDDS_STATIC_SOLVE_MAX_K 131072
 pdds_status pdds_solve_bicgstab_static(int device, int32_t K, int64_t nnz, const int64_t* row_ptr,
                                        const int32_t* col, const double* val, const double* B,

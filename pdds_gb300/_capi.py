@@ -59,7 +59,7 @@ OUTER_LINEAR_SHIFT = 1
 class LayoutInfo(C.Structure):
     _fields_ = [("nknots", C.c_int32), ("nboundary", C.c_int32), ("nstencils", C.c_int32),
                 ("nsides", C.c_int32), ("nshapes", C.c_int32), ("max_side", C.c_int32),
-                ("nnz", C.c_int64)]
+                ("nnz", C.c_int64), ("h2d_bytes", C.c_int64)]
 
 
 class EstimateDesc(C.Structure):
@@ -75,7 +75,8 @@ class EstimateDesc(C.Structure):
 class EstimateInfo(C.Structure):
     _fields_ = [("path_steps", C.c_int64), ("paths", C.c_int64), ("exits_global", C.c_int64),
                 ("exits_stencil", C.c_int64), ("ms_setup", C.c_double), ("ms_paths", C.c_double),
-                ("kernel_launches", C.c_int32)]
+                ("kernel_launches", C.c_int32), ("cta_threads", C.c_int32), ("h2d_bytes", C.c_int64),
+                ("d2h_bytes", C.c_int64)]
 
 
 class TuneInfo(C.Structure):
@@ -91,7 +92,8 @@ class SolveDesc(C.Structure):
 
 class SolveInfo(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("refinements", C.c_int32), ("rel_residual", C.c_double),
-                ("ms", C.c_double), ("kernel_launches", C.c_int32)]
+                ("ms", C.c_double), ("kernel_launches", C.c_int32), ("h2d_bytes", C.c_int64),
+                ("d2h_bytes", C.c_int64)]
 
 
 class InstanceDesc(C.Structure):

@@ -356,9 +356,11 @@ class PDDSparseGM:
                         {f: getattr(info, f) for f, _ in capi.EstimateInfo._fields_}, kn)
 
     def autotune(self, bvp: BVP, npaths: int, h: float, sample_knots: int = 0, seed: int = 1234,
-                 adaptive_h: bool = False, richardson: bool = False, want_var: bool = False) -> dict:
+                 adaptive_h: bool = False, richardson: bool = False, want_var: bool = False,
+                 cta_threads: int = 0) -> dict:
         """Times the MIXED path kernel's launch shapes on a sample of knots and
-        keeps the fastest for later estimates of this problem kind."""
+        keeps the fastest for later estimates of this problem kind
+        (cta_threads 128 or 256 keeps that block size, 0 searches both)."""
         self._check(self._lib.pdds_problem_set(self._ctx, C.byref(bvp.desc())))
         d = capi.EstimateDesc()
         d.mode = capi.MODE_MIXED
@@ -368,6 +370,7 @@ class PDDSparseGM:
         d.adaptive_h = int(bool(adaptive_h))
         d.richardson = int(bool(richardson))
         d.want_var = int(bool(want_var))
+        d.cta_threads = int(cta_threads)
         info = capi.TuneInfo()
         self._check(self._lib.pdds_autotune(self._ctx, C.byref(d), int(sample_knots), C.byref(info)))
         return {f: getattr(info, f) for f, _ in capi.TuneInfo._fields_}

@@ -95,6 +95,7 @@ pdds_status pdds_batch_build(pdds_ctx* ctx, const pdds_instance_desc* inst, int3
     CK(cudaStreamSynchronize(ctx->stream));
   }
   drop_graph(ctx);
+  clear_tune(ctx);
   const std::string e = merge_layouts(ctx->L, parts, ctx->bins);
   if (!e.empty()) return fail(ctx, PDDS_ERR_INVALID, e);
   ctx->n_inst = n;
@@ -244,11 +245,11 @@ pdds_status pdds_batch_run(pdds_ctx* ctx, const pdds_batch_run_desc* desc, pdds_
     CK(cudaEventRecord(ctx->ev1, s));
   }
   unsigned long long stats[8] = {0};
-  CK(cudaMemcpyAsync(stats, ctx->stats.p, sizeof(stats), cudaMemcpyDeviceToHost, s));
+  CK(copy_async(stats, ctx->stats.p, sizeof(stats), cudaMemcpyDeviceToHost, s));
   std::vector<int> it(ctx->n_inst);
   std::vector<double> rr(ctx->n_inst);
-  CK(cudaMemcpyAsync(it.data(), ctx->b_iters.p, ctx->n_inst * sizeof(int), cudaMemcpyDeviceToHost, s));
-  CK(cudaMemcpyAsync(rr.data(), ctx->b_relres.p, ctx->n_inst * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(copy_async(it.data(), ctx->b_iters.p, ctx->n_inst * sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(copy_async(rr.data(), ctx->b_relres.p, ctx->n_inst * sizeof(double), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   ctx->has_estimate = true;
   ctx->has_batch_run = true;
@@ -290,12 +291,12 @@ pdds_status pdds_batch_instance(pdds_ctx* ctx, int32_t i, int32_t* nknots, doubl
   int it = 0;
   double rr = 0.0;
   unsigned long long t[2] = {0, 0};
-  if (u) CK(cudaMemcpyAsync(u, ctx->su.p + k0, nk * sizeof(double), cudaMemcpyDeviceToHost, s));
-  if (B) CK(cudaMemcpyAsync(B, ctx->B.p + k0, nk * sizeof(double), cudaMemcpyDeviceToHost, s));
-  CK(cudaMemcpyAsync(&it, ctx->b_iters.p + i, sizeof(int), cudaMemcpyDeviceToHost, s));
-  CK(cudaMemcpyAsync(&rr, ctx->b_relres.p + i, sizeof(double), cudaMemcpyDeviceToHost, s));
-  CK(cudaMemcpyAsync(&t[0], ctx->b_tend.p + i, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
-  CK(cudaMemcpyAsync(&t[1], ctx->b_tend.p + ctx->n_inst, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+  if (u) CK(copy_async(u, ctx->su.p + k0, nk * sizeof(double), cudaMemcpyDeviceToHost, s));
+  if (B) CK(copy_async(B, ctx->B.p + k0, nk * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(copy_async(&it, ctx->b_iters.p + i, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(copy_async(&rr, ctx->b_relres.p + i, sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(copy_async(&t[0], ctx->b_tend.p + i, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+  CK(copy_async(&t[1], ctx->b_tend.p + ctx->n_inst, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   if (iterations) *iterations = it;
   if (rel_residual) *rel_residual = rr;

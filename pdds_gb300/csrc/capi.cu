@@ -19,6 +19,11 @@ using namespace pdds;
 
 namespace pdds {
 
+XferCount& xfer() {
+  thread_local XferCount t;
+  return t;
+}
+
 pdds_status fail(pdds_ctx* c, pdds_status s, const std::string& msg) {
   if (c) c->err = msg;
   return s;
@@ -32,6 +37,14 @@ void drop_graph(pdds_ctx* ctx) {
   ctx->graph_key.clear();
   ctx->graph_launches = 0;
   ctx->graph_path_nodes.clear();
+}
+
+void clear_tune(pdds_ctx* ctx) {
+  ctx->tune_bps = 0;
+  ctx->tune_ppc = 0;
+  ctx->tune_threads = 0;
+  ctx->tune_kind = -1;
+  ctx->tune_rich = -1;
 }
 
 pdds_status upload_layout(pdds_ctx* ctx) {
@@ -207,7 +220,7 @@ ProblemDev problem_dev(const pdds_ctx* ctx) {
 
 pdds_status check_err_flags(pdds_ctx* ctx) {
   unsigned f = 0;
-  CK(cudaMemcpyAsync(&f, ctx->errf.p, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(copy_async(&f, ctx->errf.p, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   if (f & ERR_FLAG_SINGULAR) return fail(ctx, PDDS_ERR_ILL_CONDITIONED, "RBF matrix numerically singular");
   if (f & ERR_FLAG_STEP_LIMIT) return fail(ctx, PDDS_ERR_STEP_LIMIT, "a path exceeded max_steps");
@@ -427,8 +440,8 @@ pdds_status adaptive_continue(pdds_ctx* ctx, const pdds_estimate_desc* desc, con
   const int nmax = std::max(N0, desc->npaths_max > 0 ? desc->npaths_max : 100000);
   const double eps = desc->target_stderr > 0 ? desc->target_stderr : 1e-3;
   std::vector<double> bs(K), bbs(K);
-  CK(cudaMemcpyAsync(bs.data(), ctx->Bsum.p, K * sizeof(double), cudaMemcpyDeviceToHost, s));
-  CK(cudaMemcpyAsync(bbs.data(), ctx->BBsum.p, K * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(copy_async(bs.data(), ctx->Bsum.p, K * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(copy_async(bbs.data(), ctx->BBsum.p, K * sizeof(double), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   std::vector<int> kn(K, 0), ik, ip0, ip1;
   std::vector<double> scale(K, 1.0), inv(K, 0.0);
@@ -614,8 +627,8 @@ pdds_status pdds_problem_set_lut(pdds_ctx* ctx, const float* coef, const float* 
   const size_t n = (size_t)nx * ny;
   CK(ctx->lut_coef.resize(8 * n));
   CK(ctx->lut_g.resize(n));
-  CK(cudaMemcpyAsync(ctx->lut_coef.p, coef, 8 * n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
-  CK(cudaMemcpyAsync(ctx->lut_g.p, g, n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+  CK(copy_async(ctx->lut_coef.p, coef, 8 * n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+  CK(copy_async(ctx->lut_g.p, g, n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->lut_nx = nx;
   ctx->lut_ny = ny;
@@ -632,6 +645,7 @@ pdds_status pdds_layout_build(pdds_ctx* ctx, const pdds_layout_desc* desc, pdds_
     CK(cudaStreamSynchronize(ctx->stream));
   }
   drop_graph(ctx);
+  clear_tune(ctx);
   ctx->is_batch = false;
   ctx->n_inst = 0;
   ctx->has_batch_run = false;
@@ -640,11 +654,13 @@ pdds_status pdds_layout_build(pdds_ctx* ctx, const pdds_layout_desc* desc, pdds_
   if (!e.empty()) return fail(ctx, PDDS_ERR_INVALID, e);
   ctx->has_layout = true;
   ctx->has_estimate = false;
+  const int64_t h2d0 = xfer().h2d;
   if (ctx->device >= 0) {
     pdds_status st = upload_layout(ctx);
     if (st != PDDS_OK) return st;
   }
   if (info) {
+    info->h2d_bytes = xfer().h2d - h2d0;
     info->nknots = ctx->L.K;
     info->nboundary = ctx->L.nboundary;
     info->nstencils = (int)ctx->L.stencils.size();
@@ -665,6 +681,7 @@ pdds_status pdds_layout_build_circle(pdds_ctx* ctx, const pdds_circle_desc* desc
     CK(cudaStreamSynchronize(ctx->stream));
   }
   drop_graph(ctx);
+  clear_tune(ctx);
   ctx->is_batch = false;
   ctx->n_inst = 0;
   ctx->has_batch_run = false;
@@ -673,11 +690,13 @@ pdds_status pdds_layout_build_circle(pdds_ctx* ctx, const pdds_circle_desc* desc
   if (!e.empty()) return fail(ctx, PDDS_ERR_INVALID, e);
   ctx->has_layout = true;
   ctx->has_estimate = false;
+  const int64_t h2d0 = xfer().h2d;
   if (ctx->device >= 0) {
     pdds_status st = upload_layout(ctx);
     if (st != PDDS_OK) return st;
   }
   if (info) {
+    info->h2d_bytes = xfer().h2d - h2d0;
     info->nknots = ctx->L.K;
     info->nboundary = ctx->L.nboundary;
     info->nstencils = (int)ctx->L.stencils.size();
@@ -753,6 +772,7 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
   CK(cudaSetDevice(ctx->device));
   cudaStream_t s = ctx->stream;
   HostLayout& L = ctx->L;
+  const XferCount x0 = xfer();
   const int bins = desc->bins_per_gap > 0 ? desc->bins_per_gap : 16;
   if (bins != ctx->bins) {
     ctx->bins = bins;
@@ -813,7 +833,7 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
     if (desc->ipsi_override) {
       CK(ctx->knot_ipsi_off.upload(kipoff, s));
       CK(ctx->ipsi_knot.resize(std::max<int64_t>(ipo, 1)));
-      CK(cudaMemcpyAsync(ctx->ipsi_knot.p, desc->ipsi_override, ipo * sizeof(double),
+      CK(copy_async(ctx->ipsi_knot.p, desc->ipsi_override, ipo * sizeof(double),
                          cudaMemcpyHostToDevice, s));
     }
     ReplayArgs a;
@@ -846,8 +866,8 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
     if (info) {
       // step counts from the exit records
       std::vector<int> sl(total), ss(total), sd(total);
-      CK(cudaMemcpyAsync(sl.data(), ctx->rsl.p, total * sizeof(int), cudaMemcpyDeviceToHost, s));
-      CK(cudaMemcpyAsync(sd.data(), ctx->rside.p, total * sizeof(int), cudaMemcpyDeviceToHost, s));
+      CK(copy_async(sl.data(), ctx->rsl.p, total * sizeof(int), cudaMemcpyDeviceToHost, s));
+      CK(copy_async(sd.data(), ctx->rside.p, total * sizeof(int), cudaMemcpyDeviceToHost, s));
       CK(cudaStreamSynchronize(s));
       int64_t steps = 0, ng = 0, nsn = 0;
       for (int64_t q = 0; q < total; q++) {
@@ -922,15 +942,15 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
     for (int v = 0; v < L.K; v++)
       if (!L.knot_boundary[v]) ctx->last_knot_N[v] = N;
   }
-  if (val && nnz) CK(cudaMemcpyAsync(val, ctx->G.p, nnz * sizeof(double), cudaMemcpyDeviceToHost, s));
+  if (val && nnz) CK(copy_async(val, ctx->G.p, nnz * sizeof(double), cudaMemcpyDeviceToHost, s));
   if (var && nnz) {
     if (mode == PDDS_MODE_FP64) std::fill(var, var + nnz, 0.0);
-    else CK(cudaMemcpyAsync(var, ctx->GG.p, nnz * sizeof(double), cudaMemcpyDeviceToHost, s));
+    else CK(copy_async(var, ctx->GG.p, nnz * sizeof(double), cudaMemcpyDeviceToHost, s));
   }
-  if (Bout) CK(cudaMemcpyAsync(Bout, ctx->B.p, L.K * sizeof(double), cudaMemcpyDeviceToHost, s));
-  if (BBout) CK(cudaMemcpyAsync(BBout, ctx->BB.p, L.K * sizeof(double), cudaMemcpyDeviceToHost, s));
+  if (Bout) CK(copy_async(Bout, ctx->B.p, L.K * sizeof(double), cudaMemcpyDeviceToHost, s));
+  if (BBout) CK(copy_async(BBout, ctx->BB.p, L.K * sizeof(double), cudaMemcpyDeviceToHost, s));
   unsigned long long st[8] = {0};
-  CK(cudaMemcpyAsync(st, ctx->stats.p, sizeof(st), cudaMemcpyDeviceToHost, s));
+  CK(copy_async(st, ctx->stats.p, sizeof(st), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   ctx->has_estimate = true;
   if (info) {
@@ -952,8 +972,14 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
       info->exits_global = (int64_t)st[2];
       info->exits_stencil = (int64_t)st[3];
     }
+    info->cta_threads = mode == PDDS_MODE_MIXED ? cta_threads_for(ctx, desc) : 0;
   }
-  return check_err_flags(ctx);
+  const pdds_status fst = check_err_flags(ctx);
+  if (info) {
+    info->h2d_bytes = xfer().h2d - x0.h2d;
+    info->d2h_bytes = xfer().d2h - x0.d2h;
+  }
+  return fst;
 }
 
 pdds_status pdds_autotune(pdds_ctx* ctx, const pdds_estimate_desc* desc, int32_t sample_knots,
@@ -963,6 +989,8 @@ pdds_status pdds_autotune(pdds_ctx* ctx, const pdds_estimate_desc* desc, int32_t
   if (!ctx->has_problem || !ctx->has_layout) return fail(ctx, PDDS_ERR_INVALID, "problem and layout needed");
   if (desc->mode != PDDS_MODE_MIXED) return fail(ctx, PDDS_ERR_INVALID, "the autotuner tunes PDDS_MODE_MIXED");
   if (desc->npaths < 1 || !(desc->h > 0.0)) return fail(ctx, PDDS_ERR_INVALID, "npaths >= 1 and h > 0 required");
+  if (desc->cta_threads != 0 && desc->cta_threads != 128 && desc->cta_threads != 256)
+    return fail(ctx, PDDS_ERR_INVALID, "cta_threads must be 0, 128 or 256");
   CK(cudaSetDevice(ctx->device));
   cudaStream_t s = ctx->stream;
   const HostLayout& L = ctx->L;
@@ -984,7 +1012,10 @@ pdds_status pdds_autotune(pdds_ctx* ctx, const pdds_estimate_desc* desc, int32_t
   int launches = 0;
   pdds_status st = enqueue_prefix(ctx, &d, P, false, &launches);
   if (st != PDDS_OK) return st;
-  d.cta_threads = mixed_threads(ctx->n_mc);  // the default shape first
+  // a block size imposed by the caller is kept: only the other shape
+  // parameters are searched; 0 searches both block sizes
+  const int fixed_threads = desc->cta_threads;
+  d.cta_threads = fixed_threads > 0 ? fixed_threads : mixed_threads(ctx->n_mc);  // the default shape first
   auto occupancy = [&](int threads) {
     const size_t smem = ctx->mixed_smem * (d.want_var ? 2 : 1) + mixed_queue_smem(threads, d.richardson);
     return std::max(1, mixed_blocks_per_sm(P.kind, smem, d.richardson, threads));
@@ -1034,6 +1065,7 @@ pdds_status pdds_autotune(pdds_ctx* ctx, const pdds_estimate_desc* desc, int32_t
   st = time_shape(occ, def_ppc, &def_ms);
   if (st != PDDS_OK) return st;
   for (int th : {128, 256}) {
+    if (fixed_threads > 0 && th != fixed_threads) continue;
     d.cta_threads = th;
     const int occ_t = occupancy(th);
     for (int b = 1; b <= occ_t; b++)
@@ -1058,6 +1090,7 @@ pdds_status pdds_autotune(pdds_ctx* ctx, const pdds_estimate_desc* desc, int32_t
   ctx->tune_kind = ctx->prob.kind;
   ctx->tune_rich = d.richardson ? 1 : 0;
   ctx->has_estimate = false;
+  drop_graph(ctx);  // a captured batch sequence holds the old launch shape
   if (info) {
     info->blocks_per_sm = best_bps;
     info->paths_per_item = best_ppc;
@@ -1120,7 +1153,7 @@ pdds_status pdds_subdomain_solve(pdds_ctx* ctx, int32_t m, const double* u, doub
   const double* ud = ctx->su.p;
   if (u) {
     CK(ctx->sub_u.resize(std::max(L.K, 1)));
-    CK(cudaMemcpyAsync(ctx->sub_u.p, u, L.K * sizeof(double), cudaMemcpyHostToDevice, s));
+    CK(copy_async(ctx->sub_u.p, u, L.K * sizeof(double), cudaMemcpyHostToDevice, s));
     ud = ctx->sub_u.p;
   }
   CK(ctx->sub_out.resize((size_t)S * m * m));
@@ -1135,7 +1168,7 @@ pdds_status pdds_subdomain_solve(pdds_ctx* ctx, int32_t m, const double* u, doub
   } else {
     CK(launch_subdomain(ctx->dl, problem_dev(ctx), ns, m, n, ctx->edge_knots.p, ud, ctx->sub_out.p, ctx->ugrid.p, s));
   }
-  CK(cudaMemcpyAsync(out, ctx->sub_out.p, (size_t)S * m * m * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(copy_async(out, ctx->sub_out.p, (size_t)S * m * m * sizeof(double), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   ctx->ugrid_m = m;
   if (kind == PDDS_LUT) return check_err_flags(ctx);
@@ -1200,7 +1233,7 @@ pdds_status pdds_estimate_knot_steps(pdds_ctx* ctx, int64_t* steps) {
   if (!ctx || !steps) return PDDS_ERR_INVALID;
   if (!ctx->has_estimate || !ctx->has_knot_steps) return fail(ctx, PDDS_ERR_INVALID, "no MIXED estimate on this layout");
   CK(cudaSetDevice(ctx->device));
-  CK(cudaMemcpyAsync(steps, ctx->knot_steps.p, ctx->L.K * sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(copy_async(steps, ctx->knot_steps.p, ctx->L.K * sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   return PDDS_OK;
 }
@@ -1222,6 +1255,7 @@ pdds_status pdds_solve_interface(pdds_ctx* ctx, const pdds_solve_desc* desc, dou
   const HostLayout& L = ctx->L;
   const int K = L.K;
   const int64_t nnz = L.row_ptr[K];
+  const XferCount x0 = xfer();
   // GMRES(20): on config 2 every restart length from 20 to 40 needs the same
   // 120 Arnoldi steps, and the shorter basis makes each step cheaper
   const int m = std::max(2, std::min(desc->restart > 0 ? desc->restart : 20, 40));
@@ -1270,7 +1304,7 @@ pdds_status pdds_solve_interface(pdds_ctx* ctx, const pdds_solve_desc* desc, dou
     return fail(ctx, PDDS_ERR_INVALID, "unknown solve method");
   }
   CK(cudaEventRecord(ctx->ev1, s));
-  if (u) CK(cudaMemcpyAsync(u, ctx->su.p, K * sizeof(double), cudaMemcpyDeviceToHost, s));
+  if (u) CK(copy_async(u, ctx->su.p, K * sizeof(double), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   ctx->has_solution = true;
   if (info) {
@@ -1284,6 +1318,10 @@ pdds_status pdds_solve_interface(pdds_ctx* ctx, const pdds_solve_desc* desc, dou
   }
   {
     pdds_status st = check_err_flags(ctx);
+    if (info) {
+      info->h2d_bytes = xfer().h2d - x0.h2d;
+      info->d2h_bytes = xfer().d2h - x0.d2h;
+    }
     if (st != PDDS_OK) return st;
   }
   if (!(relres <= tol * 1.0000001) && !(relres == 0.0))

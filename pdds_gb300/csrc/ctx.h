@@ -9,6 +9,7 @@
 #include "../../include/pdds.h"
 #include "kernels.h"
 #include "pdds_internal.h"
+#include "xfer.h"
 
 namespace pdds {
 
@@ -29,7 +30,7 @@ struct DBuf {
   cudaError_t upload(const std::vector<T>& v, cudaStream_t s) {
     cudaError_t e = resize(std::max<size_t>(v.size(), 1));
     if (e != cudaSuccess || v.empty()) return e;
-    return cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s);
+    return copy_async(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s);
   }
   void release() {
     if (p) cudaFree(p);
@@ -145,6 +146,8 @@ pdds_status check_err_flags(pdds_ctx* ctx);
 pdds_status enqueue_mixed(pdds_ctx* ctx, const pdds_estimate_desc* desc, int* launches);
 // Destroys the captured batch graph (its kernels hold buffer addresses).
 void drop_graph(pdds_ctx* ctx);
+// Forgets the autotuned launch shape (it was timed on the previous layout).
+void clear_tune(pdds_ctx* ctx);
 
 }  // namespace pdds
 

@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "solve.h"
+#include "xfer.h"
 
 namespace pdds {
 
@@ -184,18 +185,27 @@ cudaError_t solve_bicgstab(const SolveCsr& A, const double* b, double* x, SolveW
   k_init_scal<<<1, 1, 0, s>>>(sc);
   dot2(s, n, b, b, nullptr, nullptr, w.part, sc + S_COUNT, nullptr, &w.launches);
   double rhs_sq = 0.0;
-  cudaMemcpyAsync(&rhs_sq, sc + S_COUNT, sizeof(double), cudaMemcpyDeviceToHost, s);
-  cudaStreamSynchronize(s);
   *iters = 0;
   *relres = 0.0;
-  if (rhs_sq == 0.0) return cudaGetLastError();
+  // launch errors of this solve, then the copy and the wait: the first
+  // failure ends the solve (no further launches against a stale residual)
+  cudaError_t e = cudaPeekAtLastError();
+  if (e == cudaSuccess) e = copy_async(&rhs_sq, sc + S_COUNT, sizeof(double), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return e;
+  if (rhs_sq == 0.0) return cudaSuccess;
   const double tol2 = tol * tol * rhs_sq;
   int it = 0;
   double rr = rhs_sq;
   while (it < max_iter) {
     dot2(s, n, r, r, r0, r, w.part, sc + S_RR, sc + S_RHO_NEW, &w.launches);
-    cudaMemcpyAsync(w.host_rr, sc + S_RR, sizeof(double), cudaMemcpyDeviceToHost, s);
-    cudaStreamSynchronize(s);
+    e = cudaPeekAtLastError();
+    if (e == cudaSuccess) e = copy_async(w.host_rr, sc + S_RR, sizeof(double), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+      *iters = it;
+      return e;
+    }
     rr = *w.host_rr;
     if (!(rr > tol2)) break;
     ++w.launches;
@@ -218,15 +228,17 @@ cudaError_t solve_bicgstab(const SolveCsr& A, const double* b, double* x, SolveW
     k_bicg_x<<<vg, 256, 0, s>>>(n, x, p, sv, r, t, sc);
     ++it;
   }
+  *iters = it;
   if (it == max_iter) {
     dot2(s, n, r, r, nullptr, nullptr, w.part, sc + S_RR, nullptr, &w.launches);
-    cudaMemcpyAsync(w.host_rr, sc + S_RR, sizeof(double), cudaMemcpyDeviceToHost, s);
-    cudaStreamSynchronize(s);
+    e = cudaPeekAtLastError();
+    if (e == cudaSuccess) e = copy_async(w.host_rr, sc + S_RR, sizeof(double), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return e;
     rr = *w.host_rr;
   }
-  *iters = it;
   *relres = std::sqrt(rr / rhs_sq);
-  return cudaGetLastError();
+  return cudaSuccess;
 }
 
 // ---------------------------------------------------------------- fused GMRES
@@ -459,7 +471,7 @@ cudaError_t solve_gmres_ir(const SolveCsr& A, const double* b, double* x, SolveW
   k_fill<<<vg, 256, 0, s>>>(n, x, 0.0);
   dot2(s, n, b, b, nullptr, nullptr, w.part, bb, nullptr, &w.launches);
   double hb = 0.0;
-  cudaMemcpyAsync(&hb, bb, sizeof(double), cudaMemcpyDeviceToHost, s);
+  copy_async(&hb, bb, sizeof(double), cudaMemcpyDeviceToHost, s);
   cudaStreamSynchronize(s);
   *iters = 0;
   *refines = 0;
@@ -476,7 +488,7 @@ cudaError_t solve_gmres_ir(const SolveCsr& A, const double* b, double* x, SolveW
     k_resid<<<vg, 256, 0, s>>>(n, b, Ax, r);
     dot2(s, n, r, r, nullptr, nullptr, w.part, rr, nullptr, &w.launches);
     double hv[2] = {0.0, 0.0};
-    cudaMemcpyAsync(hv, rr, 2 * sizeof(double), cudaMemcpyDeviceToHost, s);
+    copy_async(hv, rr, 2 * sizeof(double), cudaMemcpyDeviceToHost, s);
     cudaStreamSynchronize(s);
     hr = hv[0];
     if (ref > 0) total += (int)hv[1];
@@ -556,8 +568,8 @@ cudaError_t solve_gmres_ir_cluster(const SolveCsr& A, const double* b, double* x
   if (e != cudaSuccess) return e;
   int hi[2] = {0, 0};
   double hr = 0.0;
-  cudaMemcpyAsync(hi, ctl + 2, 2 * sizeof(int), cudaMemcpyDeviceToHost, s);
-  cudaMemcpyAsync(&hr, w.scal, sizeof(double), cudaMemcpyDeviceToHost, s);
+  copy_async(hi, ctl + 2, 2 * sizeof(int), cudaMemcpyDeviceToHost, s);
+  copy_async(&hr, w.scal, sizeof(double), cudaMemcpyDeviceToHost, s);
   e = cudaStreamSynchronize(s);
   *iters = hi[0];
   *refines = hi[1];

@@ -21,6 +21,10 @@
 //   * The first call on a device looks up the array's device address with
 //     cudaGetSymbolAddress (once per device); make that first call before any
 //     stream capture on that device.
+//   * The looked-up address belongs to the device's current primary context.
+//     cudaDeviceReset destroys that context (and the array with it); the
+//     library, this entry point included, must not be used on a device after
+//     it has been reset (the address kept here would then be stale).
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -95,6 +99,9 @@ extern "C" pdds_status pdds_solve_bicgstab_static(int device, int32_t K, int64_t
     base = g_scratch_addr[device];
   }
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // an error left behind by an earlier, unrelated runtime call of the caller
+  // is not this solve's failure: clear it before the first enqueue
+  (void)cudaGetLastError();
   pdds::SolveWork w;
   std::memset(&w, 0, sizeof w);
   for (int q = 0; q < 6; q++) w.v64[q] = base + (size_t)q * K;

@@ -67,6 +67,17 @@ def test_autotuner_keeps_results_and_picks_a_valid_shape():
         t = pd.autotune(bvp, 3000, H, sample_knots=64, adaptive_h=True, richardson=True)
         assert 1 <= t["blocks_per_sm"] <= 8 and 1 <= t["paths_per_item"] <= 3000
         assert t["candidates"] >= 2 and 0 < t["best_ms"] <= t["default_ms"] * 1.2  # timing noise
+        assert t["cta_threads"] in (128, 256)
         after = pd.estimate(bvp, 3000, H, mode=P.MODE_MIXED, seed=4, adaptive_h=True, richardson=True)
         assert np.max(np.abs(after.B - before.B)) < 1e-9
         assert np.max(np.abs(after.val - before.val)) < 1e-5
+        # a later estimate without a block size of its own runs the tuned one
+        assert after.info["cta_threads"] == t["cta_threads"]
+        # a block size imposed by the caller is kept and only the rest is searched
+        other = 384 - t["cta_threads"]
+        t2 = pd.autotune(bvp, 3000, H, sample_knots=64, adaptive_h=True, richardson=True, cta_threads=other)
+        assert t2["cta_threads"] == other
+        again = pd.estimate(bvp, 3000, H, mode=P.MODE_MIXED, seed=4, adaptive_h=True, richardson=True)
+        assert again.info["cta_threads"] == other
+        with pytest.raises(P.PDDSError):
+            pd.autotune(bvp, 3000, H, sample_knots=64, cta_threads=192)

@@ -5,10 +5,11 @@ whose device memory belongs to another allocator, serving loops where
 cudaMalloc/cudaFree would synchronise or stall, foreign-language hosts that
 only lend device buffers.  The test hands it caller-owned device buffers (here
 allocated by torch, playing such a host) and checks its solution against the
-regular entry point pdds_solve_interface on the same system, for two calls in
-a row on different systems (the shared static work array must not carry state
-from one call into the next), and checks that a system larger than the static
-limit is refused with a message.  This file is collected last on purpose.
+regular entry point pdds_solve_interface and against a dense solve of the
+same system, for two calls in a row on different systems (the shared static
+work array must not carry state from one call into the next), and checks that
+a system larger than the static limit is refused with a message.  This file is
+collected last on purpose.
 """
 import ctypes as C
 
@@ -56,6 +57,12 @@ def test_static_solve_matches_regular_entry_twice():
             assert np.all(np.isfinite(u_st))
             np.testing.assert_allclose(u_st, u_ref, rtol=0, atol=ATOL)
             assert rr <= tol and it == info["iterations"]
+            # and against a dense solve of the same system, independent of
+            # the BiCGSTAB kernels both entry points share
+            A = np.eye(pd.K)
+            r, c, v = est.triplets()
+            np.add.at(A, (r, c), v)
+            np.testing.assert_allclose(u_st, np.linalg.solve(A, est.B), rtol=0, atol=ATOL)
 
 
 def test_static_solve_rejects_oversized_systems():
