@@ -152,6 +152,38 @@ pdds_status pdds_layout_csr(pdds_ctx* ctx, int64_t* row_ptr, int32_t* col);
 pdds_status pdds_layout_stencil(pdds_ctx* ctx, int32_t knot, double* rect, int32_t* kinds,
                                 int32_t* sizes, int32_t* idx, int32_t maxn);
 
+/* A stencil built by the caller, as the reference's Stencil::Init and
+ * Compute_ipsi receive it (Meshes/stencil.hpp:57-98, Meshes/stencil.cpp:11-85,
+ * 115-243): the rectangle stencil_parameters = {x0, y0, x1, y1} and, per side
+ * N, S, E, W, the knot indices and positions in the caller's order (a
+ * repeated index keeps its last position and consecutive repeats are
+ * dropped, as Init does) and the side's RBF shape c2.  n[d] = 0: no side.
+ * A side's knots lie on that side of the rectangle, in increasing order
+ * along it (the reference's interfaces list them so); at most 160 per side. */
+typedef struct {
+  double rect[4];
+  int32_t n[4];
+  const int32_t* index[4];
+  const double* x[4];
+  const double* y[4];
+  double c2[4];
+} pdds_stencil_desc;
+
+/* Replaces the context's layout with caller-built knots and stencils (the
+ * reference's worker receives a knot and builds its stencil itself,
+ * PDDAlgorithms/PDDSparseGM.cpp:795-848, Compute_Stencil :1845-2041): knot i
+ * sits at (x[i], y[i]) with stencil st[i] and draws the Philox knot word
+ * knot_id[i] (NULL: i), so a knot of a built layout can be re-run alone on
+ * its own random stream.  domain = {x0, y0, x1, y1} is the problem's
+ * rectangle (the stencil's global_parameters): exits on it score g, and a
+ * knot on it takes B = g.  G's columns are the caller's knot indices;
+ * pdds_solve_interface needs them in [0, nknots), and subdomain solves need a
+ * layout from pdds_layout_build.  Estimation then runs in every mode; the
+ * replay mode's ipsi_override lists the knots in index order. */
+pdds_status pdds_stencils_set(pdds_ctx* ctx, const double domain[4], int32_t nknots, const double* x,
+                              const double* y, const int32_t* knot_id, const pdds_stencil_desc* st,
+                              pdds_layout_info* info);
+
 /* ---------------------------------------------------------------- estimate */
 typedef enum {
   PDDS_MODE_REPLAY_FP64 = 0, /* bit-exact replay of the CPU restatement          */
@@ -226,6 +258,22 @@ pdds_status pdds_estimate_knot_paths(pdds_ctx* ctx, int32_t* npaths);
  * over its paths (both levels of a Richardson pair): steps[K]. */
 pdds_status pdds_estimate_knot_steps(pdds_ctx* ctx, int64_t* steps);
 
+/* One knot as EMFKACSolver::Solve_OMP_Analytic computes it
+ * (Solvers/EMFKACSolver.hpp:711-729): from X0 = (x0, y0) inside the stencil
+ * st of the problem's rectangle domain, with the paths, step and weight rule
+ * of desc, the knot's G row -- G_j (sorted knot indices, the order of
+ * G_return_withrep), G, G_var (want_var, or the replay mode) -- and B, BB.
+ * A knot on the domain boundary takes B = g(X0), BB = B^2 and an empty row,
+ * as the reference does.  knot_id is the Philox knot word (the knot's index
+ * in its layout gives the stream pdds_estimate draws for it).  The arrays
+ * hold max_nnz entries; *nnz receives the row length (PDDS_ERR_INVALID when
+ * it exceeds max_nnz).  Replaces the context's layout by this one knot
+ * (pdds_stencils_set). */
+pdds_status pdds_estimate_knot(pdds_ctx* ctx, const double domain[4], double x0, double y0, int32_t knot_id,
+                               const pdds_stencil_desc* st, const pdds_estimate_desc* desc, int32_t* G_j,
+                               double* G, double* G_var, int32_t max_nnz, int32_t* nnz, double* B, double* BB,
+                               pdds_estimate_info* info);
+
 /* Autotuner of the MIXED path kernel (no counterpart in the reference):
  * times the kernel on a sample of knots of the current layout and problem
  * for candidate launch shapes -- persistent CTAs per SM (1 .. the occupancy
@@ -264,6 +312,10 @@ typedef struct {
   int32_t max_iter;      /* inner iterations per call / refinement step */
   int32_t max_refine;    /* FP64 refinement steps */
   double tol;            /* relative residual in FP64 */
+  /* GMRES over the whole GPU (systems of 4096 knots and more): polls of a
+   * grid-barrier wait before it gives up and the solve returns
+   * PDDS_ERR_TIMEOUT (0 = 2^24, about a second; >= 0) */
+  int32_t barrier_poll_limit;
 } pdds_solve_desc;
 
 typedef struct {
@@ -399,6 +451,40 @@ typedef struct {
   double c2, alpha, k;    /* LINEAR_SHIFT: reaction, shift, time rescale (> 0) */
 } pdds_semilinear_desc;
 pdds_status pdds_semilinear_tables(pdds_ctx* ctx, const pdds_semilinear_desc* desc);
+
+/* ---------------------------------------------------------------- self-checks
+ * No counterpart in the reference (its increments come from Boost's
+ * mt19937 + normal_distribution, Integrators/FKACIntegrator.hpp:15-19, and
+ * its exponentials from libm, BVPs/BVP.hpp:84-87).  The library's own
+ * generator and FP64 functions, evaluated on given inputs so that they can be
+ * held against published known answers and libm: on the device (device >= 0,
+ * compiled exactly as the path kernels use them) or on the host (device < 0,
+ * the code the CPU restatement shares).  err, if given, receives a message of
+ * at most err_len bytes.
+ *
+ * pdds_check_philox: out[4i..4i+3] = Philox-4x32-10 (Salmon et al., SC'11) of
+ * the counter ctr[4i..4i+3] under the key (key[2i], key[2i+1]).  The path
+ * kernels put (step pair, path, knot, instance) in the counter and the seed's
+ * low and high words in the key.  form PDDS_PHILOX_PORTABLE is the generator of
+ * the replay and FP64 kernels (host and device), PDDS_PHILOX_ROUND_KEYS the
+ * MIXED kernel's form with the key schedule passed as kernel parameters
+ * (device only). */
+#define PDDS_PHILOX_PORTABLE 0
+#define PDDS_PHILOX_ROUND_KEYS 1
+pdds_status pdds_check_philox(int device, int32_t form, const uint32_t* ctr, const uint32_t* key, int32_t n,
+                              uint32_t* out, char* err, int32_t err_len);
+/* pdds_check_portable_math: out[i] = fn(x[i]) with the portable FP64
+ * functions of the replay kernels (no FMA contraction); for the Box-Muller
+ * pair, the bits of x[i] hold the two Philox words (low word = the radius
+ * word) and out[i] is the first or second normal. */
+#define PDDS_FN_EXP 0
+#define PDDS_FN_LOG 1
+#define PDDS_FN_SIN 2
+#define PDDS_FN_COS 3
+#define PDDS_FN_BOX_MULLER_Z0 4
+#define PDDS_FN_BOX_MULLER_Z1 5
+pdds_status pdds_check_portable_math(int device, int32_t fn, const double* x, int32_t n, double* out, char* err,
+                                     int32_t err_len);
 
 /* ---------------------------------------------------------------- allocation-free solve
  * No counterpart in the reference.  For callers that cannot let a library

@@ -10,7 +10,10 @@
  *     B, B_var = B^2 - BB per knot
  *   Compute_Solution :3168-3246                Compute_Solution(method, tol) -> u
  *   EMFKACSolver::Solve_OMP_Analytic           Solve_Knot(k, ...): one knot's G row, G_var, G_j, B, BB
- *     (Solvers/EMFKACSolver.hpp:711-729)          read from the all-knot estimate
+ *     (Solvers/EMFKACSolver.hpp:711-729)          read from the all-knot estimate, and
+ *                                              pdds::EMFKACSolver::Solve_GPU_Analytic: one knot from
+ *                                              any X0 and a caller-built pdds::Stencil
+ *   Stencil (Meshes/stencil.hpp:13-98)         pdds::Stencil (Init, Compute_ipsi)
  *
  * Errors are thrown as pdds::Error (status + the library's message).
  */
@@ -19,6 +22,7 @@
 
 #include <array>
 #include <cmath>
+#include <map>
 #include <stdexcept>
 #include <string>
 #include <utility>
@@ -201,6 +205,115 @@ class PDDSparseGM {
   std::vector<int64_t> row_ptr_;
   std::vector<int32_t> col_;
   std::vector<double> G_, Gvar_, B_, BB_;
+};
+
+// Side directions of a stencil, the reference's enum (Meshes/stencil.hpp:13).
+enum direction { North, South, East, West };
+
+// A knot's stencil as the reference's Stencil class receives it
+// (Meshes/stencil.hpp:13-98): Init with the side knot lists, Compute_ipsi
+// with the RBF shapes, the rectangle stencil_parameters and the problem's
+// rectangle global_parameters.  The library factorises the RBF matrices.
+class Stencil {
+ public:
+  double stencil_parameters[4] = {0, 0, 0, 0};
+  double global_parameters[4] = {0, 0, 0, 0};
+
+  void Init(std::map<direction, std::vector<int>> s_index, std::map<direction, std::vector<double>> s_x,
+            std::map<direction, std::vector<double>> s_y, const double* parameters) {
+    for (int i = 0; i < 4; i++) stencil_parameters[i] = parameters[i];
+    for (int d = 0; d < 4; d++) {
+      const direction dd = static_cast<direction>(d);
+      index_[d] = s_index[dd];
+      x_[d] = s_x[dd];
+      y_[d] = s_y[dd];
+      if (x_[d].size() != index_[d].size() || y_[d].size() != index_[d].size())
+        throw Error(PDDS_ERR_INVALID, "Stencil::Init: index, x and y differ in length");
+    }
+  }
+  // c2[4] in the order North, South, East, West (Stencil::Compute_ipsi)
+  void Compute_ipsi(const double c2[4]) {
+    for (int d = 0; d < 4; d++) c2_[d] = c2[d];
+  }
+  void Compute_ipsi(double c2) {
+    for (int d = 0; d < 4; d++) c2_[d] = c2;
+  }
+  pdds_stencil_desc desc() const {
+    pdds_stencil_desc s{};
+    for (int i = 0; i < 4; i++) s.rect[i] = stencil_parameters[i];
+    for (int d = 0; d < 4; d++) {
+      s.n[d] = (int32_t)index_[d].size();
+      s.index[d] = index_[d].empty() ? nullptr : index_[d].data();
+      s.x[d] = x_[d].empty() ? nullptr : x_[d].data();
+      s.y[d] = y_[d].empty() ? nullptr : y_[d].data();
+      s.c2[d] = c2_[d];
+    }
+    return s;
+  }
+  size_t side_size(direction d) const { return index_[d].size(); }
+
+ private:
+  std::vector<int32_t> index_[4];
+  std::vector<double> x_[4], y_[4];
+  double c2_[4] = {1, 1, 1, 1};
+};
+
+// The reference's per-knot solver (Solvers/EMFKACSolver.hpp) on the GPU.
+// Solve_GPU_Analytic has the argument list of Solve_OMP_Analytic
+// (:711-729); the choices it has no argument for -- precision mode, seed,
+// weight rule, replay inverses, the Philox knot word -- are the members
+// `options` and `knot_id`.  rho and c2 are accepted and, as in the
+// reference's G_update, unused: the side shapes come from the stencil.
+class EMFKACSolver {
+ public:
+  explicit EMFKACSolver(int device = 0) {
+    options = estimate_desc(1, 1e-3, PDDS_MODE_FP64);
+    options.want_var = 1;
+    const pdds_status s = pdds_create(&ctx_, device, 0);
+    if (s != PDDS_OK) throw Error(s, "pdds_create");
+  }
+  EMFKACSolver(const EMFKACSolver&) = delete;
+  EMFKACSolver& operator=(const EMFKACSolver&) = delete;
+  ~EMFKACSolver() {
+    if (ctx_) pdds_destroy(ctx_);
+  }
+
+  pdds_estimate_desc options;  // mode, seed, instance, dup_sum, want_var, ipsi_override, ...
+  int32_t knot_id = 0;         // Philox knot word of the knot
+
+  void Solve_GPU_Analytic(std::array<double, 2> X0, unsigned int N_tray, double time_discretization, double rho,
+                          const pdds_problem_desc& BoundaryValueProblem, Stencil& stencil_knot, double c2,
+                          std::vector<double>& G, std::vector<double>& G_var, std::vector<int>& G_j, double& B,
+                          double& BB) {
+    (void)rho;
+    (void)c2;
+    check(pdds_problem_set(ctx_, &BoundaryValueProblem), "pdds_problem_set");
+    pdds_estimate_desc d = options;
+    d.npaths = (int32_t)N_tray;
+    d.h = time_discretization;
+    const pdds_stencil_desc sd = stencil_knot.desc();
+    size_t cap = 1;
+    for (int q = 0; q < 4; q++) cap += stencil_knot.side_size(static_cast<direction>(q));
+    std::vector<int32_t> gj(cap);
+    G.assign(cap, 0.0);
+    G_var.assign(cap, 0.0);
+    int32_t nnz = 0;
+    check(pdds_estimate_knot(ctx_, stencil_knot.global_parameters, X0[0], X0[1], knot_id, &sd, &d, gj.data(),
+                             G.data(), G_var.data(), (int32_t)cap, &nnz, &B, &BB, &info_),
+          "pdds_estimate_knot");
+    G.resize(nnz);
+    G_var.resize(nnz);
+    G_j.assign(gj.begin(), gj.begin() + nnz);
+  }
+
+  const pdds_estimate_info& info() const { return info_; }
+
+ private:
+  void check(pdds_status s, const char* what) const {
+    if (s != PDDS_OK) throw Error(s, std::string(what) + ": " + pdds_last_error(ctx_));
+  }
+  pdds_ctx* ctx_ = nullptr;
+  pdds_estimate_info info_{};
 };
 
 }  // namespace pdds

@@ -6,7 +6,7 @@ reference's BVP / PDDSparseGM call surface.
 """
 from ._capi import (MODE_FP64, MODE_MIXED, MODE_REPLAY_FP64, SOLVE_BICGSTAB_FP64, SOLVE_GMRES_FP32_IR,
                     PDDSError)
-from .api import BVP, Batch, Estimate, Instance, PDDSparseGM, read_configuration
+from .api import BVP, Batch, EMFKACSolver, Estimate, Instance, PDDSparseGM, Stencil, read_configuration
 
-__all__ = ["BVP", "Batch", "Estimate", "Instance", "PDDSparseGM", "PDDSError", "read_configuration", "MODE_FP64", "MODE_MIXED",
+__all__ = ["BVP", "Batch", "EMFKACSolver", "Estimate", "Stencil", "Instance", "PDDSparseGM", "PDDSError", "read_configuration", "MODE_FP64", "MODE_MIXED",
            "MODE_REPLAY_FP64", "SOLVE_BICGSTAB_FP64", "SOLVE_GMRES_FP32_IR"]

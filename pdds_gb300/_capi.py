@@ -27,9 +27,12 @@ EXPORTS = [
     "pdds_layout_build", "pdds_layout_build_circle", "pdds_layout_knots", "pdds_layout_csr", "pdds_layout_stencil",
     "pdds_estimate", "pdds_estimate_knot_paths", "pdds_estimate_knot_steps", "pdds_autotune", "pdds_solve_interface",
     "pdds_subdomain_solve", "pdds_semilinear_tables", "pdds_batch_build", "pdds_batch_run", "pdds_batch_instance",
-    "pdds_solve_bicgstab_static",
+    "pdds_solve_bicgstab_static", "pdds_check_philox", "pdds_check_portable_math", "pdds_stencils_set",
+    "pdds_estimate_knot",
 ]
 STATIC_SOLVE_MAX_K = 131072
+PHILOX_PORTABLE, PHILOX_ROUND_KEYS = 0, 1
+FN_EXP, FN_LOG, FN_SIN, FN_COS, FN_BOX_MULLER_Z0, FN_BOX_MULLER_Z1 = range(6)
 
 
 class ProblemDesc(C.Structure):
@@ -62,6 +65,11 @@ class LayoutInfo(C.Structure):
                 ("nnz", C.c_int64), ("h2d_bytes", C.c_int64)]
 
 
+class StencilDesc(C.Structure):
+    _fields_ = [("rect", C.c_double * 4), ("n", C.c_int32 * 4), ("index", C.POINTER(C.c_int32) * 4),
+                ("x", C.POINTER(C.c_double) * 4), ("y", C.POINTER(C.c_double) * 4), ("c2", C.c_double * 4)]
+
+
 class EstimateDesc(C.Structure):
     _fields_ = [("mode", C.c_int32), ("npaths", C.c_int32), ("h", C.c_double), ("seed", C.c_uint64),
                 ("instance", C.c_uint32), ("dup_sum", C.c_int32), ("want_var", C.c_int32),
@@ -87,7 +95,7 @@ class TuneInfo(C.Structure):
 
 class SolveDesc(C.Structure):
     _fields_ = [("method", C.c_int32), ("restart", C.c_int32), ("max_iter", C.c_int32),
-                ("max_refine", C.c_int32), ("tol", C.c_double)]
+                ("max_refine", C.c_int32), ("tol", C.c_double), ("barrier_poll_limit", C.c_int32)]
 
 
 class SolveInfo(C.Structure):
@@ -145,6 +153,11 @@ def load(path: str = LIB_PATH):
     L.pdds_layout_stencil.argtypes = [vp, C.c_int32, dp, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                       C.POINTER(C.c_int32), C.c_int32]
     L.pdds_estimate.argtypes = [vp, C.POINTER(EstimateDesc), dp, dp, dp, dp, C.POINTER(EstimateInfo)]
+    i32p = C.POINTER(C.c_int32)
+    L.pdds_stencils_set.argtypes = [vp, dp, C.c_int32, dp, dp, i32p, C.POINTER(StencilDesc), C.POINTER(LayoutInfo)]
+    L.pdds_estimate_knot.argtypes = [vp, dp, C.c_double, C.c_double, C.c_int32, C.POINTER(StencilDesc),
+                                     C.POINTER(EstimateDesc), i32p, dp, dp, C.c_int32, i32p, dp, dp,
+                                     C.POINTER(EstimateInfo)]
     L.pdds_autotune.argtypes = [vp, C.POINTER(EstimateDesc), C.c_int32, C.POINTER(TuneInfo)]
     L.pdds_estimate_knot_steps.argtypes = [vp, C.POINTER(C.c_int64)]
     L.pdds_estimate_knot_paths.argtypes = [vp, C.POINTER(C.c_int32)]
@@ -156,6 +169,9 @@ def load(path: str = LIB_PATH):
                                       dp]
     L.pdds_solve_bicgstab_static.argtypes = [C.c_int, C.c_int32, C.c_int64, vp, vp, vp, vp, vp, C.c_double,
                                              C.c_int32, vp, C.POINTER(C.c_int32), dp, C.c_char_p, C.c_int32]
+    u32p = C.POINTER(C.c_uint32)
+    L.pdds_check_philox.argtypes = [C.c_int, C.c_int32, u32p, u32p, C.c_int32, u32p, C.c_char_p, C.c_int32]
+    L.pdds_check_portable_math.argtypes = [C.c_int, C.c_int32, dp, C.c_int32, dp, C.c_char_p, C.c_int32]
     for name in EXPORTS:
         if not hasattr(L, name):
             raise RuntimeError("missing export " + name)

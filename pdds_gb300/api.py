@@ -203,7 +203,7 @@ class PDDSparseGM:
     (the reference's c2[kind], Meshes/stencil.cpp:211-243)."""
 
     def __init__(self, sw=(-1.0, -1.0), ne=(1.0, 1.0), nsub: int = 4, nnode: int = 11,
-                 fac=(1.0, 1.0, 1.0, 1.0), device: int = 0, circle=None):
+                 fac=(1.0, 1.0, 1.0, 1.0), device: int = 0, circle=None, stencils=None):
         self._lib = capi.load()
         self._ctx = C.c_void_p()
         st = self._lib.pdds_create(C.byref(self._ctx), int(device), 0)
@@ -211,7 +211,22 @@ class PDDSparseGM:
             raise PDDSError(st, "pdds_create failed (device %d)" % device)
         self.device = device
         info = capi.LayoutInfo()
-        if circle is not None:
+        if stencils is not None:
+            domain, kx, ky, knot_id, sts = stencils
+            kx = np.ascontiguousarray(kx, np.float64)
+            ky = np.ascontiguousarray(ky, np.float64)
+            n = len(kx)
+            arr = (capi.StencilDesc * n)()
+            for i, st in enumerate(sts):
+                arr[i] = st.desc()
+            self._keep_stencils = list(sts)
+            dom = np.ascontiguousarray(domain, np.float64)
+            kid = None if knot_id is None else np.ascontiguousarray(knot_id, np.int32)
+            self._check(self._lib.pdds_stencils_set(self._ctx, _p(dom, C.c_double), n, _p(kx, C.c_double),
+                                                    _p(ky, C.c_double), None if kid is None else _p(kid, C.c_int32),
+                                                    arr, C.byref(info)))
+            sw, ne, nsub, fac = (dom[0], dom[1]), (dom[2], dom[3]), 0, (1.0, 1.0, 1.0, 1.0)
+        elif circle is not None:
             radius, nrings, nsectors, kappa = circle
             d = capi.CircleDesc()
             d.radius, d.nrings, d.nsectors, d.nnode = float(radius), int(nrings), int(nsectors), int(nnode)
@@ -252,6 +267,13 @@ class PDDSparseGM:
         sectors (MIXED mode, sigma = sqrt2 I problems); kappa[kind] scales
         the RBF shape to each side's knot spacing."""
         return cls(nnode=nnode, device=device, circle=(radius, nrings, nsectors, kappa))
+
+    @classmethod
+    def from_stencils(cls, domain, x, y, stencils, knot_id=None, device: int = 0):
+        """Knots at (x[i], y[i]) with caller-built stencils (Stencil objects)
+        in the problem's rectangle domain {x0, y0, x1, y1}; knot i draws the
+        Philox knot word knot_id[i] (default i)."""
+        return cls(device=device, stencils=(domain, x, y, knot_id, list(stencils)))
 
     @classmethod
     def from_configuration(cls, path: str, device: int = 0):
@@ -485,7 +507,7 @@ class PDDSparseGM:
                       bvp.u(self.x, self.y))
 
     def solve_interface(self, method: int = capi.SOLVE_GMRES_FP32_IR, tol: float = 1e-10,
-                        restart: int = 20, max_iter: int = 0, max_refine: int = 0):
+                        restart: int = 20, max_iter: int = 0, max_refine: int = 0, barrier_poll_limit: int = 0):
         """Solves (I + G) u = B for the last estimate; returns (u, info)."""
         d = capi.SolveDesc()
         d.method = int(method)
@@ -493,6 +515,7 @@ class PDDSparseGM:
         d.max_iter = int(max_iter)
         d.max_refine = int(max_refine)
         d.tol = float(tol)
+        d.barrier_poll_limit = int(barrier_poll_limit)
         u = np.zeros(self.K)
         info = capi.SolveInfo()
         self._check(self._lib.pdds_solve_interface(self._ctx, C.byref(d), _p(u, C.c_double), C.byref(info)))
@@ -504,6 +527,173 @@ class PDDSparseGM:
         est = self.estimate(bvp, npaths, h, mode=mode, seed=seed, **kw)
         u, sinfo = self.solve_interface(method=method, tol=tol)
         return u, est, sinfo
+
+
+_DIRS = ("N", "S", "E", "W")
+
+
+class Stencil:
+    """A knot's stencil as the reference's Stencil class holds it
+    (Meshes/stencil.hpp:13-98): the rectangle stencil_parameters
+    {x0, y0, x1, y1}, the problem's rectangle global_parameters, and per side
+    N, S, E, W the knot indices and positions (Init) and the RBF shape c2
+    (Compute_ipsi).  The library factorises the RBF matrices itself."""
+
+    def __init__(self, stencil_parameters=None, global_parameters=None):
+        self.stencil_parameters = None if stencil_parameters is None else tuple(float(v) for v in stencil_parameters)
+        self.global_parameters = None if global_parameters is None else tuple(float(v) for v in global_parameters)
+        self.index = {d: np.zeros(0, np.int32) for d in _DIRS}
+        self.x = {d: np.zeros(0) for d in _DIRS}
+        self.y = {d: np.zeros(0) for d in _DIRS}
+        self.c2 = {d: 1.0 for d in _DIRS}
+
+    def Init(self, s_index: dict, s_x: dict, s_y: dict, parameters):
+        """Stencil::Init (Meshes/stencil.cpp:11-85): side knot lists by
+        direction ('N', 'S', 'E', 'W'), given as the reference lists them (the
+        library drops consecutive repeats and keeps an index's last position)."""
+        self.stencil_parameters = tuple(float(v) for v in parameters)
+        for d in _DIRS:
+            self.index[d] = np.ascontiguousarray(s_index.get(d, ()), np.int32)
+            self.x[d] = np.ascontiguousarray(s_x.get(d, ()), np.float64)
+            self.y[d] = np.ascontiguousarray(s_y.get(d, ()), np.float64)
+        return self
+
+    def Compute_ipsi(self, c2):
+        """The RBF shape of each side (Stencil::Compute_ipsi with c2[4] in the
+        order N, S, E, W, or one value for every side)."""
+        vals = [float(c2)] * 4 if np.isscalar(c2) else [float(v) for v in c2]
+        self.c2 = dict(zip(_DIRS, vals))
+        return self
+
+    @classmethod
+    def of_knot(cls, pd: "PDDSparseGM", knot: int, maxn: int = 512):
+        """The stencil a built layout gives knot `knot` (positions from the
+        layout's knots, shapes from its fac)."""
+        rect, kinds, sides = pd.stencil(knot, maxn)
+        st = cls(rect, (pd.sw[0], pd.sw[1], pd.ne[0], pd.ne[1]))
+        for d, idx in zip(_DIRS, sides):
+            st.index[d] = np.ascontiguousarray(idx, np.int32)
+            st.x[d] = np.ascontiguousarray(pd.x[idx], np.float64)
+            st.y[d] = np.ascontiguousarray(pd.y[idx], np.float64)
+        for q, d in enumerate(_DIRS):
+            st.c2[d] = float(pd.fac[kinds[q]]) if kinds[q] >= 0 else 1.0
+        return st
+
+    def desc(self):
+        """The C descriptor (the arrays it points to stay owned by self)."""
+        if self.stencil_parameters is None:
+            raise ValueError("stencil rectangle not set (Init)")
+        d = capi.StencilDesc()
+        for q in range(4):
+            d.rect[q] = self.stencil_parameters[q]
+        for q, dd in enumerate(_DIRS):
+            n = len(self.index[dd])
+            if len(self.x[dd]) != n or len(self.y[dd]) != n:
+                raise ValueError("side %s: index, x and y differ in length" % dd)
+            d.n[q] = n
+            d.c2[q] = self.c2[dd]
+            if n:
+                d.index[q] = _p(self.index[dd], C.c_int32)
+                d.x[q] = _p(self.x[dd], C.c_double)
+                d.y[q] = _p(self.y[dd], C.c_double)
+        return d
+
+
+def _estimate_desc(mode, npaths, h, seed, instance, dup_sum, want_var, max_steps=0, adaptive_h=False,
+                   richardson=False, ipsi_override=None):
+    d = capi.EstimateDesc()
+    d.mode = int(mode)
+    d.npaths = int(npaths)
+    d.h = float(h)
+    d.seed = int(seed)
+    d.instance = int(instance)
+    d.dup_sum = int(bool(dup_sum))
+    d.want_var = int(bool(want_var))
+    d.max_steps = int(max_steps)
+    d.adaptive_h = int(bool(adaptive_h))
+    d.richardson = int(bool(richardson))
+    keep = None
+    if ipsi_override is not None:
+        keep = np.ascontiguousarray(ipsi_override, np.float64)
+        d.ipsi_override = _p(keep, C.c_double)
+        d.ipsi_override_len = keep.size
+    return d, keep
+
+
+class EMFKACSolver:
+    """The reference's per-knot Feynman-Kac solver
+    (Solvers/EMFKACSolver.hpp:711-729) on the GPU: one knot from any X0 with a
+    caller-built stencil.  Per-knot calls are too fine-grained to fill a GPU;
+    PDDSparseGM.estimate runs every knot of a layout at once."""
+
+    def __init__(self, device: int = 0):
+        self._lib = capi.load()
+        self._ctx = C.c_void_p()
+        st = self._lib.pdds_create(C.byref(self._ctx), int(device), 0)
+        if st != capi.OK:
+            raise PDDSError(st, "pdds_create failed (device %d)" % device)
+
+    def _check(self, st):
+        if st != capi.OK:
+            raise PDDSError(st, self._lib.pdds_last_error(self._ctx).decode())
+
+    def close(self):
+        if getattr(self, "_ctx", None) and self._ctx.value:
+            self._lib.pdds_destroy(self._ctx)
+            self._ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def Solve_GPU_Analytic(self, X0, N: int, h: float, rho: float, bvp: BVP, stencil: Stencil, c2: float = 0.0,
+                           mode: int = capi.MODE_FP64, seed: int = 1234, knot_id: int = 0, instance: int = 0,
+                           dup_sum: bool = False, want_var: bool = True, max_steps: int = 0,
+                           adaptive_h: bool = False, richardson: bool = False, ipsi_override=None):
+        """Solve_OMP_Analytic's outputs (G, G_var, G_j, B, BB) for the knot at
+        X0: N paths of step h in the stencil, G_j the sorted knot indices of
+        its sides.  rho and c2 are accepted for the reference's signature;
+        like its G_update, the side shapes come from the stencil.  knot_id is
+        the Philox knot word (a layout knot's index reproduces its stream in
+        PDDSparseGM.estimate)."""
+        del rho, c2
+        if bvp.kind == BVP.LUT and bvp.tables is not None:
+            coef, g, bounds = bvp.tables
+            ny, nx = g.shape
+            b = np.ascontiguousarray(bounds, np.float64)
+            self._check(self._lib.pdds_problem_set_lut(self._ctx, _p(coef, C.c_float), _p(g, C.c_float), nx, ny,
+                                                       _p(b, C.c_double)))
+        self._check(self._lib.pdds_problem_set(self._ctx, C.byref(bvp.desc())))
+        if stencil.global_parameters is None:
+            raise ValueError("stencil.global_parameters (the problem's rectangle) not set")
+        dom = np.ascontiguousarray(stencil.global_parameters, np.float64)
+        sd = stencil.desc()
+        ed, keep = _estimate_desc(mode, N, h, seed, instance, dup_sum, want_var, max_steps, adaptive_h, richardson,
+                                  ipsi_override)
+        cap = sum(len(stencil.index[d]) for d in _DIRS) + 1
+        gj = np.zeros(cap, np.int32)
+        G = np.zeros(cap)
+        Gv = np.zeros(cap)
+        nnz = C.c_int32()
+        B = C.c_double()
+        BB = C.c_double()
+        info = capi.EstimateInfo()
+        self._check(self._lib.pdds_estimate_knot(self._ctx, _p(dom, C.c_double), float(X0[0]), float(X0[1]),
+                                                 int(knot_id), C.byref(sd), C.byref(ed), _p(gj, C.c_int32),
+                                                 _p(G, C.c_double), _p(Gv, C.c_double), cap, C.byref(nnz),
+                                                 C.byref(B), C.byref(BB), C.byref(info)))
+        del keep
+        n = nnz.value
+        self.info = {f: getattr(info, f) for f, _ in capi.EstimateInfo._fields_}
+        return G[:n].copy(), Gv[:n].copy(), gj[:n].copy(), B.value, BB.value
 
 
 @dataclass

@@ -35,6 +35,7 @@ UNITS = {
     "layout.cpp": ["-x", "cu"],
     "layout_circle.cpp": ["-x", "cu"],
     "noalloc.cu": [],
+    "selfcheck.cu": ["-fmad=false"],
 }
 
 

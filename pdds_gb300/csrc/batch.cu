@@ -33,7 +33,7 @@ pdds_status enqueue_batch(pdds_ctx* ctx, const pdds_batch_run_desc* d, int clust
   if (st != PDDS_OK) return st;
   CK(launch_to_f32(ctx->G.p, ctx->sval32.p, nnz, s));
   ++*launches;
-  ClusterGmresArgs a;
+  ClusterGmresArgs a{};
   a.n_sys = n;
   a.sys_row0 = ctx->inst_knot0.p;
   a.K = K;

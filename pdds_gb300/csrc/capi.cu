@@ -197,6 +197,12 @@ pdds_status upload_layout(pdds_ctx* ctx) {
   d.knot_inst = ctx->is_batch ? ctx->knot_inst.p : nullptr;
   d.inst_knot0 = ctx->is_batch ? ctx->inst_knot0.p : nullptr;
   d.inst_p = ctx->is_batch ? ctx->inst_pd.p : nullptr;
+  d.knot_rng = nullptr;
+  if (!L.knot_rng.empty()) {
+    std::vector<int> kr(L.knot_rng.begin(), L.knot_rng.end());
+    CK(ctx->knot_rng.upload(kr, s));
+    d.knot_rng = ctx->knot_rng.p;
+  }
   ctx->tables_ready = false;
   return PDDS_OK;
 }
@@ -708,6 +714,81 @@ pdds_status pdds_layout_build_circle(pdds_ctx* ctx, const pdds_circle_desc* desc
   return PDDS_OK;
 }
 
+pdds_status pdds_stencils_set(pdds_ctx* ctx, const double domain[4], int32_t nknots, const double* x,
+                              const double* y, const int32_t* knot_id, const pdds_stencil_desc* st,
+                              pdds_layout_info* info) {
+  if (!ctx || !domain || !x || !y || !st || nknots < 1) return fail(ctx, PDDS_ERR_INVALID, "invalid arguments");
+  if (ctx->device >= 0) {
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  drop_graph(ctx);
+  clear_tune(ctx);
+  ctx->is_batch = false;
+  ctx->n_inst = 0;
+  ctx->has_batch_run = false;
+  std::vector<CustomStencil> cs((size_t)nknots);
+  for (int k = 0; k < nknots; k++) {
+    for (int q = 0; q < 4; q++) {
+      cs[k].rect[q] = st[k].rect[q];
+      cs[k].n[q] = st[k].n[q];
+      cs[k].index[q] = st[k].index[q];
+      cs[k].x[q] = st[k].x[q];
+      cs[k].y[q] = st[k].y[q];
+      cs[k].c2[q] = st[k].c2[q];
+    }
+  }
+  const std::string e = build_custom_layout(ctx->L, domain, nknots, x, y, knot_id, cs.data(), ctx->bins);
+  if (!e.empty()) {
+    ctx->has_layout = false;
+    ctx->has_estimate = false;
+    return fail(ctx, PDDS_ERR_INVALID, e);
+  }
+  ctx->has_layout = true;
+  ctx->has_estimate = false;
+  const int64_t h2d0 = xfer().h2d;
+  if (ctx->device >= 0) {
+    pdds_status s = upload_layout(ctx);
+    if (s != PDDS_OK) return s;
+  }
+  if (info) {
+    info->h2d_bytes = xfer().h2d - h2d0;
+    info->nknots = ctx->L.K;
+    info->nboundary = ctx->L.nboundary;
+    info->nstencils = (int)ctx->L.stencils.size();
+    info->nsides = (int)ctx->L.sides.size();
+    info->nshapes = (int)ctx->L.shapes.size();
+    info->max_side = ctx->L.max_side;
+    info->nnz = ctx->L.row_ptr[ctx->L.K];
+  }
+  return PDDS_OK;
+}
+
+pdds_status pdds_estimate_knot(pdds_ctx* ctx, const double domain[4], double x0, double y0, int32_t knot_id,
+                               const pdds_stencil_desc* st, const pdds_estimate_desc* desc, int32_t* G_j,
+                               double* G, double* G_var, int32_t max_nnz, int32_t* nnz, double* B, double* BB,
+                               pdds_estimate_info* info) {
+  if (!ctx || !desc || !st || !nnz || max_nnz < 0 || knot_id < 0)
+    return fail(ctx, PDDS_ERR_INVALID, "invalid arguments");
+  pdds_status s = pdds_stencils_set(ctx, domain, 1, &x0, &y0, &knot_id, st, nullptr);
+  if (s != PDDS_OK) return s;
+  const int64_t len = ctx->L.row_ptr[1];
+  *nnz = (int32_t)len;
+  if (len > max_nnz) return fail(ctx, PDDS_ERR_INVALID, "G row longer than max_nnz (see *nnz)");
+  std::vector<double> val(std::max<int64_t>(len, 1)), var(std::max<int64_t>(len, 1));
+  double b = 0.0, bb = 0.0;
+  s = pdds_estimate(ctx, desc, val.data(), G_var ? var.data() : nullptr, &b, &bb, info);
+  if (s != PDDS_OK) return s;
+  if (G_j && len > 0) layout_csr_cols(ctx->L, G_j);
+  for (int64_t e = 0; e < len; e++) {
+    if (G) G[e] = val[e];
+    if (G_var) G_var[e] = var[e];
+  }
+  if (B) *B = b;
+  if (BB) *BB = bb;
+  return PDDS_OK;
+}
+
 pdds_status pdds_layout_knots(pdds_ctx* ctx, double* x, double* y, int32_t* order) {
   if (!ctx || !ctx->has_layout) return fail(ctx, PDDS_ERR_INVALID, "no layout");
   const HostLayout& L = ctx->L;
@@ -1106,7 +1187,7 @@ pdds_status pdds_autotune(pdds_ctx* ctx, const pdds_estimate_desc* desc, int32_t
 pdds_status pdds_subdomain_solve(pdds_ctx* ctx, int32_t m, const double* u, double* out) {
   if (!ctx || !out) return PDDS_ERR_INVALID;
   if (ctx->device < 0) return fail(ctx, PDDS_ERR_INVALID, "context has no device");
-  if (!ctx->has_layout || ctx->L.geom != 0 || ctx->is_batch)
+  if (!ctx->has_layout || ctx->L.geom != 0 || ctx->is_batch || ctx->L.custom)
     return fail(ctx, PDDS_ERR_INVALID, "subdomain solves need a rectangular layout");
   if (!ctx->has_problem) return fail(ctx, PDDS_ERR_INVALID, "no problem set");
   const int kind = ctx->prob.kind;
@@ -1178,7 +1259,7 @@ pdds_status pdds_subdomain_solve(pdds_ctx* ctx, int32_t m, const double* u, doub
 pdds_status pdds_semilinear_tables(pdds_ctx* ctx, const pdds_semilinear_desc* desc) {
   if (!ctx || !desc) return PDDS_ERR_INVALID;
   if (ctx->device < 0) return fail(ctx, PDDS_ERR_INVALID, "context has no device");
-  if (!ctx->has_layout || ctx->L.geom != 0 || ctx->is_batch)
+  if (!ctx->has_layout || ctx->L.geom != 0 || ctx->is_batch || ctx->L.custom)
     return fail(ctx, PDDS_ERR_INVALID, "the semilinear step needs a rectangular layout");
   const HostLayout& L = ctx->L;
   if (desc->equation != PDDS_OUTER_NEWTON_U3 && desc->equation != PDDS_OUTER_LINEAR_SHIFT)
@@ -1250,6 +1331,9 @@ pdds_status pdds_solve_interface(pdds_ctx* ctx, const pdds_solve_desc* desc, dou
                                  pdds_solve_info* info) {
   if (!ctx || !desc) return PDDS_ERR_INVALID;
   if (!ctx->has_estimate) return fail(ctx, PDDS_ERR_INVALID, "no estimate to solve");
+  if (ctx->L.custom && ctx->L.max_col >= ctx->L.K)
+    return fail(ctx, PDDS_ERR_INVALID, "G has columns outside the layout's knots (column " +
+                                           std::to_string(ctx->L.max_col) + "): the system is not square");
   CK(cudaSetDevice(ctx->device));
   cudaStream_t s = ctx->stream;
   const HostLayout& L = ctx->L;
@@ -1268,8 +1352,10 @@ pdds_status pdds_solve_interface(pdds_ctx* ctx, const pdds_solve_desc* desc, dou
   CK(ctx->sbar.resize(2));
   CK(ctx->su.resize(std::max(K, 1)));
   SolveCsr A{K, nnz, ctx->row_ptr.p, ctx->col.p, ctx->G.p};
-  SolveWork w;
+  if (desc->barrier_poll_limit < 0) return fail(ctx, PDDS_ERR_INVALID, "barrier_poll_limit must be >= 0");
+  SolveWork w{};
   w.err = ctx->errf.p;
+  w.spin_limit = (unsigned)desc->barrier_poll_limit;
   CK(cudaMemsetAsync(ctx->errf.p, 0, sizeof(unsigned), s));
   for (int q = 0; q < 6; q++) w.v64[q] = ctx->sv64.p + (size_t)q * K;
   w.scal = ctx->sscal.p;

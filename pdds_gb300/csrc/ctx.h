@@ -69,6 +69,7 @@ struct pdds_ctx {
   DBuf<int> rbf_piv;
   DBuf<int64_t> row_ptr, st_map_off, sd_knot_off, sh_tab_off, sh_ipsi_off, sh_t_off;
   DBuf<unsigned char> map_owner;
+  DBuf<int> knot_rng;             // Philox knot word per knot (caller-built stencils)
   DBuf<float> tab;
   DevLayout dl{};
   int n_mc = 0, n_bnd = 0;

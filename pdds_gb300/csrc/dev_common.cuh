@@ -59,7 +59,15 @@ struct DevLayout {
   const int* knot_inst;
   const int* inst_knot0;
   const double* inst_p;
+  // Philox knot word of each knot (null: the knot's own index); set for
+  // layouts built from caller stencils, whose knots carry the caller's ids
+  const int* knot_rng;
 };
+
+// Philox knot word of knot k outside batches.
+__device__ __forceinline__ uint32_t knot_word(const DevLayout& L, int k) {
+  return L.knot_rng ? (uint32_t)L.knot_rng[k] : (uint32_t)k;
+}
 
 // Coefficient tables of the PK_LUT problem: node (i, j) of an nx x ny grid
 // over [x0, x0 + (nx-1) dx] x [y0, y0 + (ny-1) dy] holds two float4,
@@ -91,7 +99,7 @@ __device__ __forceinline__ void instance_params(const DevLayout& L, int k, Probl
     rng_inst += (uint32_t)i;
     rng_knot = (uint32_t)(k - L.inst_knot0[i]);
   } else {
-    rng_knot = (uint32_t)k;
+    rng_knot = knot_word(L, k);
   }
 }
 

@@ -159,6 +159,11 @@ k_paths_fp64(const Fp64Args a) {
     // or radius on polar stencils), projection (Ex, Ey)
     auto exit_level = [&](const Lvl64& s, double wgt, double Ex, double Ey, int d, bool glob,
                           double along) -> double {
+      if (isnan(s.x) || isnan(s.y)) {
+        // a position that is not a number lies on no side: reported, scores nothing
+        atomicOr(a.err_flags, ERR_FLAG_EXIT_SIDE);
+        return 0.0;
+      }
       if (glob) {
         ++nglob;
         return s.Z + s.Y * u_f64<KIND>(a.P, Ex, Ey) + s.xi;
@@ -317,13 +322,13 @@ k_paths_fp64(const Fp64Args a) {
         bool fin = false;  // the lane's path (pair) finished in this iteration
         if (RICH) {
           const unsigned mi = m++;
-          blk = path_block(a.seed, a.instance, (uint32_t)knot, path, mi);
+          blk = path_block(a.seed, a.instance, knot_word(a.L, knot), path, mi);
           double za0, za1, zb0, zb1;
           normals_f64(blk.v[0], blk.v[1], za0, za1);
           normals_f64(blk.v[2], blk.v[3], zb0, zb1);
           double x0e = 0.0, x1e = 0.0, x2e = 0.0;  // Exp(1) samples of reflected steps
           if (KIND == PK_ROBIN && rmask) {
-            const u32x4 bx = path_block(a.seed, a.instance, (uint32_t)knot | 0x80000000u, path, mi);
+            const u32x4 bx = path_block(a.seed, a.instance, knot_word(a.L, knot) | 0x80000000u, path, mi);
             x0e = -::log(u01_fp64(bx.v[0]));
             x1e = -::log(u01_fp64(bx.v[1]));
             x2e = -::log(u01_fp64(bx.v[2]));
@@ -342,13 +347,13 @@ k_paths_fp64(const Fp64Args a) {
             fin = true;
           }
         } else {
-          if ((m & 1u) == 0) blk = path_block(a.seed, a.instance, (uint32_t)knot, path, m >> 1);
+          if ((m & 1u) == 0) blk = path_block(a.seed, a.instance, knot_word(a.L, knot), path, m >> 1);
           double z0, z1;
           if (m & 1u) normals_f64(blk.v[2], blk.v[3], z0, z1);
           else normals_f64(blk.v[0], blk.v[1], z0, z1);
           double xe = 0.0;
           if (KIND == PK_ROBIN && rmask) {
-            const u32x4 bx = path_block(a.seed, a.instance, (uint32_t)knot | 0x80000000u, path, m >> 1);
+            const u32x4 bx = path_block(a.seed, a.instance, knot_word(a.L, knot) | 0x80000000u, path, m >> 1);
             xe = -::log(u01_fp64(bx.v[m & 1u]));
           }
           ++m;

@@ -134,6 +134,7 @@ struct GridGroup {
   unsigned* count;  // arrivals since the launch
   unsigned* err;    // ERR_FLAG_TIMEOUT on a wait that ran out
   double* gpart;    // [2][gridDim.x][CG_MAXV + 2] published partials
+  unsigned limit;   // polls before a wait gives up
   __device__ unsigned rank() const { return blockIdx.x; }
   __device__ unsigned size() const { return gridDim.x; }
   __device__ int system() const { return 0; }
@@ -149,7 +150,7 @@ struct GridGroup {
       for (;;) {
         asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(count) : "memory");
         if ((int)(cur - target) >= 0) break;
-        if (++spins > GRID_SPIN_LIMIT) {
+        if (++spins > limit) {
           atomicOr(err, ERR_FLAG_TIMEOUT);
           ok = 0;
           break;
@@ -464,7 +465,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_gmres_cluster(const ClusterGm
 // One system over the whole grid (cooperative launch, one CTA per SM).
 __global__ void __launch_bounds__(CG_THREADS, 1) k_gmres_grid(const ClusterGmresArgs a, unsigned* bar,
                                                               unsigned* err, double* gpart) {
-  GridGroup grp{bar, err, gpart};
+  GridGroup grp{bar, err, gpart, a.spin_limit ? a.spin_limit : GRID_SPIN_LIMIT};
   gmres_body(a, grp);
 }
 

@@ -404,6 +404,13 @@ k_paths_mixed(const MixedArgs a) {
           val = 0.f;
         }
       }
+      if (ok && (isnan(x) || isnan(y))) {
+        // a position that is not a number lies on no side (the reference's
+        // G_update stops there): reported, and the pair scores nothing
+        atomicOr(a.err_flags, ERR_FLAG_EXIT_SIDE);
+        ok = false;
+        val = 0.f;
+      }
       if (ok && GEOM == 1) {
         // polar stencil: the side with the largest outside distance (ties
         // S, N, W, E); arcs are parameterised by the angle (measured from
@@ -729,6 +736,25 @@ static cudaError_t launch_mixed_t(const MixedArgs& a, int kind, int grid, int th
     }
   }
 #undef PDDS_MIXED_CASE
+  return cudaGetLastError();
+}
+
+// Known-answer check of path_block_rk, the generator form of the MIXED path
+// kernel: block i of out is the Philox-4x32-10 output for the counter
+// ctr[4i..4i+3] = (step pair, path, knot, instance) under the key schedule
+// rk of one key, exactly as the path kernel calls it.
+__global__ void k_philox_rk_check(const MixedArgs a, const uint32_t* __restrict__ ctr, int n,
+                                  uint32_t* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const u32x4 b = path_block_rk(a.rk, ctr[4 * i + 3], ctr[4 * i + 2], ctr[4 * i + 1], ctr[4 * i]);
+  for (int q = 0; q < 4; q++) out[4 * i + q] = b.v[q];
+}
+
+cudaError_t launch_philox_rk_check(uint64_t key, const uint32_t* ctr, int n, uint32_t* out, cudaStream_t s) {
+  MixedArgs a{};
+  mixed_set_rng(a, key, 0);
+  if (n > 0) k_philox_rk_check<<<(n + 127) / 128, 128, 0, s>>>(a, ctr, n, out);
   return cudaGetLastError();
 }
 

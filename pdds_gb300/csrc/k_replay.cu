@@ -157,7 +157,7 @@ __global__ void k_replay_paths(const ReplayArgs a) {
   }
   ps.seed = a.seed;
   ps.inst = a.instance;
-  ps.knot = (uint32_t)knot;
+  ps.knot = knot_word(a.L, knot);
   ps.path = (uint32_t)n;
   ps.step = 0;
   ps.blk.v[0] = ps.blk.v[1] = ps.blk.v[2] = ps.blk.v[3] = 0;
@@ -180,7 +180,8 @@ __global__ void k_replay_paths(const ReplayArgs a) {
     double E0, E1, Nx, Ny;
     int onm;
     const double gd = rect2d<double>(L.dom, ex, ey, E0, E1, Nx, Ny, onm);
-    if (gd >= -1e-08) side = -1;
+    if (isnan(ps.X0) || isnan(ps.X1)) side = -2;  // a position that is not a number lies on no side
+    else if (gd >= -1e-08) side = -1;
     else if (fabs(ey - sp[1]) < 1e-8) side = DIR_S_;
     else if (fabs(ey - sp[3]) < 1e-8) side = DIR_N_;
     else if (fabs(ex - sp[0]) < 1e-8) side = DIR_W_;

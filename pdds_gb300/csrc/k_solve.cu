@@ -542,7 +542,7 @@ cudaError_t solve_gmres_ir_cluster(const SolveCsr& A, const double* b, double* x
   k_to_f32<<<vgrid((int)std::min<int64_t>(A.nnz, 1 << 28)), 256, 0, s>>>(A.nnz, A.val64, w.val32);
   ++w.launches;
   k_cl_single_rows<<<1, 1, 0, s>>>(ctl, n);
-  ClusterGmresArgs a;
+  ClusterGmresArgs a{};
   a.n_sys = 1;
   a.sys_row0 = ctl;
   a.K = n;
@@ -563,6 +563,7 @@ cudaError_t solve_gmres_ir_cluster(const SolveCsr& A, const double* b, double* x
   a.out_refines = ctl + 3;
   a.out_relres = w.scal;
   a.out_t_end = nullptr;
+  a.spin_limit = w.spin_limit;
   ++w.launches;
   cudaError_t e = gb > 0 ? launch_gmres_grid(a, gb, n, w.bar, w.err, w.gpart, s) : launch_gmres_cluster(a, cl, n, s);
   if (e != cudaSuccess) return e;

@@ -115,6 +115,14 @@ size_t mixed_queue_smem(int threads, int richardson);
 cudaError_t launch_lpt_order(const int* mc, int n, const unsigned long long* steps, int* out, cudaStream_t s);
 // Sets the Philox key schedule (rk) of `seed` and the instance word.
 void mixed_set_rng(MixedArgs& a, uint64_t seed, uint32_t instance);
+// out[4i..4i+3] = the MIXED kernel's Philox block for counter ctr[4i..4i+3]
+// and the 64-bit key (low word first), device arrays.
+cudaError_t launch_philox_rk_check(uint64_t key, const uint32_t* ctr, int n, uint32_t* out, cudaStream_t s);
+// The portable Philox (form 0) and FP64 functions (selfcheck.cu).
+cudaError_t launch_philox_check(const uint32_t* ctr, const uint32_t* key, int n, uint32_t* out, cudaStream_t s);
+cudaError_t launch_portable_math_check(int fn, const double* x, int n, double* out, cudaStream_t s);
+void philox_check_host(const uint32_t* ctr, const uint32_t* key, int n, uint32_t* out);
+void portable_math_check_host(int fn, const double* x, int n, double* out);
 // True when `func` is one of the MIXED path kernels (a captured graph's
 // nodes are re-keyed with a new seed through their parameters).
 bool is_mixed_path_kernel(const void* func);

@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <climits>
 #include <cstdint>
+#include <cstring>
 #include <cmath>
 #include <map>
 #include <string>
@@ -105,11 +106,22 @@ double rect_dist(const double* p, double x, double y) {
 
 }  // namespace
 
+// Knot spacing of a side from its local coordinates: the first gap, or the
+// mean spacing when the first two knots coincide (caller-built stencils),
+// 1 for a single knot.
+double side_gap(const std::vector<double>& t) {
+  const size_t n = t.size();
+  if (n < 2) return 1.0;
+  if (t[1] - t[0] > 0.0) return t[1] - t[0];
+  const double mean = (t[n - 1] - t[0]) / (double)(n - 1);
+  return mean > 0.0 ? mean : 1.0;
+}
+
 void set_shape_bins(HostLayout& L, int bps) {
   if (bps <= 0) bps = 16;
   int64_t tab = 0;
   for (auto& sh : L.shapes) {
-    const double gap = (sh.n > 1) ? (sh.t[1] - sh.t[0]) : 1.0;
+    const double gap = side_gap(sh.t);
     sh.delta = gap / bps;
     const int inner = (int)std::ceil((sh.hi - sh.lo) / sh.delta - 1e-9);
     sh.nbins = inner + 4;  // grid covers [lo - delta, hi + 2 delta]
@@ -117,6 +129,72 @@ void set_shape_bins(HostLayout& L, int bps) {
     tab += (int64_t)sh.nbins * sh.n;
   }
 }
+
+// Derived parts of a layout whose knots, stencils and sides are set:
+// boundary knots (Solve_OMP_Analytic: |dist| <= 1e-8 -> B = g, no row), row
+// offsets of G, side shapes (translates with equal knot spacing, size, c and
+// exit extent share one) with their inverse and table offsets and bin grids.
+void finish_layout(HostLayout& L, const double gparams[4], int bps) {
+  L.row_ptr.assign(L.K + 1, 0);
+  for (int v = 0; v < L.K; v++) {
+    L.knot_boundary[v] = !(std::fabs(rect_dist(gparams, L.kx[v], L.ky[v])) > 1e-08);
+    L.nboundary += L.knot_boundary[v];
+    const int len = L.knot_boundary[v] ? 0 : L.stencils[L.knot_stencil[v]].row_len;
+    L.row_ptr[v + 1] = L.row_ptr[v] + len;
+  }
+  // side shapes: translates with equal knot spacing, size, c and exit extent
+  std::map<std::tuple<int, long long, long long, long long, long long>, int> shape_key;
+  std::vector<std::vector<std::pair<int, int>>> uses(L.sides.size());  // (stencil, dir)
+  for (size_t s = 0; s < L.stencils.size(); s++)
+    for (int d = 0; d < 4; d++)
+      if (L.stencils[s].side[d] >= 0) uses[L.stencils[s].side[d]].push_back({(int)s, d});
+  for (size_t sd = 0; sd < L.sides.size(); sd++) {
+    SideRec& sr = L.sides[sd];
+    std::vector<double> t(sr.n);
+    const double* crd = (sr.orient == 0) ? &L.side_px[sr.knot_off] : &L.side_py[sr.knot_off];
+    for (int q = 0; q < sr.n; q++) t[q] = crd[q] - sr.origin;
+    const double gap = side_gap(t);
+    bool uniform = sr.n < 2 || t[1] - t[0] > 0.0;
+    for (int q = 0; q < sr.n; q++)
+      if (std::fabs(t[q] - q * gap) > 1e-9 * (1.0 + std::fabs(t[q]))) uniform = false;
+    double lo = 1e300, hi = -1e300;
+    for (auto& u : uses[sd]) {
+      const StencilRec& st = L.stencils[u.first];
+      const double a = (sr.orient == 0) ? st.rect[0] : st.rect[1];
+      const double b = (sr.orient == 0) ? st.rect[2] : st.rect[3];
+      lo = std::min(lo, a - sr.origin);
+      hi = std::max(hi, b - sr.origin);
+    }
+    auto key = std::make_tuple(sr.n, (long long)std::llround(gap * 1e12),
+                               (long long)std::llround(sr.c * 1e12),
+                               (long long)std::llround(lo / gap * 1e6),
+                               uniform ? (long long)std::llround(hi / gap * 1e6) : -1 - (long long)sd);
+    auto it = shape_key.find(key);
+    if (it == shape_key.end()) {
+      ShapeRec sh;
+      sh.n = sr.n;
+      sh.c = sr.c;
+      sh.t = t;
+      sh.lo = lo;
+      sh.hi = hi;
+      shape_key[key] = (int)L.shapes.size();
+      sr.shape = (int)L.shapes.size();
+      L.shapes.push_back(sh);
+    } else {
+      sr.shape = it->second;
+      ShapeRec& sh = L.shapes[it->second];
+      sh.lo = std::min(sh.lo, lo);
+      sh.hi = std::max(sh.hi, hi);
+    }
+  }
+  int64_t ip = 0;
+  for (auto& sh : L.shapes) {
+    sh.ipsi_off = ip;
+    ip += (int64_t)sh.n * sh.n;
+  }
+  set_shape_bins(L, bps);
+}
+
 
 std::string build_rect_layout(HostLayout& L, const double sw[2], const double ne[2], int nsub,
                               int nnode, const double fac[4], int bps, int max_threads) {
@@ -442,65 +520,152 @@ std::string build_rect_layout(HostLayout& L, const double sw[2], const double ne
     L.map_owner.insert(L.map_owner.end(), W.map_owner.begin(), W.map_owner.end());
     L.stencils.push_back(std::move(st));
   }
-  // boundary knots (Solve_OMP_Analytic: |dist| <= 1e-8 -> B = g, no row)
-  L.row_ptr.assign(L.K + 1, 0);
-  for (int v = 0; v < L.K; v++) {
-    L.knot_boundary[v] = !(std::fabs(rect_dist(gparams, L.kx[v], L.ky[v])) > 1e-08);
-    L.nboundary += L.knot_boundary[v];
-    const int len = L.knot_boundary[v] ? 0 : L.stencils[L.knot_stencil[v]].row_len;
-    L.row_ptr[v + 1] = L.row_ptr[v] + len;
+  finish_layout(L, gparams, bps);
+  return "";
+}
+
+std::string build_custom_layout(HostLayout& L, const double domain[4], int nknots, const double* x,
+                                const double* y, const int32_t* knot_id, const CustomStencil* cst, int bps) {
+  if (nknots < 1 || !x || !y || !cst) return "stencils need nknots >= 1 and knot positions";
+  if (!(domain[2] > domain[0] && domain[3] > domain[1])) return "domain needs x1 > x0 and y1 > y0";
+  L = HostLayout();
+  L.custom = true;
+  L.sw[0] = domain[0];
+  L.sw[1] = domain[1];
+  L.ne[0] = domain[2];
+  L.ne[1] = domain[3];
+  for (int q = 0; q < 4; q++) L.fac[q] = 0.0;
+  L.K = nknots;
+  L.kx.assign(x, x + nknots);
+  L.ky.assign(y, y + nknots);
+  L.order.resize(nknots);
+  L.knot_stencil.resize(nknots);
+  L.knot_boundary.assign(nknots, 0);
+  for (int i = 0; i < nknots; i++) {
+    L.order[i] = i;
+    L.knot_stencil[i] = i;
+    if (knot_id && knot_id[i] < 0) return "knot ids must be >= 0";
   }
-  // side shapes: translates with equal knot spacing, size, c and exit extent
-  std::map<std::tuple<int, long long, long long, long long, long long>, int> shape_key;
-  std::vector<std::vector<std::pair<int, int>>> uses(L.sides.size());  // (stencil, dir)
-  for (size_t s = 0; s < L.stencils.size(); s++)
+  if (knot_id) L.knot_rng.assign(knot_id, knot_id + nknots);
+  const double* gparams = domain;
+  struct SideKeyHash {
+    size_t operator()(const std::pair<std::vector<double>, std::vector<int>>& k) const {
+      uint64_t h = 1469598103934665603ull;
+      for (double v : k.first) {
+        uint64_t b;
+        std::memcpy(&b, &v, sizeof b);
+        h = (h ^ b) * 1099511628211ull;
+      }
+      for (int v : k.second) h = (h ^ (uint64_t)(uint32_t)v) * 1099511628211ull;
+      return (size_t)h;
+    }
+  };
+  // identical sides (same shape c, knot list and positions) share one record
+  std::unordered_map<std::pair<std::vector<double>, std::vector<int>>, int, SideKeyHash> side_key;
+  std::map<int, int> lastq, last_writer;
+  std::map<int, double> posx, posy;
+  for (int k = 0; k < nknots; k++) {
+    const CustomStencil& cs = cst[k];
+    const std::string at = "stencil " + std::to_string(k) + ": ";
+    if (!(cs.rect[2] > cs.rect[0] && cs.rect[3] > cs.rect[1])) return at + "rect needs x1 > x0 and y1 > y0";
+    StencilRec st;
+    for (int q = 0; q < 4; q++) st.rect[q] = cs.rect[q];
+    std::vector<int> idx[4];
+    std::vector<double> px[4], py[4];
+    for (int d = 0; d < 4; d++) {
+      st.side[d] = -1;
+      st.kind[d] = -3;
+      if (cs.n[d] < 0) return at + "negative side size";
+      if (cs.n[d] == 0) continue;
+      if (!cs.index[d] || !cs.x[d] || !cs.y[d]) return at + "side arrays missing";
+      if (!(cs.c2[d] > 0.0)) return at + "RBF shape c2 must be positive";
+      // Stencil::Init: a repeated index keeps its last position, consecutive
+      // repeats are dropped
+      posx.clear();
+      posy.clear();
+      for (int q = 0; q < cs.n[d]; q++) {
+        if (cs.index[d][q] < 0) return at + "knot indices must be >= 0";
+        posx[cs.index[d][q]] = cs.x[d][q];
+        posy[cs.index[d][q]] = cs.y[d][q];
+        idx[d].push_back(cs.index[d][q]);
+      }
+      idx[d].erase(std::unique(idx[d].begin(), idx[d].end()), idx[d].end());
+      for (int v : idx[d]) {
+        px[d].push_back(posx[v]);
+        py[d].push_back(posy[v]);
+      }
+      // the binned exit weights of the MIXED form take the side's knots on
+      // the side's line, in increasing order along it
+      const bool horiz = (d == DIR_N || d == DIR_S);
+      const double line = horiz ? (d == DIR_N ? cs.rect[3] : cs.rect[1]) : (d == DIR_E ? cs.rect[2] : cs.rect[0]);
+      const double tol = 1e-9 * (1.0 + std::fabs(line));
+      for (size_t q = 0; q < idx[d].size(); q++) {
+        const double off = horiz ? py[d][q] : px[d][q];
+        if (std::fabs(off - line) > tol) return at + "a side knot does not lie on its side of the rectangle";
+        if (q > 0 && (horiz ? px[d][q] < px[d][q - 1] : py[d][q] < py[d][q - 1]))
+          return at + "side knots must be in increasing order along the side";
+      }
+      if ((int)idx[d].size() > 160) return at + "stencil side larger than 160 knots";
+      st.kind[d] = 0;
+    }
+    {
+      const double mx = 0.5 * (st.rect[0] + st.rect[2]), my = 0.5 * (st.rect[1] + st.rect[3]);
+      st.glob[DIR_N] = rect_dist(gparams, mx, st.rect[3]) >= -1e-08;
+      st.glob[DIR_S] = rect_dist(gparams, mx, st.rect[1]) >= -1e-08;
+      st.glob[DIR_E] = rect_dist(gparams, st.rect[2], my) >= -1e-08;
+      st.glob[DIR_W] = rect_dist(gparams, st.rect[0], my) >= -1e-08;
+    }
+    std::vector<int32_t>& cols = st.cols;
+    for (int d = 0; d < 4; d++) cols.insert(cols.end(), idx[d].begin(), idx[d].end());
+    std::sort(cols.begin(), cols.end());
+    cols.erase(std::unique(cols.begin(), cols.end()), cols.end());
+    st.row_len = (int)cols.size();
+    if (!cols.empty()) L.max_col = std::max(L.max_col, cols.back());
+    // row positions of the (side, knot) entries, sides N, S, E, W; the last
+    // side that lists a knot owns its entry (G_return_withrep)
+    st.map_off = (int64_t)L.map_pos.size();
     for (int d = 0; d < 4; d++)
-      if (L.stencils[s].side[d] >= 0) uses[L.stencils[s].side[d]].push_back({(int)s, d});
-  for (size_t sd = 0; sd < L.sides.size(); sd++) {
-    SideRec& sr = L.sides[sd];
-    std::vector<double> t(sr.n);
-    const double* crd = (sr.orient == 0) ? &L.side_px[sr.knot_off] : &L.side_py[sr.knot_off];
-    for (int q = 0; q < sr.n; q++) t[q] = crd[q] - sr.origin;
-    const double gap = sr.n > 1 ? t[1] - t[0] : 1.0;
-    bool uniform = true;
-    for (int q = 0; q < sr.n; q++)
-      if (std::fabs(t[q] - q * gap) > 1e-9 * (1.0 + std::fabs(t[q]))) uniform = false;
-    double lo = 1e300, hi = -1e300;
-    for (auto& u : uses[sd]) {
-      const StencilRec& st = L.stencils[u.first];
-      const double a = (sr.orient == 0) ? st.rect[0] : st.rect[1];
-      const double b = (sr.orient == 0) ? st.rect[2] : st.rect[3];
-      lo = std::min(lo, a - sr.origin);
-      hi = std::max(hi, b - sr.origin);
+      for (int v : idx[d]) {
+        last_writer[v] = (int)L.map_pos.size();
+        L.map_pos.push_back((int32_t)(std::lower_bound(cols.begin(), cols.end(), v) - cols.begin()));
+        L.map_owner.push_back(0);
+      }
+    for (auto& lw : last_writer) L.map_owner[lw.second] = 1;
+    last_writer.clear();
+    for (int d = 0; d < 4; d++) {
+      if (idx[d].empty()) continue;
+      // (the positions fix the orientation: an N side of one stencil and
+      // the S side of the next share their record, as built layouts do)
+      std::vector<double> pk;
+      pk.push_back(cs.c2[d]);
+      pk.insert(pk.end(), px[d].begin(), px[d].end());
+      pk.insert(pk.end(), py[d].begin(), py[d].end());
+      auto key = std::make_pair(std::move(pk), idx[d]);
+      auto it = side_key.find(key);
+      if (it != side_key.end()) {
+        st.side[d] = it->second;
+        continue;
+      }
+      SideRec sr;
+      sr.n = (int)idx[d].size();
+      sr.orient = (d == DIR_N || d == DIR_S) ? 0 : 1;
+      sr.kind = 0;
+      sr.c = cs.c2[d];
+      sr.shape = -1;
+      sr.knot_off = (int64_t)L.side_knot.size();
+      L.side_knot.insert(L.side_knot.end(), idx[d].begin(), idx[d].end());
+      L.side_px.insert(L.side_px.end(), px[d].begin(), px[d].end());
+      L.side_py.insert(L.side_py.end(), py[d].begin(), py[d].end());
+      sr.origin = (sr.orient == 0) ? px[d][0] : py[d][0];
+      sr.fixed = (sr.orient == 0) ? py[d][0] : px[d][0];
+      L.max_side = std::max(L.max_side, sr.n);
+      st.side[d] = (int)L.sides.size();
+      side_key.emplace(std::move(key), (int)L.sides.size());
+      L.sides.push_back(sr);
     }
-    auto key = std::make_tuple(sr.n, (long long)std::llround(gap * 1e12),
-                               (long long)std::llround(sr.c * 1e12),
-                               (long long)std::llround(lo / gap * 1e6),
-                               uniform ? (long long)std::llround(hi / gap * 1e6) : -1 - (long long)sd);
-    auto it = shape_key.find(key);
-    if (it == shape_key.end()) {
-      ShapeRec sh;
-      sh.n = sr.n;
-      sh.c = sr.c;
-      sh.t = t;
-      sh.lo = lo;
-      sh.hi = hi;
-      shape_key[key] = (int)L.shapes.size();
-      sr.shape = (int)L.shapes.size();
-      L.shapes.push_back(sh);
-    } else {
-      sr.shape = it->second;
-      ShapeRec& sh = L.shapes[it->second];
-      sh.lo = std::min(sh.lo, lo);
-      sh.hi = std::max(sh.hi, hi);
-    }
+    L.stencils.push_back(std::move(st));
   }
-  int64_t ip = 0;
-  for (auto& sh : L.shapes) {
-    sh.ipsi_off = ip;
-    ip += (int64_t)sh.n * sh.n;
-  }
-  set_shape_bins(L, bps);
+  finish_layout(L, gparams, bps);
   return "";
 }
 

@@ -83,7 +83,35 @@ struct HostLayout {
   std::vector<ShapeRec> shapes;
   int32_t max_side = 0;
   int32_t nboundary = 0;
+  // layouts built from caller stencils (pdds_stencils_set): no subdomain
+  // grid; knot i draws the Philox knot word knot_rng[i] (empty: i) and G's
+  // columns are the caller's knot indices (max_col: the largest)
+  bool custom = false;
+  std::vector<int32_t> knot_rng;
+  int32_t max_col = -1;
 };
+
+// Derived parts of a layout whose knots, stencils and sides are set: boundary
+// knots, G row offsets, side shapes and their bin grids.
+void finish_layout(HostLayout& L, const double gparams[4], int bins_per_gap);
+
+// A caller-built stencil: rectangle, and per side N, S, E, W the knot
+// indices and positions as Stencil::Init receives them, and the RBF shape.
+struct CustomStencil {
+  double rect[4];
+  int32_t n[4];
+  const int32_t* index[4];
+  const double* x[4];
+  const double* y[4];
+  double c2[4];
+};
+
+// Layout of caller-built knots and stencils (pdds_stencils_set): knot i at
+// (x[i], y[i]) with stencil st[i] and Philox knot word knot_id[i] (null: i);
+// domain = {x0, y0, x1, y1}.  Empty string on success, else the error text.
+std::string build_custom_layout(HostLayout& L, const double domain[4], int nknots, const double* x,
+                                const double* y, const int32_t* knot_id, const CustomStencil* st,
+                                int bins_per_gap);
 
 // CSR column indices of G (nnz = row_ptr[K] values) written into out: row k
 // is its stencil's sorted column list (empty for boundary knots).

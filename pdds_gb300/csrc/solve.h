@@ -26,6 +26,7 @@ struct SolveWork {
   unsigned* ctl;    // 4 unsigned: GMRES ticket, convergence flag, basis size
   unsigned* bar;    // 2 unsigned: grid barrier count and generation
   double* gpart;    // grid-reduction partials, 2 * SMs * (GMRES_CLUSTER_MAX_M + 3)
+  unsigned spin_limit;  // grid-barrier polls before a wait gives up (0: the default)
   int launches;     // kernels launched by the last solve
 };
 
@@ -56,6 +57,7 @@ struct ClusterGmresArgs {
   int* out_refines;
   double* out_relres;
   unsigned long long* out_t_end;  // optional: %globaltimer when the system finished
+  unsigned spin_limit;   // grid barrier: polls before a wait gives up (0: 2^24, about 1 s)
 };
 
 // Cluster size for systems of at most max_rows rows (about 512 rows per CTA,
