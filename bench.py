@@ -62,6 +62,22 @@ PATH_KERNEL_DRAM_BYTES = {
 }
 
 
+def knot_residual_rms(est, exact):
+    """RMS over the knots with paths of B_k - u_k - sum_j G_kj u_j at the exact
+    solution u: the per-knot error of the estimated system (bias and Monte
+    Carlo noise) that the interface solve turns into the solution error."""
+    rows = np.repeat(np.arange(len(est.row_ptr) - 1), np.diff(est.row_ptr))
+    gu = np.zeros(len(est.row_ptr) - 1)
+    np.add.at(gu, rows, est.val * exact[est.col])
+    mc = np.diff(est.row_ptr) > 0
+    r = est.B - exact - gu
+    return float(np.sqrt(np.mean(r[mc] ** 2)))
+
+
+def poisson_sincos_u(x, y):
+    return np.sin(np.pi * x) * np.cos(np.pi * y) + x * y
+
+
 def _env_rank():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), \
         int(os.environ.get("LOCAL_RANK", "0"))
@@ -150,10 +166,21 @@ def cpu_baseline(workload: dict, fac, n_knots: int, seed: int = 1234, npaths=Non
     res = L.run(prob, prm, knots=sel)
     dt = time.perf_counter() - t0
     steps = int(res["stats"][0])
+    # per-knot residual of the estimated rows at the exact solution
+    kx, ky = np.zeros(L.nknots), np.zeros(L.nknots)
+    kx[L.work_idx], ky[L.work_idx] = L.work_x, L.work_y
+    if workload.get("problem") == "varcoef_lut":
+        u = np.exp(kx) * np.cos(2 * ky) + 1.0
+    else:
+        u = poisson_sincos_u(kx, ky)
+    r = []
+    for k, kn in enumerate(res["knots"]):
+        a, b = res["row_ptr"][k], res["row_ptr"][k + 1]
+        r.append(res["B"][k] - u[kn] - float(res["g"][a:b] @ u[res["gj"][a:b]]))
     return {"value": steps / dt, "unit": "path-steps/s", "cores": threads, "kind": "port",
             "sample": f"{len(sel)} random knots (seed {seed}) of {workload['name']}, {N} paths each, "
                       f"{steps} path steps in {dt:.2f} s",
-            "seconds": dt, "knots": len(sel), "path_steps": steps}
+            "seconds": dt, "knots": len(sel), "path_steps": steps, "residuals": r}
 
 
 def many_instance_batch(local: int, n_inst: int = 256, reps: int = 3, npaths: int = 10_000, h: float = 1e-3):
@@ -198,7 +225,25 @@ def many_instance_batch(local: int, n_inst: int = 256, reps: int = 3, npaths: in
            "plain_method": {"ms_per_batch": plain["ms"], "solves_per_s": n_inst / (plain["ms"] / 1000.0),
                             "rmse_vs_analytic_mean": float(np.mean(plain_rmse)),
                             "rmse_vs_analytic_max": float(np.max(plain_rmse))}}
+    # error against the FP64 form on 4 instances: each instance alone, FP64,
+    # Philox instance word base + i (the streams it draws in the batch)
+    base = 1000 * reps
+    ub, bb_ = {}, {}
+    pick = [int(v) for v in np.random.default_rng(7).choice(n_inst, size=4, replace=False)]
+    for i in pick:
+        r = bt.result(i)
+        ub[i], bb_[i] = r["u"], r["B"]
     bt.close()
+    uerr, berr = 0.0, 0.0
+    for i in pick:
+        ins = insts[i]
+        with P.PDDSparseGM(ins.sw, ins.ne, ins.nsub, ins.nnode, ins.fac, device=local) as q:
+            e = q.estimate(P.BVP.helmholtz(*ins.params), npaths, h, mode=P.MODE_FP64, seed=1234, instance=base + i,
+                           adaptive_h=True, richardson=True, dup_sum=True)
+            u64, _ = q.solve_interface(P.SOLVE_BICGSTAB_FP64, tol=1e-12)
+        uerr = max(uerr, float(np.max(np.abs(ub[i] - u64))))
+        berr = max(berr, float(np.max(np.abs(bb_[i] - e.B))))
+    out["mixed_err_vs_fp64"] = {"instances": pick, "u_max_abs": uerr, "B_max_abs": berr}
     return out
 
 
@@ -335,12 +380,29 @@ def varcoef_lut(local: int, reps: int = 2):
     rmse = float(np.sqrt(np.mean((u - bvp.u(pd.x, pd.y)) ** 2)))
     e64 = pd.estimate(bvp, 2000, w["h"], mode=P.MODE_FP64, seed=1234, **opts)
     e32 = pd.estimate(bvp, 2000, w["h"], mode=P.MODE_MIXED, seed=1234, **opts)
+    # the error against the FP64 form at the benchmark's 5e4 paths, on 16
+    # knots (the per-knot call, the same Philox streams as the layout run)
+    full = pd.estimate(bvp, w["npaths"], w["h"], mode=P.MODE_MIXED, seed=1234, instance=7, **opts)
+    mc = np.flatnonzero(np.diff(pd.row_ptr) > 0)
+    pick = np.random.default_rng(1234).choice(mc, size=16, replace=False)
+    gerr, berr = 0.0, 0.0
+    with P.EMFKACSolver(local) as sv:
+        for k in pick:
+            st = P.Stencil.of_knot(pd, int(k))
+            G, _, Gj, B, _ = sv.Solve_GPU_Analytic((pd.x[k], pd.y[k]), w["npaths"], w["h"], 0.0, bvp, st,
+                                                   mode=P.MODE_FP64, seed=1234, instance=7, knot_id=int(k),
+                                                   want_var=False, **opts)
+            r0, r1 = full.row_ptr[k], full.row_ptr[k + 1]
+            gerr = max(gerr, float(np.max(np.abs(full.val[r0:r1] - G))))
+            berr = max(berr, abs(float(full.B[k] - B)))
     out = {"knots": int(pd.K), "paths_per_knot": w["npaths"], "h": w["h"], "table": "1024^2 x 8 FP32, bicubic",
            "ms_paths": float(np.mean(ms)), "path_steps_per_s": steps / (1e-3 * float(np.mean(ms))),
            "rmse_vs_analytic": rmse, "solve_ms": float(si["ms"]),
            "fp64": {"paths_per_knot": 2000, "ms_paths": e64.info["ms_paths"],
                     "mixed_over_fp64": (e32.info["path_steps"] / e32.info["ms_paths"]) /
-                                       (e64.info["path_steps"] / e64.info["ms_paths"])}}
+                                       (e64.info["path_steps"] / e64.info["ms_paths"]),
+                    "mixed_err_vs_fp64": {"knots": 16, "paths_per_knot": w["npaths"], "G_max_abs": gerr,
+                                          "B_max_abs": berr}}}
     pd.close()
     return out
 
@@ -395,19 +457,33 @@ def run_reference(args, workload, fac):
         return
     per_step = []
     steps_total = 0
+    knots_total = 0
+    residuals = []
     base = None
     for s in range(args.warmup + args.steps):
         r = cpu_baseline(workload, fac, args.ref_knots, seed=1234 + s)
         if s >= args.warmup:
             per_step.append(r["seconds"])
             steps_total += r["path_steps"]
+            knots_total += r["knots"]
+            residuals += r["residuals"]
             base = r
     value = steps_total / sum(per_step)
+    # The reference's algorithm: every knot's row from N paths of the fixed
+    # step, no Richardson pair, the overwrite of shared side knots; the
+    # accuracy of its rows is their residual at the exact solution (an
+    # interface RMSE would need every knot: about 5 hours on these cores).
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "path-steps/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * float(np.mean(per_step)),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": workload["name"], "knots_per_step": base["knots"],
-                                            "paths_per_knot": workload["npaths"], "h": workload["h"]},
+            "data": "synthetic",
+            "config": {"workload": workload["name"], "knots": base["knots"], "knots_per_step": base["knots"],
+                       "paths_per_knot": workload["npaths"], "h": workload["h"], "mode": "FP64 (CPU, OpenMP paths, "
+                       "serial reduction)", "adaptive_h": False, "richardson": False,
+                       "shared_side_knots": "overwrite (reference)"},
+            "knots_per_s": knots_total / sum(per_step),
+            "knot_residual_rms": float(np.sqrt(np.mean(np.square(residuals)))),
+            "rmse_vs_analytic": None,
             "cpu_baseline": {"value": value, "unit": "path-steps/s", "cores": base["cores"], "kind": "port",
                              "sample": base["sample"]},
             "e2e": {"value": value, "unit": "path-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -527,8 +603,11 @@ def main():
         estp, up, sp = step(999, adaptive_h=False, richardson=False, dup_sum=False)
         tp = (estp.info["ms_setup"] + estp.info["ms_paths"] + sp["ms"]) / 1000.0
         extra["plain_method"] = {"path_steps_per_s": estp.info["path_steps"] / tp, "ms_per_step": 1000 * tp,
-                                 "path_steps": estp.info["path_steps"],
-                                 "rmse_vs_analytic": float(np.sqrt(np.mean((up - exact) ** 2)))}
+                                 "knots_per_s": pd.K / tp, "path_steps": estp.info["path_steps"],
+                                 "rmse_vs_analytic": float(np.sqrt(np.mean((up - exact) ** 2))),
+                                 "knot_residual_rms": knot_residual_rms(estp, exact),
+                                 "form": "the reference's algorithm: fixed step, no Richardson pair, overwrite "
+                                         "of shared side knots"}
     # plain FP64 GPU form on the same workload (the >= 3x comparison)
     if not args.no_fp64 and rank == 0:
         est64, u64, s64 = step(7, mode=P.MODE_FP64, method=P.SOLVE_BICGSTAB_FP64)
@@ -550,11 +629,14 @@ def main():
     # and G, B, u back on the host, every step
     e2e = None
     if not args.no_e2e:
+        # every step: a new context (layout built on the host and uploaded),
+        # the estimate, the solve, G, B and u read back to host memory; the
+        # bytes are the library's own counts of what it copied
         h2d = d2h = 0
         ph = {"layout": 0.0, "estimate": 0.0, "solve": 0.0, "close": 0.0}
         t0 = time.perf_counter()
         e2e_steps = 0
-        for s in range(max(1, min(args.steps, 3))):
+        for s in range(args.steps):
             ta = time.perf_counter()
             q = P.PDDSparseGM(workload["sw"], workload["ne"], workload["nsub"], workload["nnode"], fac,
                               device=local)
@@ -564,18 +646,17 @@ def main():
             u2, si2 = q.solve_interface()
             td = time.perf_counter()
             e2e_steps += est2.info["path_steps"]
-            K, nnz = q.K, q.nnz
+            h2d += q.layout_info["h2d_bytes"] + est2.info["h2d_bytes"] + si2["h2d_bytes"]
+            d2h += est2.info["d2h_bytes"] + si2["d2h_bytes"]
             q.close()
             te = time.perf_counter()
             for k, v in zip(ph, (tb - ta, tc - tb, td - tc, te - td)):
                 ph[k] += v
         dt = time.perf_counter() - t0
-        ns = max(1, min(args.steps, 3))
-        # layout arrays uploaded (knots, stencils, sides, shapes, CSR) and results read back
-        h2d = K * (8 + 8 + 4 + 8) + nnz * 4 + 4096
-        d2h = nnz * 16 + K * 24
-        e2e = {"value": e2e_steps / dt, "unit": "path-steps/s", "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h), "ms_per_step": 1000 * dt / ns,
+        ns = args.steps
+        e2e = {"value": e2e_steps / dt, "unit": "path-steps/s", "h2d_bytes_per_step": int(h2d // ns),
+               "d2h_bytes_per_step": int(d2h // ns), "ms_per_step": 1000 * dt / ns, "steps": ns,
+               "knots_per_s": pd.K * ns / dt,
                "phases_ms": {k: round(1000 * v / ns, 2) for k, v in ph.items()}}
 
     if not args.no_batch and rank == 0:
@@ -597,6 +678,7 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
             cpu = cpu_baseline(workload, fac, args.cpu_knots)
+            cpu["knot_residual_rms"] = float(np.sqrt(np.mean(np.square(cpu.pop("residuals")))))
             fast = cpu_baseline(workload, fac, args.cpu_knots, fast=True)
             extra["cpu_linearity_form"] = {
                 "value": fast["value"], "unit": "path-steps/s", "cores": fast["cores"],
@@ -627,8 +709,10 @@ def main():
                    "mode": "MIXED", "adaptive_h": True, "richardson": "h/2,h",
                    "solver": "GMRES(20) FP32 + FP64 refinement", "l2": "flushed (256 MB write)",
                    "shared_side_knots": "weights summed (dup_sum)"},
-        "interface_solves_per_s": args.steps / t_dev,
+        "interface_solves_per_s": world * args.steps / t_dev,
+        "knots_per_s": world * pd.K * args.steps / t_dev,
         "rmse_vs_analytic": float(np.mean(rmses)),
+        "knot_residual_rms": knot_residual_rms(est, exact),
         "solve_ms": float(np.mean(solve_ms)),
         "wall_s": wall,
         "gpu_launches": int(launches),
