@@ -347,6 +347,11 @@ pdds_status pdds_solve_interface(pdds_ctx* ctx, const pdds_solve_desc* desc, dou
 typedef struct {
   pdds_layout_desc layout; /* the instance's domain, grid and RBF shapes */
   double p[8];             /* the instance's problem parameters            */
+  /* the instance's Euler-Maruyama step (0: the run's estimate.h).  The
+   * step's bias scales with sqrt(h) over the subdomain size, so instances
+   * with finer grids need smaller steps for the same accuracy; the steps per
+   * path stay the same when h scales with the square of the subdomain size. */
+  double h;
 } pdds_instance_desc;
 
 typedef struct {
@@ -364,6 +369,11 @@ typedef struct {
   int32_t use_graph;           /* 1: capture the sequence in a CUDA graph on
                                   the first run and replay it while the batch
                                   and the descriptor stay the same          */
+  /* the instances run in this many consecutive groups (0 = 16, at most the
+   * instance count): one path-kernel launch per group, and the solves of a
+   * group, on a second stream of higher priority, overlap the next group's
+   * paths, so an instance completes when its group does */
+  int32_t waves;
 } pdds_batch_run_desc;
 
 typedef struct {

@@ -105,7 +105,7 @@ class SolveInfo(C.Structure):
 
 
 class InstanceDesc(C.Structure):
-    _fields_ = [("layout", LayoutDesc), ("p", C.c_double * 8)]
+    _fields_ = [("layout", LayoutDesc), ("p", C.c_double * 8), ("h", C.c_double)]
 
 
 class BatchInfo(C.Structure):
@@ -113,7 +113,7 @@ class BatchInfo(C.Structure):
 
 
 class BatchRunDesc(C.Structure):
-    _fields_ = [("estimate", EstimateDesc), ("solve", SolveDesc), ("use_graph", C.c_int32)]
+    _fields_ = [("estimate", EstimateDesc), ("solve", SolveDesc), ("use_graph", C.c_int32), ("waves", C.c_int32)]
 
 
 class BatchRunInfo(C.Structure):

@@ -706,6 +706,7 @@ class Instance:
     nnode: int
     fac: tuple
     params: tuple = ()
+    h: float = 0.0  # the instance's step (0: the run's h)
 
 
 class Batch:
@@ -740,6 +741,7 @@ class Batch:
                 d.layout.fac[q] = float(ins.fac[q])
             for q, v in enumerate(ins.params):
                 d.p[q] = float(v)
+            d.h = float(ins.h)
         info = capi.BatchInfo()
         self._check(self._lib.pdds_batch_build(self._ctx, arr, n, C.byref(info)))
         self.info = {f: getattr(info, f) for f, _ in capi.BatchInfo._fields_}
@@ -772,8 +774,10 @@ class Batch:
 
     def run(self, npaths: int, h: float, seed: int = 1234, instance: int = 0, adaptive_h: bool = True,
             richardson: bool = False, tol: float = 1e-10, restart: int = 30, use_graph: bool = True,
-            bins_per_gap: int = 0, reuse_tables: bool = False, dup_sum: bool = False) -> dict:
-        """Estimates and solves every instance; returns the run counters."""
+            bins_per_gap: int = 0, reuse_tables: bool = False, dup_sum: bool = False, waves: int = 0) -> dict:
+        """Estimates and solves every instance (in `waves` consecutive groups
+        whose solves overlap the next group's paths; 0 = 16); returns the run
+        counters."""
         d = capi.BatchRunDesc()
         e = d.estimate
         e.mode = capi.MODE_MIXED
@@ -790,6 +794,7 @@ class Batch:
         d.solve.restart = int(restart)
         d.solve.tol = float(tol)
         d.use_graph = int(bool(use_graph))
+        d.waves = int(waves)
         info = capi.BatchRunInfo()
         self._check(self._lib.pdds_batch_run(self._ctx, C.byref(d), C.byref(info)))
         return {f: getattr(info, f) for f, _ in capi.BatchRunInfo._fields_}

@@ -64,13 +64,22 @@ def varcoef_tables(n: int = 1024, bounds=(0.0, 0.0, 1.0, 1.0)):
     return np.ascontiguousarray(coef), np.ascontiguousarray(u.astype(np.float32)), tuple(float(b) for b in bounds)
 
 
-def batch_instances(n: int = 256, seed: int = 1234, grid=(4, 16), nodes=(11, 41)):
+def instance_step(g: int, h_ref: float = 1e-3, g_ref: int = 4) -> float:
+    """Step of an instance with g x g subdomains on the unit square: h_ref at
+    g_ref x g_ref, scaled with the square of the subdomain size above it, so
+    sqrt(h) stays the same fraction of a subdomain (the step's bias is a
+    function of that ratio) and paths take the same number of steps."""
+    return h_ref * min(1.0, (g_ref / g) ** 2)
+
+
+def batch_instances(n: int = 256, seed: int = 1234, grid=(4, 16), nodes=(11, 41), scaled_h: float = 0.0):
     """The many-instance workload: n Helmholtz problems Lap u + c u + f = 0
     on [0,1]^2 with u = sin(a x) cos(b y), a, b ~ U[1,4], c ~ U[-4,0], each
     on its own g x g subdomain grid, g ~ U{4..16}, with k ~ U{11..41} knots
     per segment (seeded).  The grids are square: the reference's layout
     (Fullfill_interfaces and its configuration reader) takes one subdomain
-    count for both directions."""
+    count for both directions.  scaled_h > 0 gives each instance the step
+    instance_step(g, scaled_h) (0: the run's step for all)."""
     import numpy as np
     from .api import Instance
     rng = np.random.default_rng(seed)
@@ -80,5 +89,6 @@ def batch_instances(n: int = 256, seed: int = 1234, grid=(4, 16), nodes=(11, 41)
         k = int(rng.integers(nodes[0], nodes[1] + 1))
         a, b = rng.uniform(1.0, 4.0, size=2)
         c = -rng.uniform(0.0, 4.0)
-        out.append(Instance((0.0, 0.0), (1.0, 1.0), g, k, fac_rule(1.0, g, k), (float(a), float(b), float(c))))
+        out.append(Instance((0.0, 0.0), (1.0, 1.0), g, k, fac_rule(1.0, g, k), (float(a), float(b), float(c)),
+                            instance_step(g, scaled_h) if scaled_h > 0 else 0.0))
     return out

@@ -21,22 +21,27 @@ using namespace pdds;
 
 namespace {
 
-// The whole batch step on ctx->stream, without host synchronisation.
+// Number of instance groups of a run.
+int batch_waves(const pdds_ctx* ctx, const pdds_batch_run_desc* d) {
+  return std::max(1, std::min(ctx->n_inst, d->waves > 0 ? d->waves : 16));
+}
+
+// The whole batch step, without host synchronisation.  The stream runs the
+// factorisation, zeroing and boundary knots, then the instances in W
+// consecutive groups (a path-kernel launch and the finalisation per group);
+// the solve stream, once a group's finalisation is done, copies its G rows
+// to FP32 and runs the cluster GMRES of its systems while the next group's
+// paths run.  The last solve joins the stream again.
 pdds_status enqueue_batch(pdds_ctx* ctx, const pdds_batch_run_desc* d, int cluster, int* launches) {
-  cudaStream_t s = ctx->stream;
+  cudaStream_t s = ctx->stream, s2 = ctx->solve_stream;
   const int n = ctx->n_inst;
-  const int64_t K = ctx->L.K;
-  const int64_t nnz = ctx->L.row_ptr[ctx->L.K];
+  const int W = batch_waves(ctx, d);
   CK(launch_stamp(ctx->b_tend.p + n, s));
   ++*launches;
-  pdds_status st = enqueue_mixed(ctx, &d->estimate, launches);
+  pdds_status st = enqueue_mixed(ctx, &d->estimate, launches, 0, 0, true);  // prefix only
   if (st != PDDS_OK) return st;
-  CK(launch_to_f32(ctx->G.p, ctx->sval32.p, nnz, s));
-  ++*launches;
   ClusterGmresArgs a{};
-  a.n_sys = n;
-  a.sys_row0 = ctx->inst_knot0.p;
-  a.K = K;
+  a.K = ctx->L.K;
   a.row_ptr = ctx->row_ptr.p;
   a.col = ctx->col.p;
   a.val64 = ctx->G.p;
@@ -50,12 +55,27 @@ pdds_status enqueue_batch(pdds_ctx* ctx, const pdds_batch_run_desc* d, int clust
   a.max_refine = d->solve.max_refine > 0 ? d->solve.max_refine : 30;
   a.tol = d->solve.tol > 0 ? d->solve.tol : 1e-10;
   a.inner_tol = 1e-6;
-  a.out_iters = ctx->b_iters.p;
-  a.out_refines = ctx->b_refines.p;
-  a.out_relres = ctx->b_relres.p;
-  a.out_t_end = ctx->b_tend.p;
-  CK(launch_gmres_cluster(a, cluster, ctx->max_inst_knots, s));
-  ++*launches;
+  for (int w = 0; w < W; w++) {
+    const int i0 = (int)((int64_t)n * w / W), i1 = (int)((int64_t)n * (w + 1) / W);
+    const int m0 = ctx->inst_mc0[i0], m1 = ctx->inst_mc0[i1];
+    st = enqueue_mixed(ctx, &d->estimate, launches, m0, m1 - m0, false);
+    if (st != PDDS_OK) return st;
+    CK(cudaEventRecord(ctx->wave_ev[w], s));
+    CK(cudaStreamWaitEvent(s2, ctx->wave_ev[w], 0));
+    const int64_t e0 = ctx->inst_nnz0[i0], e1 = ctx->inst_nnz0[i1];
+    CK(launch_to_f32(ctx->G.p + e0, ctx->sval32.p + e0, e1 - e0, s2));
+    ++*launches;
+    a.n_sys = i1 - i0;
+    a.sys_row0 = ctx->inst_knot0.p + i0;
+    a.out_iters = ctx->b_iters.p + i0;
+    a.out_refines = ctx->b_refines.p + i0;
+    a.out_relres = ctx->b_relres.p + i0;
+    a.out_t_end = ctx->b_tend.p + i0;
+    CK(launch_gmres_cluster(a, cluster, ctx->max_inst_knots, s2));
+    ++*launches;
+  }
+  CK(cudaEventRecord(ctx->wave_ev[W], s2));
+  CK(cudaStreamWaitEvent(s, ctx->wave_ev[W], 0));
   return PDDS_OK;
 }
 
@@ -102,8 +122,11 @@ pdds_status pdds_batch_build(pdds_ctx* ctx, const pdds_instance_desc* inst, int3
   ctx->inst_k0.assign(n + 1, 0);
   ctx->inst_nnz0.assign(n + 1, 0);
   ctx->inst_p.assign((size_t)8 * n, 0.0);
+  ctx->inst_hv.assign((size_t)n, 0.0);
   ctx->max_inst_knots = 0;
   for (int i = 0; i < n; i++) {
+    if (!(inst[i].h >= 0.0)) return fail(ctx, PDDS_ERR_INVALID, "instance " + std::to_string(i) + ": h must be >= 0");
+    ctx->inst_hv[i] = inst[i].h;
     ctx->inst_k0[i + 1] = ctx->inst_k0[i] + parts[i].K;
     ctx->inst_nnz0[i + 1] = ctx->inst_nnz0[i] + parts[i].row_ptr[parts[i].K];
     for (int q = 0; q < 8; q++) ctx->inst_p[8 * i + q] = inst[i].p[q];
@@ -121,6 +144,7 @@ pdds_status pdds_batch_build(pdds_ctx* ctx, const pdds_instance_desc* inst, int3
     CK(ctx->knot_inst.upload(knot_inst, s));
     CK(ctx->inst_knot0.upload(ctx->inst_k0, s));
     CK(ctx->inst_pd.upload(ctx->inst_p, s));
+    CK(ctx->inst_hd.upload(ctx->inst_hv, s));
     CK(ctx->b_iters.resize(n));
     CK(ctx->b_refines.resize(n));
     CK(ctx->b_relres.resize(n));
@@ -128,6 +152,15 @@ pdds_status pdds_batch_build(pdds_ctx* ctx, const pdds_instance_desc* inst, int3
     pdds_status st = upload_layout(ctx);
     if (st != PDDS_OK) return st;
     CK(cudaStreamSynchronize(s));
+    // first entry of each instance in the list of knots with paths (the
+    // merged hand-out order runs instance by instance)
+    const std::vector<int>& mc = ctx->mc_host;
+    ctx->inst_mc0.assign(n + 1, (int)mc.size());
+    int m = 0;
+    for (int i = 0; i < n; i++) {
+      while (m < (int)mc.size() && knot_inst[mc[m]] < i) m++;
+      ctx->inst_mc0[i] = m;
+    }
   }
   if (info) {
     info->ninstances = n;
@@ -161,6 +194,17 @@ pdds_status pdds_batch_run(pdds_ctx* ctx, const pdds_batch_run_desc* desc, pdds_
     set_shape_bins(L, bins);
     pdds_status st = upload_layout(ctx);
     if (st != PDDS_OK) return st;
+  }
+  if (desc->waves < 0) return fail(ctx, PDDS_ERR_INVALID, "waves must be >= 0");
+  if (!ctx->solve_stream) {
+    int least = 0, greatest = 0;
+    CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    CK(cudaStreamCreateWithPriority(&ctx->solve_stream, cudaStreamNonBlocking, greatest));
+  }
+  while ((int)ctx->wave_ev.size() < batch_waves(ctx, desc) + 1) {
+    cudaEvent_t ev = nullptr;
+    CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    ctx->wave_ev.push_back(ev);
   }
   const int cluster = gmres_cluster_pick(ctx->max_inst_knots);
   if (cluster <= 0)

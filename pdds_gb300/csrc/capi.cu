@@ -103,6 +103,7 @@ pdds_status upload_layout(pdds_ctx* ctx) {
   std::vector<int> mc, bnd;
   for (int v : L.order) (L.knot_boundary[v] ? bnd : mc).push_back(v);
   ctx->n_mc = (int)mc.size();
+  ctx->mc_host = mc;
   ctx->n_bnd = (int)bnd.size();
   // shared-memory needs of the path kernels
   size_t msm = 0, fsm = 0;
@@ -197,6 +198,7 @@ pdds_status upload_layout(pdds_ctx* ctx) {
   d.knot_inst = ctx->is_batch ? ctx->knot_inst.p : nullptr;
   d.inst_knot0 = ctx->is_batch ? ctx->inst_knot0.p : nullptr;
   d.inst_p = ctx->is_batch ? ctx->inst_pd.p : nullptr;
+  d.inst_h = ctx->is_batch ? ctx->inst_hd.p : nullptr;
   d.knot_rng = nullptr;
   if (!L.knot_rng.empty()) {
     std::vector<int> kr(L.knot_rng.begin(), L.knot_rng.end());
@@ -281,7 +283,8 @@ int cta_threads_for(const pdds_ctx* ctx, const pdds_estimate_desc* d) {
   return mixed_threads(ctx->n_mc);
 }
 
-void item_split(const pdds_ctx* ctx, int N, int* chunks_out, int* ppc_out, int tuned_ppc = 0, int threads = 0) {
+void item_split(const pdds_ctx* ctx, int N, int* chunks_out, int* ppc_out, int tuned_ppc = 0, int threads = 0,
+                int n_knots = -1) {
   if (tuned_ppc > 0) {
     const int ppc = std::max(1, std::min(N, tuned_ppc));
     *chunks_out = (N + ppc - 1) / ppc;
@@ -289,8 +292,8 @@ void item_split(const pdds_ctx* ctx, int N, int* chunks_out, int* ppc_out, int t
     return;
   }
   // about four items per persistent CTA (1024 / threads CTAs per SM)
-  const int n_mc = ctx->n_mc;
-  const int target = 4 * std::max(ctx->num_sms, 1) * (1024 / (threads > 0 ? threads : mixed_threads(n_mc)));
+  const int n_mc = n_knots >= 0 ? n_knots : ctx->n_mc;
+  const int target = 4 * std::max(ctx->num_sms, 1) * (1024 / (threads > 0 ? threads : mixed_threads(ctx->n_mc)));
   int chunks = std::max(1, (target + std::max(n_mc, 1) - 1) / std::max(n_mc, 1));
   chunks = std::min(chunks, std::max(1, N / 256));
   const int ppc = (N + chunks - 1) / chunks;
@@ -308,8 +311,10 @@ struct ItemList {
 };
 
 pdds_status enqueue_mixed_paths(pdds_ctx* ctx, const pdds_estimate_desc* desc, const ProblemDev& P, int chunks,
-                                int ppc, int* launches, const ItemList* items = nullptr) {
+                                int ppc, int* launches, const ItemList* items = nullptr, int mc0 = 0,
+                                int mc_n = -1) {
   cudaStream_t s = ctx->stream;
+  if (mc_n < 0) mc_n = ctx->n_mc;
   if (!items && P.kind == PK_ROBIN && (int)P.p[0] != 0 && !ctx->is_batch) {
     // Knots whose stencil has a reflecting side take several times the
     // steps per path of the others (their paths leave only through the
@@ -347,7 +352,7 @@ pdds_status enqueue_mixed_paths(pdds_ctx* ctx, const pdds_estimate_desc* desc, c
     return enqueue_mixed_paths(ctx, desc, P, 1, ppc, launches, &il);
   }
   const int N = desc->npaths;
-  const int n_items = items ? items->n : ctx->n_mc * chunks;
+  const int n_items = items ? items->n : mc_n * chunks;
   const long long max_steps = desc->max_steps > 0 ? desc->max_steps : 1000000LL;
   CK(cudaMemsetAsync(ctx->counter.p, 0, sizeof(int), s));
   MixedArgs a;
@@ -397,7 +402,7 @@ pdds_status enqueue_mixed_paths(pdds_ctx* ctx, const pdds_estimate_desc* desc, c
     CK(ctx->mc_lpt.upload(ord, s));
     ctx->lpt_ready = true;
   }
-  a.mc_knots = (lpt && ctx->lpt_ready) ? ctx->mc_lpt.p : ctx->mc_knots.p;
+  a.mc_knots = (lpt && ctx->lpt_ready) ? ctx->mc_lpt.p : ctx->mc_knots.p + mc0;
   a.item_counter = ctx->counter.p;
   a.G = ctx->G.p;
   a.GG = ctx->GG.p;
@@ -487,17 +492,34 @@ pdds_status adaptive_continue(pdds_ctx* ctx, const pdds_estimate_desc* desc, con
   return PDDS_OK;
 }
 
-pdds_status enqueue_mixed(pdds_ctx* ctx, const pdds_estimate_desc* desc, int* launches) {
+pdds_status enqueue_mixed(pdds_ctx* ctx, const pdds_estimate_desc* desc, int* launches, int mc0, int mc_n,
+                          bool prefix) {
   const ProblemDev P = problem_dev(ctx);
-  pdds_status st = enqueue_prefix(ctx, desc, P, false, launches);
-  if (st != PDDS_OK) return st;
+  if (prefix) {
+    pdds_status st = enqueue_prefix(ctx, desc, P, false, launches);
+    if (st != PDDS_OK) return st;
+  }
+  if (mc_n < 0) mc_n = ctx->n_mc - mc0;
+  if (mc_n == 0) return PDDS_OK;
   int chunks = 1, ppc = 1;
-  item_split(ctx, desc->npaths, &chunks, &ppc, tuned_for(ctx, desc) ? ctx->tune_ppc : 0, cta_threads_for(ctx, desc));
-  st = enqueue_mixed_paths(ctx, desc, P, chunks, ppc, launches);
+  item_split(ctx, desc->npaths, &chunks, &ppc, tuned_for(ctx, desc) ? ctx->tune_ppc : 0, cta_threads_for(ctx, desc),
+             mc_n);
+  pdds_status st = enqueue_mixed_paths(ctx, desc, P, chunks, ppc, launches, nullptr, mc0, mc_n);
   if (st != PDDS_OK) return st;
-  const int64_t nnz = ctx->L.row_ptr[ctx->L.K];
-  CK(launch_finalize(ctx->mc_knots.p, ctx->n_mc, desc->npaths, ctx->Bsum.p, ctx->BBsum.p, ctx->B.p, ctx->BB.p,
-                     ctx->row_ptr.p, nnz, ctx->G.p, ctx->GG.p, desc->want_var ? 1 : 0, ctx->stream));
+  // finalisation of the range's knots: B and BB, and G_var over the range's rows
+  const HostLayout& L = ctx->L;
+  int64_t e0 = 0, e1 = L.row_ptr[L.K];
+  if (!(mc0 == 0 && mc_n == ctx->n_mc)) {  // the rows of the range's knots
+    e0 = e1;
+    e1 = 0;
+    for (int m = mc0; m < mc0 + mc_n; m++) {
+      const int k = ctx->mc_host[m];
+      e0 = std::min(e0, L.row_ptr[k]);
+      e1 = std::max(e1, L.row_ptr[k + 1]);
+    }
+  }
+  CK(launch_finalize(ctx->mc_knots.p + mc0, mc_n, desc->npaths, ctx->Bsum.p, ctx->BBsum.p, ctx->B.p, ctx->BB.p,
+                     ctx->row_ptr.p, e1 - e0, ctx->G.p + e0, ctx->GG.p + e0, desc->want_var ? 1 : 0, ctx->stream));
   *launches += 1 + (desc->want_var ? 1 : 0);
   return PDDS_OK;
 }
@@ -574,6 +596,7 @@ pdds_status pdds_destroy(pdds_ctx* ctx) {
     ctx->b_iters.release();
     ctx->b_refines.release();
     ctx->inst_pd.release();
+    ctx->inst_hd.release();
     ctx->b_relres.release();
     ctx->b_tend.release();
     ctx->knot_N.release();
@@ -594,6 +617,8 @@ pdds_status pdds_destroy(pdds_ctx* ctx) {
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->ev2) cudaEventDestroy(ctx->ev2);
+    for (cudaEvent_t ev : ctx->wave_ev) cudaEventDestroy(ev);
+    if (ctx->solve_stream) cudaStreamDestroy(ctx->solve_stream);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
   }
   delete ctx;

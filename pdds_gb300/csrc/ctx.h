@@ -73,6 +73,7 @@ struct pdds_ctx {
   DBuf<float> tab;
   DevLayout dl{};
   int n_mc = 0, n_bnd = 0;
+  std::vector<int> mc_host;  // knots with paths, in hand-out order (the device mc_knots)
   size_t mixed_smem = 0, fp64_smem = 0;
   int max_nbins = 0;
   // results and scratch
@@ -100,8 +101,10 @@ struct pdds_ctx {
   std::vector<int> inst_k0;         // first knot of each instance, n_inst + 1
   std::vector<int64_t> inst_nnz0;   // first G entry of each instance, n_inst + 1
   std::vector<double> inst_p;       // 8 problem parameters per instance
+  std::vector<double> inst_hv;      // step per instance (0: the run's)
+  std::vector<int> inst_mc0;        // first entry of each instance in mc_host, n_inst + 1
   DBuf<int> knot_inst, inst_knot0, b_iters, b_refines;
-  DBuf<double> inst_pd, b_relres;
+  DBuf<double> inst_pd, inst_hd, b_relres;
   DBuf<unsigned long long> b_tend;  // per instance, then the start stamp
   int max_inst_knots = 0;
   cudaGraph_t graph = nullptr;
@@ -110,6 +113,10 @@ struct pdds_ctx {
   int graph_launches = 0;
   std::vector<cudaGraphNode_t> graph_path_nodes;  // path-kernel nodes, re-keyed per run
   bool has_batch_run = false;
+  // batch waves: the solves of a wave run on solve_stream (higher priority)
+  // while the next wave's paths run on stream; wave_ev orders them
+  cudaStream_t solve_stream = nullptr;
+  std::vector<cudaEvent_t> wave_ev;
   // subdomain solves: knots of each subdomain edge (S, N, W, E; -1 = domain boundary)
   DBuf<int> edge_knots;
   DBuf<double> sub_u, sub_out;
@@ -144,7 +151,10 @@ pdds_status check_err_flags(pdds_ctx* ctx);
 // Enqueues the MIXED estimation on ctx->stream: RBF factorisation and tables
 // (unless reused), zeroing, boundary knots, the path kernel and the
 // finalisation.  No host synchronisation, so it can be graph-captured.
-pdds_status enqueue_mixed(pdds_ctx* ctx, const pdds_estimate_desc* desc, int* launches);
+// mc0, mc_n: only the knots mc_knots[mc0 .. mc0 + mc_n) (mc_n < 0: to the
+// end); prefix: also the factorisation, zeroing and boundary knots.
+pdds_status enqueue_mixed(pdds_ctx* ctx, const pdds_estimate_desc* desc, int* launches, int mc0 = 0,
+                          int mc_n = -1, bool prefix = true);
 // Destroys the captured batch graph (its kernels hold buffer addresses).
 void drop_graph(pdds_ctx* ctx);
 // Forgets the autotuned launch shape (it was timed on the previous layout).

@@ -59,6 +59,7 @@ struct DevLayout {
   const int* knot_inst;
   const int* inst_knot0;
   const double* inst_p;
+  const double* inst_h;  // step per instance (0: the run's), batches only
   // Philox knot word of each knot (null: the knot's own index); set for
   // layouts built from caller stencils, whose knots carry the caller's ids
   const int* knot_rng;

@@ -160,16 +160,22 @@ k_paths_mixed(const MixedArgs a) {
         s_dir[2] = (float)cos(L.st_rect[4 * st + 3]);
         s_dir[3] = (float)sin(L.st_rect[4 * st + 3]);
       }
-      s_h = a.h;
-      s_sqrth = a.sqrth;
+      // the step of the knot's instance (batches), else the run's
+      double h0 = a.h64;
+      if (L.inst_h && L.knot_inst) {
+        const double hi = L.inst_h[L.knot_inst[k]];
+        if (hi > 0.0) h0 = hi;
+      }
+      s_h = (float)h0;
+      s_sqrth = (float)sqrt(h0);
       if (a.adaptive_h) {
         ProblemDev Pk = a.P;
         uint32_t ri = 0, rk = 0;
         instance_params(L, k, Pk, ri, rk);
         Coef<double> kd;
         coef_f64<KIND>(Pk, L.kx[k], L.ky[k], kd);
-        const double hk = GEOM == 1 ? adaptive_step_polar(L.st_rect + 4 * st, L.kx[k], L.ky[k], a.h64, kd)
-                                    : adaptive_step<double>(L.st_rect + 4 * st, L.kx[k], L.ky[k], a.h64, kd);
+        const double hk = GEOM == 1 ? adaptive_step_polar(L.st_rect + 4 * st, L.kx[k], L.ky[k], h0, kd)
+                                    : adaptive_step<double>(L.st_rect + 4 * st, L.kx[k], L.ky[k], h0, kd);
         s_h = (float)hk;
         s_sqrth = (float)sqrt(hk);
       }

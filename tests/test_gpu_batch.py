@@ -62,6 +62,34 @@ def test_batch_graph_replay_matches_direct_launch():
         assert np.max(np.abs(d - o)) < 1e-6
 
 
+def test_batch_scaled_steps_reach_the_accuracy_target_in_waves():
+    """The many-instance workload's policy: each instance's step scaled with
+    the square of its subdomain size (h at 4 x 4, h (4/g)^2 on g x g), the
+    Richardson pair and the adaptive step, 1e4 paths: every instance's
+    interface RMSE is below 2e-3, grids up to 16 x 16 and 11..41 knots per
+    segment.  Run in groups whose solves overlap the next group's paths, the
+    first instances complete well before the batch; the grouping changes no
+    result beyond summation order."""
+    insts = batch_instances(20, seed=11, scaled_h=1e-3)
+    assert max(i.nsub for i in insts) >= 14 and min(i.h for i in insts) < 1e-4
+    opts = dict(seed=5, instance=40, use_graph=True, richardson=True, dup_sum=True)
+    with P.Batch(P.BVP.HELMHOLTZ, insts) as bt:
+        one = bt.run(10_000, 1e-3, waves=1, **opts)
+        u1 = [bt.result(i)["u"] for i in range(len(insts))]
+        info = bt.run(10_000, 1e-3, waves=5, **opts)
+        assert info["unconverged"] == 0
+        lat, rmse = [], []
+        for i, ins in enumerate(insts):
+            r = bt.result(i)
+            x, y = bt.knots(i)
+            rmse.append(float(np.sqrt(np.mean((r["u"] - P.BVP.helmholtz(*ins.params).u(x, y)) ** 2))))
+            lat.append(r["latency_ms"])
+            np.testing.assert_allclose(r["u"], u1[i], rtol=0, atol=2e-5)
+    assert max(rmse) < 2e-3, rmse
+    assert min(lat) < 0.5 * info["ms"] and max(lat) <= info["ms"] * 1.05
+    assert one["path_steps"] == info["path_steps"]
+
+
 def test_batch_many_instances_converge():
     insts = batch_instances(24, seed=3, grid=(4, 10), nodes=(11, 25))
     with P.Batch(P.BVP.HELMHOLTZ, insts) as bt:
