@@ -414,15 +414,18 @@ def varcoef_lut(local: int, reps: int = 2):
     return out
 
 
-def circle_uneven(local: int, reps: int = 3, h: float = 1e-3):
+def circle_uneven(local: int, reps: int = 2, h: float = 2e-5):
     """Uneven path lengths on the unit disk: 6 rings x 16 sectors (the central
     ring one disk subdomain), 11 knots per segment, Poisson with
-    u = r^2 sin(3 theta) + cos x; per-knot adaptive step (knots near their
-    stencil side take steps down to ~1e-6, so mean path lengths span orders
-    of magnitude), Richardson pair, variance-adaptive paths per knot
-    N_k in [1e3, 1e5] for a score standard error of 1e-3, the launch shape
-    picked by the autotuner.  The FP64 form runs the same layout with 1e3
-    paths per knot for the MIXED/FP64 comparison."""
+    u = r^2 sin(3 theta) + cos x; h = 2e-5 with the per-knot adaptive step, so
+    a path takes from 1 to a few 1e4 steps (the paths' step counts fill every
+    log2 bin from 1 to 2^14..2^15) and a knot's mean from ~50 to ~1600;
+    Richardson pair, variance-adaptive paths per knot N_k in [1e3, 1e5] for a
+    score standard error of 1e-3, the launch shape picked by the autotuner.
+    The same estimate with one CTA per work item in layout order shows what
+    the persistent CTAs and the heaviest-first order do on it.  The FP64
+    form runs the same layout with 1e3 paths per knot for the MIXED/FP64
+    comparison."""
     import pdds_gb300 as P
     bvp = P.BVP.circle_poisson()
     pd = P.PDDSparseGM.circle_mesh(1.0, 6, 16, 11, device=local)
@@ -437,14 +440,22 @@ def circle_uneven(local: int, reps: int = 3, h: float = 1e-3):
         if r > 0:
             runs.append((est, u, si))
     est, u, si = runs[-1]
+    hist = pd.step_histogram()
     steps = pd.knot_steps().astype(np.float64)
     mc = est.npaths > 0
     per_path = steps[mc] / (2.0 * est.npaths[mc])  # both levels of the pair count; per level
     ms = [e.info["ms_setup"] + e.info["ms_paths"] + s_["ms"] for e, _, s_ in runs]
-    out = {"knots": int(pd.K), "paths_per_knot_min": int(est.npaths[mc].min()),
+    plain = pd.estimate(bvp, 1000, h, mode=P.MODE_MIXED, seed=1234, instance=reps, adaptive_n=True,
+                        npaths_max=100_000, target_stderr=1e-3, plain_launch=True, **opts)
+    nz = np.flatnonzero(hist)
+    out = {"knots": int(pd.K), "h": h, "adaptive_h": True, "paths_per_knot_min": int(est.npaths[mc].min()),
            "paths_per_knot_max": int(est.npaths[mc].max()), "paths": int(est.info["paths"]),
            "path_steps": int(est.info["path_steps"]), "ms_per_step": float(np.mean(ms)),
            "path_steps_per_s": float(np.mean([e.info["path_steps"] / (m / 1000.0) for (e, _, _), m in zip(runs, ms)])),
+           "path_kernel_ms": float(np.mean([e.info["ms_paths"] for e, _, _ in runs])),
+           "plain_launch_path_kernel_ms": float(plain.info["ms_paths"]),
+           "steps_per_path_histogram_log2": hist[:nz.max() + 1].tolist(),
+           "steps_per_path_min": int(2 ** nz.min()), "steps_per_path_max_at_least": int(2 ** nz.max()),
            "mean_steps_per_path_min": float(per_path.min()), "mean_steps_per_path_max": float(per_path.max()),
            "rmse_vs_analytic": float(np.sqrt(np.mean((u - ex) ** 2))), "solver_iterations": int(si["iterations"]),
            "autotune": tune}
@@ -615,6 +626,13 @@ def main():
                                  "knot_residual_rms": knot_residual_rms(estp, exact),
                                  "form": "the reference's algorithm: fixed step, no Richardson pair, overwrite "
                                          "of shared side knots"}
+    # the same estimate with one CTA per work item, knots in layout order
+    # (what the persistent CTAs and the heaviest-first order replace)
+    if rank == 0:
+        estl = pd.estimate(bvp, N, h, mode=P.MODE_MIXED, seed=1234, instance=998, plain_launch=True, **OPTS)
+        extra["launch_policy"] = {"path_kernel_ms": float(np.mean(ms_paths)),
+                                  "plain_launch_path_kernel_ms": float(estl.info["ms_paths"]),
+                                  "plain_launch": "one CTA per work item, knots in layout order"}
     # plain FP64 GPU form on the same workload (the >= 3x comparison)
     if not args.no_fp64 and rank == 0:
         est64, u64, s64 = step(7, mode=P.MODE_FP64, method=P.SOLVE_BICGSTAB_FP64)

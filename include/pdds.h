@@ -139,6 +139,12 @@ typedef struct {
   int32_t nsectors;
   int32_t nnode;
   double kappa[4];
+  /* ring widths: ring i (i = 0 the central disk) is ring_ratio^i times as
+   * wide as the central disk's radius (0 or 1: equal widths R / nrings).  A
+   * ratio below 1 gives a boundary-layer mesh whose thin outer rings hold
+   * knots that leave their stencils in a step while knots of the wide inner
+   * rings need thousands at the same h. */
+  double ring_ratio;
 } pdds_circle_desc;
 
 pdds_status pdds_layout_build_circle(pdds_ctx* ctx, const pdds_circle_desc* desc, pdds_layout_info* info);
@@ -232,6 +238,11 @@ typedef struct {
    * layout size (128 from 8192 Monte Carlo knots).  Results do not depend
    * on it beyond FP32 summation order. */
   int32_t cta_threads;
+  /* MIXED only, 1: the launch the persistent refill replaces, for
+   * comparison -- one CTA per work item (not a CTA per SM slot pulling
+   * items) and the knots in layout order (not heaviest first).  Same
+   * results up to FP32 summation order. */
+  int32_t plain_launch;
 } pdds_estimate_desc;
 
 typedef struct {
@@ -257,6 +268,10 @@ pdds_status pdds_estimate_knot_paths(pdds_ctx* ctx, int32_t* npaths);
 /* Euler-Maruyama steps per knot of the last MIXED pdds_estimate, summed
  * over its paths (both levels of a Richardson pair): steps[K]. */
 pdds_status pdds_estimate_knot_steps(pdds_ctx* ctx, int64_t* steps);
+/* Exit step counts of the last MIXED pdds_estimate: hist[b] paths (each level
+ * of a Richardson pair counts) took between 2^b and 2^(b+1) - 1 steps,
+ * b = 0 .. 31. */
+pdds_status pdds_estimate_step_histogram(pdds_ctx* ctx, int64_t* hist);
 
 /* One knot as EMFKACSolver::Solve_OMP_Analytic computes it
  * (Solvers/EMFKACSolver.hpp:711-729): from X0 = (x0, y0) inside the stencil

@@ -28,7 +28,7 @@ EXPORTS = [
     "pdds_estimate", "pdds_estimate_knot_paths", "pdds_estimate_knot_steps", "pdds_autotune", "pdds_solve_interface",
     "pdds_subdomain_solve", "pdds_semilinear_tables", "pdds_batch_build", "pdds_batch_run", "pdds_batch_instance",
     "pdds_solve_bicgstab_static", "pdds_check_philox", "pdds_check_portable_math", "pdds_stencils_set",
-    "pdds_estimate_knot",
+    "pdds_estimate_knot", "pdds_estimate_step_histogram",
 ]
 STATIC_SOLVE_MAX_K = 131072
 PHILOX_PORTABLE, PHILOX_ROUND_KEYS = 0, 1
@@ -46,7 +46,7 @@ class LayoutDesc(C.Structure):
 
 class CircleDesc(C.Structure):
     _fields_ = [("radius", C.c_double), ("nrings", C.c_int32), ("nsectors", C.c_int32), ("nnode", C.c_int32),
-                ("kappa", C.c_double * 4)]
+                ("kappa", C.c_double * 4), ("ring_ratio", C.c_double)]
 
 
 class SemilinearDesc(C.Structure):
@@ -77,7 +77,7 @@ class EstimateDesc(C.Structure):
                 ("ipsi_override", C.POINTER(C.c_double)), ("ipsi_override_len", C.c_int64),
                 ("adaptive_h", C.c_int32), ("richardson", C.c_int32), ("reuse_tables", C.c_int32),
                 ("adaptive_n", C.c_int32), ("npaths_max", C.c_int32), ("target_stderr", C.c_double),
-                ("cta_threads", C.c_int32)]
+                ("cta_threads", C.c_int32), ("plain_launch", C.c_int32)]
 
 
 class EstimateInfo(C.Structure):
@@ -160,6 +160,7 @@ def load(path: str = LIB_PATH):
                                      C.POINTER(EstimateInfo)]
     L.pdds_autotune.argtypes = [vp, C.POINTER(EstimateDesc), C.c_int32, C.POINTER(TuneInfo)]
     L.pdds_estimate_knot_steps.argtypes = [vp, C.POINTER(C.c_int64)]
+    L.pdds_estimate_step_histogram.argtypes = [vp, C.POINTER(C.c_int64)]
     L.pdds_estimate_knot_paths.argtypes = [vp, C.POINTER(C.c_int32)]
     L.pdds_subdomain_solve.argtypes = [vp, C.c_int32, dp, dp]
     L.pdds_solve_interface.argtypes = [vp, C.POINTER(SolveDesc), dp, C.POINTER(SolveInfo)]

@@ -227,9 +227,10 @@ class PDDSparseGM:
                                                     arr, C.byref(info)))
             sw, ne, nsub, fac = (dom[0], dom[1]), (dom[2], dom[3]), 0, (1.0, 1.0, 1.0, 1.0)
         elif circle is not None:
-            radius, nrings, nsectors, kappa = circle
+            radius, nrings, nsectors, kappa = circle[:4]
             d = capi.CircleDesc()
             d.radius, d.nrings, d.nsectors, d.nnode = float(radius), int(nrings), int(nsectors), int(nnode)
+            d.ring_ratio = float(circle[4]) if len(circle) > 4 else 0.0
             for i in range(4):
                 d.kappa[i] = float(kappa[i])
             self._check(self._lib.pdds_layout_build_circle(self._ctx, C.byref(d), C.byref(info)))
@@ -262,11 +263,12 @@ class PDDSparseGM:
 
     @classmethod
     def circle_mesh(cls, radius: float = 1.0, nrings: int = 6, nsectors: int = 16, nnode: int = 11,
-                    kappa=(3.164, 3.164, 3.164, 3.164), device: int = 0):
+                    kappa=(3.164, 3.164, 3.164, 3.164), device: int = 0, ring_ratio: float = 0.0):
         """Disk of the given radius split into nrings x nsectors annular
         sectors (MIXED mode, sigma = sqrt2 I problems); kappa[kind] scales
-        the RBF shape to each side's knot spacing."""
-        return cls(nnode=nnode, device=device, circle=(radius, nrings, nsectors, kappa))
+        the RBF shape to each side's knot spacing; ring i is ring_ratio^i as
+        wide as the central disk's radius (0: equal rings)."""
+        return cls(nnode=nnode, device=device, circle=(radius, nrings, nsectors, kappa, ring_ratio))
 
     @classmethod
     def from_stencils(cls, domain, x, y, stencils, knot_id=None, device: int = 0):
@@ -319,8 +321,12 @@ class PDDSparseGM:
                  bins_per_gap: int = 0, max_steps: int = 0, ipsi_override=None,
                  adaptive_h: bool = False, richardson: bool = False, reuse_tables: bool = False,
                  adaptive_n: bool = False, npaths_max: int = 0, target_stderr: float = 0.0,
-                 cta_threads: int = 0) -> Estimate:
+                 cta_threads: int = 0, plain_launch: bool = False) -> Estimate:
         """Runs the Feynman-Kac estimation of every knot's G row and B entry.
+
+        plain_launch: one CTA per work item, knots in layout order (the launch
+        the persistent CTAs and the heaviest-first order replace; for
+        comparison).
 
         adaptive_n: npaths is the pilot per knot; each knot then runs
         N_k = 4 Var_k / (0.66666 target_stderr)^2 paths (multiple of 256,
@@ -350,6 +356,7 @@ class PDDSparseGM:
         d.npaths_max = int(npaths_max)
         d.target_stderr = float(target_stderr)
         d.cta_threads = int(cta_threads)
+        d.plain_launch = int(bool(plain_launch))
         keep = None
         if ipsi_override is not None:
             keep = np.ascontiguousarray(ipsi_override, np.float64)
@@ -402,6 +409,13 @@ class PDDSparseGM:
         st = np.zeros(self.K, np.int64)
         self._check(self._lib.pdds_estimate_knot_steps(self._ctx, _p(st, C.c_int64)))
         return st
+
+    def step_histogram(self):
+        """Paths of the last MIXED estimate by exit step count: entry b counts
+        the paths (each Richardson level) that took 2^b .. 2^(b+1) - 1 steps."""
+        hst = np.zeros(32, np.int64)
+        self._check(self._lib.pdds_estimate_step_histogram(self._ctx, _p(hst, C.c_int64)))
+        return hst
 
     def subdomain_solve(self, m: int = 32, u=None):
         """Interior solution of every subdomain (the reference's Subdomain::Solve):

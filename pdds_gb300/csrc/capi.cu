@@ -263,6 +263,8 @@ pdds_status enqueue_prefix(pdds_ctx* ctx, const pdds_estimate_desc* desc, const 
   CK(cudaMemsetAsync(ctx->Bsum.p, 0, L.K * sizeof(double), s));
   CK(cudaMemsetAsync(ctx->BBsum.p, 0, L.K * sizeof(double), s));
   CK(cudaMemsetAsync(ctx->knot_steps.p, 0, L.K * sizeof(unsigned long long), s));
+  CK(ctx->step_hist.resize(32));
+  CK(cudaMemsetAsync(ctx->step_hist.p, 0, 32 * sizeof(unsigned long long), s));
   ctx->has_knot_steps = (mode == PDDS_MODE_MIXED);
   CK(launch_boundary_b(ctx->dl, P, mode, ctx->bnd_knots.p, ctx->n_bnd, ctx->B.p, ctx->BB.p, s));
   *launches += ctx->n_bnd > 0;
@@ -375,7 +377,7 @@ pdds_status enqueue_mixed_paths(pdds_ctx* ctx, const pdds_estimate_desc* desc, c
   // work items of the default split are handed out heaviest knot first: by
   // the steps per knot that the last estimate on this layout counted, or
   // before the first one by a geometric estimate of the steps per path
-  const bool lpt = !items && !ctx->is_batch;
+  const bool lpt = !items && !ctx->is_batch && !desc->plain_launch;
   if (lpt && !ctx->lpt_ready && ctx->L.geom == 0) {
     // E[steps] ~ tau / h_k: tau = tx ty / (tx + ty) combines the expected
     // exit times a (w - a) / 2 across the stencil in x and in y, h_k is the
@@ -415,6 +417,7 @@ pdds_status enqueue_mixed_paths(pdds_ctx* ctx, const pdds_estimate_desc* desc, c
   a.item_p1 = items ? items->p1 : nullptr;
   a.knot_invN = items ? items->knot_invN : nullptr;
   a.knot_steps = ctx->knot_steps.p;
+  a.step_hist = ctx->step_hist.p;
   const int threads = cta_threads_for(ctx, desc);
   const size_t smem = ctx->mixed_smem * (a.want_var ? 2 : 1) + mixed_queue_smem(threads, a.richardson);
   if (smem > 200 * 1024) return fail(ctx, PDDS_ERR_INVALID, "exit histograms exceed shared memory; lower bins_per_gap");
@@ -423,6 +426,7 @@ pdds_status enqueue_mixed_paths(pdds_ctx* ctx, const pdds_estimate_desc* desc, c
   if (ctx->force_bps > 0) bps = std::min(bps, ctx->force_bps);
   else if (tuned_for(ctx, desc)) bps = std::min(bps, ctx->tune_bps);
   int grid = std::max(1, std::min(n_items, bps * ctx->num_sms));
+  if (desc->plain_launch) grid = std::max(1, n_items);  // one CTA per work item
   if (ctx->force_grid_frac > 0.0 && ctx->force_grid_frac < 1.0)
     grid = std::max(1, std::min(grid, (int)std::lround(ctx->force_grid_frac * bps * ctx->num_sms)));
   if (n_items > 0) {
@@ -716,8 +720,9 @@ pdds_status pdds_layout_build_circle(pdds_ctx* ctx, const pdds_circle_desc* desc
   ctx->is_batch = false;
   ctx->n_inst = 0;
   ctx->has_batch_run = false;
+  if (!(desc->ring_ratio >= 0.0)) return fail(ctx, PDDS_ERR_INVALID, "ring_ratio must be >= 0");
   const std::string e = build_circle_layout(ctx->L, desc->radius, desc->nrings, desc->nsectors, desc->nnode,
-                                            desc->kappa, ctx->bins);
+                                            desc->kappa, ctx->bins, desc->ring_ratio > 0.0 ? desc->ring_ratio : 1.0);
   if (!e.empty()) return fail(ctx, PDDS_ERR_INVALID, e);
   ctx->has_layout = true;
   ctx->has_estimate = false;
@@ -1340,6 +1345,15 @@ pdds_status pdds_estimate_knot_steps(pdds_ctx* ctx, int64_t* steps) {
   if (!ctx->has_estimate || !ctx->has_knot_steps) return fail(ctx, PDDS_ERR_INVALID, "no MIXED estimate on this layout");
   CK(cudaSetDevice(ctx->device));
   CK(copy_async(steps, ctx->knot_steps.p, ctx->L.K * sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return PDDS_OK;
+}
+
+pdds_status pdds_estimate_step_histogram(pdds_ctx* ctx, int64_t* hist) {
+  if (!ctx || !hist) return PDDS_ERR_INVALID;
+  if (!ctx->has_estimate || !ctx->has_knot_steps) return fail(ctx, PDDS_ERR_INVALID, "no MIXED estimate on this layout");
+  CK(cudaSetDevice(ctx->device));
+  CK(copy_async(hist, ctx->step_hist.p, 32 * sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   return PDDS_OK;
 }

@@ -135,6 +135,7 @@ struct pdds_ctx {
   DBuf<double> knot_scale, knot_invN;
   std::vector<int> last_knot_N;  // paths per knot of the last estimate
   DBuf<unsigned long long> knot_steps;  // path steps per knot of the last MIXED estimate
+  DBuf<unsigned long long> step_hist;   // [32] paths by steps (log2 bins) of the last MIXED estimate
   DBuf<int> mc_lpt;               // MIXED hand-out order, heaviest knots first (from knot_steps)
   bool lpt_ready = false;
   bool has_knot_steps = false;

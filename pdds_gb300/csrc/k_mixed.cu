@@ -125,6 +125,7 @@ k_paths_mixed(const MixedArgs a) {
   __shared__ unsigned s_next_path;
   __shared__ double s_red[MIXED_MAX_THREADS / 32][4];
   __shared__ unsigned long long s_redi[MIXED_MAX_THREADS / 32][3];
+  __shared__ unsigned s_sth[32];  // this item's paths by steps (log2 bins), when step_hist is set
   // exit queue of each warp: word w of slot i at q[w][i]
   constexpr int QW = RICH ? 9 : 5;
   const int nthr = blockDim.x, nwarps = nthr >> 5;
@@ -223,6 +224,7 @@ k_paths_mixed(const MixedArgs a) {
     const float h = s_h, sqrth = s_sqrth;
     const int nh = a.want_var ? 2 * hist_len : hist_len;
     for (int i = tid; i < nh; i += nthr) hist[i] = 0.f;
+    if (tid < 32) s_sth[tid] = 0u;
     float* hist2 = hist + hist_len;
     __syncthreads();
 
@@ -542,6 +544,10 @@ k_paths_mixed(const MixedArgs a) {
         meta |= Cs.steps >= maxs ? 2u : 0u;
       }
       q[QW - 1][i] = __uint_as_float(meta);
+      if (a.step_hist && ex) {
+        atomicAdd(&s_sth[31 - __clz(max(F.steps, 1u))], 1u);
+        if (RICH) atomicAdd(&s_sth[31 - __clz(max(Cs.steps, 1u))], 1u);
+      }
       qcount += __popc(mk);
       return mk;
     };
@@ -680,6 +686,7 @@ k_paths_mixed(const MixedArgs a) {
       atomicAdd(a.stats + 2, tg);
       atomicAdd(a.stats + 3, tt);
     }
+    if (a.step_hist && tid < 32 && s_sth[tid]) atomicAdd(a.step_hist + tid, (unsigned long long)s_sth[tid]);
     // ------------------------------------------------------------ contract G
     const int64_t row0 = L.row_ptr[knot];
     const double invN = a.knot_invN ? a.knot_invN[knot] : a.inv_N;

@@ -52,6 +52,9 @@ struct MixedArgs {
   const int* item_p1;
   const double* knot_invN;
   unsigned long long* knot_steps;  // optional: path steps per knot (both levels)
+  // optional [32]: paths (each level of a Richardson pair counts) by their
+  // steps, bin b = steps in [2^b, 2^(b+1))
+  unsigned long long* step_hist;
 };
 
 struct Fp64Args {

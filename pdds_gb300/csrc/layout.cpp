@@ -106,15 +106,17 @@ double rect_dist(const double* p, double x, double y) {
 
 }  // namespace
 
-// Knot spacing of a side from its local coordinates: the first gap, or the
-// mean spacing when the first two knots coincide (caller-built stencils),
-// 1 for a single knot.
+// Knot spacing of a side from its local coordinates: the smallest positive
+// gap (sides of graded layouts and caller-built stencils are not uniform; a
+// uniform side's gaps agree to rounding), 1 for a single knot or knots that
+// all coincide.
 double side_gap(const std::vector<double>& t) {
-  const size_t n = t.size();
-  if (n < 2) return 1.0;
-  if (t[1] - t[0] > 0.0) return t[1] - t[0];
-  const double mean = (t[n - 1] - t[0]) / (double)(n - 1);
-  return mean > 0.0 ? mean : 1.0;
+  double g = 0.0;
+  for (size_t k = 1; k < t.size(); k++) {
+    const double d = t[k] - t[k - 1];
+    if (d > 0.0 && (g == 0.0 || d < g)) g = d;
+  }
+  return g > 0.0 ? g : 1.0;
 }
 
 void set_shape_bins(HostLayout& L, int bps) {

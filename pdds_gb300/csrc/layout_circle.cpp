@@ -44,11 +44,11 @@ struct PolarIface {
 // Stencils, sides, G rows and side shapes of a polar layout.  kst[v] =
 // {p, q, s, w}: rings [p, q), sectors [s, s + w) (s may be -1: angles are
 // unwrapped, sector indices taken modulo NS).
-std::string circle_stencils(HostLayout& L, double R, int NR, int NS, int n, const double kappa[4], int bps,
-                            const std::vector<PolarIface>& arcs, const std::vector<PolarIface>& rays,
-                            const std::vector<std::array<int, 4>>& kst) {
+std::string circle_stencils(HostLayout& L, const std::vector<double>& rad, int NR, int NS, int n,
+                            const double kappa[4], int bps, bool graded, const std::vector<PolarIface>& arcs,
+                            const std::vector<PolarIface>& rays, const std::vector<std::array<int, 4>>& kst) {
   const double PI = 3.141592653589793;
-  const double dth = 2.0 * PI / NS, drho = R / NR;
+  const double dth = 2.0 * PI / NS;
   const double STEN_ELONG = 0.5;
   auto wrap = [&](int j) { return ((j % NS) + NS) % NS; };
   const int K = L.K;
@@ -75,7 +75,7 @@ std::string circle_stencils(HostLayout& L, double R, int NR, int NS, int n, cons
   };
   auto arc_side = [&](int ring, int s, int w) {  // arc rho_ring over sectors [s, s + w)
     Pending P;
-    const double r = drho * ring;
+    const double r = rad[ring];
     auto iface = [&](int jj) -> const PolarIface& { return arcs[(size_t)ring * NS + wrap(jj)]; };
     auto shift = [&](int jj) { return dth * (jj - wrap(jj)); };
     {
@@ -128,9 +128,9 @@ std::string circle_stencils(HostLayout& L, double R, int NR, int NS, int n, cons
     const int p = st4[0], q = st4[1], s = st4[2], w = st4[3];
     const bool full = (w == NS);  // the disk of radius rho_q: one periodic arc side
     StencilRec st;
-    st.rect[0] = drho * p;
+    st.rect[0] = rad[p];
     st.rect[1] = dth * s;
-    st.rect[2] = drho * q;
+    st.rect[2] = rad[q];
     st.rect[3] = dth * (s + w);
     Pending sides[4];
     bool has[4] = {false, false, false, false};
@@ -139,7 +139,7 @@ std::string circle_stencils(HostLayout& L, double R, int NR, int NS, int n, cons
       if (q >= NR) return "internal: full-circle stencil on the boundary";
       Pending& P = sides[DIR_N];
       for (int jj = 0; jj < NS; jj++) add_from(P, arcs[(size_t)q * NS + jj], 0.0, 0,
-                                               (int)arcs[(size_t)q * NS + jj].index.size() - 1, true, drho * q);
+                                               (int)arcs[(size_t)q * NS + jj].index.size() - 1, true, rad[q]);
       P.kind = 3;
       has[DIR_N] = true;
     } else {
@@ -168,8 +168,15 @@ std::string circle_stencils(HostLayout& L, double R, int NR, int NS, int n, cons
       sr.n = (int)P.idx.size();
       sr.orient = arc ? 0 : 1;
       sr.kind = kd;
-      const double rr = arc ? drho * (d == DIR_N ? q : p) : 0.0;
-      const double spacing = arc ? 2.0 * rr * std::sin(0.5 * dth / (n - 1)) : drho / (n - 1);
+      const double rr = arc ? rad[d == DIR_N ? q : p] : 0.0;
+      double spacing = arc ? 2.0 * rr * std::sin(0.5 * dth / (n - 1)) : (rad[1] - rad[0]) / (n - 1);
+      if (graded && !arc) {  // a ray crosses rings of different widths: its finest spacing
+        spacing = 0.0;
+        for (size_t k = 1; k < P.along.size(); k++) {
+          const double g = P.along[k] - P.along[k - 1];
+          if (g > 0.0 && (spacing == 0.0 || g < spacing)) spacing = g;
+        }
+      }
       sr.c = kappa[kd] * spacing;
       sr.shape = -1;
       sr.knot_off = (int64_t)L.side_knot.size();
@@ -222,7 +229,7 @@ std::string circle_stencils(HostLayout& L, double R, int NR, int NS, int n, cons
     L.row_ptr[v + 1] = L.row_ptr[v] + len;
   }
   // shapes: sides equal up to rotation (arcs) or translation (rays)
-  std::map<std::tuple<int, int, long long, long long, long long, long long, long long>, int> shape_key;
+  std::map<std::tuple<int, int, long long, long long, long long, long long, long long, long long>, int> shape_key;
   std::vector<std::vector<std::pair<int, int>>> uses(L.sides.size());
   for (size_t si = 0; si < L.stencils.size(); si++)
     for (int d = 0; d < 4; d++)
@@ -231,6 +238,8 @@ std::string circle_stencils(HostLayout& L, double R, int NR, int NS, int n, cons
     SideRec& sr = L.sides[sd];
     std::vector<double> t(L.side_along.begin() + sr.knot_off, L.side_along.begin() + sr.knot_off + sr.n);
     const double gap = sr.n > 1 ? t[1] - t[0] : 1.0;
+    long long sig = 0;  // the knots' positions along the side (graded rays differ inside)
+    for (int k = 0; k < sr.n; k++) sig = sig * 1000003LL + std::llround(t[k] / gap * 1e6);
     double lo = 1e300, hi = -1e300;
     for (auto& u : uses[sd]) {
       const StencilRec& st = L.stencils[u.first];
@@ -247,7 +256,7 @@ std::string circle_stencils(HostLayout& L, double R, int NR, int NS, int n, cons
     const double Rs = sr.orient == 0 ? sr.fixed : 0.0;
     auto key = std::make_tuple(sr.n, sr.orient, (long long)std::llround(gap * 1e12), (long long)std::llround(sr.c * 1e12),
                                (long long)std::llround(Rs * 1e12), (long long)std::llround(lo / gap * 1e6),
-                               (long long)std::llround(hi / gap * 1e6));
+                               (long long)std::llround(hi / gap * 1e6), sig);
     auto it = shape_key.find(key);
     if (it == shape_key.end()) {
       ShapeRec sh;
@@ -275,7 +284,8 @@ std::string circle_stencils(HostLayout& L, double R, int NR, int NS, int n, cons
 
 }  // namespace
 
-std::string build_circle_layout(HostLayout& L, double R, int NR, int NS, int n, const double kappa[4], int bps) {
+std::string build_circle_layout(HostLayout& L, double R, int NR, int NS, int n, const double kappa[4], int bps,
+                                double ring_ratio) {
   if (!(R > 0.0)) return "circle layout needs R > 0";
   if (NR < 2 || NS < 3 || n < 3) return "circle layout needs nrings >= 2, nsectors >= 3, nnode >= 3";
   if (NS < 5) return "circle layout needs nsectors >= 5 (stencils span two sectors each side)";
@@ -291,7 +301,22 @@ std::string build_circle_layout(HostLayout& L, double R, int NR, int NS, int n, 
   for (int i = 0; i < 4; i++) L.fac[i] = kappa[i];
   const double PI = 3.141592653589793;
   const double dth = 2.0 * PI / NS, drho = R / NR;
-  auto rho = [&](int i) { return drho * i; };
+  // ring boundaries: equal rings, or ring i ring_ratio^i times as wide as the
+  // central disk's radius (the outer boundary exactly R)
+  const bool graded = ring_ratio != 1.0;
+  if (!(ring_ratio > 0.0)) return "circle layout needs ring_ratio > 0";
+  std::vector<double> rad(NR + 1);
+  {
+    double tot = 0.0, w = 1.0;
+    for (int i = 0; i < NR; i++, w *= ring_ratio) tot += w;
+    double acc = 0.0;
+    w = 1.0;
+    for (int i = 0; i <= NR; i++, w *= ring_ratio) {
+      rad[i] = graded ? (i == NR ? R : R * acc / tot) : drho * i;
+      acc += w;
+    }
+  }
+  auto rho = [&](int i) { return rad[i]; };
   auto theta = [&](int j) { return dth * j; };
   auto wrap = [&](int j) { return ((j % NS) + NS) % NS; };
   // ---- knots: cross points, arc interiors, ray interiors, boundary points
@@ -327,7 +352,7 @@ std::string build_circle_layout(HostLayout& L, double R, int NR, int NS, int n, 
       f.index.push_back(cross[(size_t)i * NS + j]);
       f.along.push_back(rho(i));
       for (int k = 1; k < n - 1; k++) {
-        const double r = rho(i) + drho * k / (n - 1);
+        const double r = rho(i) + (graded ? rad[i + 1] - rad[i] : drho) * k / (n - 1);
         f.index.push_back(add_knot(r, theta(j)));
         f.along.push_back(r);
       }
@@ -360,7 +385,7 @@ std::string build_circle_layout(HostLayout& L, double R, int NR, int NS, int n, 
       for (size_t k = 1; k + 1 < f.index.size(); k++) kst[f.index[k]] = {i, i + 1, j - 1, 2};
       if (i == NR - 1) kst[f.index.back()] = {i, i + 1, j - 1, 2};  // boundary knot: no paths, B = g
     }
-  return circle_stencils(L, R, NR, NS, n, kappa, bps, arcs, rays, kst);
+  return circle_stencils(L, rad, NR, NS, n, kappa, bps, graded, arcs, rays, kst);
 }
 
 }  // namespace pdds

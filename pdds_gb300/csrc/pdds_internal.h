@@ -132,8 +132,10 @@ std::string build_rect_layout(HostLayout& L, const double sw[2], const double ne
 // interfaces, sides elongated by half a segment as the rectangular rule
 // does.  kappa[kind] scales the RBF shape to the side's knot spacing:
 // c = kappa[kind] * chord between neighbouring side knots.
+// ring_ratio (0 or 1: equal rings): ring i is ring_ratio^i times as wide as
+// the central disk's radius.
 std::string build_circle_layout(HostLayout& L, double R, int nrings, int nsectors, int nnode,
-                                const double kappa[4], int bins_per_gap);
+                                const double kappa[4], int bins_per_gap, double ring_ratio = 1.0);
 
 // Block-diagonal union of independent layouts (a batch of instances): knots,
 // stencils, sides and shapes of part i follow those of part i-1 with all
