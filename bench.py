@@ -435,7 +435,7 @@ def circle_uneven(local: int, reps: int = 2, h: float = 2e-5):
     runs = []
     for r in range(reps + 1):
         est = pd.estimate(bvp, 1000, h, mode=P.MODE_MIXED, seed=1234, instance=r, adaptive_n=True,
-                          npaths_max=100_000, target_stderr=1e-3, **opts)
+                          npaths_max=100_000, target_stderr=1e-3, step_histogram=True, **opts)
         u, si = pd.solve_interface()
         if r > 0:
             runs.append((est, u, si))

@@ -243,6 +243,10 @@ typedef struct {
    * items) and the knots in layout order (not heaviest first).  Same
    * results up to FP32 summation order. */
   int32_t plain_launch;
+  /* MIXED only, 1: count the paths by their exit step counts for
+   * pdds_estimate_step_histogram (two shared-memory atomics per finished
+   * path pair; 0 leaves the histogram empty) */
+  int32_t step_histogram;
 } pdds_estimate_desc;
 
 typedef struct {
@@ -268,9 +272,9 @@ pdds_status pdds_estimate_knot_paths(pdds_ctx* ctx, int32_t* npaths);
 /* Euler-Maruyama steps per knot of the last MIXED pdds_estimate, summed
  * over its paths (both levels of a Richardson pair): steps[K]. */
 pdds_status pdds_estimate_knot_steps(pdds_ctx* ctx, int64_t* steps);
-/* Exit step counts of the last MIXED pdds_estimate: hist[b] paths (each level
- * of a Richardson pair counts) took between 2^b and 2^(b+1) - 1 steps,
- * b = 0 .. 31. */
+/* Exit step counts of the last MIXED pdds_estimate run with step_histogram:
+ * hist[b] paths (each level of a Richardson pair counts) took between 2^b
+ * and 2^(b+1) - 1 steps, b = 0 .. 31. */
 pdds_status pdds_estimate_step_histogram(pdds_ctx* ctx, int64_t* hist);
 
 /* One knot as EMFKACSolver::Solve_OMP_Analytic computes it
@@ -331,7 +335,19 @@ typedef struct {
    * grid-barrier wait before it gives up and the solve returns
    * PDDS_ERR_TIMEOUT (0 = 2^24, about a second; >= 0) */
   int32_t barrier_poll_limit;
+  /* PDDS_SOLVE_GMRES_FP32_IR: PDDS_GMRES_PIPELINED (0, the default) keeps
+   * G V beside the basis and applies each step's product to the not yet
+   * orthogonalised vector, one group barrier per Arnoldi step;
+   * PDDS_GMRES_CLASSICAL forms the basis vector first (two barriers) */
+  int32_t gmres_form;
+  /* GMRES over the whole GPU: its CTAs (0 = one per SM).  Each Arnoldi step
+   * is a chain of latency-bound phases over a few dozen rows per CTA; fewer
+   * CTAs make the barrier and the reductions over the CTAs' partials shorter */
+  int32_t grid_ctas;
 } pdds_solve_desc;
+
+#define PDDS_GMRES_PIPELINED 0
+#define PDDS_GMRES_CLASSICAL 1
 
 typedef struct {
   int32_t iterations;

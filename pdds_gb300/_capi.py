@@ -77,7 +77,7 @@ class EstimateDesc(C.Structure):
                 ("ipsi_override", C.POINTER(C.c_double)), ("ipsi_override_len", C.c_int64),
                 ("adaptive_h", C.c_int32), ("richardson", C.c_int32), ("reuse_tables", C.c_int32),
                 ("adaptive_n", C.c_int32), ("npaths_max", C.c_int32), ("target_stderr", C.c_double),
-                ("cta_threads", C.c_int32), ("plain_launch", C.c_int32)]
+                ("cta_threads", C.c_int32), ("plain_launch", C.c_int32), ("step_histogram", C.c_int32)]
 
 
 class EstimateInfo(C.Structure):
@@ -95,7 +95,11 @@ class TuneInfo(C.Structure):
 
 class SolveDesc(C.Structure):
     _fields_ = [("method", C.c_int32), ("restart", C.c_int32), ("max_iter", C.c_int32),
-                ("max_refine", C.c_int32), ("tol", C.c_double), ("barrier_poll_limit", C.c_int32)]
+                ("max_refine", C.c_int32), ("tol", C.c_double), ("barrier_poll_limit", C.c_int32),
+                ("gmres_form", C.c_int32), ("grid_ctas", C.c_int32)]
+
+
+GMRES_PIPELINED, GMRES_CLASSICAL = 0, 1
 
 
 class SolveInfo(C.Structure):

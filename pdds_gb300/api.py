@@ -321,7 +321,7 @@ class PDDSparseGM:
                  bins_per_gap: int = 0, max_steps: int = 0, ipsi_override=None,
                  adaptive_h: bool = False, richardson: bool = False, reuse_tables: bool = False,
                  adaptive_n: bool = False, npaths_max: int = 0, target_stderr: float = 0.0,
-                 cta_threads: int = 0, plain_launch: bool = False) -> Estimate:
+                 cta_threads: int = 0, plain_launch: bool = False, step_histogram: bool = False) -> Estimate:
         """Runs the Feynman-Kac estimation of every knot's G row and B entry.
 
         plain_launch: one CTA per work item, knots in layout order (the launch
@@ -357,6 +357,7 @@ class PDDSparseGM:
         d.target_stderr = float(target_stderr)
         d.cta_threads = int(cta_threads)
         d.plain_launch = int(bool(plain_launch))
+        d.step_histogram = int(bool(step_histogram))
         keep = None
         if ipsi_override is not None:
             keep = np.ascontiguousarray(ipsi_override, np.float64)
@@ -521,9 +522,12 @@ class PDDSparseGM:
                       bvp.u(self.x, self.y))
 
     def solve_interface(self, method: int = capi.SOLVE_GMRES_FP32_IR, tol: float = 1e-10,
-                        restart: int = 20, max_iter: int = 0, max_refine: int = 0, barrier_poll_limit: int = 0):
+                        restart: int = 20, max_iter: int = 0, max_refine: int = 0, barrier_poll_limit: int = 0,
+                        gmres_form: int = capi.GMRES_PIPELINED, grid_ctas: int = 0):
         """Solves (I + G) u = B for the last estimate; returns (u, info)."""
         d = capi.SolveDesc()
+        d.gmres_form = int(gmres_form)
+        d.grid_ctas = int(grid_ctas)
         d.method = int(method)
         d.restart = int(restart)
         d.max_iter = int(max_iter)
@@ -788,7 +792,8 @@ class Batch:
 
     def run(self, npaths: int, h: float, seed: int = 1234, instance: int = 0, adaptive_h: bool = True,
             richardson: bool = False, tol: float = 1e-10, restart: int = 30, use_graph: bool = True,
-            bins_per_gap: int = 0, reuse_tables: bool = False, dup_sum: bool = False, waves: int = 0) -> dict:
+            bins_per_gap: int = 0, reuse_tables: bool = False, dup_sum: bool = False, waves: int = 0,
+            gmres_form: int = capi.GMRES_PIPELINED) -> dict:
         """Estimates and solves every instance (in `waves` consecutive groups
         whose solves overlap the next group's paths; 0 = 16); returns the run
         counters."""
@@ -809,6 +814,7 @@ class Batch:
         d.solve.tol = float(tol)
         d.use_graph = int(bool(use_graph))
         d.waves = int(waves)
+        d.solve.gmres_form = int(gmres_form)
         info = capi.BatchRunInfo()
         self._check(self._lib.pdds_batch_run(self._ctx, C.byref(d), C.byref(info)))
         return {f: getattr(info, f) for f, _ in capi.BatchRunInfo._fields_}

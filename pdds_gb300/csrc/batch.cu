@@ -50,6 +50,7 @@ pdds_status enqueue_batch(pdds_ctx* ctx, const pdds_batch_run_desc* d, int clust
   a.x = ctx->su.p;
   a.r64 = ctx->sv64.p;
   a.V = ctx->sV32.p;
+  a.Z = d->solve.gmres_form == PDDS_GMRES_PIPELINED ? ctx->sZ32.p : nullptr;
   a.m = std::max(2, std::min(d->solve.restart > 0 ? d->solve.restart : 30, GMRES_CLUSTER_MAX_M));
   a.max_iter = d->solve.max_iter > 0 ? d->solve.max_iter : 1000;
   a.max_refine = d->solve.max_refine > 0 ? d->solve.max_refine : 30;
@@ -214,12 +215,13 @@ pdds_status pdds_batch_run(pdds_ctx* ctx, const pdds_batch_run_desc* desc, pdds_
   const int64_t nnz = L.row_ptr[L.K];
   const int m = std::max(2, std::min(desc->solve.restart > 0 ? desc->solve.restart : 30, GMRES_CLUSTER_MAX_M));
   // buffers first: a captured graph holds their addresses
-  const void* before[4] = {ctx->sV32.p, ctx->sval32.p, ctx->sv64.p, ctx->su.p};
+  const void* before[5] = {ctx->sV32.p, ctx->sval32.p, ctx->sv64.p, ctx->su.p, ctx->sZ32.p};
   CK(ctx->sV32.resize((size_t)(m + 1) * K));
+  if (desc->solve.gmres_form == PDDS_GMRES_PIPELINED) CK(ctx->sZ32.resize((size_t)(m + 1) * K));
   CK(ctx->sval32.resize(std::max<int64_t>(nnz, 1)));
   CK(ctx->sv64.resize(std::max<int64_t>(K, 1) * 6));
   CK(ctx->su.resize(std::max<int64_t>(K, 1)));
-  const void* after[4] = {ctx->sV32.p, ctx->sval32.p, ctx->sv64.p, ctx->su.p};
+  const void* after[5] = {ctx->sV32.p, ctx->sval32.p, ctx->sv64.p, ctx->su.p, ctx->sZ32.p};
   if (std::memcmp(before, after, sizeof(before)) != 0) drop_graph(ctx);
   // the graph is reused while the descriptor, the cluster size and the solve
   // scratch (which pdds_solve_interface may also reallocate) are unchanged;

@@ -417,14 +417,14 @@ pdds_status enqueue_mixed_paths(pdds_ctx* ctx, const pdds_estimate_desc* desc, c
   a.item_p1 = items ? items->p1 : nullptr;
   a.knot_invN = items ? items->knot_invN : nullptr;
   a.knot_steps = ctx->knot_steps.p;
-  a.step_hist = ctx->step_hist.p;
+  a.step_hist = desc->step_histogram ? ctx->step_hist.p : nullptr;
   const int threads = cta_threads_for(ctx, desc);
   const size_t smem = ctx->mixed_smem * (a.want_var ? 2 : 1) + mixed_queue_smem(threads, a.richardson);
   if (smem > 200 * 1024) return fail(ctx, PDDS_ERR_INVALID, "exit histograms exceed shared memory; lower bins_per_gap");
   int bps = mixed_blocks_per_sm(P.kind, smem, a.richardson, threads);
   if (bps < 1) bps = 1;
   if (ctx->force_bps > 0) bps = std::min(bps, ctx->force_bps);
-  else if (tuned_for(ctx, desc)) bps = std::min(bps, ctx->tune_bps);
+  else if (tuned_for(ctx, desc) && !items) bps = std::min(bps, ctx->tune_bps);  // the shape it was timed on
   int grid = std::max(1, std::min(n_items, bps * ctx->num_sms));
   if (desc->plain_launch) grid = std::max(1, n_items);  // one CTA per work item
   if (ctx->force_grid_frac > 0.0 && ctx->force_grid_frac < 1.0)
@@ -455,11 +455,14 @@ pdds_status adaptive_continue(pdds_ctx* ctx, const pdds_estimate_desc* desc, con
   const int nmax = std::max(N0, desc->npaths_max > 0 ? desc->npaths_max : 100000);
   const double eps = desc->target_stderr > 0 ? desc->target_stderr : 1e-3;
   std::vector<double> bs(K), bbs(K);
+  std::vector<unsigned long long> pst(K);
   CK(copy_async(bs.data(), ctx->Bsum.p, K * sizeof(double), cudaMemcpyDeviceToHost, s));
   CK(copy_async(bbs.data(), ctx->BBsum.p, K * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(copy_async(pst.data(), ctx->knot_steps.p, K * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   std::vector<int> kn(K, 0), ik, ip0, ip1;
   std::vector<double> scale(K, 1.0), inv(K, 0.0);
+  std::vector<std::pair<double, int>> cost;  // the continuation's steps per knot, from the pilot
   const int granule = 256, ppc = 2048;
   for (int v : L.order) {
     if (L.knot_boundary[v]) continue;
@@ -472,10 +475,16 @@ pdds_status adaptive_continue(pdds_ctx* ctx, const pdds_estimate_desc* desc, con
     kn[v] = (int)nk;
     scale[v] = (double)N0 / (double)nk;
     inv[v] = 1.0 / (double)nk;
-    for (long long p = N0; p < nk; p += ppc) {
+    if (nk > N0) cost.push_back({-(double)pst[v] * (double)(nk - N0) / (double)N0, v});
+  }
+  // work items heaviest knot first, so that no long item starts near the end
+  std::stable_sort(cost.begin(), cost.end());
+  for (auto& c : cost) {
+    const int v = c.second;
+    for (long long p = N0; p < kn[v]; p += ppc) {
       ik.push_back(v);
       ip0.push_back((int)p);
-      ip1.push_back((int)std::min<long long>(nk, p + ppc));
+      ip1.push_back((int)std::min<long long>(kn[v], p + ppc));
     }
   }
   ctx->last_knot_N = kn;
@@ -589,6 +598,7 @@ pdds_status pdds_destroy(pdds_ctx* ctx) {
     ctx->stats.release();
     ctx->errf.release();
     ctx->sV32.release();
+    ctx->sZ32.release();
     ctx->sw32.release();
     ctx->sval32.release();
     ctx->sctl.release();
@@ -1395,6 +1405,8 @@ pdds_status pdds_solve_interface(pdds_ctx* ctx, const pdds_solve_desc* desc, dou
   SolveWork w{};
   w.err = ctx->errf.p;
   w.spin_limit = (unsigned)desc->barrier_poll_limit;
+  if (desc->grid_ctas < 0) return fail(ctx, PDDS_ERR_INVALID, "grid_ctas must be >= 0");
+  w.grid_ctas = desc->grid_ctas;
   CK(cudaMemsetAsync(ctx->errf.p, 0, sizeof(unsigned), s));
   for (int q = 0; q < 6; q++) w.v64[q] = ctx->sv64.p + (size_t)q * K;
   w.scal = ctx->sscal.p;
@@ -1415,6 +1427,8 @@ pdds_status pdds_solve_interface(pdds_ctx* ctx, const pdds_solve_desc* desc, dou
     CK(ctx->sV32.resize((size_t)(m + 1) * K));
     CK(ctx->sw32.resize(std::max(K, 1)));
     CK(ctx->sval32.resize(std::max<int64_t>(nnz, 1)));
+    if (desc->gmres_form == PDDS_GMRES_PIPELINED) CK(ctx->sZ32.resize((size_t)(m + 1) * K));
+    w.Z32 = desc->gmres_form == PDDS_GMRES_PIPELINED ? ctx->sZ32.p : nullptr;
     w.V32 = ctx->sV32.p;
     w.w32 = ctx->sw32.p;
     w.val32 = ctx->sval32.p;

@@ -88,7 +88,7 @@ struct pdds_ctx {
   DBuf<int64_t> task_out, knot_task_off, knot_ipsi_off;
   // solve scratch
   DBuf<double> sv64, sscal, spart, shess, su;
-  DBuf<float> sV32, sw32, sval32;
+  DBuf<float> sV32, sw32, sval32, sZ32;
   DBuf<unsigned> sctl, sbar;
   DBuf<double> sgpart;
   double* host_rr = nullptr;

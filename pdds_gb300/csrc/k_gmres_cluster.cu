@@ -457,16 +457,324 @@ __device__ __forceinline__ void gmres_body(const ClusterGmresArgs& a, Group& grp
   }
 }
 
+// Pipelined GMRES(m): one group barrier per Arnoldi step.
+//
+// The Krylov space of I + G is the one of G, so the Arnoldi process runs on
+// G, and the Hessenberg matrix of I + G is the one of G plus the identity.
+// Besides the basis V it keeps Z = G V.  Step j (after the barrier that ends
+// step j - 1, at which t_j = G v_{j-1} = Z[j-1] is complete in every CTA and
+// its dots with v_0 .. v_{j-1} and |t_j|^2 are reduced) forms column j - 1
+// of the Hessenberg matrix, h_i = v_i . t_j and beta = |t_j - V h|, and then,
+// for its own rows:
+//   the product a = G t_j (t_j staged whole in shared memory),
+//   v_j = (t_j - sum_i h_i v_i) / beta  and  z_j = (a - sum_i h_i z_i) / beta,
+// since G v_j = (G t_j - sum_i h_i G v_i) / beta; z_j is the next t.  Its
+// dots with v_0 .. v_j and |z_j|^2 go into the step's one reduction, whose
+// barrier also publishes V[j] and Z[j].  The classical two-barrier step
+// needs the reduced h before it can form v_j and a second barrier before the
+// product of v_j; here the product is applied to t_j, which is complete one
+// barrier earlier.  The recurrence for z_j carries the rounding of earlier
+// steps (the Arnoldi relation holds only to that accuracy): the FP64
+// residual of every refinement step is formed from the FP64 G, so that
+// error costs inner iterations, not accuracy.
+template <class Group>
+__device__ __forceinline__ void gmres_body_p1(const ClusterGmresArgs& a, Group& grp) {
+  const unsigned crank = grp.rank(), csize = grp.size();
+  const int sys = grp.system();
+  if (sys >= a.n_sys) return;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int R0 = a.sys_row0[sys], R1 = a.sys_row0[sys + 1];
+  const int nr = R1 - R0;
+  const int per = (nr + (int)csize - 1) / (int)csize;
+  const int r0 = min(R1, R0 + (int)crank * per), r1 = min(R1, r0 + per);
+  const int nown = r1 - r0;
+  const int m = a.m;
+  const int64_t K = a.K;
+
+  extern __shared__ __align__(16) unsigned char s_dyn[];
+  float* s_w = reinterpret_cast<float*>(s_dyn);  // own rows of the product G t
+  const size_t wbytes = ((size_t)per * sizeof(float) + 15) & ~(size_t)15;
+  float* s_vf = reinterpret_cast<float*>(s_dyn + wbytes);    // system vector, FP32
+  double* s_vd = reinterpret_cast<double*>(s_dyn + wbytes);  // system iterate, FP64
+  __shared__ float2 s_slot[2][CG_MAXV + 2];
+  __shared__ float2 s_red[CG_MAXV + 2];
+  __shared__ float s_H[CG_MAXV * CG_MAXM];  // column j at s_H[j * (m + 1)]
+  __shared__ float s_cs[CG_MAXM], s_sn[CG_MAXM], s_g[CG_MAXV], s_y[CG_MAXM];
+  __shared__ float s_h[CG_MAXV];            // h_i of the current column (G part)
+  __shared__ float2 s_bsum[CG_WARPS];
+  __shared__ int s_flag[2];
+  __shared__ float s_inv;
+  __shared__ double s_beta[2];
+  int parity = 0;
+
+  bool alive = true;
+  auto allreduce = [&](int nv) {
+    alive = grp.reduce(&s_slot[parity][0], nv, s_red, parity) && alive;
+    parity ^= 1;
+  };
+  auto block_sum = [&](float2 v) {
+    v = warp_sum_df(v);
+    if (lane == 0) s_bsum[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+      const float2 t = warp_sum_df(s_bsum[lane]);
+      if (lane == 0) s_slot[parity][0] = t;
+    }
+    __syncthreads();
+  };
+  // own-row dots of y (global, own rows at y + r0) with V[0 .. nv) into
+  // s_slot[parity][0 .. nv) and |y|^2 into s_slot[parity][nv]
+  auto dots_and_norm = [&](const float* y, int nv) {
+    {
+      float2 pn = make_float2(0.f, 0.f);
+      for (int r = tid; r < nown; r += CG_THREADS) pn = df_add(pn, df_sq(__ldcg(y + r0 + r)));
+      pn = warp_sum_df(pn);
+      if (lane == 0) s_bsum[warp] = pn;
+    }
+    for (int i = warp; i < nv; i += CG_WARPS) {
+      const float* Vi = a.V + (int64_t)i * K + r0;
+      float acc = 0.f;
+      for (int q = lane; q < nown; q += 32) acc = fmaf(__ldcg(Vi + q), __ldcg(y + r0 + q), acc);
+      const float2 t = warp_sum_df(make_float2(acc, 0.f));
+      if (lane == 0) s_slot[parity][i] = t;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      const float2 t = warp_sum_df(s_bsum[lane]);
+      if (lane == 0) s_slot[parity][nv] = t;
+    }
+    __syncthreads();
+  };
+  // s_w = G x over the own rows, x (FP32, the whole system vector) staged first
+  auto spmv_g = [&](const float* x) {
+    const float* xs = x + R0;
+    for (int i0 = tid; i0 < nr; i0 += CG_THREADS * 8) {
+      float t[8];
+#pragma unroll
+      for (int u = 0; u < 8; u++) t[u] = i0 + CG_THREADS * u < nr ? __ldcg(xs + i0 + CG_THREADS * u) : 0.f;
+#pragma unroll
+      for (int u = 0; u < 8; u++)
+        if (i0 + CG_THREADS * u < nr) s_vf[i0 + CG_THREADS * u] = t[u];
+    }
+    __syncthreads();
+    for (int r = r0 + warp; r < r1; r += CG_WARPS) {
+      float acc0 = 0.f, acc1 = 0.f;
+      const int64_t e1 = a.row_ptr[r + 1];
+      for (int64_t e = a.row_ptr[r] + lane; e < e1; e += 32 * SPMV_U) {
+        float v[SPMV_U];
+        int c[SPMV_U];
+#pragma unroll
+        for (int u = 0; u < SPMV_U; u++) {
+          const bool in = e + 32 * u < e1;
+          v[u] = in ? __ldg(a.val32 + e + 32 * u) : 0.f;
+          c[u] = in ? __ldg(a.col + e + 32 * u) - R0 : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < SPMV_U; u += 2) {
+          acc0 = fmaf(v[u], s_vf[c[u]], acc0);
+          acc1 = fmaf(v[u + 1], s_vf[c[u + 1]], acc1);
+        }
+      }
+      float acc = acc0 + acc1;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      if (lane == 0) s_w[r - r0] = acc;
+    }
+    __syncthreads();
+  };
+
+  // ||b||^2 and x = 0
+  {
+    double bb = 0.0;
+    for (int r = r0 + tid; r < r1; r += CG_THREADS) {
+      const double v = a.b[r];
+      bb += v * v;
+      a.x[r] = 0.0;
+    }
+    block_sum(df_from(bb));
+    allreduce(1);
+  }
+  const double bnorm2 = df_val(s_red[0]);
+  int total = 0, ref = 0;
+  double rr = bnorm2;
+  if (bnorm2 > 0.0 && alive) {
+    const double tol2 = a.tol * a.tol * bnorm2;
+    for (ref = 0;; ref++) {
+      // FP64 residual r = b - x - G x of the own rows
+      for (int i0 = tid; i0 < nr; i0 += CG_THREADS * 4) {
+        double t[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) t[u] = i0 + CG_THREADS * u < nr ? __ldcg(a.x + R0 + i0 + CG_THREADS * u) : 0.0;
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+          if (i0 + CG_THREADS * u < nr) s_vd[i0 + CG_THREADS * u] = t[u];
+      }
+      __syncthreads();
+      double prr = 0.0;
+      for (int r = r0 + warp; r < r1; r += CG_WARPS) {
+        double acc0 = 0.0, acc1 = 0.0;
+        const int64_t e1 = a.row_ptr[r + 1];
+        for (int64_t e = a.row_ptr[r] + lane; e < e1; e += 32 * 4) {
+          double v[4];
+          int c[4];
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            const bool in = e + 32 * u < e1;
+            v[u] = in ? __ldg(a.val64 + e + 32 * u) : 0.0;
+            c[u] = in ? __ldg(a.col + e + 32 * u) - R0 : 0;
+          }
+          acc0 += v[0] * s_vd[c[0]];
+          acc1 += v[1] * s_vd[c[1]];
+          acc0 += v[2] * s_vd[c[2]];
+          acc1 += v[3] * s_vd[c[3]];
+        }
+        const double acc = warp_sum(acc0 + acc1);
+        if (lane == 0) {
+          const double rv = a.b[r] - s_vd[r - R0] - acc;
+          a.r64[r] = rv;
+          prr += rv * rv;
+        }
+      }
+      block_sum(df_from(prr));
+      allreduce(1);
+      rr = df_val(s_red[0]);
+      if (!(rr > tol2) || ref >= a.max_refine || total >= a.max_iter || !alive) break;
+      if (tid == 0) {
+        s_beta[0] = sqrt(rr);
+        s_beta[1] = 1.0 / s_beta[0];
+        for (int i = 0; i <= m; i++) s_g[i] = 0.f;
+        s_g[0] = 1.f;
+      }
+      __syncthreads();
+      const double beta = s_beta[0], ibeta = s_beta[1];
+      // v0 = r / |r| over the own rows; the next group barrier publishes it
+      for (int r = r0 + tid; r < r1; r += CG_THREADS) a.V[r] = (float)(a.r64[r] * ibeta);
+      alive = grp.sync() && alive;
+      int jdim = 0;
+      for (int j = 0;; j++) {
+        if (j >= 1) {
+          // column j - 1 from the reduced dots of t_j (s_red[0 .. j), |t_j|^2
+          // at s_red[j]): h_i, beta = |t_j - V h|, Givens update (one lane)
+          if (warp == CG_WARPS - 1) {
+            float2 hh = make_float2(0.f, 0.f);
+            for (int i = lane; i < j; i += 32) {
+              float2 t = df_sq(s_red[i].x);
+              t.y = fmaf(2.f * s_red[i].x, s_red[i].y, t.y);
+              hh = df_add(hh, t);
+              s_h[i] = s_red[i].x;
+            }
+            hh = warp_sum_df(hh);
+            if (lane == 0) {
+              const float2 d = df_add(s_red[j], make_float2(-hh.x, -hh.y));
+              const float hn = sqrtf(fmaxf(d.x + d.y, 0.f));
+              float* col = s_H + (j - 1) * (m + 1);
+              for (int i = 0; i < j; i++) col[i] = s_red[i].x;
+              col[j - 1] += 1.f;  // the identity of I + G
+              col[j] = hn;
+              for (int i = 0; i < j - 1; i++) {
+                const float p = col[i], q = col[i + 1];
+                col[i] = s_cs[i] * p + s_sn[i] * q;
+                col[i + 1] = -s_sn[i] * p + s_cs[i] * q;
+              }
+              const float p = col[j - 1], q = col[j];
+              const float rho = sqrtf(p * p + q * q);
+              s_cs[j - 1] = rho > 0.f ? p / rho : 1.f;
+              s_sn[j - 1] = rho > 0.f ? q / rho : 0.f;
+              col[j - 1] = rho;
+              col[j] = 0.f;
+              s_g[j] = -s_sn[j - 1] * s_g[j - 1];
+              s_g[j - 1] = s_cs[j - 1] * s_g[j - 1];
+              s_flag[0] = (fabsf(s_g[j]) <= (float)a.inner_tol || !(hn > 0.f)) ? 1 : 0;
+              s_inv = hn > 0.f ? 1.f / hn : 0.f;
+            }
+          }
+          __syncthreads();
+          jdim = j;
+          if (s_flag[0] || j >= m || total >= a.max_iter || !alive) break;
+        }
+        // a = G t_j (t_0 = v_0)
+        const float* tj = j == 0 ? a.V : a.Z + (int64_t)(j - 1) * K;
+        spmv_g(tj);
+        float* vj = a.V + (int64_t)j * K;
+        float* zj = a.Z + (int64_t)j * K;
+        if (j == 0) {
+          for (int r = tid; r < nown; r += CG_THREADS) zj[r0 + r] = s_w[r];
+        } else {
+          // v_j and z_j of the own rows: the j basis terms of a row are split
+          // over pp lanes of one warp (a CTA has a few dozen rows and 1024
+          // threads: one thread per row would wait on j dependent loads)
+          const float inv = s_inv;
+          int pp = 1;
+          while (pp < 32 && pp < j && 2 * pp * nown <= CG_THREADS) pp *= 2;
+          const int rows_w = 32 / pp, part = lane & (pp - 1);
+          for (int base = warp * rows_w; base < nown; base += CG_WARPS * rows_w) {
+            const int r = base + lane / pp;
+            float v = 0.f, z = 0.f;
+            if (r < nown) {
+              for (int i = part; i < j; i += pp) {
+                const float hi = s_h[i];
+                v = fmaf(-hi, __ldcg(a.V + (int64_t)i * K + r0 + r), v);
+                z = fmaf(-hi, __ldcg(a.Z + (int64_t)i * K + r0 + r), z);
+              }
+            }
+            for (int o = pp >> 1; o > 0; o >>= 1) {
+              v += __shfl_xor_sync(0xffffffffu, v, o);
+              z += __shfl_xor_sync(0xffffffffu, z, o);
+            }
+            if (r < nown && part == 0) {
+              vj[r0 + r] = (__ldcg(tj + r0 + r) + v) * inv;
+              zj[r0 + r] = (s_w[r] + z) * inv;
+            }
+          }
+          __syncthreads();
+        }
+        // dots of t_{j+1} = z_j with v_0 .. v_j and |z_j|^2, one reduction
+        // (its barrier also publishes V[j] and Z[j])
+        __syncthreads();
+        dots_and_norm(zj, j + 1);
+        allreduce(j + 2);
+        ++total;
+      }
+      // y = H^-1 g (upper triangular, FP32), x += beta V y (FP64 iterate)
+      if (tid == 0) {
+        for (int i = jdim - 1; i >= 0; i--) {
+          float sacc = s_g[i];
+          for (int k = i + 1; k < jdim; k++) sacc -= s_H[k * (m + 1) + i] * s_y[k];
+          const float d = s_H[i * (m + 1) + i];
+          s_y[i] = d != 0.f ? sacc / d : 0.f;
+        }
+      }
+      __syncthreads();
+      for (int r = r0 + tid; r < r1; r += CG_THREADS) {
+        float acc = 0.f;
+#pragma unroll 4
+        for (int i = 0; i < jdim; i++) acc = fmaf(s_y[i], __ldcg(a.V + (int64_t)i * K + r), acc);
+        a.x[r] += beta * (double)acc;
+      }
+      alive = grp.sync() && alive;  // x complete before the next residual
+    }
+  }
+  if (alive) grp.sync();  // no CTA leaves while another may still read its shared memory
+  if (crank == 0 && tid == 0) {
+    a.out_iters[sys] = total;
+    a.out_refines[sys] = ref;
+    a.out_relres[sys] = !alive ? -1.0 : (bnorm2 > 0.0 ? sqrt(rr / bnorm2) : 0.0);
+    if (a.out_t_end) a.out_t_end[sys] = global_ns();
+  }
+}
+
 __global__ void __launch_bounds__(CG_THREADS, 1) k_gmres_cluster(const ClusterGmresArgs a) {
   ClusterGroup grp;
-  gmres_body(a, grp);
+  if (a.Z) gmres_body_p1(a, grp);
+  else gmres_body(a, grp);
 }
 
 // One system over the whole grid (cooperative launch, one CTA per SM).
 __global__ void __launch_bounds__(CG_THREADS, 1) k_gmres_grid(const ClusterGmresArgs a, unsigned* bar,
                                                               unsigned* err, double* gpart) {
   GridGroup grp{bar, err, gpart, a.spin_limit ? a.spin_limit : GRID_SPIN_LIMIT};
-  gmres_body(a, grp);
+  if (a.Z) gmres_body_p1(a, grp);
+  else gmres_body(a, grp);
 }
 
 __global__ void k_stamp(unsigned long long* t) { *t = global_ns(); }

@@ -544,10 +544,6 @@ k_paths_mixed(const MixedArgs a) {
         meta |= Cs.steps >= maxs ? 2u : 0u;
       }
       q[QW - 1][i] = __uint_as_float(meta);
-      if (a.step_hist && ex) {
-        atomicAdd(&s_sth[31 - __clz(max(F.steps, 1u))], 1u);
-        if (RICH) atomicAdd(&s_sth[31 - __clz(max(Cs.steps, 1u))], 1u);
-      }
       qcount += __popc(mk);
       return mk;
     };
@@ -643,6 +639,10 @@ k_paths_mixed(const MixedArgs a) {
         if (lane == leader) base = atomicAdd(&s_next_path, (unsigned)__popc(dm));
         base = __shfl_sync(FULL, base, leader);
         if (done) {
+          if (a.step_hist) {  // finished pairs only: a few lanes per iteration
+            atomicAdd(&s_sth[31 - __clz(max(F.steps, 1u))], 1u);
+            if (RICH) atomicAdd(&s_sth[31 - __clz(max(Cs.steps, 1u))], 1u);
+          }
           nsteps += F.steps + (RICH ? Cs.steps : 0u);
           path = base + __popc(dm & lt);
           active = (int)path < path_end;

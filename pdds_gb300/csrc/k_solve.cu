@@ -533,7 +533,8 @@ cudaError_t solve_gmres_ir_cluster(const SolveCsr& A, const double* b, double* x
   const int n = A.K;
   if (m < 2 || m > GMRES_CLUSTER_MAX_M) return cudaSuccess;
   // large systems: the whole GPU with grid barriers; small ones: one cluster
-  const int gb = (n >= 4096 && w.bar && w.gpart && w.err) ? gmres_grid_blocks(n) : 0;
+  int gb = (n >= 4096 && w.bar && w.gpart && w.err) ? gmres_grid_blocks(n) : 0;
+  if (gb > 0 && w.grid_ctas > 0) gb = std::min(gb, w.grid_ctas);
   const int cl = gb > 0 ? 0 : gmres_cluster_pick(n);
   if (gb <= 0 && cl <= 0) return cudaSuccess;
   *used = true;
@@ -554,6 +555,7 @@ cudaError_t solve_gmres_ir_cluster(const SolveCsr& A, const double* b, double* x
   a.x = x;
   a.r64 = w.v64[0];
   a.V = w.V32;
+  a.Z = w.Z32;
   a.m = m;
   a.max_iter = max_iter;
   a.max_refine = max_refine;

@@ -20,6 +20,7 @@ struct SolveWork {
   double* part;     // reduction partials, >= 2*256 and 48*64 doubles
   double* hess;     // (m+1)m + 2m + 4(m+1) doubles
   float* V32;       // (m+1) K floats
+  float* Z32;       // (m+1) K floats (pipelined GMRES; null: the two-barrier step)
   float* w32;       // K floats
   float* val32;     // nnz floats
   double* host_rr;  // pinned host scalar
@@ -27,6 +28,7 @@ struct SolveWork {
   unsigned* bar;    // 2 unsigned: grid barrier count and generation
   double* gpart;    // grid-reduction partials, 2 * SMs * (GMRES_CLUSTER_MAX_M + 3)
   unsigned spin_limit;  // grid-barrier polls before a wait gives up (0: the default)
+  int grid_ctas;        // CTAs of the whole-GPU solve (0: one per SM)
   int launches;     // kernels launched by the last solve
 };
 
@@ -48,6 +50,7 @@ struct ClusterGmresArgs {
   double* x;
   double* r64;           // K
   float* V;              // (m + 1) K
+  float* Z;              // (m + 1) K: G V, the pipelined one-barrier step (null: two barriers per step)
   int m;
   int max_iter;
   int max_refine;
