@@ -385,6 +385,24 @@ def varcoef_lut(local: int, reps: int = 2):
         ms.append(est.info["ms_paths"])
         steps = est.info["path_steps"]
     rmse = float(np.sqrt(np.mean((u - bvp.u(pd.x, pd.y)) ** 2)))
+    # the Catmull-Rom node sampler (the FP64 form's) in the MIXED path kernel
+    cr = P.BVP(P.BVP.LUT, (1.0,), tables=bvp.tables, exact=bvp.exact)
+    pd.estimate(cr, 256, w["h"], mode=P.MODE_MIXED, **opts)
+    ms_cr = []
+    for r in range(reps):
+        est_cr = pd.estimate(cr, w["npaths"], w["h"], mode=P.MODE_MIXED, seed=1234, instance=r, **opts)
+        u_cr, _ = pd.solve_interface()
+        ms_cr.append(est_cr.info["ms_paths"])
+    rmse_cr = float(np.sqrt(np.mean((u_cr - bvp.u(pd.x, pd.y)) ** 2)))
+    # hardware-filtered bilinear interpolation of the nodes
+    bl = P.BVP(P.BVP.LUT, (2.0,), tables=bvp.tables, exact=bvp.exact)
+    pd.estimate(bl, 256, w["h"], mode=P.MODE_MIXED, **opts)
+    ms_bl = []
+    for r in range(reps):
+        est_bl = pd.estimate(bl, w["npaths"], w["h"], mode=P.MODE_MIXED, seed=1234, instance=r, **opts)
+        u_bl, _ = pd.solve_interface()
+        ms_bl.append(est_bl.info["ms_paths"])
+    rmse_bl = float(np.sqrt(np.mean((u_bl - bvp.u(pd.x, pd.y)) ** 2)))
     e64 = pd.estimate(bvp, 2000, w["h"], mode=P.MODE_FP64, seed=1234, **opts)
     e32 = pd.estimate(bvp, 2000, w["h"], mode=P.MODE_MIXED, seed=1234, **opts)
     # the error against the FP64 form at the benchmark's 5e4 paths, on 16
@@ -402,9 +420,16 @@ def varcoef_lut(local: int, reps: int = 2):
             r0, r1 = full.row_ptr[k], full.row_ptr[k + 1]
             gerr = max(gerr, float(np.max(np.abs(full.val[r0:r1] - G))))
             berr = max(berr, abs(float(full.B[k] - B)))
-    out = {"knots": int(pd.K), "paths_per_knot": w["npaths"], "h": w["h"], "table": "1024^2 x 8 FP32, bicubic",
+    out = {"knots": int(pd.K), "paths_per_knot": w["npaths"], "h": w["h"],
+           "table": "1024^2 x 8 FP32; MIXED: cubic B-spline from textures",
            "ms_paths": float(np.mean(ms)), "path_steps_per_s": steps / (1e-3 * float(np.mean(ms))),
            "rmse_vs_analytic": rmse, "solve_ms": float(si["ms"]),
+           "catmull_rom_nodes": {"ms_paths": float(np.mean(ms_cr)),
+                                 "path_steps_per_s": est_cr.info["path_steps"] / (1e-3 * float(np.mean(ms_cr))),
+                                 "rmse_vs_analytic": rmse_cr},
+           "bilinear_texture": {"ms_paths": float(np.mean(ms_bl)),
+                                "path_steps_per_s": est_bl.info["path_steps"] / (1e-3 * float(np.mean(ms_bl))),
+                                "rmse_vs_analytic": rmse_bl},
            "fp64": {"paths_per_knot": 2000, "ms_paths": e64.info["ms_paths"],
                     "mixed_over_fp64": (e32.info["path_steps"] / e32.info["ms_paths"]) /
                                        (e64.info["path_steps"] / e64.info["ms_paths"]),
@@ -543,6 +568,8 @@ def main():
     ap.add_argument("--no-lut", action="store_true")
     ap.add_argument("--no-config1", action="store_true")
     ap.add_argument("--no-robin", action="store_true")
+    ap.add_argument("--lut-sampler", default="bspline", choices=["bspline", "catmull_rom", "bilinear"],
+                    help="MIXED table sampler of the table-served workload")
     args = ap.parse_args()
 
     from pdds_gb300.config import WORKLOADS, fac_rule
@@ -570,7 +597,7 @@ def main():
 
     if workload.get("problem") == "varcoef_lut":
         bvp = P.BVP.varcoef_lut(workload["lut_n"], (workload["sw"][0], workload["sw"][1],
-                                                     workload["ne"][0], workload["ne"][1]))
+                                                     workload["ne"][0], workload["ne"][1]), sampler=args.lut_sampler)
     else:
         bvp = P.BVP.poisson_sincos()
     N, h = workload["npaths"], workload["h"]
@@ -743,6 +770,8 @@ def main():
         "gpu_launches": int(launches),
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
     }
+    if workload.get("problem") == "varcoef_lut":
+        line["config"]["lut_sampler"] = args.lut_sampler
     line.update(extra)
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -87,8 +87,17 @@ pdds_status pdds_problem_set(pdds_ctx* ctx, const pdds_problem_desc* desc);
  * LUT texture, BVPs/LUT2.cuh:11-92).  coef is host memory [ny][nx][8] FP32,
  * fields (sigma11, sigma22, b1, b2, c, f, du/dx, du/dy) on the grid
  * x_i = bounds[0] + i (bounds[2]-bounds[0])/(nx-1), y_j likewise; g is
- * [ny][nx] FP32 boundary values.  Sampled with bicubic Catmull-Rom
- * interpolation, clamped at the table edges.  Copied to the device. */
+ * [ny][nx] FP32 boundary values.  Copied to the device.  The FP64 and
+ * replay forms sample the tables with bicubic Catmull-Rom interpolation,
+ * clamped at the table edges.  The MIXED (FP32) form samples by problem
+ * p[0]: 0 the cubic B-spline through the nodes (coefficients prefiltered
+ * here, in FP64, held as two float4 textures; four linearly filtered fetches
+ * per texture and sample), 1 the Catmull-Rom nodes (16 node loads), 2
+ * bilinear interpolation of the nodes (one filtered fetch per texture).
+ * All pass through the nodes; between them they differ by interpolation
+ * error, O(node spacing^3) for the cubics and O(node spacing^2) for the
+ * bilinear one, and the texture filter's 8-bit blend fractions add at most
+ * 1/512 of the difference of neighbouring values. */
 pdds_status pdds_problem_set_lut(pdds_ctx* ctx, const float* coef, const float* g, int32_t nx, int32_t ny,
                                  const double bounds[4]);
 
@@ -247,6 +256,19 @@ typedef struct {
    * pdds_estimate_step_histogram (two shared-memory atomics per finished
    * path pair; 0 leaves the histogram empty) */
   int32_t step_histogram;
+  /* 1: per-knot diagnostic sums of the reduction for
+   * pdds_estimate_diagnostics (all modes; MIXED on rectangular stencils) */
+  int32_t diagnostics;
+  /* Only the knots with paths at hand-out positions [knot_first,
+   * knot_first + knot_count) (knot_count 0: to the last); the others' rows
+   * and B are left zero (boundary knots always take B = g).  A knot's
+   * results depend only on its own Philox streams, so a run split into
+   * ranges gives every knot the values of one whole run: bit for bit in the
+   * replay mode, up to summation order in FP64 and MIXED (a knot's paths
+   * may be split into other chunks).  The unit of checkpoint/resume.  Not
+   * with adaptive_n, batches or the autotuner. */
+  int32_t knot_first;
+  int32_t knot_count;
 } pdds_estimate_desc;
 
 typedef struct {
@@ -267,7 +289,8 @@ typedef struct {
  * B[K], BB[K] (mean of the squared score, as Reduce_Analytic's BB). */
 pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double* val, double* var,
                           double* B, double* BB, pdds_estimate_info* info);
-/* Paths per knot of the last pdds_estimate (npaths[K]; 0 for boundary knots). */
+/* Paths per knot of the last pdds_estimate (npaths[K]; 0 for boundary knots
+ * and for knots outside its knot range). */
 pdds_status pdds_estimate_knot_paths(pdds_ctx* ctx, int32_t* npaths);
 /* Euler-Maruyama steps per knot of the last MIXED pdds_estimate, summed
  * over its paths (both levels of a Richardson pair): steps[K]. */
@@ -276,6 +299,40 @@ pdds_status pdds_estimate_knot_steps(pdds_ctx* ctx, int64_t* steps);
  * hist[b] paths (each level of a Richardson pair counts) took between 2^b
  * and 2^(b+1) - 1 steps, b = 0 .. 31. */
 pdds_status pdds_estimate_step_histogram(pdds_ctx* ctx, int64_t* hist);
+
+/* Per-knot diagnostic sums of Reduce_Analytic (the sums[] of
+ * Solvers/EMFKACSolver.hpp:14-47, accumulated at :542-558 and turned into
+ * moments by Update, :656-685), over the knot's paths, with
+ * phi = Z + Y g(X_tau) the score without the control variate and xi the
+ * control variate, at the end of the linear leg (exit by the Gobet-shifted
+ * rule) and of the sublinear leg (the reference's continuation to the first
+ * step outside the stencil; the replay mode runs it, the FP64 and MIXED
+ * modes do not, and their sublinear sums repeat the linear ones).  tau is
+ * the elapsed time, steps x h (the reference starts its clock at +infinity
+ * and counts down, so its tau sums are infinite).  The reference's enum
+ * gives xi and xi^2 one slot (XiLinear2 = XiLinear); here they have two.
+ * With Richardson pairs each pair adds 2 x fine - coarse of phi and xi (the
+ * pair's estimate) and the fine level's tau.  MIXED sums FP32 values in
+ * FP64 shared-memory atomics; the replay mode sums in path order, in FP64,
+ * like the reference's serial loop. */
+enum {
+  PDDS_DIAG_SCORE = 0,        /* sum phi                       (ScoreLinear)     */
+  PDDS_DIAG_SCORE2 = 1,       /* sum phi^2                     (ScoreLinear2)    */
+  PDDS_DIAG_XI = 2,           /* sum xi                        (XiLinear)        */
+  PDDS_DIAG_XI2 = 3,          /* sum xi^2                      (XiLinear2)       */
+  PDDS_DIAG_SCORE_VR = 4,     /* sum (phi + xi)                (ScoreLinearVR)   */
+  PDDS_DIAG_SCORE_VR2 = 5,    /* sum (phi + xi)^2              (ScoreLinearVR2)  */
+  PDDS_DIAG_XI_SCORE = 6,     /* sum xi phi                    (XiScoreLinear)   */
+  PDDS_DIAG_TAU = 7,          /* sum tau                       (tauLinear)       */
+  PDDS_DIAG_SUB = 8,          /* + 0..7: the same sums of the sublinear leg      */
+  PDDS_DIAG_RNG = 16,         /* normal variates drawn, 2 per step (RNGCalls)    */
+  PDDS_DIAG_PATHS = 17,       /* paths summed (a Richardson pair counts once)    */
+  PDDS_DIAG_N = 18
+};
+/* The diagnostic sums of the last pdds_estimate (or pdds_estimate_knot) run
+ * with diagnostics = 1: sums[K * PDDS_DIAG_N], knot k's at k * PDDS_DIAG_N
+ * (zeros for knots without paths). */
+pdds_status pdds_estimate_diagnostics(pdds_ctx* ctx, double* sums);
 
 /* One knot as EMFKACSolver::Solve_OMP_Analytic computes it
  * (Solvers/EMFKACSolver.hpp:711-729): from X0 = (x0, y0) inside the stencil

@@ -278,8 +278,12 @@ class EMFKACSolver {
     if (ctx_) pdds_destroy(ctx_);
   }
 
-  pdds_estimate_desc options;  // mode, seed, instance, dup_sum, want_var, ipsi_override, ...
+  pdds_estimate_desc options;  // mode, seed, instance, dup_sum, want_var, ipsi_override, diagnostics, ...
   int32_t knot_id = 0;         // Philox knot word of the knot
+  // the reduction's diagnostic sums of the last solve, slots PDDS_DIAG_*
+  // (the reference's sums[] member, Solvers/EMFKACSolver.hpp:60); filled
+  // when options.diagnostics is set
+  double sums[PDDS_DIAG_N] = {};
 
   void Solve_GPU_Analytic(std::array<double, 2> X0, unsigned int N_tray, double time_discretization, double rho,
                           const pdds_problem_desc& BoundaryValueProblem, Stencil& stencil_knot, double c2,
@@ -304,6 +308,7 @@ class EMFKACSolver {
     G.resize(nnz);
     G_var.resize(nnz);
     G_j.assign(gj.begin(), gj.begin() + nnz);
+    if (d.diagnostics) check(pdds_estimate_diagnostics(ctx_, sums), "pdds_estimate_diagnostics");
   }
 
   const pdds_estimate_info& info() const { return info_; }

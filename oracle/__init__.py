@@ -22,6 +22,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
 
 POISSON_SINCOS, MONEGROS, HELMHOLTZ, VARCOEF, LUT = 0, 1, 2, 3, 4
+DIAG_N = 18  # diagnostic sums per knot (orc_run_diag)
 
 
 class Problem(C.Structure):
@@ -81,6 +82,7 @@ def lib():
                                      C.POINTER(C.c_int32)]
         L.orc_run.argtypes = [vp, C.POINTER(Problem), C.POINTER(Params), ip, dp, dp, C.c_int, ip,
                               ip, dp, dp, C.c_int64, dp, dp, i64p]
+        L.orc_run_diag.argtypes = [vp, C.POINTER(Problem), C.POINTER(Params), ip, dp, dp, C.c_int, dp]
         L.orc_bicgstab.argtypes = [C.c_int, C.c_int64, ip, ip, dp, dp, dp, C.c_int, C.c_double, ip, dp]
         L.orc_set_lut.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int, C.c_int, dp]
         L.orc_problem_u.restype = C.c_double
@@ -228,6 +230,18 @@ class Layout:
         nnz = int(rp[-1])
         return dict(status=rc, knots=kn, x=x0, y=y0, row_ptr=rp, gj=gj[:nnz], g=g[:nnz],
                     gvar=gv[:nnz], B=B, BB=BB, stats=st)
+
+    def run_diag(self, problem: Problem, prm: Params, knots=None):
+        """Diagnostic sums of Reduce_Analytic per knot of the hand-out list (or
+        a subset of its positions): (status, knots, sums [nk, DIAG_N])."""
+        sel = np.arange(len(self.work_idx)) if knots is None else np.asarray(knots)
+        kn = np.ascontiguousarray(self.work_idx[sel], np.int32)
+        x0 = np.ascontiguousarray(self.work_x[sel])
+        y0 = np.ascontiguousarray(self.work_y[sel])
+        sums = np.zeros((len(kn), DIAG_N))
+        rc = lib().orc_run_diag(self._h, C.byref(problem), C.byref(prm), _p(kn, C.c_int), _p(x0, C.c_double),
+                                _p(y0, C.c_double), len(kn), _p(sums, C.c_double))
+        return rc, kn, sums
 
 
 def ipsi(x, y, c, portable=False):

@@ -300,7 +300,8 @@ double rbf(double ax, double ay, double bx, double by, double c) {
 }
 
 struct PathOut {
-  double x, y, Y, Z, xi;
+  double x, y, Y, Z, xi;       // end of the linear leg (projection, weights)
+  double sx, sy, sY, sZ, sxi;  // end of the sublinear leg (the linear one's when it does not run)
   int32_t steps_l, steps_s;
   int status;
 };
@@ -360,6 +361,8 @@ PathOut run_path(const Problem<M>& pb, const double* sp, double x0, double y0, d
     } while (inside(0.0));
   }
   o.steps_s = (int32_t)ns;
+  // X_tau_sublin etc. of Simulate_OMP (EMFKACSolver.hpp:205-209)
+  o.sx = ns ? E[0] : o.x; o.sy = ns ? E[1] : o.y; o.sY = Y; o.sZ = Z; o.sxi = xi;
   return o;
 }
 
@@ -439,7 +442,7 @@ template <class M>
 int knot_impl(const Layout& L, const orc_problem* P, const orc_params* prm, int knot, double x0,
               double y0, const double* ipsi_in, std::vector<int>& gj, std::vector<double>& g,
               std::vector<double>& gvar, double* B, double* BB, int64_t* stats,
-              std::vector<PathOut>* paths_out) {
+              std::vector<PathOut>* paths_out, double* diag) {
   Problem<M> pb{P};
   Stencil st = compute_stencil(L, knot);
   SideData sd[4];
@@ -610,6 +613,38 @@ int knot_impl(const Layout& L, const orc_problem* P, const orc_params* prm, int 
   }
   *B = b / N;
   *BB = bb / N;
+  if (diag) {
+    // the diagnostic sums of Reduce_Analytic (EMFKACSolver.hpp:542-558), paths
+    // in order, xi and xi^2 in their own slots (the reference's enum gives
+    // them one, :22-25) and tau = steps x h (the reference's clock starts at
+    // +infinity, :145, and counts down, FKACIntegrator.hpp:56)
+    for (int q = 0; q < ORC_DIAG_N; q++) diag[q] = 0.0;
+    for (int n = 0; n < N; n++) {
+      const PathOut& o = paths[n];
+      const double phl = o.Z + o.Y * pb.g(o.x, o.y);
+      const double phs = o.sZ + o.sY * pb.g(o.sx, o.sy);
+      const double xl = o.xi, xs = o.sxi;
+      const double sl = (double)o.steps_l, ss = sl + (double)o.steps_s;
+      diag[0] += phl;
+      diag[8] += phs;
+      diag[1] += phl * phl;
+      diag[9] += phs * phs;
+      diag[2] += xl;
+      diag[10] += xs;
+      diag[3] += xl * xl;
+      diag[11] += xs * xs;
+      diag[4] += phl + xl;
+      diag[12] += phs + xs;
+      diag[5] += (phl + xl) * (phl + xl);
+      diag[13] += (phs + xs) * (phs + xs);
+      diag[6] += xl * phl;
+      diag[14] += xs * phs;
+      diag[16] += 2.0 * ss;  // RNGCalls: 2 normals per step, both legs
+      diag[7] += sl * h;
+      diag[15] += ss * h;
+      diag[17] += 1.0;
+    }
+  }
   if (paths_out) paths_out->swap(paths);
   return status;
 }
@@ -685,13 +720,13 @@ int orc_ipsi_ex(int n, const double* x, const double* y, double c, int portable,
 static int knot_dispatch(const void* Lv, const orc_problem* P, const orc_params* prm, int knot,
                          double x0, double y0, const double* ipsi_in, std::vector<int>& gj,
                          std::vector<double>& g, std::vector<double>& gv, double* B, double* BB,
-                         int64_t* stats, std::vector<PathOut>* po) {
+                         int64_t* stats, std::vector<PathOut>* po, double* diag = nullptr) {
   const Layout& L = *(const Layout*)Lv;
   if (prm->portable) {
     if (P->kind == ORC_MONEGROS) return 2;  // libm-only problem
-    return knot_impl<PortMath>(L, P, prm, knot, x0, y0, ipsi_in, gj, g, gv, B, BB, stats, po);
+    return knot_impl<PortMath>(L, P, prm, knot, x0, y0, ipsi_in, gj, g, gv, B, BB, stats, po, diag);
   }
-  return knot_impl<LibmMath>(L, P, prm, knot, x0, y0, ipsi_in, gj, g, gv, B, BB, stats, po);
+  return knot_impl<LibmMath>(L, P, prm, knot, x0, y0, ipsi_in, gj, g, gv, B, BB, stats, po, diag);
 }
 
 int orc_knot(const void* Lv, const orc_problem* P, const orc_params* prm, int knot, double x0,
@@ -742,6 +777,22 @@ int orc_run(const void* Lv, const orc_problem* P, const orc_params* prm, const i
     for (size_t i = 0; i < vj.size(); i++, pos++) { gj[pos] = vj[i]; g[pos] = vg[i]; gvar[pos] = vv[i]; }
     row_ptr[k + 1] = (int)pos;
     for (int q = 0; q < 4; q++) stats[q] += st[q];
+  }
+  return status;
+}
+
+int orc_run_diag(const void* Lv, const orc_problem* P, const orc_params* prm, const int* knots,
+                 const double* x0, const double* y0, int nk, double* sums) {
+  int status = 0;
+  std::vector<int> vj;
+  std::vector<double> vg, vv;
+  for (int k = 0; k < nk; k++) {
+    int64_t st[4];
+    double B, BB;
+    double* d = sums + (size_t)k * ORC_DIAG_N;
+    for (int q = 0; q < ORC_DIAG_N; q++) d[q] = 0.0;
+    const int s = knot_dispatch(Lv, P, prm, knots[k], x0[k], y0[k], nullptr, vj, vg, vv, &B, &BB, st, nullptr, d);
+    if (s) status = s;
   }
   return status;
 }

@@ -73,6 +73,14 @@ int orc_knot(const void* L, const orc_problem* P, const orc_params* prm, int kno
 int orc_knot_paths(const void* L, const orc_problem* P, const orc_params* prm, int knot,
                    double x0, double y0, double* xl, double* yl, double* Yl, double* Zl,
                    double* xil, int32_t* steps_l, int32_t* steps_s);
+/* Diagnostic sums of Reduce_Analytic per knot of a list (Solvers/
+ * EMFKACSolver.hpp:542-558): sums[k * ORC_DIAG_N + q], q in the order
+ * phi, phi^2, xi, xi^2, phi+xi, (phi+xi)^2, xi phi, tau of the linear leg,
+ * the same 8 of the sublinear leg, normals drawn, paths (zeros for a knot
+ * on the domain boundary). */
+enum { ORC_DIAG_N = 18 };
+int orc_run_diag(const void* L, const orc_problem* P, const orc_params* prm, const int* knots,
+                 const double* x0, const double* y0, int nk, double* sums);
 /* All knots of a list, in order.  Row k of G occupies [row_ptr[k], row_ptr[k+1]). */
 int orc_run(const void* L, const orc_problem* P, const orc_params* prm, const int* knots,
             const double* x0, const double* y0, int nk, int* row_ptr, int* gj, double* g,

@@ -28,8 +28,13 @@ EXPORTS = [
     "pdds_estimate", "pdds_estimate_knot_paths", "pdds_estimate_knot_steps", "pdds_autotune", "pdds_solve_interface",
     "pdds_subdomain_solve", "pdds_semilinear_tables", "pdds_batch_build", "pdds_batch_run", "pdds_batch_instance",
     "pdds_solve_bicgstab_static", "pdds_check_philox", "pdds_check_portable_math", "pdds_stencils_set",
-    "pdds_estimate_knot", "pdds_estimate_step_histogram",
+    "pdds_estimate_knot", "pdds_estimate_step_histogram", "pdds_estimate_diagnostics",
 ]
+# per-knot diagnostic sums (pdds_estimate_diagnostics), in slot order
+DIAG_N = 18
+DIAG_NAMES = ("score", "score2", "xi", "xi2", "score_vr", "score_vr2", "xi_score", "tau",
+              "sub_score", "sub_score2", "sub_xi", "sub_xi2", "sub_score_vr", "sub_score_vr2", "sub_xi_score",
+              "sub_tau", "rng", "paths")
 STATIC_SOLVE_MAX_K = 131072
 PHILOX_PORTABLE, PHILOX_ROUND_KEYS = 0, 1
 FN_EXP, FN_LOG, FN_SIN, FN_COS, FN_BOX_MULLER_Z0, FN_BOX_MULLER_Z1 = range(6)
@@ -77,7 +82,8 @@ class EstimateDesc(C.Structure):
                 ("ipsi_override", C.POINTER(C.c_double)), ("ipsi_override_len", C.c_int64),
                 ("adaptive_h", C.c_int32), ("richardson", C.c_int32), ("reuse_tables", C.c_int32),
                 ("adaptive_n", C.c_int32), ("npaths_max", C.c_int32), ("target_stderr", C.c_double),
-                ("cta_threads", C.c_int32), ("plain_launch", C.c_int32), ("step_histogram", C.c_int32)]
+                ("cta_threads", C.c_int32), ("plain_launch", C.c_int32), ("step_histogram", C.c_int32),
+                ("diagnostics", C.c_int32), ("knot_first", C.c_int32), ("knot_count", C.c_int32)]
 
 
 class EstimateInfo(C.Structure):
@@ -165,6 +171,7 @@ def load(path: str = LIB_PATH):
     L.pdds_autotune.argtypes = [vp, C.POINTER(EstimateDesc), C.c_int32, C.POINTER(TuneInfo)]
     L.pdds_estimate_knot_steps.argtypes = [vp, C.POINTER(C.c_int64)]
     L.pdds_estimate_step_histogram.argtypes = [vp, C.POINTER(C.c_int64)]
+    L.pdds_estimate_diagnostics.argtypes = [vp, C.POINTER(C.c_double)]
     L.pdds_estimate_knot_paths.argtypes = [vp, C.POINTER(C.c_int32)]
     L.pdds_subdomain_solve.argtypes = [vp, C.c_int32, dp, dp]
     L.pdds_solve_interface.argtypes = [vp, C.POINTER(SolveDesc), dp, C.POINTER(SolveInfo)]

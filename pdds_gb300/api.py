@@ -76,20 +76,29 @@ class BVP:
     def varcoef(cls):
         return cls(cls.VARCOEF)
 
-    @classmethod
-    def lut(cls, coef, g, bounds, exact=None):
-        """Problem with diagonal sigma, b, c, f, grad u and g served from FP32
-        tables (bicubic Catmull-Rom); coef [ny][nx][8], g [ny][nx]."""
-        import numpy as np
-        return cls(cls.LUT, tables=(np.ascontiguousarray(coef, np.float32),
-                                    np.ascontiguousarray(g, np.float32), tuple(bounds)), exact=exact)
+    SAMPLERS = ("bspline", "catmull_rom", "bilinear")  # problem p[0] = position
 
     @classmethod
-    def varcoef_lut(cls, n: int = 1024, bounds=(0.0, 0.0, 1.0, 1.0)):
+    def lut(cls, coef, g, bounds, exact=None, sampler: str = "bspline"):
+        """Problem with diagonal sigma, b, c, f, grad u and g served from FP32
+        tables; coef [ny][nx][8], g [ny][nx].  The FP64 and replay forms sample
+        them with bicubic Catmull-Rom interpolation; the MIXED form with the
+        interpolating cubic B-spline from textures (sampler "bspline"), the
+        same Catmull-Rom node sampler ("catmull_rom") or hardware-filtered
+        bilinear interpolation of the nodes ("bilinear")."""
+        import numpy as np
+        if sampler not in cls.SAMPLERS:
+            raise ValueError(f"sampler must be one of {cls.SAMPLERS}")
+        return cls(cls.LUT, (float(cls.SAMPLERS.index(sampler)),),
+                   tables=(np.ascontiguousarray(coef, np.float32), np.ascontiguousarray(g, np.float32),
+                           tuple(bounds)), exact=exact)
+
+    @classmethod
+    def varcoef_lut(cls, n: int = 1024, bounds=(0.0, 0.0, 1.0, 1.0), sampler: str = "bspline"):
         """The variable-coefficient problem served from n x n tables."""
         from .config import varcoef_tables
         coef, g, b = varcoef_tables(n, bounds)
-        return cls.lut(coef, g, b, exact=lambda x, y: np.exp(x) * np.cos(2 * y) + 1.0)
+        return cls.lut(coef, g, b, exact=lambda x, y: np.exp(x) * np.cos(2 * y) + 1.0, sampler=sampler)
 
     def desc(self) -> capi.ProblemDesc:
         d = capi.ProblemDesc()
@@ -185,11 +194,51 @@ class Estimate:
     BB: np.ndarray
     info: dict = field(default_factory=dict)
     npaths: np.ndarray = None  # paths per knot (0 for boundary knots)
+    diag: np.ndarray = None    # [K, DIAG_N] diagnostic sums (estimate(diagnostics=True))
 
     @property
     def B_var(self):
         """The reference's signed B_var = B^2 - BB (PDDSparseGM.cpp:833)."""
         return self.B * self.B - self.BB
+
+    def knot_metadata(self) -> dict:
+        """Per-knot columns of the reference's knot_metadata.csv
+        (Process_Metadata, PDDAlgorithms/PDDSparseGM.cpp:3092-3155) from the
+        diagnostic sums, as its iterative loops fill them (:4049-4069) after
+        Update (Solvers/EMFKACSolver.hpp:656-685), with the analytic
+        reduction's sums: APL = mean tau, RNGCalls = normals drawn, the
+        plain and control-variate score variances, the correlation of the
+        score with xi at the linear (PCoeff_old) and sublinear (PCoeff_new)
+        exit, and the sublinear-minus-linear score (bias_num, bias_trap).
+        WCtime is 0: the reference's collection of per-knot times is
+        commented out (:3015-3018).  Knots without paths give NaN moments."""
+        if self.diag is None:
+            raise ValueError("no diagnostics: run estimate(..., diagnostics=True)")
+        s = np.asarray(self.diag, np.float64)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            m = s / s[:, capi.DIAG_N - 1:capi.DIAG_N]
+            ix = {n: i for i, n in enumerate(capi.DIAG_NAMES)}
+            phi, phiphi = m[:, ix["score"]], m[:, ix["score2"]]
+            xi, xixi = m[:, ix["xi"]], m[:, ix["xi2"]]
+            vr, vrvr = m[:, ix["score_vr"]], m[:, ix["score_vr2"]]
+            xiphi = m[:, ix["xi_score"]]
+            phs, phsphs, xiphs = m[:, ix["sub_score"]], m[:, ix["sub_score2"]], m[:, ix["sub_xi_score"]]
+            sd_xi = np.sqrt(xixi - xi * xi)
+            var_plain = phiphi - phi * phi
+            var_vr = vrvr - vr * vr
+            return {
+                "APL": m[:, ix["tau"]],
+                "WCtime": np.zeros(len(s)),
+                "RNGCalls": s[:, ix["rng"]],
+                "Estimated_Variance": var_plain,
+                "Estimated_Variance_VR": var_vr,
+                "PCoeff_old": (xiphi - phi * xi) / (np.sqrt(var_plain) * sd_xi),
+                "PCoeff_new": (xiphs - phs * xi) / (np.sqrt(phsphs - phs * phs) * sd_xi),
+                "Var_Plain": var_plain,
+                "Var_VR": var_vr,
+                "bias_num": phs - phi,
+                "bias_trap": phs - phi,
+            }
 
     def triplets(self):
         rows = np.repeat(np.arange(len(self.row_ptr) - 1), np.diff(self.row_ptr))
@@ -260,6 +309,7 @@ class PDDSparseGM:
                                               _p(self.col, C.c_int32)))
         self.col = self.col[:info.nnz]
         self.nnz = int(info.nnz)
+        self.n_mc = K - int(info.nboundary)  # knots with paths (hand-out positions of a knot range)
 
     @classmethod
     def circle_mesh(cls, radius: float = 1.0, nrings: int = 6, nsectors: int = 16, nnode: int = 11,
@@ -321,8 +371,17 @@ class PDDSparseGM:
                  bins_per_gap: int = 0, max_steps: int = 0, ipsi_override=None,
                  adaptive_h: bool = False, richardson: bool = False, reuse_tables: bool = False,
                  adaptive_n: bool = False, npaths_max: int = 0, target_stderr: float = 0.0,
-                 cta_threads: int = 0, plain_launch: bool = False, step_histogram: bool = False) -> Estimate:
+                 cta_threads: int = 0, plain_launch: bool = False, step_histogram: bool = False,
+                 diagnostics: bool = False, knot_first: int = 0, knot_count: int = 0) -> Estimate:
         """Runs the Feynman-Kac estimation of every knot's G row and B entry.
+
+        knot_first, knot_count: only the knots with paths at these hand-out
+        positions (count 0: to the last; n_mc = K - nboundary positions);
+        the others' rows stay zero and Estimate.npaths is 0 for them (the
+        unit of pdds_gb300.checkpoint.estimate_resumable).
+
+        diagnostics: also the reduction's per-knot diagnostic sums
+        (Estimate.diag, Estimate.knot_metadata(); pdds_estimate_diagnostics).
 
         plain_launch: one CTA per work item, knots in layout order (the launch
         the persistent CTAs and the heaviest-first order replace; for
@@ -358,6 +417,9 @@ class PDDSparseGM:
         d.cta_threads = int(cta_threads)
         d.plain_launch = int(bool(plain_launch))
         d.step_histogram = int(bool(step_histogram))
+        d.diagnostics = int(bool(diagnostics))
+        d.knot_first = int(knot_first)
+        d.knot_count = int(knot_count)
         keep = None
         if ipsi_override is not None:
             keep = np.ascontiguousarray(ipsi_override, np.float64)
@@ -382,8 +444,12 @@ class PDDSparseGM:
         del keep
         kn = np.zeros(self.K, np.int32)
         self._check(self._lib.pdds_estimate_knot_paths(self._ctx, _p(kn, C.c_int32)))
+        dg = None
+        if diagnostics:
+            dg = np.zeros((self.K, capi.DIAG_N))
+            self._check(self._lib.pdds_estimate_diagnostics(self._ctx, _p(dg, C.c_double)))
         return Estimate(self.row_ptr, self.col, val[:self.nnz], var[:self.nnz], B, BB,
-                        {f: getattr(info, f) for f, _ in capi.EstimateInfo._fields_}, kn)
+                        {f: getattr(info, f) for f, _ in capi.EstimateInfo._fields_}, kn, dg)
 
     def autotune(self, bvp: BVP, npaths: int, h: float, sample_knots: int = 0, seed: int = 1234,
                  adaptive_h: bool = False, richardson: bool = False, want_var: bool = False,
@@ -675,13 +741,15 @@ class EMFKACSolver:
     def Solve_GPU_Analytic(self, X0, N: int, h: float, rho: float, bvp: BVP, stencil: Stencil, c2: float = 0.0,
                            mode: int = capi.MODE_FP64, seed: int = 1234, knot_id: int = 0, instance: int = 0,
                            dup_sum: bool = False, want_var: bool = True, max_steps: int = 0,
-                           adaptive_h: bool = False, richardson: bool = False, ipsi_override=None):
+                           adaptive_h: bool = False, richardson: bool = False, ipsi_override=None,
+                           diagnostics: bool = False):
         """Solve_OMP_Analytic's outputs (G, G_var, G_j, B, BB) for the knot at
         X0: N paths of step h in the stencil, G_j the sorted knot indices of
         its sides.  rho and c2 are accepted for the reference's signature;
         like its G_update, the side shapes come from the stencil.  knot_id is
         the Philox knot word (a layout knot's index reproduces its stream in
-        PDDSparseGM.estimate)."""
+        PDDSparseGM.estimate).  diagnostics: self.sums receives the
+        reduction's diagnostic sums (the reference's sums[] member)."""
         del rho, c2
         if bvp.kind == BVP.LUT and bvp.tables is not None:
             coef, g, bounds = bvp.tables
@@ -696,6 +764,7 @@ class EMFKACSolver:
         sd = stencil.desc()
         ed, keep = _estimate_desc(mode, N, h, seed, instance, dup_sum, want_var, max_steps, adaptive_h, richardson,
                                   ipsi_override)
+        ed.diagnostics = int(bool(diagnostics))
         cap = sum(len(stencil.index[d]) for d in _DIRS) + 1
         gj = np.zeros(cap, np.int32)
         G = np.zeros(cap)
@@ -711,6 +780,9 @@ class EMFKACSolver:
         del keep
         n = nnz.value
         self.info = {f: getattr(info, f) for f, _ in capi.EstimateInfo._fields_}
+        if diagnostics:
+            self.sums = np.zeros(capi.DIAG_N)
+            self._check(self._lib.pdds_estimate_diagnostics(self._ctx, _p(self.sums, C.c_double)))
         return G[:n].copy(), Gv[:n].copy(), gj[:n].copy(), B.value, BB.value
 
 

@@ -182,6 +182,8 @@ pdds_status pdds_batch_run(pdds_ctx* ctx, const pdds_batch_run_desc* desc, pdds_
   if (ed.npaths < 1 || !(ed.h > 0.0)) return fail(ctx, PDDS_ERR_INVALID, "npaths >= 1 and h > 0 required");
   if (ed.ipsi_override) return fail(ctx, PDDS_ERR_INVALID, "ipsi_override is a replay option");
   if (ed.adaptive_n) return fail(ctx, PDDS_ERR_INVALID, "batches use a fixed number of paths per knot");
+  if (ed.diagnostics || ed.knot_first || ed.knot_count)
+    return fail(ctx, PDDS_ERR_INVALID, "diagnostics and knot ranges are pdds_estimate options");
   if (desc->solve.method != PDDS_SOLVE_GMRES_FP32_IR)
     return fail(ctx, PDDS_ERR_INVALID, "batches solve with PDDS_SOLVE_GMRES_FP32_IR");
   if (desc->solve.restart > GMRES_CLUSTER_MAX_M) return fail(ctx, PDDS_ERR_INVALID, "restart must be <= 40");

@@ -47,6 +47,85 @@ void clear_tune(pdds_ctx* ctx) {
   ctx->tune_rich = -1;
 }
 
+void release_lut_tex(pdds_ctx* ctx) {
+  for (int t = 0; t < 4; t++) {
+    if (ctx->lut_tex[t]) cudaDestroyTextureObject(ctx->lut_tex[t]);
+    if (ctx->lut_arr[t]) cudaFreeArray(ctx->lut_arr[t]);
+    ctx->lut_tex[t] = 0;
+    ctx->lut_arr[t] = nullptr;
+  }
+}
+
+namespace {
+
+// Cubic B-spline coefficients c of the samples f along one line of n nodes
+// with stride `stride`, in place: (c_{i-1} + 4 c_i + c_{i+1}) / 6 = f_i, with
+// c_{-1} = c_0 and c_n = c_{n-1} (the texture's clamp addressing), so the
+// spline the FP32 sampler evaluates passes through every node.  Thomas
+// elimination of the tridiagonal system (diagonally dominant).
+void bspline_line(double* v, int n, size_t stride, std::vector<double>& cp) {
+  cp.resize(n);
+  const double off = 1.0 / 6.0;
+  double d = 5.0 / 6.0;
+  cp[0] = off / d;
+  v[0] /= d;
+  for (int i = 1; i < n; i++) {
+    d = (i == n - 1 ? 5.0 / 6.0 : 4.0 / 6.0) - off * cp[i - 1];
+    cp[i] = off / d;
+    v[i * stride] = (v[i * stride] - off * v[(i - 1) * stride]) / d;
+  }
+  for (int i = n - 2; i >= 0; i--) v[i * stride] -= cp[i] * v[(i + 1) * stride];
+}
+
+// The float4 textures of the tables coef [ny][nx][8] (fields 0-3 and 4-7),
+// linear filtering, clamped, unnormalised coordinates (node k's texel centre
+// at k + 0.5): lut_tex[0..1] their cubic B-spline coefficients, lut_tex[2..3]
+// the node values.
+pdds_status build_lut_tex(pdds_ctx* ctx, const float* coef, int nx, int ny) {
+  release_lut_tex(ctx);
+  const size_t n = (size_t)nx * ny;
+  std::vector<double> c(coef, coef + 8 * n);
+  std::vector<double> cp;
+  for (int f = 0; f < 8; f++) {
+    for (int j = 0; j < ny; j++) bspline_line(c.data() + (size_t)j * nx * 8 + f, nx, 8, cp);
+    for (int i = 0; i < nx; i++) bspline_line(c.data() + (size_t)i * 8 + f, ny, (size_t)nx * 8, cp);
+  }
+  std::vector<float4> tx(n);
+  const cudaChannelFormatDesc ch = cudaCreateChannelDesc<float4>();
+  for (int t = 0; t < 4; t++) {
+    const int h = t & 1;  // fields 4h .. 4h+3
+    for (size_t q = 0; q < n; q++) {
+      if (t < 2)
+        tx[q] = make_float4((float)c[8 * q + 4 * h], (float)c[8 * q + 4 * h + 1], (float)c[8 * q + 4 * h + 2],
+                            (float)c[8 * q + 4 * h + 3]);
+      else
+        tx[q] = make_float4(coef[8 * q + 4 * h], coef[8 * q + 4 * h + 1], coef[8 * q + 4 * h + 2],
+                            coef[8 * q + 4 * h + 3]);
+    }
+    CK(cudaMallocArray(&ctx->lut_arr[t], &ch, nx, ny));
+    const size_t pitch = (size_t)nx * sizeof(float4);
+    xfer().h2d += (int64_t)(pitch * ny);
+    CK(cudaMemcpy2DToArrayAsync(ctx->lut_arr[t], 0, 0, tx.data(), pitch, pitch, ny, cudaMemcpyHostToDevice,
+                                ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));  // tx is reused for the second texture
+    cudaResourceDesc rd;
+    std::memset(&rd, 0, sizeof(rd));
+    rd.resType = cudaResourceTypeArray;
+    rd.res.array.array = ctx->lut_arr[t];
+    cudaTextureDesc td;
+    std::memset(&td, 0, sizeof(td));
+    td.addressMode[0] = cudaAddressModeClamp;
+    td.addressMode[1] = cudaAddressModeClamp;
+    td.filterMode = cudaFilterModeLinear;
+    td.readMode = cudaReadModeElementType;
+    td.normalizedCoords = 0;
+    CK(cudaCreateTextureObject(&ctx->lut_tex[t], &rd, &td, nullptr));
+  }
+  return PDDS_OK;
+}
+
+}  // namespace
+
 pdds_status upload_layout(pdds_ctx* ctx) {
   drop_graph(ctx);  // the buffers below may move
   ctx->edges_ready = false;
@@ -223,6 +302,12 @@ ProblemDev problem_dev(const pdds_ctx* ctx) {
   d.lut.y0 = ctx->lut_bounds[1];
   d.lut.inv_dx = ctx->lut_nx > 1 ? 1.0 / ((ctx->lut_bounds[2] - ctx->lut_bounds[0]) / (ctx->lut_nx - 1)) : 0.0;
   d.lut.inv_dy = ctx->lut_ny > 1 ? 1.0 / ((ctx->lut_bounds[3] - ctx->lut_bounds[1]) / (ctx->lut_ny - 1)) : 0.0;
+  // the FP32 sampler by p[0]: 0 cubic B-spline (textures), 1 Catmull-Rom
+  // (node loads), 2 bilinear (textures)
+  const int sm = p.kind == PK_LUT && ctx->lut_tex[0] ? (p.p[0] == 1.0 ? 0 : (p.p[0] == 2.0 ? 2 : 1)) : 0;
+  d.lut.tex_mode = sm;
+  d.lut.tex[0] = sm ? (unsigned long long)ctx->lut_tex[sm == 2 ? 2 : 0] : 0ull;
+  d.lut.tex[1] = sm ? (unsigned long long)ctx->lut_tex[sm == 2 ? 3 : 1] : 0ull;
   return d;
 }
 
@@ -317,7 +402,7 @@ pdds_status enqueue_mixed_paths(pdds_ctx* ctx, const pdds_estimate_desc* desc, c
                                 int mc_n = -1) {
   cudaStream_t s = ctx->stream;
   if (mc_n < 0) mc_n = ctx->n_mc;
-  if (!items && P.kind == PK_ROBIN && (int)P.p[0] != 0 && !ctx->is_batch) {
+  if (!items && P.kind == PK_ROBIN && (int)P.p[0] != 0 && !ctx->is_batch && mc0 == 0 && mc_n == ctx->n_mc) {
     // Knots whose stencil has a reflecting side take several times the
     // steps per path of the others (their paths leave only through the
     // absorbing sides): they go first, in chunks of an eighth of the paths,
@@ -357,7 +442,7 @@ pdds_status enqueue_mixed_paths(pdds_ctx* ctx, const pdds_estimate_desc* desc, c
   const int n_items = items ? items->n : mc_n * chunks;
   const long long max_steps = desc->max_steps > 0 ? desc->max_steps : 1000000LL;
   CK(cudaMemsetAsync(ctx->counter.p, 0, sizeof(int), s));
-  MixedArgs a;
+  MixedArgs a{};
   a.L = ctx->dl;
   a.P = P;
   a.N = N;
@@ -377,7 +462,7 @@ pdds_status enqueue_mixed_paths(pdds_ctx* ctx, const pdds_estimate_desc* desc, c
   // work items of the default split are handed out heaviest knot first: by
   // the steps per knot that the last estimate on this layout counted, or
   // before the first one by a geometric estimate of the steps per path
-  const bool lpt = !items && !ctx->is_batch && !desc->plain_launch;
+  const bool lpt = !items && !ctx->is_batch && !desc->plain_launch && mc0 == 0 && mc_n == ctx->n_mc;
   if (lpt && !ctx->lpt_ready && ctx->L.geom == 0) {
     // E[steps] ~ tau / h_k: tau = tx ty / (tx + ty) combines the expected
     // exit times a (w - a) / 2 across the stencil in x and in y, h_k is the
@@ -418,6 +503,7 @@ pdds_status enqueue_mixed_paths(pdds_ctx* ctx, const pdds_estimate_desc* desc, c
   a.knot_invN = items ? items->knot_invN : nullptr;
   a.knot_steps = ctx->knot_steps.p;
   a.step_hist = desc->step_histogram ? ctx->step_hist.p : nullptr;
+  a.diag = (desc->diagnostics && ctx->diag.n >= (size_t)ctx->L.K * PDDS_DIAG_N) ? ctx->diag.p : nullptr;
   const int threads = cta_threads_for(ctx, desc);
   const size_t smem = ctx->mixed_smem * (a.want_var ? 2 : 1) + mixed_queue_smem(threads, a.richardson);
   if (smem > 200 * 1024) return fail(ctx, PDDS_ERR_INVALID, "exit histograms exceed shared memory; lower bins_per_gap");
@@ -595,6 +681,7 @@ pdds_status pdds_destroy(pdds_ctx* ctx) {
     ctx->tab.release();
     ctx->lut_coef.release();
     ctx->lut_g.release();
+    release_lut_tex(ctx);
     ctx->stats.release();
     ctx->errf.release();
     ctx->sV32.release();
@@ -675,6 +762,8 @@ pdds_status pdds_problem_set_lut(pdds_ctx* ctx, const float* coef, const float* 
   CK(copy_async(ctx->lut_coef.p, coef, 8 * n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
   CK(copy_async(ctx->lut_g.p, g, n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  const pdds_status st = build_lut_tex(ctx, coef, nx, ny);
+  if (st != PDDS_OK) return st;
   ctx->lut_nx = nx;
   ctx->lut_ny = ny;
   for (int q = 0; q < 4; q++) ctx->lut_bounds[q] = bounds[q];
@@ -890,10 +979,24 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
   if (desc->adaptive_n && desc->target_stderr < 0.0) return fail(ctx, PDDS_ERR_INVALID, "target_stderr < 0");
   if (desc->cta_threads != 0 && desc->cta_threads != 128 && desc->cta_threads != 256)
     return fail(ctx, PDDS_ERR_INVALID, "cta_threads must be 0, 128 or 256");
+  if (desc->knot_first < 0 || desc->knot_count < 0)
+    return fail(ctx, PDDS_ERR_INVALID, "knot_first and knot_count must be >= 0");
+  if ((desc->knot_first > 0 || desc->knot_count > 0) && desc->adaptive_n)
+    return fail(ctx, PDDS_ERR_INVALID, "a knot range runs a fixed number of paths per knot (adaptive_n = 0)");
+  const bool diag = desc->diagnostics != 0;
+  if (diag && mode == PDDS_MODE_MIXED && ctx->L.geom == 1)
+    return fail(ctx, PDDS_ERR_INVALID, "MIXED diagnostics need rectangular stencils (FP64 mode on circle layouts)");
+  if (diag && desc->adaptive_n)
+    return fail(ctx, PDDS_ERR_INVALID, "diagnostics need a fixed number of paths per knot (adaptive_n = 0)");
   CK(cudaSetDevice(ctx->device));
   cudaStream_t s = ctx->stream;
   HostLayout& L = ctx->L;
   const XferCount x0 = xfer();
+  ctx->has_diag = false;
+  if (diag) {
+    CK(ctx->diag.resize((size_t)L.K * PDDS_DIAG_N));
+    CK(cudaMemsetAsync(ctx->diag.p, 0, (size_t)L.K * PDDS_DIAG_N * sizeof(double), s));
+  }
   const int bins = desc->bins_per_gap > 0 ? desc->bins_per_gap : 16;
   if (bins != ctx->bins) {
     ctx->bins = bins;
@@ -911,8 +1014,13 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
     if (st != PDDS_OK) return st;
   }
   const int n_mc = ctx->n_mc;
+  // the hand-out positions this call runs
+  const int r0 = desc->knot_first;
+  const int rn = desc->knot_count > 0 ? desc->knot_count : n_mc - r0;
+  if (r0 > n_mc || (int64_t)r0 + rn > n_mc)
+    return fail(ctx, PDDS_ERR_INVALID, "knot range beyond the layout's " + std::to_string(n_mc) + " knots with paths");
   if (mode == PDDS_MODE_REPLAY_FP64) {
-    const int64_t total = (int64_t)n_mc * N;
+    const int64_t total = (int64_t)rn * N;
     CK(ctx->rx.resize(std::max<int64_t>(total, 1)));
     CK(ctx->ry.resize(std::max<int64_t>(total, 1)));
     CK(ctx->rY.resize(std::max<int64_t>(total, 1)));
@@ -921,20 +1029,30 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
     CK(ctx->rside.resize(std::max<int64_t>(total, 1)));
     CK(ctx->rsl.resize(std::max<int64_t>(total, 1)));
     CK(ctx->rss.resize(std::max<int64_t>(total, 1)));
-    // (knot, side, side knot) tasks in hand-out order
+    if (diag) {
+      DBuf<double>* db[] = {&ctx->rsx, &ctx->rsy, &ctx->rsY, &ctx->rsZ, &ctx->rsxi};
+      for (auto* b : db) CK(b->resize(std::max<int64_t>(total, 1)));
+      CK(ctx->rknot_h.resize(std::max(rn, 1)));
+    }
+    // (knot, side, side knot) tasks of the range's knots in hand-out order;
+    // knot m of the range is hand-out position r0 + m (ipsi_override packs
+    // every knot, so its offsets count them all)
     std::vector<int> tm, td, ti;
-    std::vector<int64_t> tout, ktoff(std::max(n_mc, 1), 0), kipoff(4 * std::max(n_mc, 1), -1);
+    std::vector<int64_t> tout, ktoff(std::max(rn, 1), 0), kipoff(4 * std::max(rn, 1), -1);
     std::vector<int> mc;
     for (int v : L.order) if (!L.knot_boundary[v]) mc.push_back(v);
     int64_t ipo = 0;
-    for (int m = 0; m < n_mc; m++) {
-      const StencilRec& st = L.stencils[L.knot_stencil[mc[m]]];
-      ktoff[m] = (int64_t)tm.size();
+    for (int mg = 0; mg < n_mc; mg++) {
+      const StencilRec& st = L.stencils[L.knot_stencil[mc[mg]]];
+      const bool in = mg >= r0 && mg < r0 + rn;
+      const int m = mg - r0;
+      if (in) ktoff[m] = (int64_t)tm.size();
       for (int d = 0; d < 4; d++) {
         if (st.side[d] < 0) continue;
         const int n = L.sides[st.side[d]].n;
-        kipoff[4 * m + d] = ipo;
+        if (in) kipoff[4 * m + d] = ipo;
         ipo += (int64_t)n * n;
+        if (!in) continue;
         for (int i = 0; i < n; i++) {
           tm.push_back(m); td.push_back(d); ti.push_back(i);
           tout.push_back((int64_t)tout.size());
@@ -957,7 +1075,7 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
       CK(copy_async(ctx->ipsi_knot.p, desc->ipsi_override, ipo * sizeof(double),
                          cudaMemcpyHostToDevice, s));
     }
-    ReplayArgs a;
+    ReplayArgs a{};
     a.L = ctx->dl;
     a.P = P;
     a.N = N;
@@ -968,12 +1086,16 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
     a.sublinear = 1;
     a.adaptive_h = desc->adaptive_h ? 1 : 0;
     a.max_steps = max_steps;
-    a.mc_knots = ctx->mc_knots.p;
-    a.n_mc = n_mc;
+    a.mc_knots = ctx->mc_knots.p + r0;
+    a.n_mc = rn;
     a.knot_ipsi_off = desc->ipsi_override ? ctx->knot_ipsi_off.p : nullptr;
     a.ipsi_knot = desc->ipsi_override ? ctx->ipsi_knot.p : nullptr;
     a.ex = ctx->rx.p; a.ey = ctx->ry.p; a.eY = ctx->rY.p; a.eZ = ctx->rZ.p; a.exi = ctx->rxi.p;
     a.eside = ctx->rside.p; a.esteps_l = ctx->rsl.p; a.esteps_s = ctx->rss.p;
+    a.diag = diag ? ctx->diag.p : nullptr;
+    a.sx = diag ? ctx->rsx.p : nullptr; a.sy = diag ? ctx->rsy.p : nullptr;
+    a.sY = diag ? ctx->rsY.p : nullptr; a.sZ = diag ? ctx->rsZ.p : nullptr;
+    a.sxi = diag ? ctx->rsxi.p : nullptr; a.knot_h = diag ? ctx->rknot_h.p : nullptr;
     a.G = ctx->G.p;
     a.GG = ctx->GG.p;
     a.B = ctx->B.p;
@@ -1003,18 +1125,18 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
   } else {
     int chunks = 1, ppc = 1;
     item_split(ctx, N, &chunks, &ppc, (mode == PDDS_MODE_MIXED && tuned_for(ctx, desc)) ? ctx->tune_ppc : 0,
-               cta_threads_for(ctx, desc));
-    const int n_items = n_mc * chunks;
+               cta_threads_for(ctx, desc), rn);
+    const int n_items = rn * chunks;
     CK(cudaMemsetAsync(ctx->counter.p, 0, sizeof(int), s));
     if (mode == PDDS_MODE_MIXED) {
-      pdds_status st = enqueue_mixed_paths(ctx, desc, P, chunks, ppc, &launches);
+      pdds_status st = enqueue_mixed_paths(ctx, desc, P, chunks, ppc, &launches, nullptr, r0, rn);
       if (st != PDDS_OK) return st;
       if (desc->adaptive_n) {
         st = adaptive_continue(ctx, desc, P, &launches);
         if (st != PDDS_OK) return st;
       }
     } else {
-      Fp64Args a;
+      Fp64Args a{};
       a.L = ctx->dl;
       a.P = P;
       a.N = N;
@@ -1030,13 +1152,14 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
       a.adaptive_h = desc->adaptive_h ? 1 : 0;
       a.richardson = desc->richardson ? 1 : 0;
       a.max_steps = max_steps;
-      a.mc_knots = ctx->mc_knots.p;
+      a.mc_knots = ctx->mc_knots.p + r0;
       a.item_counter = ctx->counter.p;
       a.G = ctx->G.p;
       a.Bsum = ctx->Bsum.p;
       a.BBsum = ctx->BBsum.p;
       a.stats = ctx->stats.p;
       a.err_flags = ctx->errf.p;
+      a.diag = diag ? ctx->diag.p : nullptr;
       const size_t smem = ctx->fp64_smem;
       cudaFuncAttributes fa;
       (void)fa;
@@ -1060,8 +1183,7 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
   CK(cudaEventRecord(ctx->ev2, s));
   if (!(mode == PDDS_MODE_MIXED && desc->adaptive_n)) {
     ctx->last_knot_N.assign(L.K, 0);
-    for (int v = 0; v < L.K; v++)
-      if (!L.knot_boundary[v]) ctx->last_knot_N[v] = N;
+    for (int m = r0; m < r0 + rn; m++) ctx->last_knot_N[ctx->mc_host[m]] = N;
   }
   if (val && nnz) CK(copy_async(val, ctx->G.p, nnz * sizeof(double), cudaMemcpyDeviceToHost, s));
   if (var && nnz) {
@@ -1074,6 +1196,7 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
   CK(copy_async(st, ctx->stats.p, sizeof(st), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   ctx->has_estimate = true;
+  ctx->has_diag = diag;
   if (info) {
     float ms_setup = 0.f, ms_paths = 0.f;
     cudaEventElapsedTime(&ms_setup, ctx->ev0, ctx->ev1);
@@ -1109,6 +1232,8 @@ pdds_status pdds_autotune(pdds_ctx* ctx, const pdds_estimate_desc* desc, int32_t
   if (ctx->device < 0) return fail(ctx, PDDS_ERR_INVALID, "context has no device");
   if (!ctx->has_problem || !ctx->has_layout) return fail(ctx, PDDS_ERR_INVALID, "problem and layout needed");
   if (desc->mode != PDDS_MODE_MIXED) return fail(ctx, PDDS_ERR_INVALID, "the autotuner tunes PDDS_MODE_MIXED");
+  if (desc->knot_first || desc->knot_count || desc->diagnostics)
+    return fail(ctx, PDDS_ERR_INVALID, "the autotuner times whole runs (no knot range, no diagnostics)");
   if (desc->npaths < 1 || !(desc->h > 0.0)) return fail(ctx, PDDS_ERR_INVALID, "npaths >= 1 and h > 0 required");
   if (desc->cta_threads != 0 && desc->cta_threads != 128 && desc->cta_threads != 256)
     return fail(ctx, PDDS_ERR_INVALID, "cta_threads must be 0, 128 or 256");
@@ -1322,6 +1447,7 @@ pdds_status pdds_semilinear_tables(pdds_ctx* ctx, const pdds_semilinear_desc* de
   const int ns = L.nsub;
   const int G = ns * (m + 1) + 1;
   const size_t nn = (size_t)G * G;
+  release_lut_tex(ctx);  // tables computed on the device: the FP32 sampler reads the nodes
   CK(ctx->lut_coef.resize(8 * nn));
   CK(ctx->lut_g.resize(nn));
   const double hx = (L.ne[0] - L.sw[0]) / ns / (m + 1), hy = (L.ne[1] - L.sw[1]) / ns / (m + 1);
@@ -1355,6 +1481,17 @@ pdds_status pdds_estimate_knot_steps(pdds_ctx* ctx, int64_t* steps) {
   if (!ctx->has_estimate || !ctx->has_knot_steps) return fail(ctx, PDDS_ERR_INVALID, "no MIXED estimate on this layout");
   CK(cudaSetDevice(ctx->device));
   CK(copy_async(steps, ctx->knot_steps.p, ctx->L.K * sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return PDDS_OK;
+}
+
+pdds_status pdds_estimate_diagnostics(pdds_ctx* ctx, double* sums) {
+  if (!ctx || !sums) return PDDS_ERR_INVALID;
+  if (!ctx->has_estimate || !ctx->has_diag)
+    return fail(ctx, PDDS_ERR_INVALID, "no estimate with diagnostics on this layout");
+  CK(cudaSetDevice(ctx->device));
+  CK(copy_async(sums, ctx->diag.p, (size_t)ctx->L.K * PDDS_DIAG_N * sizeof(double), cudaMemcpyDeviceToHost,
+                ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   return PDDS_OK;
 }

@@ -53,6 +53,11 @@ struct pdds_ctx {
   bool has_problem = false;
   pdds_problem_desc prob{};
   DBuf<float> lut_coef, lut_g;
+  // textures of the 8 table fields for the FP32 sampler, two float4 each
+  // (linear filtering), built by pdds_problem_set_lut: [0..1] cubic B-spline
+  // coefficients, [2..3] the node values (bilinear)
+  cudaArray_t lut_arr[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaTextureObject_t lut_tex[4] = {0, 0, 0, 0};
   int lut_nx = 0, lut_ny = 0;
   double lut_bounds[4] = {0, 0, 0, 0};
   bool has_layout = false;
@@ -136,6 +141,9 @@ struct pdds_ctx {
   std::vector<int> last_knot_N;  // paths per knot of the last estimate
   DBuf<unsigned long long> knot_steps;  // path steps per knot of the last MIXED estimate
   DBuf<unsigned long long> step_hist;   // [32] paths by steps (log2 bins) of the last MIXED estimate
+  DBuf<double> diag;              // [K][PDDS_DIAG_N] diagnostic sums of the last estimate
+  bool has_diag = false;
+  DBuf<double> rsx, rsy, rsY, rsZ, rsxi, rknot_h;  // replay diagnostics: sublinear ends, knot steps
   DBuf<int> mc_lpt;               // MIXED hand-out order, heaviest knots first (from knot_steps)
   bool lpt_ready = false;
   bool has_knot_steps = false;
@@ -160,6 +168,8 @@ pdds_status enqueue_mixed(pdds_ctx* ctx, const pdds_estimate_desc* desc, int* la
 void drop_graph(pdds_ctx* ctx);
 // Forgets the autotuned launch shape (it was timed on the previous layout).
 void clear_tune(pdds_ctx* ctx);
+// Destroys the textures of the tables (the FP32 sampler then reads the nodes).
+void release_lut_tex(pdds_ctx* ctx);
 
 }  // namespace pdds
 

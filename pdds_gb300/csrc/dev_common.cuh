@@ -79,6 +79,11 @@ struct LutDev {
   const float* g;
   int nx, ny;
   double x0, y0, inv_dx, inv_dy;
+  // the FP32 sampler's textures (fields 0-3 and 4-7, linear filtering,
+  // clamped): tex_mode 1 cubic B-spline coefficients, 2 the node values
+  // (bilinear); 0 no textures, it samples the nodes (Catmull-Rom)
+  unsigned long long tex[2];
+  int tex_mode;
 };
 
 struct ProblemDev {
@@ -189,6 +194,71 @@ __device__ __forceinline__ T lut_sample_g(const LutDev& L, T x, T y) {
   return out;
 }
 
+// Cubic B-spline interpolation of the tables from textures of their B-spline
+// coefficients (prefiltered on the host so that the spline takes the table's
+// values at the nodes), each axis' four weights folded into two linearly
+// filtered fetches (Sigg and Hadwiger, "Fast third-order texture filtering",
+// GPU Gems 2, ch. 20): four fetches per texture in place of sixteen node
+// loads.  The filtering hardware blends with 8-bit fractions, an error of at
+// most |c_{i+1} - c_i| / 512 per blend: O(node spacing x gradient) / 512 for
+// smooth tables.
+__device__ __forceinline__ void bspline_axis(float p, int n, float& c0, float& c1, float& g0, float& g1) {
+  p = fminf(fmaxf(p, 0.f), (float)(n - 1));  // clamped to the table, as the node sampler clamps
+  const float i = floorf(p);
+  const float t = p - i, t2 = t * t, t3 = t2 * t;
+  const float s = 1.f - t;
+  const float w0 = (1.f / 6.f) * (s * s * s);
+  const float w1 = (1.f / 6.f) * ((3.f * t3 - 6.f * t2) + 4.f);
+  const float w3 = (1.f / 6.f) * t3;
+  const float w2 = (1.f - w0) - (w1 + w3);
+  g0 = w0 + w1;  // >= 1/6 for t in [0, 1]
+  g1 = w2 + w3;  // >= 1/6
+  // node k's texel centre is k + 0.5: blend nodes i-1, i and nodes i+1, i+2
+  c0 = (i - 0.5f) + w1 / g0;
+  c1 = (i + 1.5f) + w3 / g1;
+}
+template <int NF>
+__device__ __forceinline__ void lut_sample_tex(const LutDev& L, float x, float y, float* out) {
+  float cx0, cx1, gx0, gx1, cy0, cy1, gy0, gy1;
+  bspline_axis((x - (float)L.x0) * (float)L.inv_dx, L.nx, cx0, cx1, gx0, gx1);
+  bspline_axis((y - (float)L.y0) * (float)L.inv_dy, L.ny, cy0, cy1, gy0, gy1);
+#pragma unroll
+  for (int t = 0; t < (NF > 4 ? 2 : 1); t++) {
+    const cudaTextureObject_t tx = (cudaTextureObject_t)L.tex[t];
+    const float4 a = tex2D<float4>(tx, cx0, cy0), b = tex2D<float4>(tx, cx1, cy0);
+    const float4 c = tex2D<float4>(tx, cx0, cy1), d = tex2D<float4>(tx, cx1, cy1);
+    out[4 * t + 0] = gy0 * (gx0 * a.x + gx1 * b.x) + gy1 * (gx0 * c.x + gx1 * d.x);
+    out[4 * t + 1] = gy0 * (gx0 * a.y + gx1 * b.y) + gy1 * (gx0 * c.y + gx1 * d.y);
+    out[4 * t + 2] = gy0 * (gx0 * a.z + gx1 * b.z) + gy1 * (gx0 * c.z + gx1 * d.z);
+    out[4 * t + 3] = gy0 * (gx0 * a.w + gx1 * b.w) + gy1 * (gx0 * c.w + gx1 * d.w);
+  }
+}
+// Bilinear interpolation of the node values, one linearly filtered fetch per
+// texture (8-bit blend fractions: an error of at most |f_{i+1} - f_i| / 512
+// per axis on top of the O(node spacing^2) interpolation error).
+template <int NF>
+__device__ __forceinline__ void lut_sample_lin(const LutDev& L, float x, float y, float* out) {
+  const float px = fminf(fmaxf((x - (float)L.x0) * (float)L.inv_dx, 0.f), (float)(L.nx - 1)) + 0.5f;
+  const float py = fminf(fmaxf((y - (float)L.y0) * (float)L.inv_dy, 0.f), (float)(L.ny - 1)) + 0.5f;
+#pragma unroll
+  for (int t = 0; t < (NF > 4 ? 2 : 1); t++) {
+    const float4 a = tex2D<float4>((cudaTextureObject_t)L.tex[t], px, py);
+    out[4 * t + 0] = a.x;
+    out[4 * t + 1] = a.y;
+    out[4 * t + 2] = a.z;
+    out[4 * t + 3] = a.w;
+  }
+}
+// The FP32 (MIXED) sampler: the problem's textures when it has them (cubic
+// B-spline or bilinear), else the Catmull-Rom node sampler of the FP64 and
+// replay forms.
+template <int NF>
+__device__ __forceinline__ void lut_sample_f32(const LutDev& L, float x, float y, float* out) {
+  if (L.tex_mode == 1) lut_sample_tex<NF>(L, x, y, out);
+  else if (L.tex_mode == 2) lut_sample_lin<NF>(L, x, y, out);
+  else lut_sample<float, NF>(L, x, y, out);
+}
+
 // Single-precision approximations (the PTX .approx forms, flush-to-zero) for
 // the FP32 path, whose Euler step error is far above their rounding.
 __device__ __forceinline__ float sqrt_approx(float x) {
@@ -223,7 +293,7 @@ __device__ __forceinline__ void coef_f32(const ProblemDev& P, float x, float y, 
   const float PI = 3.14159265358979f;
   if (KIND == PK_LUT) {
     float v[8];
-    lut_sample<float, 8>(P.lut, x, y, v);
+    lut_sample_f32<8>(P.lut, x, y, v);
     k.s00 = v[0]; k.s01 = 0.f; k.s10 = 0.f; k.s11 = v[1];
     k.b0 = v[2]; k.b1 = v[3]; k.c = v[4]; k.f = v[5]; k.g0 = v[6]; k.g1 = v[7];
   } else if (KIND == PK_POISSON_SINCOS) {
@@ -328,7 +398,7 @@ __device__ __forceinline__ void sigma_f32(const ProblemDev& P, float x, float y,
                                           float& s10, float& s11) {
   if (KIND == PK_LUT) {
     float v[4];
-    lut_sample<float, 4>(P.lut, x, y, v);
+    lut_sample_f32<4>(P.lut, x, y, v);
     s00 = v[0]; s01 = 0.f; s10 = 0.f; s11 = v[1];
   } else if (KIND == PK_VARCOEF) {
     s00 = 1.f + 0.5f * (x * x); s01 = 0.f; s10 = 0.f; s11 = 1.f + 0.5f * (y * y);
@@ -344,7 +414,7 @@ template <int KIND>
 __device__ __forceinline__ void sigma_normals_f32(const ProblemDev& P, float x, float y, float& nx, float& ny) {
   if (KIND == PK_LUT) {
     float v[4];
-    lut_sample<float, 4>(P.lut, x, y, v);
+    lut_sample_f32<4>(P.lut, x, y, v);
     nx = fabsf(v[0]);
     ny = fabsf(v[1]);
   } else if (KIND == PK_VARCOEF) {

@@ -36,6 +36,7 @@ constexpr unsigned FULL = 0xffffffffu;
 
 struct Lvl64 {
   double x, y, Y, Z, xi;
+  double phi;  // Z + Y g(X_tau) at the exit (diagnostics)
   Coef<double> k;
   unsigned steps;
 };
@@ -64,6 +65,7 @@ k_paths_fp64(const Fp64Args a) {
   __shared__ double s_h;
   __shared__ unsigned s_next_path;
   __shared__ double s_red[FP64_THREADS / 32][2];
+  __shared__ double s_diag[PDDS_DIAG_N];
   __shared__ unsigned long long s_redi[FP64_THREADS / 32][3];
   const DevLayout& L = a.L;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -77,6 +79,7 @@ k_paths_fp64(const Fp64Args a) {
       const int k = a.mc_knots[item / a.chunks];
       const int chunk = item % a.chunks;
       s_knot = k;
+      for (int q = 0; q < PDDS_DIAG_N; q++) s_diag[q] = 0.0;
       const int p0 = chunk * a.paths_per_chunk;
       s_path_end = min(a.N, p0 + a.paths_per_chunk);
       s_next_path = (unsigned)(p0 + FP64_THREADS);
@@ -157,7 +160,7 @@ k_paths_fp64(const Fp64Args a) {
     unsigned long long nsteps = 0, nglob = 0, nsten = 0;
     // exit on side d at side coordinate `along` (x or y on rectangles, angle
     // or radius on polar stencils), projection (Ex, Ey)
-    auto exit_level = [&](const Lvl64& s, double wgt, double Ex, double Ey, int d, bool glob,
+    auto exit_level = [&](Lvl64& s, double wgt, double Ex, double Ey, int d, bool glob,
                           double along) -> double {
       if (isnan(s.x) || isnan(s.y)) {
         // a position that is not a number lies on no side: reported, scores nothing
@@ -166,8 +169,10 @@ k_paths_fp64(const Fp64Args a) {
       }
       if (glob) {
         ++nglob;
-        return s.Z + s.Y * u_f64<KIND>(a.P, Ex, Ey) + s.xi;
+        s.phi = s.Z + s.Y * u_f64<KIND>(a.P, Ex, Ey);
+        return s.phi + s.xi;
       }
+      if (a.diag) s.phi = s.Z + s.Y * u_f64<KIND>(a.P, Ex, Ey);
       ++nsten;
       if (d < 0) {
         atomicOr(a.err_flags, ERR_FLAG_EXIT_SIDE);
@@ -308,7 +313,8 @@ k_paths_fp64(const Fp64Args a) {
     };
     Lvl64 fine, coarse;
     auto reset = [&]() {
-      fine.x = x0; fine.y = y0; fine.Y = 1.0; fine.Z = 0.0; fine.xi = 0.0; fine.k = k0; fine.steps = 0;
+      fine.x = x0; fine.y = y0; fine.Y = 1.0; fine.Z = 0.0; fine.xi = 0.0; fine.phi = 0.0; fine.k = k0;
+      fine.steps = 0;
       coarse = fine;
     };
     reset();
@@ -345,6 +351,9 @@ k_paths_fp64(const Fp64Args a) {
             bb += v * v;
             nsteps += fine.steps + coarse.steps;
             fin = true;
+            if (a.diag)
+              diag_add(s_diag, 2.0 * fine.phi - coarse.phi, 2.0 * fine.xi - coarse.xi, fine.steps * hf,
+                       2.0 * fine.steps);
           }
         } else {
           if ((m & 1u) == 0) blk = path_block(a.seed, a.instance, knot_word(a.L, knot), path, m >> 1);
@@ -362,6 +371,7 @@ k_paths_fp64(const Fp64Args a) {
             bb += val_f * val_f;
             nsteps += fine.steps;
             fin = true;
+            if (a.diag) diag_add(s_diag, fine.phi, fine.xi, fine.steps * h, 2.0 * fine.steps);
           }
         }
         if (fin) {
@@ -415,6 +425,7 @@ k_paths_fp64(const Fp64Args a) {
       atomicAdd(a.stats + 2, tg);
       atomicAdd(a.stats + 3, tt);
     }
+    if (a.diag) diag_flush(s_diag, a.diag + (int64_t)knot * PDDS_DIAG_N, tid);
     // G_i = -(1/N) sum_j ipsi(j,i) S_j
     const int64_t row0 = L.row_ptr[knot];
     for (int pr = tid; pr < nall; pr += FP64_THREADS) {

@@ -126,6 +126,7 @@ k_paths_mixed(const MixedArgs a) {
   __shared__ double s_red[MIXED_MAX_THREADS / 32][4];
   __shared__ unsigned long long s_redi[MIXED_MAX_THREADS / 32][3];
   __shared__ unsigned s_sth[32];  // this item's paths by steps (log2 bins), when step_hist is set
+  __shared__ double s_dg[PDDS_DIAG_N];  // this item's diagnostic sums, when diag is set
   // exit queue of each warp: word w of slot i at q[w][i]
   constexpr int QW = RICH ? 9 : 5;
   const int nthr = blockDim.x, nwarps = nthr >> 5;
@@ -225,6 +226,7 @@ k_paths_mixed(const MixedArgs a) {
     const int nh = a.want_var ? 2 * hist_len : hist_len;
     for (int i = tid; i < nh; i += nthr) hist[i] = 0.f;
     if (tid < 32) s_sth[tid] = 0u;
+    if (tid < PDDS_DIAG_N) s_dg[tid] = 0.0;
     float* hist2 = hist + hist_len;
     __syncthreads();
 
@@ -364,7 +366,7 @@ k_paths_mixed(const MixedArgs a) {
         const float dx = fabsf(s.x - cx) - hx, dy = fabsf(s.y - cy) - hy;
         float t = thr;
         if constexpr (KIND == PK_LUT) {
-          lut_sample<float, 8>(P.lut, s.x, s.y, s.cf);
+          lut_sample_f32<8>(P.lut, s.x, s.y, s.cf);
           t *= dx > dy ? fabsf(s.cf[0]) : fabsf(s.cf[1]);
         } else if constexpr (!KindTraits<KIND>::iso) {
           float nx, ny;  // |N^T sigma| for the x and y normals
@@ -582,7 +584,7 @@ k_paths_mixed(const MixedArgs a) {
     };
 
     float cf0[8];  // table fields at the knot (PK_LUT)
-    if constexpr (KIND == PK_LUT) lut_sample<float, 8>(P.lut, x0, y0, cf0);
+    if constexpr (KIND == PK_LUT) lut_sample_f32<8>(P.lut, x0, y0, cf0);
     auto reset = [&]() {
       F.x = x0; F.y = y0; F.Y = 1.f; F.Z = 0.f; F.xi = 0.f; F.steps = 0;
       if constexpr (KIND == PK_LUT) {
@@ -643,6 +645,24 @@ k_paths_mixed(const MixedArgs a) {
             atomicAdd(&s_sth[31 - __clz(max(F.steps, 1u))], 1u);
             if (RICH) atomicAdd(&s_sth[31 - __clz(max(Cs.steps, 1u))], 1u);
           }
+          if constexpr (GEOM == 0) {
+            if (a.diag) {
+              // phi = Z + Y g at the nearest point of the stencil rectangle
+              // (the exit projection), per level; a pair adds 2 fine - coarse
+              auto phi_of = [&](const Lvl<KIND>& v) -> float {
+                float Ex, Ey, Nx, Ny;
+                int om;
+                rect2d<float>(rect, v.x, v.y, Ex, Ey, Nx, Ny, om);
+                return v.Z + v.Y * u_f32<KIND>(P, Ex, Ey);
+              };
+              float ph = phi_of(F), xv = F.xi;
+              if (RICH) {
+                ph = 2.f * ph - phi_of(Cs);
+                xv = 2.f * xv - Cs.xi;
+              }
+              diag_add(s_dg, ph, xv, (double)F.steps * (RICH ? 0.5 * (double)h : (double)h), 2.0 * F.steps);
+            }
+          }
           nsteps += F.steps + (RICH ? Cs.steps : 0u);
           path = base + __popc(dm & lt);
           active = (int)path < path_end;
@@ -687,6 +707,7 @@ k_paths_mixed(const MixedArgs a) {
       atomicAdd(a.stats + 3, tt);
     }
     if (a.step_hist && tid < 32 && s_sth[tid]) atomicAdd(a.step_hist + tid, (unsigned long long)s_sth[tid]);
+    if (a.diag) diag_flush(s_dg, a.diag + (int64_t)knot * PDDS_DIAG_N, tid);
     // ------------------------------------------------------------ contract G
     const int64_t row0 = L.row_ptr[knot];
     const double invN = a.knot_invN ? a.knot_invN[knot] : a.inv_N;

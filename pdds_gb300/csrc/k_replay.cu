@@ -190,6 +190,10 @@ __global__ void k_replay_paths(const ReplayArgs a) {
   }
   const int64_t o = gid;
   a.ex[o] = ex; a.ey[o] = ey; a.eY[o] = eY; a.eZ[o] = eZ; a.exi[o] = exi;
+  if (a.diag) {  // the sublinear leg's end (the linear one's when it did not run)
+    a.sx[o] = ps.E0; a.sy[o] = ps.E1; a.sY[o] = ps.Y; a.sZ[o] = ps.Z; a.sxi[o] = ps.xi;
+    if (n == 0) a.knot_h[m] = ps.h;
+  }
   a.esteps_l[o] = (int)nl;
   a.esteps_s[o] = (int)ns;
   a.eside[o] = capped ? -4 : side;
@@ -220,6 +224,39 @@ __global__ void k_replay_b(const ReplayArgs a) {
   }
   a.B[knot] = b / a.N;
   a.BB[knot] = bb / a.N;
+  if (a.diag) {
+    // the diagnostic sums of Reduce_Analytic (Solvers/EMFKACSolver.hpp:542-558),
+    // paths in order; tau = steps x h (elapsed time)
+    double sm[PDDS_DIAG_N];
+    for (int q = 0; q < PDDS_DIAG_N; q++) sm[q] = 0.0;
+    const double hk = a.knot_h[m];
+    for (int n = 0; n < a.N; n++) {
+      const int64_t o = (int64_t)m * a.N + n;
+      const double phl = a.eZ[o] + a.eY[o] * u_port<KIND>(a.P, a.ex[o], a.ey[o]);
+      const double phs = a.sZ[o] + a.sY[o] * u_port<KIND>(a.P, a.sx[o], a.sy[o]);
+      const double xl = a.exi[o], xs = a.sxi[o];
+      const double sl = (double)a.esteps_l[o], ss = sl + (double)a.esteps_s[o];
+      sm[PDDS_DIAG_SCORE] += phl;
+      sm[PDDS_DIAG_SUB + PDDS_DIAG_SCORE] += phs;
+      sm[PDDS_DIAG_SCORE2] += phl * phl;
+      sm[PDDS_DIAG_SUB + PDDS_DIAG_SCORE2] += phs * phs;
+      sm[PDDS_DIAG_XI] += xl;
+      sm[PDDS_DIAG_SUB + PDDS_DIAG_XI] += xs;
+      sm[PDDS_DIAG_XI2] += xl * xl;
+      sm[PDDS_DIAG_SUB + PDDS_DIAG_XI2] += xs * xs;
+      sm[PDDS_DIAG_SCORE_VR] += phl + xl;
+      sm[PDDS_DIAG_SUB + PDDS_DIAG_SCORE_VR] += phs + xs;
+      sm[PDDS_DIAG_SCORE_VR2] += (phl + xl) * (phl + xl);
+      sm[PDDS_DIAG_SUB + PDDS_DIAG_SCORE_VR2] += (phs + xs) * (phs + xs);
+      sm[PDDS_DIAG_XI_SCORE] += xl * phl;
+      sm[PDDS_DIAG_SUB + PDDS_DIAG_XI_SCORE] += xs * phs;
+      sm[PDDS_DIAG_RNG] += 2.0 * ss;
+      sm[PDDS_DIAG_TAU] += sl * hk;
+      sm[PDDS_DIAG_SUB + PDDS_DIAG_TAU] += ss * hk;
+      sm[PDDS_DIAG_PATHS] += 1.0;
+    }
+    for (int q = 0; q < PDDS_DIAG_N; q++) a.diag[(int64_t)knot * PDDS_DIAG_N + q] = sm[q];
+  }
 }
 
 // G_update accumulation for one (knot, side, side knot i), paths in order.

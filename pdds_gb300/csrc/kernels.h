@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "../../include/pdds.h"
 #include "dev_common.cuh"
 
 namespace pdds {
@@ -19,6 +20,32 @@ constexpr unsigned ERR_FLAG_EXIT_SIDE = 2u;
 constexpr unsigned ERR_FLAG_SINGULAR = 4u;
 constexpr unsigned ERR_FLAG_TIMEOUT = 8u;  // a bounded device wait ran out
 constexpr unsigned ERR_FLAG_SUB_NOCONV = 16u;  // a subdomain solve missed its tolerance
+
+// Diagnostic sums of one finished path (or Richardson pair) into a CTA's
+// shared sums: phi, phi^2, xi, xi^2, phi + xi, (phi + xi)^2, xi phi, tau, normals.
+__device__ __forceinline__ void diag_add(double* sd, double phi, double xi, double tau, double rng) {
+  atomicAdd(sd + PDDS_DIAG_SCORE, phi);
+  atomicAdd(sd + PDDS_DIAG_SCORE2, phi * phi);
+  atomicAdd(sd + PDDS_DIAG_XI, xi);
+  atomicAdd(sd + PDDS_DIAG_XI2, xi * xi);
+  atomicAdd(sd + PDDS_DIAG_SCORE_VR, phi + xi);
+  atomicAdd(sd + PDDS_DIAG_SCORE_VR2, (phi + xi) * (phi + xi));
+  atomicAdd(sd + PDDS_DIAG_XI_SCORE, xi * phi);
+  atomicAdd(sd + PDDS_DIAG_TAU, tau);
+  atomicAdd(sd + PDDS_DIAG_RNG, rng);
+  atomicAdd(sd + PDDS_DIAG_PATHS, 1.0);
+}
+// A CTA's sums into the knot's (the linear sums also fill the sublinear
+// slots: the FP64 and MIXED forms run no sublinear leg).
+__device__ __forceinline__ void diag_flush(const double* sd, double* out, int tid) {
+  if (tid < PDDS_DIAG_SUB) {
+    atomicAdd(out + tid, sd[tid]);
+    atomicAdd(out + PDDS_DIAG_SUB + tid, sd[tid]);
+  } else if (tid == PDDS_DIAG_SUB || tid == PDDS_DIAG_SUB + 1) {
+    const int q = tid == PDDS_DIAG_SUB ? PDDS_DIAG_RNG : PDDS_DIAG_PATHS;
+    atomicAdd(out + q, sd[q]);
+  }
+}
 
 struct MixedArgs {
   DevLayout L;
@@ -55,6 +82,8 @@ struct MixedArgs {
   // optional [32]: paths (each level of a Richardson pair counts) by their
   // steps, bin b = steps in [2^b, 2^(b+1))
   unsigned long long* step_hist;
+  // optional [K][PDDS_DIAG_N]: the reduction's diagnostic sums per knot
+  double* diag;
 };
 
 struct Fp64Args {
@@ -76,6 +105,7 @@ struct Fp64Args {
   double* BBsum;
   unsigned long long* stats;
   unsigned* err_flags;
+  double* diag;          // optional [K][PDDS_DIAG_N]: diagnostic sums per knot
 };
 
 struct ReplayArgs {
@@ -102,6 +132,15 @@ struct ReplayArgs {
   int* eside;            // -1 global, 0..3 stencil side, -2 no side
   int* esteps_l;
   int* esteps_s;
+  // diagnostics (all null when off): sums [K][PDDS_DIAG_N], the sublinear
+  // leg's end states [n_mc * N] and each knot's step [n_mc]
+  double* diag;
+  double* sx;
+  double* sy;
+  double* sY;
+  double* sZ;
+  double* sxi;
+  double* knot_h;
   // outputs
   double* G;             // [nnz] final values
   double* GG;            // [nnz] final GG/N values (before - G^2)

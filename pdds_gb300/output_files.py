@@ -69,6 +69,23 @@ def write_outputs(directory: str, x, y, row_ptr, col, G, G_var, B, BB, u, u_exac
             f.write("%d,%e,%e,%e,%e,%e,%e\n" % (i, x[i], y[i], ex[i], u[i], err[i], rerr[i]))
 
 
+KNOT_METADATA_COLUMNS = ("APL", "WCtime", "RNGCalls", "Estimated_Variance", "Estimated_Variance_VR",
+                         "PCoeff_old", "PCoeff_new", "Var_Plain", "Var_VR", "bias_num", "bias_trap")
+
+
+def write_knot_metadata(directory: str, metadata: dict):
+    """directory/Output/Debug/knot_metadata.csv in the reference's format
+    (Process_Metadata, PDDAlgorithms/PDDSparseGM.cpp:3128-3154): one line per
+    knot, index then the columns of Estimate.knot_metadata() in C's %e."""
+    dbg = os.path.join(directory, "Output", "Debug")
+    os.makedirs(dbg, exist_ok=True)
+    cols = [np.asarray(metadata[c], np.float64) for c in KNOT_METADATA_COLUMNS]
+    with open(os.path.join(dbg, "knot_metadata.csv"), "w") as f:
+        f.write("index," + ",".join(KNOT_METADATA_COLUMNS) + "\n")
+        for i in range(len(cols[0])):
+            f.write("%u," % i + ",".join("%e" % c[i] for c in cols) + "\n")
+
+
 def read_triplets(path):
     """(i, j, value) columns of one of the Debug CSV files."""
     data = np.loadtxt(path, delimiter=",", skiprows=1, ndmin=2)
