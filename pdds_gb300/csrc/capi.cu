@@ -507,7 +507,8 @@ pdds_status enqueue_mixed_paths(pdds_ctx* ctx, const pdds_estimate_desc* desc, c
   const int threads = cta_threads_for(ctx, desc);
   const size_t smem = ctx->mixed_smem * (a.want_var ? 2 : 1) + mixed_queue_smem(threads, a.richardson);
   if (smem > 200 * 1024) return fail(ctx, PDDS_ERR_INVALID, "exit histograms exceed shared memory; lower bins_per_gap");
-  int bps = mixed_blocks_per_sm(P.kind, smem, a.richardson, threads);
+  const int mk = mixed_kind(P);
+  int bps = mixed_blocks_per_sm(mk, smem, a.richardson, threads, a.diag != nullptr);
   if (bps < 1) bps = 1;
   if (ctx->force_bps > 0) bps = std::min(bps, ctx->force_bps);
   else if (tuned_for(ctx, desc) && !items) bps = std::min(bps, ctx->tune_bps);  // the shape it was timed on
@@ -516,7 +517,7 @@ pdds_status enqueue_mixed_paths(pdds_ctx* ctx, const pdds_estimate_desc* desc, c
   if (ctx->force_grid_frac > 0.0 && ctx->force_grid_frac < 1.0)
     grid = std::max(1, std::min(grid, (int)std::lround(ctx->force_grid_frac * bps * ctx->num_sms)));
   if (n_items > 0) {
-    CK(launch_paths_mixed(a, P.kind, grid, threads, smem, s));
+    CK(launch_paths_mixed(a, mk, grid, threads, smem, s));
     ++*launches;
     if (lpt) {
       CK(ctx->mc_lpt.resize(std::max(ctx->n_mc, 1)));
@@ -1264,7 +1265,7 @@ pdds_status pdds_autotune(pdds_ctx* ctx, const pdds_estimate_desc* desc, int32_t
   d.cta_threads = fixed_threads > 0 ? fixed_threads : mixed_threads(ctx->n_mc);  // the default shape first
   auto occupancy = [&](int threads) {
     const size_t smem = ctx->mixed_smem * (d.want_var ? 2 : 1) + mixed_queue_smem(threads, d.richardson);
-    return std::max(1, mixed_blocks_per_sm(P.kind, smem, d.richardson, threads));
+    return std::max(1, mixed_blocks_per_sm(mixed_kind(P), smem, d.richardson, threads));
   };
   const int occ = occupancy(d.cta_threads);
   std::vector<int> ppc_c;

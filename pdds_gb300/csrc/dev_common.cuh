@@ -94,6 +94,11 @@ struct ProblemDev {
 };
 
 enum { PK_POISSON_SINCOS = 0, PK_MONEGROS = 1, PK_HELMHOLTZ = 2, PK_VARCOEF = 3, PK_LUT = 4, PK_CIRCLE = 5, PK_ROBIN = 6 };
+// The PK_LUT problem sampled from its textures: an instantiation of the FP32
+// path kernel only (the problem's kind stays PK_LUT), so that neither form
+// carries the other's sampler in its registers.
+constexpr int PK_LUT_TEX = 7;
+__host__ __device__ constexpr bool is_lut_kind(int k) { return k == PK_LUT || k == PK_LUT_TEX; }
 
 // Problem parameters of the instance that owns knot k (batches), else P's own.
 __device__ __forceinline__ void instance_params(const DevLayout& L, int k, ProblemDev& P, uint32_t& rng_inst,
@@ -249,14 +254,17 @@ __device__ __forceinline__ void lut_sample_lin(const LutDev& L, float x, float y
     out[4 * t + 3] = a.w;
   }
 }
-// The FP32 (MIXED) sampler: the problem's textures when it has them (cubic
-// B-spline or bilinear), else the Catmull-Rom node sampler of the FP64 and
-// replay forms.
-template <int NF>
+// The FP32 (MIXED) sampler of a path-kernel instantiation: PK_LUT_TEX the
+// problem's textures (cubic B-spline, or bilinear with tex_mode 2), PK_LUT
+// the Catmull-Rom node sampler of the FP64 and replay forms.
+template <int KIND, int NF>
 __device__ __forceinline__ void lut_sample_f32(const LutDev& L, float x, float y, float* out) {
-  if (L.tex_mode == 1) lut_sample_tex<NF>(L, x, y, out);
-  else if (L.tex_mode == 2) lut_sample_lin<NF>(L, x, y, out);
-  else lut_sample<float, NF>(L, x, y, out);
+  if constexpr (KIND == PK_LUT_TEX) {
+    if (L.tex_mode == 2) lut_sample_lin<NF>(L, x, y, out);
+    else lut_sample_tex<NF>(L, x, y, out);
+  } else {
+    lut_sample<float, NF>(L, x, y, out);
+  }
 }
 
 // Single-precision approximations (the PTX .approx forms, flush-to-zero) for
@@ -291,9 +299,9 @@ struct Coef {
 template <int KIND>
 __device__ __forceinline__ void coef_f32(const ProblemDev& P, float x, float y, Coef<float>& k) {
   const float PI = 3.14159265358979f;
-  if (KIND == PK_LUT) {
+  if (is_lut_kind(KIND)) {
     float v[8];
-    lut_sample_f32<8>(P.lut, x, y, v);
+    lut_sample_f32<KIND, 8>(P.lut, x, y, v);
     k.s00 = v[0]; k.s01 = 0.f; k.s10 = 0.f; k.s11 = v[1];
     k.b0 = v[2]; k.b1 = v[3]; k.c = v[4]; k.f = v[5]; k.g0 = v[6]; k.g1 = v[7];
   } else if (KIND == PK_POISSON_SINCOS) {
@@ -389,16 +397,16 @@ template <int KIND>
 struct KindTraits {
   static constexpr bool iso = KIND == PK_POISSON_SINCOS || KIND == PK_MONEGROS || KIND == PK_HELMHOLTZ ||
                               KIND == PK_CIRCLE || KIND == PK_ROBIN;
-  static constexpr bool react = KIND == PK_HELMHOLTZ || KIND == PK_VARCOEF || KIND == PK_LUT;
+  static constexpr bool react = KIND == PK_HELMHOLTZ || KIND == PK_VARCOEF || is_lut_kind(KIND);
 };
 
 // sigma alone (for the exit threshold)
 template <int KIND>
 __device__ __forceinline__ void sigma_f32(const ProblemDev& P, float x, float y, float& s00, float& s01,
                                           float& s10, float& s11) {
-  if (KIND == PK_LUT) {
+  if (is_lut_kind(KIND)) {
     float v[4];
-    lut_sample_f32<4>(P.lut, x, y, v);
+    lut_sample_f32<KIND, 4>(P.lut, x, y, v);
     s00 = v[0]; s01 = 0.f; s10 = 0.f; s11 = v[1];
   } else if (KIND == PK_VARCOEF) {
     s00 = 1.f + 0.5f * (x * x); s01 = 0.f; s10 = 0.f; s11 = 1.f + 0.5f * (y * y);
@@ -412,9 +420,9 @@ __device__ __forceinline__ void sigma_f32(const ProblemDev& P, float x, float y,
 // |N^T sigma| for the x normal (1,0) and the y normal (0,1) (diagonal sigma)
 template <int KIND>
 __device__ __forceinline__ void sigma_normals_f32(const ProblemDev& P, float x, float y, float& nx, float& ny) {
-  if (KIND == PK_LUT) {
+  if (is_lut_kind(KIND)) {
     float v[4];
-    lut_sample_f32<4>(P.lut, x, y, v);
+    lut_sample_f32<KIND, 4>(P.lut, x, y, v);
     nx = fabsf(v[0]);
     ny = fabsf(v[1]);
   } else if (KIND == PK_VARCOEF) {
@@ -429,7 +437,7 @@ __device__ __forceinline__ void sigma_normals_f32(const ProblemDev& P, float x, 
 
 template <int KIND>
 __device__ __forceinline__ float u_f32(const ProblemDev& P, float x, float y) {
-  if (KIND == PK_LUT) {
+  if (is_lut_kind(KIND)) {
     return lut_sample_g<float>(P.lut, x, y);
   } else if (KIND == PK_POISSON_SINCOS) {
     float sx, cx, sy, cy;
@@ -457,7 +465,7 @@ __device__ __forceinline__ float u_f32(const ProblemDev& P, float x, float y) {
 template <int KIND>
 __device__ __forceinline__ void coef_f64(const ProblemDev& P, double x, double y, Coef<double>& k) {
   const double PI = 3.141592653589793;
-  if (KIND == PK_LUT) {
+  if (is_lut_kind(KIND)) {
     double v[8];
     lut_sample<double, 8>(P.lut, x, y, v);
     k.s00 = v[0]; k.s01 = 0.0; k.s10 = 0.0; k.s11 = v[1];
@@ -539,7 +547,7 @@ __device__ __forceinline__ void coef_f64(const ProblemDev& P, double x, double y
 
 template <int KIND>
 __device__ __forceinline__ double u_f64(const ProblemDev& P, double x, double y) {
-  if (KIND == PK_LUT) {
+  if (is_lut_kind(KIND)) {
     return lut_sample_g<double>(P.lut, x, y);
   } else if (KIND == PK_POISSON_SINCOS) {
     double sx, cx, sy, cy;

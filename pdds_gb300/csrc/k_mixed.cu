@@ -53,6 +53,8 @@ struct Lvl<PK_LUT> {
   unsigned steps;
   float cf[8];
 };
+template <>
+struct Lvl<PK_LUT_TEX> : Lvl<PK_LUT> {};
 
 // Exit queue of a warp: a lane whose path pair has finished pushes both
 // levels' exit states (x, y, Y, Z + xi of the fine level, then of the coarse
@@ -107,12 +109,17 @@ __device__ __forceinline__ u32x4 path_block_rk(const uint32_t (&rk)[20], uint32_
   return c;
 }
 
-// Table-served coefficients (PK_LUT) need more live registers for the
-// bicubic accumulation: 128 registers there, 64 otherwise.  The block size
-// is chosen at launch (mixed_threads: 128 or 256 threads), with
-// 2048 / 4096 threads' worth of registers per SM either way.
-template <int KIND, bool RICH, int GEOM>
-__global__ void __launch_bounds__(MIXED_MAX_THREADS, KIND == PK_LUT ? 2 : 4)
+// Table-served coefficients sampled from the nodes (PK_LUT) need more live
+// registers for the bicubic accumulation: 128 registers there; the texture
+// samplers (PK_LUT_TEX) leave the interpolation to the texture units and
+// run with LUT_TEX_MIN_BLOCKS blocks' worth; 64 otherwise.  The block size
+// is chosen at launch (mixed_threads: 128 or 256 threads).
+constexpr int LUT_TEX_MIN_BLOCKS = 2;
+// DIAG: the instantiation that also accumulates the reduction's diagnostic
+// sums (pdds_estimate_diagnostics); a separate one, so that the estimate
+// without them carries none of that code.
+template <int KIND, bool RICH, int GEOM, bool DIAG>
+__global__ void __launch_bounds__(MIXED_MAX_THREADS, KIND == PK_LUT ? 2 : (KIND == PK_LUT_TEX ? LUT_TEX_MIN_BLOCKS : 4))
 k_paths_mixed(const MixedArgs a) {
   // dynamic shared memory: the warps' exit queues, then the exit histograms
   // [sum nbins] (and the Y^2 histogram after them)
@@ -126,7 +133,7 @@ k_paths_mixed(const MixedArgs a) {
   __shared__ double s_red[MIXED_MAX_THREADS / 32][4];
   __shared__ unsigned long long s_redi[MIXED_MAX_THREADS / 32][3];
   __shared__ unsigned s_sth[32];  // this item's paths by steps (log2 bins), when step_hist is set
-  __shared__ double s_dg[PDDS_DIAG_N];  // this item's diagnostic sums, when diag is set
+  __shared__ double s_dg[DIAG ? PDDS_DIAG_N : 1];  // this item's diagnostic sums (DIAG)
   // exit queue of each warp: word w of slot i at q[w][i]
   constexpr int QW = RICH ? 9 : 5;
   const int nthr = blockDim.x, nwarps = nthr >> 5;
@@ -226,7 +233,7 @@ k_paths_mixed(const MixedArgs a) {
     const int nh = a.want_var ? 2 * hist_len : hist_len;
     for (int i = tid; i < nh; i += nthr) hist[i] = 0.f;
     if (tid < 32) s_sth[tid] = 0u;
-    if (tid < PDDS_DIAG_N) s_dg[tid] = 0.0;
+    if (DIAG && tid < PDDS_DIAG_N) s_dg[tid] = 0.0;
     float* hist2 = hist + hist_len;
     __syncthreads();
 
@@ -313,7 +320,7 @@ k_paths_mixed(const MixedArgs a) {
     // back along -n and enters dZ = psi Y dL, dY = varphi Y dL.
     auto advance = [&](Lvl<KIND>& s, float e0, float e1, float hh, float thr, float ex) -> bool {
       Coef<float> k;
-      if constexpr (KIND == PK_LUT) {
+      if constexpr (is_lut_kind(KIND)) {
         k.s00 = s.cf[0]; k.s11 = s.cf[1];
         k.b0 = s.cf[2]; k.b1 = s.cf[3]; k.c = s.cf[4]; k.f = s.cf[5];
         k.g0 = s.cf[6]; k.g1 = s.cf[7];
@@ -365,8 +372,8 @@ k_paths_mixed(const MixedArgs a) {
       } else {
         const float dx = fabsf(s.x - cx) - hx, dy = fabsf(s.y - cy) - hy;
         float t = thr;
-        if constexpr (KIND == PK_LUT) {
-          lut_sample_f32<8>(P.lut, s.x, s.y, s.cf);
+        if constexpr (is_lut_kind(KIND)) {
+          lut_sample_f32<KIND, 8>(P.lut, s.x, s.y, s.cf);
           t *= dx > dy ? fabsf(s.cf[0]) : fabsf(s.cf[1]);
         } else if constexpr (!KindTraits<KIND>::iso) {
           float nx, ny;  // |N^T sigma| for the x and y normals
@@ -583,11 +590,11 @@ k_paths_mixed(const MixedArgs a) {
       }
     };
 
-    float cf0[8];  // table fields at the knot (PK_LUT)
-    if constexpr (KIND == PK_LUT) lut_sample_f32<8>(P.lut, x0, y0, cf0);
+    float cf0[8];  // table fields at the knot (table-served kinds)
+    if constexpr (is_lut_kind(KIND)) lut_sample_f32<KIND, 8>(P.lut, x0, y0, cf0);
     auto reset = [&]() {
       F.x = x0; F.y = y0; F.Y = 1.f; F.Z = 0.f; F.xi = 0.f; F.steps = 0;
-      if constexpr (KIND == PK_LUT) {
+      if constexpr (is_lut_kind(KIND)) {
 #pragma unroll
         for (int f = 0; f < 8; f++) F.cf[f] = cf0[f];
       }
@@ -645,23 +652,21 @@ k_paths_mixed(const MixedArgs a) {
             atomicAdd(&s_sth[31 - __clz(max(F.steps, 1u))], 1u);
             if (RICH) atomicAdd(&s_sth[31 - __clz(max(Cs.steps, 1u))], 1u);
           }
-          if constexpr (GEOM == 0) {
-            if (a.diag) {
-              // phi = Z + Y g at the nearest point of the stencil rectangle
-              // (the exit projection), per level; a pair adds 2 fine - coarse
-              auto phi_of = [&](const Lvl<KIND>& v) -> float {
-                float Ex, Ey, Nx, Ny;
-                int om;
-                rect2d<float>(rect, v.x, v.y, Ex, Ey, Nx, Ny, om);
-                return v.Z + v.Y * u_f32<KIND>(P, Ex, Ey);
-              };
-              float ph = phi_of(F), xv = F.xi;
-              if (RICH) {
-                ph = 2.f * ph - phi_of(Cs);
-                xv = 2.f * xv - Cs.xi;
-              }
-              diag_add(s_dg, ph, xv, (double)F.steps * (RICH ? 0.5 * (double)h : (double)h), 2.0 * F.steps);
+          if constexpr (DIAG && GEOM == 0) {
+            // phi = Z + Y g at the nearest point of the stencil rectangle
+            // (the exit projection), per level; a pair adds 2 fine - coarse
+            auto phi_of = [&](const Lvl<KIND>& v) -> float {
+              float Ex, Ey, Nx, Ny;
+              int om;
+              rect2d<float>(rect, v.x, v.y, Ex, Ey, Nx, Ny, om);
+              return v.Z + v.Y * u_f32<KIND>(P, Ex, Ey);
+            };
+            float ph = phi_of(F), xv = F.xi;
+            if (RICH) {
+              ph = 2.f * ph - phi_of(Cs);
+              xv = 2.f * xv - Cs.xi;
             }
+            diag_add(s_dg, ph, xv, (double)F.steps * (RICH ? 0.5 * (double)h : (double)h), 2.0 * F.steps);
           }
           nsteps += F.steps + (RICH ? Cs.steps : 0u);
           path = base + __popc(dm & lt);
@@ -707,7 +712,7 @@ k_paths_mixed(const MixedArgs a) {
       atomicAdd(a.stats + 3, tt);
     }
     if (a.step_hist && tid < 32 && s_sth[tid]) atomicAdd(a.step_hist + tid, (unsigned long long)s_sth[tid]);
-    if (a.diag) diag_flush(s_dg, a.diag + (int64_t)knot * PDDS_DIAG_N, tid);
+    if constexpr (DIAG) diag_flush(s_dg, a.diag + (int64_t)knot * PDDS_DIAG_N, tid);
     // ------------------------------------------------------------ contract G
     const int64_t row0 = L.row_ptr[knot];
     const double invN = a.knot_invN ? a.knot_invN[knot] : a.inv_N;
@@ -746,10 +751,16 @@ k_paths_mixed(const MixedArgs a) {
 // Polar stencils are instantiated for the isotropic problems only.
 template <bool RICH>
 static cudaError_t launch_mixed_t(const MixedArgs& a, int kind, int grid, int threads, size_t smem, cudaStream_t s) {
-#define PDDS_MIXED_CASE(KK, GG)                                                                           \
-  case KK:                                                                                                \
-    cudaFuncSetAttribute(k_paths_mixed<KK, RICH, GG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
-    k_paths_mixed<KK, RICH, GG><<<grid, threads, smem, s>>>(a);                                           \
+#define PDDS_MIXED_LAUNCH(KK, GG, DD)                                                                         \
+  cudaFuncSetAttribute(k_paths_mixed<KK, RICH, GG, DD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+  k_paths_mixed<KK, RICH, GG, DD><<<grid, threads, smem, s>>>(a);
+#define PDDS_MIXED_CASE(KK, GG)            \
+  case KK:                                 \
+    if (GG == 0 && a.diag) {               \
+      PDDS_MIXED_LAUNCH(KK, GG * 0, true)  \
+    } else {                               \
+      PDDS_MIXED_LAUNCH(KK, GG, false)     \
+    }                                      \
     break;
   if (a.L.geom == 1) {
     switch (kind) {
@@ -766,10 +777,12 @@ static cudaError_t launch_mixed_t(const MixedArgs& a, int kind, int grid, int th
       PDDS_MIXED_CASE(4, 0)
       PDDS_MIXED_CASE(5, 0)
       PDDS_MIXED_CASE(6, 0)
+      PDDS_MIXED_CASE(7, 0)
       default: return cudaErrorInvalidValue;
     }
   }
 #undef PDDS_MIXED_CASE
+#undef PDDS_MIXED_LAUNCH
   return cudaGetLastError();
 }
 
@@ -805,11 +818,11 @@ void mixed_set_rng(MixedArgs& a, uint64_t seed, uint32_t instance) {
 
 template <bool RICH>
 static bool is_mixed_t(const void* f) {
-  return f == (const void*)k_paths_mixed<0, RICH, 0> || f == (const void*)k_paths_mixed<1, RICH, 0> ||
-         f == (const void*)k_paths_mixed<2, RICH, 0> || f == (const void*)k_paths_mixed<3, RICH, 0> ||
-         f == (const void*)k_paths_mixed<4, RICH, 0> || f == (const void*)k_paths_mixed<5, RICH, 0> ||
-         f == (const void*)k_paths_mixed<6, RICH, 0> ||
-         f == (const void*)k_paths_mixed<0, RICH, 1> || f == (const void*)k_paths_mixed<5, RICH, 1>;
+  return f == (const void*)k_paths_mixed<0, RICH, 0, false> || f == (const void*)k_paths_mixed<1, RICH, 0, false> ||
+         f == (const void*)k_paths_mixed<2, RICH, 0, false> || f == (const void*)k_paths_mixed<3, RICH, 0, false> ||
+         f == (const void*)k_paths_mixed<4, RICH, 0, false> || f == (const void*)k_paths_mixed<5, RICH, 0, false> ||
+         f == (const void*)k_paths_mixed<6, RICH, 0, false> || f == (const void*)k_paths_mixed<7, RICH, 0, false> ||
+         f == (const void*)k_paths_mixed<0, RICH, 1, false> || f == (const void*)k_paths_mixed<5, RICH, 1, false>;
 }
 
 bool is_mixed_path_kernel(const void* func) { return is_mixed_t<true>(func) || is_mixed_t<false>(func); }
@@ -824,13 +837,13 @@ cudaError_t launch_paths_mixed(const MixedArgs& a, int kind, int grid, int threa
                       : launch_mixed_t<false>(a, kind, grid, threads, smem, s);
 }
 
-template <bool RICH>
+template <bool RICH, bool DIAG>
 static int blocks_t(int kind, size_t smem, int threads) {
   int nb = 0;
-#define PDDS_OCC(KK)                                                                                    \
-  case KK:                                                                                              \
-    cudaFuncSetAttribute(k_paths_mixed<KK, RICH, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_paths_mixed<KK, RICH, 0>, threads, smem);       \
+#define PDDS_OCC(KK)                                                                                          \
+  case KK:                                                                                                    \
+    cudaFuncSetAttribute(k_paths_mixed<KK, RICH, 0, DIAG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_paths_mixed<KK, RICH, 0, DIAG>, threads, smem);       \
     break;
   switch (kind) {
     PDDS_OCC(0)
@@ -839,6 +852,7 @@ static int blocks_t(int kind, size_t smem, int threads) {
     PDDS_OCC(4)
     PDDS_OCC(5)
     PDDS_OCC(6)
+    PDDS_OCC(7)
     default:
     PDDS_OCC(3)
   }
@@ -846,8 +860,9 @@ static int blocks_t(int kind, size_t smem, int threads) {
   return nb;
 }
 
-int mixed_blocks_per_sm(int kind, size_t smem, int richardson, int threads) {
-  return richardson ? blocks_t<true>(kind, smem, threads) : blocks_t<false>(kind, smem, threads);
+int mixed_blocks_per_sm(int kind, size_t smem, int richardson, int threads, bool diag) {
+  if (diag) return richardson ? blocks_t<true, true>(kind, smem, threads) : blocks_t<false, true>(kind, smem, threads);
+  return richardson ? blocks_t<true, false>(kind, smem, threads) : blocks_t<false, false>(kind, smem, threads);
 }
 
 }  // namespace pdds

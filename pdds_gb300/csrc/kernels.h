@@ -150,6 +150,10 @@ struct ReplayArgs {
   unsigned* err_flags;
 };
 
+// The FP32 path-kernel instantiation of a problem: table-served problems
+// with textures run PK_LUT_TEX, every other problem its own kind.
+inline int mixed_kind(const ProblemDev& P) { return P.kind == PK_LUT && P.lut.tex_mode ? PK_LUT_TEX : P.kind; }
+
 // smem: mixed_queue_smem(threads, richardson) + the exit histograms
 cudaError_t launch_paths_mixed(const MixedArgs& a, int kind, int grid, int threads, size_t smem, cudaStream_t s);
 size_t mixed_queue_smem(int threads, int richardson);
@@ -168,7 +172,7 @@ void portable_math_check_host(int fn, const double* x, int n, double* out);
 // True when `func` is one of the MIXED path kernels (a captured graph's
 // nodes are re-keyed with a new seed through their parameters).
 bool is_mixed_path_kernel(const void* func);
-int mixed_blocks_per_sm(int kind, size_t smem, int richardson, int threads);
+int mixed_blocks_per_sm(int kind, size_t smem, int richardson, int threads, bool diag = false);
 cudaError_t launch_paths_fp64(const Fp64Args& a, int kind, int grid, size_t smem, cudaStream_t s);
 int fp64_blocks_per_sm(int kind, size_t smem, int richardson);
 cudaError_t launch_replay_paths(const ReplayArgs& a, int kind, cudaStream_t s);
