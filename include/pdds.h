@@ -457,10 +457,12 @@ typedef struct {
   int32_t use_graph;           /* 1: capture the sequence in a CUDA graph on
                                   the first run and replay it while the batch
                                   and the descriptor stay the same          */
-  /* the instances run in this many consecutive groups (0 = 16, at most the
-   * instance count): one path-kernel launch per group, and the solves of a
-   * group, on a second stream of higher priority, overlap the next group's
-   * paths, so an instance completes when its group does */
+  /* the instances run in this many consecutive groups of the order given to
+   * pdds_batch_build (0 = 16, at most the instance count): one path-kernel
+   * launch per group, and the solves of a group, on a second stream of
+   * higher priority, overlap the next group's paths, so an instance
+   * completes when its group does; instances given smallest first complete
+   * soonest on average */
   int32_t waves;
 } pdds_batch_run_desc;
 

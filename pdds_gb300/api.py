@@ -606,10 +606,22 @@ class PDDSparseGM:
         return u, {f: getattr(info, f) for f, _ in capi.SolveInfo._fields_}
 
     def Solve(self, bvp: BVP, npaths: int, h: float, mode: int = capi.MODE_MIXED, seed: int = 1234,
-              method: int = capi.SOLVE_GMRES_FP32_IR, tol: float = 1e-10, **kw):
-        """Estimate G and B for all knots, then solve the interface system."""
+              method: int = capi.SOLVE_GMRES_FP32_IR, tol: float = 1e-10, trace_dir: str = None, **kw):
+        """Estimate G and B for all knots, then solve the interface system.
+        trace_dir: also write the reference's phase trace
+        (trace_dir/Output/Debug/times.txt) and its output files there."""
+        tf = None
+        if trace_dir is not None:
+            from .output_files import TimeFile
+            tf = TimeFile(trace_dir)
         est = self.estimate(bvp, npaths, h, mode=mode, seed=seed, **kw)
+        if tf:
+            tf.update("MC Simulations")
         u, sinfo = self.solve_interface(method=method, tol=tol)
+        if tf:
+            tf.update("Solving system")
+            self.write_outputs(trace_dir, est, u, bvp)
+            tf.update("Writing Solution")
         return u, est, sinfo
 
 
@@ -803,14 +815,23 @@ class Batch:
     """Many independent instances of one problem kind solved as one sequence.
 
     No counterpart in the reference, whose PDDSparseGM solves one problem per
-    run.  All instances' knots are estimated by one path-kernel launch and all
-    interface systems are solved by one cluster-GMRES launch; with
-    use_graph=True the sequence is captured once in a CUDA graph and replayed.
-    Instance i uses Philox instance word `instance + i` and its own knot
-    numbering, so its random stream equals the one of a PDDSparseGM run of
-    that instance alone with instance word `instance + i`."""
+    run.  The instances run in waves (consecutive groups in processing
+    order): one path-kernel launch per wave, and one cluster-GMRES launch per
+    wave on a higher-priority stream while the next wave's paths run; with
+    use_graph=True the sequence is captured once in a CUDA graph and
+    replayed.  order="smallest_first" processes the instances by increasing
+    knot count, so the small ones finish in the first waves (lower median
+    latency, the same batch time); indices in knots() and result() stay the
+    caller's.  The instance at processing position j uses Philox instance
+    word `instance + j` and its own knot numbering, so its random stream
+    equals the one of a PDDSparseGM run of that instance alone with instance
+    word `instance + j` (j = i in the given order)."""
 
-    def __init__(self, kind: int, instances, use_cv: bool = True, device: int = 0):
+    ORDERS = ("given", "smallest_first")
+
+    def __init__(self, kind: int, instances, use_cv: bool = True, device: int = 0, order: str = "given"):
+        if order not in self.ORDERS:
+            raise ValueError(f"order must be one of {self.ORDERS}")
         self._lib = capi.load()
         self._ctx = C.c_void_p()
         st = self._lib.pdds_create(C.byref(self._ctx), int(device), 0)
@@ -820,9 +841,20 @@ class Batch:
         self.use_cv = bool(use_cv)
         self.instances = list(instances)
         n = len(self.instances)
+        # processing position of each instance (pos[i]) and its inverse
+        if order == "smallest_first":
+            from .config import layout_knot_count
+            size = [layout_knot_count(ins.nsub, ins.nnode) for ins in self.instances]
+            self._proc = sorted(range(n), key=lambda i: (size[i], i))
+        else:
+            self._proc = list(range(n))
+        self._pos = [0] * n
+        for j, i in enumerate(self._proc):
+            self._pos[i] = j
         arr = (capi.InstanceDesc * n)()
-        for i, ins in enumerate(self.instances):
-            d = arr[i]
+        for j, i in enumerate(self._proc):
+            ins = self.instances[i]
+            d = arr[j]
             d.layout.sw[0], d.layout.sw[1] = float(ins.sw[0]), float(ins.sw[1])
             d.layout.ne[0], d.layout.ne[1] = float(ins.ne[0]), float(ins.ne[1])
             d.layout.nsub = int(ins.nsub)
@@ -891,18 +923,25 @@ class Batch:
         self._check(self._lib.pdds_batch_run(self._ctx, C.byref(d), C.byref(info)))
         return {f: getattr(info, f) for f, _ in capi.BatchRunInfo._fields_}
 
+    def position(self, i: int) -> int:
+        """Processing position of instance i (its Philox instance word is the
+        run's instance word plus this)."""
+        return self._pos[int(i)]
+
     def knots(self, i: int):
+        j = self._pos[int(i)]
         n = C.c_int32()
-        self._check(self._lib.pdds_batch_instance(self._ctx, int(i), C.byref(n), None, None, None, None, None,
+        self._check(self._lib.pdds_batch_instance(self._ctx, j, C.byref(n), None, None, None, None, None,
                                                   None, None))
         x = np.zeros(n.value)
         y = np.zeros(n.value)
-        self._check(self._lib.pdds_batch_instance(self._ctx, int(i), None, _p(x, C.c_double), _p(y, C.c_double),
+        self._check(self._lib.pdds_batch_instance(self._ctx, j, None, _p(x, C.c_double), _p(y, C.c_double),
                                                   None, None, None, None, None))
         return x, y
 
     def result(self, i: int) -> dict:
         """u, B, solver iterations, relative residual and latency (ms) of instance i."""
+        i = self._pos[int(i)]
         n = C.c_int32()
         self._check(self._lib.pdds_batch_instance(self._ctx, int(i), C.byref(n), None, None, None, None, None,
                                                   None, None))

@@ -64,6 +64,13 @@ def varcoef_tables(n: int = 1024, bounds=(0.0, 0.0, 1.0, 1.0)):
     return np.ascontiguousarray(coef), np.ascontiguousarray(u.astype(np.float32)), tuple(float(b) for b in bounds)
 
 
+def layout_knot_count(nsub: int, nnode: int) -> int:
+    """Knots of an nsub x nsub layout with nnode knots per interface segment
+    (shared cross knots counted once): (g-1)(g(n-1)+1) + (g-1)(g(n-2)+2)."""
+    g, n = int(nsub), int(nnode)
+    return (g - 1) * (g * (n - 1) + 1) + (g - 1) * (g * (n - 2) + 2)
+
+
 def instance_step(g: int, h_ref: float = 1e-3, g_ref: int = 4) -> float:
     """Step of an instance with g x g subdomains on the unit square: h_ref at
     g_ref x g_ref, scaled with the square of the subdomain size above it, so

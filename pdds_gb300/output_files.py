@@ -69,6 +69,31 @@ def write_outputs(directory: str, x, y, row_ptr, col, G, G_var, B, BB, u, u_exac
             f.write("%d,%e,%e,%e,%e,%e,%e\n" % (i, x[i], y[i], ex[i], u[i], err[i], rerr[i]))
 
 
+class TimeFile:
+    """The reference's phase trace, Output/Debug/times.txt (Update_TimeFile,
+    PDDAlgorithms/PDDSparseGM.cpp:4397-4404): one line per phase,
+    `task,total since start,phase time,processes` in C's %e, under the
+    reference's header.  The clock starts when the object is made."""
+
+    HEADER = "task,total_tike,task_time,N_process"
+
+    def __init__(self, directory: str):
+        import time
+        self._time = time.perf_counter
+        dbg = os.path.join(directory, "Output", "Debug")
+        os.makedirs(dbg, exist_ok=True)
+        self.path = os.path.join(dbg, "times.txt")
+        with open(self.path, "w") as f:
+            f.write(self.HEADER + "\n")
+        self.start = self.prev = self._time()
+
+    def update(self, task: str, n_processors: int = 1):
+        now = self._time()
+        with open(self.path, "a") as f:
+            f.write("%s,%e,%e,%d\n" % (task, now - self.start, now - self.prev, n_processors))
+        self.prev = now
+
+
 KNOT_METADATA_COLUMNS = ("APL", "WCtime", "RNGCalls", "Estimated_Variance", "Estimated_Variance_VR",
                          "PCoeff_old", "PCoeff_new", "Var_Plain", "Var_VR", "bias_num", "bias_trap")
 

@@ -7,6 +7,7 @@ BVPs/EDPs/Monegros_Poisson_CPP.hpp, driver main_EXTENDED.cpp):
   Output/Debug/cond.txt   RBF matrix condition numbers per stencil side
   Output/Debug/G.csv, G_var.csv, B.csv, B_var.csv   the estimated system
   Output/solution.csv     interface solution vs analytic
+  Output/Debug/times.txt  the phase trace (only its header line is kept)
 This script copies those numbers into compact fixtures.  It reads the
 reference checkout and is run by hand in a container that has it; the
 fixtures it writes are committed so the tests never need the reference.
@@ -48,6 +49,11 @@ def main(ref):
                         config=np.array([-5.0, -5.0, 5.0, 5.0, 4, 8, 5000, 0.005,
                                          1.5, 1.27, 1.2, 1.13]))
     print("wrote", out, os.path.getsize(out), "bytes")
+    with open(os.path.join(ref, "Output/Debug/times.txt")) as f:
+        header = f.readline().strip()
+    with open(os.path.join(HERE, "times_header.txt"), "w") as f:
+        f.write(header + "\n")
+    print("wrote", os.path.join(HERE, "times_header.txt"))
 
 
 if __name__ == "__main__":

@@ -37,6 +37,26 @@ def test_batch_instance_equals_single_run():
             assert rmse < 5e-2, rmse
 
 
+def test_smallest_first_order_keeps_the_callers_indices():
+    """order="smallest_first" runs the instances by increasing knot count;
+    every result still belongs to the caller's index i, and instance i draws
+    the stream of its processing position."""
+    insts = small_instances()[::-1]  # 472 (5x5/13), 465 (6x6/9), 237 (4x4/11) knots
+    with P.Batch(P.BVP.HELMHOLTZ, insts, order="smallest_first") as bt:
+        assert [bt.position(i) for i in range(3)] == [2, 1, 0]
+        info = bt.run(N, H, seed=11, instance=100, adaptive_h=True, use_graph=True)
+        assert info["unconverged"] == 0
+        res = [(bt.result(i), bt.knots(i), bt.position(i)) for i in range(len(insts))]
+    for i, ins in enumerate(insts):
+        r, (x, y), j = res[i]
+        with P.PDDSparseGM(ins.sw, ins.ne, ins.nsub, ins.nnode, ins.fac) as pd:
+            assert len(x) == pd.K
+            np.testing.assert_array_equal(x, pd.x)
+            est = pd.estimate(P.BVP.helmholtz(*ins.params), N, H, mode=P.MODE_MIXED, seed=11, instance=100 + j,
+                              adaptive_h=True)
+            assert np.max(np.abs(r["B"] - est.B)) < 1e-5
+
+
 def test_batch_graph_replay_matches_direct_launch():
     insts = small_instances()
     with P.Batch(P.BVP.HELMHOLTZ, insts) as bt:

@@ -48,3 +48,20 @@ def test_outputs_match_the_recorded_files(lib, tmp_path):
     s = np.loadtxt(os.path.join(str(tmp_path), "Output", "solution.csv"), delimiter=",", skiprows=1)
     assert np.allclose(s[:, :5], sol, rtol=2e-6)
     assert np.allclose(s[:, 5], sol[:, 4] - sol[:, 3], atol=2e-6 * np.abs(sol[:, 3]).max())
+
+
+def test_time_file_has_the_reference_format(tmp_path):
+    """Output/Debug/times.txt as Update_TimeFile writes it: the recorded run's
+    header, then task,total,phase,processes with C's %e."""
+    from pdds_gb300.output_files import TimeFile
+    rec = open(os.path.join(os.path.dirname(__file__), "golden", "times_header.txt")).read().strip()
+    tf = TimeFile(str(tmp_path))
+    tf.update("MC Simulations", 4)
+    tf.update("Solving system")
+    lines = open(tmp_path / "Output" / "Debug" / "times.txt").read().splitlines()
+    assert lines[0] == rec == TimeFile.HEADER
+    t, total, phase, n = lines[1].split(",")
+    assert t == "MC Simulations" and n == "4" and float(total) >= float(phase) >= 0.0
+    assert total == "%e" % float(total)
+    t2, total2, phase2, n2 = lines[2].split(",")
+    assert t2 == "Solving system" and n2 == "1" and float(total2) >= float(total)
