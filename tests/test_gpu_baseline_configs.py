@@ -184,3 +184,45 @@ def test_config3_sample_mixed_and_fp64_agree_with_oracle():
     for est, n in ((mixed, N), (fp64, N64)):
         zf, zb = _compare(est, n, L, ref, O.make_problem(O.LUT), prm, fac, gx, gy)
         _assert_standard_normal(zf, zb)
+
+
+def test_config5_instances_agree_with_oracle():
+    """Four instances of the many-instance workload (Helmholtz, each on its
+    own g x g grid with the step h (4/g)^2), the coarsest and finest grids
+    among them: MIXED rows and B of each instance run alone, and B of the
+    same instances run as one batch, against the oracle on 4 seeded knots of
+    each (plain method, independent streams)."""
+    from pdds_gb300.config import batch_instances
+    insts = batch_instances(256, seed=1234, scaled_h=1e-3)
+    order = sorted(range(len(insts)), key=lambda i: (insts[i].nsub, i))
+    pick = [insts[i] for i in (order[0], order[1], order[-2], order[-1])]
+    assert pick[0].nsub == 4 and pick[-1].nsub == 16
+    N = 10_000
+    zf_all, zb_all, zbb_all = [], [], []
+    with P.Batch(P.BVP.HELMHOLTZ, pick) as bt:
+        bt.run(N, 1e-3, seed=1234, instance=0, adaptive_h=False, richardson=False, use_graph=False)
+        batch_B = [bt.result(i)["B"] for i in range(len(pick))]
+    for q, ins in enumerate(pick):
+        fac = ins.fac
+        L = O.Layout(ins.sw, ins.ne, ins.nsub, ins.nnode)
+        w = {"sw": ins.sw, "ne": ins.ne}
+        sel = _sample(L, w, 4, seed=100 + q)
+        prob = O.make_problem(O.HELMHOLTZ, *ins.params)
+        prm = O.make_params(N, ins.h, seed=4321 + q, fac=fac, sublinear=False, fast_reduce=True)
+        ref = L.run(prob, prm, knots=sel)
+        assert ref["status"] == 0
+        with P.PDDSparseGM(ins.sw, ins.ne, ins.nsub, ins.nnode, fac) as pd:
+            est = pd.estimate(P.BVP.helmholtz(*ins.params), N, ins.h, mode=P.MODE_MIXED, seed=1234,
+                              instance=q, want_var=True)
+            gx, gy = pd.x.copy(), pd.y.copy()
+        zf, zb = _compare(est, N, L, ref, prob, prm, fac, gx, gy)
+        zf_all += list(zf)
+        zb_all += list(zb)
+        # the batch drew the same streams for instance q (word 0 + q): B as alone
+        np.testing.assert_allclose(batch_B[q], est.B, rtol=0, atol=1e-5)
+        for k, kn in enumerate(ref["knots"]):
+            vb = (est.BB[kn] - est.B[kn] ** 2) / N + (ref["BB"][k] - ref["B"][k] ** 2) / N
+            if vb > 1e-20:
+                zbb_all.append((batch_B[q][kn] - ref["B"][k]) / np.sqrt(vb))
+    _assert_standard_normal(np.array(zf_all), np.array(zb_all))
+    assert np.abs(np.array(zbb_all)).max() < 4.5
