@@ -40,7 +40,9 @@ typedef enum {
   PDDS_ERR_ILL_CONDITIONED = 5, /* an RBF matrix is numerically singular */
   PDDS_ERR_NOT_CONVERGED = 6,   /* interface solve missed its tolerance  */
   PDDS_ERR_NO_MEMORY = 7,
-  PDDS_ERR_EXIT_SIDE = 8        /* an exit matched no stencil side       */
+  PDDS_ERR_EXIT_SIDE = 8,       /* an exit matched no stencil side       */
+  PDDS_ERR_BOUNDS = 9           /* a device index check failed (only the
+                                   checked build, -DPDDS_CHECKED, checks) */
 } pdds_status;
 
 typedef struct pdds_ctx pdds_ctx;

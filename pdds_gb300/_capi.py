@@ -13,10 +13,10 @@ LIB_PATH = os.path.join(HERE, "_build", "libpdds_gb300.so")
 
 # status codes
 OK, ERR_INVALID, ERR_CUDA, ERR_STEP_LIMIT, ERR_TIMEOUT, ERR_ILL_CONDITIONED, ERR_NOT_CONVERGED, \
-    ERR_NO_MEMORY, ERR_EXIT_SIDE = range(9)
+    ERR_NO_MEMORY, ERR_EXIT_SIDE, ERR_BOUNDS = range(10)
 STATUS_NAMES = {0: "PDDS_OK", 1: "PDDS_ERR_INVALID", 2: "PDDS_ERR_CUDA", 3: "PDDS_ERR_STEP_LIMIT",
                 4: "PDDS_ERR_TIMEOUT", 5: "PDDS_ERR_ILL_CONDITIONED", 6: "PDDS_ERR_NOT_CONVERGED",
-                7: "PDDS_ERR_NO_MEMORY", 8: "PDDS_ERR_EXIT_SIDE"}
+                7: "PDDS_ERR_NO_MEMORY", 8: "PDDS_ERR_EXIT_SIDE", 9: "PDDS_ERR_BOUNDS"}
 
 POISSON_SINCOS, MONEGROS, HELMHOLTZ, VARCOEF, LUT, CIRCLE_POISSON, ROBIN_POISSON = 0, 1, 2, 3, 4, 5, 6
 MODE_REPLAY_FP64, MODE_FP64, MODE_MIXED = 0, 1, 2

@@ -53,8 +53,20 @@ def _newer(target: str, deps) -> bool:
     return all(os.path.getmtime(d) <= t for d in deps)
 
 
-def build(force: bool = False, verbose: bool = False, extra=None) -> str:
-    os.makedirs(OUT_DIR, exist_ok=True)
+OUT_DIR_CHECKED = os.path.join(HERE, "_build_checked")
+LIB_CHECKED = os.path.join(OUT_DIR_CHECKED, "libpdds_gb300.so")
+
+
+def build(force: bool = False, verbose: bool = False, extra=None, checked: bool = False) -> str:
+    """Compiles the library (pdds_gb300/_build) and returns its path.
+    checked=True builds the index-checked library instead
+    (pdds_gb300/_build_checked, -DPDDS_CHECKED): every checked device index
+    that falls outside its array sets an error flag, the access is skipped
+    and the call returns PDDS_ERR_BOUNDS; for debugging and tests, slower."""
+    out_dir, lib = (OUT_DIR_CHECKED, LIB_CHECKED) if checked else (OUT_DIR, LIB)
+    if checked:
+        extra = list(extra or []) + ["-DPDDS_CHECKED"]
+    os.makedirs(out_dir, exist_ok=True)
     headers = [os.path.join(SRC, f) for f in os.listdir(SRC) if f.endswith((".h", ".cuh"))]
     headers.append(os.path.join(HERE, "..", "include", "pdds.h"))
     cc = nvcc()
@@ -62,7 +74,7 @@ def build(force: bool = False, verbose: bool = False, extra=None) -> str:
     objs = []
     for unit, flags in UNITS.items():
         src = os.path.join(SRC, unit)
-        obj = os.path.join(OUT_DIR, unit + ".o")
+        obj = os.path.join(out_dir, unit + ".o")
         objs.append(obj)
         if not force and _newer(obj, [src] + headers):
             continue
@@ -74,13 +86,13 @@ def build(force: bool = False, verbose: bool = False, extra=None) -> str:
                 sys.stderr.write(" ".join(cmd) + "\n" + res.stdout + res.stderr)
             if res.returncode != 0:
                 raise RuntimeError("nvcc failed for " + cmd[-3])
-    if force or jobs or not _newer(LIB, objs):
-        cmd = [cc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
+    if force or jobs or not _newer(lib, objs):
+        cmd = [cc] + ARCH + ["-shared", "-o", lib] + objs + ["-lcudart"]
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             sys.stderr.write(res.stdout + res.stderr)
             raise RuntimeError("link failed")
-    return LIB
+    return lib
 
 
 if __name__ == "__main__":

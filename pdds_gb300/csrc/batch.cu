@@ -41,6 +41,7 @@ pdds_status enqueue_batch(pdds_ctx* ctx, const pdds_batch_run_desc* d, int clust
   pdds_status st = enqueue_mixed(ctx, &d->estimate, launches, 0, 0, true);  // prefix only
   if (st != PDDS_OK) return st;
   ClusterGmresArgs a{};
+  a.err_flags = ctx->errf.p;
   a.K = ctx->L.K;
   a.row_ptr = ctx->row_ptr.p;
   a.col = ctx->col.p;

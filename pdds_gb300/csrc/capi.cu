@@ -321,6 +321,8 @@ pdds_status check_err_flags(pdds_ctx* ctx) {
   if (f & ERR_FLAG_SUB_NOCONV)
     return fail(ctx, PDDS_ERR_NOT_CONVERGED, "a subdomain solve missed its tolerance in 200 iterations");
   if (f & ERR_FLAG_TIMEOUT) return fail(ctx, PDDS_ERR_TIMEOUT, "a grid barrier of the interface solve timed out");
+  if (f & ERR_FLAG_BOUNDS)
+    return fail(ctx, PDDS_ERR_BOUNDS, "a device index check failed (checked build): an access was skipped");
   return PDDS_OK;
 }
 

@@ -180,9 +180,11 @@ k_paths_fp64(const Fp64Args a) {
         // queue the exit: < 32 left over + at most 2 exits per lane and
         // iteration fit in FP64_QCAP
         const int e = atomicAdd(&s_qn[warp], 1);
-        s_qd[warp][e] = d;
-        s_qs[warp][e] = along - s_side[d].origin;
-        s_qy[warp][e] = wgt * s.Y;
+        if (idx_ok(e, FP64_QCAP, a.err_flags)) {
+          s_qd[warp][e] = d;
+          s_qs[warp][e] = along - s_side[d].origin;
+          s_qy[warp][e] = wgt * s.Y;
+        }
       }
       return s.Z + s.xi;
     };
@@ -192,7 +194,7 @@ k_paths_fp64(const Fp64Args a) {
       __syncwarp();
       const int n = s_qn[warp];
       if (n < minq) return;
-      for (int e = 0; e < n; e++) {
+      for (int e = 0; e < min(n, FP64_QCAP); e++) {
         const ItemSide64& is = s_side[s_qd[warp][e]];
         const double sc = s_qs[warp][e], yw = s_qy[warp][e];
         for (int j = lane; j < is.n; j += 32) {
@@ -437,7 +439,8 @@ k_paths_fp64(const Fp64Args a) {
       const double* ip = L.ipsi + is.ipsi_off + i;
       double acc = 0.0;
       for (int j = 0; j < is.n; j++) acc += ip[(int64_t)j * is.n] * Ssum[is.s_off + j];
-      atomicAdd(a.G + row0 + L.map_pos[m], -acc * a.inv_N);
+      if (idx_ok(L.map_pos[m], L.row_ptr[knot + 1] - row0, a.err_flags))
+        atomicAdd(a.G + row0 + L.map_pos[m], -acc * a.inv_N);
     }
     __syncthreads();
   }

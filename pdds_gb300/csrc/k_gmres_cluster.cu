@@ -296,6 +296,7 @@ __device__ __forceinline__ void gmres_body(const ClusterGmresArgs& a, Group& grp
             const bool in = e + 32 * u < e1;
             v[u] = in ? __ldg(a.val64 + e + 32 * u) : 0.0;
             c[u] = in ? __ldg(a.col + e + 32 * u) - R0 : 0;
+            if (!idx_ok(c[u], nr, a.err_flags)) c[u] = 0;
           }
           acc0 += v[0] * s_vd[c[0]];
           acc1 += v[1] * s_vd[c[1]];
@@ -350,6 +351,7 @@ __device__ __forceinline__ void gmres_body(const ClusterGmresArgs& a, Group& grp
               const bool in = e + 32 * u < e1;
               v[u] = in ? __ldg(a.val32 + e + 32 * u) : 0.f;
               c[u] = in ? __ldg(a.col + e + 32 * u) - R0 : 0;
+              if (!idx_ok(c[u], nr, a.err_flags)) c[u] = 0;
             }
 #pragma unroll
             for (int u = 0; u < SPMV_U; u += 2) {
@@ -568,6 +570,7 @@ __device__ __forceinline__ void gmres_body_p1(const ClusterGmresArgs& a, Group& 
           const bool in = e + 32 * u < e1;
           v[u] = in ? __ldg(a.val32 + e + 32 * u) : 0.f;
           c[u] = in ? __ldg(a.col + e + 32 * u) - R0 : 0;
+          if (!idx_ok(c[u], nr, a.err_flags)) c[u] = 0;
         }
 #pragma unroll
         for (int u = 0; u < SPMV_U; u += 2) {
@@ -622,6 +625,7 @@ __device__ __forceinline__ void gmres_body_p1(const ClusterGmresArgs& a, Group& 
             const bool in = e + 32 * u < e1;
             v[u] = in ? __ldg(a.val64 + e + 32 * u) : 0.0;
             c[u] = in ? __ldg(a.col + e + 32 * u) - R0 : 0;
+            if (!idx_ok(c[u], nr, a.err_flags)) c[u] = 0;
           }
           acc0 += v[0] * s_vd[c[0]];
           acc1 += v[1] * s_vd[c[1]];

@@ -469,9 +469,13 @@ k_paths_mixed(const MixedArgs a) {
             cubic_weights(uu - (float)b0, w[0], w[1], w[2], w[3]);
             const float yw = wgt * Y;
             float* hp = hist + is.hist_off + b0 - 1;
+            // the 4 bins lie in the side's histogram, inside the CTA's
+            const bool in = idx_ok(b0 - 1, is.nbins - 3, a.err_flags) &&
+                            idx_ok(is.hist_off + b0 + 2, hist_len, a.err_flags);
 #pragma unroll
-            for (int r = 0; r < 4; r++) atomicAdd(hp + r, yw * w[r]);
-            if (a.want_var) {
+            for (int r = 0; r < 4; r++)
+              if (in) atomicAdd(hp + r, yw * w[r]);
+            if (a.want_var && in) {
               float* hq = hist2 + is.hist_off + b0 - 1;
               const float y2 = yw * yw;
 #pragma unroll
@@ -519,9 +523,13 @@ k_paths_mixed(const MixedArgs a) {
             cubic_weights(uu - (float)b0, w[0], w[1], w[2], w[3]);
             const float yw = wgt * Y;
             float* hp = hist + is.hist_off + b0 - 1;
+            // the 4 bins lie in the side's histogram, inside the CTA's
+            const bool in = idx_ok(b0 - 1, is.nbins - 3, a.err_flags) &&
+                            idx_ok(is.hist_off + b0 + 2, hist_len, a.err_flags);
 #pragma unroll
-            for (int r = 0; r < 4; r++) atomicAdd(hp + r, yw * w[r]);
-            if (a.want_var) {
+            for (int r = 0; r < 4; r++)
+              if (in) atomicAdd(hp + r, yw * w[r]);
+            if (a.want_var && in) {
               float* hq = hist2 + is.hist_off + b0 - 1;
               const float y2 = yw * yw;
 #pragma unroll
@@ -539,7 +547,8 @@ k_paths_mixed(const MixedArgs a) {
     // branching around the stores.
     auto push = [&](bool ex) -> unsigned {
       const unsigned mk = __ballot_sync(FULL, ex);
-      const int i = ex ? qcount + __popc(mk & lt) : XQCAP;
+      int i = ex ? qcount + __popc(mk & lt) : XQCAP;
+      if (!idx_ok(i, XQCAP + 1, a.err_flags)) i = XQCAP;
       q[0][i] = F.x;
       q[1][i] = F.y;
       q[2][i] = F.Y;
@@ -739,6 +748,7 @@ k_paths_mixed(const MixedArgs a) {
         acc2 += (double)part2;
       }
       const int64_t e = row0 + L.map_pos[m];
+      if (!idx_ok(e - row0, L.row_ptr[knot + 1] - row0, a.err_flags)) continue;
       atomicAdd(a.G + e, -acc * invN);
       if (a.want_var) atomicAdd(a.GG + e, acc2 * invN);
     }

@@ -310,6 +310,7 @@ __global__ void k_replay_row(const ReplayArgs a, const int64_t* knot_task_off, c
     const int n = L.sd_n[sd];
     for (int i = 0; i < n; i++, mo++, to++) {
       const int64_t e = r0 + L.map_pos[mo];
+      if (!idx_ok(e - r0, r1 - r0, a.err_flags)) continue;
       if (a.dup_sum) {
         a.G[e] += Gside[to] * norm;
         a.GG[e] += GGside[to] * norm;

@@ -544,6 +544,7 @@ cudaError_t solve_gmres_ir_cluster(const SolveCsr& A, const double* b, double* x
   ++w.launches;
   k_cl_single_rows<<<1, 1, 0, s>>>(ctl, n);
   ClusterGmresArgs a{};
+  a.err_flags = w.err;
   a.n_sys = 1;
   a.sys_row0 = ctl;
   a.K = n;

@@ -20,6 +20,24 @@ constexpr unsigned ERR_FLAG_EXIT_SIDE = 2u;
 constexpr unsigned ERR_FLAG_SINGULAR = 4u;
 constexpr unsigned ERR_FLAG_TIMEOUT = 8u;  // a bounded device wait ran out
 constexpr unsigned ERR_FLAG_SUB_NOCONV = 16u;  // a subdomain solve missed its tolerance
+constexpr unsigned ERR_FLAG_BOUNDS = 32u;      // an index check of the checked build failed
+
+// Index check of the checked build (compiled with -DPDDS_CHECKED,
+// pdds_gb300.build.build(checked=True)): i must lie in [0, n); a failed
+// check sets ERR_FLAG_BOUNDS and the caller skips the access.  The default
+// build compiles every check to true.
+__device__ __forceinline__ bool idx_ok(long long i, long long n, unsigned* flags) {
+#ifdef PDDS_CHECKED
+  if (i >= 0 && i < n) return true;
+  if (flags) atomicOr(flags, ERR_FLAG_BOUNDS);
+  return false;
+#else
+  (void)i;
+  (void)n;
+  (void)flags;
+  return true;
+#endif
+}
 
 // Diagnostic sums of one finished path (or Richardson pair) into a CTA's
 // shared sums: phi, phi^2, xi, xi^2, phi + xi, (phi + xi)^2, xi phi, tau, normals.

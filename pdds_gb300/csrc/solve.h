@@ -61,6 +61,7 @@ struct ClusterGmresArgs {
   double* out_relres;
   unsigned long long* out_t_end;  // optional: %globaltimer when the system finished
   unsigned spin_limit;   // grid barrier: polls before a wait gives up (0: 2^24, about 1 s)
+  unsigned* err_flags;   // optional: index checks of the checked build
 };
 
 // Cluster size for systems of at most max_rows rows (about 512 rows per CTA,
