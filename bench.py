@@ -314,7 +314,7 @@ def linear_fixed_point(local: int, iterations: int = 6, npaths: int = 20_000, h:
     return out
 
 
-def plain_config1(local: int, reps: int = 3):
+def plain_poisson_4x4(local: int, reps: int = 3):
     """The CPU-runnable configuration: Poisson on [-1,1]^2, 4 x 4 subdomains,
     11 knots per segment (237 knots), 1e4 paths per knot, h = 1e-3, the plain
     method (fixed step, no Richardson pair, the reference's overwrite of shared
@@ -578,7 +578,7 @@ def main():
     ap.add_argument("--no-semilinear", action="store_true")
     ap.add_argument("--no-linloop", action="store_true")
     ap.add_argument("--no-lut", action="store_true")
-    ap.add_argument("--no-config1", action="store_true")
+    ap.add_argument("--no-poisson-4x4", action="store_true")
     ap.add_argument("--no-robin", action="store_true")
     ap.add_argument("--lut-sampler", default="bspline", choices=["bspline", "catmull_rom", "bilinear"],
                     help="MIXED table sampler of the table-served workload")
@@ -727,8 +727,8 @@ def main():
         extra["many_instance_batch"] = many_instance_batch(local)
     if not args.no_circle and rank == 0:
         extra["circle_uneven_lengths"] = circle_uneven(local)
-    if not args.no_config1 and rank == 0:
-        extra["config1_plain"] = plain_config1(local)
+    if not args.no_poisson_4x4 and rank == 0:
+        extra["poisson_4x4_n11_plain"] = plain_poisson_4x4(local)
     if not args.no_lut and rank == 0:
         extra["varcoef_lut"] = varcoef_lut(local)
     if not args.no_robin and rank == 0:

@@ -1529,7 +1529,7 @@ pdds_status pdds_solve_interface(pdds_ctx* ctx, const pdds_solve_desc* desc, dou
   const int K = L.K;
   const int64_t nnz = L.row_ptr[K];
   const XferCount x0 = xfer();
-  // GMRES(20): on config 2 every restart length from 20 to 40 needs the same
+  // GMRES(20): on the 12x12 / 43-knot layout every restart length from 20 to 40 needs the same
   // 120 Arnoldi steps, and the shorter basis makes each step cheaper
   const int m = std::max(2, std::min(desc->restart > 0 ? desc->restart : 20, 40));
   CK(ctx->sv64.resize((size_t)6 * K));

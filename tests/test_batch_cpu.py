@@ -81,7 +81,7 @@ def test_batch_rejects_bad_input(lib):
         lib.pdds_destroy(ctx)
 
 
-def test_config5_instances_are_seeded_and_in_range():
+def test_many_instance_workload_is_seeded_and_in_range():
     a = batch_instances(256, seed=5)
     b = batch_instances(256, seed=5)
     assert [i.params for i in a] == [i.params for i in b]

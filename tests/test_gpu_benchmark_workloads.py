@@ -115,7 +115,7 @@ def _assert_standard_normal(zf, zb):
     assert np.abs(zf).max() < 4.5 and np.abs(zb).max() < 4.5, (zf, zb)
 
 
-def test_config1_replay_bit_exact_in_full():
+def test_poisson_4x4_n11_replay_bit_exact_in_full():
     w = WORKLOADS["poisson_4x4_n11"]
     nsub, nnode, N, h, seed = w["nsub"], w["nnode"], w["npaths"], w["h"], 1234
     assert (nsub, nnode, N, h) == (4, 11, 10_000, 1e-3)
@@ -141,7 +141,7 @@ def test_config1_replay_bit_exact_in_full():
     assert est.info["exits_stencil"] == ref["stats"][3]
 
 
-def test_config2_sample_mixed_and_fp64_agree_with_oracle():
+def test_poisson_12x12_n43_sample_mixed_and_fp64_agree_with_oracle():
     w = WORKLOADS["poisson_12x12_n43"]
     nsub, nnode, N, h = w["nsub"], w["nnode"], w["npaths"], w["h"]
     assert (nsub, nnode, N, h) == (12, 43, 20_000, 5e-4)
@@ -162,7 +162,7 @@ def test_config2_sample_mixed_and_fp64_agree_with_oracle():
         _assert_standard_normal(zf, zb)
 
 
-def test_config3_sample_mixed_and_fp64_agree_with_oracle():
+def test_varcoef_lut_8x8_n31_sample_mixed_and_fp64_agree_with_oracle():
     w = WORKLOADS["varcoef_lut_8x8_n31"]
     nsub, nnode, N, h = w["nsub"], w["nnode"], w["npaths"], w["h"]
     assert (nsub, nnode, N, h, w["lut_n"]) == (8, 31, 50_000, 5e-4, 1024)
@@ -186,7 +186,7 @@ def test_config3_sample_mixed_and_fp64_agree_with_oracle():
         _assert_standard_normal(zf, zb)
 
 
-def test_config5_instances_agree_with_oracle():
+def test_many_instance_helmholtz_agree_with_oracle():
     """Four instances of the many-instance workload (Helmholtz, each on its
     own g x g grid with the step h (4/g)^2), the coarsest and finest grids
     among them: MIXED rows and B of each instance run alone, and B of the

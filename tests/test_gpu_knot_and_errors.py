@@ -56,13 +56,13 @@ def _oracle_knot(L, fac, pos):
 
 
 @pytest.fixture(scope="module")
-def cfg1():
+def poisson_4x4():
     fac = fac_rule(2.0, NSUB, NNODE)
     return O.Layout(SW, NE, NSUB, NNODE), fac
 
 
-def test_single_knot_replay_bit_exact(cfg1):
-    L, fac = cfg1
+def test_single_knot_replay_bit_exact(poisson_4x4):
+    L, fac = poisson_4x4
     N, h, seed = 300, 1e-3, 1234
     prob = O.make_problem(O.POISSON_SINCOS)
     prm = O.make_params(N, h, seed=seed, fac=fac, portable=True, sublinear=True)
@@ -79,7 +79,7 @@ def test_single_knot_replay_bit_exact(cfg1):
             assert B == ref["B"] and BB == ref["BB"], kn
 
 
-def test_single_knot_replay_bit_exact_through_the_cpp_shim(cfg1, tmp_path):
+def test_single_knot_replay_bit_exact_through_the_cpp_shim(poisson_4x4, tmp_path):
     from pdds_gb300 import build as Bld
     import shutil
     lib = Bld.build()
@@ -93,7 +93,7 @@ def test_single_knot_replay_bit_exact_through_the_cpp_shim(cfg1, tmp_path):
                           "-Wl,-rpath," + os.path.dirname(lib), "-L" + cuda_lib, "-Wl,-rpath," + cuda_lib,
                           "-lcudart"], capture_output=True, text=True)
     assert res.returncode == 0, res.stderr
-    L, fac = cfg1
+    L, fac = poisson_4x4
     N, h, seed = 256, 1e-3, 77
     prm = O.make_params(N, h, seed=seed, fac=fac, portable=True, sublinear=True)
     for pos in (5, 131):

@@ -1,4 +1,4 @@
-"""LUT-served coefficients (config 3's coefficient source).
+"""LUT-served coefficients (the table-served variable-coefficient workload's coefficient source).
 
 The variable-coefficient problem is served from FP32 tables.  The FP64 and
 replay forms sample them with bicubic Catmull-Rom interpolation: replay is

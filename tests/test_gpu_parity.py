@@ -48,7 +48,7 @@ def _replay(nsub, nnode, N, bvp, prob, dup_sum=False, seed=1234, h=1e-3):
 
 
 def test_replay_bit_exact_poisson_4x4_n11():
-    """Config 1 layout (4x4 subdomains, 11 knots per segment, K=237)."""
+    """The 4x4-subdomain layout with 11 knots per segment (K = 237)."""
     est, ref = _replay(4, 11, 400, P.BVP.poisson_sincos(), O.make_problem(O.POISSON_SINCOS))
     assert ref["status"] == 0
     assert len(ref["knots"]) == 237
@@ -98,7 +98,7 @@ def test_device_factorisation_matches_oracle_inverse():
 
 
 @pytest.fixture(scope="module")
-def cfg1_runs():
+def poisson_4x4_runs():
     nsub, nnode, N, h = 4, 11, 10_000, 1e-3
     fac = fac_rule(2.0, nsub, nnode)
     bvp = P.BVP.poisson_sincos()
@@ -109,8 +109,8 @@ def cfg1_runs():
     return dict(mixed=mixed, fp64=fp64, N=N, h=h, fac=fac, x=x, y=y)
 
 
-def test_mixed_matches_fp64_on_the_same_stream(cfg1_runs):
-    m, f, N = cfg1_runs["mixed"], cfg1_runs["fp64"], cfg1_runs["N"]
+def test_mixed_matches_fp64_on_the_same_stream(poisson_4x4_runs):
+    m, f, N = poisson_4x4_runs["mixed"], poisson_4x4_runs["fp64"], poisson_4x4_runs["N"]
     se_g = np.sqrt(np.maximum(m.var, 1e-12) / N)
     dg = np.abs(m.val - f.val)
     assert np.max(dg / se_g) < 0.5, np.max(dg / se_g)
@@ -119,8 +119,8 @@ def test_mixed_matches_fp64_on_the_same_stream(cfg1_runs):
     assert m.info["path_steps"] > 0 and abs(m.info["path_steps"] - f.info["path_steps"]) < 1e-3 * f.info["path_steps"]
 
 
-def test_mixed_statistical_agreement_with_oracle(cfg1_runs):
-    m, N, h, fac = cfg1_runs["mixed"], cfg1_runs["N"], cfg1_runs["h"], cfg1_runs["fac"]
+def test_mixed_statistical_agreement_with_oracle(poisson_4x4_runs):
+    m, N, h, fac = poisson_4x4_runs["mixed"], poisson_4x4_runs["N"], poisson_4x4_runs["h"], poisson_4x4_runs["fac"]
     L = O.Layout(SW, NE, 4, 11)
     sel = list(range(0, 237, 9))
     ref = L.run(O.make_problem(O.POISSON_SINCOS), O.make_params(N, h, seed=777, fac=fac, sublinear=False),
@@ -143,9 +143,9 @@ def test_mixed_statistical_agreement_with_oracle(cfg1_runs):
     assert np.abs(zb).max() < 4.5
 
 
-def test_interface_solution_against_analytic(cfg1_runs):
-    """Check (c) on config 1: (I+G)u = B solved on the device, u vs the exact u."""
-    nsub, nnode, N, h, fac = 4, 11, cfg1_runs["N"], cfg1_runs["h"], cfg1_runs["fac"]
+def test_interface_solution_against_analytic(poisson_4x4_runs):
+    """Check (c) on the 4x4 layout: (I+G)u = B solved on the device, u vs the exact u."""
+    nsub, nnode, N, h, fac = 4, 11, poisson_4x4_runs["N"], poisson_4x4_runs["h"], poisson_4x4_runs["fac"]
     bvp = P.BVP.poisson_sincos()
     with P.PDDSparseGM(SW, NE, nsub, nnode, fac) as pd:
         res = {}
@@ -158,8 +158,8 @@ def test_interface_solution_against_analytic(cfg1_runs):
     assert res[False] < 2e-2, res
 
 
-def test_solvers_agree_with_dense_solution(cfg1_runs):
-    nsub, nnode, fac = 4, 11, cfg1_runs["fac"]
+def test_solvers_agree_with_dense_solution(poisson_4x4_runs):
+    nsub, nnode, fac = 4, 11, poisson_4x4_runs["fac"]
     with P.PDDSparseGM(SW, NE, nsub, nnode, fac) as pd:
         est = pd.estimate(P.BVP.poisson_sincos(), 2000, 1e-3, mode=P.MODE_MIXED, seed=11)
         u1, i1 = pd.solve_interface(P.SOLVE_BICGSTAB_FP64, tol=1e-12)
