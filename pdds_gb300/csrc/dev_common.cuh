@@ -305,14 +305,19 @@ __device__ __forceinline__ void coef_f32(const ProblemDev& P, float x, float y, 
     k.s00 = v[0]; k.s01 = 0.f; k.s10 = 0.f; k.s11 = v[1];
     k.b0 = v[2]; k.b1 = v[3]; k.c = v[4]; k.f = v[5]; k.g0 = v[6]; k.g1 = v[7];
   } else if (KIND == PK_POISSON_SINCOS) {
+    // the x and y halves in paired FP32 instructions (same roundings)
+    const float2 arg = __fmul2_rn(make_float2(PI, PI), make_float2(x, y));
     float sx, cx, sy, cy;
-    __sincosf(PI * x, &sx, &cx);
-    __sincosf(PI * y, &sy, &cy);
+    __sincosf(arg.x, &sx, &cx);
+    __sincosf(arg.y, &sy, &cy);
     k.s00 = 1.41421356f; k.s01 = 0.f; k.s10 = 0.f; k.s11 = 1.41421356f;
     k.b0 = 0.f; k.b1 = 0.f; k.c = 0.f;
     k.f = 19.7392088f * (sx * cy);
-    k.g0 = PI * (cx * cy) + y;
-    k.g1 = x - PI * (sx * sy);
+    // g = (pi cx cy + y, x - pi sx sy)
+    const float2 g = __ffma2_rn(make_float2(PI, -PI), __fmul2_rn(make_float2(cx, sx), make_float2(cy, sy)),
+                                make_float2(y, x));
+    k.g0 = g.x;
+    k.g1 = g.y;
   } else if (KIND == PK_HELMHOLTZ) {
     const float a = (float)P.p[0], b = (float)P.p[1], c = (float)P.p[2];
     float sa, ca, sb, cb;

@@ -76,14 +76,14 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
 // z1 = rho sin(2 pi u1) with rho = sqrt(-2 ln u0), u = (word + 1/2) 2^-32,
 // evaluated as -rho cos/sin(a) at a = 2 pi u1 - pi in [-pi, pi], which the
 // fast intrinsics take directly (a is formed from the word in one FMA).
-__device__ __forceinline__ void normals_f32(uint32_t ua, uint32_t ub, float& z0, float& z1) {
+__device__ __forceinline__ float2 normals_f32(uint32_t ua, uint32_t ub) {
   const float u0 = fmaf((float)ua, 2.3283064e-10f, 1.1641532e-10f);
   const float rho = sqrt_approx(-1.38629436f * lg2_approx(u0));  // -2 ln u0 = -2 ln2 log2 u0
   const float ang = fmaf((float)ub, 1.46291808e-9f, -3.14159265f);
   float sn, cs;
   __sincosf(ang, &sn, &cs);
-  z0 = -rho * cs;
-  z1 = -rho * sn;
+  // (z0, z1) = -rho (cos, sin) in one paired multiply (the same two roundings)
+  return __fmul2_rn(make_float2(-rho, -rho), make_float2(cs, sn));
 }
 
 // path_block (counter = (step pair, path, knot, instance)) with the key
@@ -318,7 +318,10 @@ k_paths_mixed(const MixedArgs a) {
     // maximum of the Brownian bridge); the local time dL = max(0, M + d),
     // d the signed distance to the side (negative inside), pushes the path
     // back along -n and enters dZ = psi Y dL, dY = varphi Y dL.
-    auto advance = [&](Lvl<KIND>& s, float e0, float e1, float hh, float thr, float ex) -> bool {
+    // The (x, y) arithmetic of a step runs as paired FP32 instructions
+    // (FADD2 / FMUL2 / FFMA2: two lanes' worth of work per issue slot, the
+    // same roundings as the scalar pair).
+    auto advance = [&](Lvl<KIND>& s, float2 e, float hh, float thr, float ex) -> bool {
       Coef<float> k;
       if constexpr (is_lut_kind(KIND)) {
         k.s00 = s.cf[0]; k.s11 = s.cf[1];
@@ -327,8 +330,9 @@ k_paths_mixed(const MixedArgs a) {
       } else {
         coef_f32<KIND>(P, s.x, s.y, k);
       }
-      float d0 = e0, d1 = e1;
-      if constexpr (!KindTraits<KIND>::iso) { d0 = k.s00 * e0; d1 = k.s11 * e1; }
+      float2 d = e;
+      if constexpr (!KindTraits<KIND>::iso) d = __fmul2_rn(make_float2(k.s00, k.s11), e);
+      const float d0 = d.x, d1 = d.y;
       s.xi -= s.Y * (k.g0 * d0 + k.g1 * d1);
       s.Z += k.f * s.Y * hh;
       if constexpr (KindTraits<KIND>::react) s.Y += k.c * s.Y * hh;
@@ -357,11 +361,14 @@ k_paths_mixed(const MixedArgs a) {
         absorb_out(s.x, s.y, o);
         return !(fmaxf(fmaxf(o[0], o[1]), fmaxf(o[2], o[3])) < thr) || s.steps >= (unsigned)a.max_steps;
       } else if constexpr (KindTraits<KIND>::iso) {
-        s.x += d0;
-        s.y += d1;
+        const float2 np = __fadd2_rn(make_float2(s.x, s.y), d);
+        s.x = np.x;
+        s.y = np.y;
       } else {
-        s.x += k.b0 * hh + d0;
-        s.y += k.b1 * hh + d1;
+        const float2 np =
+            __fadd2_rn(make_float2(s.x, s.y), __ffma2_rn(make_float2(k.b0, k.b1), make_float2(hh, hh), d));
+        s.x = np.x;
+        s.y = np.y;
       }
       ++s.steps;
       if constexpr (GEOM == 1) {  // iso kinds only: |N^T sigma| = sqrt2 for every normal
@@ -616,9 +623,7 @@ k_paths_mixed(const MixedArgs a) {
       if (active) {
         const unsigned mi = m++;
         const u32x4 blk = path_block_rk(a.rk, rng_inst, rng_knot, path, mi);
-        float za0, za1, zb0, zb1;
-        normals_f32(blk.v[0], blk.v[1], za0, za1);
-        normals_f32(blk.v[2], blk.v[3], zb0, zb1);
+        const float2 za = normals_f32(blk.v[0], blk.v[1]), zb = normals_f32(blk.v[2], blk.v[3]);
         // Exp(1) samples of the reflected steps: a second Philox block with
         // the knot word's top bit set (fine A, fine B, coarse)
         float x0e = 0.f, x1e = 0.f, x2e = 0.f;
@@ -633,16 +638,18 @@ k_paths_mixed(const MixedArgs a) {
           // on the same Brownian increments (dW_coarse = dW_fine1 + dW_fine2);
           // 2 E[fine] - E[coarse] cancels the O(h) bias.  A level that has
           // exited keeps its exit state until the pair is pushed.
-          const float ea0 = scf * za0, ea1 = scf * za1, eb0 = scf * zb0, eb1 = scf * zb1;
+          const float2 sf = make_float2(scf, scf);
+          const float2 ea = __fmul2_rn(sf, za), eb = __fmul2_rn(sf, zb);
           if (f_alive) {
-            bool fx = advance(F, ea0, ea1, hf, thrf, x0e);
-            if (!fx) fx = advance(F, eb0, eb1, hf, thrf, x1e);
+            bool fx = advance(F, ea, hf, thrf, x0e);
+            if (!fx) fx = advance(F, eb, hf, thrf, x1e);
             f_alive = !fx;
           }
-          if (c_alive) c_alive = !advance(Cs, ea0 + eb0, ea1 + eb1, h, thrc, x2e);
+          if (c_alive) c_alive = !advance(Cs, __fadd2_rn(ea, eb), h, thrc, x2e);
         } else {
-          bool fx = advance(F, scc * za0, scc * za1, h, thrc, x0e);
-          if (!fx) fx = advance(F, scc * zb0, scc * zb1, h, thrc, x1e);
+          const float2 sc = make_float2(scc, scc);
+          bool fx = advance(F, __fmul2_rn(sc, za), h, thrc, x0e);
+          if (!fx) fx = advance(F, __fmul2_rn(sc, zb), h, thrc, x1e);
           f_alive = !fx;
         }
       }
