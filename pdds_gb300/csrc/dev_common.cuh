@@ -320,14 +320,18 @@ __device__ __forceinline__ void coef_f32(const ProblemDev& P, float x, float y, 
     k.g1 = g.y;
   } else if (KIND == PK_HELMHOLTZ) {
     const float a = (float)P.p[0], b = (float)P.p[1], c = (float)P.p[2];
+    // the x and y halves in paired FP32 instructions (same roundings)
+    const float2 arg = __fmul2_rn(make_float2(a, b), make_float2(x, y));
     float sa, ca, sb, cb;
-    __sincosf(a * x, &sa, &ca);
-    __sincosf(b * y, &sb, &cb);
+    __sincosf(arg.x, &sa, &ca);
+    __sincosf(arg.y, &sb, &cb);
     k.s00 = 1.41421356f; k.s01 = 0.f; k.s10 = 0.f; k.s11 = 1.41421356f;
     k.b0 = 0.f; k.b1 = 0.f; k.c = c;
     k.f = ((a * a + b * b) - c) * (sa * cb);
-    k.g0 = a * (ca * cb);
-    k.g1 = -(b * (sa * sb));
+    // g = (a ca cb, -b sa sb)
+    const float2 g = __fmul2_rn(make_float2(a, -b), __fmul2_rn(make_float2(ca, sa), make_float2(cb, sb)));
+    k.g0 = g.x;
+    k.g1 = g.y;
   } else if (KIND == PK_VARCOEF) {
     const float s1 = 1.f + 0.5f * (x * x), s2 = 1.f + 0.5f * (y * y);
     float sn, cs;
