@@ -79,6 +79,7 @@ struct Iface {
 // dropped) and each knot's last written position.
 struct SideWork {
   bool present = false;
+  uint64_t hash = 0;  // FNV-1a of the side kind and knot list
   std::vector<int> idx;
   std::vector<double> px, py;
 };
@@ -289,48 +290,73 @@ std::string build_rect_layout(HostLayout& L, const double sw[2], const double ne
     }
   }
   if ((int)L.order.size() != L.K) return "internal: hand-out list does not cover all knots";
-  // interfaces of every knot, in interface-vector order (Get_Interfaces)
-  std::vector<std::vector<int>> knot_ifs(L.K);
+  // interfaces of every knot, in interface-vector order (Get_Interfaces): one
+  // for a knot inside an interface, four for a cross point; kif_n counts
+  // them, the first four are kept (more is reported as an error below)
+  std::vector<int> kif((size_t)L.K * 4, -1), kif_n(L.K, 0);
   for (int id = 0; id < nif; id++)
-    for (int v : ifs[id].index)
-      if (knot_ifs[v].empty() || knot_ifs[v].back() != id) knot_ifs[v].push_back(id);
+    for (int v : ifs[id].index) {
+      int& n = kif_n[v];
+      if (n > 0 && n <= 4 && kif[(size_t)v * 4 + n - 1] == id) continue;
+      if (n < 4) kif[(size_t)v * 4 + n] = id;
+      n++;
+    }
 
   const double gparams[4] = {sw[0], sw[1], ne[0], ne[1]};
   // 1. stencil ids in knot order: knots with the same interfaces share one
-  std::map<std::vector<int>, int> stencil_key;
+  //    (one-interface knots by interface id, the others by their id list)
+  std::vector<int> sid_of_if(nif, -1);
+  std::map<std::vector<int>, int> multi_key;
   std::vector<int> rep;  // first knot of each stencil
   L.knot_stencil.assign(L.K, -1);
   L.knot_boundary.assign(L.K, 0);
   for (int v = 0; v < L.K; v++) {
-    auto it = stencil_key.find(knot_ifs[v]);
-    if (it != stencil_key.end()) {
-      L.knot_stencil[v] = it->second;
-      continue;
+    const int n = kif_n[v];
+    int* slot;
+    if (n == 1) {
+      slot = &sid_of_if[kif[(size_t)v * 4]];
+    } else {
+      std::vector<int> key(kif.begin() + (size_t)v * 4, kif.begin() + (size_t)v * 4 + std::min(n, 4));
+      if (n > 4) key.push_back(-n);
+      slot = &multi_key.emplace(std::move(key), -1).first->second;
     }
-    const int sid = (int)rep.size();
-    stencil_key.emplace(knot_ifs[v], sid);
-    rep.push_back(v);
-    L.knot_stencil[v] = sid;
+    if (*slot < 0) {
+      *slot = (int)rep.size();
+      rep.push_back(v);
+    }
+    L.knot_stencil[v] = *slot;
   }
   // 2. every stencil on its own (host threads): rect, sides' knot lists with
   //    their last written positions, G row, row positions and owner flags
   const int nst = (int)rep.size();
   const double STEN_ELONG = 0.5;
   std::vector<StencilWork> work(nst);
-  auto build_one = [&](int sid, std::vector<Lab>& tmp, std::vector<int>& lastq, std::vector<int>& col_pos,
-                       std::vector<int64_t>& last_writer) {
+  // per-thread scratch of build_one: knot-indexed arrays and side lists
+  struct Scratch {
+    std::vector<Lab> tmp, lab[4];
+    std::vector<int> lastq, col_pos, sidx;
+    std::vector<int64_t> last_writer;
+    std::vector<double> spx, spy;
+  };
+  auto build_one = [&](int sid, Scratch& sc) {
     StencilWork& W = work[sid];
-    const std::vector<int>& ki = knot_ifs[rep[sid]];
+    const int* ki = &kif[(size_t)rep[sid] * 4];
+    const int nki = kif_n[rep[sid]];
+    std::vector<Lab>& tmp = sc.tmp;
+    std::vector<int>& lastq = sc.lastq;
+    std::vector<int>& col_pos = sc.col_pos;
+    std::vector<int64_t>& last_writer = sc.last_writer;
     // Labels_Stencil
-    std::vector<Lab> lab[4];
+    std::vector<Lab>* lab = sc.lab;
+    for (int d = 0; d < 4; d++) lab[d].clear();
     auto push_if = [&](int d, Lab l) { if (lab_id(iN, l) >= 0) lab[d].push_back(l); };
-    if (ki.size() == 1) {
+    if (nki == 1) {
       const Lab l = ifs[ki[0]].label;
       lab_N(l, tmp); for (auto& q : tmp) push_if(DIR_N, q);
       lab_S(l, tmp); for (auto& q : tmp) push_if(DIR_S, q);
       lab_E(l, tmp); for (auto& q : tmp) push_if(DIR_E, q);
       lab_W(l, tmp); for (auto& q : tmp) push_if(DIR_W, q);
-    } else if (ki.size() == 4) {
+    } else if (nki == 4) {
       int max_h = -1 << 30, max_v = -1 << 30;
       for (int q = 0; q < 4; q++) {
         max_h = std::max(max_h, ifs[ki[q]].label.a);
@@ -351,7 +377,7 @@ std::string build_rect_layout(HostLayout& L, const double sw[2], const double ne
       lab_W(is, tmp); push_if(DIR_W, tmp[0]);
       lab_W(in, tmp); push_if(DIR_W, tmp[0]);
     } else {
-      W.err = "internal: knot on " + std::to_string(ki.size()) + " interfaces";
+      W.err = "internal: knot on " + std::to_string(nki) + " interfaces";
       return;
     }
     auto IF = [&](Lab l) -> const Iface& { return ifs[lab_id(iN, l)]; };
@@ -362,8 +388,9 @@ std::string build_rect_layout(HostLayout& L, const double sw[2], const double ne
     if (!lab[DIR_W].empty()) st.rect[0] = IF(lab[DIR_W][0]).px[0];
     if (!lab[DIR_N].empty()) st.rect[3] = IF(lab[DIR_N].back()).py.back();
     if (!lab[DIR_E].empty()) st.rect[2] = IF(lab[DIR_E].back()).px.back();
-    std::vector<int> sidx;
-    std::vector<double> spx, spy;
+    std::vector<int>& sidx = sc.sidx;
+    std::vector<double>& spx = sc.spx;
+    std::vector<double>& spy = sc.spy;
     for (int d = 0; d < 4; d++) {
       int kind = -3;
       st.side[d] = -1;
@@ -420,6 +447,9 @@ std::string build_rect_layout(HostLayout& L, const double sw[2], const double ne
         S.py.push_back(spy[lastq[v2]]);
       }
       for (int v2 : sidx) lastq[v2] = -1;
+      uint64_t h = 1469598103934665603ull ^ (uint64_t)kind;
+      for (int v2 : S.idx) h = (h ^ (uint64_t)(uint32_t)v2) * 1099511628211ull;
+      S.hash = h;
     }
     // global-boundary flags of the rect sides: midpoint within 1e-8 of the
     // domain boundary (Reduce_Analytic's test, EMFKACSolver.hpp:559)
@@ -440,12 +470,17 @@ std::string build_rect_layout(HostLayout& L, const double sw[2], const double ne
     // row position of every (side, knot) entry, sides in N, S, E, W order;
     // the last side that wrote a knot owns its entry
     for (int p = 0; p < (int)cols.size(); p++) col_pos[cols[p]] = p;
+    size_t nmap = 0;
+    for (int d = 0; d < 4; d++)
+      if (W.side[d].present) nmap += W.side[d].idx.size();
+    W.map_pos.resize(nmap);
+    W.map_owner.assign(nmap, 0);
+    size_t m = 0;
     for (int d = 0; d < 4; d++) {
       if (!W.side[d].present) continue;
       for (int v2 : W.side[d].idx) {
-        last_writer[v2] = (int64_t)W.map_pos.size();
-        W.map_pos.push_back(col_pos[v2]);
-        W.map_owner.push_back(0);
+        last_writer[v2] = (int64_t)m;
+        W.map_pos[m++] = col_pos[v2];
       }
     }
     for (int v2 : cols) {
@@ -460,10 +495,11 @@ std::string build_rect_layout(HostLayout& L, const double sw[2], const double ne
     std::vector<std::string> terr(nth);
     auto worker = [&](int t) {
       try {
-        std::vector<Lab> tmp;
-        std::vector<int> lastq(L.K, -1), col_pos(L.K, 0);
-        std::vector<int64_t> last_writer(L.K, -1);
-        for (int sid = t; sid < nst; sid += nth) build_one(sid, tmp, lastq, col_pos, last_writer);
+        Scratch sc;
+        sc.lastq.assign(L.K, -1);
+        sc.col_pos.assign(L.K, 0);
+        sc.last_writer.assign(L.K, -1);
+        for (int sid = t; sid < nst; sid += nth) build_one(sid, sc);
       } catch (const std::exception& e) {
         terr[t] = std::string("layout worker: ") + e.what();
       }
@@ -476,50 +512,75 @@ std::string build_rect_layout(HostLayout& L, const double sw[2], const double ne
       if (!e.empty()) return e;
   }
   // 3. in stencil order: side records shared by equal (kind, knot list), the
-  //    first stencil that meets a side giving its knot positions
-  struct SideKeyHash {
-    size_t operator()(const std::pair<int, std::vector<int>>& k) const {
-      uint64_t h = 1469598103934665603ull ^ (uint64_t)k.first;
-      for (int v : k.second) h = (h ^ (uint64_t)(uint32_t)v) * 1099511628211ull;
-      return (size_t)h;
-    }
-  };
-  std::unordered_map<std::pair<int, std::vector<int>>, int, SideKeyHash> side_key;
+  //    first stencil that meets a side giving its knot positions; records
+  //    with one hash are chained (side_next) and compared in full
+  size_t nside_knots = 0, nmap = 0;
+  for (int sid = 0; sid < nst; sid++) {
+    if (!work[sid].err.empty()) return work[sid].err;
+    for (int d = 0; d < 4; d++)
+      if (work[sid].side[d].present) nside_knots += work[sid].side[d].idx.size();
+    nmap += work[sid].map_pos.size();
+  }
+  std::unordered_map<uint64_t, int> side_by_hash;
+  std::vector<int> side_next;
+  side_by_hash.reserve(4 * (size_t)nst);
+  L.side_knot.reserve(nside_knots);
+  L.side_px.reserve(nside_knots);
+  L.side_py.reserve(nside_knots);
+  L.map_pos.resize(nmap);
+  L.map_owner.resize(nmap);
   L.stencils.reserve(nst);
+  int64_t moff = 0;
   for (int sid = 0; sid < nst; sid++) {
     StencilWork& W = work[sid];
-    if (!W.err.empty()) return W.err;
     StencilRec& st = W.st;
     for (int d = 0; d < 4; d++) {
       SideWork& S = W.side[d];
       if (!S.present) continue;
       const int kd = st.kind[d];
-      auto key = std::make_pair(kd, std::move(S.idx));
-      auto sit = side_key.find(key);
-      if (sit != side_key.end()) {
-        st.side[d] = sit->second;
+      const int n = (int)S.idx.size();
+      auto hit = side_by_hash.find(S.hash);
+      int found = -1;
+      if (hit != side_by_hash.end())
+        for (int c = hit->second; c >= 0; c = side_next[c]) {
+          const SideRec& r = L.sides[c];
+          if (r.kind == kd && r.n == n && std::equal(S.idx.begin(), S.idx.end(), L.side_knot.begin() + r.knot_off)) {
+            found = c;
+            break;
+          }
+        }
+      if (found >= 0) {
+        st.side[d] = found;
         continue;
       }
       SideRec sr;
-      sr.n = (int)key.second.size();
+      sr.n = n;
       sr.orient = (d == DIR_N || d == DIR_S) ? 0 : 1;
       sr.kind = kd;
       sr.c = fac[kd];
       sr.shape = -1;
       sr.knot_off = (int64_t)L.side_knot.size();
-      L.side_knot.insert(L.side_knot.end(), key.second.begin(), key.second.end());
+      L.side_knot.insert(L.side_knot.end(), S.idx.begin(), S.idx.end());
       L.side_px.insert(L.side_px.end(), S.px.begin(), S.px.end());
       L.side_py.insert(L.side_py.end(), S.py.begin(), S.py.end());
       sr.origin = (sr.orient == 0) ? L.side_px[sr.knot_off] : L.side_py[sr.knot_off];
       sr.fixed = (sr.orient == 0) ? L.side_py[sr.knot_off] : L.side_px[sr.knot_off];
       L.max_side = std::max(L.max_side, sr.n);
-      st.side[d] = (int)L.sides.size();
-      side_key.emplace(std::move(key), (int)L.sides.size());
+      const int id = (int)L.sides.size();
+      st.side[d] = id;
+      if (hit != side_by_hash.end()) {
+        side_next.push_back(hit->second);
+        hit->second = id;
+      } else {
+        side_next.push_back(-1);
+        side_by_hash.emplace(S.hash, id);
+      }
       L.sides.push_back(sr);
     }
-    st.map_off = (int64_t)L.map_pos.size();
-    L.map_pos.insert(L.map_pos.end(), W.map_pos.begin(), W.map_pos.end());
-    L.map_owner.insert(L.map_owner.end(), W.map_owner.begin(), W.map_owner.end());
+    st.map_off = moff;
+    std::copy(W.map_pos.begin(), W.map_pos.end(), L.map_pos.begin() + moff);
+    std::copy(W.map_owner.begin(), W.map_owner.end(), L.map_owner.begin() + moff);
+    moff += (int64_t)W.map_pos.size();
     L.stencils.push_back(std::move(st));
   }
   finish_layout(L, gparams, bps);
