@@ -12,8 +12,10 @@ plain FP64 GPU form are measured beside it.
 
   value  path-steps/s of the device-timed step (inputs resident in HBM),
          CUDA events on the library's stream, L2 flushed between steps
-  e2e    the same metric through the public API call a user makes: layout
-         upload from host, estimation, solve, and G/B/u copied back to host
+  e2e    the same metric through the public API call a user makes: a new
+         context with the layout built on the host and uploaded, estimation,
+         solve, and G/B/u copied back to host, every step (after the same
+         warm-up steps as the device-timed step)
   roofline  FP32 issue-slot roof of the path kernel (the path is issue-bound:
          it reads a few MB of stencil tables and no large arrays)
   cpu_baseline  the CPU restatement of the reference (OpenMP paths, serial
@@ -696,6 +698,12 @@ def main():
         # every step: a new context (layout built on the host and uploaded),
         # the estimate, the solve, G, B and u read back to host memory; the
         # bytes are the library's own counts of what it copied
+        for s in range(args.warmup):  # untimed, like the device-timed steps
+            q = P.PDDSparseGM(workload["sw"], workload["ne"], workload["nsub"], workload["nnode"], fac,
+                              device=local)
+            q.estimate(bvp, N, h, mode=P.MODE_MIXED, seed=1234, instance=40 + s, **OPTS)
+            q.solve_interface()
+            q.close()
         h2d = d2h = 0
         ph = {"layout": 0.0, "estimate": 0.0, "solve": 0.0, "close": 0.0}
         t0 = time.perf_counter()

@@ -49,7 +49,14 @@ typedef struct pdds_ctx pdds_ctx;
 
 /* ---------------------------------------------------------------- context */
 pdds_status pdds_create(pdds_ctx** ctx, int device, uint32_t flags);
+/* Frees the context.  Its device buffers are kept by the library (up to
+ * 8 GB per device, blocks up to 2 GB) for the next context on the same
+ * device, which then allocates no device memory for buffers of the same
+ * sizes; pdds_release_cached_blocks returns them to the device. */
 pdds_status pdds_destroy(pdds_ctx* ctx);
+/* Frees the device buffers kept from destroyed contexts (device -1: on every
+ * device).  The library also does so by itself when an allocation fails. */
+pdds_status pdds_release_cached_blocks(int32_t device);
 const char* pdds_last_error(const pdds_ctx* ctx);
 const char* pdds_version(void);
 
@@ -288,7 +295,9 @@ typedef struct {
 
 /* Runs the estimation for all knots and keeps G and B on the device.  Any of
  * the host output pointers may be NULL: val[nnz], var[nnz] (needs want_var),
- * B[K], BB[K] (mean of the squared score, as Reduce_Analytic's BB). */
+ * B[K], BB[K] (mean of the squared score, as Reduce_Analytic's BB).  val and
+ * var may be fresh, never-touched host memory: the call touches their pages
+ * while the device runs the paths, before the copies fill them. */
 pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double* val, double* var,
                           double* B, double* BB, pdds_estimate_info* info);
 /* Paths per knot of the last pdds_estimate (npaths[K]; 0 for boundary knots

@@ -6,10 +6,11 @@ reference's BVP / PDDSparseGM call surface.
 """
 from ._capi import (MODE_FP64, MODE_MIXED, MODE_REPLAY_FP64, SOLVE_BICGSTAB_FP64, SOLVE_GMRES_FP32_IR,
                     PDDSError)
-from .api import BVP, Batch, EMFKACSolver, Estimate, Instance, PDDSparseGM, Stencil, read_configuration
+from .api import (BVP, Batch, EMFKACSolver, Estimate, Instance, PDDSparseGM, Stencil, read_configuration,
+                  release_cached_blocks)
 from .checkpoint import estimate_resumable
 from .output_files import TimeFile, write_knot_metadata, write_outputs
 
 __all__ = ["BVP", "Batch", "EMFKACSolver", "Estimate", "Stencil", "Instance", "PDDSparseGM", "PDDSError",
-           "read_configuration", "estimate_resumable", "TimeFile", "write_knot_metadata", "write_outputs",
+           "read_configuration", "release_cached_blocks", "estimate_resumable", "TimeFile", "write_knot_metadata", "write_outputs",
            "MODE_FP64", "MODE_MIXED", "MODE_REPLAY_FP64", "SOLVE_BICGSTAB_FP64", "SOLVE_GMRES_FP32_IR"]

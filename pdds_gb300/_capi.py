@@ -23,7 +23,8 @@ MODE_REPLAY_FP64, MODE_FP64, MODE_MIXED = 0, 1, 2
 SOLVE_BICGSTAB_FP64, SOLVE_GMRES_FP32_IR = 0, 1
 
 EXPORTS = [
-    "pdds_create", "pdds_destroy", "pdds_last_error", "pdds_version", "pdds_problem_set", "pdds_problem_set_lut",
+    "pdds_create", "pdds_destroy", "pdds_release_cached_blocks", "pdds_last_error", "pdds_version",
+    "pdds_problem_set", "pdds_problem_set_lut",
     "pdds_layout_build", "pdds_layout_build_circle", "pdds_layout_knots", "pdds_layout_csr", "pdds_layout_stencil",
     "pdds_estimate", "pdds_estimate_knot_paths", "pdds_estimate_knot_steps", "pdds_autotune", "pdds_solve_interface",
     "pdds_subdomain_solve", "pdds_semilinear_tables", "pdds_batch_build", "pdds_batch_run", "pdds_batch_instance",
@@ -150,6 +151,7 @@ def load(path: str = LIB_PATH):
     dp = C.POINTER(C.c_double)
     L.pdds_create.argtypes = [C.POINTER(vp), C.c_int, C.c_uint32]
     L.pdds_destroy.argtypes = [vp]
+    L.pdds_release_cached_blocks.argtypes = [C.c_int32]
     L.pdds_last_error.restype = C.c_char_p
     L.pdds_last_error.argtypes = [vp]
     L.pdds_version.restype = C.c_char_p

@@ -132,13 +132,6 @@ class BVP:
                               np.tanh(np.sin(0.12 * x + 0.05 * y) + np.sin(0.05 * x - 0.12 * y)))
 
 
-def _touched(n: int):
-    """Uninitialised float64 array with every 4 KB page touched."""
-    a = np.empty(n)
-    a[::512] = 0.0
-    return a
-
-
 def linear_iteration_u(x, y):
     """Exact solution of the linear fixed-point loop's test problem
     (Equation_u, BVPs/EDPs/Salou_Iterative.hpp)."""
@@ -243,6 +236,15 @@ class Estimate:
     def triplets(self):
         rows = np.repeat(np.arange(len(self.row_ptr) - 1), np.diff(self.row_ptr))
         return rows, self.col, self.val
+
+
+def release_cached_blocks(device: int = -1) -> None:
+    """Returns to the device the buffers the library keeps from closed
+    PDDSparseGM contexts (pdds_release_cached_blocks; device -1: every
+    device), e.g. before handing the GPU's memory to another allocator."""
+    st = capi.load().pdds_release_cached_blocks(int(device))
+    if st != capi.OK:
+        raise PDDSError(st, "pdds_release_cached_blocks failed")
 
 
 class PDDSparseGM:
@@ -425,13 +427,13 @@ class PDDSparseGM:
             keep = np.ascontiguousarray(ipsi_override, np.float64)
             d.ipsi_override = _p(keep, C.c_double)
             d.ipsi_override_len = keep.size
-        # the read-back targets are touched on the CPU first, one element per
-        # 4 KB: a device-to-host copy into never-touched pages faults them in
-        # one by one from the copy (tens of ms for the 32 MB of G on the
-        # 12x12/43 layout); the copy then overwrites every element
+        # the read-back targets stay uninitialised: pdds_estimate touches
+        # their pages while the device runs the paths (a device-to-host copy
+        # into never-touched pages faults them in one by one from inside the
+        # copy), and the copy then overwrites every element
         read_var = want_var or mode == capi.MODE_REPLAY_FP64
-        val = _touched(max(self.nnz, 1))
-        var = _touched(max(self.nnz, 1)) if read_var else np.zeros(max(self.nnz, 1))
+        val = np.empty(max(self.nnz, 1))
+        var = np.empty(max(self.nnz, 1)) if read_var else np.zeros(max(self.nnz, 1))
         B = np.zeros(self.K)
         BB = np.zeros(self.K)
         info = capi.EstimateInfo()

@@ -106,7 +106,12 @@ pdds_status pdds_batch_build(pdds_ctx* ctx, const pdds_instance_desc* inst, int3
       }
     };
     std::vector<std::thread> pool;
-    for (int t = 1; t < nth; t++) pool.emplace_back(worker, t);
+    int t = 1;
+    try {
+      for (; t < nth; t++) pool.emplace_back(worker, t);
+    } catch (const std::exception&) {  // no thread: the workers left run here
+    }
+    for (int r = t; r < nth; r++) worker(r);
     worker(0);
     for (auto& th : pool) th.join();
     for (int i = 0; i < n; i++)

@@ -6,6 +6,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -22,6 +24,100 @@ namespace pdds {
 XferCount& xfer() {
   thread_local XferCount t;
   return t;
+}
+
+namespace {
+
+struct BlockCache {
+  std::mutex mu;
+  std::map<int, std::multimap<size_t, void*>> free_blocks;  // per device: bytes -> block
+  std::map<int, size_t> held;                                // per device: bytes cached
+};
+
+BlockCache& block_cache() {
+  static BlockCache* c = new BlockCache();  // never destroyed: no CUDA calls at exit
+  return *c;
+}
+
+constexpr size_t CACHE_MAX_BLOCK = size_t(2) << 30;  // larger blocks are freed at once
+constexpr size_t CACHE_MAX_HELD = size_t(8) << 30;   // per device
+
+}  // namespace
+
+// 512 B, then four classes per octave up to 64 MB, then multiples of 2 MB;
+// a class size maps to itself.
+size_t block_class(size_t bytes) {
+  if (bytes <= 512) return 512;
+  if (bytes > (size_t(64) << 20)) {
+    const size_t m = size_t(2) << 20;
+    return (bytes + m - 1) / m * m;
+  }
+  int e = 0;
+  while ((size_t(1) << (e + 1)) < bytes) e++;  // 2^e < bytes <= 2^(e+1)
+  const size_t step = size_t(1) << (e - 2);
+  return (bytes + step - 1) / step * step;
+}
+
+cudaError_t block_alloc(void** p, size_t bytes) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  {
+    BlockCache& c = block_cache();
+    std::lock_guard<std::mutex> lk(c.mu);
+    auto& fb = c.free_blocks[dev];
+    auto it = fb.find(bytes);
+    if (it != fb.end()) {
+      *p = it->second;
+      fb.erase(it);
+      c.held[dev] -= bytes;
+      return cudaSuccess;
+    }
+  }
+  e = cudaMalloc(p, bytes);
+  if (e == cudaErrorMemoryAllocation) {
+    cudaGetLastError();
+    block_cache_clear(dev);
+    e = cudaMalloc(p, bytes);
+  }
+  return e;
+}
+
+void block_recycle(void* p, size_t bytes) {
+  if (!p) return;
+  int dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess && bytes <= CACHE_MAX_BLOCK) {
+    BlockCache& c = block_cache();
+    std::lock_guard<std::mutex> lk(c.mu);
+    if (c.held[dev] + bytes <= CACHE_MAX_HELD) {
+      c.free_blocks[dev].emplace(bytes, p);
+      c.held[dev] += bytes;
+      return;
+    }
+  }
+  cudaFree(p);
+}
+
+void block_cache_clear(int device) {
+  std::vector<std::pair<int, void*>> drop;
+  {
+    BlockCache& c = block_cache();
+    std::lock_guard<std::mutex> lk(c.mu);
+    for (auto& kv : c.free_blocks) {
+      if (device >= 0 && kv.first != device) continue;
+      for (auto& b : kv.second) drop.push_back({kv.first, b.second});
+      kv.second.clear();
+      c.held[kv.first] = 0;
+    }
+  }
+  if (drop.empty()) return;
+  int cur = 0;
+  const bool have = cudaGetDevice(&cur) == cudaSuccess;
+  for (auto& d : drop) {
+    cudaSetDevice(d.first);
+    cudaFree(d.second);
+  }
+  if (have) cudaSetDevice(cur);
 }
 
 pdds_status fail(pdds_ctx* c, pdds_status s, const std::string& msg) {
@@ -57,6 +153,18 @@ void release_lut_tex(pdds_ctx* ctx) {
 }
 
 namespace {
+
+// Writes one zero byte per 4 KB of a host output buffer.  A device-to-host
+// copy into pages that were never touched faults them in from inside the
+// copy; touching them from the host thread while the device still runs the
+// kernels takes that cost off the critical path (the copy then overwrites
+// every byte).
+void prefault(void* p, size_t bytes) {
+  if (!p) return;
+  volatile unsigned char* c = static_cast<volatile unsigned char*>(p);
+  for (size_t i = 0; i < bytes; i += 4096) c[i] = 0;
+  if (bytes) c[bytes - 1] = 0;
+}
 
 // Cubic B-spline coefficients c of the samples f along one line of n nodes
 // with stride `stride`, in place: (c_{i-1} + 4 c_i + c_{i+1}) / 6 = f_i, with
@@ -200,47 +308,54 @@ pdds_status upload_layout(pdds_ctx* ctx) {
   ctx->fp64_smem = (FP64_THREADS / 32 + 1) * fsm * sizeof(double);  // per-warp sums, knot coordinates
   std::vector<unsigned char> owner(L.map_owner.begin(), L.map_owner.end());
   std::vector<int> knot_stencil(L.knot_stencil.begin(), L.knot_stencil.end());
-  CK(ctx->kx.upload(L.kx, s));
-  CK(ctx->ky.upload(L.ky, s));
-  CK(ctx->knot_stencil.upload(knot_stencil, s));
-  CK(ctx->row_ptr.upload(L.row_ptr, s));
-  {  // G's column indices, expanded on the device from the stencils' lists
-    std::vector<int64_t> st_col_off;
-    std::vector<int32_t> st_cols;
-    layout_stencil_cols(L, st_col_off, st_cols);
-    CK(ctx->st_col_off.upload(st_col_off, s));
-    CK(ctx->st_cols.upload(st_cols, s));
-    CK(ctx->col.resize(std::max<int64_t>(L.row_ptr[L.K], 1)));
-    CK(launch_expand_cols(L.K, ctx->row_ptr.p, ctx->knot_stencil.p, ctx->st_col_off.p, ctx->st_cols.p, ctx->col.p,
-                          s));
-  }
-  CK(ctx->st_rect.upload(st_rect, s));
-  CK(ctx->st_side.upload(st_side, s));
-  CK(ctx->st_glob.upload(st_glob, s));
-  CK(ctx->st_map_off.upload(st_map_off, s));
-  CK(ctx->map_pos.upload(L.map_pos, s));
-  CK(ctx->map_owner.upload(owner, s));
-  CK(ctx->sd_n.upload(sd_n, s));
-  CK(ctx->sd_orient.upload(sd_orient, s));
-  CK(ctx->sd_shape.upload(sd_shape, s));
-  CK(ctx->sd_c.upload(sd_c, s));
-  CK(ctx->sd_origin.upload(sd_origin, s));
-  CK(ctx->sd_knot_off.upload(sd_knot_off, s));
-  CK(ctx->side_knot.upload(L.side_knot, s));
-  CK(ctx->side_px.upload(L.side_px, s));
-  CK(ctx->side_py.upload(L.side_py, s));
-  CK(ctx->sh_n.upload(sh_n, s));
-  CK(ctx->sh_nbins.upload(sh_nbins, s));
-  CK(ctx->sh_c.upload(sh_c, s));
-  CK(ctx->sh_R.upload(sh_R, s));
-  CK(ctx->sh_lo.upload(sh_lo, s));
-  CK(ctx->sh_delta.upload(sh_delta, s));
-  CK(ctx->sh_tab_off.upload(sh_tab_off, s));
-  CK(ctx->sh_ipsi_off.upload(sh_ipsi_off, s));
-  CK(ctx->sh_t_off.upload(sh_t_off, s));
-  CK(ctx->sh_t.upload(sh_t, s));
-  CK(ctx->mc_knots.upload(mc, s));
-  CK(ctx->bnd_knots.upload(bnd, s));
+  // the layout's arrays in one device block: one allocation and one copy
+  // (a small pageable copy or an allocation costs about as much as the
+  // whole 3 MB block of the 12x12/43 layout)
+  std::vector<int64_t> st_col_off;
+  std::vector<int32_t> st_cols;
+  layout_stencil_cols(L, st_col_off, st_cols);  // G's columns, expanded on the device
+  std::vector<int> kr(L.knot_rng.begin(), L.knot_rng.end());
+  PackedUpload pk;
+  pk.add(ctx->kx, L.kx);
+  pk.add(ctx->ky, L.ky);
+  pk.add(ctx->knot_stencil, knot_stencil);
+  pk.add(ctx->row_ptr, L.row_ptr);
+  pk.add(ctx->st_col_off, st_col_off);
+  pk.add(ctx->st_cols, st_cols);
+  pk.add(ctx->st_rect, st_rect);
+  pk.add(ctx->st_side, st_side);
+  pk.add(ctx->st_glob, st_glob);
+  pk.add(ctx->st_map_off, st_map_off);
+  pk.add(ctx->map_pos, L.map_pos);
+  pk.add(ctx->map_owner, owner);
+  pk.add(ctx->sd_n, sd_n);
+  pk.add(ctx->sd_orient, sd_orient);
+  pk.add(ctx->sd_shape, sd_shape);
+  pk.add(ctx->sd_c, sd_c);
+  pk.add(ctx->sd_origin, sd_origin);
+  pk.add(ctx->sd_knot_off, sd_knot_off);
+  pk.add(ctx->side_knot, L.side_knot);
+  pk.add(ctx->side_px, L.side_px);
+  pk.add(ctx->side_py, L.side_py);
+  pk.add(ctx->sh_n, sh_n);
+  pk.add(ctx->sh_nbins, sh_nbins);
+  pk.add(ctx->sh_c, sh_c);
+  pk.add(ctx->sh_R, sh_R);
+  pk.add(ctx->sh_lo, sh_lo);
+  pk.add(ctx->sh_delta, sh_delta);
+  pk.add(ctx->sh_tab_off, sh_tab_off);
+  pk.add(ctx->sh_ipsi_off, sh_ipsi_off);
+  pk.add(ctx->sh_t_off, sh_t_off);
+  pk.add(ctx->sh_t, sh_t);
+  pk.add(ctx->mc_knots, mc);
+  pk.add(ctx->bnd_knots, bnd);
+  if (!kr.empty()) pk.add(ctx->knot_rng, kr);
+  else ctx->knot_rng.release();
+  CK(ctx->lay_block.resize(pk.host.size()));
+  CK(copy_async(ctx->lay_block.p, pk.host.data(), pk.host.size(), cudaMemcpyHostToDevice, s));
+  pk.bind(ctx->lay_block.p);
+  CK(ctx->col.resize(std::max<int64_t>(L.row_ptr[L.K], 1)));
+  CK(launch_expand_cols(L.K, ctx->row_ptr.p, ctx->knot_stencil.p, ctx->st_col_off.p, ctx->st_cols.p, ctx->col.p, s));
   CK(ctx->ipsi.resize(std::max<int64_t>(ipsi_len, 1)));
   CK(ctx->rbf_lu.resize(std::max<int64_t>(ipsi_len, 1)));
   CK(ctx->rbf_uinv.resize(std::max<size_t>(sh_t.size(), 1)));
@@ -278,12 +393,7 @@ pdds_status upload_layout(pdds_ctx* ctx) {
   d.inst_knot0 = ctx->is_batch ? ctx->inst_knot0.p : nullptr;
   d.inst_p = ctx->is_batch ? ctx->inst_pd.p : nullptr;
   d.inst_h = ctx->is_batch ? ctx->inst_hd.p : nullptr;
-  d.knot_rng = nullptr;
-  if (!L.knot_rng.empty()) {
-    std::vector<int> kr(L.knot_rng.begin(), L.knot_rng.end());
-    CK(ctx->knot_rng.upload(kr, s));
-    d.knot_rng = ctx->knot_rng.p;
-  }
+  d.knot_rng = kr.empty() ? nullptr : ctx->knot_rng.p;
   ctx->tables_ready = false;
   return PDDS_OK;
 }
@@ -657,66 +767,78 @@ pdds_status pdds_create(pdds_ctx** out, int device, uint32_t flags) {
   return PDDS_OK;
 }
 
+pdds_status pdds_release_cached_blocks(int32_t device) {
+  block_cache_clear(device);
+  return PDDS_OK;
+}
+
 pdds_status pdds_destroy(pdds_ctx* ctx) {
   if (!ctx) return PDDS_ERR_INVALID;
   if (ctx->device >= 0) {
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    if (ctx->solve_stream) cudaStreamSynchronize(ctx->solve_stream);
+    // both streams are idle: the buffers go to the block cache for the next
+    // context
     DBuf<double>* d64[] = {&ctx->kx, &ctx->ky, &ctx->st_rect, &ctx->sd_c, &ctx->sd_origin, &ctx->side_px,
                            &ctx->side_py, &ctx->sh_c, &ctx->sh_R, &ctx->sh_lo, &ctx->sh_delta, &ctx->sh_t, &ctx->ipsi,
                            &ctx->G, &ctx->GG, &ctx->B, &ctx->BB, &ctx->Bsum, &ctx->BBsum, &ctx->rx,
                            &ctx->ry, &ctx->rY, &ctx->rZ, &ctx->rxi, &ctx->Gside, &ctx->GGside,
                            &ctx->ipsi_knot, &ctx->sv64, &ctx->sscal, &ctx->spart, &ctx->shess, &ctx->su,
                            &ctx->rbf_lu, &ctx->rbf_uinv};
-    for (auto* b : d64) b->release();
+    for (auto* b : d64) b->recycle();
     DBuf<int>* di[] = {&ctx->knot_stencil, &ctx->st_side, &ctx->st_glob, &ctx->map_pos, &ctx->sd_n,
                        &ctx->sd_orient, &ctx->sd_shape, &ctx->side_knot, &ctx->sh_n, &ctx->sh_nbins,
                        &ctx->col, &ctx->mc_knots, &ctx->bnd_knots, &ctx->counter, &ctx->rside,
                        &ctx->rsl, &ctx->rss, &ctx->task_m, &ctx->task_d, &ctx->task_i, &ctx->rbf_piv};
-    for (auto* b : di) b->release();
+    for (auto* b : di) b->recycle();
     DBuf<int64_t>* dl[] = {&ctx->row_ptr, &ctx->st_map_off, &ctx->sd_knot_off, &ctx->sh_tab_off,
                            &ctx->sh_ipsi_off, &ctx->sh_t_off, &ctx->task_out, &ctx->knot_task_off,
                            &ctx->knot_ipsi_off};
-    for (auto* b : dl) b->release();
-    ctx->st_col_off.release();
-    ctx->st_cols.release();
-    ctx->map_owner.release();
-    ctx->tab.release();
-    ctx->lut_coef.release();
-    ctx->lut_g.release();
+    for (auto* b : dl) b->recycle();
+    ctx->st_col_off.recycle();
+    ctx->st_cols.recycle();
+    ctx->map_owner.recycle();
+    ctx->lay_block.recycle();
+    ctx->knot_rng.recycle();
+    ctx->tab.recycle();
+    ctx->lut_coef.recycle();
+    ctx->lut_g.recycle();
     release_lut_tex(ctx);
-    ctx->stats.release();
-    ctx->errf.release();
-    ctx->sV32.release();
-    ctx->sZ32.release();
-    ctx->sw32.release();
-    ctx->sval32.release();
-    ctx->sctl.release();
-    ctx->sgpart.release();
-    ctx->sbar.release();
+    ctx->stats.recycle();
+    ctx->errf.recycle();
+    ctx->sV32.recycle();
+    ctx->sZ32.recycle();
+    ctx->sw32.recycle();
+    ctx->sval32.recycle();
+    ctx->sctl.recycle();
+    ctx->sgpart.recycle();
+    ctx->sbar.recycle();
     drop_graph(ctx);
-    ctx->knot_inst.release();
-    ctx->inst_knot0.release();
-    ctx->b_iters.release();
-    ctx->b_refines.release();
-    ctx->inst_pd.release();
-    ctx->inst_hd.release();
-    ctx->b_relres.release();
-    ctx->b_tend.release();
-    ctx->knot_N.release();
-    ctx->knot_steps.release();
-    ctx->mc_lpt.release();
-    ctx->edge_knots.release();
-    ctx->sub_u.release();
-    ctx->sub_out.release();
-    ctx->sub_work.release();
-    ctx->sub_iters.release();
-    ctx->ugrid.release();
-    ctx->item_knot.release();
-    ctx->item_p0.release();
-    ctx->item_p1.release();
-    ctx->knot_scale.release();
-    ctx->knot_invN.release();
+    ctx->knot_inst.recycle();
+    ctx->inst_knot0.recycle();
+    ctx->b_iters.recycle();
+    ctx->b_refines.recycle();
+    ctx->inst_pd.recycle();
+    ctx->inst_hd.recycle();
+    ctx->b_relres.recycle();
+    ctx->b_tend.recycle();
+    ctx->knot_N.recycle();
+    ctx->knot_steps.recycle();
+    ctx->mc_lpt.recycle();
+    ctx->edge_knots.recycle();
+    ctx->sub_u.recycle();
+    ctx->sub_out.recycle();
+    ctx->sub_work.recycle();
+    ctx->sub_iters.recycle();
+    ctx->ugrid.recycle();
+    ctx->item_knot.recycle();
+    ctx->item_p0.recycle();
+    ctx->item_p1.recycle();
+    ctx->knot_scale.recycle();
+    ctx->knot_invN.recycle();
+    ctx->step_hist.recycle();
+    for (auto* b : {&ctx->diag, &ctx->rsx, &ctx->rsy, &ctx->rsY, &ctx->rsZ, &ctx->rsxi, &ctx->rknot_h}) b->recycle();
     if (ctx->host_rr) cudaFreeHost(ctx->host_rr);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -1188,6 +1310,8 @@ pdds_status pdds_estimate(pdds_ctx* ctx, const pdds_estimate_desc* desc, double*
     ctx->last_knot_N.assign(L.K, 0);
     for (int m = r0; m < r0 + rn; m++) ctx->last_knot_N[ctx->mc_host[m]] = N;
   }
+  prefault(val, nnz * sizeof(double));
+  if (mode != PDDS_MODE_FP64) prefault(var, nnz * sizeof(double));
   if (val && nnz) CK(copy_async(val, ctx->G.p, nnz * sizeof(double), cudaMemcpyDeviceToHost, s));
   if (var && nnz) {
     if (mode == PDDS_MODE_FP64) std::fill(var, var + nnz, 0.0);

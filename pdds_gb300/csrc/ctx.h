@@ -3,6 +3,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <cstring>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -13,18 +15,32 @@
 
 namespace pdds {
 
+// Device blocks of destroyed contexts, kept per device for the next context
+// (a context allocates some 60 buffers; each cudaMalloc and cudaFree costs
+// about 10 us).  Only pdds_destroy hands blocks back, after synchronizing
+// its stream, so a cached block has no work in flight.  block_alloc rounds
+// the size up to the block classes and takes a cached block of that class,
+// else calls cudaMalloc (after emptying the cache if that fails).
+size_t block_class(size_t bytes);
+cudaError_t block_alloc(void** p, size_t bytes);
+void block_recycle(void* p, size_t bytes);  // into the cache (or cudaFree)
+void block_cache_clear(int device);         // -1: every device
+
+// A device array: owned (cudaMalloc) or a view into another buffer's block
+// (set_view; not freed here, and replaced by an owned block if it must grow).
 template <typename T>
 struct DBuf {
   T* p = nullptr;
   size_t n = 0;
+  bool view = false;
   cudaError_t resize(size_t count) {
     if (count <= n && p) return cudaSuccess;
-    if (p) cudaFree(p);
-    p = nullptr;
-    n = 0;
+    release();
     if (count == 0) return cudaSuccess;
-    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
-    if (e == cudaSuccess) n = count;
+    const size_t bytes = block_class(count * sizeof(T));
+    cudaError_t e = block_alloc(reinterpret_cast<void**>(&p), bytes);
+    if (e == cudaSuccess) n = bytes / sizeof(T);
+    else p = nullptr;
     return e;
   }
   cudaError_t upload(const std::vector<T>& v, cudaStream_t s) {
@@ -32,10 +48,46 @@ struct DBuf {
     if (e != cudaSuccess || v.empty()) return e;
     return copy_async(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s);
   }
+  void set_view(void* base, size_t count) {
+    release();
+    p = static_cast<T*>(base);
+    n = count;
+    view = true;
+  }
   void release() {
-    if (p) cudaFree(p);
+    if (p && !view) cudaFree(p);
     p = nullptr;
     n = 0;
+    view = false;
+  }
+  // release into the block cache (pdds_destroy, after its stream is idle)
+  void recycle() {
+    if (p && !view) block_recycle(p, block_class(n * sizeof(T)));
+    p = nullptr;
+    n = 0;
+    view = false;
+  }
+};
+
+// Host arrays packed into one block (each at a 256-byte offset) that is
+// copied to the device at once; bind() then points each DBuf at its part.
+struct PackedUpload {
+  std::vector<unsigned char> host;
+  std::vector<std::function<void(unsigned char*)>> binds;
+  template <typename T>
+  void add(DBuf<T>& b, const T* src, size_t count) {
+    const size_t off = (host.size() + 255) & ~size_t(255);
+    const size_t cnt = std::max<size_t>(count, 1);
+    host.resize(off + cnt * sizeof(T));
+    if (count) std::memcpy(host.data() + off, src, count * sizeof(T));
+    binds.push_back([&b, off, cnt](unsigned char* base) { b.set_view(base + off, cnt); });
+  }
+  template <typename T>
+  void add(DBuf<T>& b, const std::vector<T>& v) {
+    add(b, v.data(), v.size());
+  }
+  void bind(unsigned char* base) {
+    for (auto& f : binds) f(base);
   }
 };
 
@@ -74,6 +126,7 @@ struct pdds_ctx {
   DBuf<int> rbf_piv;
   DBuf<int64_t> row_ptr, st_map_off, sd_knot_off, sh_tab_off, sh_ipsi_off, sh_t_off;
   DBuf<unsigned char> map_owner;
+  DBuf<unsigned char> lay_block;  // one device block holding the layout arrays above (views)
   DBuf<int> knot_rng;             // Philox knot word per knot (caller-built stencils)
   DBuf<float> tab;
   DevLayout dl{};
