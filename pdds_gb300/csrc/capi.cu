@@ -306,8 +306,6 @@ pdds_status upload_layout(pdds_ctx* ctx) {
   }
   ctx->mixed_smem = msm * sizeof(float);
   ctx->fp64_smem = (FP64_THREADS / 32 + 1) * fsm * sizeof(double);  // per-warp sums, knot coordinates
-  std::vector<unsigned char> owner(L.map_owner.begin(), L.map_owner.end());
-  std::vector<int> knot_stencil(L.knot_stencil.begin(), L.knot_stencil.end());
   // the layout's arrays in one device block: one allocation and one copy
   // (a small pageable copy or an allocation costs about as much as the
   // whole 3 MB block of the 12x12/43 layout)
@@ -318,7 +316,7 @@ pdds_status upload_layout(pdds_ctx* ctx) {
   PackedUpload pk;
   pk.add(ctx->kx, L.kx);
   pk.add(ctx->ky, L.ky);
-  pk.add(ctx->knot_stencil, knot_stencil);
+  pk.add(ctx->knot_stencil, L.knot_stencil);
   pk.add(ctx->row_ptr, L.row_ptr);
   pk.add(ctx->st_col_off, st_col_off);
   pk.add(ctx->st_cols, st_cols);
@@ -327,7 +325,7 @@ pdds_status upload_layout(pdds_ctx* ctx) {
   pk.add(ctx->st_glob, st_glob);
   pk.add(ctx->st_map_off, st_map_off);
   pk.add(ctx->map_pos, L.map_pos);
-  pk.add(ctx->map_owner, owner);
+  pk.add(ctx->map_owner, L.map_owner);
   pk.add(ctx->sd_n, sd_n);
   pk.add(ctx->sd_orient, sd_orient);
   pk.add(ctx->sd_shape, sd_shape);
@@ -351,6 +349,7 @@ pdds_status upload_layout(pdds_ctx* ctx) {
   pk.add(ctx->bnd_knots, bnd);
   if (!kr.empty()) pk.add(ctx->knot_rng, kr);
   else ctx->knot_rng.release();
+  pk.pack();
   CK(ctx->lay_block.resize(pk.host.size()));
   CK(copy_async(ctx->lay_block.p, pk.host.data(), pk.host.size(), cudaMemcpyHostToDevice, s));
   pk.bind(ctx->lay_block.p);

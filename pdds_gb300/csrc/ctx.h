@@ -70,21 +70,34 @@ struct DBuf {
 };
 
 // Host arrays packed into one block (each at a 256-byte offset) that is
-// copied to the device at once; bind() then points each DBuf at its part.
+// copied to the device at once: add() records the parts, pack() sizes the
+// host block once and copies them in, bind() points each DBuf at its part.
+// The sources must stay alive until pack().
 struct PackedUpload {
+  struct Part {
+    const void* src;
+    size_t bytes, off;
+  };
+  std::vector<Part> parts;
   std::vector<unsigned char> host;
   std::vector<std::function<void(unsigned char*)>> binds;
+  size_t size = 0;
   template <typename T>
   void add(DBuf<T>& b, const T* src, size_t count) {
-    const size_t off = (host.size() + 255) & ~size_t(255);
+    const size_t off = (size + 255) & ~size_t(255);
     const size_t cnt = std::max<size_t>(count, 1);
-    host.resize(off + cnt * sizeof(T));
-    if (count) std::memcpy(host.data() + off, src, count * sizeof(T));
+    size = off + cnt * sizeof(T);
+    parts.push_back({src, count * sizeof(T), off});
     binds.push_back([&b, off, cnt](unsigned char* base) { b.set_view(base + off, cnt); });
   }
   template <typename T>
   void add(DBuf<T>& b, const std::vector<T>& v) {
     add(b, v.data(), v.size());
+  }
+  void pack() {
+    host.assign(size, 0);
+    for (const Part& q : parts)
+      if (q.bytes) std::memcpy(host.data() + q.off, q.src, q.bytes);
   }
   void bind(unsigned char* base) {
     for (auto& f : binds) f(base);
