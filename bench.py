@@ -460,7 +460,9 @@ def circle_uneven(local: int, reps: int = 2, h: float = 2e-5):
     a path takes from 1 to a few 1e4 steps (the paths' step counts fill every
     log2 bin from 1 to 2^14..2^15) and a knot's mean from ~50 to ~1600;
     Richardson pair, variance-adaptive paths per knot N_k in [1e3, 1e5] for a
-    score standard error of 1e-3, the launch shape picked by the autotuner.
+    score standard error of 1e-3, the launch shape picked by the autotuner
+    (after the warm-up estimate, whose continuation it times at both block
+    sizes).
     The same estimate with one CTA per work item in layout order shows what
     the persistent CTAs and the heaviest-first order do on it.  The FP64
     form runs the same layout with 1e3 paths per knot for the MIXED/FP64
@@ -470,14 +472,16 @@ def circle_uneven(local: int, reps: int = 2, h: float = 2e-5):
     pd = P.PDDSparseGM.circle_mesh(1.0, 6, 16, 11, device=local)
     ex = bvp.u(pd.x, pd.y)
     opts = dict(adaptive_h=True, richardson=True, dup_sum=True)
-    tune = pd.autotune(bvp, 1000, h, adaptive_h=True, richardson=True)
     runs = []
+    tune = None
     for r in range(reps + 1):
         est = pd.estimate(bvp, 1000, h, mode=P.MODE_MIXED, seed=1234, instance=r, adaptive_n=True,
                           npaths_max=100_000, target_stderr=1e-3, step_histogram=True, **opts)
         u, si = pd.solve_interface()
         if r > 0:
             runs.append((est, u, si))
+        else:  # after the warm-up: the shapes, and the block size of its continuation
+            tune = pd.autotune(bvp, 1000, h, adaptive_h=True, richardson=True, adaptive_n=True)
     est, u, si = runs[-1]
     hist = pd.step_histogram()
     steps = pd.knot_steps().astype(np.float64)

@@ -372,8 +372,13 @@ pdds_status pdds_estimate_knot(pdds_ctx* ctx, const double domain[4], double x0,
  * scaled by the sampled fraction of knots, so each CTA sees as many work
  * items as in the full run.  desc->cta_threads = 128 or 256 keeps that
  * block size and searches only the other shape parameters; 0 searches both
- * block sizes.  The tuned shape is forgotten when a new layout or batch is
- * built.  Overwrites the device results of the last estimate. */
+ * block sizes.  With desc->adaptive_n set and a variance-adaptive estimate
+ * run before on this layout, it also times that estimate's continuation
+ * (its work items after the pilot, each knot's paths N0 .. N_k) at both
+ * block sizes and keeps the faster for the continuation of later adaptive
+ * estimates: those items hold the long paths, and a uniform sample does not
+ * show their tail.  The tuned shape is forgotten when a new layout or batch
+ * is built.  Overwrites the device results of the last estimate. */
 typedef struct {
   int32_t blocks_per_sm;     /* chosen persistent CTAs per SM            */
   int32_t paths_per_item;    /* chosen paths per work item (knot, chunk) */
@@ -382,6 +387,9 @@ typedef struct {
   double best_ms;            /* sample time with the chosen shape        */
   double default_ms;         /* sample time with the default shape       */
   int32_t cta_threads;       /* chosen threads per CTA (128 or 256)      */
+  int32_t continuation_threads; /* adaptive continuation's threads per CTA
+                                   (0: not timed)                        */
+  double continuation_ms[2]; /* its time at 128 and 256 threads          */
 } pdds_tune_info;
 
 pdds_status pdds_autotune(pdds_ctx* ctx, const pdds_estimate_desc* desc, int32_t sample_knots,

@@ -455,10 +455,13 @@ class PDDSparseGM:
 
     def autotune(self, bvp: BVP, npaths: int, h: float, sample_knots: int = 0, seed: int = 1234,
                  adaptive_h: bool = False, richardson: bool = False, want_var: bool = False,
-                 cta_threads: int = 0) -> dict:
+                 cta_threads: int = 0, adaptive_n: bool = False) -> dict:
         """Times the MIXED path kernel's launch shapes on a sample of knots and
         keeps the fastest for later estimates of this problem kind
-        (cta_threads 128 or 256 keeps that block size, 0 searches both)."""
+        (cta_threads 128 or 256 keeps that block size, 0 searches both).
+        adaptive_n: also times the continuation of the last variance-adaptive
+        estimate on this layout at both block sizes and keeps the faster for
+        later adaptive estimates (continuation_threads; 0 when there was none)."""
         self._check(self._lib.pdds_problem_set(self._ctx, C.byref(bvp.desc())))
         d = capi.EstimateDesc()
         d.mode = capi.MODE_MIXED
@@ -469,9 +472,12 @@ class PDDSparseGM:
         d.richardson = int(bool(richardson))
         d.want_var = int(bool(want_var))
         d.cta_threads = int(cta_threads)
+        d.adaptive_n = int(bool(adaptive_n))
         info = capi.TuneInfo()
         self._check(self._lib.pdds_autotune(self._ctx, C.byref(d), int(sample_knots), C.byref(info)))
-        return {f: getattr(info, f) for f, _ in capi.TuneInfo._fields_}
+        out = {f: getattr(info, f) for f, _ in capi.TuneInfo._fields_}
+        out["continuation_ms"] = list(info.continuation_ms)
+        return out
 
     def knot_steps(self):
         """Path steps per knot of the last MIXED estimate (both Richardson levels)."""

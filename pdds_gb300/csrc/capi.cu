@@ -139,8 +139,12 @@ void clear_tune(pdds_ctx* ctx) {
   ctx->tune_bps = 0;
   ctx->tune_ppc = 0;
   ctx->tune_threads = 0;
+  ctx->tune_cont_threads = 0;
   ctx->tune_kind = -1;
   ctx->tune_rich = -1;
+  ctx->cont_ik.clear();
+  ctx->cont_ip0.clear();
+  ctx->cont_ip1.clear();
 }
 
 void release_lut_tex(pdds_ctx* ctx) {
@@ -692,12 +696,20 @@ pdds_status adaptive_continue(pdds_ctx* ctx, const pdds_estimate_desc* desc, con
   CK(launch_scale_rows(ctx->mc_knots.p, ctx->n_mc, ctx->row_ptr.p, ctx->knot_scale.p, ctx->G.p,
                        desc->want_var ? ctx->GG.p : nullptr, s));
   ++*launches;
+  // kept for the autotuner, which times this continuation at both block sizes
+  ctx->cont_ik = ik;
+  ctx->cont_ip0 = ip0;
+  ctx->cont_ip1 = ip1;
+  ctx->cont_ppc = ppc;
   if (!ik.empty()) {
     CK(ctx->item_knot.upload(ik, s));
     CK(ctx->item_p0.upload(ip0, s));
     CK(ctx->item_p1.upload(ip1, s));
     ItemList items{ctx->item_knot.p, ctx->item_p0.p, ctx->item_p1.p, (int)ik.size(), ctx->knot_invN.p};
-    pdds_status st = enqueue_mixed_paths(ctx, desc, P, 1, ppc, launches, &items);
+    pdds_estimate_desc dc = *desc;  // the continuation's block size, when the autotuner timed one
+    if (dc.cta_threads == 0 && tuned_for(ctx, desc) && ctx->tune_cont_threads > 0)
+      dc.cta_threads = ctx->tune_cont_threads;
+    pdds_status st = enqueue_mixed_paths(ctx, &dc, P, 1, ppc, launches, &items);
     if (st != PDDS_OK) return st;
   }
   return PDDS_OK;
@@ -1454,11 +1466,42 @@ pdds_status pdds_autotune(pdds_ctx* ctx, const pdds_estimate_desc* desc, int32_t
         }
       }
   }
+  // the last adaptive estimate's continuation (knot paths N0 .. N_k), whole,
+  // at each block size: its items carry the long paths whose tail a uniform
+  // sample does not show
+  int cont_threads = 0;
+  float cont_ms[2] = {0.f, 0.f};
+  if (desc->adaptive_n && fixed_threads == 0 && !ctx->cont_ik.empty() && ctx->cont_ppc > 0) {
+    CK(ctx->item_knot.upload(ctx->cont_ik, s));
+    CK(ctx->item_p0.upload(ctx->cont_ip0, s));
+    CK(ctx->item_p1.upload(ctx->cont_ip1, s));
+    ItemList items{ctx->item_knot.p, ctx->item_p0.p, ctx->item_p1.p, (int)ctx->cont_ik.size(), ctx->knot_invN.p};
+    float best_c = 1e30f;
+    for (int ti = 0; ti < 2; ti++) {
+      pdds_estimate_desc dc = d;
+      dc.cta_threads = ti == 0 ? 128 : 256;
+      CK(cudaEventRecord(ctx->ev0, s));
+      int nl = 0;
+      st = enqueue_mixed_paths(ctx, &dc, P, 1, ctx->cont_ppc, &nl, &items);
+      if (st != PDDS_OK) return st;
+      CK(cudaEventRecord(ctx->ev1, s));
+      CK(cudaEventSynchronize(ctx->ev1));
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+      cont_ms[ti] = ms;
+      ++ncand;
+      if (ms < best_c) {
+        best_c = ms;
+        cont_threads = dc.cta_threads;
+      }
+    }
+  }
   st = check_err_flags(ctx);
   if (st != PDDS_OK) return st;
   ctx->tune_bps = best_bps;
   ctx->tune_ppc = best_ppc;
   ctx->tune_threads = best_threads;
+  ctx->tune_cont_threads = cont_threads;
   ctx->tune_kind = ctx->prob.kind;
   ctx->tune_rich = d.richardson ? 1 : 0;
   ctx->has_estimate = false;
@@ -1467,6 +1510,9 @@ pdds_status pdds_autotune(pdds_ctx* ctx, const pdds_estimate_desc* desc, int32_t
     info->blocks_per_sm = best_bps;
     info->paths_per_item = best_ppc;
     info->cta_threads = best_threads;
+    info->continuation_threads = cont_threads;
+    info->continuation_ms[0] = cont_ms[0];
+    info->continuation_ms[1] = cont_ms[1];
     info->candidates = ncand;
     info->sample_knots = ns;
     info->best_ms = best_ms;

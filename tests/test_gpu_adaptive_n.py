@@ -81,3 +81,26 @@ def test_autotuner_keeps_results_and_picks_a_valid_shape():
         assert again.info["cta_threads"] == other
         with pytest.raises(P.PDDSError):
             pd.autotune(bvp, 3000, H, sample_knots=64, cta_threads=192)
+
+
+def test_autotuner_times_the_adaptive_continuation():
+    """With adaptive_n the tuner also times the last adaptive estimate's
+    continuation (the items of paths N0 .. N_k) at both block sizes and the
+    next adaptive estimate continues with the faster one: a different work
+    split of the same Philox streams, so the same estimate up to summation
+    order where the recomputed pilot gives the same N_k."""
+    fac = fac_rule(2.0, NSUB, NNODE)
+    bvp = P.BVP.poisson_sincos()
+    opts = dict(adaptive_h=True, richardson=True, adaptive_n=True, npaths_max=NMAX, target_stderr=EPS)
+    with P.PDDSparseGM(SW, NE, NSUB, NNODE, fac) as pd:
+        t0 = pd.autotune(bvp, N0, H, sample_knots=64, adaptive_h=True, richardson=True, adaptive_n=True)
+        assert t0["continuation_threads"] == 0  # no adaptive estimate on this layout yet
+        before = pd.estimate(bvp, N0, H, mode=P.MODE_MIXED, seed=4, **opts)
+        t = pd.autotune(bvp, N0, H, sample_knots=64, adaptive_h=True, richardson=True, adaptive_n=True)
+        assert t["continuation_threads"] in (128, 256)
+        assert min(t["continuation_ms"]) > 0
+        assert t["continuation_ms"][(t["continuation_threads"] // 128) - 1] == min(t["continuation_ms"])
+        after = pd.estimate(bvp, N0, H, mode=P.MODE_MIXED, seed=4, **opts)
+        same = after.npaths == before.npaths
+        assert np.mean(same) > 0.95
+        assert np.max(np.abs(after.B - before.B)[same]) < 1e-9
