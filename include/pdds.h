@@ -375,9 +375,9 @@ pdds_status pdds_estimate_knot(pdds_ctx* ctx, const double domain[4], double x0,
  * block sizes.  With desc->adaptive_n set and a variance-adaptive estimate
  * run before on this layout, it also times that estimate's continuation
  * (its work items after the pilot, each knot's paths N0 .. N_k) at both
- * block sizes and keeps the faster for the continuation of later adaptive
- * estimates: those items hold the long paths, and a uniform sample does not
- * show their tail.  The tuned shape is forgotten when a new layout or batch
+ * block sizes, then at 2048 .. 16384 paths per item (4096 untuned), and
+ * keeps the fastest for the continuation of later adaptive estimates: those
+ * items hold the long paths, and a uniform sample does not show their tail.  The tuned shape is forgotten when a new layout or batch
  * is built.  Overwrites the device results of the last estimate. */
 typedef struct {
   int32_t blocks_per_sm;     /* chosen persistent CTAs per SM            */
@@ -389,7 +389,9 @@ typedef struct {
   int32_t cta_threads;       /* chosen threads per CTA (128 or 256)      */
   int32_t continuation_threads; /* adaptive continuation's threads per CTA
                                    (0: not timed)                        */
-  double continuation_ms[2]; /* its time at 128 and 256 threads          */
+  double continuation_ms[2]; /* its time at 128 and 256 threads (4096
+                                paths per item)                          */
+  int32_t continuation_paths_per_item; /* its chosen paths per item      */
 } pdds_tune_info;
 
 pdds_status pdds_autotune(pdds_ctx* ctx, const pdds_estimate_desc* desc, int32_t sample_knots,

@@ -98,7 +98,7 @@ class TuneInfo(C.Structure):
     _fields_ = [("blocks_per_sm", C.c_int32), ("paths_per_item", C.c_int32), ("candidates", C.c_int32),
                 ("sample_knots", C.c_int32), ("best_ms", C.c_double), ("default_ms", C.c_double),
                 ("cta_threads", C.c_int32), ("continuation_threads", C.c_int32),
-                ("continuation_ms", C.c_double * 2)]
+                ("continuation_ms", C.c_double * 2), ("continuation_paths_per_item", C.c_int32)]
 
 
 class SolveDesc(C.Structure):

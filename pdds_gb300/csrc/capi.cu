@@ -140,12 +140,32 @@ void clear_tune(pdds_ctx* ctx) {
   ctx->tune_ppc = 0;
   ctx->tune_threads = 0;
   ctx->tune_cont_threads = 0;
+  ctx->tune_cont_ppc = 0;
   ctx->tune_kind = -1;
   ctx->tune_rich = -1;
-  ctx->cont_ik.clear();
-  ctx->cont_ip0.clear();
-  ctx->cont_ip1.clear();
+  ctx->cont_knots.clear();
+  ctx->cont_N0 = 0;
 }
+
+// Work items of an adaptive continuation: each knot's paths N0 .. N_k-1 in
+// chunks of ppc, knots in the given order.
+void continuation_items(const std::vector<int>& knots, const std::vector<int>& nk, int N0, int ppc,
+                        std::vector<int>& ik, std::vector<int>& ip0, std::vector<int>& ip1) {
+  ik.clear();
+  ip0.clear();
+  ip1.clear();
+  for (int v : knots)
+    for (long long p = N0; p < nk[v]; p += ppc) {
+      ik.push_back(v);
+      ip0.push_back((int)p);
+      ip1.push_back((int)std::min<long long>(nk[v], p + ppc));
+    }
+}
+
+// paths per work item of an adaptive continuation when the autotuner timed
+// none: long items amortise the end of an item, where a CTA waits for its
+// longest path (circle at h = 2e-5: 389, 339, 317, 315 ms at 1024 .. 8192)
+constexpr int CONT_PPC_DEFAULT = 4096;
 
 void release_lut_tex(pdds_ctx* ctx) {
   for (int t = 0; t < 4; t++) {
@@ -665,7 +685,8 @@ pdds_status adaptive_continue(pdds_ctx* ctx, const pdds_estimate_desc* desc, con
   std::vector<int> kn(K, 0), ik, ip0, ip1;
   std::vector<double> scale(K, 1.0), inv(K, 0.0);
   std::vector<std::pair<double, int>> cost;  // the continuation's steps per knot, from the pilot
-  const int granule = 256, ppc = 2048;
+  const int granule = 256;
+  const int ppc = tuned_for(ctx, desc) && ctx->tune_cont_ppc > 0 ? ctx->tune_cont_ppc : CONT_PPC_DEFAULT;
   for (int v : L.order) {
     if (L.knot_boundary[v]) continue;
     const double mean = bs[v] / N0;
@@ -681,14 +702,10 @@ pdds_status adaptive_continue(pdds_ctx* ctx, const pdds_estimate_desc* desc, con
   }
   // work items heaviest knot first, so that no long item starts near the end
   std::stable_sort(cost.begin(), cost.end());
-  for (auto& c : cost) {
-    const int v = c.second;
-    for (long long p = N0; p < kn[v]; p += ppc) {
-      ik.push_back(v);
-      ip0.push_back((int)p);
-      ip1.push_back((int)std::min<long long>(kn[v], p + ppc));
-    }
-  }
+  std::vector<int> order;
+  order.reserve(cost.size());
+  for (auto& c : cost) order.push_back(c.second);
+  continuation_items(order, kn, N0, ppc, ik, ip0, ip1);
   ctx->last_knot_N = kn;
   CK(ctx->knot_N.upload(kn, s));
   CK(ctx->knot_scale.upload(scale, s));
@@ -696,11 +713,9 @@ pdds_status adaptive_continue(pdds_ctx* ctx, const pdds_estimate_desc* desc, con
   CK(launch_scale_rows(ctx->mc_knots.p, ctx->n_mc, ctx->row_ptr.p, ctx->knot_scale.p, ctx->G.p,
                        desc->want_var ? ctx->GG.p : nullptr, s));
   ++*launches;
-  // kept for the autotuner, which times this continuation at both block sizes
-  ctx->cont_ik = ik;
-  ctx->cont_ip0 = ip0;
-  ctx->cont_ip1 = ip1;
-  ctx->cont_ppc = ppc;
+  // kept for the autotuner, which times this continuation's shapes
+  ctx->cont_knots = order;
+  ctx->cont_N0 = N0;
   if (!ik.empty()) {
     CK(ctx->item_knot.upload(ik, s));
     CK(ctx->item_p0.upload(ip0, s));
@@ -1466,33 +1481,58 @@ pdds_status pdds_autotune(pdds_ctx* ctx, const pdds_estimate_desc* desc, int32_t
         }
       }
   }
-  // the last adaptive estimate's continuation (knot paths N0 .. N_k), whole,
-  // at each block size: its items carry the long paths whose tail a uniform
+  // the last adaptive estimate's continuation (knot paths N0 .. N_k), whole:
+  // both block sizes at the default item size, then item sizes at the
+  // faster block size; its items carry the long paths whose tail a uniform
   // sample does not show
-  int cont_threads = 0;
+  int cont_threads = 0, cont_ppc = 0;
   float cont_ms[2] = {0.f, 0.f};
-  if (desc->adaptive_n && fixed_threads == 0 && !ctx->cont_ik.empty() && ctx->cont_ppc > 0) {
-    CK(ctx->item_knot.upload(ctx->cont_ik, s));
-    CK(ctx->item_p0.upload(ctx->cont_ip0, s));
-    CK(ctx->item_p1.upload(ctx->cont_ip1, s));
-    ItemList items{ctx->item_knot.p, ctx->item_p0.p, ctx->item_p1.p, (int)ctx->cont_ik.size(), ctx->knot_invN.p};
-    float best_c = 1e30f;
-    for (int ti = 0; ti < 2; ti++) {
+  if (desc->adaptive_n && fixed_threads == 0 && !ctx->cont_knots.empty() &&
+      (int)ctx->last_knot_N.size() == L.K) {
+    std::vector<int> ik, ip0, ip1;
+    auto time_cont = [&](int threads, int ppc, float* ms_out) -> pdds_status {
+      continuation_items(ctx->cont_knots, ctx->last_knot_N, ctx->cont_N0, ppc, ik, ip0, ip1);
+      if (ik.empty()) {
+        *ms_out = 0.f;
+        return PDDS_OK;
+      }
+      CK(ctx->item_knot.upload(ik, s));
+      CK(ctx->item_p0.upload(ip0, s));
+      CK(ctx->item_p1.upload(ip1, s));
+      ItemList items{ctx->item_knot.p, ctx->item_p0.p, ctx->item_p1.p, (int)ik.size(), ctx->knot_invN.p};
       pdds_estimate_desc dc = d;
-      dc.cta_threads = ti == 0 ? 128 : 256;
+      dc.cta_threads = threads;
       CK(cudaEventRecord(ctx->ev0, s));
       int nl = 0;
-      st = enqueue_mixed_paths(ctx, &dc, P, 1, ctx->cont_ppc, &nl, &items);
-      if (st != PDDS_OK) return st;
+      pdds_status e = enqueue_mixed_paths(ctx, &dc, P, 1, ppc, &nl, &items);
+      if (e != PDDS_OK) return e;
       CK(cudaEventRecord(ctx->ev1, s));
       CK(cudaEventSynchronize(ctx->ev1));
       float ms = 0.f;
       CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
-      cont_ms[ti] = ms;
+      *ms_out = ms;
+      return PDDS_OK;
+    };
+    float best_c = 1e30f;
+    for (int ti = 0; ti < 2; ti++) {
+      const int th = ti == 0 ? 128 : 256;
+      st = time_cont(th, CONT_PPC_DEFAULT, &cont_ms[ti]);
+      if (st != PDDS_OK) return st;
+      ++ncand;
+      if (cont_ms[ti] < best_c) {
+        best_c = cont_ms[ti];
+        cont_threads = th;
+        cont_ppc = CONT_PPC_DEFAULT;
+      }
+    }
+    for (int ppc : {2048, 8192, 16384}) {
+      float ms = 0.f;
+      st = time_cont(cont_threads, ppc, &ms);
+      if (st != PDDS_OK) return st;
       ++ncand;
       if (ms < best_c) {
         best_c = ms;
-        cont_threads = dc.cta_threads;
+        cont_ppc = ppc;
       }
     }
   }
@@ -1502,6 +1542,7 @@ pdds_status pdds_autotune(pdds_ctx* ctx, const pdds_estimate_desc* desc, int32_t
   ctx->tune_ppc = best_ppc;
   ctx->tune_threads = best_threads;
   ctx->tune_cont_threads = cont_threads;
+  ctx->tune_cont_ppc = cont_ppc;
   ctx->tune_kind = ctx->prob.kind;
   ctx->tune_rich = d.richardson ? 1 : 0;
   ctx->has_estimate = false;
@@ -1511,6 +1552,7 @@ pdds_status pdds_autotune(pdds_ctx* ctx, const pdds_estimate_desc* desc, int32_t
     info->paths_per_item = best_ppc;
     info->cta_threads = best_threads;
     info->continuation_threads = cont_threads;
+    info->continuation_paths_per_item = cont_ppc;
     info->continuation_ms[0] = cont_ms[0];
     info->continuation_ms[1] = cont_ms[1];
     info->candidates = ncand;

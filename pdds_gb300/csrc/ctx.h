@@ -199,9 +199,9 @@ struct pdds_ctx {
   bool has_solution = false;
   // autotuned launch shape of the MIXED path kernel (0 = defaults)
   int tune_bps = 0, tune_ppc = 0, tune_kind = -1, tune_rich = -1, tune_threads = 0;
-  int tune_cont_threads = 0;                    // adaptive continuation's block size (0: untuned)
-  std::vector<int> cont_ik, cont_ip0, cont_ip1;  // work items of the last adaptive continuation
-  int cont_ppc = 0;
+  int tune_cont_threads = 0, tune_cont_ppc = 0;  // adaptive continuation's shape (0: untuned)
+  std::vector<int> cont_knots;                   // last adaptive continuation: knots, heaviest first
+  int cont_N0 = 0;                               // and its pilot's paths (N_k in last_knot_N)
   int force_bps = 0;             // CTAs per SM imposed while the autotuner times a shape
   double force_grid_frac = 0.0;  // grid scaled to a knot sample while it times
   // variance-adaptive paths (pdds_estimate with adaptive_n)

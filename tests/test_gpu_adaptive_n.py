@@ -85,8 +85,8 @@ def test_autotuner_keeps_results_and_picks_a_valid_shape():
 
 def test_autotuner_times_the_adaptive_continuation():
     """With adaptive_n the tuner also times the last adaptive estimate's
-    continuation (the items of paths N0 .. N_k) at both block sizes and the
-    next adaptive estimate continues with the faster one: a different work
+    continuation (the items of paths N0 .. N_k) at both block sizes and item
+    sizes, and the next adaptive estimate continues with the fastest: a different work
     split of the same Philox streams, so the same estimate up to summation
     order where the recomputed pilot gives the same N_k."""
     fac = fac_rule(2.0, NSUB, NNODE)
@@ -100,6 +100,7 @@ def test_autotuner_times_the_adaptive_continuation():
         assert t["continuation_threads"] in (128, 256)
         assert min(t["continuation_ms"]) > 0
         assert t["continuation_ms"][(t["continuation_threads"] // 128) - 1] == min(t["continuation_ms"])
+        assert t["continuation_paths_per_item"] in (2048, 4096, 8192, 16384)
         after = pd.estimate(bvp, N0, H, mode=P.MODE_MIXED, seed=4, **opts)
         same = after.npaths == before.npaths
         assert np.mean(same) > 0.95
