@@ -55,7 +55,9 @@ pdds_status pdds_create(pdds_ctx** ctx, int device, uint32_t flags);
  * sizes; pdds_release_cached_blocks returns them to the device. */
 pdds_status pdds_destroy(pdds_ctx* ctx);
 /* Frees the device buffers kept from destroyed contexts (device -1: on every
- * device).  The library also does so by itself when an allocation fails. */
+ * device).  The library also does so by itself when an allocation fails.
+ * Call it before a cudaDeviceReset of the device: the reset frees them
+ * behind the library's back. */
 pdds_status pdds_release_cached_blocks(int32_t device);
 const char* pdds_last_error(const pdds_ctx* ctx);
 const char* pdds_version(void);
