@@ -375,7 +375,8 @@ pdds_status pdds_estimate_knot(pdds_ctx* ctx, const double domain[4], double x0,
  * items as in the full run.  desc->cta_threads = 128 or 256 keeps that
  * block size and searches only the other shape parameters; 0 searches both
  * block sizes.  With desc->adaptive_n set and a variance-adaptive estimate
- * run before on this layout, it also times that estimate's continuation
+ * of the same problem kind run before on this layout, it also times that
+ * estimate's continuation
  * (its work items after the pilot, each knot's paths N0 .. N_k) at both
  * block sizes, then at 2048 .. 16384 paths per item (4096 untuned), and
  * keeps the fastest for the continuation of later adaptive estimates: those

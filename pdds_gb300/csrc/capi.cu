@@ -145,6 +145,7 @@ void clear_tune(pdds_ctx* ctx) {
   ctx->tune_rich = -1;
   ctx->cont_knots.clear();
   ctx->cont_N0 = 0;
+  ctx->cont_kind = -1;
 }
 
 // Work items of an adaptive continuation: each knot's paths N0 .. N_k-1 in
@@ -716,6 +717,7 @@ pdds_status adaptive_continue(pdds_ctx* ctx, const pdds_estimate_desc* desc, con
   // kept for the autotuner, which times this continuation's shapes
   ctx->cont_knots = order;
   ctx->cont_N0 = N0;
+  ctx->cont_kind = ctx->prob.kind;
   if (!ik.empty()) {
     CK(ctx->item_knot.upload(ik, s));
     CK(ctx->item_p0.upload(ip0, s));
@@ -1487,7 +1489,7 @@ pdds_status pdds_autotune(pdds_ctx* ctx, const pdds_estimate_desc* desc, int32_t
   // sample does not show
   int cont_threads = 0, cont_ppc = 0;
   float cont_ms[2] = {0.f, 0.f};
-  if (desc->adaptive_n && fixed_threads == 0 && !ctx->cont_knots.empty() &&
+  if (desc->adaptive_n && fixed_threads == 0 && !ctx->cont_knots.empty() && ctx->cont_kind == ctx->prob.kind &&
       (int)ctx->last_knot_N.size() == L.K) {
     std::vector<int> ik, ip0, ip1;
     auto time_cont = [&](int threads, int ppc, float* ms_out) -> pdds_status {

@@ -202,6 +202,7 @@ struct pdds_ctx {
   int tune_cont_threads = 0, tune_cont_ppc = 0;  // adaptive continuation's shape (0: untuned)
   std::vector<int> cont_knots;                   // last adaptive continuation: knots, heaviest first
   int cont_N0 = 0;                               // and its pilot's paths (N_k in last_knot_N)
+  int cont_kind = -1;                            // and its problem kind
   int force_bps = 0;             // CTAs per SM imposed while the autotuner times a shape
   double force_grid_frac = 0.0;  // grid scaled to a knot sample while it times
   // variance-adaptive paths (pdds_estimate with adaptive_n)
